@@ -1,0 +1,161 @@
+"""Generate the golden fixtures in this folder from the reference implementation.
+
+Run in a container that holds the reference source tree (read-only) with::
+
+    PYTHONPATH=tests/golden/refshim:/root/reference/src python tests/golden/make_fixtures.py
+
+It writes
+
+* ``ref_cases.npz`` -- seeded small raster stacks solved by the reference's public
+  ``rcwa.run`` (NumPy backend, SMM, sampled Li, fixed nesting): per-order R and T for ``'s'``
+  and ``'p'`` incidence, and each layer's centre-frame convolution matrices from
+  ``rcwa.operators.assemble``;
+* ``legacy_cases.npz`` -- the efficiencies that the reference's own frozen legacy golden file
+  (``tests/fixtures/legacy_rcwa/golden_legacy.npz``) holds for its 1D, conical and 2D sampled-Li
+  cases, with the inputs those cases are defined by (``tests/fixtures/legacy_rcwa/gen_goldens.py``).
+
+The refshim package is a minimal Array-API stand-in so that the reference imports without the
+third-party ``array_api_compat``. Nothing at test time needs the reference: the tests read only
+the npz files.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = '/root/reference'
+
+
+def _rast(rng, ny, nx, values=(12.25,), n_shapes=3, background=1.0):
+    a = np.full((ny, nx), background, dtype=np.complex128)
+    for _ in range(n_shapes):
+        v = values[rng.integers(0, len(values))]
+        if rng.random() < 0.5:
+            y0, x0 = rng.integers(0, ny), rng.integers(0, nx)
+            h, w = rng.integers(1, max(2, ny // 2)), rng.integers(1, max(2, nx // 2))
+            a[y0:y0 + h, x0:x0 + w] = v
+        else:
+            cy, cx, r = rng.uniform(0, ny), rng.uniform(0, nx), rng.uniform(1, min(ny, nx) / 3)
+            yy, xx = np.mgrid[0:ny, 0:nx]
+            a[(yy + 0.5 - cy) ** 2 + (xx + 0.5 - cx) ** 2 < r * r] = v
+    return a
+
+
+def ref_cases():
+    """Seeded scenes, listed in kernel order (entry layer first)."""
+    rng = np.random.default_rng(20261203)
+    cases = []
+    # the 1D binary grating of the quickstart (orders (10, 0))
+    cases.append(dict(name='grating_1d', structure=np.array([[[1., 1., 12.25, 12.25]]], complex),
+                      thickness=[300.], wavelength=900., period=(700., 700.), orders=(10, 0),
+                      theta=0.0, phi=0.0, eps_top=1.0, eps_bot=2.25))
+    # crossed gratings: oblique, lossy, negative-eps uniform layer, rectangular cells
+    specs = [
+        (16, 16, 2, (3, 3), 0.0, 0.0, 700.),
+        (16, 16, 2, (3, 3), 0.2, 0.3, 650.),
+        (12, 20, 3, (2, 4), 0.4, 1.1, 830.),
+        (24, 24, 1, (4, 4), 0.1, 2.5, 900.),
+        (8, 8, 2, (2, 2), 0.6, 4.0, 480.),
+        (32, 32, 4, (5, 5), 0.0, 0.0, 1000.),
+    ]
+    for k, (ny, nx, L, orders, theta, phi, wl) in enumerate(specs):
+        layers = []
+        for i in range(L):
+            if i == L - 1 and L > 1:
+                layers.append(np.full((ny, nx), -20 + 1.5j))
+            else:
+                layers.append(_rast(rng, ny, nx, values=(12.25, 2.25, 4.0 + 0.3j)))
+        cases.append(dict(name=f'crossed_{k}', structure=np.stack(layers),
+                          thickness=list(rng.uniform(100, 400, size=L)), wavelength=wl,
+                          period=(1000., 1000. if k != 2 else 1200.), orders=orders,
+                          theta=theta, phi=phi, eps_top=1.0, eps_bot=2.25))
+    # a symmetric pillar at normal incidence: exactly degenerate mode pairs
+    a = np.ones((20, 20), complex)
+    a[5:15, 5:15] = 12.25
+    cases.append(dict(name='symmetric_pillar', structure=a[None], thickness=[250.],
+                      wavelength=760., period=(800., 800.), orders=(3, 3), theta=0.0, phi=0.0,
+                      eps_top=1.0, eps_bot=2.25))
+    return cases
+
+
+def run_ref(case, pol):
+    from wavebit import Material, Units, rcwa
+    from wavebit.rcwa import operators
+    st = case['structure'][::-1]          # public stacks list layers bottom to top
+    th = list(case['thickness'])[::-1]
+    layers = tuple(rcwa.Layer(thickness=float(t), epsilon=np.asarray(e)) for e, t in zip(st, th))
+    prob = rcwa.Problem(
+        units=Units(length='nm'),
+        stack=rcwa.Stack(period=case['period'], top=Material(epsilon=case['eps_top']),
+                         bottom=Material(epsilon=case['eps_bot']), layers=layers),
+        excitation=rcwa.Excitation(wavelength=case['wavelength'], sources=(
+            rcwa.PlaneWave(polarization=pol, theta=case['theta'], phi=case['phi']),)))
+    num = rcwa.Numerics(orders=case['orders'])
+    res = rcwa.run(prob, numerics=num)
+    ops = operators.assemble(prob, numerics=num)
+    conv = ops.epsilon[0]
+    return np.asarray(res.R)[0], np.asarray(res.T)[0], [np.asarray(c) for c in conv[:3]]
+
+
+def make_ref_cases():
+    out = {}
+    names = []
+    for case in ref_cases():
+        n = case['name']
+        names.append(n)
+        for key in ('structure', 'thickness', 'wavelength', 'period', 'orders', 'theta', 'phi',
+                    'eps_top', 'eps_bot'):
+            out[f'{n}__{key}'] = np.asarray(case[key])
+        for pol in ('s', 'p'):
+            R, T, conv = run_ref(case, pol)
+            out[f'{n}__R_{pol}'] = R
+            out[f'{n}__T_{pol}'] = T
+        # public order is bottom to top; store conv in kernel order (entry layer first),
+        # only for the smaller cases to keep the fixture small
+        if conv[0].shape[-1] <= 50:
+            for slot, arr in zip(('epx', 'epy', 'epz_i'), conv):
+                out[f'{n}__{slot}'] = arr[::-1]
+    out['names'] = np.array(names)
+    np.savez_compressed(os.path.join(HERE, 'ref_cases.npz'), **out)
+    print('ref_cases.npz:', len(names), 'cases')
+
+
+def make_legacy_cases():
+    """Efficiencies from the reference's frozen legacy golden file, with their inputs."""
+    gold = np.load(os.path.join(REF, 'tests/fixtures/legacy_rcwa/golden_legacy.npz'))
+
+    def rand(shape, seed):   # gen_goldens.py: an index raster drawn and squared to permittivity
+        return np.random.default_rng(seed).uniform(1.0, 4.0, size=shape) ** 2
+
+    # Inputs as in tests/fixtures/legacy_rcwa/gen_goldens.py CASES (layers listed top to bottom).
+    cases = {
+        'te_1layer': dict(psi=np.pi / 2, phi=0.0, structure=[[[9., 9., 9., 1., 1., 1.]]], thickness=[0.15], top=4., bot=1., theta=0., orders=[6, 0], period=[0.77, 0.77], wavelength=0.777),
+        'tm_1layer': dict(psi=0.0, phi=0.0, structure=[[[9., 9., 9., 1., 1., 1.]]], thickness=[0.15], top=4., bot=1., theta=0., orders=[6, 0], period=[0.77, 0.77], wavelength=0.777),
+        'te_oblique': dict(psi=np.pi / 2, phi=0.0, structure=[[[9., 9., 9., 1., 1., 1.]]], thickness=[0.2], top=1., bot=2.25, theta=0.3, orders=[6, 0], period=[0.77, 0.77], wavelength=0.777),
+        'tm_oblique': dict(psi=0.0, phi=0.0, structure=[[[9., 9., 9., 1., 1., 1.]]], thickness=[0.2], top=1., bot=2.25, theta=0.3, orders=[6, 0], period=[0.77, 0.77], wavelength=0.777),
+        'te_2layer': dict(psi=np.pi / 2, phi=0.0, structure=[[[9., 9., 1., 1., 9., 1.]], [[4., 4., 4., 1., 1., 1.]]], thickness=[0.15, 0.22], top=1., bot=1., theta=0., orders=[5, 0], period=[0.7, 0.7], wavelength=0.9),
+        'conical': dict(psi=0.4, phi=0.3, structure=[[[9., 9., 9., 1., 1., 1.]]], thickness=[0.15], top=4., bot=1., theta=0.2, orders=[6, 0], period=[0.77, 0.77], wavelength=0.777),
+        'conical_2l': dict(psi=1.1, phi=0.5, structure=[[[9., 9., 1., 1., 9., 1.]], [[4., 4., 4., 1., 1., 1.]]], thickness=[0.15, 0.22], top=1., bot=2.25, theta=0.3, orders=[5, 0], period=[0.7, 0.7], wavelength=0.9),
+        '2d_normal': dict(psi=0., phi=0., structure=rand((1, 5, 5), 0), thickness=[0.2], top=1., bot=1., theta=0., orders=[2, 2], period=[1., 1.], wavelength=0.9),
+        '2d_oblique': dict(psi=0.9, phi=0.4, structure=rand((1, 6, 6), 1), thickness=[0.3], top=1., bot=2.25, theta=0.3, orders=[2, 2], period=[1., 1.2], wavelength=0.8),
+        '2d_2layer': dict(psi=1.1, phi=0.5, structure=rand((2, 4, 4), 2), thickness=[0.15, 0.22], top=1.44, bot=1., theta=0.2, orders=[2, 2], period=[0.9, 0.9], wavelength=0.7),
+    }
+    out = {}
+    for name, kw in cases.items():
+        for key, val in kw.items():
+            out[f'{name}__{key}'] = np.asarray(val)
+        for sub in ('res', 'res_te_inc', 'res_tm_inc'):
+            for f in ('de_ri', 'de_ti'):
+                key = f'{name}__{sub}__{f}'
+                if key in gold.files:
+                    out[key] = np.asarray(gold[key])
+    out['names'] = np.array(list(cases))
+    np.savez_compressed(os.path.join(HERE, 'legacy_cases.npz'), **out)
+    print('legacy_cases.npz:', len(cases), 'cases')
+
+
+if __name__ == '__main__':
+    sys.path.insert(0, os.path.join(REF, 'src'))
+    make_ref_cases()
+    make_legacy_cases()

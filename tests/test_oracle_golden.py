@@ -1,0 +1,121 @@
+"""Pins the CPU oracle against the reference: fixtures made by the reference itself, the
+reference's frozen legacy goldens, and RETICOLO's 2D Li-nesting totals."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import rcwa_oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(__file__), 'golden')
+
+
+def _ref():
+    return np.load(os.path.join(GOLDEN, 'ref_cases.npz'))
+
+
+def _case(d, n):
+    return {k.split('__', 1)[1]: d[k] for k in d.files if k.startswith(n + '__')}
+
+
+REF_NAMES = list(np.load(os.path.join(GOLDEN, 'ref_cases.npz'))['names'])
+
+
+@pytest.mark.parametrize('name', REF_NAMES)
+def test_oracle_matches_reference_run(name):
+    """Per-order R/T of the reference's public rcwa.run, both polarizations."""
+    c = _case(_ref(), name)
+    hu, hv = (int(v) for v in c['orders'])
+    for k, pol in enumerate(('s', 'p')):
+        out = O.solve_stack(c['structure'], c['thickness'], float(c['wavelength']),
+                            tuple(c['period']), hu, hv, float(c['theta']), float(c['phi']),
+                            complex(c['eps_top']), complex(c['eps_bot']), pol)
+        R, T = out['R'][0], out['T'][0]
+        scale = max(np.abs(c[f'R_{pol}']).max(), np.abs(c[f'T_{pol}']).max())
+        assert np.abs(R - c[f'R_{pol}']).max() <= 1e-12 * scale, name
+        assert np.abs(T - c[f'T_{pol}']).max() <= 1e-12 * scale, name
+        # the pure s/p columns are the same numbers
+        assert np.allclose(out['R'][1 + k], c[f'R_{pol}'], rtol=0, atol=1e-12 * scale)
+
+
+@pytest.mark.parametrize('name', REF_NAMES)
+def test_oracle_conv_matrices_match_reference_assemble(name):
+    """Stage A slots against ``rcwa.operators.assemble`` (centre frame)."""
+    c = _case(_ref(), name)
+    if 'epx' not in c:
+        pytest.skip('no stored slots for this case')
+    hu, hv = (int(v) for v in c['orders'])
+    epx, epy, epz_i = O.to_conv_mat_raster_sampled(c['structure'], hu, hv)
+    for mine, theirs in ((epx, c['epx']), (epy, c['epy']), (epz_i, c['epz_i'])):
+        for i in range(mine.shape[0]):
+            got = O.swap_fourier_origin(mine[i], hu, hv)
+            assert np.abs(got - theirs[i]).max() <= 1e-12 * np.abs(theirs[i]).max()
+
+
+LEGACY_NAMES = list(np.load(os.path.join(GOLDEN, 'legacy_cases.npz'))['names'])
+
+
+@pytest.mark.parametrize('name', LEGACY_NAMES)
+def test_oracle_matches_legacy_goldens(name):
+    """Frozen efficiencies of the reference's legacy golden file, at its own TOL = 1e-12."""
+    d = np.load(os.path.join(GOLDEN, 'legacy_cases.npz'))
+    c = _case(d, name)
+    hu, hv = (int(v) for v in c['orders'])
+    psi = float(c['psi'])
+    out = O.solve_stack(np.asarray(c['structure'], complex), c['thickness'],
+                        float(c['wavelength']), tuple(c['period']), hu, hv, float(c['theta']),
+                        float(c['phi']), complex(c['top']), complex(c['bot']),
+                        (np.sin(psi), np.cos(psi)))
+    for col, sub in enumerate(('res', 'res_te_inc', 'res_tm_inc')):
+        if f'{sub}__de_ri' not in c:
+            continue
+        want_r = np.asarray(c[f'{sub}__de_ri']).reshape(out['R'][col].shape)
+        want_t = np.asarray(c[f'{sub}__de_ti']).reshape(out['T'][col].shape)
+        assert np.abs(out['R'][col] - want_r).max() < 1e-12, (name, sub)
+        assert np.abs(out['T'][col] - want_t).max() < 1e-12, (name, sub)
+
+
+def test_toeplitz_tables_are_the_reference_convention():
+    """``r - c + 2h`` row-major (factorization.py:276-286, :358-366), bit-exact."""
+    for h in range(0, 6):
+        got = O.toeplitz_positions(h).reshape(2 * h + 1, 2 * h + 1)
+        for r in range(2 * h + 1):
+            for c in range(2 * h + 1):
+                assert got[r, c] == r - c + 2 * h
+    assert list(O.order_labels(3)) == [-3, -2, -1, 0, 1, 2, 3]
+
+
+def test_uniform_layer_is_exactly_eps_identity():
+    """A uniform raster factorizes to exactly ``eps * I`` (test_factorization_core.py:927)."""
+    eps = 4.0 + 0.5j
+    epx, epy, epz_i = O.li_conv(np.full((7, 9), eps), 2, 3)
+    N = epx.shape[0]
+    assert np.array_equal(epx, eps * np.eye(N)) or np.abs(epx - eps * np.eye(N)).max() < 1e-15
+    assert np.abs(epy - eps * np.eye(N)).max() < 1e-15
+    assert np.abs(epz_i - np.eye(N) / eps).max() < 1e-15
+
+
+@pytest.mark.parametrize('order,pol,want', [
+    (3, 's', 0.9822061471), (3, 'p', 0.8913451356)])
+def test_oracle_matches_reticolo_li_nesting(order, pol, want):
+    """RETICOLO V10 totals for the 2D eps=6 rectangle under fixed nesting
+    (tests/references/test_reticolo_li_nesting.py:34-41), TOL 1e-9."""
+    n, period = 650, 325.0
+    pixel = period / n
+    x0, x1 = round((period - 200.0) / 2 / pixel), round((period + 200.0) / 2 / pixel)
+    y0, y1 = round((period - 150.0) / 2 / pixel), round((period + 150.0) / 2 / pixel)
+    eps = np.ones((1, n, n), complex)
+    eps[0, y0:y1, x0:x1] = 6.0
+    out = O.solve_stack(eps, np.array([600.0]), 532.0, (period, period), order, order,
+                        0.0, 0.0, 1.0, 1.46 ** 2, pol)
+    assert abs(out['T'][0].sum() - want) < 1e-9
+
+
+def test_lossless_energy_balance():
+    """R + T = 1 on a lossless stack (test_scattering_core.py:137)."""
+    rng = np.random.default_rng(5)
+    st = np.where(rng.random((2, 10, 10)) < 0.4, 12.25, 1.0).astype(complex)
+    out = O.solve_stack(st, np.array([120.0, 200.0]), 640.0, (900., 800.), 3, 2, 0.3, 0.7,
+                        1.0, 2.25, 'p')
+    for col in range(3):
+        assert abs(out['R'][col].sum() + out['T'][col].sum() - 1) < 1e-12
