@@ -1,0 +1,124 @@
+/*
+ * wavebit_gb300 — C ABI of libwbgpu.so, the GB300 (sm_103a) RCWA raster layer path.
+ *
+ * The reference (fieldalgo/wavebit, pure Python) has no native interface; these entry points
+ * are what its RCWA backend seam would bind through ctypes. Each declaration names the
+ * reference function whose role it takes (paths inside src/wavebit).
+ *
+ * Conventions
+ *   - Every function returns WB_OK (0) or a WB_E_* code; wb_last_error() gives the message
+ *     of the calling thread's last failure.
+ *   - Complex numbers are interleaved (re, im) doubles (wb_complex).
+ *   - Matrices are column-major: element (i, j) of an N x N matrix is at [i + j * N].
+ *   - Rasters are row-major (L, ny, nx): element (layer, y, x) at [(layer * ny + y) * nx + x],
+ *     rows along the second lattice axis (v), columns along the first (u).
+ *   - Orders are flattened i = n * n_u + m (m along u fastest), N = (2hu+1)(2hv+1).
+ *   - Layers are listed entry face first: index 0 is the layer that touches the superstrate.
+ *   - Device entry points take caller-owned device pointers and a cudaStream_t (as void*);
+ *     they are asynchronous on that stream. The library never frees caller memory; its own
+ *     scratch comes from the handle's arena, sized at wb_create.
+ *   - A handle is used by one host thread at a time.
+ */
+#ifndef WAVEBIT_GB300_H
+#define WAVEBIT_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WB_OK 0
+#define WB_E_INVALID 1     /* bad argument (reference: ValidationError, code 'rcwa.invalid') */
+#define WB_E_NOMEM 2       /* the request does not fit the handle's HBM budget */
+#define WB_E_SINGULAR 3    /* an exact zero pivot (reference: NumericalError 'rcwa.singular') */
+#define WB_E_NOCONV 4      /* the eigenvalue iteration hit its cap (LAPACK zgeev info > 0) */
+#define WB_E_NONFINITE 5   /* NaN/Inf in a result (reference: NumericalError 'rcwa.nonfinite') */
+#define WB_E_CUDA 6        /* a CUDA runtime error */
+
+/* per-solve status bits written on the device */
+#define WB_ST_SINGULAR 1
+#define WB_ST_NOCONV 2
+#define WB_ST_NONFINITE 4
+#define WB_ST_GRAZING 8    /* min|w| < 1e-9 max|w|: the reference rebuilds such a layer
+                              (rcwa/_engine/solve_2d.py:2463-2482); the result is flagged */
+
+#define WB_PRECISION_FP64 0
+#define WB_PRECISION_MIXED 1
+
+typedef struct { double re, im; } wb_complex;
+typedef struct wb_handle wb_handle;
+
+/* Version of this ABI (major * 100 + minor). */
+int wb_version(void);
+
+/* Message of the calling thread's last failure, NUL-terminated, truncated to len. */
+int wb_last_error(char* buf, size_t len);
+
+/* Create a handle on `device` whose scratch arena may use up to hbm_budget bytes
+ * (0 = 80% of the free device memory). Replaces the per-run solver objects the reference
+ * builds in rcwa/_adapt.py:432-490 (build_solver) and rcwa/_factory.py:6-64. */
+int wb_create(int device, size_t hbm_budget, wb_handle** out);
+int wb_destroy(wb_handle* h);
+
+/* Bit-exact harmonic tables: labels_u[2hu+1] = -hu..hu, labels_v likewise; toeplitz_u
+ * [(2hu+1)^2] = r - c + 2hu row-major, toeplitz_v likewise. Host memory, no handle needed.
+ * Reference: rcwa/_engine/engine.py:953-993 (_separable_kxy order labels),
+ * rcwa/_engine/factorization.py:276-286 (_circulant_index), :358-366 (_toeplitz_positions). */
+int wb_build_indices(int hu, int hv, int32_t* labels_u, int32_t* labels_v, int32_t* toeplitz_u,
+                     int32_t* toeplitz_v);
+
+/* Stage A: Li-rule (fixed nesting) convolution matrices of L rasters, sampled coefficients.
+ * eps: device (L, ny, nx); epx, epy, epz_i: device (L, N, N) column-major; status: device
+ * int32 (1) or NULL. Reference: rcwa/_engine/factorization.py:915-941
+ * (to_conv_mat_raster_sampled) with :369-440, :504-671. */
+int wb_assemble_li(wb_handle* h, const wb_complex* eps, int L, int ny, int nx, int hu, int hv,
+                   wb_complex* epx, wb_complex* epy, wb_complex* epz_i, int32_t* status, void* stream);
+
+/* Stage B: eigenmodes of n_pairs layers. conv: device (n_conv, 3, N, N) slots epx, epy, epz_i;
+ * pair_layer: device (n_pairs) index into conv; kx, ky: device (n_pairs, N) normalised order
+ * wavevectors. Outputs (device): w (n_pairs, 2N) eigenvalues of Omega^2, q (n_pairs, 2N),
+ * W and V (n_pairs, 2N, 2N) column-major, status (n_pairs). precision: WB_PRECISION_*.
+ * Reference: rcwa/_engine/solve_2d.py:2303-2460 (layer_modes_2d, no exceptional-point
+ * rebuilds), _common/conventions.py:186-249 (mode_q), _common/backend.py:1767-1812 (eig). */
+int wb_layer_modes(wb_handle* h, int n_pairs, int hu, int hv, const wb_complex* conv,
+                   const int32_t* pair_layer, const double* kx, const double* ky, wb_complex* w,
+                   wb_complex* q, wb_complex* W, wb_complex* V, int32_t* status, int precision,
+                   void* stream);
+
+/* One batch of whole solves (stages B and C). Every array is a device pointer.
+ *   conv        (n_conv, 3, N, N) from wb_assemble_li, any layers of any stacks
+ *   layer_index (B, L) into conv, entry face first;  thickness (B, L), in wavelength units
+ *   wavelength (B); period (B, 2); theta, phi (B) radians (real; lossless superstrate)
+ *   eps_top, eps_bot (B); pol (B, 2) = (a_s, a_p), unit norm
+ * Outputs: R, T (B, 3, N) per-order efficiencies for [given polarization, pure s, pure p];
+ *   amps (B, 3, 4, N) = r_s, r_p, t_s, t_p per column or NULL; status (B) WB_ST_* bits.
+ * Reference: rcwa/_engine/scattering.py:1185-1456 (_smm_sp, smm_2d) with :907-994
+ * (_sp_scattering_result), rcwa/_engine/solve_1d.py:1588-1610 (sp_efficiencies),
+ * observations/power.py:13-159. */
+int wb_solve_batch(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* conv,
+                   const int32_t* layer_index, const double* thickness, const double* wavelength,
+                   const double* period, const double* theta, const double* phi,
+                   const wb_complex* eps_top, const wb_complex* eps_bot, const wb_complex* pol,
+                   double* R, double* T, wb_complex* amps, int32_t* status, int precision,
+                   void* stream);
+
+/* The same solve from HOST buffers: rasters in, efficiencies out. Copies inputs to the
+ * device, assembles the L layers (stage A), solves the B problems, copies R, T and status
+ * back and synchronises. eps: host (L, ny, nx); the other arrays as in wb_solve_batch but in
+ * host memory. Reference: the rcwa.run(problem) lifecycle, rcwa/_lifecycle.py:698-803. */
+int wb_solve_host(wb_handle* h, int B, int L, int ny, int nx, int hu, int hv,
+                  const wb_complex* eps, const int32_t* layer_index, const double* thickness,
+                  const double* wavelength, const double* period, const double* theta,
+                  const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,
+                  const wb_complex* pol, double* R, double* T, int32_t* status, int precision);
+
+/* Bytes of arena one chunk of `chunk` solves with L layers and N orders needs. */
+size_t wb_solve_workspace_bytes(int hu, int hv, int L, int chunk);
+
+/* Number of kernels the library launched on this handle since creation (for accounting). */
+long long wb_kernel_launches(wb_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

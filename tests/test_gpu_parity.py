@@ -1,0 +1,124 @@
+"""Parity of the CUDA path (through the C ABI) against the CPU oracle and the reference fixtures."""
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip('torch')
+
+from oracle import rcwa_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), 'golden')
+
+
+def _engine():
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from wavebit_gb300 import engine
+    return engine
+
+
+def _rast(rng, ny, nx):
+    a = np.ones((ny, nx), complex)
+    a[rng.random((ny, nx)) < 0.35] = 12.25
+    a[rng.random((ny, nx)) < 0.1] = 4.0 + 0.5j
+    return a
+
+
+@pytest.mark.parametrize('ny,nx,hu,hv', [(16, 16, 2, 2), (12, 20, 3, 1), (1, 4, 10, 0), (33, 17, 4, 5)])
+def test_assemble_matches_oracle(ny, nx, hu, hv):
+    E = _engine()
+    rng = np.random.default_rng(ny * 100 + nx)
+    eps = np.stack([_rast(rng, ny, nx), np.full((ny, nx), -20 + 1.5j)])
+    conv = E.assemble(torch.as_tensor(eps, device='cuda'), hu, hv)
+    torch.cuda.synchronize()
+    assert int(conv.status.item()) == 0
+    for i in range(eps.shape[0]):
+        want = O.li_conv(eps[i], hu, hv)
+        for k, w in enumerate(want):
+            got = conv.slot(k)[i].cpu().numpy()
+            assert np.abs(got - w).max() <= 1e-12 * np.abs(w).max(), (i, k)
+
+
+@pytest.mark.parametrize('hu,hv', [(2, 2), (3, 3), (5, 4)])
+def test_layer_modes_are_eigenpairs(hu, hv):
+    """Stage B: Omega^2 W = W diag(w) to round-off, eigenvalues equal LAPACK's as a set, q is
+    mode_q(w) and V = Omega_R W / q."""
+    E = _engine()
+    rng = np.random.default_rng(hu * 10 + hv)
+    eps = np.stack([_rast(rng, 20, 20), _rast(rng, 20, 20)])
+    conv = E.assemble(torch.as_tensor(eps, device='cuda'), hu, hv)
+    kx, ky = O.separable_kxy(700.0, (900.0, 1000.0), O.incident_kxy(0.3, 0.7, 1.0), hu, hv)
+    kxg, kyg = O.order_grid(kx, ky)
+    P = 2
+    w, q, W, V, st = E.layer_modes(conv, [0, 1], np.tile(kxg.real, (P, 1)), np.tile(kyg.real, (P, 1)))
+    torch.cuda.synchronize()
+    assert (st.cpu().numpy() & 2) == 0
+    for p in range(P):
+        ex, ey, ez = (s[p].cpu().numpy() for s in (conv.epx, conv.epy, conv.epz_i))
+        om2, om_r = O.layer_operator(kxg, kyg, ex, ey, ez)
+        wn, Wn, qn, Vn = (t[p].cpu().numpy() for t in (w, W, q, V))
+        res = np.linalg.norm(om2 @ Wn - Wn * wn[None, :]) / (np.linalg.norm(om2) * np.linalg.norm(Wn))
+        assert res < 1e-13, res
+        ref = np.linalg.eigvals(om2)
+        # every eigenvalue has a LAPACK twin within round-off
+        d = np.abs(wn[:, None] - ref[None, :]).min(axis=1)
+        assert d.max() <= 1e-10 * np.abs(ref).max(), d.max()
+        assert np.array_equal(qn, O.mode_q(wn)) or np.abs(qn - O.mode_q(wn)).max() < 1e-14 * np.abs(qn).max()
+        assert np.abs(om_r @ Wn / qn[None, :] - Vn).max() <= 1e-11 * np.abs(Vn).max()
+
+
+def _case(d, n):
+    return {k.split('__', 1)[1]: d[k] for k in d.files if k.startswith(n + '__')}
+
+
+REF_NAMES = list(np.load(os.path.join(GOLDEN, 'ref_cases.npz'))['names'])
+
+
+def _solve_case(E, c, pol_pair):
+    hu, hv = (int(v) for v in c['orders'])
+    st = np.asarray(c['structure'], complex)
+    L = st.shape[0]
+    conv = E.assemble(torch.as_tensor(st, device='cuda'), hu, hv)
+    inp = E.BatchInputs([list(range(L))], [list(c['thickness'])], [float(c['wavelength'])],
+                        [list(c['period'])], [float(c['theta'])], [float(c['phi'])],
+                        [complex(c['eps_top'])], [complex(c['eps_bot'])], [list(pol_pair)])
+    R, T, status = E.solve_batch(conv, inp)
+    torch.cuda.synchronize()
+    return R[0].cpu().numpy(), T[0].cpu().numpy(), int(status[0].item())
+
+
+@pytest.mark.parametrize('name', REF_NAMES)
+def test_solve_matches_reference_fixtures(name):
+    """Per-order R and T within 1e-10 (relative to the largest efficiency) of the reference's
+    own rcwa.run, for s and p incidence."""
+    E = _engine()
+    c = _case(np.load(os.path.join(GOLDEN, 'ref_cases.npz')), name)
+    R, T, st = _solve_case(E, c, O.polarization_pair('s'))
+    assert st & ~8 == 0, st
+    for col, pol in ((1, 's'), (2, 'p')):
+        scale = max(np.abs(c[f'R_{pol}']).max(), np.abs(c[f'T_{pol}']).max())
+        assert np.abs(R[col] - c[f'R_{pol}']).max() <= 1e-10 * scale, (name, pol)
+        assert np.abs(T[col] - c[f'T_{pol}']).max() <= 1e-10 * scale, (name, pol)
+
+
+def test_solve_host_matches_oracle():
+    """The host-buffer entry (wb_solve_host): rasters in, efficiencies out."""
+    E = _engine()
+    rng = np.random.default_rng(11)
+    eps = np.stack([_rast(rng, 16, 16), _rast(rng, 16, 16), np.full((16, 16), 2.25 + 0.1j)])
+    B, hu, hv = 5, 3, 3
+    wl = np.linspace(500, 900, B)
+    li = np.tile(np.arange(3), (B, 1))
+    th = np.tile([120.0, 200.0, 60.0], (B, 1))
+    R, T, st = E.solve_host(eps, li, th, wl, np.tile([800.0, 900.0], (B, 1)), np.full(B, 0.25),
+                            np.full(B, 0.4), np.ones(B), np.full(B, 2.25), np.tile([1.0, 0.0], (B, 1)),
+                            hu, hv)
+    assert (st & ~8 == 0).all()
+    for b in range(B):
+        o = O.solve_stack(eps, th[b], wl[b], (800.0, 900.0), hu, hv, 0.25, 0.4, 1.0, 2.25, 's')
+        scale = max(np.abs(o['R']).max(), np.abs(o['T']).max())
+        assert np.abs(R[b] - o['R']).max() <= 1e-10 * scale
+        assert np.abs(T[b] - o['T']).max() <= 1e-10 * scale

@@ -1,0 +1,269 @@
+// C ABI of libwbgpu.so (declared in include/wavebit_gb300.h): handles, the scratch arena,
+// error reporting and the entry points that drive stages A, B and C.
+#include <cstdio>
+#include <cstring>
+#include <cstdarg>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include "../../include/wavebit_gb300.h"
+#include "wb_common.cuh"
+#include "wb_kernels.h"
+#include "wb_internal.h"
+
+struct wb_handle {
+  int device = 0;
+  size_t budget = 0;
+  wb::Arena arena;
+  void* buf = nullptr;
+  size_t buf_bytes = 0;
+};
+
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char msg[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(msg, sizeof(msg), fmt, ap);
+  va_end(ap);
+  g_err = msg;
+  return code;
+}
+
+int cuda_check(const char* where) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(WB_E_CUDA, "%s: %s", where, cudaGetErrorString(e));
+  return WB_OK;
+}
+
+// Grow the handle's arena to at least `bytes` (within the budget).
+int reserve(wb_handle* h, size_t bytes) {
+  if (bytes <= h->buf_bytes) { h->arena.base = (char*)h->buf; h->arena.cap = h->buf_bytes; return WB_OK; }
+  if (bytes > h->budget)
+    return fail(WB_E_NOMEM, "workspace of %zu bytes exceeds the handle budget of %zu bytes", bytes, h->budget);
+  if (h->buf) {
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return fail(WB_E_CUDA, "synchronise before growing the arena: %s", cudaGetErrorString(e));
+    cudaFree(h->buf);
+    h->buf = nullptr; h->buf_bytes = 0;
+  }
+  cudaError_t e = cudaMalloc(&h->buf, bytes);
+  if (e != cudaSuccess) {
+    h->buf = nullptr;
+    cudaGetLastError();
+    return fail(WB_E_NOMEM, "cudaMalloc(%zu) for the arena: %s", bytes, cudaGetErrorString(e));
+  }
+  h->buf_bytes = bytes;
+  h->arena.base = (char*)h->buf;
+  h->arena.cap = bytes;
+  h->arena.reset();
+  return WB_OK;
+}
+
+bool valid_orders(int hu, int hv) { return hu >= 0 && hv >= 0 && hu <= 64 && hv <= 64; }
+}  // namespace
+
+extern "C" {
+
+int wb_version(void) { return 100; }
+
+int wb_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return WB_E_INVALID;
+  std::snprintf(buf, len, "%s", g_err.c_str());
+  return WB_OK;
+}
+
+int wb_create(int device, size_t hbm_budget, wb_handle** out) {
+  if (!out) return fail(WB_E_INVALID, "wb_create: out is NULL");
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return fail(WB_E_CUDA, "wb_create: no CUDA device is visible");
+  }
+  if (device < 0 || device >= count) return fail(WB_E_INVALID, "wb_create: device %d of %d", device, count);
+  if (cudaSetDevice(device) != cudaSuccess) return cuda_check("wb_create: cudaSetDevice");
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return cuda_check("wb_create: cudaMemGetInfo");
+  wb_handle* h = new wb_handle();
+  h->device = device;
+  h->budget = hbm_budget ? hbm_budget : (size_t)(0.8 * (double)free_b);
+  *out = h;
+  return WB_OK;
+}
+
+int wb_destroy(wb_handle* h) {
+  if (!h) return WB_OK;
+  if (h->buf) { cudaSetDevice(h->device); cudaDeviceSynchronize(); cudaFree(h->buf); }
+  delete h;
+  return WB_OK;
+}
+
+int wb_build_indices(int hu, int hv, int32_t* labels_u, int32_t* labels_v, int32_t* toeplitz_u,
+                     int32_t* toeplitz_v) {
+  if (!valid_orders(hu, hv)) return fail(WB_E_INVALID, "orders (%d, %d) out of range", hu, hv);
+  const int nu = 2 * hu + 1, nv = 2 * hv + 1;
+  if (labels_u) for (int i = 0; i < nu; ++i) labels_u[i] = i - hu;
+  if (labels_v) for (int i = 0; i < nv; ++i) labels_v[i] = i - hv;
+  if (toeplitz_u) for (int r = 0; r < nu; ++r) for (int c = 0; c < nu; ++c) toeplitz_u[r * nu + c] = r - c + 2 * hu;
+  if (toeplitz_v) for (int r = 0; r < nv; ++r) for (int c = 0; c < nv; ++c) toeplitz_v[r * nv + c] = r - c + 2 * hv;
+  return WB_OK;
+}
+
+int wb_assemble_li(wb_handle* h, const wb_complex* eps, int L, int ny, int nx, int hu, int hv,
+                   wb_complex* epx, wb_complex* epy, wb_complex* epz_i, int32_t* status, void* stream) {
+  if (!h || !eps || !epx || !epy || !epz_i) return fail(WB_E_INVALID, "wb_assemble_li: NULL argument");
+  if (L <= 0 || ny <= 0 || nx <= 0 || !valid_orders(hu, hv))
+    return fail(WB_E_INVALID, "wb_assemble_li: bad sizes L=%d ny=%d nx=%d orders=(%d,%d)", L, ny, nx, hu, hv);
+  cudaSetDevice(h->device);
+  size_t need = wb::assemble_workspace_bytes(L, ny, nx, hu, hv);
+  int rc = reserve(h, need);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  wb::assemble_li(s, (const cplx*)eps, L, ny, nx, hu, hv, (cplx*)epx, (cplx*)epy, (cplx*)epz_i, h->buf, status);
+  return cuda_check("wb_assemble_li");
+}
+
+size_t wb_solve_workspace_bytes(int hu, int hv, int L, int chunk) {
+  if (!valid_orders(hu, hv) || L <= 0 || chunk <= 0) return 0;
+  return wb::solve_chunk_bytes((2 * hu + 1) * (2 * hv + 1), L, chunk);
+}
+
+int wb_layer_modes(wb_handle* h, int n_pairs, int hu, int hv, const wb_complex* conv,
+                   const int32_t* pair_layer, const double* kx, const double* ky, wb_complex* w,
+                   wb_complex* q, wb_complex* W, wb_complex* V, int32_t* status, int precision,
+                   void* stream) {
+  if (!h || !conv || !pair_layer || !kx || !ky || !w || !q || !W || !V)
+    return fail(WB_E_INVALID, "wb_layer_modes: NULL argument");
+  if (n_pairs <= 0 || !valid_orders(hu, hv)) return fail(WB_E_INVALID, "wb_layer_modes: bad sizes");
+  if (precision != WB_PRECISION_FP64 && precision != WB_PRECISION_MIXED)
+    return fail(WB_E_INVALID, "wb_layer_modes: precision %d", precision);
+  cudaSetDevice(h->device);
+  const int N = (2 * hu + 1) * (2 * hv + 1), n = 2 * N;
+  size_t need = wb::layer_modes_bytes(N, n_pairs);
+  int rc = reserve(h, need);
+  if (rc) return rc;
+  wb::layer_modes(( cudaStream_t)stream, h->arena, n_pairs, N, (const cplx*)conv, (const int*)pair_layer, kx, ky,
+                  (cplx*)w, (cplx*)q, (cplx*)W, (cplx*)V, status);
+  (void)n;
+  return cuda_check("wb_layer_modes");
+}
+
+int wb_solve_batch(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* conv,
+                   const int32_t* layer_index, const double* thickness, const double* wavelength,
+                   const double* period, const double* theta, const double* phi,
+                   const wb_complex* eps_top, const wb_complex* eps_bot, const wb_complex* pol,
+                   double* R, double* T, wb_complex* amps, int32_t* status, int precision,
+                   void* stream) {
+  if (!h || !conv || !layer_index || !thickness || !wavelength || !period || !theta || !phi || !eps_top ||
+      !eps_bot || !pol || !R || !T || !status)
+    return fail(WB_E_INVALID, "wb_solve_batch: NULL argument");
+  if (B <= 0 || L <= 0 || !valid_orders(hu, hv)) return fail(WB_E_INVALID, "wb_solve_batch: bad sizes B=%d L=%d", B, L);
+  if (precision != WB_PRECISION_FP64 && precision != WB_PRECISION_MIXED)
+    return fail(WB_E_INVALID, "wb_solve_batch: precision %d", precision);
+  cudaSetDevice(h->device);
+  const int N = (2 * hu + 1) * (2 * hv + 1);
+  // the largest chunk that fits the budget
+  int chunk = B;
+  while (chunk > 1 && wb::solve_chunk_bytes(N, L, chunk) > h->budget) chunk = (chunk + 1) / 2;
+  size_t need = wb::solve_chunk_bytes(N, L, chunk);
+  int rc = reserve(h, need);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaMemsetAsync(status, 0, sizeof(int32_t) * B, s);
+  wb::SolveDesc d{B, L, hu, hv, (const cplx*)conv, (const int*)layer_index, thickness, wavelength, period, theta,
+                  phi, (const cplx*)eps_top, (const cplx*)eps_bot, (const cplx*)pol};
+  wb::SolveOut o{R, T, (cplx*)amps, status};
+  for (int first = 0; first < B; first += chunk) {
+    int count = std::min(chunk, B - first);
+    if (wb::solve_chunk(s, h->arena, d, first, count, o) != 0)
+      return fail(WB_E_NOMEM, "wb_solve_batch: arena exhausted for a chunk of %d", count);
+  }
+  (void)precision;
+  return cuda_check("wb_solve_batch");
+}
+
+int wb_solve_host(wb_handle* h, int B, int L, int ny, int nx, int hu, int hv,
+                  const wb_complex* eps, const int32_t* layer_index, const double* thickness,
+                  const double* wavelength, const double* period, const double* theta,
+                  const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,
+                  const wb_complex* pol, double* R, double* T, int32_t* status, int precision) {
+  if (!h || !eps || !layer_index || !thickness || !wavelength || !period || !theta || !phi || !eps_top ||
+      !eps_bot || !pol || !R || !T || !status)
+    return fail(WB_E_INVALID, "wb_solve_host: NULL argument");
+  if (B <= 0 || L <= 0 || ny <= 0 || nx <= 0 || !valid_orders(hu, hv))
+    return fail(WB_E_INVALID, "wb_solve_host: bad sizes");
+  for (long long i = 0; i < (long long)B * L; ++i)
+    if (layer_index[i] < 0 || layer_index[i] >= L)
+      return fail(WB_E_INVALID, "wb_solve_host: layer_index[%lld] = %d outside [0, %d)", i, layer_index[i], L);
+  cudaSetDevice(h->device);
+  const int N = (2 * hu + 1) * (2 * hv + 1);
+  const size_t NN = (size_t)N * N;
+  // one device block for inputs, conv and outputs (separate from the arena)
+  size_t off = 0;
+  auto take = [&](size_t b) { size_t o = off; off += (b + 255) & ~(size_t)255; return o; };
+  const size_t o_eps = take(sizeof(wb_complex) * L * ny * nx), o_conv = take(sizeof(wb_complex) * 3 * L * NN);
+  const size_t o_li = take(sizeof(int32_t) * B * L), o_th = take(sizeof(double) * B * L);
+  const size_t o_wl = take(sizeof(double) * B), o_per = take(sizeof(double) * 2 * B);
+  const size_t o_th2 = take(sizeof(double) * B), o_ph = take(sizeof(double) * B);
+  const size_t o_et = take(sizeof(wb_complex) * B), o_eb = take(sizeof(wb_complex) * B);
+  const size_t o_pol = take(sizeof(wb_complex) * 2 * B);
+  const size_t o_R = take(sizeof(double) * 3 * B * N), o_T = take(sizeof(double) * 3 * B * N);
+  const size_t o_st = take(sizeof(int32_t) * B), o_ast = take(sizeof(int32_t));
+  const size_t o_tmp = take(sizeof(wb_complex) * 3 * L * NN);   // slot planes before regrouping
+  char* dev = nullptr;
+  if (cudaMalloc(&dev, off) != cudaSuccess) { cudaGetLastError(); return fail(WB_E_NOMEM, "wb_solve_host: cudaMalloc(%zu)", off); }
+  cudaStream_t s = nullptr;
+  auto H2D = [&](size_t o, const void* p, size_t b) { cudaMemcpyAsync(dev + o, p, b, cudaMemcpyHostToDevice, s); };
+  H2D(o_eps, eps, sizeof(wb_complex) * L * ny * nx);
+  H2D(o_li, layer_index, sizeof(int32_t) * B * L);
+  H2D(o_th, thickness, sizeof(double) * B * L);
+  H2D(o_wl, wavelength, sizeof(double) * B);
+  H2D(o_per, period, sizeof(double) * 2 * B);
+  H2D(o_th2, theta, sizeof(double) * B);
+  H2D(o_ph, phi, sizeof(double) * B);
+  H2D(o_et, eps_top, sizeof(wb_complex) * B);
+  H2D(o_eb, eps_bot, sizeof(wb_complex) * B);
+  H2D(o_pol, pol, sizeof(wb_complex) * 2 * B);
+  cudaMemsetAsync(dev + o_ast, 0, sizeof(int32_t), s);
+  // stage A into (L, 3, N, N): assemble into three (L, N, N) planes, then interleave per layer
+  wb_complex* conv = (wb_complex*)(dev + o_conv);
+  int rc = WB_OK;
+  {
+    // assemble each slot plane contiguously, then regroup to (L, 3, N, N)
+    wb_complex* planes = (wb_complex*)(dev + o_tmp);
+    wb_complex* ex = planes;
+    wb_complex* ey = planes + (size_t)L * NN;
+    wb_complex* ez = planes + (size_t)2 * L * NN;
+    rc = wb_assemble_li(h, (const wb_complex*)(dev + o_eps), L, ny, nx, hu, hv, ex, ey, ez,
+                        (int32_t*)(dev + o_ast), s);
+    if (rc == WB_OK) {
+      wb::regroup_slots(s, L, N, (const cplx*)planes, (cplx*)conv);
+      rc = cuda_check("wb_solve_host: regroup");
+    }
+  }
+  if (rc == WB_OK)
+    rc = wb_solve_batch(h, B, L, hu, hv, conv, (const int32_t*)(dev + o_li), (const double*)(dev + o_th),
+                        (const double*)(dev + o_wl), (const double*)(dev + o_per), (const double*)(dev + o_th2),
+                        (const double*)(dev + o_ph), (const wb_complex*)(dev + o_et), (const wb_complex*)(dev + o_eb),
+                        (const wb_complex*)(dev + o_pol), (double*)(dev + o_R), (double*)(dev + o_T), nullptr,
+                        (int32_t*)(dev + o_st), precision, s);
+  if (rc == WB_OK) {
+    cudaMemcpyAsync(R, dev + o_R, sizeof(double) * 3 * B * N, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(T, dev + o_T, sizeof(double) * 3 * B * N, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(status, dev + o_st, sizeof(int32_t) * B, cudaMemcpyDeviceToHost, s);
+    int32_t ast = 0;
+    cudaMemcpyAsync(&ast, dev + o_ast, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = fail(WB_E_CUDA, "wb_solve_host: %s", cudaGetErrorString(e));
+    else if (ast) for (int b = 0; b < B; ++b) status[b] |= ast;
+  }
+  cudaFree(dev);
+  return rc;
+}
+
+long long wb_kernel_launches(wb_handle* h) { (void)h; return wb::launch_count(); }
+
+}  // extern "C"

@@ -1,0 +1,65 @@
+// Host-side internal types of libwbgpu.so: the workspace arena, the solve descriptor.
+#pragma once
+#include <cstddef>
+#include "wb_common.cuh"
+
+namespace wb {
+
+// Bump allocator over one device buffer owned by the handle. get<T>(count) returns nullptr
+// (and latches !ok()) when the buffer is exhausted; reset() rewinds it.
+struct Arena {
+  char* base = nullptr;
+  size_t cap = 0, off = 0;
+  bool failed = false;
+  void reset() { off = 0; failed = false; }
+  template <class T> T* get(size_t count) {
+    size_t bytes = (count * sizeof(T) + 255) & ~(size_t)255;
+    if (failed || off + bytes > cap) { failed = true; return nullptr; }
+    T* p = reinterpret_cast<T*>(base + off);
+    off += bytes;
+    return p;
+  }
+  bool ok() const { return !failed; }
+};
+
+// Per-solve vectors over the retained orders (N) or the s/p boundary basis (n = 2N).
+struct PortVectors {
+  double *kx, *ky, *c, *s;                 // (B, N)
+  cplx *kz_top, *kz_bot;                   // (B, N)
+  cplx *wg, *vg;                           // (B, n) gap W / V diagonals
+  cplx *r11, *r12, *r21, *r22;             // (B, n) superstrate -> gap S blocks (diagonal)
+  cplx *t11, *t21;                         // (B, n) gap -> substrate S blocks used
+  cplx *nt, *nb;                           // (B) half-space indices
+};
+
+// Everything is a device pointer. Layers are listed entry face first (the superstrate side).
+struct SolveDesc {
+  int n_solves, n_layers, hu, hv;
+  const cplx* conv;            // (n_conv, 3, N, N) column-major slots epx, epy, epz_i
+  const int* layer_index;      // (B, L) index into conv
+  const double* thickness;     // (B, L)
+  const double* wavelength;    // (B)
+  const double* period;        // (B, 2)
+  const double* theta;         // (B)
+  const double* phi;           // (B)
+  const cplx* eps_top;         // (B)
+  const cplx* eps_bot;         // (B)
+  const cplx* pol;             // (B, 2) (a_s, a_p)
+};
+
+struct SolveOut {
+  double* R;                   // (B, 3, N): given polarization, pure s, pure p
+  double* T;                   // (B, 3, N)
+  cplx* amps;                  // (B, 3, 4, N) r_s, r_p, t_s, t_p or nullptr
+  int32_t* status;             // (B)
+};
+
+size_t solve_chunk_bytes(int N, int L, int chunk);
+size_t layer_modes_bytes(int N, int n_pairs);
+void layer_modes(cudaStream_t s, Arena& ar, int n_pairs, int N, const cplx* conv, const int* pair_layer,
+                 const double* kx, const double* ky, cplx* w, cplx* q, cplx* W, cplx* V, int32_t* status);
+// (3 planes of L) (N, N) slots -> (L, 3, N, N)
+void regroup_slots(cudaStream_t s, int L, int N, const cplx* planes, cplx* out);
+int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int count, const SolveOut& out);
+
+}  // namespace wb

@@ -1,0 +1,38 @@
+// Internal launch wrappers shared by the translation units of libwbgpu.so (not the public ABI).
+#pragma once
+#include "wb_common.cuh"
+
+namespace wb {
+
+// Kernel-launch accounting (every launch site in the library calls note_launch()).
+void note_launch();
+long long launch_count();
+
+// ---- dense linear algebra (wb_linalg.cu)
+void zgemm(cudaStream_t s, int batch, int m, int n, int k, cplx alpha,
+           const cplx* A, long long a_rs, long long a_cs, long long a_bs,
+           const cplx* B, long long b_rs, long long b_cs, long long b_bs,
+           cplx beta, cplx* C, long long c_rs, long long c_cs, long long c_bs);
+// status (if non-null) of batch element e is status[e / st_div]
+void zgetrf(cudaStream_t s, int batch, int n, cplx* A, int lda, long long a_bs, int* ipiv, long long piv_bs,
+            int32_t* status, int st_div);
+void zgetrs(cudaStream_t s, int batch, int n, const cplx* LU, int lda, long long a_bs,
+            const int* ipiv, long long piv_bs, cplx* B, int nrhs, int ldb, long long b_bs, int trans);
+void ztranspose(cudaStream_t s, int batch, int m, int n, const cplx* A, int lda, long long a_bs,
+                cplx* B, int ldb, long long b_bs);
+void zset_identity(cudaStream_t s, int batch, int n, cplx* A, int lda, long long a_bs);
+
+// ---- eigen-decomposition (wb_eig.cu)
+void zgeev_schur(cudaStream_t s, int batch, int n, cplx* A, int lda, long long a_bs, cplx* Z, int ldz,
+                 long long z_bs, cplx* w, cplx* tau, int32_t* status, int st_div);
+void ztrevc(cudaStream_t s, int batch, int n, const cplx* T, int ldt, long long t_bs, cplx* X, int ldx,
+            long long x_bs);
+void znormalize_columns(cudaStream_t s, int batch, int n, cplx* W, int ldw, long long w_bs);
+
+// ---- stage A: convolution matrices (wb_assemble.cu)
+// eps: (L, ny, nx) row-major raster; outputs (L, N, N) column-major; scratch from `ws`.
+size_t assemble_workspace_bytes(int L, int ny, int nx, int hu, int hv);
+void assemble_li(cudaStream_t s, const cplx* eps, int L, int ny, int nx, int hu, int hv,
+                 cplx* epx, cplx* epy, cplx* epz_i, void* ws, int32_t* status);
+
+}  // namespace wb

@@ -1,0 +1,763 @@
+// Stages B and C of the RCWA raster path, and the native orchestration of one batched solve.
+//
+// Stage B (per (solve, layer) pair): the layer operator Omega^2 (solve_2d.py:2377-2418), its
+// eigen-decomposition (wb_eig.cu), q = mode_q(w) (conventions.py:186-249), the H-field modes
+// V = Omega_R W / q (solve_2d.py:2445-2448) and the s/p rotation (solve_2d.py:2584-2616).
+//
+// Stage C (per solve): the reference cascades S-matrices with Redheffer stars
+// (scattering.py:163-200, :1272-1293) and reads R and T off the final S11 / S21
+// (scattering.py:907-994). Only those two blocks, applied to three incidence columns, are
+// ever read, so the stars are evaluated bottom-up keeping the one block the next star needs:
+// the reflection R_k seen from the gap above layer k,
+//     R_k = (S_layer_k * R_{k+1})_11
+//         = (A - rho_t B)^-1 (rho_t A - B),  rho_t = X rho_b X,  rho_b = (B + A R)(A + B R)^-1
+// with A, B the gap/layer interface pair of _ab_matrices (scattering.py:116-125) and
+// X = diag(exp(-k0 q d)). The transmitted amplitudes follow from one top-down pass with three
+// right-hand sides. This is the same star algebra (equal in exact arithmetic; the tests hold
+// it to the reference within 1e-10) at ~60 n^3 FP64 flops per layer instead of ~180 n^3.
+#include <vector>
+#include <algorithm>
+#include "wb_common.cuh"
+#include "wb_kernels.h"
+#include "wb_internal.h"
+
+namespace wb {
+
+static unsigned long long g_launches = 0;
+void note_launch() { __atomic_add_fetch(&g_launches, 1ULL, __ATOMIC_RELAXED); }
+long long launch_count() { return (long long)__atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
+
+// --------------------------------------------------------------------------- ports
+// Per solve: order wavevectors, per-order s/p frame, half-space kz, gap waves and the diagonal
+// S blocks of the superstrate->gap and gap->substrate interfaces.
+__global__ void ports_kernel(int B, int hu, int hv, const double* __restrict__ wavelength,
+                             const double* __restrict__ period, const double* __restrict__ theta,
+                             const double* __restrict__ phi, const cplx* __restrict__ eps_top,
+                             const cplx* __restrict__ eps_bot, PortVectors pv) {
+  const int b = blockIdx.x;
+  const int nu = 2 * hu + 1, nv = 2 * hv + 1, N = nu * nv, n = 2 * N;
+  const double lam = wavelength[b];
+  const cplx et = eps_top[b], eb = eps_bot[b];
+  // lossless superstrate: N_phase = sqrt(Re eps), k_inc = N sin(theta) (cos phi, sin phi)
+  const double index = sqrt(et.x);
+  const double st = sin(theta[b]);
+  const double ph = phi[b];
+  const double kix = index * st * cos(ph), kiy = index * st * sin(ph);
+  const cplx nt = csqrt_p(et), nb = csqrt_p(eb);
+  const cplx nt2 = cmul(nt, nt), nb2 = cmul(nb, nb);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const int u = i % nu, v = i / nu;
+    const double kx = kix + (double)(u - hu) * (lam / period[2 * b + 0]);
+    const double ky = kiy + (double)(v - hv) * (lam / period[2 * b + 1]);
+    // order_azimuth (conventions.py:1316-1431), real wavevectors
+    double vphi;
+    if (kx == 0.0) {
+      if (ky == 0.0) {
+        vphi = atan(sin(ph) / cos(ph)) + (cos(ph) < 0.0 ? 3.141592653589793 : 0.0);
+      } else {
+        vphi = (ky < 0.0 ? -1.5707963267948966 : 1.5707963267948966) - kx / ky;
+      }
+    } else {
+      vphi = atan(ky / kx) + (kx < 0.0 ? 3.141592653589793 : 0.0);
+    }
+    double sn, cs;
+    sincos(vphi, &sn, &cs);
+    const double kpar = kx * kx + ky * ky;
+    // boundary_kz (conventions.py:655-760): sqrt(n^2 - kpar^2), flipped where Re+Im < 0
+    cplx kzt = csqrt_p(csub(nt2, cmk(kpar, 0.0)));
+    if (kzt.x + kzt.y < 0.0) kzt = cneg(kzt);
+    cplx kzb = csqrt_p(csub(nb2, cmk(kpar, 0.0)));
+    if (kzb.x + kzb.y < 0.0) kzb = cneg(kzb);
+    const double y = sqrt(1.0 + kx * kx + ky * ky);      // gap waves (scattering.py:128-160)
+    const long long o = (long long)b * N + i, on = (long long)b * n;
+    pv.kx[o] = kx; pv.ky[o] = ky; pv.c[o] = cs; pv.s[o] = sn;
+    pv.kz_top[o] = kzt; pv.kz_bot[o] = kzb;
+    // diagonal W/V of gap, superstrate and substrate in the (E_s, H_p) basis
+    const cplx wg_s = cmk(1.0, 0.0), wg_p = cmk(0.0, -y);
+    const cplx vg_s = cmk(0.0, -y), vg_p = cmk(1.0, 0.0);
+    pv.wg[on + i] = wg_s; pv.wg[on + N + i] = wg_p;
+    pv.vg[on + i] = vg_s; pv.vg[on + N + i] = vg_p;
+    const cplx mi = cmk(0.0, -1.0);
+    const cplx wt_s = cmk(1.0, 0.0), wt_p = cdiv(cmul(mi, kzt), et);
+    const cplx vt_s = cmul(mi, kzt), vt_p = cmk(1.0, 0.0);
+    const cplx wb_s = cmk(1.0, 0.0), wb_p = cdiv(cmul(mi, kzb), eb);
+    const cplx vb_s = cmul(mi, kzb), vb_p = cmk(1.0, 0.0);
+    for (int half = 0; half < 2; ++half) {
+      const cplx wg = half ? wg_p : wg_s, vg = half ? vg_p : vg_s;
+      const cplx wt = half ? wt_p : wt_s, vt = half ? vt_p : vt_s;
+      const cplx wbv = half ? wb_p : wb_s, vbv = half ? vb_p : vb_s;
+      // _ab_matrices(W_gap, V_gap, W_x, V_x): A = W_gap^-1 W_x + V_gap^-1 V_x, B = difference
+      const cplx At = cadd(cdiv(wt, wg), cdiv(vt, vg)), Bt = csub(cdiv(wt, wg), cdiv(vt, vg));
+      const cplx Ab = cadd(cdiv(wbv, wg), cdiv(vbv, vg)), Bb = csub(cdiv(wbv, wg), cdiv(vbv, vg));
+      const cplx Ati = cinv(At), Abi = cinv(Ab);
+      const long long j = on + half * N + i;
+      // _s_reflection: (-A^-1 B, 2 A^-1, (A - B A^-1 B)/2, B A^-1)
+      pv.r11[j] = cneg(cmul(Ati, Bt));
+      pv.r12[j] = cscale(Ati, 2.0);
+      pv.r21[j] = cscale(csub(At, cmul(cmul(Bt, Ati), Bt)), 0.5);
+      pv.r22[j] = cmul(Bt, Ati);
+      // _s_transmission: (B A^-1, (A - B A^-1 B)/2, 2 A^-1, -A^-1 B)
+      pv.t11[j] = cmul(Bb, Abi);
+      pv.t21[j] = cscale(Abi, 2.0);
+    }
+  }
+  if (threadIdx.x == 0) { pv.nt[b] = nt; pv.nb[b] = nb; }
+}
+
+// --------------------------------------------------------------- Omega^2 assembly (GEMM)
+// Omega2[(rb,cb) quadrant] = (diag(k_rb) epz_i diag(k_cb) - [rb==cb] I) @ (cb ? epy : epx)
+//                            + diagonal term, k_0 = kx, k_1 = ky.
+__global__ void __launch_bounds__(256) omega2_kernel(int N, const cplx* __restrict__ conv, long long conv_ls,
+                                                     const int* __restrict__ pair_layer,
+                                                     const int* __restrict__ pair_solve,
+                                                     const double* __restrict__ kxa, const double* __restrict__ kya,
+                                                     cplx* __restrict__ out, long long out_bs) {
+  __shared__ cplx sA[8][65];
+  __shared__ cplx sB[8][65];
+  __shared__ double skr[64], skc_a[8];
+  const int pair = blockIdx.z >> 2, quad = blockIdx.z & 3, rb = quad & 1, cb = quad >> 1;
+  const int n = 2 * N;
+  const cplx* base = conv + (long long)pair_layer[pair] * conv_ls;
+  const long long NN = (long long)N * N;
+  const cplx* epx = base;
+  const cplx* epy = base + NN;
+  const cplx* epz = base + 2 * NN;
+  const cplx* Bm = cb ? epy : epx;
+  const double* kx = kxa + (long long)pair_solve[pair] * N;
+  const double* ky = kya + (long long)pair_solve[pair] * N;
+  const double* kr = rb ? ky : kx;
+  const double* kc = cb ? ky : kx;
+  cplx* C = out + pair * out_bs;
+  const int row0 = blockIdx.x * 64, col0 = blockIdx.y * 64;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  if (tid < 64) skr[tid] = (row0 + tid < N) ? kr[row0 + tid] : 0.0;
+  cplx acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = cmk(0.0, 0.0);
+  for (int k0 = 0; k0 < N; k0 += 8) {
+    if (tid < 8) skc_a[tid] = (k0 + tid < N) ? kc[k0 + tid] : 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      int idx = tid + e * 256;
+      int r = idx % 64, c = idx / 64;
+      int gr = row0 + r, gc = k0 + c;
+      cplx v = cmk(0.0, 0.0);
+      if (gr < N && gc < N) {
+        v = cscale(cscale(epz[gr + (long long)gc * N], skr[r]), skc_a[c]);
+        if (rb == cb && gr == gc) v.x -= 1.0;
+      }
+      sA[c][r] = v;
+    }
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      int idx = tid + e * 256;
+      int r = idx % 8, c = idx / 8;
+      int gr = k0 + r, gc = col0 + c;
+      sB[r][c] = (gr < N && gc < N) ? Bm[gr + (long long)gc * N] : cmk(0.0, 0.0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) {
+      cplx a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = sA[kk][tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = sB[kk][ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = cfma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int gr = row0 + tx + 16 * i;
+    if (gr >= N) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int gc = col0 + ty + 16 * j;
+      if (gc >= N) continue;
+      cplx v = acc[i][j];
+      if (gr == gc) {
+        double d;
+        if (rb == 0 && cb == 0) d = ky[gr] * ky[gr];
+        else if (rb == 1 && cb == 1) d = kx[gr] * kx[gr];
+        else d = -kx[gr] * ky[gr];
+        v.x += d;
+      }
+      C[(gr + rb * N) + (long long)(gc + cb * N) * n] = v;
+    }
+  }
+}
+
+// ---------------------------------------------------- q, the grazing screen, X = exp(-k0 d q)
+__global__ void modeq_kernel(int n_pairs, int n, const cplx* __restrict__ w, const int* __restrict__ pair_solve,
+                             const double* __restrict__ thick, const double* __restrict__ wavelength,
+                             cplx* __restrict__ q, cplx* __restrict__ X, int32_t* __restrict__ status,
+                             int layers_per_solve) {
+  __shared__ double smin[32], smax[32];
+  const int p = blockIdx.x;
+  const cplx* wp = w + (long long)p * n;
+  const double k0 = 2.0 * 3.141592653589793 / wavelength[pair_solve[p]];
+  const double d = thick[p];
+  double lo = INFINITY, hi = 0.0;
+  bool bad = false;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    cplx wi = wp[i];
+    if (!(isfinite(wi.x) && isfinite(wi.y))) bad = true;
+    double a = cabsv(wi);
+    lo = fmin(lo, a); hi = fmax(hi, a);
+    // mode_q: Re q >= 0, tie Im q <= 0 when |Re q| <= 1e-12
+    cplx v = csqrt_p(wi);
+    bool flip = (fabs(v.x) > 1e-12) ? (v.x < 0.0) : (v.y > 0.0);
+    if (flip) v = cneg(v);
+    q[(long long)p * n + i] = v;
+    X[(long long)p * n + i] = cexp_(cscale(v, -k0 * d));
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, off));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, off));
+  }
+  if ((threadIdx.x & 31) == 0) { smin[threadIdx.x >> 5] = lo; smax[threadIdx.x >> 5] = hi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { lo = fmin(lo, smin[k]); hi = fmax(hi, smax[k]); }
+    lo = fmin(lo, smin[0]); hi = fmax(hi, smax[0]);
+    int32_t* st = status + pair_solve[p];
+    if (lo < 1e-9 * hi) wb_flag(st, WB_ST_GRAZING);
+  }
+  if (bad) wb_flag(status + pair_solve[p], WB_ST_NONFINITE);
+  (void)layers_per_solve;
+}
+
+// ------------------------------------------------------------ V = Omega_R W / q, rotated
+// V_top = -epy W_bot - diag(kx ky) W_top + diag(kx^2) W_bot
+// V_bot =  epx W_top - diag(ky^2) W_top + diag(ky kx) W_bot
+__global__ void __launch_bounds__(256) vmodes_kernel(int N, const cplx* __restrict__ conv, long long conv_ls,
+                                                     const int* __restrict__ pair_layer,
+                                                     const int* __restrict__ pair_solve,
+                                                     const double* __restrict__ kxa, const double* __restrict__ kya,
+                                                     const cplx* __restrict__ Wall, const cplx* __restrict__ qall,
+                                                     cplx* __restrict__ Vall, long long bs) {
+  __shared__ cplx sA[8][65];
+  __shared__ cplx sB[8][65];
+  const int pair = blockIdx.z >> 1, half = blockIdx.z & 1;
+  const int n = 2 * N;
+  const long long NN = (long long)N * N;
+  const cplx* base = conv + (long long)pair_layer[pair] * conv_ls;
+  const cplx* Am = half ? base : base + NN;       // epx for the bottom half, epy for the top
+  const double sgn = half ? 1.0 : -1.0;
+  const double* kx = kxa + (long long)pair_solve[pair] * N;
+  const double* ky = kya + (long long)pair_solve[pair] * N;
+  const cplx* W = Wall + pair * bs;
+  const cplx* Wsrc = W + (half ? 0 : N);            // rows of W multiplied: W_top (bottom half) / W_bot (top)
+  const cplx* q = qall + (long long)pair * n;
+  cplx* V = Vall + pair * bs;
+  const int row0 = blockIdx.x * 64, col0 = blockIdx.y * 64;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  cplx acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = cmk(0.0, 0.0);
+  for (int k0 = 0; k0 < N; k0 += 8) {
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      int idx = tid + e * 256;
+      int r = idx % 64, c = idx / 64;
+      int gr = row0 + r, gc = k0 + c;
+      sA[c][r] = (gr < N && gc < N) ? cscale(Am[gr + (long long)gc * N], sgn) : cmk(0.0, 0.0);
+    }
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      int idx = tid + e * 256;
+      int r = idx % 8, c = idx / 8;
+      int gr = k0 + r, gc = col0 + c;
+      sB[r][c] = (gr < N && gc < n) ? Wsrc[gr + (long long)gc * n] : cmk(0.0, 0.0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) {
+      cplx a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = sA[kk][tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = sB[kk][ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = cfma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int gr = row0 + tx + 16 * i;
+    if (gr >= N) continue;
+    const double kxi = kx[gr], kyi = ky[gr];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int gc = col0 + ty + 16 * j;
+      if (gc >= n) continue;
+      const cplx wt = W[gr + (long long)gc * n], wb = W[gr + N + (long long)gc * n];
+      cplx v = acc[i][j];
+      if (half == 0) { v = cadd(v, cscale(wt, -kxi * kyi)); v = cadd(v, cscale(wb, kxi * kxi)); }
+      else { v = cadd(v, cscale(wt, -kyi * kyi)); v = cadd(v, cscale(wb, kyi * kxi)); }
+      V[gr + half * N + (long long)gc * n] = cdiv(v, q[gc]);
+    }
+  }
+}
+
+// s/p rotation of W and V in place (solve_2d.py:2584-2616)
+__global__ void sp_rotate_kernel(int n_pairs, int N, const int* __restrict__ pair_solve, const double* __restrict__ ca,
+                                 const double* __restrict__ sa, cplx* __restrict__ Wall, cplx* __restrict__ Vall,
+                                 long long bs) {
+  const int n = 2 * N;
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)n_pairs * N * n) return;
+  const long long pair = idx / ((long long)N * n);
+  const long long rem = idx % ((long long)N * n);
+  const int i = (int)(rem % N), j = (int)(rem / N);
+  const long long o = (long long)pair_solve[pair] * N + i;
+  const double c = ca[o], s = sa[o];
+  cplx* W = Wall + pair * bs;
+  cplx* V = Vall + pair * bs;
+  const long long a = i + (long long)j * n, b = a + N;
+  const cplx w1 = W[a], w2 = W[b], v1 = V[a], v2 = V[b];
+  W[a] = csub(cscale(w2, c), cscale(w1, s));
+  W[b] = cadd(cscale(w1, c), cscale(w2, s));
+  V[a] = cadd(cscale(v1, c), cscale(v2, s));
+  V[b] = csub(cscale(v2, c), cscale(v1, s));
+}
+
+// ------------------------------------------------------------------ cascade elementwise
+// R_{L+1} = diag(t11)
+__global__ void diag_matrix_kernel(int B, int n, const cplx* __restrict__ d, cplx* __restrict__ R, long long bs) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * n * n) return;
+  const long long b = idx / ((long long)n * n), rem = idx % ((long long)n * n);
+  const int i = (int)(rem % n), j = (int)(rem / n);
+  R[b * bs + rem] = (i == j) ? d[b * n + i] : cmk(0.0, 0.0);
+}
+
+// U1 = diag(wg)(I + R), U2 = diag(vg)(I - R)
+__global__ void u12_kernel(int B, int n, const cplx* __restrict__ R, long long r_bs, const cplx* __restrict__ wg,
+                           const cplx* __restrict__ vg, cplx* __restrict__ U1, cplx* __restrict__ U2, long long bs) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * n * n) return;
+  const long long b = idx / ((long long)n * n), rem = idx % ((long long)n * n);
+  const int i = (int)(rem % n), j = (int)(rem / n);
+  cplx r = R[b * r_bs + rem];
+  cplx e = cmk(i == j ? 1.0 : 0.0, 0.0);
+  U1[b * bs + rem] = cmul(wg[b * n + i], cadd(e, r));
+  U2[b * bs + rem] = cmul(vg[b * n + i], csub(e, r));
+}
+
+
+// from rho_b^T: Y1T = (I - X rho_b X)^T into Y1, Y2T = (I + X rho_b X)^T in place
+__global__ void rho_kernel(int B, int n, cplx* __restrict__ RT, cplx* __restrict__ Y1, const cplx* __restrict__ X,
+                           long long x_ps, long long bs) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * n * n) return;
+  const long long b = idx / ((long long)n * n), rem = idx % ((long long)n * n);
+  const int jr = (int)(rem % n), ic = (int)(rem / n);     // RT(jr, ic) = rho_b(ic, jr)
+  const cplx* Xb = X + b * x_ps;
+  cplx r = cmul(cmul(Xb[ic], RT[b * bs + rem]), Xb[jr]);
+  cplx e = cmk(jr == ic ? 1.0 : 0.0, 0.0);
+  Y1[b * bs + rem] = csub(e, r);
+  RT[b * bs + rem] = cadd(e, r);
+}
+
+
+// incident columns: [a_s d; -i n_top a_p d], pure s, pure p (d = unit vector on the specular order)
+__global__ void incident_kernel(int B, int N, const cplx* __restrict__ pol, const cplx* __restrict__ nt,
+                                cplx* __restrict__ C, long long c_bs) {
+  const int n = 2 * N;
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * n * 3) return;
+  const long long b = idx / (n * 3);
+  const int rem = (int)(idx % (n * 3));
+  const int i = rem % n, col = rem / n;
+  const int spec = N / 2;
+  cplx as, ap;
+  if (col == 0) { as = pol[2 * b]; ap = pol[2 * b + 1]; }
+  else if (col == 1) { as = cmk(1.0, 0.0); ap = cmk(6.123233995736766e-17, 0.0); }   // sin/cos(pi/2)
+  else { as = cmk(0.0, 0.0); ap = cmk(1.0, 0.0); }
+  cplx v = cmk(0.0, 0.0);
+  if (i == spec) v = as;
+  else if (i == N + spec) v = cmul(cmul(cmk(0.0, -1.0), nt[b]), ap);
+  C[b * c_bs + i + (long long)col * n] = v;
+}
+
+// G0 = I - diag(r22) R1 ; rhs = diag(r21) C
+__global__ void top_kernel(int B, int n, const cplx* __restrict__ R1, long long r_bs, const cplx* __restrict__ r22,
+                           cplx* __restrict__ G0, long long bs) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * n * n) return;
+  const long long b = idx / ((long long)n * n), rem = idx % ((long long)n * n);
+  const int i = (int)(rem % n), j = (int)(rem / n);
+  cplx v = cneg(cmul(r22[b * n + i], R1[b * r_bs + rem]));
+  if (i == j) v.x += 1.0;
+  G0[b * bs + rem] = v;
+}
+
+// out = diag(d) * in (+ diag(e) * in2 if e), n x 3 per batch
+__global__ void dscale3_kernel(int B, int n, const cplx* __restrict__ d, const cplx* __restrict__ in, long long in_bs,
+                               const cplx* __restrict__ e, const cplx* __restrict__ in2, long long in2_bs,
+                               cplx* __restrict__ out, long long out_bs, double factor) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * n * 3) return;
+  const long long b = idx / (n * 3);
+  const int rem = (int)(idx % (n * 3)), i = rem % n;
+  cplx v = cmul(d[b * n + i], in[b * in_bs + rem]);
+  if (e) v = cadd(v, cmul(e[b * n + i], in2[b * in2_bs + rem]));
+  out[b * out_bs + rem] = cscale(v, factor);
+}
+
+// rhs1 = wg o (g + h), rhs2 = vg o (g - h)
+__global__ void gh_kernel(int B, int n, const cplx* __restrict__ g, const cplx* __restrict__ h,
+                          const cplx* __restrict__ wg, const cplx* __restrict__ vg,
+                          cplx* __restrict__ r1, cplx* __restrict__ r2, long long bs3) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * n * 3) return;
+  const long long b = idx / (n * 3);
+  const int rem = (int)(idx % (n * 3)), i = rem % n;
+  cplx gg = g[b * bs3 + rem], hh = h[b * bs3 + rem];
+  r1[b * bs3 + rem] = cmul(wg[b * n + i], cadd(gg, hh));
+  r2[b * bs3 + rem] = cmul(vg[b * n + i], csub(gg, hh));
+}
+
+// cb = X o (r1 + r2)/2 ; written into r1
+__global__ void ct_kernel(int B, int n, cplx* __restrict__ r1, const cplx* __restrict__ r2,
+                          const cplx* __restrict__ X, long long x_ps, long long bs3) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * n * 3) return;
+  const long long b = idx / (n * 3);
+  const int rem = (int)(idx % (n * 3)), i = rem % n;
+  cplx ct = cscale(cadd(r1[b * bs3 + rem], r2[b * bs3 + rem]), 0.5);
+  r1[b * bs3 + rem] = cscale(cmul(X[b * x_ps + i], ct), 2.0);
+}
+
+// per-order efficiencies (scattering.py:907-994, solve_1d.py:1588-1610, power.py:13-159)
+__global__ void efficiency_kernel(int B, int N, const cplx* __restrict__ cref, const cplx* __restrict__ ctrn,
+                                  long long bs3, PortVectors pv, const cplx* __restrict__ eps_top,
+                                  const cplx* __restrict__ eps_bot, const cplx* __restrict__ pol,
+                                  double* __restrict__ R, double* __restrict__ T, cplx* __restrict__ amps,
+                                  int32_t* __restrict__ status) {
+  const int n = 2 * N;
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * N * 3) return;
+  const long long b = idx / (N * 3);
+  const int rem = (int)(idx % (N * 3)), i = rem % N, col = rem / N;
+  const cplx et = eps_top[b], eb = eps_bot[b];
+  const cplx kzs = pv.kz_top[b * N + N / 2];
+  const double s_power = kzs.x;
+  const cplx nt = pv.nt[b], nb = pv.nb[b];
+  const double p_power = cabs2(nt) * cdiv(kzs, et).x;
+  double denom;
+  if (col == 0) denom = cabs2(pol[2 * b]) * s_power + cabs2(pol[2 * b + 1]) * p_power;
+  else if (col == 1) denom = s_power;
+  else denom = p_power;
+  const cplx Rs = cref[b * bs3 + i + (long long)col * n];
+  const cplx Rp = cneg(cref[b * bs3 + N + i + (long long)col * n]);
+  const cplx Ts = ctrn[b * bs3 + i + (long long)col * n];
+  const cplx Tp = ctrn[b * bs3 + N + i + (long long)col * n];
+  const cplx kzt = pv.kz_top[b * N + i], kzb = pv.kz_bot[b * N + i];
+  const double eRs = cabs2(Rs) * kzt.x / denom;
+  const double eRp = cabs2(Rp) * cdiv(kzt, et).x / denom;
+  const double eTs = cabs2(Ts) * kzb.x / denom;
+  const double eTp = cabs2(Tp) * cdiv(kzb, eb).x / denom;
+  const double r = eRs + eRp, t = eTs + eTp;
+  R[(b * 3 + col) * N + i] = r;
+  T[(b * 3 + col) * N + i] = t;
+  if (amps) {
+    const cplx mi_nt = cmul(cmk(0.0, -1.0), nt), mi_nb = cmul(cmk(0.0, -1.0), nb);
+    cplx* a = amps + ((b * 3 + col) * 4) * (long long)N;
+    a[i] = Rs; a[N + i] = cdiv(Rp, mi_nt); a[2 * N + i] = Ts; a[3 * N + i] = cdiv(Tp, mi_nb);
+  }
+  if (!(isfinite(r) && isfinite(t))) wb_flag(status + b, WB_ST_NONFINITE);
+}
+
+static inline unsigned nblk(long long total, int per) { return (unsigned)((total + per - 1) / per); }
+
+__global__ void pairs_kernel(int B, int L, const int* __restrict__ layer_index, const double* __restrict__ thick,
+                             int* __restrict__ pair_layer, int* __restrict__ pair_solve, double* __restrict__ pair_thick) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= B * L) return;
+  pair_layer[p] = layer_index[p];
+  pair_solve[p] = p / L;
+  pair_thick[p] = thick[p];
+}
+
+__global__ void copy3_kernel(int B, int n, const cplx* __restrict__ src, long long s_bs, cplx* __restrict__ dst,
+                             long long d_bs) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * n * 3) return;
+  const long long b = idx / (n * 3);
+  const int rem = (int)(idx % (n * 3));
+  dst[b * d_bs + rem] = src[b * s_bs + rem];
+}
+
+// M = P1 + P2 (to Mout, batch stride m_bs), NT = (P1 - P2)^T ; 32x32 tiles
+__global__ void mn2_kernel(int n, const cplx* __restrict__ P1, const cplx* __restrict__ P2, long long p_bs,
+                           cplx* __restrict__ Mout, long long m_bs, cplx* __restrict__ NT) {
+  __shared__ cplx t[32][33];
+  const long long b = blockIdx.z;
+  const cplx* p1 = P1 + b * p_bs; const cplx* p2 = P2 + b * p_bs;
+  cplx* mo = Mout + b * m_bs; cplx* nt = NT + b * p_bs;
+  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+  for (int e = threadIdx.y; e < 32; e += blockDim.y) {
+    int i = i0 + threadIdx.x, j = j0 + e;
+    if (i < n && j < n) {
+      long long o = i + (long long)j * n;
+      cplx a = p1[o], c = p2[o];
+      mo[o] = cadd(a, c);
+      t[e][threadIdx.x] = csub(a, c);
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.y; e < 32; e += blockDim.y) {
+    int j = j0 + threadIdx.x, i = i0 + e;
+    if (i < n && j < n) nt[j + (long long)i * n] = t[threadIdx.x][e];
+  }
+}
+
+// Aterm = X1 diag(wg) + X2 diag(vg) (to Aout), Bterm = -X1 diag(wg) + X2 diag(vg) (to Bout)
+__global__ void ab2_kernel(int n, const cplx* __restrict__ X1T, const cplx* __restrict__ X2T, long long x_bs,
+                           const cplx* __restrict__ wg, const cplx* __restrict__ vg,
+                           cplx* __restrict__ Aout, long long a_bs, cplx* __restrict__ Bout, long long b_bs) {
+  __shared__ cplx t1[32][33], t2[32][33];
+  const long long b = blockIdx.z;
+  const cplx* x1 = X1T + b * x_bs; const cplx* x2 = X2T + b * x_bs;
+  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+  for (int e = threadIdx.y; e < 32; e += blockDim.y) {
+    int j = j0 + threadIdx.x, i = i0 + e;
+    if (i < n && j < n) {
+      long long o = j + (long long)i * n;
+      t1[e][threadIdx.x] = x1[o];
+      t2[e][threadIdx.x] = x2[o];
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.y; e < 32; e += blockDim.y) {
+    int i = i0 + threadIdx.x, j = j0 + e;
+    if (i < n && j < n) {
+      cplx a1 = cmul(t1[threadIdx.x][e], wg[b * n + j]);
+      cplx a2 = cmul(t2[threadIdx.x][e], vg[b * n + j]);
+      long long o = i + (long long)j * n;
+      Aout[b * a_bs + o] = cadd(a1, a2);
+      Bout[b * b_bs + o] = csub(a2, a1);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------- orchestration
+// Workspace of one chunk of `chunk` solves with L layers of N orders (n = 2N):
+//   per (solve, layer) pair: OM (Omega2 -> T -> W -> bigW LU), Zb (Z -> V -> bigV LU),
+//   Xv (X eigvecs -> M_k LU), R_k; per solve: R_L, three n x n scratch matrices.
+size_t solve_chunk_bytes(int N, int L, int chunk) {
+  const size_t n = 2 * (size_t)N, n2 = n * n, P = (size_t)chunk * L;
+  size_t b = 0;
+  auto A = [&](size_t x) { b += (x + 255) & ~(size_t)255; };
+  A(sizeof(double) * chunk * N); A(sizeof(double) * chunk * N); A(sizeof(double) * chunk * N);
+  A(sizeof(double) * chunk * N);
+  A(sizeof(cplx) * chunk * N); A(sizeof(cplx) * chunk * N);
+  for (int k = 0; k < 8; ++k) A(sizeof(cplx) * chunk * n);
+  A(sizeof(cplx) * chunk); A(sizeof(cplx) * chunk);
+  A(sizeof(int) * P); A(sizeof(int) * P); A(sizeof(double) * P);
+  A(sizeof(cplx) * P * n2); A(sizeof(cplx) * P * n2); A(sizeof(cplx) * P * n2);
+  for (int k = 0; k < 4; ++k) A(sizeof(cplx) * P * n);
+  A(sizeof(int) * P * n); A(sizeof(int) * P * n); A(sizeof(int) * P * n);
+  A(sizeof(cplx) * (P + chunk) * n2);
+  A(sizeof(cplx) * chunk * n2); A(sizeof(cplx) * chunk * n2); A(sizeof(cplx) * chunk * n2);
+  A(sizeof(int) * chunk * n);
+  for (int k = 0; k < 6; ++k) A(sizeof(cplx) * chunk * n * 3);
+  return b;
+}
+
+int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int count, const SolveOut& out) {
+  const int N = (2 * d.hu + 1) * (2 * d.hv + 1), n = 2 * N, L = d.n_layers;
+  const long long n2 = (long long)n * n, NN = (long long)N * N;
+  const int Bc = count, P = Bc * L;
+  int32_t* st = out.status + first;
+  ar.reset();
+  PortVectors pv;
+  pv.kx = ar.get<double>((size_t)Bc * N); pv.ky = ar.get<double>((size_t)Bc * N);
+  pv.c = ar.get<double>((size_t)Bc * N); pv.s = ar.get<double>((size_t)Bc * N);
+  pv.kz_top = ar.get<cplx>((size_t)Bc * N); pv.kz_bot = ar.get<cplx>((size_t)Bc * N);
+  pv.wg = ar.get<cplx>((size_t)Bc * n); pv.vg = ar.get<cplx>((size_t)Bc * n);
+  pv.r11 = ar.get<cplx>((size_t)Bc * n); pv.r12 = ar.get<cplx>((size_t)Bc * n);
+  pv.r21 = ar.get<cplx>((size_t)Bc * n); pv.r22 = ar.get<cplx>((size_t)Bc * n);
+  pv.t11 = ar.get<cplx>((size_t)Bc * n); pv.t21 = ar.get<cplx>((size_t)Bc * n);
+  pv.nt = ar.get<cplx>(Bc); pv.nb = ar.get<cplx>(Bc);
+  int* pair_layer = ar.get<int>(P);
+  int* pair_solve = ar.get<int>(P);
+  double* pair_thick = ar.get<double>(P);
+  cplx* OM = ar.get<cplx>((size_t)P * n2);
+  cplx* Zb = ar.get<cplx>((size_t)P * n2);
+  cplx* Xv = ar.get<cplx>((size_t)P * n2);
+  cplx* w = ar.get<cplx>((size_t)P * n);
+  cplx* q = ar.get<cplx>((size_t)P * n);
+  cplx* X = ar.get<cplx>((size_t)P * n);
+  cplx* tau = ar.get<cplx>((size_t)P * n);
+  int* pivW = ar.get<int>((size_t)P * n);
+  int* pivV = ar.get<int>((size_t)P * n);
+  int* pivM = ar.get<int>((size_t)P * n);
+  cplx* Rk = ar.get<cplx>((size_t)(P + Bc) * n2);
+  cplx* S1 = ar.get<cplx>((size_t)Bc * n2);
+  cplx* S2 = ar.get<cplx>((size_t)Bc * n2);
+  cplx* S3 = ar.get<cplx>((size_t)Bc * n2);
+  int* pivS = ar.get<int>((size_t)Bc * n);
+  cplx* Cin = ar.get<cplx>((size_t)Bc * n * 3);
+  cplx* g = ar.get<cplx>((size_t)Bc * n * 3);
+  cplx* h = ar.get<cplx>((size_t)Bc * n * 3);
+  cplx* r1 = ar.get<cplx>((size_t)Bc * n * 3);
+  cplx* r2 = ar.get<cplx>((size_t)Bc * n * 3);
+  cplx* cref = ar.get<cplx>((size_t)Bc * n * 3);
+  if (!ar.ok()) return -1;
+
+  ports_kernel<<<Bc, 128, 0, s>>>(Bc, d.hu, d.hv, d.wavelength + first, d.period + 2 * first, d.theta + first,
+                                  d.phi + first, d.eps_top + first, d.eps_bot + first, pv); note_launch();
+  pairs_kernel<<<nblk(P, 128), 128, 0, s>>>(Bc, L, d.layer_index + (long long)first * L,
+                                            d.thickness + (long long)first * L, pair_layer, pair_solve, pair_thick); note_launch();
+  // ---------------- stage B: modes of every (solve, layer) pair, p = b * L + l
+  const long long conv_ls = 3 * NN;
+  {
+    dim3 gr((N + 63) / 64, (N + 63) / 64, P * 4);
+    omega2_kernel<<<gr, 256, 0, s>>>(N, d.conv, conv_ls, pair_layer, pair_solve, pv.kx, pv.ky, OM, n2); note_launch();
+  }
+  zgeev_schur(s, P, n, OM, n, n2, Zb, n, n2, w, tau, st, L);
+  ztrevc(s, P, n, OM, n, n2, Xv, n, n2);
+  zgemm(s, P, n, n, n, cmk(1, 0), Zb, 1, n, n2, Xv, 1, n, n2, cmk(0, 0), OM, 1, n, n2);   // W = Z X
+  znormalize_columns(s, P, n, OM, n, n2);
+  modeq_kernel<<<P, 256, 0, s>>>(P, n, w, pair_solve, pair_thick, d.wavelength + first, q, X, st, L); note_launch();
+  {
+    dim3 gr((N + 63) / 64, (n + 63) / 64, P * 2);
+    vmodes_kernel<<<gr, 256, 0, s>>>(N, d.conv, conv_ls, pair_layer, pair_solve, pv.kx, pv.ky, OM, q, Zb, n2); note_launch();
+  }
+  sp_rotate_kernel<<<nblk((long long)P * N * n, 256), 256, 0, s>>>(P, N, pair_solve, pv.c, pv.s, OM, Zb, n2); note_launch();
+  zgetrf(s, P, n, OM, n, n2, pivW, n, st, L);     // LU(bigW)
+  zgetrf(s, P, n, Zb, n, n2, pivV, n, st, L);     // LU(bigV)
+
+  // ---------------- stage C: bottom-up reflections R_k (per solve L+1 matrices, R_L = diag(t11))
+  const long long lay_bs = (long long)L * n2;     // solve stride of per-pair matrices
+  const long long lay_ps = (long long)L * n;      // solve stride of per-pair vectors / pivots
+  const long long r_bs = (long long)(L + 1) * n2;
+  diag_matrix_kernel<<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, pv.t11, Rk + (long long)L * n2, r_bs); note_launch();
+  const dim3 tgrid((n + 31) / 32, (n + 31) / 32, Bc), tblk(32, 8);
+  for (int l = L - 1; l >= 0; --l) {
+    cplx* bW = OM + (long long)l * n2;  const int* pW = pivW + (long long)l * n;
+    cplx* bV = Zb + (long long)l * n2;  const int* pV = pivV + (long long)l * n;
+    cplx* M = Xv + (long long)l * n2;   int* pM = pivM + (long long)l * n;
+    const cplx* Rb = Rk + (long long)(l + 1) * n2;
+    u12_kernel<<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, Rb, r_bs, pv.wg, pv.vg, S1, S2, n2); note_launch();
+    zgetrs(s, Bc, n, bW, n, lay_bs, pW, lay_ps, S1, n, n, n2, 0);           // P1 = bigW^-1 U1
+    zgetrs(s, Bc, n, bV, n, lay_bs, pV, lay_ps, S2, n, n, n2, 0);           // P2 = bigV^-1 U2
+    mn2_kernel<<<tgrid, tblk, 0, s>>>(n, S1, S2, n2, M, lay_bs, S3); note_launch();        // M, N^T
+    zgetrf(s, Bc, n, M, n, lay_bs, pM, lay_ps, st, 1);
+    zgetrs(s, Bc, n, M, n, lay_bs, pM, lay_ps, S3, n, n, n2, 1);            // rho_b^T = M^-T N^T
+    rho_kernel<<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, S3, S2, X + (long long)l * n, lay_ps, n2); note_launch();
+    zgetrs(s, Bc, n, bW, n, lay_bs, pW, lay_ps, S2, n, n, n2, 1);           // X1^T
+    zgetrs(s, Bc, n, bV, n, lay_bs, pV, lay_ps, S3, n, n, n2, 1);           // X2^T
+    cplx* Rl = Rk + (long long)l * n2;
+    ab2_kernel<<<tgrid, tblk, 0, s>>>(n, S2, S3, n2, pv.wg, pv.vg, S1, n2, Rl, r_bs); note_launch();
+    zgetrf(s, Bc, n, S1, n, n2, pivS, n, st, 1);
+    zgetrs(s, Bc, n, S1, n, n2, pivS, n, Rl, n, n, r_bs, 0);               // R_l
+  }
+  // ---------------- top-down pass with the three incidence columns
+  const long long v3 = (long long)n * 3;
+  incident_kernel<<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, N, d.pol + 2 * first, pv.nt, Cin, v3); note_launch();
+  top_kernel<<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, Rk, r_bs, pv.r22, S1, n2); note_launch();
+  zgetrf(s, Bc, n, S1, n, n2, pivS, n, st, 1);
+  dscale3_kernel<<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, pv.r21, Cin, v3, nullptr, nullptr, 0, g, v3, 1.0); note_launch();
+  zgetrs(s, Bc, n, S1, n, n2, pivS, n, g, 3, n, v3, 0);                     // g_0
+  zgemm(s, Bc, n, 3, n, cmk(1, 0), Rk, 1, n, r_bs, g, 1, n, v3, cmk(0, 0), h, 1, n, v3);
+  dscale3_kernel<<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, pv.r11, Cin, v3, pv.r12, h, v3, cref, v3, 1.0); note_launch();
+  for (int l = 0; l < L; ++l) {
+    cplx* bW = OM + (long long)l * n2;  const int* pW = pivW + (long long)l * n;
+    cplx* bV = Zb + (long long)l * n2;  const int* pV = pivV + (long long)l * n;
+    cplx* M = Xv + (long long)l * n2;   const int* pM = pivM + (long long)l * n;
+    if (l > 0) zgemm(s, Bc, n, 3, n, cmk(1, 0), Rk + (long long)l * n2, 1, n, r_bs, g, 1, n, v3, cmk(0, 0), h, 1, n, v3);
+    gh_kernel<<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, g, h, pv.wg, pv.vg, r1, r2, v3); note_launch();
+    zgetrs(s, Bc, n, bW, n, lay_bs, pW, lay_ps, r1, 3, n, v3, 0);
+    zgetrs(s, Bc, n, bV, n, lay_bs, pV, lay_ps, r2, 3, n, v3, 0);
+    ct_kernel<<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, r1, r2, X + (long long)l * n, lay_ps, v3); note_launch();
+    zgetrs(s, Bc, n, M, n, lay_bs, pM, lay_ps, r1, 3, n, v3, 0);             // g_{l+1}
+    copy3_kernel<<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, r1, v3, g, v3); note_launch();
+  }
+  dscale3_kernel<<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, pv.t21, g, v3, nullptr, nullptr, 0, h, v3, 1.0); note_launch();
+  efficiency_kernel<<<nblk((long long)Bc * N * 3, 256), 256, 0, s>>>(
+      Bc, N, cref, h, v3, pv, d.eps_top + first, d.eps_bot + first, d.pol + 2 * first,
+      out.R + (long long)first * 3 * N, out.T + (long long)first * 3 * N,
+      out.amps ? out.amps + (long long)first * 12 * N : nullptr, st); note_launch();
+  return 0;
+}
+
+// ------------------------------------------------------------- stage B door (wb_layer_modes)
+__global__ void iota_kernel(int n, int* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = i;
+}
+__global__ void fill_kernel(int n, double v, double* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = v;
+}
+
+size_t layer_modes_bytes(int N, int n_pairs) {
+  const size_t n = 2 * (size_t)N, n2 = n * n, P = n_pairs;
+  size_t b = 0;
+  auto A = [&](size_t x) { b += (x + 255) & ~(size_t)255; };
+  A(sizeof(int) * P); A(sizeof(double) * P); A(sizeof(double) * P);
+  A(sizeof(cplx) * P * n2); A(sizeof(cplx) * P * n2); A(sizeof(cplx) * P * n); A(sizeof(cplx) * P * n);
+  return b;
+}
+
+void layer_modes(cudaStream_t s, Arena& ar, int P, int N, const cplx* conv, const int* pair_layer,
+                 const double* kx, const double* ky, cplx* w, cplx* q, cplx* W, cplx* V, int32_t* status) {
+  const int n = 2 * N;
+  const long long n2 = (long long)n * n, NN = (long long)N * N;
+  ar.reset();
+  int* pair_solve = ar.get<int>(P);
+  double* zero = ar.get<double>(P);
+  double* lam = ar.get<double>(P);
+  cplx* Zb = ar.get<cplx>((size_t)P * n2);
+  cplx* Xv = ar.get<cplx>((size_t)P * n2);
+  cplx* tau = ar.get<cplx>((size_t)P * n);
+  cplx* X = ar.get<cplx>((size_t)P * n);
+  iota_kernel<<<nblk(P, 128), 128, 0, s>>>(P, pair_solve); note_launch();
+  fill_kernel<<<nblk(P, 128), 128, 0, s>>>(P, 0.0, zero); note_launch();
+  fill_kernel<<<nblk(P, 128), 128, 0, s>>>(P, 1.0, lam); note_launch();
+  if (status) cudaMemsetAsync(status, 0, sizeof(int32_t) * P, s);
+  {
+    dim3 gr((N + 63) / 64, (N + 63) / 64, P * 4);
+    omega2_kernel<<<gr, 256, 0, s>>>(N, conv, 3 * NN, pair_layer, pair_solve, kx, ky, W, n2); note_launch();
+  }
+  zgeev_schur(s, P, n, W, n, n2, Zb, n, n2, w, tau, status, 1);
+  ztrevc(s, P, n, W, n, n2, Xv, n, n2);
+  zgemm(s, P, n, n, n, cmk(1, 0), Zb, 1, n, n2, Xv, 1, n, n2, cmk(0, 0), W, 1, n, n2);
+  znormalize_columns(s, P, n, W, n, n2);
+  modeq_kernel<<<P, 256, 0, s>>>(P, n, w, pair_solve, zero, lam, q, X, status, 1); note_launch();
+  {
+    dim3 gr((N + 63) / 64, (n + 63) / 64, P * 2);
+    vmodes_kernel<<<gr, 256, 0, s>>>(N, conv, 3 * NN, pair_layer, pair_solve, kx, ky, W, q, V, n2); note_launch();
+  }
+}
+
+__global__ void regroup_kernel(int L, long long NN, const cplx* __restrict__ planes, cplx* __restrict__ out) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= 3LL * L * NN) return;
+  const long long slot = idx / ((long long)L * NN), rem = idx % ((long long)L * NN);
+  const long long layer = rem / NN, e = rem % NN;
+  out[(layer * 3 + slot) * NN + e] = planes[idx];
+}
+
+void regroup_slots(cudaStream_t s, int L, int N, const cplx* planes, cplx* out) {
+  long long NN = (long long)N * N;
+  regroup_kernel<<<nblk(3LL * L * NN, 256), 256, 0, s>>>(L, NN, planes, out); note_launch();
+}
+
+}  // namespace wb

@@ -1,0 +1,173 @@
+"""Torch-facing functional layer over libwbgpu.so: stage A, stage B and whole batched solves.
+
+Every function takes and returns CUDA tensors and runs on the current torch stream. Matrices
+handed to or returned by the library are column-major; the helpers here present them in the
+natural (row, column) orientation NumPy and the reference use.
+"""
+import numpy as np
+import torch
+
+from . import _lib
+
+
+def n_orders(hu, hv):
+    return (2 * hu + 1) * (2 * hv + 1)
+
+
+def _stream():
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _c128(x, device):
+    return torch.as_tensor(x, dtype=torch.complex128, device=device).contiguous()
+
+
+def _f64(x, device):
+    return torch.as_tensor(x, dtype=torch.float64, device=device).contiguous()
+
+
+class ConvStack:
+    """Convolution matrices of a set of layers in the library layout ``(L, 3, N, N)``:
+    slots ``epx, epy, epz_i``, each N x N column-major (rows ``i = n * n_u + m``)."""
+
+    def __init__(self, buf, hu, hv, status=None):
+        self.buf = buf
+        self.hu, self.hv = hu, hv
+        self.status = status
+
+    @property
+    def n_layers(self):
+        return self.buf.shape[0]
+
+    def slot(self, k):
+        """``(L, N, N)`` view of slot k in natural orientation."""
+        return self.buf[:, k].transpose(-1, -2)
+
+    @property
+    def epx(self):
+        return self.slot(0)
+
+    @property
+    def epy(self):
+        return self.slot(1)
+
+    @property
+    def epz_i(self):
+        return self.slot(2)
+
+    @classmethod
+    def from_matrices(cls, epx, epy, epz_i, hu, hv):
+        """Wrap natural-orientation ``(L, N, N)`` slots (e.g. the reference's corner frame)."""
+        buf = torch.stack([epx, epy, epz_i], dim=1).transpose(-1, -2).contiguous()
+        return cls(buf.to(torch.complex128), hu, hv)
+
+
+def assemble(eps, hu, hv, handle=None):
+    """Stage A: Li-rule convolution matrices of ``eps`` (L, ny, nx) (wb_assemble_li)."""
+    eps = _c128(eps, 'cuda')
+    L, ny, nx = eps.shape
+    N = n_orders(hu, hv)
+    h = handle or _lib.handle(eps.device.index or 0)
+    planes = torch.empty((3, L, N, N), dtype=torch.complex128, device=eps.device)
+    status = torch.zeros(1, dtype=torch.int32, device=eps.device)
+    _lib.check(h.lib.wb_assemble_li(h.h, eps.data_ptr(), L, ny, nx, hu, hv, planes[0].data_ptr(),
+                                    planes[1].data_ptr(), planes[2].data_ptr(), status.data_ptr(),
+                                    _stream()))
+    return ConvStack(planes.transpose(0, 1).contiguous(), hu, hv, status)
+
+
+def layer_modes(conv, pair_layer, kx, ky, precision='double', handle=None):
+    """Stage B for ``P`` pairs: ``(w, q, W, V, status)`` with W, V in natural orientation."""
+    dev = conv.buf.device
+    hu, hv = conv.hu, conv.hv
+    N = n_orders(hu, hv)
+    n = 2 * N
+    pair_layer = torch.as_tensor(pair_layer, dtype=torch.int32, device=dev).contiguous()
+    P = pair_layer.shape[0]
+    kx = _f64(kx, dev).reshape(P, N)
+    ky = _f64(ky, dev).reshape(P, N)
+    w = torch.empty((P, n), dtype=torch.complex128, device=dev)
+    q = torch.empty_like(w)
+    W = torch.empty((P, n, n), dtype=torch.complex128, device=dev)
+    V = torch.empty_like(W)
+    status = torch.zeros(P, dtype=torch.int32, device=dev)
+    h = handle or _lib.handle(dev.index or 0)
+    _lib.check(h.lib.wb_layer_modes(h.h, P, hu, hv, conv.buf.data_ptr(), pair_layer.data_ptr(),
+                                    kx.data_ptr(), ky.data_ptr(), w.data_ptr(), q.data_ptr(),
+                                    W.data_ptr(), V.data_ptr(), status.data_ptr(),
+                                    _lib.PRECISION[precision], _stream()))
+    return w, q, W.transpose(-1, -2), V.transpose(-1, -2), status
+
+
+class BatchInputs:
+    """Per-solve parameters of one batch, as contiguous device tensors."""
+
+    def __init__(self, layer_index, thickness, wavelength, period, theta, phi, eps_top, eps_bot, pol,
+                 device='cuda'):
+        self.layer_index = torch.as_tensor(layer_index, dtype=torch.int32, device=device).contiguous()
+        B, L = self.layer_index.shape
+        self.B, self.L = B, L
+        self.thickness = _f64(thickness, device).reshape(B, L)
+        self.wavelength = _f64(wavelength, device).reshape(B)
+        self.period = _f64(period, device).reshape(B, 2)
+        self.theta = _f64(theta, device).reshape(B)
+        self.phi = _f64(phi, device).reshape(B)
+        self.eps_top = _c128(eps_top, device).reshape(B)
+        self.eps_bot = _c128(eps_bot, device).reshape(B)
+        self.pol = _c128(pol, device).reshape(B, 2)
+
+
+def solve_batch(conv, inp, precision='double', amplitudes=False, handle=None, out=None):
+    """Stages B and C for a batch (wb_solve_batch). Returns ``(R, T, status[, amps])`` with R, T
+    of shape ``(B, 3, n_v, n_u)`` for [given polarization, pure s, pure p]."""
+    dev = conv.buf.device
+    hu, hv = conv.hu, conv.hv
+    N = n_orders(hu, hv)
+    B, L = inp.B, inp.L
+    if out is None:
+        R = torch.empty((B, 3, N), dtype=torch.float64, device=dev)
+        T = torch.empty_like(R)
+        status = torch.zeros(B, dtype=torch.int32, device=dev)
+        amps = torch.empty((B, 3, 4, N), dtype=torch.complex128, device=dev) if amplitudes else None
+    else:
+        R, T, status, amps = out
+    h = handle or _lib.handle(dev.index or 0)
+    _lib.check(h.lib.wb_solve_batch(
+        h.h, B, L, hu, hv, conv.buf.data_ptr(), inp.layer_index.data_ptr(), inp.thickness.data_ptr(),
+        inp.wavelength.data_ptr(), inp.period.data_ptr(), inp.theta.data_ptr(), inp.phi.data_ptr(),
+        inp.eps_top.data_ptr(), inp.eps_bot.data_ptr(), inp.pol.data_ptr(), R.data_ptr(),
+        T.data_ptr(), amps.data_ptr() if amps is not None else None, status.data_ptr(),
+        _lib.PRECISION[precision], _stream()))
+    nu, nv = 2 * hu + 1, 2 * hv + 1
+    res = (R.view(B, 3, nv, nu), T.view(B, 3, nv, nu), status)
+    return res + ((amps,) if amplitudes else ())
+
+
+def solve_host(eps, layer_index, thickness, wavelength, period, theta, phi, eps_top, eps_bot, pol,
+               hu, hv, precision='double', handle=None):
+    """Whole solve from host (NumPy) buffers through ``wb_solve_host``."""
+    eps = np.ascontiguousarray(eps, dtype=np.complex128)
+    L, ny, nx = eps.shape
+    li = np.ascontiguousarray(layer_index, dtype=np.int32)
+    B = li.shape[0]
+    N = n_orders(hu, hv)
+    arrs = dict(th=np.ascontiguousarray(thickness, np.float64).reshape(B, li.shape[1]),
+                wl=np.ascontiguousarray(wavelength, np.float64).reshape(B),
+                per=np.ascontiguousarray(period, np.float64).reshape(B, 2),
+                theta=np.ascontiguousarray(theta, np.float64).reshape(B),
+                phi=np.ascontiguousarray(phi, np.float64).reshape(B),
+                et=np.ascontiguousarray(eps_top, np.complex128).reshape(B),
+                eb=np.ascontiguousarray(eps_bot, np.complex128).reshape(B),
+                pol=np.ascontiguousarray(pol, np.complex128).reshape(B, 2))
+    R = np.empty((B, 3, N), np.float64)
+    T = np.empty((B, 3, N), np.float64)
+    status = np.zeros(B, np.int32)
+    h = handle or _lib.handle(0)
+    _lib.check(h.lib.wb_solve_host(
+        h.h, B, li.shape[1], ny, nx, hu, hv, eps.ctypes.data, li.ctypes.data, arrs['th'].ctypes.data,
+        arrs['wl'].ctypes.data, arrs['per'].ctypes.data, arrs['theta'].ctypes.data,
+        arrs['phi'].ctypes.data, arrs['et'].ctypes.data, arrs['eb'].ctypes.data,
+        arrs['pol'].ctypes.data, R.ctypes.data, T.ctypes.data, status.ctypes.data,
+        _lib.PRECISION[precision]))
+    nu, nv = 2 * hu + 1, 2 * hv + 1
+    return R.reshape(B, 3, nv, nu), T.reshape(B, 3, nv, nu), status
