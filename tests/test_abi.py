@@ -1,0 +1,74 @@
+"""The C ABI library loads on a CPU-only host and exports every symbol its header declares;
+the host-only entry points behave (no GPU calls here)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, 'include', 'wavebit_gb300.h')
+
+
+def _declared():
+    text = open(HEADER).read()
+    text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
+    return sorted(set(re.findall(r'\b(wb_[a-z_0-9]+)\s*\(', text)))
+
+
+@pytest.fixture(scope='module')
+def lib():
+    from wavebit_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        import __graft_entry__ as g
+        g.build()
+    return _lib.load()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = _declared()
+    assert len(names) >= 10
+    for name in names:
+        assert hasattr(lib, name), name
+
+
+def test_binding_table_covers_the_header():
+    from wavebit_gb300 import _lib
+    assert set(_declared()) == set(_lib.SIGNATURES)
+
+
+def test_index_tables_are_bit_exact(lib):
+    from oracle import rcwa_oracle as O
+    for hu, hv in ((0, 0), (3, 1), (7, 7), (12, 5)):
+        nu, nv = 2 * hu + 1, 2 * hv + 1
+        lu, lv = np.zeros(nu, np.int32), np.zeros(nv, np.int32)
+        tu, tv = np.zeros(nu * nu, np.int32), np.zeros(nv * nv, np.int32)
+        assert lib.wb_build_indices(hu, hv, lu.ctypes.data, lv.ctypes.data, tu.ctypes.data, tv.ctypes.data) == 0
+        assert np.array_equal(lu, O.order_labels(hu)) and np.array_equal(lv, O.order_labels(hv))
+        assert np.array_equal(tu, O.toeplitz_positions(hu)) and np.array_equal(tv, O.toeplitz_positions(hv))
+
+
+def test_invalid_orders_are_refused_with_a_message(lib):
+    from wavebit_gb300 import _lib
+    rc = lib.wb_build_indices(-1, 2, None, None, None, None)
+    assert rc == _lib.WB_E_INVALID
+    assert 'orders' in _lib.last_error()
+
+
+def test_create_without_a_gpu_fails_cleanly(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip('a GPU is present')
+    from wavebit_gb300 import _lib
+    h = ctypes.c_void_p()
+    rc = lib.wb_create(0, 0, ctypes.byref(h))
+    assert rc == _lib.WB_E_CUDA and not h.value
+    assert 'device' in _lib.last_error().lower()
+
+
+def test_workspace_estimate_grows_with_the_chunk(lib):
+    a = lib.wb_solve_workspace_bytes(7, 7, 4, 16)
+    b = lib.wb_solve_workspace_bytes(7, 7, 4, 32)
+    assert 0 < a < b
+    assert lib.wb_solve_workspace_bytes(-1, 7, 4, 16) == 0

@@ -4,5 +4,6 @@
 """
 from . import _lib  # noqa: F401
 from . import engine  # noqa: F401
+from . import rcwa  # noqa: F401
 
-__all__ = ['engine']
+__all__ = ['engine', 'rcwa']

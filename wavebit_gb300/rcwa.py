@@ -1,0 +1,350 @@
+"""The ``rcwa.check -> prepare -> run`` lifecycle of the reference, as a GB300 backend.
+
+Mirrors ``wavebit.rcwa`` (rcwa/_lifecycle.py:422 ``check``, :737 ``prepare``, :698
+``Prepared.run``, :801 ``run``) for raster stacks under the default numerics (SMM, sampled
+Li coefficients, fixed nesting). It accepts the reference's own declaration objects
+(``wavebit.rcwa.Problem`` and friends) unchanged, by their attributes, or the small mirror
+dataclasses defined here when the reference is not installed. Results come back as torch
+tensors on the device with the reference's ``(wavelength, order_v, order_u)`` axes.
+
+Everything numerical runs in libwbgpu.so; there is no CPU path.
+"""
+from dataclasses import dataclass, field
+import math
+
+import numpy as np
+import torch
+
+from . import _lib, engine
+
+# ------------------------------------------------------------------------------- errors
+
+
+class WavebitError(Exception):
+    """Base error with a machine-readable ``code`` (errors.py:18-66 of the reference)."""
+    default_code = 'wavebit.error'
+
+    def __init__(self, message, *, code=None, path=None):
+        self.code = code or self.default_code
+        self.path = path
+        super().__init__(f'{path}: {message}' if path else message)
+
+
+class ValidationError(WavebitError, ValueError):
+    default_code = 'input.invalid'
+
+
+class UnsupportedFeatureError(ValidationError):
+    default_code = 'feature.unsupported'
+
+
+class NumericalError(WavebitError):
+    default_code = 'numerical.failure'
+
+# ------------------------------------------------------------- declarations (mirror)
+
+
+@dataclass(frozen=True)
+class Units:
+    length: str = 'm'
+
+
+@dataclass(frozen=True)
+class Material:
+    epsilon: object = 1.0
+    mu: object = None
+
+
+@dataclass(frozen=True)
+class Layer:
+    """A raster layer: ``epsilon`` is a ``(ny, nx)`` permittivity raster (rows along v) or a
+    scalar for a uniform layer."""
+    thickness: object
+    epsilon: object = None
+    background: object = None
+    regions: tuple = ()
+    mu: object = None
+
+
+@dataclass(frozen=True)
+class Stack:
+    """Bottom-to-top layers between two half spaces (problem.py:414)."""
+    layers: tuple = ()
+    top: object = field(default_factory=lambda: Material(1.0))
+    bottom: object = field(default_factory=lambda: Material(1.0))
+    period: object = (1.0, 1.0)
+    lattice: object = None
+
+
+@dataclass(frozen=True)
+class PlaneWave:
+    side: str = 'top'
+    polarization: object = 's'
+    amplitude: object = 1.0
+    theta: object = None
+    phi: object = None
+    kx: object = None
+    ky: object = None
+
+
+@dataclass(frozen=True)
+class Excitation:
+    wavelength: object
+    sources: tuple
+
+
+@dataclass(frozen=True)
+class Problem:
+    stack: Stack
+    excitation: Excitation
+    units: Units = field(default_factory=Units)
+
+
+@dataclass(frozen=True)
+class Numerics:
+    orders: tuple = (0, 0)
+    algorithm: str = 'smm'
+    fourier_coefficients: object = None
+    factorization: object = None
+    li_nesting: object = None
+    detuning: object = None
+    exceptional_points: str = 'rebuild'
+
+# ------------------------------------------------------------------------ resolution
+
+
+def _scalar_eps(material, path):
+    if material is None:
+        return 1.0 + 0j
+    if getattr(material, 'mu', None) not in (None, 1, 1.0):
+        raise UnsupportedFeatureError('magnetic half-spaces are outside the GB300 raster path',
+                                      code='feature.unsupported', path=path)
+    eps = getattr(material, 'epsilon', material)
+    if callable(eps):
+        raise UnsupportedFeatureError('dispersive materials are outside the GB300 raster path',
+                                      path=path)
+    return complex(np.asarray(eps).reshape(()))
+
+
+def _numerics_orders(numerics):
+    orders = tuple(int(v) for v in getattr(numerics, 'orders', (0, 0)))
+    if len(orders) != 2 or min(orders) < 0:
+        raise ValidationError('orders must be a pair of nonnegative integers', path='numerics.orders')
+    for name, allowed in (('algorithm', ('smm',)), ('fourier_coefficients', (None, 'sampled')),
+                          ('factorization', (None, 'li')), ('li_nesting', (None, 'fixed'))):
+        val = getattr(numerics, name, None)
+        if isinstance(val, str):
+            val = val.lower()
+        if val not in allowed:
+            raise UnsupportedFeatureError(
+                f'numerics.{name}={val!r}: the GB300 path implements {allowed[-1]!r} only',
+                path=f'numerics.{name}')
+    if getattr(numerics, 'detuning', None) is not None:
+        raise UnsupportedFeatureError('detuning is not implemented on the GB300 path',
+                                      path='numerics.detuning')
+    return orders
+
+
+def _resolve(problem, numerics):
+    """Problem -> flat arrays in kernel order (entry layer first)."""
+    stack = problem.stack
+    if getattr(stack, 'lattice', None) is not None:
+        raise UnsupportedFeatureError('oblique lattices are outside the GB300 raster path',
+                                      path='stack.lattice')
+    period = tuple(float(p) for p in stack.period)
+    if len(period) == 1:
+        period = (period[0], period[0])
+    layers = tuple(stack.layers)
+    if not layers:
+        raise ValidationError('the stack has no layers', path='stack.layers')
+    rasters, thick = [], []
+    for i, layer in enumerate(layers):
+        if getattr(layer, 'regions', ()):
+            raise UnsupportedFeatureError('region (shape) layers are outside the GB300 raster path',
+                                          path=f'stack.layers[{i}]')
+        if getattr(layer, 'mu', None) is not None:
+            raise UnsupportedFeatureError('magnetic layers are outside the GB300 raster path',
+                                          path=f'stack.layers[{i}].mu')
+        eps = layer.epsilon
+        if eps is None:
+            eps = _scalar_eps(layer.background, f'stack.layers[{i}].background')
+        eps = np.asarray(eps.detach().cpu().numpy() if hasattr(eps, 'detach') else eps, dtype=np.complex128)
+        if eps.ndim == 0:
+            eps = eps.reshape(1, 1)
+        if eps.ndim == 1:
+            eps = eps.reshape(1, -1)
+        if eps.ndim != 2 or not np.all(np.isfinite(eps)):
+            raise ValidationError('a layer raster must be a finite 2D array', path=f'stack.layers[{i}].epsilon')
+        d = float(np.asarray(layer.thickness.detach().cpu() if hasattr(layer.thickness, 'detach') else layer.thickness))
+        if not (d >= 0 and math.isfinite(d)):
+            raise ValidationError('thickness must be finite and >= 0', path=f'stack.layers[{i}].thickness')
+        rasters.append(eps)
+        thick.append(d)
+    # public order is bottom to top; kernels take the entry face (top) first
+    rasters, thick = rasters[::-1], thick[::-1]
+    eps_top = _scalar_eps(stack.top, 'stack.top')
+    eps_bot = _scalar_eps(stack.bottom, 'stack.bottom')
+    if eps_top.imag != 0 or eps_top.real <= 0:
+        raise UnsupportedFeatureError('the lit superstrate must be lossless with Re(eps) > 0',
+                                      path='stack.top')
+    exc = problem.excitation
+    wl = np.atleast_1d(np.asarray(exc.wavelength, dtype=np.float64)).reshape(-1)
+    if not np.all(wl > 0):
+        raise ValidationError('wavelengths must be positive', path='excitation.wavelength')
+    sources = tuple(exc.sources)
+    if len(sources) != 1:
+        raise UnsupportedFeatureError('one PlaneWave source per problem on the GB300 path',
+                                      path='excitation.sources')
+    src = sources[0]
+    if getattr(src, 'side', 'top') != 'top' or getattr(src, 'kx', None) is not None or getattr(src, 'ky', None) is not None:
+        raise UnsupportedFeatureError('top-side incidence given by theta/phi only', path='excitation.sources[0]')
+    theta = float(np.real(0.0 if src.theta is None else src.theta))
+    phi = float(np.real(0.0 if src.phi is None else src.phi))
+    if not abs(theta) < math.pi / 2:
+        raise ValidationError('theta must be a real angle below pi/2', path='excitation.sources[0].theta')
+    pol = src.polarization
+    if isinstance(pol, str):
+        if pol not in ('s', 'p'):
+            raise ValidationError("polarization must be 's', 'p' or an (s, p) pair")
+        a_s, a_p = (complex(1.0, 0.0), complex(math.cos(math.pi / 2))) if pol == 's' else (0j, 1 + 0j)
+    else:
+        a_s, a_p = (complex(v) for v in pol)
+        nrm = math.sqrt(abs(a_s) ** 2 + abs(a_p) ** 2)
+        a_s, a_p = a_s / nrm, a_p / nrm
+    orders = _numerics_orders(_numerics_or_default(numerics))
+    return dict(rasters=rasters, thickness=np.array(thick), period=period, eps_top=eps_top,
+                eps_bot=eps_bot, wavelengths=wl, theta=theta, phi=phi, pol=(a_s, a_p), orders=orders)
+
+
+def _numerics_or_default(numerics):
+    return Numerics() if numerics is None else numerics
+
+# -------------------------------------------------------------------------- lifecycle
+
+
+@dataclass
+class CheckReport:
+    issues: tuple
+    estimates: dict
+    resolved: dict
+
+
+def check(problem, *, numerics=None, backend='gb300', device='cuda', precision='double'):
+    """Admission without a solve (_lifecycle.py:422-457): report keys plus GB300 estimates."""
+    r = _resolve(problem, numerics)
+    hu, hv = r['orders']
+    N = engine.n_orders(hu, hv)
+    L = len(r['rasters'])
+    chunk = max(1, min(len(r['wavelengths']), 128))
+    ws = int(_lib.load().wb_solve_workspace_bytes(hu, hv, L, chunk))
+    est = {'retained_spatial_modes': N,
+           'one_dense_material_matrix_bytes': 16 * N * N,
+           'one_first_order_matrix_bytes': 16 * (2 * N) ** 2,
+           'device_workspace_bytes': ws,
+           'device_chunk': chunk}
+    if torch.cuda.is_available():
+        free, total = torch.cuda.mem_get_info()
+        est['device_free_bytes'] = int(free)
+        est['admissible'] = ws <= free
+    resolved = {'order_window': ((0, hu), (0, hv)), 'wavelength_count': len(r['wavelengths']),
+                'layer_count': L, 'fourier_coefficients': 'sampled', 'factorization': 'li',
+                'algorithm': 'smm', 'solve_path': '2d', 'backend': backend, 'device': device,
+                'precision': precision}
+    return CheckReport(issues=(), estimates=est, resolved=resolved)
+
+
+class Result:
+    """R and T with the reference's ``(wavelength, order_v, order_u)`` axes, on the device."""
+
+    def __init__(self, R, T, R_sp, T_sp, status, wavelengths, diagnostics, amplitudes=None):
+        self.R, self.T = R, T
+        self.outputs = {'incident': {'R': R, 'T': T},
+                        's_inc': {'R': R_sp[0], 'T': T_sp[0]},
+                        'p_inc': {'R': R_sp[1], 'T': T_sp[1]}}
+        self.status = status
+        self.wavelengths = wavelengths
+        self.diagnostics = diagnostics
+        self.amplitudes = amplitudes
+
+    @property
+    def absorption(self):
+        return 1.0 - self.R.sum(dim=(-2, -1)) - self.T.sum(dim=(-2, -1))
+
+
+class Prepared:
+    """Stage A done once and kept on the device (_lifecycle.py:698-733 ``Prepared.run``)."""
+
+    def __init__(self, problem, numerics, precision, handle):
+        self.problem = problem
+        self.numerics = numerics
+        self.precision = precision
+        self.handle = handle
+        r = _resolve(problem, numerics)
+        self.resolved = r
+        hu, hv = r['orders']
+        self.conv = _assemble_layers(r['rasters'], hu, hv, handle)
+
+    def run(self, problem=None, *, amplitudes=False):
+        r = self.resolved if problem is None else _resolve(problem, self.numerics)
+        conv = self.conv
+        if problem is not None and not _same_rasters(r['rasters'], self.resolved['rasters']):
+            conv = _assemble_layers(r['rasters'], *r['orders'], self.handle)
+        hu, hv = r['orders']
+        wl = r['wavelengths']
+        B, L = len(wl), len(r['rasters'])
+        inp = engine.BatchInputs(np.tile(np.arange(L), (B, 1)), np.tile(r['thickness'], (B, 1)), wl,
+                                 np.tile(r['period'], (B, 1)), np.full(B, r['theta']),
+                                 np.full(B, r['phi']), np.full(B, r['eps_top']),
+                                 np.full(B, r['eps_bot']), np.tile(r['pol'], (B, 1)))
+        out = engine.solve_batch(conv, inp, precision=self.precision, amplitudes=amplitudes,
+                                 handle=self.handle)
+        R, T, status = out[:3]
+        st = status.cpu().numpy()
+        bad = st & ~_lib.WB_ST_GRAZING
+        if np.any(bad & _lib.WB_ST_SINGULAR):
+            raise NumericalError('a factorization met an exact zero pivot', code='rcwa.singular')
+        if np.any(bad & (_lib.WB_ST_NONFINITE | _lib.WB_ST_NOCONV)):
+            raise NumericalError('the solve produced non-finite results', code='rcwa.nonfinite')
+        diag = {'solve_path': ('2d',) * B, 'effective_wavelengths': tuple(wl),
+                'grazing': tuple(bool(s & _lib.WB_ST_GRAZING) for s in st),
+                'status': st, 'precision': self.precision}
+        return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]), status, wl, diag,
+                      out[3] if amplitudes else None)
+
+
+def _same_rasters(a, b):
+    return len(a) == len(b) and all(x.shape == y.shape and np.array_equal(x, y) for x, y in zip(a, b))
+
+
+def _assemble_layers(rasters, hu, hv, handle):
+    """Stage A for every layer; rasters of different shapes are assembled separately."""
+    bufs = []
+    i = 0
+    while i < len(rasters):
+        j = i
+        while j < len(rasters) and rasters[j].shape == rasters[i].shape:
+            j += 1
+        eps = torch.as_tensor(np.stack(rasters[i:j]), device='cuda')
+        bufs.append(engine.assemble(eps, hu, hv, handle=handle).buf)
+        i = j
+    return engine.ConvStack(torch.cat(bufs, dim=0), hu, hv)
+
+
+def prepare(problem, *, numerics=None, backend='gb300', device='cuda', precision='double'):
+    """Resolve and assemble once (_lifecycle.py:737-797)."""
+    if backend not in ('gb300', 'cuda'):
+        raise ValidationError(f'backend {backend!r}: this package is the gb300 backend', path='backend')
+    if precision not in ('double', 'mixed'):
+        raise ValidationError("precision must be 'double' or 'mixed'", path='precision')
+    dev = torch.device(device)
+    if dev.type != 'cuda':
+        raise ValidationError('the GB300 backend runs on a CUDA device only; there is no CPU path',
+                              path='device')
+    handle = _lib.handle(dev.index or 0)
+    return Prepared(problem, numerics, precision, handle)
+
+
+def run(problem, *, numerics=None, backend='gb300', device='cuda', precision='double', amplitudes=False):
+    """``prepare(...).run()`` (_lifecycle.py:801-803)."""
+    return prepare(problem, numerics=numerics, backend=backend, device=device,
+                   precision=precision).run(amplitudes=amplitudes)
