@@ -159,7 +159,7 @@ def main():
     ap.add_argument('--steps', type=int, default=3)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
-    ap.add_argument('--precision', default='double', choices=['double', 'mixed'])
+    ap.add_argument('--precision', default='double', choices=['double', 'mixed', 'mixed_fp32'])
     ap.add_argument('--solves', type=int, default=128)
     ap.add_argument('--ref-sample', type=int, default=4)
     ap.add_argument('--no-cpu-baseline', action='store_true')

@@ -42,8 +42,9 @@ extern "C" {
 #define WB_ST_GRAZING 8    /* min|w| < 1e-9 max|w|: the reference rebuilds such a layer
                               (rcwa/_engine/solve_2d.py:2463-2482); the result is flagged */
 
-#define WB_PRECISION_FP64 0
-#define WB_PRECISION_MIXED 1
+#define WB_PRECISION_FP64 0        /* IEEE FP64 throughout */
+#define WB_PRECISION_MIXED 1       /* eigen-solve and cascade in double-float (2 x FP32) arithmetic */
+#define WB_PRECISION_MIXED_FP32 2  /* double-float eigen-solve, FP32 cascade */
 
 typedef struct { double re, im; } wb_complex;
 typedef struct wb_handle wb_handle;

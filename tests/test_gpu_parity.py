@@ -122,3 +122,44 @@ def test_solve_host_matches_oracle():
         scale = max(np.abs(o['R']).max(), np.abs(o['T']).max())
         assert np.abs(R[b] - o['R']).max() <= 1e-10 * scale
         assert np.abs(T[b] - o['T']).max() <= 1e-10 * scale
+
+
+@pytest.mark.parametrize('precision,tol', [('mixed', 1e-9), ('mixed_fp32', 1e-6)])
+def test_mixed_precision_within_tolerance(precision, tol):
+    """The mixed forms against the FP64 oracle: max |dR, dT| <= tol (1e-6 is the stated bound
+    for the FP32 cascade; the double-float form is held far tighter)."""
+    E = _engine()
+    rng = np.random.default_rng(21)
+    eps = np.stack([_rast(rng, 24, 24), _rast(rng, 24, 24), np.full((24, 24), -20 + 1.5j)])
+    hu = hv = 4
+    B = 6
+    wl = np.linspace(450, 950, B)
+    th = np.array([150.0, 230.0, 50.0])
+    conv = E.assemble(torch.as_tensor(eps, device='cuda'), hu, hv)
+    inp = E.BatchInputs(np.tile(np.arange(3), (B, 1)), np.tile(th, (B, 1)), wl, np.tile([900.0, 1000.0], (B, 1)),
+                        np.full(B, 0.3), np.full(B, 0.2), np.ones(B), np.full(B, 2.25), np.tile([0.6, 0.8], (B, 1)))
+    R, T, st = E.solve_batch(conv, inp, precision=precision)
+    torch.cuda.synchronize()
+    assert (st.cpu().numpy() & ~8 == 0).all()
+    worst = 0.0
+    for b in range(B):
+        o = O.solve_stack(eps, th, wl[b], (900.0, 1000.0), hu, hv, 0.3, 0.2, 1.0, 2.25, (0.6, 0.8))
+        worst = max(worst, np.abs(R[b].cpu().numpy() - o['R']).max(), np.abs(T[b].cpu().numpy() - o['T']).max())
+    assert worst <= tol, worst
+
+
+def test_layer_modes_double_float_eigenpairs():
+    """The double-float eigen-solve returns FP64-class eigenpairs."""
+    E = _engine()
+    rng = np.random.default_rng(5)
+    eps = np.stack([_rast(rng, 20, 20)])
+    hu = hv = 4
+    conv = E.assemble(torch.as_tensor(eps, device='cuda'), hu, hv)
+    kx, ky = O.separable_kxy(640.0, (900.0, 900.0), O.incident_kxy(0.2, 0.4, 1.0), hu, hv)
+    kxg, kyg = O.order_grid(kx, ky)
+    w, q, W, V, st = E.layer_modes(conv, [0], kxg.real[None], kyg.real[None], precision='mixed')
+    torch.cuda.synchronize()
+    om2, _ = O.layer_operator(kxg, kyg, *(s[0].cpu().numpy() for s in (conv.epx, conv.epy, conv.epz_i)))
+    wn, Wn = w[0].cpu().numpy(), W[0].cpu().numpy()
+    res = np.linalg.norm(om2 @ Wn - Wn * wn[None, :]) / (np.linalg.norm(om2) * np.linalg.norm(Wn))
+    assert res < 1e-12, res

@@ -128,7 +128,7 @@ int wb_assemble_li(wb_handle* h, const wb_complex* eps, int L, int ny, int nx, i
 
 size_t wb_solve_workspace_bytes(int hu, int hv, int L, int chunk) {
   if (!valid_orders(hu, hv) || L <= 0 || chunk <= 0) return 0;
-  return wb::solve_chunk_bytes((2 * hu + 1) * (2 * hv + 1), L, chunk);
+  return wb::solve_chunk_bytes((2 * hu + 1) * (2 * hv + 1), L, chunk, WB_PRECISION_FP64);
 }
 
 int wb_layer_modes(wb_handle* h, int n_pairs, int hu, int hv, const wb_complex* conv,
@@ -145,8 +145,8 @@ int wb_layer_modes(wb_handle* h, int n_pairs, int hu, int hv, const wb_complex* 
   size_t need = wb::layer_modes_bytes(N, n_pairs);
   int rc = reserve(h, need);
   if (rc) return rc;
-  wb::layer_modes(( cudaStream_t)stream, h->arena, n_pairs, N, (const cplx*)conv, (const int*)pair_layer, kx, ky,
-                  (cplx*)w, (cplx*)q, (cplx*)W, (cplx*)V, status);
+  wb::layer_modes((cudaStream_t)stream, h->arena, n_pairs, N, (const cplx*)conv, (const int*)pair_layer, kx, ky,
+                  (cplx*)w, (cplx*)q, (cplx*)W, (cplx*)V, status, precision);
   (void)n;
   return cuda_check("wb_layer_modes");
 }
@@ -161,14 +161,14 @@ int wb_solve_batch(wb_handle* h, int B, int L, int hu, int hv, const wb_complex*
       !eps_bot || !pol || !R || !T || !status)
     return fail(WB_E_INVALID, "wb_solve_batch: NULL argument");
   if (B <= 0 || L <= 0 || !valid_orders(hu, hv)) return fail(WB_E_INVALID, "wb_solve_batch: bad sizes B=%d L=%d", B, L);
-  if (precision != WB_PRECISION_FP64 && precision != WB_PRECISION_MIXED)
+  if (precision != WB_PRECISION_FP64 && precision != WB_PRECISION_MIXED && precision != WB_PRECISION_MIXED_FP32)
     return fail(WB_E_INVALID, "wb_solve_batch: precision %d", precision);
   cudaSetDevice(h->device);
   const int N = (2 * hu + 1) * (2 * hv + 1);
   // the largest chunk that fits the budget
   int chunk = B;
-  while (chunk > 1 && wb::solve_chunk_bytes(N, L, chunk) > h->budget) chunk = (chunk + 1) / 2;
-  size_t need = wb::solve_chunk_bytes(N, L, chunk);
+  while (chunk > 1 && wb::solve_chunk_bytes(N, L, chunk, precision) > h->budget) chunk = (chunk + 1) / 2;
+  size_t need = wb::solve_chunk_bytes(N, L, chunk, precision);
   int rc = reserve(h, need);
   if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
@@ -178,10 +178,9 @@ int wb_solve_batch(wb_handle* h, int B, int L, int hu, int hv, const wb_complex*
   wb::SolveOut o{R, T, (cplx*)amps, status};
   for (int first = 0; first < B; first += chunk) {
     int count = std::min(chunk, B - first);
-    if (wb::solve_chunk(s, h->arena, d, first, count, o) != 0)
+    if (wb::solve_chunk(s, h->arena, d, first, count, o, precision) != 0)
       return fail(WB_E_NOMEM, "wb_solve_batch: arena exhausted for a chunk of %d", count);
   }
-  (void)precision;
   return cuda_check("wb_solve_batch");
 }
 

@@ -1,38 +1,58 @@
-// Batched complex non-Hermitian eigen-decomposition, FP64, one CTA per matrix.
+// Batched complex non-Hermitian eigen-decomposition, one CTA per matrix, templated over the
+// real type R in {double, float, df64} (wb_num.cuh).
 //
 // The layer operator Omega^2 of every (solve, layer) pair is decomposed as
 //   Omega^2 = Z T Z^H  (Hessenberg reduction, then Francis single-shift QR to Schur form)
 //   Omega^2 W = W diag(w),  W = Z X  (X: eigenvectors of the triangular T by back-substitution)
 // which is the factorisation LAPACK's zgeev performs for numpy.linalg.eig (right vectors only).
 //
-// GB300 note: FP64 runs at ~1 TFLOP/s, i.e. about 2 FP64 FMAs per clock per SM. A rotation
-// applied across a row/column of a few hundred elements costs more in FP64 issue than in
-// latency, so a plain one-CTA-per-matrix layout with the matrix resident in L2/HBM keeps the
-// FP64 pipe busy; several CTAs per SM overlap each other's synchronisation latency.
+// GB300 note: FP64 runs at ~1 TFLOP/s, about 2 FP64 FMAs per clock per SM. A rotation applied
+// across a row/column of a few hundred elements costs more in FP64 issue than in latency, so a
+// one-CTA-per-matrix layout with the matrix resident in L2/HBM keeps the FP64 pipe busy. The
+// df64 instantiation (mixed form) runs the same algorithm on the FP32 pipes.
 //
 // Every iteration is capped; a matrix that hits the cap gets WB_ST_NOCONV in its status word
 // and NaN eigenvalues, and the kernel returns normally.
 #include "wb_common.cuh"
+#include "wb_num.cuh"
 #include "wb_kernels.h"
 
 namespace wb {
 
 constexpr int EIG_THREADS = 256;
+constexpr int QR_SEG = 32;             // bulge-chase steps per window
+constexpr int QR_WIN = QR_SEG + 3;     // window edge
+constexpr int QR_CH = 8;               // far-field register chunk
 
-__device__ double block_sum(double v, double* red) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+__device__ __forceinline__ double shfl_xor(double v, int off) { return __shfl_xor_sync(0xffffffffu, v, off); }
+__device__ __forceinline__ float shfl_xor(float v, int off) { return __shfl_xor_sync(0xffffffffu, v, off); }
+__device__ __forceinline__ df64 shfl_xor(df64 v, int off) {
+  return df64(__shfl_xor_sync(0xffffffffu, v.hi, off), __shfl_xor_sync(0xffffffffu, v.lo, off));
+}
+__device__ __forceinline__ double shfl_idx(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ float shfl_idx(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ df64 shfl_idx(df64 v, int src) {
+  return df64(__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src));
+}
+template <class R> __device__ __forceinline__ R warp_sum(R v) {
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  for (int off = 16; off > 0; off >>= 1) v = v + shfl_xor(v, off);
+  return v;
+}
+
+template <class R> __device__ R block_sum(R v, R* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = warp_sum(v);
   __syncthreads();
   if (lane == 0) red[warp] = v;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+    R s = R(0.0);
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s = s + red[w];
     red[0] = s;
   }
   __syncthreads();
-  double r = red[0];
+  R r = red[0];
   __syncthreads();
   return r;
 }
@@ -55,136 +75,132 @@ __device__ int block_max_int(int v, int* red) {
   return r;
 }
 
-// Householder reflector for (alpha, x): returns beta (real), tau and scales x in place so
-// that (I - tau v v^H)^H (alpha; x) = (beta; 0), v = (1; x_scaled).
-struct Refl { double beta; cplx tau; cplx scale; bool identity; };
-__device__ __forceinline__ Refl make_reflector(cplx alpha, double xnorm) {
-  Refl r;
-  if (xnorm == 0.0 && alpha.y == 0.0) {
-    r.identity = true; r.beta = alpha.x; r.tau = cmk(0.0, 0.0); r.scale = cmk(0.0, 0.0);
+// Householder reflector for (alpha, x): returns beta (real), tau and the scale of x so that
+// (I - tau v v^H)^H (alpha; x) = (beta; 0), v = (1; x * scale).
+template <class R> struct Refl { R beta; Cx<R> tau; Cx<R> scale; bool identity; };
+template <class R> __device__ __forceinline__ Refl<R> make_reflector(Cx<R> alpha, R xnorm) {
+  Refl<R> r;
+  if (xnorm == R(0.0) && alpha.y == R(0.0)) {
+    r.identity = true; r.beta = alpha.x; r.tau = cxzero<R>(); r.scale = cxzero<R>();
     return r;
   }
-  double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm * xnorm);
-  double beta = (alpha.x >= 0.0) ? -nrm : nrm;
+  R ax = rabs(alpha.x), ay = rabs(alpha.y);
+  R m = rmax(rmax(ax, ay), xnorm);
+  R u = ax / m, v = ay / m, w = xnorm / m;
+  R nrm = m * rsqrt_(u * u + v * v + w * w);
+  R beta = (alpha.x >= R(0.0)) ? -nrm : nrm;
   r.identity = false;
   r.beta = beta;
-  r.tau = cmk((beta - alpha.x) / beta, -alpha.y / beta);
-  r.scale = cinv(cmk(alpha.x - beta, alpha.y));
+  r.tau = cxmk<R>((beta - alpha.x) / beta, -alpha.y / beta);
+  r.scale = cxinv(cxmk<R>(alpha.x - beta, alpha.y));
   return r;
 }
 
 // ------------------------------------------------------------- 1. Hessenberg reduction
 // H := Q^H A Q, reflectors stored below the subdiagonal (v_0 = 1 implicit), tau[k].
-__global__ void __launch_bounds__(EIG_THREADS) zgehrd_kernel(cplx* __restrict__ Aall, int n, int lda,
-                                                             long long a_bs, cplx* __restrict__ tau_all,
-                                                             cplx* __restrict__ work_all) {
-  extern __shared__ cplx sv[];         // v (n), then y/z (n)
-  __shared__ double red[32];
-  __shared__ cplx s_tau;
-  cplx* A = Aall + blockIdx.x * a_bs;
-  cplx* tau = tau_all + (long long)blockIdx.x * n;
-  cplx* sy = sv + n;
+template <class R>
+__global__ void __launch_bounds__(EIG_THREADS) gehrd_kernel(Cx<R>* __restrict__ Aall, int n, int lda,
+                                                            long long a_bs, Cx<R>* __restrict__ tau_all) {
+  using C_ = Cx<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C_* sv = reinterpret_cast<C_*>(smraw);          // v (n), then t*y (n)
+  __shared__ R red[32];
+  __shared__ C_ s_tau;
+  C_* A = Aall + blockIdx.x * a_bs;
+  C_* tau = tau_all + (long long)blockIdx.x * n;
+  C_* sy = sv + n;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   for (int k = 0; k + 2 < n; ++k) {
-    const int m = n - k - 1;           // reflector length
-    cplx* col = A + (long long)k * lda;
-    double part = 0.0;
-    for (int i = k + 2 + tid; i < n; i += blockDim.x) part += cabs2(col[i]);
-    double xn2 = block_sum(part, red);
-    cplx alpha = col[k + 1];
-    Refl r = make_reflector(alpha, sqrt(xn2));
+    const int m = n - k - 1;
+    C_* col = A + (long long)k * lda;
+    R part = R(0.0);
+    for (int i = k + 2 + tid; i < n; i += blockDim.x) part = part + cxabs2(col[i]);
+    R xn2 = block_sum(part, red);
+    C_ alpha = col[k + 1];
+    Refl<R> r = make_reflector(alpha, rsqrt_(xn2));
     if (r.identity) {
-      if (tid == 0) tau[k] = cmk(0.0, 0.0);
+      if (tid == 0) tau[k] = cxzero<R>();
       __syncthreads();
       continue;
     }
     for (int i = k + 2 + tid; i < n; i += blockDim.x) {
-      cplx v = cmul(col[i], r.scale);
+      C_ v = col[i] * r.scale;
       col[i] = v;
       sv[i - k - 1] = v;
     }
     if (tid == 0) {
-      sv[0] = cmk(1.0, 0.0);
-      col[k + 1] = cmk(r.beta, 0.0);
+      sv[0] = cxone<R>();
+      col[k + 1] = cxmk<R>(r.beta, R(0.0));
       tau[k] = r.tau;
       s_tau = r.tau;
     }
     __syncthreads();
-    const cplx t = s_tau;
+    const C_ t = s_tau;
     // right: y = A[:, k+1:n] v ; A[:, k+1:n] -= t y v^H  (all rows)
     for (int i = tid; i < n; i += blockDim.x) {
-      cplx acc = cmk(0.0, 0.0);
-      for (int j = 0; j < m; ++j) acc = cfma(A[i + (long long)(k + 1 + j) * lda], sv[j], acc);
-      sy[i] = cmul(t, acc);
+      C_ acc = cxzero<R>();
+      for (int j = 0; j < m; ++j) acc = cxfma(A[i + (long long)(k + 1 + j) * lda], sv[j], acc);
+      sy[i] = t * acc;
     }
     __syncthreads();
     for (int j = warp; j < m; j += nw) {
-      cplx* cj = A + (long long)(k + 1 + j) * lda;
-      cplx vjc = cconj(sv[j]);
-      for (int i = lane; i < n; i += 32) cj[i] = csub(cj[i], cmul(sy[i], vjc));
+      C_* cj = A + (long long)(k + 1 + j) * lda;
+      const C_ vjc = cxconj(sv[j]);
+      for (int i = lane; i < n; i += 32) cj[i] = cj[i] - sy[i] * vjc;
     }
     __syncthreads();
     // left: z_j = v^H A[k+1:n, j] ; A[k+1:n, j] -= conj(t) v z_j   for j = k+1 .. n-1
-    const cplx tc = cconj(t);
+    const C_ tc = cxconj(t);
     for (int j = warp; j < m; j += nw) {
-      cplx* cj = A + (long long)(k + 1 + j) * lda;
-      cplx acc = cmk(0.0, 0.0);
-      for (int i = lane; i < m; i += 32) acc = cfma_conj(sv[i], cj[k + 1 + i], acc);
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, off);
-        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, off);
-      }
-      cplx f = cmul(tc, acc);
-      for (int i = lane; i < m; i += 32) cj[k + 1 + i] = csub(cj[k + 1 + i], cmul(sv[i], f));
+      C_* cj = A + (long long)(k + 1 + j) * lda;
+      C_ acc = cxzero<R>();
+      for (int i = lane; i < m; i += 32) acc = cxfma_conj(sv[i], cj[k + 1 + i], acc);
+      acc.x = warp_sum(acc.x);
+      acc.y = warp_sum(acc.y);
+      const C_ f = tc * acc;
+      for (int i = lane; i < m; i += 32) cj[k + 1 + i] = cj[k + 1 + i] - sv[i] * f;
     }
     __syncthreads();
   }
-  (void)work_all;
 }
 
 // ------------------------------------------------------------------ 2. form Q = Z
-// Z = H_0 H_1 ... H_{n-3} by backward accumulation; then clears the reflectors from A so that
-// A holds the Hessenberg matrix only.
-__global__ void __launch_bounds__(EIG_THREADS) zunghr_kernel(cplx* __restrict__ Aall, int n, int lda,
-                                                             long long a_bs, const cplx* __restrict__ tau_all,
-                                                             cplx* __restrict__ Zall, int ldz, long long z_bs) {
-  extern __shared__ cplx sv[];
-  cplx* A = Aall + blockIdx.x * a_bs;
-  cplx* Z = Zall + blockIdx.x * z_bs;
-  const cplx* tau = tau_all + (long long)blockIdx.x * n;
+template <class R>
+__global__ void __launch_bounds__(EIG_THREADS) unghr_kernel(Cx<R>* __restrict__ Aall, int n, int lda,
+                                                            long long a_bs, const Cx<R>* __restrict__ tau_all,
+                                                            Cx<R>* __restrict__ Zall, int ldz, long long z_bs) {
+  using C_ = Cx<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C_* sv = reinterpret_cast<C_*>(smraw);
+  C_* A = Aall + blockIdx.x * a_bs;
+  C_* Z = Zall + blockIdx.x * z_bs;
+  const C_* tau = tau_all + (long long)blockIdx.x * n;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   for (long long e = tid; e < (long long)n * n; e += blockDim.x) {
     int i = (int)(e % n), j = (int)(e / n);
-    Z[i + (long long)j * ldz] = cmk(i == j ? 1.0 : 0.0, 0.0);
+    Z[i + (long long)j * ldz] = (i == j) ? cxone<R>() : cxzero<R>();
   }
   __syncthreads();
   for (int k = n - 3; k >= 0; --k) {
     const int m = n - k - 1;
-    const cplx t = tau[k];
-    if (t.x == 0.0 && t.y == 0.0) continue;
-    for (int i = tid; i < m; i += blockDim.x)
-      sv[i] = (i == 0) ? cmk(1.0, 0.0) : A[k + 1 + i + (long long)k * lda];
+    const C_ t = tau[k];
+    if (t.x == R(0.0) && t.y == R(0.0)) continue;
+    for (int i = tid; i < m; i += blockDim.x) sv[i] = (i == 0) ? cxone<R>() : A[k + 1 + i + (long long)k * lda];
     __syncthreads();
-    // Z[k+1:n, k+1:n] -= t v (v^H Z[k+1:n, k+1:n]); columns j <= k untouched (identity there)
     for (int j = warp; j < m; j += nw) {
-      cplx* cj = Z + (long long)(k + 1 + j) * ldz;
-      cplx acc = cmk(0.0, 0.0);
-      for (int i = lane; i < m; i += 32) acc = cfma_conj(sv[i], cj[k + 1 + i], acc);
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, off);
-        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, off);
-      }
-      cplx f = cmul(t, acc);
-      for (int i = lane; i < m; i += 32) cj[k + 1 + i] = csub(cj[k + 1 + i], cmul(sv[i], f));
+      C_* cj = Z + (long long)(k + 1 + j) * ldz;
+      C_ acc = cxzero<R>();
+      for (int i = lane; i < m; i += 32) acc = cxfma_conj(sv[i], cj[k + 1 + i], acc);
+      acc.x = warp_sum(acc.x);
+      acc.y = warp_sum(acc.y);
+      const C_ f = t * acc;
+      for (int i = lane; i < m; i += 32) cj[k + 1 + i] = cj[k + 1 + i] - sv[i] * f;
     }
     __syncthreads();
   }
-  // clear the reflector storage below the subdiagonal
   for (long long e = tid; e < (long long)n * n; e += blockDim.x) {
     int i = (int)(e % n), j = (int)(e / n);
-    if (i > j + 1) A[i + (long long)j * lda] = cmk(0.0, 0.0);
+    if (i > j + 1) A[i + (long long)j * lda] = cxzero<R>();
   }
 }
 
@@ -192,48 +208,53 @@ __global__ void __launch_bounds__(EIG_THREADS) zunghr_kernel(cplx* __restrict__ 
 // Francis single-shift implicit QR on the Hessenberg H (complex), full Schur form: T in H,
 // Schur vectors accumulated into Z. The subdiagonal is kept real so that each 2-element
 // reflector has a real second coefficient. Deflation uses the standard small-subdiagonal test
-// with the Ahues-Tisseur refinement; shifts are Wilkinson shifts with exceptional shifts after
-// 10 and 20 stalled iterations.
-__global__ void __launch_bounds__(EIG_THREADS) zhseqr_kernel(cplx* __restrict__ Hall, int n, int ldh,
-                                                             long long h_bs, cplx* __restrict__ Zall, int ldz,
-                                                             long long z_bs, cplx* __restrict__ w_all,
-                                                             int32_t* __restrict__ status, int st_div,
-                                                             int itmax) {
+// with the Ahues-Tisseur refinement; shifts are Wilkinson shifts with exceptional shifts every
+// 10 stalled iterations. Each sweep is chased in windows of QR_SEG steps: warp 0 runs the
+// bulge through a shared-memory window around the diagonal and records the reflectors, then
+// every thread applies the window's reflectors, in order, to one far-field line (a column
+// right of the window, a row above it, or a row of Z) carrying the running element in a
+// register. Two CTA barriers per window instead of three per step, and no extra flops.
+template <class R>
+__global__ void __launch_bounds__(EIG_THREADS) hseqr_kernel(Cx<R>* __restrict__ Hall, int n, int ldh,
+                                                            long long h_bs, Cx<R>* __restrict__ Zall, int ldz,
+                                                            long long z_bs, Cx<R>* __restrict__ w_all,
+                                                            int32_t* __restrict__ status, int st_div, int itmax) {
+  using C_ = Cx<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C_* sphase = reinterpret_cast<C_*>(smraw);
   __shared__ int ired[32];
-  __shared__ cplx s_t1, s_v2;
-  __shared__ double s_t2;
-  __shared__ int s_l, s_m, s_done;
-  __shared__ cplx s_v0, s_v1;
-  cplx* H = Hall + blockIdx.x * h_bs;
-  cplx* Z = Zall + blockIdx.x * z_bs;
-  cplx* w = w_all + (long long)blockIdx.x * n;
+  __shared__ C_ swin[QR_WIN * QR_WIN];
+  __shared__ C_ srot_t1[QR_SEG], srot_v2[QR_SEG];
+  __shared__ R srot_t2[QR_SEG];
+  __shared__ int s_done;
+  __shared__ C_ s_v0, s_v1;
+  C_* H = Hall + blockIdx.x * h_bs;
+  C_* Z = Zall + blockIdx.x * z_bs;
+  C_* w = w_all + (long long)blockIdx.x * n;
   int32_t* st = status ? status + blockIdx.x / st_div : nullptr;
   const int tid = threadIdx.x;
-  const double ulp = 2.220446049250313e-16;        // DBL_EPSILON
-  const double safmin = 2.2250738585072014e-308;   // DBL_MIN
-  const double smlnum = safmin * ((double)n / ulp);
-  auto h = [&](int i, int j) -> cplx& { return H[i + (long long)j * ldh]; };
-  // make every subdiagonal real with a diagonal similarity D^-1 H D, |d_i| = 1:
-  // d_0 = 1, d_i = d_{i-1} * sd_i / |sd_i| (a prefix product of phases, computed by one thread)
-  extern __shared__ cplx sphase[];
+  const R ulp = RealT<R>::eps();
+  const R smlnum = RealT<R>::tiny() * (R((double)n) / ulp);
+  auto h = [&](int i, int j) -> C_& { return H[i + (long long)j * ldh]; };
+  // subdiagonal made real by a diagonal similarity D^-1 H D, |d_i| = 1, d_i = d_{i-1} sd_i/|sd_i|
   if (tid == 0) {
-    cplx d = cmk(1.0, 0.0);
+    C_ d = cxone<R>();
     sphase[0] = d;
     for (int r = 1; r < n; ++r) {
-      cplx sd = h(r, r - 1);
-      double a = cabsv(sd);
-      if (a > 0.0 && sd.y != 0.0) d = cmul(d, cscale(sd, 1.0 / a));
+      C_ sd = h(r, r - 1);
+      R a = cxabs(sd);
+      if (a > R(0.0) && sd.y != R(0.0)) d = d * (sd * (R(1.0) / a));
       sphase[r] = d;
     }
   }
   __syncthreads();
   for (long long e = tid; e < (long long)n * n; e += blockDim.x) {
     int r = (int)(e % n), c = (int)(e / n);
-    if (r <= c + 1) h(r, c) = cmul(cmul(cconj(sphase[r]), h(r, c)), sphase[c]);
-    Z[r + (long long)c * ldz] = cmul(Z[r + (long long)c * ldz], sphase[c]);
+    if (r <= c + 1) h(r, c) = (cxconj(sphase[r]) * h(r, c)) * sphase[c];
+    Z[r + (long long)c * ldz] = Z[r + (long long)c * ldz] * sphase[c];
   }
   __syncthreads();
-  for (int r = 1 + tid; r < n; r += blockDim.x) h(r, r - 1) = cmk(h(r, r - 1).x, 0.0);
+  for (int r = 1 + tid; r < n; r += blockDim.x) h(r, r - 1) = cxmk<R>(h(r, r - 1).x, R(0.0));
   __syncthreads();
   int i = n - 1;
   int total = 0;
@@ -244,125 +265,173 @@ __global__ void __launch_bounds__(EIG_THREADS) zhseqr_kernel(cplx* __restrict__ 
       // --- deflation: largest k in [1, i] with a negligible subdiagonal H(k, k-1)
       int cand = 0;
       for (int k = 1 + tid; k <= i; k += blockDim.x) {
-        cplx sub = h(k, k - 1);
+        C_ sub = h(k, k - 1);
         bool small = false;
-        if (cabs1(sub) <= smlnum) {
+        if (cxabs1(sub) <= smlnum) {
           small = true;
         } else {
-          double tst = cabs1(h(k - 1, k - 1)) + cabs1(h(k, k));
-          if (tst == 0.0) {
-            if (k - 2 >= 0) tst += fabs(h(k - 1, k - 2).x);
-            if (k + 1 <= i) tst += fabs(h(k + 1, k).x);
+          R tst = cxabs1(h(k - 1, k - 1)) + cxabs1(h(k, k));
+          if (tst == R(0.0)) {
+            if (k - 2 >= 0) tst = tst + rabs(h(k - 1, k - 2).x);
+            if (k + 1 <= i) tst = tst + rabs(h(k + 1, k).x);
           }
-          if (fabs(sub.x) <= ulp * tst) {
-            double ab = fmax(cabs1(sub), cabs1(h(k - 1, k)));
-            double ba = fmin(cabs1(sub), cabs1(h(k - 1, k)));
-            cplx dd = csub(h(k - 1, k - 1), h(k, k));
-            double aa = fmax(cabs1(h(k, k)), cabs1(dd));
-            double bb = fmin(cabs1(h(k, k)), cabs1(dd));
-            double s = aa + ab;
-            if (ba * (ab / s) <= fmax(smlnum, ulp * (bb * (aa / s)))) small = true;
+          if (rabs(sub.x) <= ulp * tst) {
+            R ab = rmax(cxabs1(sub), cxabs1(h(k - 1, k)));
+            R ba = rmin(cxabs1(sub), cxabs1(h(k - 1, k)));
+            C_ dd = h(k - 1, k - 1) - h(k, k);
+            R aa = rmax(cxabs1(h(k, k)), cxabs1(dd));
+            R bb = rmin(cxabs1(h(k, k)), cxabs1(dd));
+            R s = aa + ab;
+            if (ba * (ab / s) <= rmax(smlnum, ulp * (bb * (aa / s)))) small = true;
           }
         }
         if (small) cand = max(cand, k);
       }
       const int l = block_max_int(cand, ired);
-      if (l >= i) break;                          // H(i,i) isolated: converged
-      if (tid == 0 && l > 0) h(l, l - 1) = cmk(0.0, 0.0);
+      if (l >= i) break;
+      if (tid == 0 && l > 0) h(l, l - 1) = cxzero<R>();
       if (its >= 60 || total >= itmax) { failed = true; break; }
       ++its; ++total;
-      // --- shift (thread 0)
+      // --- shift and first reflector vector (thread 0)
       if (tid == 0) {
-        cplx t;
+        C_ t;
         if (its % 20 == 10) {
-          double s = 0.75 * fabs(h(l + 1, l).x);
-          t = cadd(cmk(s, 0.0), h(l, l));
+          R s = R(0.75) * rabs(h(l + 1, l).x);
+          t = cxmk<R>(s, R(0.0)) + h(l, l);
         } else if (its % 20 == 0) {
-          double s = 0.75 * fabs(h(i, i - 1).x);
-          t = cadd(cmk(s, 0.0), h(i, i));
+          R s = R(0.75) * rabs(h(i, i - 1).x);
+          t = cxmk<R>(s, R(0.0)) + h(i, i);
         } else {
           // Wilkinson: eigenvalue of the trailing 2x2 block closer to H(i,i)
           t = h(i, i);
-          cplx u = cmul(csqrt_p(h(i - 1, i)), csqrt_p(h(i, i - 1)));
-          double s = cabs1(u);
-          if (s != 0.0) {
-            cplx x = cscale(csub(h(i - 1, i - 1), t), 0.5);
-            double sx = cabs1(x);
-            s = fmax(s, cabs1(x));
-            cplx xs = cscale(x, 1.0 / s), us = cscale(u, 1.0 / s);
-            cplx y = cscale(csqrt_p(cadd(cmul(xs, xs), cmul(us, us))), s);
-            if (sx > 0.0) {
-              cplx xn = cscale(x, 1.0 / sx);
-              if (xn.x * y.x + xn.y * y.y < 0.0) y = cneg(y);
+          C_ u = cxsqrt(h(i - 1, i)) * cxsqrt(h(i, i - 1));
+          R s = cxabs1(u);
+          if (s != R(0.0)) {
+            C_ x = (h(i - 1, i - 1) - t) * R(0.5);
+            R sx = cxabs1(x);
+            s = rmax(s, cxabs1(x));
+            C_ xs = x * (R(1.0) / s), us = u * (R(1.0) / s);
+            C_ y = cxsqrt(xs * xs + us * us) * s;
+            if (sx > R(0.0)) {
+              C_ xn = x * (R(1.0) / sx);
+              if (xn.x * y.x + xn.y * y.y < R(0.0)) y = -y;
             }
-            t = csub(t, cmul(u, cdiv(u, cadd(x, y))));
+            t = t - u * cxdiv(u, x + y);
           }
         }
-        // --- the bulge starts at the top of the active block
-        const int m = l;
-        cplx h11s = csub(h(l, l), t);
-        double h21 = h(l + 1, l).x;
-        double sc = cabs1(h11s) + fabs(h21);
-        cplx v0 = cscale(h11s, 1.0 / sc);
-        cplx v1 = cmk(h21 / sc, 0.0);
-        s_m = m; s_l = l; s_v0 = v0; s_v1 = v1;
+        C_ h11s = h(l, l) - t;
+        R h21 = h(l + 1, l).x;
+        R sc = cxabs1(h11s) + rabs(h21);
+        s_v0 = h11s * (R(1.0) / sc);
+        s_v1 = cxmk<R>(h21 / sc, R(0.0));
       }
       __syncthreads();
-      const int m = s_m;
-      // --- single-shift sweep from m to i-1
-      for (int k = m; k < i; ++k) {
-        if (tid == 0) {
-          cplx a0, a1;
-          if (k > m) { a0 = h(k, k - 1); a1 = h(k + 1, k - 1); } else { a0 = s_v0; a1 = s_v1; }
-          Refl r = make_reflector(a0, cabsv(a1));
-          cplx v2, t1;
-          if (r.identity) { t1 = cmk(0.0, 0.0); v2 = cmk(0.0, 0.0); }
-          else { t1 = r.tau; v2 = cmul(a1, r.scale); }
-          if (k > m) { h(k, k - 1) = cmk(r.identity ? a0.x : r.beta, r.identity ? a0.y : 0.0); h(k + 1, k - 1) = cmk(0.0, 0.0); }
-          s_t1 = t1; s_v2 = v2; s_t2 = cmul(t1, v2).x;
+      const int m = l;
+      for (int k0 = m; k0 < i; k0 += QR_SEG) {
+        const int k1 = min(k0 + QR_SEG, i);
+        const int w0 = (k0 > m) ? k0 - 1 : k0;
+        const int w1 = min(k1 + 1, i);
+        const int nwin = w1 - w0 + 1;
+        for (int e = tid; e < nwin * nwin; e += blockDim.x) {
+          int r = e % nwin, c = e / nwin;
+          swin[r + c * QR_WIN] = h(w0 + r, w0 + c);
         }
         __syncthreads();
-        const cplx t1 = s_t1, v2 = s_v2;
-        const double t2 = s_t2;
-        const cplx t1c = cconj(t1), v2c = cconj(v2);
-        // left: rows k, k+1, columns k..n-1
-        for (int j = k + tid; j < n; j += blockDim.x) {
-          cplx a = h(k, j), b = h(k + 1, j);
-          cplx sum = cadd(cmul(t1c, a), cscale(b, t2));
-          h(k, j) = csub(a, sum);
-          h(k + 1, j) = csub(b, cmul(sum, v2));
+        if (tid < 32) {
+          const int lane = tid;
+          auto W = [&](int r, int c) -> C_& { return swin[(r - w0) + (c - w0) * QR_WIN]; };
+          for (int k = k0; k < k1; ++k) {
+            if (lane == 0) {
+              C_ a0, a1;
+              if (k > m) { a0 = W(k, k - 1); a1 = W(k + 1, k - 1); } else { a0 = s_v0; a1 = s_v1; }
+              Refl<R> rf = make_reflector(a0, cxabs(a1));
+              C_ v2, t1;
+              if (rf.identity) { t1 = cxzero<R>(); v2 = cxzero<R>(); }
+              else { t1 = rf.tau; v2 = a1 * rf.scale; }
+              if (k > m) { W(k, k - 1) = rf.identity ? a0 : cxmk<R>(rf.beta, R(0.0)); W(k + 1, k - 1) = cxzero<R>(); }
+              srot_t1[k - k0] = t1; srot_v2[k - k0] = v2; srot_t2[k - k0] = (t1 * v2).x;
+            }
+            __syncwarp();
+            const C_ t1 = srot_t1[k - k0], v2 = srot_v2[k - k0];
+            const R t2 = srot_t2[k - k0];
+            const C_ t1c = cxconj(t1), v2c = cxconj(v2);
+            for (int j = k + lane; j <= w1; j += 32) {
+              C_ a = W(k, j), b = W(k + 1, j);
+              C_ sum = t1c * a + b * t2;
+              W(k, j) = a - sum;
+              W(k + 1, j) = b - sum * v2;
+            }
+            __syncwarp();
+            const int rlast = min(k + 2, i);
+            for (int r = w0 + lane; r <= rlast; r += 32) {
+              C_ a = W(r, k), b = W(r, k + 1);
+              C_ sum = t1 * a + b * t2;
+              W(r, k) = a - sum;
+              W(r, k + 1) = b - sum * v2c;
+            }
+            __syncwarp();
+          }
         }
         __syncthreads();
-        // right: columns k, k+1, rows 0..min(k+2, i); and Z rows 0..n-1
-        const int rlast = min(k + 2, i);
-        for (int e = tid; e <= rlast + n; e += blockDim.x) {
-          cplx* pa; cplx* pb;
-          if (e <= rlast) { pa = &h(e, k); pb = &h(e, k + 1); }
-          else { int j = e - rlast - 1; pa = Z + j + (long long)k * ldz; pb = Z + j + (long long)(k + 1) * ldz; }
-          cplx a = *pa, b = *pb;
-          cplx sum = cadd(cmul(t1, a), cscale(b, t2));
-          *pa = csub(a, sum);
-          *pb = csub(b, cmul(sum, v2c));
+        for (int e = tid; e < nwin * nwin; e += blockDim.x) {
+          int r = e % nwin, c = e / nwin;
+          h(w0 + r, w0 + c) = swin[r + c * QR_WIN];
+        }
+        const int nleft = n - 1 - w1, nright = w0;
+        const int items = nleft + nright + n;
+        const int ns = k1 - k0;
+        for (int it = tid; it < items; it += blockDim.x) {
+          // the line's elements k0..k1 (stride `ld`), rotated in register chunks of QR_CH so
+          // that each chunk's loads are independent of the previous chunk's stores
+          C_* p; long long ld; bool left;
+          if (it < nleft) { p = H + (long long)(w1 + 1 + it) * ldh; ld = 1; left = true; }
+          else if (it < nleft + nright) { p = H + (it - nleft); ld = ldh; left = false; }
+          else { p = Z + (it - nleft - nright); ld = ldz; left = false; }
+          C_ a = p[(long long)k0 * ld];
+          for (int q0 = 0; q0 < ns; q0 += QR_CH) {
+            C_ buf[QR_CH];
+#pragma unroll
+            for (int u = 0; u < QR_CH; ++u)
+              if (q0 + u < ns) buf[u] = p[(long long)(k0 + q0 + u + 1) * ld];
+#pragma unroll
+            for (int u = 0; u < QR_CH; ++u) {
+              if (q0 + u < ns) {
+                const int q = q0 + u;
+                const C_ t1 = srot_t1[q], v2 = srot_v2[q];
+                const R t2 = srot_t2[q];
+                const C_ b = buf[u];
+                C_ sum, nb;
+                if (left) { sum = cxconj(t1) * a + b * t2; nb = b - sum * v2; }
+                else { sum = t1 * a + b * t2; nb = b - sum * cxconj(v2); }
+                buf[u] = a - sum;
+                a = nb;
+              }
+            }
+#pragma unroll
+            for (int u = 0; u < QR_CH; ++u)
+              if (q0 + u < ns) p[(long long)(k0 + q0 + u) * ld] = buf[u];
+          }
+          p[(long long)k1 * ld] = a;
         }
         __syncthreads();
       }
       // make H(i, i-1) real again
       if (tid == 0) {
-        cplx sd = h(i, i - 1);
+        C_ sd = h(i, i - 1);
         s_done = 0;
-        if (sd.y != 0.0) {
-          double a = cabsv(sd);
-          h(i, i - 1) = cmk(a, 0.0);
-          s_v0 = cdiv(sd, cmk(a, 0.0));
+        if (sd.y != R(0.0)) {
+          R a = cxabs(sd);
+          h(i, i - 1) = cxmk<R>(a, R(0.0));
+          s_v0 = sd * (R(1.0) / a);
           s_done = 1;
         }
       }
       __syncthreads();
       if (s_done) {
-        const cplx sc = s_v0;
-        for (int j = i + 1 + tid; j < n; j += blockDim.x) h(i, j) = cmul(cconj(sc), h(i, j));
-        for (int j = tid; j < i; j += blockDim.x) h(j, i) = cmul(sc, h(j, i));
-        for (int j = tid; j < n; j += blockDim.x) Z[j + (long long)i * ldz] = cmul(sc, Z[j + (long long)i * ldz]);
+        const C_ sc = s_v0;
+        for (int j = i + 1 + tid; j < n; j += blockDim.x) h(i, j) = cxconj(sc) * h(i, j);
+        for (int j = tid; j < i; j += blockDim.x) h(j, i) = sc * h(j, i);
+        for (int j = tid; j < n; j += blockDim.x) Z[j + (long long)i * ldz] = sc * Z[j + (long long)i * ldz];
       }
       __syncthreads();
     }
@@ -372,7 +441,7 @@ __global__ void __launch_bounds__(EIG_THREADS) zhseqr_kernel(cplx* __restrict__ 
     i -= 1;
   }
   if (failed) {
-    for (int j = tid; j <= i; j += blockDim.x) w[j] = cmk(NAN, NAN);
+    for (int j = tid; j <= i; j += blockDim.x) w[j] = cxmk<R>(R(NAN), R(NAN));
     if (tid == 0) wb_flag(st, WB_ST_NOCONV);
   }
 }
@@ -380,84 +449,114 @@ __global__ void __launch_bounds__(EIG_THREADS) zhseqr_kernel(cplx* __restrict__ 
 // -------------------------------------------------- 4. eigenvectors of the triangular T
 // X[:, k] solves (T[0:k,0:k] - T(k,k) I) x = -T[0:k, k] with x_k = 1, x_j = 0 for j > k.
 // One warp per column; tiny pivots are replaced by max(ulp |T(k,k)|, smlnum).
-__global__ void __launch_bounds__(256) ztrevc_kernel(const cplx* __restrict__ Tall, int n, int ldt,
-                                                     long long t_bs, cplx* __restrict__ Xall, int ldx,
-                                                     long long x_bs, int batch) {
+template <class R>
+__global__ void __launch_bounds__(256) trevc_kernel(const Cx<R>* __restrict__ Tall, int n, int ldt,
+                                                    long long t_bs, Cx<R>* __restrict__ Xall, int ldx,
+                                                    long long x_bs, int batch) {
+  using C_ = Cx<R>;
   const int warps_per_block = blockDim.x >> 5;
   long long gw = (long long)blockIdx.x * warps_per_block + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (gw >= (long long)batch * n) return;
   const int b = (int)(gw / n), k = (int)(gw % n);
-  const cplx* T = Tall + b * t_bs;
-  cplx* x = Xall + b * x_bs + (long long)k * ldx;
-  const double ulp = 2.220446049250313e-16;
-  const double smlnum = 2.2250738585072014e-308 * ((double)n / ulp);
-  const cplx lam = T[k + (long long)k * ldt];
-  const double smin = fmax(ulp * cabs1(lam), smlnum);
+  const C_* T = Tall + b * t_bs;
+  C_* x = Xall + b * x_bs + (long long)k * ldx;
+  const R ulp = RealT<R>::eps();
+  const R smlnum = RealT<R>::tiny() * (R((double)n) / ulp);
+  const C_ lam = T[k + (long long)k * ldt];
+  const R smin = rmax(ulp * cxabs1(lam), smlnum);
   for (int r = lane; r < n; r += 32) {
-    cplx v;
-    if (r < k) v = cneg(T[r + (long long)k * ldt]);
-    else v = cmk(r == k ? 1.0 : 0.0, 0.0);
+    C_ v;
+    if (r < k) v = -T[r + (long long)k * ldt];
+    else v = (r == k) ? cxone<R>() : cxzero<R>();
     x[r] = v;
   }
   __syncwarp();
   for (int j = k - 1; j >= 0; --j) {
-    cplx xj = cmk(0.0, 0.0);
+    C_ xj = cxzero<R>();
     if (lane == (j & 31)) {
-      cplx d = csub(T[j + (long long)j * ldt], lam);
-      if (cabs1(d) < smin) d = cmk(smin, 0.0);
-      xj = cdiv(x[j], d);
+      C_ d = T[j + (long long)j * ldt] - lam;
+      if (cxabs1(d) < smin) d = cxmk<R>(smin, R(0.0));
+      xj = cxdiv(x[j], d);
       x[j] = xj;
     }
-    xj.x = __shfl_sync(0xffffffffu, xj.x, j & 31);
-    xj.y = __shfl_sync(0xffffffffu, xj.y, j & 31);
-    const cplx* tc = T + (long long)j * ldt;
-    for (int r = lane; r < j; r += 32) x[r] = csub(x[r], cmul(xj, tc[r]));
+    xj.x = shfl_idx(xj.x, j & 31);
+    xj.y = shfl_idx(xj.y, j & 31);
+    const C_* tc = T + (long long)j * ldt;
+    for (int r = lane; r < j; r += 32) x[r] = x[r] - xj * tc[r];
     __syncwarp();
   }
 }
 
 // ------------------------------------------------------------- 5. column normalisation
-__global__ void znormalize_columns_kernel(cplx* __restrict__ Wall, int n, int ldw, long long w_bs, int batch) {
+template <class R>
+__global__ void normalize_columns_kernel(Cx<R>* __restrict__ Wall, int n, int ldw, long long w_bs, int batch) {
+  using C_ = Cx<R>;
   const int warps_per_block = blockDim.x >> 5;
   long long gw = (long long)blockIdx.x * warps_per_block + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (gw >= (long long)batch * n) return;
   const int b = (int)(gw / n), k = (int)(gw % n);
-  cplx* c = Wall + b * w_bs + (long long)k * ldw;
-  double s = 0.0;
-  for (int r = lane; r < n; r += 32) s += cabs2(c[r]);
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-  double inv = (s > 0.0) ? 1.0 / sqrt(s) : 1.0;
-  for (int r = lane; r < n; r += 32) c[r] = cscale(c[r], inv);
+  C_* c = Wall + b * w_bs + (long long)k * ldw;
+  R s = R(0.0);
+  for (int r = lane; r < n; r += 32) s = s + cxabs2(c[r]);
+  s = warp_sum(s);
+  R inv = (s > R(0.0)) ? R(1.0) / rsqrt_(s) : R(1.0);
+  for (int r = lane; r < n; r += 32) c[r] = c[r] * inv;
 }
 
+template <class R>
+void geev_schur(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a_bs, Cx<R>* Z, int ldz,
+                long long z_bs, Cx<R>* w, Cx<R>* tau, int32_t* status, int st_div) {
+  if (batch <= 0 || n <= 0) return;
+  size_t sm = 2 * (size_t)n * sizeof(Cx<R>);
+  cudaFuncSetAttribute(gehrd_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaFuncSetAttribute(unghr_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  gehrd_kernel<R><<<batch, EIG_THREADS, sm, s>>>(A, n, lda, a_bs, tau); note_launch();
+  unghr_kernel<R><<<batch, EIG_THREADS, sm, s>>>(A, n, lda, a_bs, tau, Z, ldz, z_bs); note_launch();
+  int itmax = 30 * (n > 10 ? n : 10);
+  size_t sm2 = (size_t)n * sizeof(Cx<R>);
+  cudaFuncSetAttribute(hseqr_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+  hseqr_kernel<R><<<batch, EIG_THREADS, sm2, s>>>(A, n, lda, a_bs, Z, ldz, z_bs, w, status, st_div < 1 ? 1 : st_div,
+                                                  itmax); note_launch();
+}
+
+template <class R>
+void trevc(cudaStream_t s, int batch, int n, const Cx<R>* T, int ldt, long long t_bs, Cx<R>* X, int ldx,
+           long long x_bs) {
+  long long warps = (long long)batch * n;
+  if (warps <= 0) return;
+  trevc_kernel<R><<<(unsigned)((warps + 7) / 8), 256, 0, s>>>(T, n, ldt, t_bs, X, ldx, x_bs, batch); note_launch();
+}
+
+template <class R>
+void normalize_columns(cudaStream_t s, int batch, int n, Cx<R>* W, int ldw, long long w_bs) {
+  long long warps = (long long)batch * n;
+  if (warps <= 0) return;
+  normalize_columns_kernel<R><<<(unsigned)((warps + 7) / 8), 256, 0, s>>>(W, n, ldw, w_bs, batch); note_launch();
+}
+
+// double2 wrappers of the plain FP64 path
 void zgeev_schur(cudaStream_t s, int batch, int n, cplx* A, int lda, long long a_bs, cplx* Z, int ldz,
                  long long z_bs, cplx* w, cplx* tau, int32_t* status, int st_div) {
-  if (batch <= 0 || n <= 0) return;
-  size_t sm = 2 * (size_t)n * sizeof(cplx);
-  if (sm > 48 * 1024) {
-    cudaFuncSetAttribute(zgehrd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    cudaFuncSetAttribute(zunghr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  }
-  zgehrd_kernel<<<batch, EIG_THREADS, sm, s>>>(A, n, lda, a_bs, tau, nullptr); note_launch();
-  zunghr_kernel<<<batch, EIG_THREADS, sm, s>>>(A, n, lda, a_bs, tau, Z, ldz, z_bs); note_launch();
-  int itmax = 30 * (n > 10 ? n : 10);
-  zhseqr_kernel<<<batch, EIG_THREADS, (size_t)n * sizeof(cplx), s>>>(A, n, lda, a_bs, Z, ldz, z_bs, w, status, st_div < 1 ? 1 : st_div, itmax); note_launch();
+  geev_schur<double>(s, batch, n, (Cx<double>*)A, lda, a_bs, (Cx<double>*)Z, ldz, z_bs, (Cx<double>*)w,
+                     (Cx<double>*)tau, status, st_div);
 }
-
 void ztrevc(cudaStream_t s, int batch, int n, const cplx* T, int ldt, long long t_bs, cplx* X, int ldx,
             long long x_bs) {
-  long long warps = (long long)batch * n;
-  if (warps <= 0) return;
-  ztrevc_kernel<<<(unsigned)((warps + 7) / 8), 256, 0, s>>>(T, n, ldt, t_bs, X, ldx, x_bs, batch); note_launch();
+  trevc<double>(s, batch, n, (const Cx<double>*)T, ldt, t_bs, (Cx<double>*)X, ldx, x_bs);
+}
+void znormalize_columns(cudaStream_t s, int batch, int n, cplx* W, int ldw, long long w_bs) {
+  normalize_columns<double>(s, batch, n, (Cx<double>*)W, ldw, w_bs);
 }
 
-void znormalize_columns(cudaStream_t s, int batch, int n, cplx* W, int ldw, long long w_bs) {
-  long long warps = (long long)batch * n;
-  if (warps <= 0) return;
-  znormalize_columns_kernel<<<(unsigned)((warps + 7) / 8), 256, 0, s>>>(W, n, ldw, w_bs, batch); note_launch();
-}
+#define WB_EIG_INST(R)                                                                                   \
+  template void geev_schur<R>(cudaStream_t, int, int, Cx<R>*, int, long long, Cx<R>*, int, long long,     \
+                              Cx<R>*, Cx<R>*, int32_t*, int);                                             \
+  template void trevc<R>(cudaStream_t, int, int, const Cx<R>*, int, long long, Cx<R>*, int, long long);  \
+  template void normalize_columns<R>(cudaStream_t, int, int, Cx<R>*, int, long long);
+WB_EIG_INST(double)
+WB_EIG_INST(float)
+WB_EIG_INST(df64)
 
 }  // namespace wb

@@ -1,6 +1,7 @@
 // Internal launch wrappers shared by the translation units of libwbgpu.so (not the public ABI).
 #pragma once
 #include "wb_common.cuh"
+#include "wb_num.cuh"
 
 namespace wb {
 
@@ -18,9 +19,24 @@ void zgetrf(cudaStream_t s, int batch, int n, cplx* A, int lda, long long a_bs, 
             int32_t* status, int st_div);
 void zgetrs(cudaStream_t s, int batch, int n, const cplx* LU, int lda, long long a_bs,
             const int* ipiv, long long piv_bs, cplx* B, int nrhs, int ldb, long long b_bs, int trans);
-void ztranspose(cudaStream_t s, int batch, int m, int n, const cplx* A, int lda, long long a_bs,
-                cplx* B, int ldb, long long b_bs);
 void zset_identity(cudaStream_t s, int batch, int n, cplx* A, int lda, long long a_bs);
+
+// templated over R in {double, float, df64}; alpha/beta are passed as doubles
+template <class R>
+void gemm(cudaStream_t s, int batch, int m, int n, int k, double2 alpha,
+          const Cx<R>* A, long long a_rs, long long a_cs, long long a_bs,
+          const Cx<R>* B, long long b_rs, long long b_cs, long long b_bs,
+          double2 beta, Cx<R>* C, long long c_rs, long long c_cs, long long c_bs);
+template <class R>
+void getrf(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a_bs, int* ipiv, long long piv_bs,
+           int32_t* status, int st_div);
+template <class R>
+void getrs(cudaStream_t s, int batch, int n, const Cx<R>* LU, int lda, long long a_bs, const int* ipiv,
+           long long piv_bs, Cx<R>* B, int nrhs, int ldb, long long b_bs, int trans);
+template <class R>
+void set_identity(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a_bs);
+template <class R1, class R2>
+void convert(cudaStream_t s, const Cx<R1>* src, Cx<R2>* dst, long long count);
 
 // ---- eigen-decomposition (wb_eig.cu)
 void zgeev_schur(cudaStream_t s, int batch, int n, cplx* A, int lda, long long a_bs, cplx* Z, int ldz,
@@ -28,6 +44,15 @@ void zgeev_schur(cudaStream_t s, int batch, int n, cplx* A, int lda, long long a
 void ztrevc(cudaStream_t s, int batch, int n, const cplx* T, int ldt, long long t_bs, cplx* X, int ldx,
             long long x_bs);
 void znormalize_columns(cudaStream_t s, int batch, int n, cplx* W, int ldw, long long w_bs);
+
+template <class R>
+void geev_schur(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a_bs, Cx<R>* Z, int ldz,
+                long long z_bs, Cx<R>* w, Cx<R>* tau, int32_t* status, int st_div);
+template <class R>
+void trevc(cudaStream_t s, int batch, int n, const Cx<R>* T, int ldt, long long t_bs, Cx<R>* X, int ldx,
+           long long x_bs);
+template <class R>
+void normalize_columns(cudaStream_t s, int batch, int n, Cx<R>* W, int ldw, long long w_bs);
 
 // ---- stage A: convolution matrices (wb_assemble.cu)
 // eps: (L, ny, nx) row-major raster; outputs (L, N, N) column-major; scratch from `ws`.

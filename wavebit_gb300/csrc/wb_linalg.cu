@@ -1,12 +1,14 @@
-// Batched dense complex FP64 linear algebra for the RCWA path: GEMM, LU with partial pivoting,
-// triangular solves with many right-hand sides, transposes and diagonal scalings.
+// Batched dense complex linear algebra for the RCWA path: GEMM, LU with partial pivoting,
+// triangular solves with many right-hand sides, transposes, conversions. Every kernel is a
+// template over the real type R in {double, float, df64} (wb_num.cuh).
 //
 // On GB300 the FP64 pipe delivers about 1 TFLOP/s (measured: DFMA 1.0, DMMA m8n8k4 1.05,
-// DGEMM 1.05), so every kernel here is written to keep the FP64 units busy rather than to
-// save bandwidth: a 64x64 CTA tile with 4x4 register blocking reaches the FP64 rate at an
-// arithmetic intensity far above what HBM needs. FP64 mma.sync runs at the same rate as DFMA
-// on this part, so plain fused multiply-adds are used.
+// DGEMM 1.05), so the FP64 instantiations are written to keep the FP64 units busy rather than
+// to save bandwidth: a 64x64 CTA tile with 4x4 register blocking is far above the arithmetic
+// intensity HBM needs. FP64 mma.sync runs at the same rate as DFMA on this part, so plain
+// fused multiply-adds are used. The float and df64 instantiations run on the FP32 pipes.
 #include "wb_common.cuh"
+#include "wb_num.cuh"
 #include "wb_kernels.h"
 
 namespace wb {
@@ -17,42 +19,43 @@ namespace wb {
 constexpr int GT = 64;   // CTA tile
 constexpr int GK = 8;    // K step
 
-__global__ void __launch_bounds__(256) zgemm_kernel(
-    int m, int n, int k, cplx alpha,
-    const cplx* __restrict__ A, long long a_rs, long long a_cs, long long a_bs,
-    const cplx* __restrict__ B, long long b_rs, long long b_cs, long long b_bs,
-    cplx beta, cplx* __restrict__ C, long long c_rs, long long c_cs, long long c_bs) {
-  __shared__ cplx sA[GK][GT + 1];
-  __shared__ cplx sB[GK][GT + 1];
+template <class R>
+__global__ void __launch_bounds__(256) gemm_kernel(
+    int m, int n, int k, double2 alpha_d,
+    const Cx<R>* __restrict__ A, long long a_rs, long long a_cs, long long a_bs,
+    const Cx<R>* __restrict__ B, long long b_rs, long long b_cs, long long b_bs,
+    double2 beta_d, Cx<R>* __restrict__ C, long long c_rs, long long c_cs, long long c_bs) {
+  using C_ = Cx<R>;
+  __shared__ C_ sA[GK][GT + 1];
+  __shared__ C_ sB[GK][GT + 1];
   const int bz = blockIdx.z;
   A += bz * a_bs; B += bz * b_bs; C += bz * c_bs;
   const int row0 = blockIdx.x * GT, col0 = blockIdx.y * GT;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  cplx acc[4][4];
+  C_ acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = cmk(0.0, 0.0);
+    for (int j = 0; j < 4; ++j) acc[i][j] = cxzero<R>();
   for (int k0 = 0; k0 < k; k0 += GK) {
-    // A tile: GT rows x GK cols; 512 elements, 2 per thread; rows fastest for column-major A
 #pragma unroll
     for (int e = 0; e < 2; ++e) {
       int idx = tid + e * 256;
       int r = idx % GT, c = idx / GT;
       int gr = row0 + r, gc = k0 + c;
-      sA[c][r] = (gr < m && gc < k) ? A[gr * a_rs + gc * a_cs] : cmk(0.0, 0.0);
+      sA[c][r] = (gr < m && gc < k) ? A[gr * a_rs + gc * a_cs] : cxzero<R>();
     }
 #pragma unroll
     for (int e = 0; e < 2; ++e) {
       int idx = tid + e * 256;
       int r = idx % GK, c = idx / GK;
       int gr = k0 + r, gc = col0 + c;
-      sB[r][c] = (gr < k && gc < n) ? B[gr * b_rs + gc * b_cs] : cmk(0.0, 0.0);
+      sB[r][c] = (gr < k && gc < n) ? B[gr * b_rs + gc * b_cs] : cxzero<R>();
     }
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < GK; ++kk) {
-      cplx a[4], b[4];
+      C_ a[4], b[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) a[i] = sA[kk][tx + 16 * i];
 #pragma unroll
@@ -60,11 +63,12 @@ __global__ void __launch_bounds__(256) zgemm_kernel(
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = cfma(a[i], b[j], acc[i][j]);
+        for (int j = 0; j < 4; ++j) acc[i][j] = cxfma(a[i], b[j], acc[i][j]);
     }
     __syncthreads();
   }
-  const bool zero_beta = (beta.x == 0.0 && beta.y == 0.0);
+  const C_ alpha = cxfrom<R>(alpha_d), beta = cxfrom<R>(beta_d);
+  const bool zero_beta = (beta_d.x == 0.0 && beta_d.y == 0.0);
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     int gr = row0 + tx + 16 * i;
@@ -73,22 +77,23 @@ __global__ void __launch_bounds__(256) zgemm_kernel(
     for (int j = 0; j < 4; ++j) {
       int gc = col0 + ty + 16 * j;
       if (gc >= n) continue;
-      cplx* p = C + gr * c_rs + gc * c_cs;
-      cplx v = cmul(alpha, acc[i][j]);
-      if (!zero_beta) v = cfma(beta, *p, v);
+      C_* p = C + gr * c_rs + gc * c_cs;
+      C_ v = alpha * acc[i][j];
+      if (!zero_beta) v = cxfma(beta, *p, v);
       *p = v;
     }
   }
 }
 
-void zgemm(cudaStream_t s, int batch, int m, int n, int k, cplx alpha,
-           const cplx* A, long long a_rs, long long a_cs, long long a_bs,
-           const cplx* B, long long b_rs, long long b_cs, long long b_bs,
-           cplx beta, cplx* C, long long c_rs, long long c_cs, long long c_bs) {
+template <class R>
+void gemm(cudaStream_t s, int batch, int m, int n, int k, double2 alpha,
+          const Cx<R>* A, long long a_rs, long long a_cs, long long a_bs,
+          const Cx<R>* B, long long b_rs, long long b_cs, long long b_bs,
+          double2 beta, Cx<R>* C, long long c_rs, long long c_cs, long long c_bs) {
   if (batch <= 0 || m <= 0 || n <= 0) return;
   dim3 grid((m + GT - 1) / GT, (n + GT - 1) / GT, batch);
-  zgemm_kernel<<<grid, 256, 0, s>>>(m, n, k, alpha, A, a_rs, a_cs, a_bs, B, b_rs, b_cs, b_bs,
-                                    beta, C, c_rs, c_cs, c_bs); note_launch();
+  gemm_kernel<R><<<grid, 256, 0, s>>>(m, n, k, alpha, A, a_rs, a_cs, a_bs, B, b_rs, b_cs, b_bs, beta, C, c_rs,
+                                      c_cs, c_bs); note_launch();
 }
 
 // ----------------------------------------------------------------------- LU factorisation
@@ -97,106 +102,114 @@ void zgemm(cudaStream_t s, int batch, int m, int n, int k, cplx alpha,
 constexpr int LU_NB = 16;
 constexpr int LU_THREADS = 256;
 
-__device__ void block_argmax(double v, int idx, double* sval, int* sidx, double& out_v, int& out_i) {
-  // reduce (value, index) to the largest value, ties to the smallest index
+template <class R>
+__device__ void block_argmax(R v, int idx, R* sval, int* sidx, R& out_v, int& out_i) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    double ov = __shfl_down_sync(0xffffffffu, v, off);
-    int oi = __shfl_down_sync(0xffffffffu, idx, off);
-    if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+  __syncthreads();
+  // warp stage through shared memory (R may be a two-word type)
+  __shared__ int s_lane_idx[LU_THREADS];
+  sval[threadIdx.x] = v;
+  s_lane_idx[threadIdx.x] = idx;
+  __syncthreads();
+  if (lane == 0) {
+    R bv = sval[threadIdx.x]; int bi = s_lane_idx[threadIdx.x];
+    for (int l = 1; l < 32; ++l) {
+      R ov = sval[threadIdx.x + l]; int oi = s_lane_idx[threadIdx.x + l];
+      if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+    }
+    sval[threadIdx.x] = bv; s_lane_idx[threadIdx.x] = bi;
   }
-  if (lane == 0) { sval[warp] = v; sidx[warp] = idx; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double bv = sval[0]; int bi = sidx[0];
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
-      if (sval[w] > bv || (sval[w] == bv && sidx[w] < bi)) { bv = sval[w]; bi = sidx[w]; }
+    R bv = sval[0]; int bi = s_lane_idx[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      R ov = sval[w * 32]; int oi = s_lane_idx[w * 32];
+      if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+    }
     sval[0] = bv; sidx[0] = bi;
   }
   __syncthreads();
   out_v = sval[0]; out_i = sidx[0];
   __syncthreads();
+  (void)warp;
 }
 
-__global__ void __launch_bounds__(LU_THREADS) zgetrf_kernel(
-    cplx* __restrict__ Aall, int n, int lda, long long a_bs, int* __restrict__ ipiv_all, long long piv_bs,
+template <class R>
+__global__ void __launch_bounds__(LU_THREADS) getrf_kernel(
+    Cx<R>* __restrict__ Aall, int n, int lda, long long a_bs, int* __restrict__ ipiv_all, long long piv_bs,
     int32_t* __restrict__ status, int st_div) {
-  __shared__ double sval[32];
-  __shared__ int sidx[32];
-  __shared__ cplx sL[GT][LU_NB + 1];
-  __shared__ cplx sU[LU_NB][GT + 1];
-  cplx* A = Aall + blockIdx.x * a_bs;
+  using C_ = Cx<R>;
+  __shared__ R sval[LU_THREADS];
+  __shared__ int sidx[1];
+  __shared__ C_ sL[GT][LU_NB + 1];
+  __shared__ C_ sU[LU_NB][GT + 1];
+  C_* A = Aall + blockIdx.x * a_bs;
   int* ipiv = ipiv_all + (long long)blockIdx.x * piv_bs;
   int32_t* st = status ? status + blockIdx.x / st_div : nullptr;
   const int tid = threadIdx.x;
   for (int k0 = 0; k0 < n; k0 += LU_NB) {
     const int kb = min(LU_NB, n - k0);
-    // ---- panel factorisation, unblocked
     for (int j = k0; j < k0 + kb; ++j) {
-      double best = -1.0; int bi = j;
+      R best = R(-1.0); int bi = j;
       for (int i = j + tid; i < n; i += blockDim.x) {
-        double v = cabs1(A[i + (long long)j * lda]);
+        R v = cxabs1(A[i + (long long)j * lda]);
         if (v > best) { best = v; bi = i; }
       }
-      double pv; int p;
-      block_argmax(best, bi, sval, sidx, pv, p);
+      R pv; int p;
+      block_argmax<R>(best, bi, sval, sidx, pv, p);
       if (tid == 0) ipiv[j] = p;
       if (p != j) {
         for (int c = tid; c < n; c += blockDim.x) {
-          cplx t = A[j + (long long)c * lda];
+          C_ t = A[j + (long long)c * lda];
           A[j + (long long)c * lda] = A[p + (long long)c * lda];
           A[p + (long long)c * lda] = t;
         }
       }
       __syncthreads();
-      cplx piv = A[j + (long long)j * lda];
-      if (piv.x == 0.0 && piv.y == 0.0) {
+      C_ piv = A[j + (long long)j * lda];
+      if (piv.x == R(0.0) && piv.y == R(0.0)) {
         if (tid == 0) wb_flag(st, WB_ST_SINGULAR);
         __syncthreads();
         continue;
       }
-      cplx rp = cinv(piv);
+      C_ rp = cxinv(piv);
       for (int i = j + 1 + tid; i < n; i += blockDim.x) {
-        cplx l = cmul(A[i + (long long)j * lda], rp);
+        C_ l = A[i + (long long)j * lda] * rp;
         A[i + (long long)j * lda] = l;
         for (int c = j + 1; c < k0 + kb; ++c)
-          A[i + (long long)c * lda] = csub(A[i + (long long)c * lda], cmul(l, A[j + (long long)c * lda]));
+          A[i + (long long)c * lda] = A[i + (long long)c * lda] - l * A[j + (long long)c * lda];
       }
       __syncthreads();
     }
     const int c0 = k0 + kb;
     if (c0 >= n) break;
-    // ---- U12 = L11^{-1} A12 (unit lower triangular), columns independent
     for (int c = c0 + tid; c < n; c += blockDim.x) {
       for (int r = k0 + 1; r < k0 + kb; ++r) {
-        cplx acc = A[r + (long long)c * lda];
-        for (int t = k0; t < r; ++t)
-          acc = csub(acc, cmul(A[r + (long long)t * lda], A[t + (long long)c * lda]));
+        C_ acc = A[r + (long long)c * lda];
+        for (int t = k0; t < r; ++t) acc = acc - A[r + (long long)t * lda] * A[t + (long long)c * lda];
         A[r + (long long)c * lda] = acc;
       }
     }
     __syncthreads();
-    // ---- A22 -= L21 * U12, 64x64 tiles, K = kb
     const int tx = tid & 15, ty = tid >> 4;
     for (int cc = c0; cc < n; cc += GT) {
       for (int e = tid; e < LU_NB * GT; e += blockDim.x) {
         int r = e % LU_NB, c = e / LU_NB;
-        sU[r][c] = (r < kb && cc + c < n) ? A[k0 + r + (long long)(cc + c) * lda] : cmk(0.0, 0.0);
+        sU[r][c] = (r < kb && cc + c < n) ? A[k0 + r + (long long)(cc + c) * lda] : cxzero<R>();
       }
       for (int rr = c0; rr < n; rr += GT) {
         for (int e = tid; e < LU_NB * GT; e += blockDim.x) {
           int r = e % GT, c = e / GT;
-          sL[r][c] = (c < kb && rr + r < n) ? A[rr + r + (long long)(k0 + c) * lda] : cmk(0.0, 0.0);
+          sL[r][c] = (c < kb && rr + r < n) ? A[rr + r + (long long)(k0 + c) * lda] : cxzero<R>();
         }
         __syncthreads();
-        cplx acc[4][4];
+        C_ acc[4][4];
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-          for (int q = 0; q < 4; ++q) acc[i][q] = cmk(0.0, 0.0);
+          for (int q = 0; q < 4; ++q) acc[i][q] = cxzero<R>();
         for (int kk = 0; kk < kb; ++kk) {
-          cplx a[4], b[4];
+          C_ a[4], b[4];
 #pragma unroll
           for (int i = 0; i < 4; ++i) a[i] = sL[tx + 16 * i][kk];
 #pragma unroll
@@ -204,7 +217,7 @@ __global__ void __launch_bounds__(LU_THREADS) zgetrf_kernel(
 #pragma unroll
           for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int q = 0; q < 4; ++q) acc[i][q] = cfma(a[i], b[q], acc[i][q]);
+            for (int q = 0; q < 4; ++q) acc[i][q] = cxfma(a[i], b[q], acc[i][q]);
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -214,8 +227,8 @@ __global__ void __launch_bounds__(LU_THREADS) zgetrf_kernel(
           for (int q = 0; q < 4; ++q) {
             int gc = cc + ty + 16 * q;
             if (gc >= n) continue;
-            cplx* p = A + gr + (long long)gc * lda;
-            *p = csub(*p, acc[i][q]);
+            C_* p = A + gr + (long long)gc * lda;
+            *p = *p - acc[i][q];
           }
         }
         __syncthreads();
@@ -224,83 +237,80 @@ __global__ void __launch_bounds__(LU_THREADS) zgetrf_kernel(
   }
 }
 
-void zgetrf(cudaStream_t s, int batch, int n, cplx* A, int lda, long long a_bs, int* ipiv, long long piv_bs,
-            int32_t* status, int st_div) {
+template <class R>
+void getrf(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a_bs, int* ipiv, long long piv_bs,
+           int32_t* status, int st_div) {
   if (batch <= 0 || n <= 0) return;
-  zgetrf_kernel<<<batch, LU_THREADS, 0, s>>>(A, n, lda, a_bs, ipiv, piv_bs, status, st_div < 1 ? 1 : st_div); note_launch();
+  getrf_kernel<R><<<batch, LU_THREADS, 0, s>>>(A, n, lda, a_bs, ipiv, piv_bs, status, st_div < 1 ? 1 : st_div);
+  note_launch();
 }
 
 // --------------------------------------------------------------------- triangular solves
-// X = op(A)^{-1} B with A = P L U from zgetrf; B (n x nrhs, column-major, ldb) is overwritten.
+// X = op(A)^{-1} B with A = P L U from getrf; B (n x nrhs, column-major, ldb) is overwritten.
 // trans = 0: A X = B.  trans = 1: A^T X = B.  Each CTA owns SV_W right-hand sides of one
 // matrix and runs blocked substitution with K = SV_NB register-tiled updates.
 constexpr int SV_W = 64;
 constexpr int SV_NB = 16;
 
-__global__ void __launch_bounds__(256) zgetrs_kernel(
-    const cplx* __restrict__ LUall, int n, int lda, long long a_bs, const int* __restrict__ ipiv_all,
-    long long piv_bs, cplx* __restrict__ Ball, int nrhs, int ldb, long long b_bs, int trans) {
-  __shared__ cplx sT[SV_NB][SV_NB + 1];
-  __shared__ cplx sX[SV_NB][SV_W + 1];
-  __shared__ cplx sM[GT][SV_NB + 1];
-  const cplx* LU = LUall + blockIdx.y * a_bs;
+template <class R>
+__global__ void __launch_bounds__(256) getrs_kernel(
+    const Cx<R>* __restrict__ LUall, int n, int lda, long long a_bs, const int* __restrict__ ipiv_all,
+    long long piv_bs, Cx<R>* __restrict__ Ball, int nrhs, int ldb, long long b_bs, int trans) {
+  using C_ = Cx<R>;
+  __shared__ C_ sT[SV_NB][SV_NB + 1];
+  __shared__ C_ sX[SV_NB][SV_W + 1];
+  __shared__ C_ sM[GT][SV_NB + 1];
+  const C_* LU = LUall + blockIdx.y * a_bs;
   const int* ipiv = ipiv_all + (long long)blockIdx.y * piv_bs;
-  cplx* B = Ball + blockIdx.y * b_bs;
+  C_* B = Ball + blockIdx.y * b_bs;
   const int r0 = blockIdx.x * SV_W;
   const int w = min(SV_W, nrhs - r0);
   if (w <= 0) return;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  auto Bat = [&](int i, int c) -> cplx& { return B[i + (long long)(r0 + c) * ldb]; };
-  auto Lat = [&](int i, int j) -> cplx { return LU[i + (long long)j * lda]; };
-  // op(A) = L_eff * U_eff after the permutation; for trans = 0 first P^T B, forward with L
-  // (unit), backward with U.  For trans = 1: forward with U^T (non-unit), backward with L^T
-  // (unit), then the inverse permutation.
+  auto Bat = [&](int i, int c) -> C_& { return B[i + (long long)(r0 + c) * ldb]; };
+  auto Lat = [&](int i, int j) -> C_ { return LU[i + (long long)j * lda]; };
   if (trans == 0) {
     for (int j = 0; j < n; ++j) {
       int p = ipiv[j];
       if (p != j)
-        for (int c = tid; c < w; c += blockDim.x) { cplx t = Bat(j, c); Bat(j, c) = Bat(p, c); Bat(p, c) = t; }
+        for (int c = tid; c < w; c += blockDim.x) { C_ t = Bat(j, c); Bat(j, c) = Bat(p, c); Bat(p, c) = t; }
       __syncthreads();
     }
   }
-  // two sweeps: sweep 0 = forward (lower), sweep 1 = backward (upper)
   for (int sweep = 0; sweep < 2; ++sweep) {
     const bool forward = (sweep == 0);
-    // which triangle and diagonal handling
     // trans 0: fwd uses L (unit, A(i,j) i>j), bwd uses U (A(i,j) i<=j)
-    // trans 1: fwd uses U^T: element (i,j) i>=j is A(j,i), non-unit; bwd uses L^T: (i,j) i<j is A(j,i), unit
+    // trans 1: fwd uses U^T: (i,j) i>=j is A(j,i), non-unit; bwd uses L^T: (i,j) i<j is A(j,i), unit
     const bool unit = (trans == 0) ? forward : !forward;
     const int nblk = (n + SV_NB - 1) / SV_NB;
     for (int bi = 0; bi < nblk; ++bi) {
       const int blk = forward ? bi : (nblk - 1 - bi);
       const int i0 = blk * SV_NB, ib = min(SV_NB, n - i0);
-      // load the diagonal block of op-triangle into sT[r][c] (row r, col c of the effective matrix)
       for (int e = tid; e < SV_NB * SV_NB; e += blockDim.x) {
         int r = e % SV_NB, c = e / SV_NB;
-        cplx v = cmk(0.0, 0.0);
+        C_ v = cxzero<R>();
         if (r < ib && c < ib) v = (trans == 0) ? Lat(i0 + r, i0 + c) : Lat(i0 + c, i0 + r);
         sT[r][c] = v;
       }
       for (int e = tid; e < SV_NB * SV_W; e += blockDim.x) {
         int r = e % SV_NB, c = e / SV_NB;
-        sX[r][c] = (r < ib && c < w) ? Bat(i0 + r, c) : cmk(0.0, 0.0);
+        sX[r][c] = (r < ib && c < w) ? Bat(i0 + r, c) : cxzero<R>();
       }
       __syncthreads();
-      // small triangular solve, one thread per right-hand side column
       if (tid < w) {
         const int c = tid;
         if (forward) {
           for (int r = 0; r < ib; ++r) {
-            cplx acc = sX[r][c];
-            for (int t = 0; t < r; ++t) acc = csub(acc, cmul(sT[r][t], sX[t][c]));
-            if (!unit) acc = cdiv(acc, sT[r][r]);
+            C_ acc = sX[r][c];
+            for (int t = 0; t < r; ++t) acc = acc - sT[r][t] * sX[t][c];
+            if (!unit) acc = cxdiv(acc, sT[r][r]);
             sX[r][c] = acc;
           }
         } else {
           for (int r = ib - 1; r >= 0; --r) {
-            cplx acc = sX[r][c];
-            for (int t = r + 1; t < ib; ++t) acc = csub(acc, cmul(sT[r][t], sX[t][c]));
-            if (!unit) acc = cdiv(acc, sT[r][r]);
+            C_ acc = sX[r][c];
+            for (int t = r + 1; t < ib; ++t) acc = acc - sT[r][t] * sX[t][c];
+            if (!unit) acc = cxdiv(acc, sT[r][r]);
             sX[r][c] = acc;
           }
         }
@@ -310,25 +320,24 @@ __global__ void __launch_bounds__(256) zgetrs_kernel(
         int r = e % SV_NB, c = e / SV_NB;
         if (r < ib && c < w) Bat(i0 + r, c) = sX[r][c];
       }
-      // update the remaining rows: B[rest] -= M[rest, block] * X[block]
       const int rs = forward ? i0 + ib : 0;
       const int re = forward ? n : i0;
       for (int rr = rs; rr < re; rr += GT) {
         for (int e = tid; e < GT * SV_NB; e += blockDim.x) {
           int r = e % GT, c = e / GT;
           int gr = rr + r;
-          cplx v = cmk(0.0, 0.0);
+          C_ v = cxzero<R>();
           if (gr < re && c < ib) v = (trans == 0) ? Lat(gr, i0 + c) : Lat(i0 + c, gr);
           sM[r][c] = v;
         }
         __syncthreads();
-        cplx acc[4][4];
+        C_ acc[4][4];
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-          for (int q = 0; q < 4; ++q) acc[i][q] = cmk(0.0, 0.0);
+          for (int q = 0; q < 4; ++q) acc[i][q] = cxzero<R>();
         for (int kk = 0; kk < ib; ++kk) {
-          cplx a[4], b[4];
+          C_ a[4], b[4];
 #pragma unroll
           for (int i = 0; i < 4; ++i) a[i] = sM[tx + 16 * i][kk];
 #pragma unroll
@@ -336,7 +345,7 @@ __global__ void __launch_bounds__(256) zgetrs_kernel(
 #pragma unroll
           for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int q = 0; q < 4; ++q) acc[i][q] = cfma(a[i], b[q], acc[i][q]);
+            for (int q = 0; q < 4; ++q) acc[i][q] = cxfma(a[i], b[q], acc[i][q]);
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -346,7 +355,7 @@ __global__ void __launch_bounds__(256) zgetrs_kernel(
           for (int q = 0; q < 4; ++q) {
             int c = ty + 16 * q;
             if (c >= w) continue;
-            Bat(gr, c) = csub(Bat(gr, c), acc[i][q]);
+            Bat(gr, c) = Bat(gr, c) - acc[i][q];
           }
         }
         __syncthreads();
@@ -358,57 +367,97 @@ __global__ void __launch_bounds__(256) zgetrs_kernel(
     for (int j = n - 1; j >= 0; --j) {
       int p = ipiv[j];
       if (p != j)
-        for (int c = tid; c < w; c += blockDim.x) { cplx t = Bat(j, c); Bat(j, c) = Bat(p, c); Bat(p, c) = t; }
+        for (int c = tid; c < w; c += blockDim.x) { C_ t = Bat(j, c); Bat(j, c) = Bat(p, c); Bat(p, c) = t; }
       __syncthreads();
     }
   }
 }
 
-void zgetrs(cudaStream_t s, int batch, int n, const cplx* LU, int lda, long long a_bs,
-            const int* ipiv, long long piv_bs, cplx* B, int nrhs, int ldb, long long b_bs, int trans) {
+template <class R>
+void getrs(cudaStream_t s, int batch, int n, const Cx<R>* LU, int lda, long long a_bs, const int* ipiv,
+           long long piv_bs, Cx<R>* B, int nrhs, int ldb, long long b_bs, int trans) {
   if (batch <= 0 || n <= 0 || nrhs <= 0) return;
   dim3 grid((nrhs + SV_W - 1) / SV_W, batch);
-  zgetrs_kernel<<<grid, 256, 0, s>>>(LU, n, lda, a_bs, ipiv, piv_bs, B, nrhs, ldb, b_bs, trans); note_launch();
+  getrs_kernel<R><<<grid, 256, 0, s>>>(LU, n, lda, a_bs, ipiv, piv_bs, B, nrhs, ldb, b_bs, trans); note_launch();
 }
 
 // ---------------------------------------------------------------------- small helpers
-__global__ void ztranspose_kernel(const cplx* __restrict__ A, int m, int n, int lda, long long a_bs,
-                                  cplx* __restrict__ B, int ldb, long long b_bs) {
-  // B (n x m) = A^T, A (m x n); 32x32 tiles through shared memory
-  __shared__ cplx t[32][33];
-  A += blockIdx.z * a_bs; B += blockIdx.z * b_bs;
-  int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
-  for (int e = threadIdx.y; e < 32; e += blockDim.y) {
-    int i = i0 + threadIdx.x, j = j0 + e;
-    if (i < m && j < n) t[e][threadIdx.x] = A[i + (long long)j * lda];
-  }
-  __syncthreads();
-  for (int e = threadIdx.y; e < 32; e += blockDim.y) {
-    int j = j0 + threadIdx.x, i = i0 + e;
-    if (i < m && j < n) B[j + (long long)i * ldb] = t[threadIdx.x][e];
-  }
-}
-
-void ztranspose(cudaStream_t s, int batch, int m, int n, const cplx* A, int lda, long long a_bs,
-                cplx* B, int ldb, long long b_bs) {
-  if (batch <= 0 || m <= 0 || n <= 0) return;
-  dim3 grid((m + 31) / 32, (n + 31) / 32, batch);
-  ztranspose_kernel<<<grid, dim3(32, 8), 0, s>>>(A, m, n, lda, a_bs, B, ldb, b_bs); note_launch();
-}
-
-__global__ void zset_identity_kernel(cplx* A, int n, int lda, long long a_bs, long long total) {
+template <class R>
+__global__ void set_identity_kernel(Cx<R>* A, int n, int lda, long long a_bs, long long total) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= total) return;
   long long per = (long long)n * n;
   long long b = idx / per, r = idx % per;
   int i = (int)(r % n), j = (int)(r / n);
-  A[b * a_bs + i + (long long)j * lda] = cmk(i == j ? 1.0 : 0.0, 0.0);
+  A[b * a_bs + i + (long long)j * lda] = (i == j) ? cxone<R>() : cxzero<R>();
 }
 
-void zset_identity(cudaStream_t s, int batch, int n, cplx* A, int lda, long long a_bs) {
+template <class R>
+void set_identity(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a_bs) {
   long long total = (long long)batch * n * n;
   if (total <= 0) return;
-  zset_identity_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(A, n, lda, a_bs, total); note_launch();
+  set_identity_kernel<R><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(A, n, lda, a_bs, total); note_launch();
 }
+
+// dst (Cx<R2>) <- src (Cx<R1>), elementwise over `count` entries
+template <class R1, class R2>
+__global__ void convert_kernel(const Cx<R1>* __restrict__ src, Cx<R2>* __restrict__ dst, long long count) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  Cx<R1> v = src[i];
+  dst[i] = cxmk<R2>(R2(rto(v.x)), R2(rto(v.y)));
+}
+template <>
+__global__ void convert_kernel<double, df64>(const Cx<double>* __restrict__ src, Cx<df64>* __restrict__ dst,
+                                            long long count) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  Cx<double> v = src[i];
+  dst[i] = cxmk<df64>(df64(v.x), df64(v.y));
+}
+
+template <class R1, class R2>
+void convert(cudaStream_t s, const Cx<R1>* src, Cx<R2>* dst, long long count) {
+  if (count <= 0) return;
+  convert_kernel<R1, R2><<<(unsigned)((count + 255) / 256), 256, 0, s>>>(src, dst, count); note_launch();
+}
+
+// ---------------------------------------------------------- double2 (plain FP64) wrappers
+void zgemm(cudaStream_t s, int batch, int m, int n, int k, cplx alpha,
+           const cplx* A, long long a_rs, long long a_cs, long long a_bs,
+           const cplx* B, long long b_rs, long long b_cs, long long b_bs,
+           cplx beta, cplx* C, long long c_rs, long long c_cs, long long c_bs) {
+  gemm<double>(s, batch, m, n, k, alpha, (const Cx<double>*)A, a_rs, a_cs, a_bs, (const Cx<double>*)B, b_rs, b_cs,
+               b_bs, beta, (Cx<double>*)C, c_rs, c_cs, c_bs);
+}
+void zgetrf(cudaStream_t s, int batch, int n, cplx* A, int lda, long long a_bs, int* ipiv, long long piv_bs,
+            int32_t* status, int st_div) {
+  getrf<double>(s, batch, n, (Cx<double>*)A, lda, a_bs, ipiv, piv_bs, status, st_div);
+}
+void zgetrs(cudaStream_t s, int batch, int n, const cplx* LU, int lda, long long a_bs,
+            const int* ipiv, long long piv_bs, cplx* B, int nrhs, int ldb, long long b_bs, int trans) {
+  getrs<double>(s, batch, n, (const Cx<double>*)LU, lda, a_bs, ipiv, piv_bs, (Cx<double>*)B, nrhs, ldb, b_bs, trans);
+}
+void zset_identity(cudaStream_t s, int batch, int n, cplx* A, int lda, long long a_bs) {
+  set_identity<double>(s, batch, n, (Cx<double>*)A, lda, a_bs);
+}
+
+#define WB_INST(R)                                                                                       \
+  template void gemm<R>(cudaStream_t, int, int, int, int, double2, const Cx<R>*, long long, long long,     \
+                        long long, const Cx<R>*, long long, long long, long long, double2, Cx<R>*,         \
+                        long long, long long, long long);                                                 \
+  template void getrf<R>(cudaStream_t, int, int, Cx<R>*, int, long long, int*, long long, int32_t*, int); \
+  template void getrs<R>(cudaStream_t, int, int, const Cx<R>*, int, long long, const int*, long long,      \
+                         Cx<R>*, int, int, long long, int);                                               \
+  template void set_identity<R>(cudaStream_t, int, int, Cx<R>*, int, long long);
+WB_INST(double)
+WB_INST(float)
+WB_INST(df64)
+template void convert<double, float>(cudaStream_t, const Cx<double>*, Cx<float>*, long long);
+template void convert<double, double>(cudaStream_t, const Cx<double>*, Cx<double>*, long long);
+template void convert<float, double>(cudaStream_t, const Cx<float>*, Cx<double>*, long long);
+template void convert<double, df64>(cudaStream_t, const Cx<double>*, Cx<df64>*, long long);
+template void convert<df64, double>(cudaStream_t, const Cx<df64>*, Cx<double>*, long long);
+template void convert<df64, float>(cudaStream_t, const Cx<df64>*, Cx<float>*, long long);
 
 }  // namespace wb

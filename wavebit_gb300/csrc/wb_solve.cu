@@ -20,6 +20,8 @@
 #include "wb_common.cuh"
 #include "wb_kernels.h"
 #include "wb_internal.h"
+#include "wb_num.cuh"
+#include <type_traits>
 
 namespace wb {
 
@@ -104,16 +106,25 @@ __global__ void ports_kernel(int B, int hu, int hv, const double* __restrict__ w
   if (threadIdx.x == 0) { pv.nt[b] = nt; pv.nb[b] = nb; }
 }
 
+
+// All kernels below are templates over the working real type R of their stage (wb_num.cuh):
+// double for the plain form; df64 (stage B) and float or df64 (stage C) for the mixed form.
+// FP64 inputs (convolution matrices, port vectors, exponentials) are converted on load.
+
+template <class R> __device__ __forceinline__ Cx<R> ld(const cplx* p) { return cxfrom<R>(*p); }
+
 // --------------------------------------------------------------- Omega^2 assembly (GEMM)
 // Omega2[(rb,cb) quadrant] = (diag(k_rb) epz_i diag(k_cb) - [rb==cb] I) @ (cb ? epy : epx)
-//                            + diagonal term, k_0 = kx, k_1 = ky.
+//                            + diagonal term, k_0 = kx, k_1 = ky  (solve_2d.py:2377-2418)
+template <class R>
 __global__ void __launch_bounds__(256) omega2_kernel(int N, const cplx* __restrict__ conv, long long conv_ls,
                                                      const int* __restrict__ pair_layer,
                                                      const int* __restrict__ pair_solve,
                                                      const double* __restrict__ kxa, const double* __restrict__ kya,
-                                                     cplx* __restrict__ out, long long out_bs) {
-  __shared__ cplx sA[8][65];
-  __shared__ cplx sB[8][65];
+                                                     Cx<R>* __restrict__ out, long long out_bs) {
+  using C_ = Cx<R>;
+  __shared__ C_ sA[8][65];
+  __shared__ C_ sB[8][65];
   __shared__ double skr[64], skc_a[8];
   const int pair = blockIdx.z >> 2, quad = blockIdx.z & 3, rb = quad & 1, cb = quad >> 1;
   const int n = 2 * N;
@@ -127,15 +138,15 @@ __global__ void __launch_bounds__(256) omega2_kernel(int N, const cplx* __restri
   const double* ky = kya + (long long)pair_solve[pair] * N;
   const double* kr = rb ? ky : kx;
   const double* kc = cb ? ky : kx;
-  cplx* C = out + pair * out_bs;
+  C_* C = out + pair * out_bs;
   const int row0 = blockIdx.x * 64, col0 = blockIdx.y * 64;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   if (tid < 64) skr[tid] = (row0 + tid < N) ? kr[row0 + tid] : 0.0;
-  cplx acc[4][4];
+  C_ acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = cmk(0.0, 0.0);
+    for (int j = 0; j < 4; ++j) acc[i][j] = cxzero<R>();
   for (int k0 = 0; k0 < N; k0 += 8) {
     if (tid < 8) skc_a[tid] = (k0 + tid < N) ? kc[k0 + tid] : 0.0;
     __syncthreads();
@@ -149,19 +160,19 @@ __global__ void __launch_bounds__(256) omega2_kernel(int N, const cplx* __restri
         v = cscale(cscale(epz[gr + (long long)gc * N], skr[r]), skc_a[c]);
         if (rb == cb && gr == gc) v.x -= 1.0;
       }
-      sA[c][r] = v;
+      sA[c][r] = cxfrom<R>(v);
     }
 #pragma unroll
     for (int e = 0; e < 2; ++e) {
       int idx = tid + e * 256;
       int r = idx % 8, c = idx / 8;
       int gr = k0 + r, gc = col0 + c;
-      sB[r][c] = (gr < N && gc < N) ? Bm[gr + (long long)gc * N] : cmk(0.0, 0.0);
+      sB[r][c] = (gr < N && gc < N) ? ld<R>(Bm + gr + (long long)gc * N) : cxzero<R>();
     }
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < 8; ++kk) {
-      cplx a[4], b[4];
+      C_ a[4], b[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) a[i] = sA[kk][tx + 16 * i];
 #pragma unroll
@@ -169,7 +180,7 @@ __global__ void __launch_bounds__(256) omega2_kernel(int N, const cplx* __restri
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = cfma(a[i], b[j], acc[i][j]);
+        for (int j = 0; j < 4; ++j) acc[i][j] = cxfma(a[i], b[j], acc[i][j]);
     }
     __syncthreads();
   }
@@ -181,13 +192,13 @@ __global__ void __launch_bounds__(256) omega2_kernel(int N, const cplx* __restri
     for (int j = 0; j < 4; ++j) {
       int gc = col0 + ty + 16 * j;
       if (gc >= N) continue;
-      cplx v = acc[i][j];
+      C_ v = acc[i][j];
       if (gr == gc) {
         double d;
         if (rb == 0 && cb == 0) d = ky[gr] * ky[gr];
         else if (rb == 1 && cb == 1) d = kx[gr] * kx[gr];
         else d = -kx[gr] * ky[gr];
-        v.x += d;
+        v.x = v.x + R(d);
       }
       C[(gr + rb * N) + (long long)(gc + cb * N) * n] = v;
     }
@@ -195,23 +206,25 @@ __global__ void __launch_bounds__(256) omega2_kernel(int N, const cplx* __restri
 }
 
 // ---------------------------------------------------- q, the grazing screen, X = exp(-k0 d q)
-__global__ void modeq_kernel(int n_pairs, int n, const cplx* __restrict__ w, const int* __restrict__ pair_solve,
+// mode_q (conventions.py:186-249) on the eigenvalues; q and X are kept in FP64.
+template <class R>
+__global__ void modeq_kernel(int n_pairs, int n, const Cx<R>* __restrict__ w, const int* __restrict__ pair_solve,
                              const double* __restrict__ thick, const double* __restrict__ wavelength,
-                             cplx* __restrict__ q, cplx* __restrict__ X, int32_t* __restrict__ status,
-                             int layers_per_solve) {
+                             cplx* __restrict__ wout, cplx* __restrict__ q, cplx* __restrict__ X,
+                             int32_t* __restrict__ status) {
   __shared__ double smin[32], smax[32];
   const int p = blockIdx.x;
-  const cplx* wp = w + (long long)p * n;
+  const Cx<R>* wp = w + (long long)p * n;
   const double k0 = 2.0 * 3.141592653589793 / wavelength[pair_solve[p]];
   const double d = thick[p];
   double lo = INFINITY, hi = 0.0;
   bool bad = false;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    cplx wi = wp[i];
+    cplx wi = cxto(wp[i]);
+    if (wout) wout[(long long)p * n + i] = wi;
     if (!(isfinite(wi.x) && isfinite(wi.y))) bad = true;
     double a = cabsv(wi);
     lo = fmin(lo, a); hi = fmax(hi, a);
-    // mode_q: Re q >= 0, tie Im q <= 0 when |Re q| <= 1e-12
     cplx v = csqrt_p(wi);
     bool flip = (fabs(v.x) > 1e-12) ? (v.x < 0.0) : (v.y > 0.0);
     if (flip) v = cneg(v);
@@ -227,62 +240,62 @@ __global__ void modeq_kernel(int n_pairs, int n, const cplx* __restrict__ w, con
   if (threadIdx.x == 0) {
     for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { lo = fmin(lo, smin[k]); hi = fmax(hi, smax[k]); }
     lo = fmin(lo, smin[0]); hi = fmax(hi, smax[0]);
-    int32_t* st = status + pair_solve[p];
-    if (lo < 1e-9 * hi) wb_flag(st, WB_ST_GRAZING);
+    if (lo < 1e-9 * hi) wb_flag(status + pair_solve[p], WB_ST_GRAZING);
   }
   if (bad) wb_flag(status + pair_solve[p], WB_ST_NONFINITE);
-  (void)layers_per_solve;
 }
 
-// ------------------------------------------------------------ V = Omega_R W / q, rotated
+// ------------------------------------------------------------ V = Omega_R W / q
 // V_top = -epy W_bot - diag(kx ky) W_top + diag(kx^2) W_bot
-// V_bot =  epx W_top - diag(ky^2) W_top + diag(ky kx) W_bot
+// V_bot =  epx W_top - diag(ky^2) W_top + diag(ky kx) W_bot      (solve_2d.py:2393-2448)
+template <class R>
 __global__ void __launch_bounds__(256) vmodes_kernel(int N, const cplx* __restrict__ conv, long long conv_ls,
                                                      const int* __restrict__ pair_layer,
                                                      const int* __restrict__ pair_solve,
                                                      const double* __restrict__ kxa, const double* __restrict__ kya,
-                                                     const cplx* __restrict__ Wall, const cplx* __restrict__ qall,
-                                                     cplx* __restrict__ Vall, long long bs) {
-  __shared__ cplx sA[8][65];
-  __shared__ cplx sB[8][65];
+                                                     const Cx<R>* __restrict__ Wall, const cplx* __restrict__ qall,
+                                                     Cx<R>* __restrict__ Vall, long long bs) {
+  using C_ = Cx<R>;
+  __shared__ C_ sA[8][65];
+  __shared__ C_ sB[8][65];
   const int pair = blockIdx.z >> 1, half = blockIdx.z & 1;
   const int n = 2 * N;
   const long long NN = (long long)N * N;
   const cplx* base = conv + (long long)pair_layer[pair] * conv_ls;
-  const cplx* Am = half ? base : base + NN;       // epx for the bottom half, epy for the top
+  const cplx* Am = half ? base : base + NN;
   const double sgn = half ? 1.0 : -1.0;
   const double* kx = kxa + (long long)pair_solve[pair] * N;
   const double* ky = kya + (long long)pair_solve[pair] * N;
-  const cplx* W = Wall + pair * bs;
-  const cplx* Wsrc = W + (half ? 0 : N);            // rows of W multiplied: W_top (bottom half) / W_bot (top)
+  const C_* W = Wall + pair * bs;
+  const C_* Wsrc = W + (half ? 0 : N);
   const cplx* q = qall + (long long)pair * n;
-  cplx* V = Vall + pair * bs;
+  C_* V = Vall + pair * bs;
   const int row0 = blockIdx.x * 64, col0 = blockIdx.y * 64;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  cplx acc[4][4];
+  C_ acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = cmk(0.0, 0.0);
+    for (int j = 0; j < 4; ++j) acc[i][j] = cxzero<R>();
   for (int k0 = 0; k0 < N; k0 += 8) {
 #pragma unroll
     for (int e = 0; e < 2; ++e) {
       int idx = tid + e * 256;
       int r = idx % 64, c = idx / 64;
       int gr = row0 + r, gc = k0 + c;
-      sA[c][r] = (gr < N && gc < N) ? cscale(Am[gr + (long long)gc * N], sgn) : cmk(0.0, 0.0);
+      sA[c][r] = (gr < N && gc < N) ? cxfrom<R>(cscale(Am[gr + (long long)gc * N], sgn)) : cxzero<R>();
     }
 #pragma unroll
     for (int e = 0; e < 2; ++e) {
       int idx = tid + e * 256;
       int r = idx % 8, c = idx / 8;
       int gr = k0 + r, gc = col0 + c;
-      sB[r][c] = (gr < N && gc < n) ? Wsrc[gr + (long long)gc * n] : cmk(0.0, 0.0);
+      sB[r][c] = (gr < N && gc < n) ? Wsrc[gr + (long long)gc * n] : cxzero<R>();
     }
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < 8; ++kk) {
-      cplx a[4], b[4];
+      C_ a[4], b[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) a[i] = sA[kk][tx + 16 * i];
 #pragma unroll
@@ -290,7 +303,7 @@ __global__ void __launch_bounds__(256) vmodes_kernel(int N, const cplx* __restri
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = cfma(a[i], b[j], acc[i][j]);
+        for (int j = 0; j < 4; ++j) acc[i][j] = cxfma(a[i], b[j], acc[i][j]);
     }
     __syncthreads();
   }
@@ -298,23 +311,24 @@ __global__ void __launch_bounds__(256) vmodes_kernel(int N, const cplx* __restri
   for (int i = 0; i < 4; ++i) {
     int gr = row0 + tx + 16 * i;
     if (gr >= N) continue;
-    const double kxi = kx[gr], kyi = ky[gr];
+    const R kxi = R(kx[gr]), kyi = R(ky[gr]);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       int gc = col0 + ty + 16 * j;
       if (gc >= n) continue;
-      const cplx wt = W[gr + (long long)gc * n], wb = W[gr + N + (long long)gc * n];
-      cplx v = acc[i][j];
-      if (half == 0) { v = cadd(v, cscale(wt, -kxi * kyi)); v = cadd(v, cscale(wb, kxi * kxi)); }
-      else { v = cadd(v, cscale(wt, -kyi * kyi)); v = cadd(v, cscale(wb, kyi * kxi)); }
-      V[gr + half * N + (long long)gc * n] = cdiv(v, q[gc]);
+      const C_ wt = W[gr + (long long)gc * n], wb = W[gr + N + (long long)gc * n];
+      C_ v = acc[i][j];
+      if (half == 0) v = v + wt * (-(kxi * kyi)) + wb * (kxi * kxi);
+      else v = v + wt * (-(kyi * kyi)) + wb * (kyi * kxi);
+      V[gr + half * N + (long long)gc * n] = cxdiv(v, ld<R>(q + gc));
     }
   }
 }
 
 // s/p rotation of W and V in place (solve_2d.py:2584-2616)
+template <class R>
 __global__ void sp_rotate_kernel(int n_pairs, int N, const int* __restrict__ pair_solve, const double* __restrict__ ca,
-                                 const double* __restrict__ sa, cplx* __restrict__ Wall, cplx* __restrict__ Vall,
+                                 const double* __restrict__ sa, Cx<R>* __restrict__ Wall, Cx<R>* __restrict__ Vall,
                                  long long bs) {
   const int n = 2 * N;
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -323,59 +337,115 @@ __global__ void sp_rotate_kernel(int n_pairs, int N, const int* __restrict__ pai
   const long long rem = idx % ((long long)N * n);
   const int i = (int)(rem % N), j = (int)(rem / N);
   const long long o = (long long)pair_solve[pair] * N + i;
-  const double c = ca[o], s = sa[o];
-  cplx* W = Wall + pair * bs;
-  cplx* V = Vall + pair * bs;
+  const R c = R(ca[o]), s = R(sa[o]);
+  Cx<R>* W = Wall + pair * bs;
+  Cx<R>* V = Vall + pair * bs;
   const long long a = i + (long long)j * n, b = a + N;
-  const cplx w1 = W[a], w2 = W[b], v1 = V[a], v2 = V[b];
-  W[a] = csub(cscale(w2, c), cscale(w1, s));
-  W[b] = cadd(cscale(w1, c), cscale(w2, s));
-  V[a] = cadd(cscale(v1, c), cscale(v2, s));
-  V[b] = csub(cscale(v2, c), cscale(v1, s));
+  const Cx<R> w1 = W[a], w2 = W[b], v1 = V[a], v2 = V[b];
+  W[a] = w2 * c - w1 * s;
+  W[b] = w1 * c + w2 * s;
+  V[a] = v1 * c + v2 * s;
+  V[b] = v2 * c - v1 * s;
 }
 
 // ------------------------------------------------------------------ cascade elementwise
-// R_{L+1} = diag(t11)
-__global__ void diag_matrix_kernel(int B, int n, const cplx* __restrict__ d, cplx* __restrict__ R, long long bs) {
+template <class R>
+__global__ void diag_matrix_kernel(int B, int n, const cplx* __restrict__ d, Cx<R>* __restrict__ M, long long bs) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= (long long)B * n * n) return;
   const long long b = idx / ((long long)n * n), rem = idx % ((long long)n * n);
   const int i = (int)(rem % n), j = (int)(rem / n);
-  R[b * bs + rem] = (i == j) ? d[b * n + i] : cmk(0.0, 0.0);
+  M[b * bs + rem] = (i == j) ? ld<R>(d + b * n + i) : cxzero<R>();
 }
 
 // U1 = diag(wg)(I + R), U2 = diag(vg)(I - R)
-__global__ void u12_kernel(int B, int n, const cplx* __restrict__ R, long long r_bs, const cplx* __restrict__ wg,
-                           const cplx* __restrict__ vg, cplx* __restrict__ U1, cplx* __restrict__ U2, long long bs) {
+template <class R>
+__global__ void u12_kernel(int B, int n, const Cx<R>* __restrict__ Rm, long long r_bs, const cplx* __restrict__ wg,
+                           const cplx* __restrict__ vg, Cx<R>* __restrict__ U1, Cx<R>* __restrict__ U2, long long bs) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= (long long)B * n * n) return;
   const long long b = idx / ((long long)n * n), rem = idx % ((long long)n * n);
   const int i = (int)(rem % n), j = (int)(rem / n);
-  cplx r = R[b * r_bs + rem];
-  cplx e = cmk(i == j ? 1.0 : 0.0, 0.0);
-  U1[b * bs + rem] = cmul(wg[b * n + i], cadd(e, r));
-  U2[b * bs + rem] = cmul(vg[b * n + i], csub(e, r));
+  Cx<R> r = Rm[b * r_bs + rem];
+  Cx<R> e = (i == j) ? cxone<R>() : cxzero<R>();
+  U1[b * bs + rem] = ld<R>(wg + b * n + i) * (e + r);
+  U2[b * bs + rem] = ld<R>(vg + b * n + i) * (e - r);
 }
 
+// M = P1 + P2 (to Mout, batch stride m_bs), NT = (P1 - P2)^T ; 32x32 tiles
+template <class R>
+__global__ void mn2_kernel(int n, const Cx<R>* __restrict__ P1, const Cx<R>* __restrict__ P2, long long p_bs,
+                           Cx<R>* __restrict__ Mout, long long m_bs, Cx<R>* __restrict__ NT) {
+  __shared__ Cx<R> t[32][33];
+  const long long b = blockIdx.z;
+  const Cx<R>* p1 = P1 + b * p_bs; const Cx<R>* p2 = P2 + b * p_bs;
+  Cx<R>* mo = Mout + b * m_bs; Cx<R>* nt = NT + b * p_bs;
+  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+  for (int e = threadIdx.y; e < 32; e += blockDim.y) {
+    int i = i0 + threadIdx.x, j = j0 + e;
+    if (i < n && j < n) {
+      long long o = i + (long long)j * n;
+      Cx<R> a = p1[o], c = p2[o];
+      mo[o] = a + c;
+      t[e][threadIdx.x] = a - c;
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.y; e < 32; e += blockDim.y) {
+    int j = j0 + threadIdx.x, i = i0 + e;
+    if (i < n && j < n) nt[j + (long long)i * n] = t[threadIdx.x][e];
+  }
+}
 
 // from rho_b^T: Y1T = (I - X rho_b X)^T into Y1, Y2T = (I + X rho_b X)^T in place
-__global__ void rho_kernel(int B, int n, cplx* __restrict__ RT, cplx* __restrict__ Y1, const cplx* __restrict__ X,
+template <class R>
+__global__ void rho_kernel(int B, int n, Cx<R>* __restrict__ RT, Cx<R>* __restrict__ Y1, const cplx* __restrict__ X,
                            long long x_ps, long long bs) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= (long long)B * n * n) return;
   const long long b = idx / ((long long)n * n), rem = idx % ((long long)n * n);
   const int jr = (int)(rem % n), ic = (int)(rem / n);     // RT(jr, ic) = rho_b(ic, jr)
   const cplx* Xb = X + b * x_ps;
-  cplx r = cmul(cmul(Xb[ic], RT[b * bs + rem]), Xb[jr]);
-  cplx e = cmk(jr == ic ? 1.0 : 0.0, 0.0);
-  Y1[b * bs + rem] = csub(e, r);
-  RT[b * bs + rem] = cadd(e, r);
+  Cx<R> r = (ld<R>(Xb + ic) * RT[b * bs + rem]) * ld<R>(Xb + jr);
+  Cx<R> e = (jr == ic) ? cxone<R>() : cxzero<R>();
+  Y1[b * bs + rem] = e - r;
+  RT[b * bs + rem] = e + r;
 }
 
+// Aterm = X1 diag(wg) + X2 diag(vg) (to Aout), Bterm = -X1 diag(wg) + X2 diag(vg) (to Bout)
+template <class R>
+__global__ void ab2_kernel(int n, const Cx<R>* __restrict__ X1T, const Cx<R>* __restrict__ X2T, long long x_bs,
+                           const cplx* __restrict__ wg, const cplx* __restrict__ vg,
+                           Cx<R>* __restrict__ Aout, long long a_bs, Cx<R>* __restrict__ Bout, long long b_bs) {
+  __shared__ Cx<R> t1[32][33], t2[32][33];
+  const long long b = blockIdx.z;
+  const Cx<R>* x1 = X1T + b * x_bs; const Cx<R>* x2 = X2T + b * x_bs;
+  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+  for (int e = threadIdx.y; e < 32; e += blockDim.y) {
+    int j = j0 + threadIdx.x, i = i0 + e;
+    if (i < n && j < n) {
+      long long o = j + (long long)i * n;
+      t1[e][threadIdx.x] = x1[o];
+      t2[e][threadIdx.x] = x2[o];
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.y; e < 32; e += blockDim.y) {
+    int i = i0 + threadIdx.x, j = j0 + e;
+    if (i < n && j < n) {
+      Cx<R> a1 = t1[threadIdx.x][e] * ld<R>(wg + b * n + j);
+      Cx<R> a2 = t2[threadIdx.x][e] * ld<R>(vg + b * n + j);
+      long long o = i + (long long)j * n;
+      Aout[b * a_bs + o] = a1 + a2;
+      Bout[b * b_bs + o] = a2 - a1;
+    }
+  }
+}
 
-// incident columns: [a_s d; -i n_top a_p d], pure s, pure p (d = unit vector on the specular order)
+// incident columns: [a_s d; -i n_top a_p d], pure s, pure p (d: unit vector on the specular order)
+template <class R>
 __global__ void incident_kernel(int B, int N, const cplx* __restrict__ pol, const cplx* __restrict__ nt,
-                                cplx* __restrict__ C, long long c_bs) {
+                                Cx<R>* __restrict__ C, long long c_bs) {
   const int n = 2 * N;
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= (long long)B * n * 3) return;
@@ -390,63 +460,67 @@ __global__ void incident_kernel(int B, int N, const cplx* __restrict__ pol, cons
   cplx v = cmk(0.0, 0.0);
   if (i == spec) v = as;
   else if (i == N + spec) v = cmul(cmul(cmk(0.0, -1.0), nt[b]), ap);
-  C[b * c_bs + i + (long long)col * n] = v;
+  C[b * c_bs + i + (long long)col * n] = cxfrom<R>(v);
 }
 
-// G0 = I - diag(r22) R1 ; rhs = diag(r21) C
-__global__ void top_kernel(int B, int n, const cplx* __restrict__ R1, long long r_bs, const cplx* __restrict__ r22,
-                           cplx* __restrict__ G0, long long bs) {
+// G0 = I - diag(r22) R0
+template <class R>
+__global__ void top_kernel(int B, int n, const Cx<R>* __restrict__ R1, long long r_bs, const cplx* __restrict__ r22,
+                           Cx<R>* __restrict__ G0, long long bs) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= (long long)B * n * n) return;
   const long long b = idx / ((long long)n * n), rem = idx % ((long long)n * n);
   const int i = (int)(rem % n), j = (int)(rem / n);
-  cplx v = cneg(cmul(r22[b * n + i], R1[b * r_bs + rem]));
-  if (i == j) v.x += 1.0;
+  Cx<R> v = -(ld<R>(r22 + b * n + i) * R1[b * r_bs + rem]);
+  if (i == j) v.x = v.x + R(1.0);
   G0[b * bs + rem] = v;
 }
 
-// out = diag(d) * in (+ diag(e) * in2 if e), n x 3 per batch
-__global__ void dscale3_kernel(int B, int n, const cplx* __restrict__ d, const cplx* __restrict__ in, long long in_bs,
-                               const cplx* __restrict__ e, const cplx* __restrict__ in2, long long in2_bs,
-                               cplx* __restrict__ out, long long out_bs, double factor) {
+// out = diag(d) in (+ diag(e) in2 when e), n x 3 per batch
+template <class R>
+__global__ void dscale3_kernel(int B, int n, const cplx* __restrict__ d, const Cx<R>* __restrict__ in, long long in_bs,
+                               const cplx* __restrict__ e, const Cx<R>* __restrict__ in2, long long in2_bs,
+                               Cx<R>* __restrict__ out, long long out_bs) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= (long long)B * n * 3) return;
   const long long b = idx / (n * 3);
   const int rem = (int)(idx % (n * 3)), i = rem % n;
-  cplx v = cmul(d[b * n + i], in[b * in_bs + rem]);
-  if (e) v = cadd(v, cmul(e[b * n + i], in2[b * in2_bs + rem]));
-  out[b * out_bs + rem] = cscale(v, factor);
+  Cx<R> v = ld<R>(d + b * n + i) * in[b * in_bs + rem];
+  if (e) v = v + ld<R>(e + b * n + i) * in2[b * in2_bs + rem];
+  out[b * out_bs + rem] = v;
 }
 
 // rhs1 = wg o (g + h), rhs2 = vg o (g - h)
-__global__ void gh_kernel(int B, int n, const cplx* __restrict__ g, const cplx* __restrict__ h,
+template <class R>
+__global__ void gh_kernel(int B, int n, const Cx<R>* __restrict__ g, const Cx<R>* __restrict__ h,
                           const cplx* __restrict__ wg, const cplx* __restrict__ vg,
-                          cplx* __restrict__ r1, cplx* __restrict__ r2, long long bs3) {
+                          Cx<R>* __restrict__ r1, Cx<R>* __restrict__ r2, long long bs3) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= (long long)B * n * 3) return;
   const long long b = idx / (n * 3);
   const int rem = (int)(idx % (n * 3)), i = rem % n;
-  cplx gg = g[b * bs3 + rem], hh = h[b * bs3 + rem];
-  r1[b * bs3 + rem] = cmul(wg[b * n + i], cadd(gg, hh));
-  r2[b * bs3 + rem] = cmul(vg[b * n + i], csub(gg, hh));
+  Cx<R> gg = g[b * bs3 + rem], hh = h[b * bs3 + rem];
+  r1[b * bs3 + rem] = ld<R>(wg + b * n + i) * (gg + hh);
+  r2[b * bs3 + rem] = ld<R>(vg + b * n + i) * (gg - hh);
 }
 
-// cb = X o (r1 + r2)/2 ; written into r1
-__global__ void ct_kernel(int B, int n, cplx* __restrict__ r1, const cplx* __restrict__ r2,
-                          const cplx* __restrict__ X, long long x_ps, long long bs3) {
+// g_next rhs = X o (r1 + r2) (= 2 c+_bottom), written into g
+template <class R>
+__global__ void ct_kernel(int B, int n, const Cx<R>* __restrict__ r1, const Cx<R>* __restrict__ r2,
+                          const cplx* __restrict__ X, long long x_ps, Cx<R>* __restrict__ g, long long bs3) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= (long long)B * n * 3) return;
   const long long b = idx / (n * 3);
   const int rem = (int)(idx % (n * 3)), i = rem % n;
-  cplx ct = cscale(cadd(r1[b * bs3 + rem], r2[b * bs3 + rem]), 0.5);
-  r1[b * bs3 + rem] = cscale(cmul(X[b * x_ps + i], ct), 2.0);
+  g[b * bs3 + rem] = ld<R>(X + b * x_ps + i) * (r1[b * bs3 + rem] + r2[b * bs3 + rem]);
 }
 
-// per-order efficiencies (scattering.py:907-994, solve_1d.py:1588-1610, power.py:13-159)
-__global__ void efficiency_kernel(int B, int N, const cplx* __restrict__ cref, const cplx* __restrict__ ctrn,
+// per-order efficiencies (scattering.py:907-994, solve_1d.py:1588-1610, power.py:13-159), in FP64
+template <class R>
+__global__ void efficiency_kernel(int B, int N, const Cx<R>* __restrict__ cref, const Cx<R>* __restrict__ ctrn,
                                   long long bs3, PortVectors pv, const cplx* __restrict__ eps_top,
                                   const cplx* __restrict__ eps_bot, const cplx* __restrict__ pol,
-                                  double* __restrict__ R, double* __restrict__ T, cplx* __restrict__ amps,
+                                  double* __restrict__ Rout, double* __restrict__ Tout, cplx* __restrict__ amps,
                                   int32_t* __restrict__ status) {
   const int n = 2 * N;
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -462,18 +536,18 @@ __global__ void efficiency_kernel(int B, int N, const cplx* __restrict__ cref, c
   if (col == 0) denom = cabs2(pol[2 * b]) * s_power + cabs2(pol[2 * b + 1]) * p_power;
   else if (col == 1) denom = s_power;
   else denom = p_power;
-  const cplx Rs = cref[b * bs3 + i + (long long)col * n];
-  const cplx Rp = cneg(cref[b * bs3 + N + i + (long long)col * n]);
-  const cplx Ts = ctrn[b * bs3 + i + (long long)col * n];
-  const cplx Tp = ctrn[b * bs3 + N + i + (long long)col * n];
+  const cplx Rs = cxto(cref[b * bs3 + i + (long long)col * n]);
+  const cplx Rp = cneg(cxto(cref[b * bs3 + N + i + (long long)col * n]));
+  const cplx Ts = cxto(ctrn[b * bs3 + i + (long long)col * n]);
+  const cplx Tp = cxto(ctrn[b * bs3 + N + i + (long long)col * n]);
   const cplx kzt = pv.kz_top[b * N + i], kzb = pv.kz_bot[b * N + i];
   const double eRs = cabs2(Rs) * kzt.x / denom;
   const double eRp = cabs2(Rp) * cdiv(kzt, et).x / denom;
   const double eTs = cabs2(Ts) * kzb.x / denom;
   const double eTp = cabs2(Tp) * cdiv(kzb, eb).x / denom;
   const double r = eRs + eRp, t = eTs + eTp;
-  R[(b * 3 + col) * N + i] = r;
-  T[(b * 3 + col) * N + i] = t;
+  Rout[(b * 3 + col) * N + i] = r;
+  Tout[(b * 3 + col) * N + i] = t;
   if (amps) {
     const cplx mi_nt = cmul(cmk(0.0, -1.0), nt), mi_nb = cmul(cmk(0.0, -1.0), nb);
     cplx* a = amps + ((b * 3 + col) * 4) * (long long)N;
@@ -493,95 +567,131 @@ __global__ void pairs_kernel(int B, int L, const int* __restrict__ layer_index, 
   pair_thick[p] = thick[p];
 }
 
-__global__ void copy3_kernel(int B, int n, const cplx* __restrict__ src, long long s_bs, cplx* __restrict__ dst,
-                             long long d_bs) {
-  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (idx >= (long long)B * n * 3) return;
-  const long long b = idx / (n * 3);
-  const int rem = (int)(idx % (n * 3));
-  dst[b * d_bs + rem] = src[b * s_bs + rem];
-}
-
-// M = P1 + P2 (to Mout, batch stride m_bs), NT = (P1 - P2)^T ; 32x32 tiles
-__global__ void mn2_kernel(int n, const cplx* __restrict__ P1, const cplx* __restrict__ P2, long long p_bs,
-                           cplx* __restrict__ Mout, long long m_bs, cplx* __restrict__ NT) {
-  __shared__ cplx t[32][33];
-  const long long b = blockIdx.z;
-  const cplx* p1 = P1 + b * p_bs; const cplx* p2 = P2 + b * p_bs;
-  cplx* mo = Mout + b * m_bs; cplx* nt = NT + b * p_bs;
-  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
-  for (int e = threadIdx.y; e < 32; e += blockDim.y) {
-    int i = i0 + threadIdx.x, j = j0 + e;
-    if (i < n && j < n) {
-      long long o = i + (long long)j * n;
-      cplx a = p1[o], c = p2[o];
-      mo[o] = cadd(a, c);
-      t[e][threadIdx.x] = csub(a, c);
-    }
+// ------------------------------------------------------------------- stage B driver
+// Omega^2, eigen-decomposition, q/X, V and the s/p rotation for P pairs, in precision RB.
+// On return OM holds bigW and Zb holds bigV (both Cx<RB>), w/q/X the FP64 modal data.
+template <class RB>
+void stage_b(cudaStream_t s, int P, int N, const cplx* conv, const int* pair_layer, const int* pair_solve,
+             const double* pair_thick, const double* wavelength, const double* kx, const double* ky,
+             Cx<RB>* OM, Cx<RB>* Zb, Cx<RB>* Xv, Cx<RB>* wr, Cx<RB>* tau, cplx* w, cplx* q, cplx* X,
+             const double* c, const double* sn, int32_t* st, int st_div, bool rotate) {
+  const int n = 2 * N;
+  const long long n2 = (long long)n * n, NN = (long long)N * N;
+  {
+    dim3 gr((N + 63) / 64, (N + 63) / 64, P * 4);
+    omega2_kernel<RB><<<gr, 256, 0, s>>>(N, conv, 3 * NN, pair_layer, pair_solve, kx, ky, OM, n2); note_launch();
   }
-  __syncthreads();
-  for (int e = threadIdx.y; e < 32; e += blockDim.y) {
-    int j = j0 + threadIdx.x, i = i0 + e;
-    if (i < n && j < n) nt[j + (long long)i * n] = t[threadIdx.x][e];
+  geev_schur<RB>(s, P, n, OM, n, n2, Zb, n, n2, wr, tau, st, st_div);
+  trevc<RB>(s, P, n, OM, n, n2, Xv, n, n2);
+  gemm<RB>(s, P, n, n, n, make_double2(1, 0), Zb, 1, n, n2, Xv, 1, n, n2, make_double2(0, 0), OM, 1, n, n2);
+  normalize_columns<RB>(s, P, n, OM, n, n2);
+  modeq_kernel<RB><<<P, 256, 0, s>>>(P, n, wr, pair_solve, pair_thick, wavelength, w, q, X, st); note_launch();
+  {
+    dim3 gr((N + 63) / 64, (n + 63) / 64, P * 2);
+    vmodes_kernel<RB><<<gr, 256, 0, s>>>(N, conv, 3 * NN, pair_layer, pair_solve, kx, ky, OM, q, Zb, n2); note_launch();
+  }
+  if (rotate) {
+    sp_rotate_kernel<RB><<<nblk((long long)P * N * n, 256), 256, 0, s>>>(P, N, pair_solve, c, sn, OM, Zb, n2);
+    note_launch();
   }
 }
 
-// Aterm = X1 diag(wg) + X2 diag(vg) (to Aout), Bterm = -X1 diag(wg) + X2 diag(vg) (to Bout)
-__global__ void ab2_kernel(int n, const cplx* __restrict__ X1T, const cplx* __restrict__ X2T, long long x_bs,
-                           const cplx* __restrict__ wg, const cplx* __restrict__ vg,
-                           cplx* __restrict__ Aout, long long a_bs, cplx* __restrict__ Bout, long long b_bs) {
-  __shared__ cplx t1[32][33], t2[32][33];
-  const long long b = blockIdx.z;
-  const cplx* x1 = X1T + b * x_bs; const cplx* x2 = X2T + b * x_bs;
-  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
-  for (int e = threadIdx.y; e < 32; e += blockDim.y) {
-    int j = j0 + threadIdx.x, i = i0 + e;
-    if (i < n && j < n) {
-      long long o = j + (long long)i * n;
-      t1[e][threadIdx.x] = x1[o];
-      t2[e][threadIdx.x] = x2[o];
-    }
+// ------------------------------------------------------------------- stage C driver
+// Bottom-up reflections, top-down incidence pass and efficiencies, in precision RC.
+// bW, bV: (P, n, n) LU-factored bigW / bigV with pivots; X: FP64 (P, n).
+template <class RC>
+void stage_c(cudaStream_t s, Arena& ar, int Bc, int L, int N, Cx<RC>* bW, Cx<RC>* bV, const int* pivW,
+             const int* pivV, const cplx* X, const PortVectors& pv, const SolveDesc& d, int first,
+             const SolveOut& out, int32_t* st, Cx<RC>* Mk, int* pivM, Cx<RC>* Rk, Cx<RC>* S1, Cx<RC>* S2,
+             Cx<RC>* S3, int* pivS, Cx<RC>* Cin, Cx<RC>* g, Cx<RC>* h, Cx<RC>* r1, Cx<RC>* r2, Cx<RC>* cref) {
+  const int n = 2 * N;
+  const long long n2 = (long long)n * n;
+  const long long lay_bs = (long long)L * n2, lay_ps = (long long)L * n, r_bs = (long long)(L + 1) * n2;
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  diag_matrix_kernel<RC><<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, pv.t11, Rk + (long long)L * n2, r_bs);
+  note_launch();
+  const dim3 tgrid((n + 31) / 32, (n + 31) / 32, Bc), tblk(32, 8);
+  for (int l = L - 1; l >= 0; --l) {
+    Cx<RC>* bWl = bW + (long long)l * n2;  const int* pW = pivW + (long long)l * n;
+    Cx<RC>* bVl = bV + (long long)l * n2;  const int* pV = pivV + (long long)l * n;
+    Cx<RC>* M = Mk + (long long)l * n2;    int* pM = pivM + (long long)l * n;
+    const Cx<RC>* Rb = Rk + (long long)(l + 1) * n2;
+    u12_kernel<RC><<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, Rb, r_bs, pv.wg, pv.vg, S1, S2, n2); note_launch();
+    getrs<RC>(s, Bc, n, bWl, n, lay_bs, pW, lay_ps, S1, n, n, n2, 0);            // P1 = bigW^-1 U1
+    getrs<RC>(s, Bc, n, bVl, n, lay_bs, pV, lay_ps, S2, n, n, n2, 0);            // P2 = bigV^-1 U2
+    mn2_kernel<RC><<<tgrid, tblk, 0, s>>>(n, S1, S2, n2, M, lay_bs, S3); note_launch();   // M, N^T
+    getrf<RC>(s, Bc, n, M, n, lay_bs, pM, lay_ps, st, 1);
+    getrs<RC>(s, Bc, n, M, n, lay_bs, pM, lay_ps, S3, n, n, n2, 1);             // rho_b^T = M^-T N^T
+    rho_kernel<RC><<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, S3, S2, X + (long long)l * n, lay_ps, n2);
+    note_launch();
+    getrs<RC>(s, Bc, n, bWl, n, lay_bs, pW, lay_ps, S2, n, n, n2, 1);            // X1^T
+    getrs<RC>(s, Bc, n, bVl, n, lay_bs, pV, lay_ps, S3, n, n, n2, 1);            // X2^T
+    Cx<RC>* Rl = Rk + (long long)l * n2;
+    ab2_kernel<RC><<<tgrid, tblk, 0, s>>>(n, S2, S3, n2, pv.wg, pv.vg, S1, n2, Rl, r_bs); note_launch();
+    getrf<RC>(s, Bc, n, S1, n, n2, pivS, n, st, 1);
+    getrs<RC>(s, Bc, n, S1, n, n2, pivS, n, Rl, n, n, r_bs, 0);                 // R_l
   }
-  __syncthreads();
-  for (int e = threadIdx.y; e < 32; e += blockDim.y) {
-    int i = i0 + threadIdx.x, j = j0 + e;
-    if (i < n && j < n) {
-      cplx a1 = cmul(t1[threadIdx.x][e], wg[b * n + j]);
-      cplx a2 = cmul(t2[threadIdx.x][e], vg[b * n + j]);
-      long long o = i + (long long)j * n;
-      Aout[b * a_bs + o] = cadd(a1, a2);
-      Bout[b * b_bs + o] = csub(a2, a1);
-    }
+  const long long v3 = (long long)n * 3;
+  incident_kernel<RC><<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, N, d.pol + 2 * first, pv.nt, Cin, v3); note_launch();
+  top_kernel<RC><<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, Rk, r_bs, pv.r22, S1, n2); note_launch();
+  getrf<RC>(s, Bc, n, S1, n, n2, pivS, n, st, 1);
+  dscale3_kernel<RC><<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, pv.r21, Cin, v3, nullptr, nullptr, 0, g, v3);
+  note_launch();
+  getrs<RC>(s, Bc, n, S1, n, n2, pivS, n, g, 3, n, v3, 0);                      // g_0
+  gemm<RC>(s, Bc, n, 3, n, one, Rk, 1, n, r_bs, g, 1, n, v3, zero, h, 1, n, v3);
+  dscale3_kernel<RC><<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, pv.r11, Cin, v3, pv.r12, h, v3, cref, v3);
+  note_launch();
+  for (int l = 0; l < L; ++l) {
+    Cx<RC>* bWl = bW + (long long)l * n2;  const int* pW = pivW + (long long)l * n;
+    Cx<RC>* bVl = bV + (long long)l * n2;  const int* pV = pivV + (long long)l * n;
+    Cx<RC>* M = Mk + (long long)l * n2;    const int* pM = pivM + (long long)l * n;
+    if (l > 0) gemm<RC>(s, Bc, n, 3, n, one, Rk + (long long)l * n2, 1, n, r_bs, g, 1, n, v3, zero, h, 1, n, v3);
+    gh_kernel<RC><<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, g, h, pv.wg, pv.vg, r1, r2, v3); note_launch();
+    getrs<RC>(s, Bc, n, bWl, n, lay_bs, pW, lay_ps, r1, 3, n, v3, 0);
+    getrs<RC>(s, Bc, n, bVl, n, lay_bs, pV, lay_ps, r2, 3, n, v3, 0);
+    ct_kernel<RC><<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, r1, r2, X + (long long)l * n, lay_ps, g, v3);
+    note_launch();
+    getrs<RC>(s, Bc, n, M, n, lay_bs, pM, lay_ps, g, 3, n, v3, 0);              // g_{l+1}
   }
+  dscale3_kernel<RC><<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, pv.t21, g, v3, nullptr, nullptr, 0, h, v3);
+  note_launch();
+  efficiency_kernel<RC><<<nblk((long long)Bc * N * 3, 256), 256, 0, s>>>(
+      Bc, N, cref, h, v3, pv, d.eps_top + first, d.eps_bot + first, d.pol + 2 * first,
+      out.R + (long long)first * 3 * N, out.T + (long long)first * 3 * N,
+      out.amps ? out.amps + (long long)first * 12 * N : nullptr, st);
+  note_launch();
 }
 
 // ------------------------------------------------------------------------- orchestration
-// Workspace of one chunk of `chunk` solves with L layers of N orders (n = 2N):
-//   per (solve, layer) pair: OM (Omega2 -> T -> W -> bigW LU), Zb (Z -> V -> bigV LU),
-//   Xv (X eigvecs -> M_k LU), R_k; per solve: R_L, three n x n scratch matrices.
-size_t solve_chunk_bytes(int N, int L, int chunk) {
+// Workspace of one chunk of `chunk` solves with L layers of N orders (n = 2N). All matrices are
+// allocated at 16 bytes per complex entry (complex128 or complex df64); the FP32 cascade of the
+// mixed form takes its own 8-byte copies.
+size_t solve_chunk_bytes(int N, int L, int chunk, int precision) {
   const size_t n = 2 * (size_t)N, n2 = n * n, P = (size_t)chunk * L;
   size_t b = 0;
   auto A = [&](size_t x) { b += (x + 255) & ~(size_t)255; };
-  A(sizeof(double) * chunk * N); A(sizeof(double) * chunk * N); A(sizeof(double) * chunk * N);
-  A(sizeof(double) * chunk * N);
+  for (int k = 0; k < 4; ++k) A(sizeof(double) * chunk * N);
   A(sizeof(cplx) * chunk * N); A(sizeof(cplx) * chunk * N);
   for (int k = 0; k < 8; ++k) A(sizeof(cplx) * chunk * n);
   A(sizeof(cplx) * chunk); A(sizeof(cplx) * chunk);
   A(sizeof(int) * P); A(sizeof(int) * P); A(sizeof(double) * P);
-  A(sizeof(cplx) * P * n2); A(sizeof(cplx) * P * n2); A(sizeof(cplx) * P * n2);
-  for (int k = 0; k < 4; ++k) A(sizeof(cplx) * P * n);
+  A(16 * P * n2); A(16 * P * n2); A(16 * P * n2);                  // OM, Zb, Xv
+  for (int k = 0; k < 5; ++k) A(16 * P * n);                        // wr, tau, w, q, X
   A(sizeof(int) * P * n); A(sizeof(int) * P * n); A(sizeof(int) * P * n);
-  A(sizeof(cplx) * (P + chunk) * n2);
-  A(sizeof(cplx) * chunk * n2); A(sizeof(cplx) * chunk * n2); A(sizeof(cplx) * chunk * n2);
+  const size_t ec = (precision == 2) ? 8 : 16;                     // stage C element size
+  if (precision == 2) { A(ec * P * n2); A(ec * P * n2); A(ec * P * n2); }   // FP32 bigW, bigV, Mk
+  A(ec * (P + chunk) * n2);
+  A(ec * chunk * n2); A(ec * chunk * n2); A(ec * chunk * n2);
   A(sizeof(int) * chunk * n);
-  for (int k = 0; k < 6; ++k) A(sizeof(cplx) * chunk * n * 3);
+  for (int k = 0; k < 6; ++k) A(ec * chunk * n * 3);
   return b;
 }
 
-int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int count, const SolveOut& out) {
+// precision: 0 plain FP64; 1 mixed (df64 stage B and C); 2 mixed (df64 stage B, FP32 stage C)
+int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int count, const SolveOut& out,
+                int precision) {
   const int N = (2 * d.hu + 1) * (2 * d.hv + 1), n = 2 * N, L = d.n_layers;
-  const long long n2 = (long long)n * n, NN = (long long)N * N;
+  const long long n2 = (long long)n * n;
   const int Bc = count, P = Bc * L;
   int32_t* st = out.status + first;
   ar.reset();
@@ -597,103 +707,80 @@ int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int co
   int* pair_layer = ar.get<int>(P);
   int* pair_solve = ar.get<int>(P);
   double* pair_thick = ar.get<double>(P);
-  cplx* OM = ar.get<cplx>((size_t)P * n2);
-  cplx* Zb = ar.get<cplx>((size_t)P * n2);
-  cplx* Xv = ar.get<cplx>((size_t)P * n2);
+  char* OMr = ar.get<char>((size_t)16 * P * n2);
+  char* Zbr = ar.get<char>((size_t)16 * P * n2);
+  char* Xvr = ar.get<char>((size_t)16 * P * n2);
+  char* wr = ar.get<char>((size_t)16 * P * n);
+  char* taur = ar.get<char>((size_t)16 * P * n);
   cplx* w = ar.get<cplx>((size_t)P * n);
   cplx* q = ar.get<cplx>((size_t)P * n);
   cplx* X = ar.get<cplx>((size_t)P * n);
-  cplx* tau = ar.get<cplx>((size_t)P * n);
   int* pivW = ar.get<int>((size_t)P * n);
   int* pivV = ar.get<int>((size_t)P * n);
   int* pivM = ar.get<int>((size_t)P * n);
-  cplx* Rk = ar.get<cplx>((size_t)(P + Bc) * n2);
-  cplx* S1 = ar.get<cplx>((size_t)Bc * n2);
-  cplx* S2 = ar.get<cplx>((size_t)Bc * n2);
-  cplx* S3 = ar.get<cplx>((size_t)Bc * n2);
-  int* pivS = ar.get<int>((size_t)Bc * n);
-  cplx* Cin = ar.get<cplx>((size_t)Bc * n * 3);
-  cplx* g = ar.get<cplx>((size_t)Bc * n * 3);
-  cplx* h = ar.get<cplx>((size_t)Bc * n * 3);
-  cplx* r1 = ar.get<cplx>((size_t)Bc * n * 3);
-  cplx* r2 = ar.get<cplx>((size_t)Bc * n * 3);
-  cplx* cref = ar.get<cplx>((size_t)Bc * n * 3);
   if (!ar.ok()) return -1;
-
   ports_kernel<<<Bc, 128, 0, s>>>(Bc, d.hu, d.hv, d.wavelength + first, d.period + 2 * first, d.theta + first,
                                   d.phi + first, d.eps_top + first, d.eps_bot + first, pv); note_launch();
   pairs_kernel<<<nblk(P, 128), 128, 0, s>>>(Bc, L, d.layer_index + (long long)first * L,
-                                            d.thickness + (long long)first * L, pair_layer, pair_solve, pair_thick); note_launch();
-  // ---------------- stage B: modes of every (solve, layer) pair, p = b * L + l
-  const long long conv_ls = 3 * NN;
+                                            d.thickness + (long long)first * L, pair_layer, pair_solve, pair_thick);
+  note_launch();
+  const double* wl = d.wavelength + first;
+  if (precision == 0) {
+    using R = double;
+    Cx<R>* OM = (Cx<R>*)OMr; Cx<R>* Zb = (Cx<R>*)Zbr; Cx<R>* Xv = (Cx<R>*)Xvr;
+    stage_b<R>(s, P, N, d.conv, pair_layer, pair_solve, pair_thick, wl, pv.kx, pv.ky, OM, Zb, Xv, (Cx<R>*)wr,
+               (Cx<R>*)taur, w, q, X, pv.c, pv.s, st, L, true);
+    getrf<R>(s, P, n, OM, n, n2, pivW, n, st, L);
+    getrf<R>(s, P, n, Zb, n, n2, pivV, n, st, L);
+    Cx<R>* Rk = ar.get<Cx<R>>((size_t)(P + Bc) * n2);
+    Cx<R>* S1 = ar.get<Cx<R>>((size_t)Bc * n2); Cx<R>* S2 = ar.get<Cx<R>>((size_t)Bc * n2);
+    Cx<R>* S3 = ar.get<Cx<R>>((size_t)Bc * n2);
+    int* pivS = ar.get<int>((size_t)Bc * n);
+    Cx<R>* v[6];
+    for (int k = 0; k < 6; ++k) v[k] = ar.get<Cx<R>>((size_t)Bc * n * 3);
+    if (!ar.ok()) return -1;
+    stage_c<R>(s, ar, Bc, L, N, OM, Zb, pivW, pivV, X, pv, d, first, out, st, Xv, pivM, Rk, S1, S2, S3, pivS,
+               v[0], v[1], v[2], v[3], v[4], v[5]);
+    return 0;
+  }
+  // mixed: stage B in df64
   {
-    dim3 gr((N + 63) / 64, (N + 63) / 64, P * 4);
-    omega2_kernel<<<gr, 256, 0, s>>>(N, d.conv, conv_ls, pair_layer, pair_solve, pv.kx, pv.ky, OM, n2); note_launch();
+    using R = df64;
+    Cx<R>* OM = (Cx<R>*)OMr; Cx<R>* Zb = (Cx<R>*)Zbr; Cx<R>* Xv = (Cx<R>*)Xvr;
+    stage_b<R>(s, P, N, d.conv, pair_layer, pair_solve, pair_thick, wl, pv.kx, pv.ky, OM, Zb, Xv, (Cx<R>*)wr,
+               (Cx<R>*)taur, w, q, X, pv.c, pv.s, st, L, true);
+    if (precision == 1) {
+      getrf<R>(s, P, n, OM, n, n2, pivW, n, st, L);
+      getrf<R>(s, P, n, Zb, n, n2, pivV, n, st, L);
+      Cx<R>* Rk = ar.get<Cx<R>>((size_t)(P + Bc) * n2);
+      Cx<R>* S1 = ar.get<Cx<R>>((size_t)Bc * n2); Cx<R>* S2 = ar.get<Cx<R>>((size_t)Bc * n2);
+      Cx<R>* S3 = ar.get<Cx<R>>((size_t)Bc * n2);
+      int* pivS = ar.get<int>((size_t)Bc * n);
+      Cx<R>* v[6];
+      for (int k = 0; k < 6; ++k) v[k] = ar.get<Cx<R>>((size_t)Bc * n * 3);
+      if (!ar.ok()) return -1;
+      stage_c<R>(s, ar, Bc, L, N, OM, Zb, pivW, pivV, X, pv, d, first, out, st, Xv, pivM, Rk, S1, S2, S3, pivS,
+                 v[0], v[1], v[2], v[3], v[4], v[5]);
+      return 0;
+    }
+    using RC = float;
+    Cx<RC>* bW = ar.get<Cx<RC>>((size_t)P * n2);
+    Cx<RC>* bV = ar.get<Cx<RC>>((size_t)P * n2);
+    Cx<RC>* Mk = ar.get<Cx<RC>>((size_t)P * n2);
+    Cx<RC>* Rk = ar.get<Cx<RC>>((size_t)(P + Bc) * n2);
+    Cx<RC>* S1 = ar.get<Cx<RC>>((size_t)Bc * n2); Cx<RC>* S2 = ar.get<Cx<RC>>((size_t)Bc * n2);
+    Cx<RC>* S3 = ar.get<Cx<RC>>((size_t)Bc * n2);
+    int* pivS = ar.get<int>((size_t)Bc * n);
+    Cx<RC>* v[6];
+    for (int k = 0; k < 6; ++k) v[k] = ar.get<Cx<RC>>((size_t)Bc * n * 3);
+    if (!ar.ok()) return -1;
+    convert<R, RC>(s, OM, bW, (long long)P * n2);
+    convert<R, RC>(s, Zb, bV, (long long)P * n2);
+    getrf<RC>(s, P, n, bW, n, n2, pivW, n, st, L);
+    getrf<RC>(s, P, n, bV, n, n2, pivV, n, st, L);
+    stage_c<RC>(s, ar, Bc, L, N, bW, bV, pivW, pivV, X, pv, d, first, out, st, Mk, pivM, Rk, S1, S2, S3, pivS,
+                v[0], v[1], v[2], v[3], v[4], v[5]);
   }
-  zgeev_schur(s, P, n, OM, n, n2, Zb, n, n2, w, tau, st, L);
-  ztrevc(s, P, n, OM, n, n2, Xv, n, n2);
-  zgemm(s, P, n, n, n, cmk(1, 0), Zb, 1, n, n2, Xv, 1, n, n2, cmk(0, 0), OM, 1, n, n2);   // W = Z X
-  znormalize_columns(s, P, n, OM, n, n2);
-  modeq_kernel<<<P, 256, 0, s>>>(P, n, w, pair_solve, pair_thick, d.wavelength + first, q, X, st, L); note_launch();
-  {
-    dim3 gr((N + 63) / 64, (n + 63) / 64, P * 2);
-    vmodes_kernel<<<gr, 256, 0, s>>>(N, d.conv, conv_ls, pair_layer, pair_solve, pv.kx, pv.ky, OM, q, Zb, n2); note_launch();
-  }
-  sp_rotate_kernel<<<nblk((long long)P * N * n, 256), 256, 0, s>>>(P, N, pair_solve, pv.c, pv.s, OM, Zb, n2); note_launch();
-  zgetrf(s, P, n, OM, n, n2, pivW, n, st, L);     // LU(bigW)
-  zgetrf(s, P, n, Zb, n, n2, pivV, n, st, L);     // LU(bigV)
-
-  // ---------------- stage C: bottom-up reflections R_k (per solve L+1 matrices, R_L = diag(t11))
-  const long long lay_bs = (long long)L * n2;     // solve stride of per-pair matrices
-  const long long lay_ps = (long long)L * n;      // solve stride of per-pair vectors / pivots
-  const long long r_bs = (long long)(L + 1) * n2;
-  diag_matrix_kernel<<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, pv.t11, Rk + (long long)L * n2, r_bs); note_launch();
-  const dim3 tgrid((n + 31) / 32, (n + 31) / 32, Bc), tblk(32, 8);
-  for (int l = L - 1; l >= 0; --l) {
-    cplx* bW = OM + (long long)l * n2;  const int* pW = pivW + (long long)l * n;
-    cplx* bV = Zb + (long long)l * n2;  const int* pV = pivV + (long long)l * n;
-    cplx* M = Xv + (long long)l * n2;   int* pM = pivM + (long long)l * n;
-    const cplx* Rb = Rk + (long long)(l + 1) * n2;
-    u12_kernel<<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, Rb, r_bs, pv.wg, pv.vg, S1, S2, n2); note_launch();
-    zgetrs(s, Bc, n, bW, n, lay_bs, pW, lay_ps, S1, n, n, n2, 0);           // P1 = bigW^-1 U1
-    zgetrs(s, Bc, n, bV, n, lay_bs, pV, lay_ps, S2, n, n, n2, 0);           // P2 = bigV^-1 U2
-    mn2_kernel<<<tgrid, tblk, 0, s>>>(n, S1, S2, n2, M, lay_bs, S3); note_launch();        // M, N^T
-    zgetrf(s, Bc, n, M, n, lay_bs, pM, lay_ps, st, 1);
-    zgetrs(s, Bc, n, M, n, lay_bs, pM, lay_ps, S3, n, n, n2, 1);            // rho_b^T = M^-T N^T
-    rho_kernel<<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, S3, S2, X + (long long)l * n, lay_ps, n2); note_launch();
-    zgetrs(s, Bc, n, bW, n, lay_bs, pW, lay_ps, S2, n, n, n2, 1);           // X1^T
-    zgetrs(s, Bc, n, bV, n, lay_bs, pV, lay_ps, S3, n, n, n2, 1);           // X2^T
-    cplx* Rl = Rk + (long long)l * n2;
-    ab2_kernel<<<tgrid, tblk, 0, s>>>(n, S2, S3, n2, pv.wg, pv.vg, S1, n2, Rl, r_bs); note_launch();
-    zgetrf(s, Bc, n, S1, n, n2, pivS, n, st, 1);
-    zgetrs(s, Bc, n, S1, n, n2, pivS, n, Rl, n, n, r_bs, 0);               // R_l
-  }
-  // ---------------- top-down pass with the three incidence columns
-  const long long v3 = (long long)n * 3;
-  incident_kernel<<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, N, d.pol + 2 * first, pv.nt, Cin, v3); note_launch();
-  top_kernel<<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, Rk, r_bs, pv.r22, S1, n2); note_launch();
-  zgetrf(s, Bc, n, S1, n, n2, pivS, n, st, 1);
-  dscale3_kernel<<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, pv.r21, Cin, v3, nullptr, nullptr, 0, g, v3, 1.0); note_launch();
-  zgetrs(s, Bc, n, S1, n, n2, pivS, n, g, 3, n, v3, 0);                     // g_0
-  zgemm(s, Bc, n, 3, n, cmk(1, 0), Rk, 1, n, r_bs, g, 1, n, v3, cmk(0, 0), h, 1, n, v3);
-  dscale3_kernel<<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, pv.r11, Cin, v3, pv.r12, h, v3, cref, v3, 1.0); note_launch();
-  for (int l = 0; l < L; ++l) {
-    cplx* bW = OM + (long long)l * n2;  const int* pW = pivW + (long long)l * n;
-    cplx* bV = Zb + (long long)l * n2;  const int* pV = pivV + (long long)l * n;
-    cplx* M = Xv + (long long)l * n2;   const int* pM = pivM + (long long)l * n;
-    if (l > 0) zgemm(s, Bc, n, 3, n, cmk(1, 0), Rk + (long long)l * n2, 1, n, r_bs, g, 1, n, v3, cmk(0, 0), h, 1, n, v3);
-    gh_kernel<<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, g, h, pv.wg, pv.vg, r1, r2, v3); note_launch();
-    zgetrs(s, Bc, n, bW, n, lay_bs, pW, lay_ps, r1, 3, n, v3, 0);
-    zgetrs(s, Bc, n, bV, n, lay_bs, pV, lay_ps, r2, 3, n, v3, 0);
-    ct_kernel<<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, r1, r2, X + (long long)l * n, lay_ps, v3); note_launch();
-    zgetrs(s, Bc, n, M, n, lay_bs, pM, lay_ps, r1, 3, n, v3, 0);             // g_{l+1}
-    copy3_kernel<<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, r1, v3, g, v3); note_launch();
-  }
-  dscale3_kernel<<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, n, pv.t21, g, v3, nullptr, nullptr, 0, h, v3, 1.0); note_launch();
-  efficiency_kernel<<<nblk((long long)Bc * N * 3, 256), 256, 0, s>>>(
-      Bc, N, cref, h, v3, pv, d.eps_top + first, d.eps_bot + first, d.pol + 2 * first,
-      out.R + (long long)first * 3 * N, out.T + (long long)first * 3 * N,
-      out.amps ? out.amps + (long long)first * 12 * N : nullptr, st); note_launch();
   return 0;
 }
 
@@ -712,39 +799,41 @@ size_t layer_modes_bytes(int N, int n_pairs) {
   size_t b = 0;
   auto A = [&](size_t x) { b += (x + 255) & ~(size_t)255; };
   A(sizeof(int) * P); A(sizeof(double) * P); A(sizeof(double) * P);
-  A(sizeof(cplx) * P * n2); A(sizeof(cplx) * P * n2); A(sizeof(cplx) * P * n); A(sizeof(cplx) * P * n);
+  A(16 * P * n2); A(16 * P * n2); A(16 * P * n2); A(16 * P * n2);
+  for (int k = 0; k < 3; ++k) A(16 * P * n);
   return b;
 }
 
-void layer_modes(cudaStream_t s, Arena& ar, int P, int N, const cplx* conv, const int* pair_layer,
-                 const double* kx, const double* ky, cplx* w, cplx* q, cplx* W, cplx* V, int32_t* status) {
+template <class R>
+void layer_modes_t(cudaStream_t s, Arena& ar, int P, int N, const cplx* conv, const int* pair_layer,
+                   const double* kx, const double* ky, cplx* w, cplx* q, cplx* W, cplx* V, int32_t* status) {
   const int n = 2 * N;
-  const long long n2 = (long long)n * n, NN = (long long)N * N;
+  const long long n2 = (long long)n * n;
   ar.reset();
   int* pair_solve = ar.get<int>(P);
   double* zero = ar.get<double>(P);
   double* lam = ar.get<double>(P);
-  cplx* Zb = ar.get<cplx>((size_t)P * n2);
-  cplx* Xv = ar.get<cplx>((size_t)P * n2);
-  cplx* tau = ar.get<cplx>((size_t)P * n);
+  Cx<R>* OM = ar.get<Cx<R>>((size_t)P * n2);
+  Cx<R>* Zb = ar.get<Cx<R>>((size_t)P * n2);
+  Cx<R>* Xv = ar.get<Cx<R>>((size_t)P * n2);
+  Cx<R>* wr = ar.get<Cx<R>>((size_t)P * n);
+  Cx<R>* tau = ar.get<Cx<R>>((size_t)P * n);
   cplx* X = ar.get<cplx>((size_t)P * n);
   iota_kernel<<<nblk(P, 128), 128, 0, s>>>(P, pair_solve); note_launch();
   fill_kernel<<<nblk(P, 128), 128, 0, s>>>(P, 0.0, zero); note_launch();
   fill_kernel<<<nblk(P, 128), 128, 0, s>>>(P, 1.0, lam); note_launch();
   if (status) cudaMemsetAsync(status, 0, sizeof(int32_t) * P, s);
-  {
-    dim3 gr((N + 63) / 64, (N + 63) / 64, P * 4);
-    omega2_kernel<<<gr, 256, 0, s>>>(N, conv, 3 * NN, pair_layer, pair_solve, kx, ky, W, n2); note_launch();
-  }
-  zgeev_schur(s, P, n, W, n, n2, Zb, n, n2, w, tau, status, 1);
-  ztrevc(s, P, n, W, n, n2, Xv, n, n2);
-  zgemm(s, P, n, n, n, cmk(1, 0), Zb, 1, n, n2, Xv, 1, n, n2, cmk(0, 0), W, 1, n, n2);
-  znormalize_columns(s, P, n, W, n, n2);
-  modeq_kernel<<<P, 256, 0, s>>>(P, n, w, pair_solve, zero, lam, q, X, status, 1); note_launch();
-  {
-    dim3 gr((N + 63) / 64, (n + 63) / 64, P * 2);
-    vmodes_kernel<<<gr, 256, 0, s>>>(N, conv, 3 * NN, pair_layer, pair_solve, kx, ky, W, q, V, n2); note_launch();
-  }
+  stage_b<R>(s, P, N, conv, pair_layer, pair_solve, zero, lam, kx, ky, OM, Zb, Xv, wr, tau, w, q, X, nullptr, nullptr,
+             status, 1, false);
+  convert<R, double>(s, OM, (Cx<double>*)W, (long long)P * n2);
+  convert<R, double>(s, Zb, (Cx<double>*)V, (long long)P * n2);
+}
+
+void layer_modes(cudaStream_t s, Arena& ar, int P, int N, const cplx* conv, const int* pair_layer,
+                 const double* kx, const double* ky, cplx* w, cplx* q, cplx* W, cplx* V, int32_t* status,
+                 int precision) {
+  if (precision == 0) layer_modes_t<double>(s, ar, P, N, conv, pair_layer, kx, ky, w, q, W, V, status);
+  else layer_modes_t<df64>(s, ar, P, N, conv, pair_layer, kx, ky, w, q, W, V, status);
 }
 
 __global__ void regroup_kernel(int L, long long NN, const cplx* __restrict__ planes, cplx* __restrict__ out) {
