@@ -116,6 +116,21 @@ int wb_solve_host(wb_handle* h, int B, int L, int ny, int nx, int hu, int hv,
 /* Bytes of arena one chunk of `chunk` solves with L layers and N orders needs. */
 size_t wb_solve_workspace_bytes(int hu, int hv, int L, int chunk);
 
+/* Stage A without any allocation, for callers that may not allocate device memory (code running
+ * inside another component's CUDA-graph capture, servers and plugins whose host owns the device
+ * pool, allocation-free real-time paths). No counterpart in the reference. Same inputs and outputs
+ * as wb_assemble_li, no handle: scratch lives in a fixed 32 MiB device array of the library
+ * (wb_assemble_li_noalloc_limit() bytes), held by every GPU that loads it until exit. Layers are
+ * assembled one at a time, so the limit is per layer; a layer that needs more scratch is refused
+ * with WB_E_INVALID before any GPU work. The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current, so make it before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race and must be ordered by the caller.
+ * status: device int32 (1) or NULL, not cleared here. */
+int wb_assemble_li_noalloc(const wb_complex* eps, int L, int ny, int nx, int hu, int hv,
+                           wb_complex* epx, wb_complex* epy, wb_complex* epz_i, int32_t* status,
+                           void* stream);
+size_t wb_assemble_li_noalloc_limit(void);
+
 /* Number of kernels the library launched on this handle since creation (for accounting). */
 long long wb_kernel_launches(wb_handle* h);
 

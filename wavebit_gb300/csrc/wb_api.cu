@@ -65,6 +65,10 @@ int reserve(wb_handle* h, size_t bytes) {
 bool valid_orders(int hu, int hv) { return hu >= 0 && hv >= 0 && hu <= 64 && hv <= 64; }
 }  // namespace
 
+namespace wb {
+int noalloc_fail(const char* msg) { g_err = msg; return WB_E_INVALID; }
+}
+
 extern "C" {
 
 int wb_version(void) { return 100; }
