@@ -20,9 +20,6 @@
 namespace wb {
 
 constexpr int EIG_THREADS = 256;
-constexpr int QR_SEG = 32;             // bulge-chase steps per window
-constexpr int QR_WIN = QR_SEG + 3;     // window edge
-constexpr int QR_CH = 8;               // far-field register chunk
 
 __device__ __forceinline__ double shfl_xor(double v, int off) { return __shfl_xor_sync(0xffffffffu, v, off); }
 __device__ __forceinline__ float shfl_xor(float v, int off) { return __shfl_xor_sync(0xffffffffu, v, off); }
@@ -206,14 +203,38 @@ __global__ void __launch_bounds__(EIG_THREADS) unghr_kernel(Cx<R>* __restrict__ 
 
 // ---------------------------------------------------------- 3. Schur form by shifted QR
 // Francis single-shift implicit QR on the Hessenberg H (complex), full Schur form: T in H,
-// Schur vectors accumulated into Z. The subdiagonal is kept real so that each 2-element
+// Schur vectors accumulated into Z. The subdiagonal is kept real so that every 2-element
 // reflector has a real second coefficient. Deflation uses the standard small-subdiagonal test
-// with the Ahues-Tisseur refinement; shifts are Wilkinson shifts with exceptional shifts every
-// 10 stalled iterations. Each sweep is chased in windows of QR_SEG steps: warp 0 runs the
-// bulge through a shared-memory window around the diagonal and records the reflectors, then
-// every thread applies the window's reflectors, in order, to one far-field line (a column
-// right of the window, a row above it, or a row of Z) carrying the running element in a
-// register. Two CTA barriers per window instead of three per step, and no extra flops.
+// with the Ahues-Tisseur refinement; shifts are Wilkinson shifts with exceptional shifts after
+// 10 and 20 stalled iterations.
+//
+// One bulge step = lane 0 builds the 2x2 reflector, then the CTA applies it to rows (k, k+1),
+// to columns (k, k+1) and to Z. The step is latency bound (three barriers and a serial
+// reflector), so the kernel is sized to run several matrices per SM: their steps interleave
+// and keep the FP64 (or, for df64, FP32) pipes busy.
+//
+// Reflector of (alpha, x) with x real, as used by the chase: beta = -sign(Re alpha)|(alpha, x)|,
+// tau = (beta - alpha)/beta, v2 = x/(alpha - beta); one square root and two reciprocals.
+template <class R> struct Rot { Cx<R> t1, v2; R t2, beta; bool identity; };
+template <class R> __device__ __forceinline__ Rot<R> chase_reflector(Cx<R> alpha, R x) {
+  Rot<R> r;
+  if (x == R(0.0) && alpha.y == R(0.0)) {
+    r.identity = true; r.t1 = cxzero<R>(); r.v2 = cxzero<R>(); r.t2 = R(0.0); r.beta = alpha.x;
+    return r;
+  }
+  R nrm = rsqrt_(alpha.x * alpha.x + alpha.y * alpha.y + x * x);
+  R beta = (alpha.x >= R(0.0)) ? -nrm : nrm;
+  R ib = R(1.0) / beta;
+  Cx<R> d = cxmk<R>(alpha.x - beta, alpha.y);
+  R idd = R(1.0) / (d.x * d.x + d.y * d.y);
+  r.identity = false;
+  r.beta = beta;
+  r.t1 = cxmk<R>((beta - alpha.x) * ib, -(alpha.y * ib));
+  r.v2 = cxmk<R>(x * d.x * idd, -(x * d.y * idd));          // x / (alpha - beta)
+  r.t2 = -(x * ib);                                          // Re(t1 v2) = -x / beta
+  return r;
+}
+
 template <class R>
 __global__ void __launch_bounds__(EIG_THREADS) hseqr_kernel(Cx<R>* __restrict__ Hall, int n, int ldh,
                                                             long long h_bs, Cx<R>* __restrict__ Zall, int ldz,
@@ -223,11 +244,9 @@ __global__ void __launch_bounds__(EIG_THREADS) hseqr_kernel(Cx<R>* __restrict__ 
   extern __shared__ __align__(16) unsigned char smraw[];
   C_* sphase = reinterpret_cast<C_*>(smraw);
   __shared__ int ired[32];
-  __shared__ C_ swin[QR_WIN * QR_WIN];
-  __shared__ C_ srot_t1[QR_SEG], srot_v2[QR_SEG];
-  __shared__ R srot_t2[QR_SEG];
+  __shared__ C_ s_t1, s_v2, s_v0, s_sc;
+  __shared__ R s_t2, s_v1;
   __shared__ int s_done;
-  __shared__ C_ s_v0, s_v1;
   C_* H = Hall + blockIdx.x * h_bs;
   C_* Z = Zall + blockIdx.x * z_bs;
   C_* w = w_all + (long long)blockIdx.x * n;
@@ -281,8 +300,8 @@ __global__ void __launch_bounds__(EIG_THREADS) hseqr_kernel(Cx<R>* __restrict__ 
             C_ dd = h(k - 1, k - 1) - h(k, k);
             R aa = rmax(cxabs1(h(k, k)), cxabs1(dd));
             R bb = rmin(cxabs1(h(k, k)), cxabs1(dd));
-            R s = aa + ab;
-            if (ba * (ab / s) <= rmax(smlnum, ulp * (bb * (aa / s)))) small = true;
+            R sx = aa + ab;
+            if (ba * (ab / sx) <= rmax(smlnum, ulp * (bb * (aa / sx)))) small = true;
           }
         }
         if (small) cand = max(cand, k);
@@ -296,24 +315,23 @@ __global__ void __launch_bounds__(EIG_THREADS) hseqr_kernel(Cx<R>* __restrict__ 
       if (tid == 0) {
         C_ t;
         if (its % 20 == 10) {
-          R s = R(0.75) * rabs(h(l + 1, l).x);
-          t = cxmk<R>(s, R(0.0)) + h(l, l);
+          R sx = R(0.75) * rabs(h(l + 1, l).x);
+          t = cxmk<R>(sx, R(0.0)) + h(l, l);
         } else if (its % 20 == 0) {
-          R s = R(0.75) * rabs(h(i, i - 1).x);
-          t = cxmk<R>(s, R(0.0)) + h(i, i);
+          R sx = R(0.75) * rabs(h(i, i - 1).x);
+          t = cxmk<R>(sx, R(0.0)) + h(i, i);
         } else {
-          // Wilkinson: eigenvalue of the trailing 2x2 block closer to H(i,i)
           t = h(i, i);
           C_ u = cxsqrt(h(i - 1, i)) * cxsqrt(h(i, i - 1));
-          R s = cxabs1(u);
-          if (s != R(0.0)) {
+          R sx = cxabs1(u);
+          if (sx != R(0.0)) {
             C_ x = (h(i - 1, i - 1) - t) * R(0.5);
-            R sx = cxabs1(x);
-            s = rmax(s, cxabs1(x));
-            C_ xs = x * (R(1.0) / s), us = u * (R(1.0) / s);
-            C_ y = cxsqrt(xs * xs + us * us) * s;
-            if (sx > R(0.0)) {
-              C_ xn = x * (R(1.0) / sx);
+            R sxx = cxabs1(x);
+            sx = rmax(sx, cxabs1(x));
+            C_ xs = x * (R(1.0) / sx), us = u * (R(1.0) / sx);
+            C_ y = cxsqrt(xs * xs + us * us) * sx;
+            if (sxx > R(0.0)) {
+              C_ xn = x * (R(1.0) / sxx);
               if (xn.x * y.x + xn.y * y.y < R(0.0)) y = -y;
             }
             t = t - u * cxdiv(u, x + y);
@@ -322,96 +340,42 @@ __global__ void __launch_bounds__(EIG_THREADS) hseqr_kernel(Cx<R>* __restrict__ 
         C_ h11s = h(l, l) - t;
         R h21 = h(l + 1, l).x;
         R sc = cxabs1(h11s) + rabs(h21);
-        s_v0 = h11s * (R(1.0) / sc);
-        s_v1 = cxmk<R>(h21 / sc, R(0.0));
+        if (sc == R(0.0)) sc = R(1.0);
+        R isc = R(1.0) / sc;
+        s_v0 = h11s * isc;
+        s_v1 = h21 * isc;
       }
       __syncthreads();
-      const int m = l;
-      for (int k0 = m; k0 < i; k0 += QR_SEG) {
-        const int k1 = min(k0 + QR_SEG, i);
-        const int w0 = (k0 > m) ? k0 - 1 : k0;
-        const int w1 = min(k1 + 1, i);
-        const int nwin = w1 - w0 + 1;
-        for (int e = tid; e < nwin * nwin; e += blockDim.x) {
-          int r = e % nwin, c = e / nwin;
-          swin[r + c * QR_WIN] = h(w0 + r, w0 + c);
+      for (int k = l; k < i; ++k) {
+        if (tid == 0) {
+          C_ a0; R a1;
+          if (k > l) { a0 = h(k, k - 1); a1 = h(k + 1, k - 1).x; } else { a0 = s_v0; a1 = s_v1; }
+          Rot<R> rf = chase_reflector(a0, a1);
+          if (k > l) { h(k, k - 1) = rf.identity ? a0 : cxmk<R>(rf.beta, R(0.0)); h(k + 1, k - 1) = cxzero<R>(); }
+          s_t1 = rf.t1; s_v2 = rf.v2; s_t2 = rf.t2;
         }
         __syncthreads();
-        if (tid < 32) {
-          const int lane = tid;
-          auto W = [&](int r, int c) -> C_& { return swin[(r - w0) + (c - w0) * QR_WIN]; };
-          for (int k = k0; k < k1; ++k) {
-            if (lane == 0) {
-              C_ a0, a1;
-              if (k > m) { a0 = W(k, k - 1); a1 = W(k + 1, k - 1); } else { a0 = s_v0; a1 = s_v1; }
-              Refl<R> rf = make_reflector(a0, cxabs(a1));
-              C_ v2, t1;
-              if (rf.identity) { t1 = cxzero<R>(); v2 = cxzero<R>(); }
-              else { t1 = rf.tau; v2 = a1 * rf.scale; }
-              if (k > m) { W(k, k - 1) = rf.identity ? a0 : cxmk<R>(rf.beta, R(0.0)); W(k + 1, k - 1) = cxzero<R>(); }
-              srot_t1[k - k0] = t1; srot_v2[k - k0] = v2; srot_t2[k - k0] = (t1 * v2).x;
-            }
-            __syncwarp();
-            const C_ t1 = srot_t1[k - k0], v2 = srot_v2[k - k0];
-            const R t2 = srot_t2[k - k0];
-            const C_ t1c = cxconj(t1), v2c = cxconj(v2);
-            for (int j = k + lane; j <= w1; j += 32) {
-              C_ a = W(k, j), b = W(k + 1, j);
-              C_ sum = t1c * a + b * t2;
-              W(k, j) = a - sum;
-              W(k + 1, j) = b - sum * v2;
-            }
-            __syncwarp();
-            const int rlast = min(k + 2, i);
-            for (int r = w0 + lane; r <= rlast; r += 32) {
-              C_ a = W(r, k), b = W(r, k + 1);
-              C_ sum = t1 * a + b * t2;
-              W(r, k) = a - sum;
-              W(r, k + 1) = b - sum * v2c;
-            }
-            __syncwarp();
-          }
+        const C_ t1 = s_t1, v2 = s_v2;
+        const R t2 = s_t2;
+        const C_ t1c = cxconj(t1), v2c = cxconj(v2);
+        // left: rows k, k+1, columns k..n-1
+        for (int j = k + tid; j < n; j += blockDim.x) {
+          C_ a = h(k, j), b = h(k + 1, j);
+          C_ sum = t1c * a + b * t2;
+          h(k, j) = a - sum;
+          h(k + 1, j) = b - sum * v2;
         }
         __syncthreads();
-        for (int e = tid; e < nwin * nwin; e += blockDim.x) {
-          int r = e % nwin, c = e / nwin;
-          h(w0 + r, w0 + c) = swin[r + c * QR_WIN];
-        }
-        const int nleft = n - 1 - w1, nright = w0;
-        const int items = nleft + nright + n;
-        const int ns = k1 - k0;
-        for (int it = tid; it < items; it += blockDim.x) {
-          // the line's elements k0..k1 (stride `ld`), rotated in register chunks of QR_CH so
-          // that each chunk's loads are independent of the previous chunk's stores
-          C_* p; long long ld; bool left;
-          if (it < nleft) { p = H + (long long)(w1 + 1 + it) * ldh; ld = 1; left = true; }
-          else if (it < nleft + nright) { p = H + (it - nleft); ld = ldh; left = false; }
-          else { p = Z + (it - nleft - nright); ld = ldz; left = false; }
-          C_ a = p[(long long)k0 * ld];
-          for (int q0 = 0; q0 < ns; q0 += QR_CH) {
-            C_ buf[QR_CH];
-#pragma unroll
-            for (int u = 0; u < QR_CH; ++u)
-              if (q0 + u < ns) buf[u] = p[(long long)(k0 + q0 + u + 1) * ld];
-#pragma unroll
-            for (int u = 0; u < QR_CH; ++u) {
-              if (q0 + u < ns) {
-                const int q = q0 + u;
-                const C_ t1 = srot_t1[q], v2 = srot_v2[q];
-                const R t2 = srot_t2[q];
-                const C_ b = buf[u];
-                C_ sum, nb;
-                if (left) { sum = cxconj(t1) * a + b * t2; nb = b - sum * v2; }
-                else { sum = t1 * a + b * t2; nb = b - sum * cxconj(v2); }
-                buf[u] = a - sum;
-                a = nb;
-              }
-            }
-#pragma unroll
-            for (int u = 0; u < QR_CH; ++u)
-              if (q0 + u < ns) p[(long long)(k0 + q0 + u) * ld] = buf[u];
-          }
-          p[(long long)k1 * ld] = a;
+        // right: columns k, k+1, rows 0..min(k+2, i); and Z rows 0..n-1
+        const int rlast = min(k + 2, i);
+        for (int e = tid; e <= rlast + n; e += blockDim.x) {
+          C_* pa; C_* pb;
+          if (e <= rlast) { pa = &h(e, k); pb = &h(e, k + 1); }
+          else { int j = e - rlast - 1; pa = Z + j + (long long)k * ldz; pb = Z + j + (long long)(k + 1) * ldz; }
+          C_ a = *pa, b = *pb;
+          C_ sum = t1 * a + b * t2;
+          *pa = a - sum;
+          *pb = b - sum * v2c;
         }
         __syncthreads();
       }
@@ -422,13 +386,13 @@ __global__ void __launch_bounds__(EIG_THREADS) hseqr_kernel(Cx<R>* __restrict__ 
         if (sd.y != R(0.0)) {
           R a = cxabs(sd);
           h(i, i - 1) = cxmk<R>(a, R(0.0));
-          s_v0 = sd * (R(1.0) / a);
+          s_sc = sd * (R(1.0) / a);
           s_done = 1;
         }
       }
       __syncthreads();
       if (s_done) {
-        const C_ sc = s_v0;
+        const C_ sc = s_sc;
         for (int j = i + 1 + tid; j < n; j += blockDim.x) h(i, j) = cxconj(sc) * h(i, j);
         for (int j = tid; j < i; j += blockDim.x) h(j, i) = sc * h(j, i);
         for (int j = tid; j < n; j += blockDim.x) Z[j + (long long)i * ldz] = sc * Z[j + (long long)i * ldz];
