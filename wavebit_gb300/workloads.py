@@ -74,6 +74,20 @@ def mixed_sweep(seed=3, n_wavelengths=256, thetas=(0.0, 0.2, 0.4, 0.6)):
                 eps_top=1.0, eps_bot=2.25)
 
 
+def adjoint_layer(seed=4, side=128, n_wavelengths=32):
+    """One 220 nm layer, eps(x, y) = 1 + 11.25 sigmoid(8 g), g seeded N(0, 1) noise Gaussian-
+    filtered at sigma = 4 px (periodic) and normalised to unit variance; substrate 2.25; orders
+    (9, 9); wavelengths over 1000-1600 nm; normal incidence, p; objective sum of T(0,0)."""
+    from scipy.ndimage import gaussian_filter
+    rng = np.random.default_rng(seed)
+    g = gaussian_filter(rng.standard_normal((side, side)), sigma=4.0, mode='wrap')
+    g = (g - g.mean()) / g.std()
+    eps = 1.0 + 11.25 / (1.0 + np.exp(-8.0 * g))
+    return dict(name='adjoint_layer', eps=eps[None].astype(np.complex128), thickness=np.array([220.0]),
+                period=(1000., 1000.), orders=(9, 9), wavelengths=np.linspace(1000., 1600., n_wavelengths),
+                theta=0.0, phi=0.0, pol='p', eps_top=1.0, eps_bot=2.25)
+
+
 ORDER_CHOICES = ((5, 5), (8, 8), (11, 11), (15, 15))
 EPS_CHOICES = (1.0, 2.25, 12.25, -20 + 1.5j)
 
