@@ -61,6 +61,10 @@ int wb_last_error(char* buf, size_t len);
 int wb_create(int device, size_t hbm_budget, wb_handle** out);
 int wb_destroy(wb_handle* h);
 
+/* Grow the handle's scratch arena to at least `bytes` now (within its budget), so that no
+ * later call on the handle allocates. Serving loops call it once per worker at start-up. */
+int wb_reserve(wb_handle* h, size_t bytes);
+
 /* Bit-exact harmonic tables: labels_u[2hu+1] = -hu..hu, labels_v likewise; toeplitz_u
  * [(2hu+1)^2] = r - c + 2hu row-major, toeplitz_v likewise. Host memory, no handle needed.
  * Reference: rcwa/_engine/engine.py:953-993 (_separable_kxy order labels),

@@ -24,6 +24,7 @@ SIGNATURES = {
     'wb_last_error': (_i, [_c.c_char_p, _sz]),
     'wb_create': (_i, [_i, _sz, _c.POINTER(_vp)]),
     'wb_destroy': (_i, [_vp]),
+    'wb_reserve': (_i, [_vp, _sz]),
     'wb_build_indices': (_i, [_i, _i, _vp, _vp, _vp, _vp]),
     'wb_assemble_li': (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     'wb_layer_modes': (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),

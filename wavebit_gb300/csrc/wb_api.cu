@@ -105,6 +105,12 @@ int wb_destroy(wb_handle* h) {
   return WB_OK;
 }
 
+int wb_reserve(wb_handle* h, size_t bytes) {
+  if (!h) return fail(WB_E_INVALID, "wb_reserve: NULL handle");
+  cudaSetDevice(h->device);
+  return reserve(h, bytes);
+}
+
 int wb_build_indices(int hu, int hv, int32_t* labels_u, int32_t* labels_v, int32_t* toeplitz_u,
                      int32_t* toeplitz_v) {
   if (!valid_orders(hu, hv)) return fail(WB_E_INVALID, "orders (%d, %d) out of range", hu, hv);

@@ -1,0 +1,286 @@
+"""Continuous-batching request loop for RCWA solves on one GPU.
+
+Requests (a raster stack, orders, wavelength, angles, polarization) arrive over time. The loop
+keeps a pool of workers, each with its own CUDA stream and its own libwbgpu.so handle (so each
+has its own scratch arena, sized from the HBM budget). Whenever a worker is free it takes the
+oldest waiting request's bucket — requests with the same orders and layer count — packs up to
+the bucket's batch limit into one ``wb_solve_batch`` launch sequence and starts it; requests
+that arrive while others are on the GPU are admitted as soon as a worker and memory free up,
+and the workers' batches overlap on the device.
+
+* Admission: a bucket's batch limit is the largest batch whose workspace
+  (``wb_solve_workspace_bytes``) fits one worker's share of the budget; a request that cannot
+  fit even alone is refused with an error result (it never blocks the queue).
+* Resident convolution matrices: stage A runs once per distinct raster (keyed by its bytes and
+  the orders) and the result stays on the device in an LRU cache charged to the budget.
+* A request whose solve reports a non-zero status (singular, non-convergent, non-finite) gets an
+  error result; the other requests of its batch keep theirs.
+
+The solver is a small interface (``GpuBackend`` here; the CPU tests pass a fake one), so the
+scheduling logic is tested without a GPU. ``python -m wavebit_gb300.serving`` replays a seeded
+request stream with Poisson arrivals and prints throughput and p50/p99 latency.
+"""
+import argparse
+import collections
+import hashlib
+import json
+import math
+import time
+
+import numpy as np
+
+Result = collections.namedtuple('Result', 'id R T status error latency')
+
+
+class Request:
+    __slots__ = ('id', 'eps', 'thickness', 'orders', 'period', 'wavelength', 'theta', 'phi', 'pol',
+                 'eps_top', 'eps_bot', 'arrival', 'start', 'layer_keys')
+
+    def __init__(self, id, eps, thickness, orders, period, wavelength, theta, phi, pol, eps_top=1.0,
+                 eps_bot=1.0, arrival=0.0):
+        self.id = id
+        self.eps = np.ascontiguousarray(eps, dtype=np.complex128)      # (L, ny, nx), entry face first
+        self.thickness = np.asarray(thickness, dtype=np.float64)
+        self.orders = tuple(int(v) for v in orders)
+        self.period = tuple(float(v) for v in period)
+        self.wavelength = float(wavelength)
+        self.theta = float(theta)
+        self.phi = float(phi)
+        self.pol = pol
+        self.eps_top = complex(eps_top)
+        self.eps_bot = complex(eps_bot)
+        self.arrival = float(arrival)
+        self.start = None
+        self.layer_keys = None
+
+    @property
+    def bucket(self):
+        return (self.orders, self.eps.shape[0])
+
+    @classmethod
+    def from_workload(cls, r):
+        return cls(r['id'], r['eps'], r['thickness'], r['orders'], r['period'], r['wavelength'], r['theta'],
+                   r['phi'], r['pol'], r.get('eps_top', 1.0), r.get('eps_bot', 1.0), r.get('arrival', 0.0))
+
+
+def _pol_pair(pol):
+    if isinstance(pol, str):
+        return (1.0 + 0j, complex(math.cos(math.pi / 2))) if pol == 's' else (0j, 1.0 + 0j)
+    a, b = (complex(v) for v in pol)
+    nrm = math.sqrt(abs(a) ** 2 + abs(b) ** 2)
+    return a / nrm, b / nrm
+
+
+class GpuBackend:
+    """libwbgpu.so behind the serving loop: one handle and one CUDA stream per worker."""
+
+    def __init__(self, n_workers, hbm_budget, precision='double', device=0):
+        import torch
+        from . import _lib, engine
+        self.torch, self.lib, self.engine = torch, _lib, engine
+        self.device = torch.device('cuda', device)
+        torch.cuda.set_device(self.device)
+        self.precision = precision
+        self.per_worker = int(hbm_budget // (n_workers + 1))          # one share for the conv cache
+        self.cache_budget = int(hbm_budget - n_workers * self.per_worker)
+        self.handles = [_lib.Handle(device, self.per_worker) for _ in range(n_workers)]
+        for h in self.handles:                       # grow every arena now, never inside the loop
+            _lib.check(h.lib.wb_reserve(h.h, self.per_worker))
+        self.streams = [torch.cuda.Stream(device=self.device) for _ in range(n_workers)]
+        self.cache = collections.OrderedDict()      # key -> ((3, N, N) tensor, ready event)
+        self.cache_bytes = 0
+        self.launches0 = sum(h.launches() for h in self.handles)
+
+    # ---- admission
+    def max_batch(self, orders, L, limit):
+        hu, hv = orders
+        b = limit
+        while b >= 1:
+            if int(self.lib.load().wb_solve_workspace_bytes(hu, hv, L, b)) <= self.per_worker:
+                return b
+            b //= 2
+        return 0
+
+    # ---- resident convolution matrices
+    def conv_for(self, req, worker):
+        torch = self.torch
+        hu, hv = req.orders
+        keys = []
+        for l in range(req.eps.shape[0]):
+            raster = req.eps[l]
+            key = (hashlib.blake2b(raster.tobytes(), digest_size=16).hexdigest(), raster.shape, hu, hv)
+            keys.append(key)
+            if key in self.cache:
+                self.cache.move_to_end(key)
+                continue
+            with torch.cuda.stream(self.streams[worker]):
+                cs = self.engine.assemble(torch.as_tensor(raster[None], device=self.device), hu, hv,
+                                          handle=self.handles[worker])
+                ev = torch.cuda.Event()
+                ev.record(self.streams[worker])
+            t = cs.buf[0]
+            self.cache[key] = (t, ev)
+            self.cache_bytes += t.numel() * 16
+            while self.cache_bytes > self.cache_budget and len(self.cache) > 1:
+                _, (old, _) = self.cache.popitem(last=False)
+                self.cache_bytes -= old.numel() * 16
+        return keys
+
+    # ---- one batch
+    def launch(self, worker, reqs):
+        torch, engine = self.torch, self.engine
+        hu, hv = reqs[0].orders
+        L = reqs[0].eps.shape[0]
+        N = engine.n_orders(hu, hv)
+        stream = self.streams[worker]
+        keys_all = [self.conv_for(r, worker) for r in reqs]
+        uniq = list(dict.fromkeys(k for ks in keys_all for k in ks))
+        index = {k: i for i, k in enumerate(uniq)}
+        with torch.cuda.stream(stream):
+            for k in uniq:                      # matrices assembled on another worker's stream
+                t, ev = self.cache[k]
+                stream.wait_event(ev)
+                t.record_stream(stream)
+            conv = engine.ConvStack(torch.stack([self.cache[k][0] for k in uniq]), hu, hv)
+            li = [[index[k] for k in ks] for ks in keys_all]
+            inp = engine.BatchInputs(li, [r.thickness for r in reqs], [r.wavelength for r in reqs],
+                                     [r.period for r in reqs], [r.theta for r in reqs], [r.phi for r in reqs],
+                                     [r.eps_top for r in reqs], [r.eps_bot for r in reqs],
+                                     [_pol_pair(r.pol) for r in reqs], device=self.device)
+            R, T, st = engine.solve_batch(conv, inp, precision=self.precision, handle=self.handles[worker])
+            Rh = torch.empty(R.shape, dtype=R.dtype, pin_memory=True)
+            Th = torch.empty(T.shape, dtype=T.dtype, pin_memory=True)
+            sh = torch.empty(st.shape, dtype=st.dtype, pin_memory=True)
+            Rh.copy_(R, non_blocking=True); Th.copy_(T, non_blocking=True); sh.copy_(st, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+        return dict(event=ev, R=Rh, T=Th, status=sh, keep=(conv, inp, R, T, st))
+
+    def done(self, token):
+        return token['event'].query()
+
+    def results(self, token):
+        return token['R'].numpy()[:, 0], token['T'].numpy()[:, 0], token['status'].numpy()
+
+    def launches(self):
+        return sum(h.launches() for h in self.handles) - self.launches0
+
+
+class Server:
+    """The continuous-batching loop over a backend (see the module docstring)."""
+
+    def __init__(self, backend, n_workers=4, max_batch=64, clock=time.perf_counter, idle_sleep=2e-4):
+        self.backend = backend
+        self.n_workers = n_workers
+        self.max_batch_cap = max_batch
+        self.clock = clock
+        self.idle_sleep = idle_sleep
+        self.limits = {}
+
+    def _limit(self, bucket):
+        if bucket not in self.limits:
+            self.limits[bucket] = self.backend.max_batch(bucket[0], bucket[1], self.max_batch_cap)
+        return self.limits[bucket]
+
+    def run(self, requests, realtime=True):
+        """Replay ``requests`` (sorted by arrival, seconds from t=0). Returns (results, stats)."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        waiting = collections.OrderedDict()          # bucket -> deque of requests (FIFO)
+        inflight = [None] * self.n_workers           # (token, reqs)
+        results = {}
+        nxt = 0
+        t0 = self.clock()
+        busy_batches = 0
+
+        def now():
+            return self.clock() - t0
+
+        while len(results) < len(reqs):
+            t = now()
+            while nxt < len(reqs) and (not realtime or reqs[nxt].arrival <= t):
+                r = reqs[nxt]
+                nxt += 1
+                b = r.bucket
+                if self._limit(b) < 1:
+                    results[r.id] = Result(r.id, None, None, -1,
+                                           'refused: the request does not fit the HBM budget', 0.0)
+                    continue
+                waiting.setdefault(b, collections.deque()).append(r)
+            progressed = False
+            for w in range(self.n_workers):
+                if inflight[w] is not None and self.backend.done(inflight[w][0]):
+                    token, batch = inflight[w]
+                    Rr, Tr, st = self.backend.results(token)
+                    tdone = now()
+                    for i, r in enumerate(batch):
+                        err = None if (int(st[i]) & ~8) == 0 else f'solve status {int(st[i])}'
+                        lat = tdone - (r.arrival if realtime else 0.0)
+                        results[r.id] = Result(r.id, None if err else Rr[i], None if err else Tr[i],
+                                               int(st[i]), err, lat)
+                    inflight[w] = None
+                    progressed = True
+                if inflight[w] is None and waiting:
+                    # the bucket holding the oldest waiting request
+                    b = min(waiting, key=lambda k: waiting[k][0].arrival)
+                    q = waiting[b]
+                    take = [q.popleft() for _ in range(min(self._limit(b), len(q)))]
+                    if not q:
+                        del waiting[b]
+                    for r in take:
+                        r.start = now()
+                    inflight[w] = (self.backend.launch(w, take), take)
+                    busy_batches += 1
+                    progressed = True
+            if not progressed:
+                if realtime and nxt < len(reqs) and not waiting and all(f is None for f in inflight):
+                    gap = reqs[nxt].arrival - now()
+                    if gap > 0:
+                        time.sleep(min(gap, 0.01))
+                else:
+                    time.sleep(self.idle_sleep)
+        wall = now()
+        lat = np.array([r.latency for r in results.values() if r.error is None])
+        ok = len(lat)
+        stats = {'requests': len(reqs), 'completed': ok, 'errors': len(reqs) - ok, 'wall_s': wall,
+                 'throughput_rps': ok / wall if wall > 0 else 0.0, 'batches': busy_batches,
+                 'p50_latency_s': float(np.percentile(lat, 50)) if ok else None,
+                 'p99_latency_s': float(np.percentile(lat, 99)) if ok else None}
+        return results, stats
+
+
+def _stream(n, rate, seed, orders=None, max_layers=6, sides=(64, 128, 256)):
+    from . import workloads as WL
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=n))
+    out = []
+    for i in range(n):
+        r = WL.serving_request(rng, i, tuple(orders) if orders else WL.ORDER_CHOICES, tuple(sides), max_layers)
+        r['arrival'] = float(t[i])
+        out.append(Request.from_workload(r))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument('--requests', type=int, default=256)
+    ap.add_argument('--rate', type=float, default=20.0, help='Poisson arrival rate, requests/s')
+    ap.add_argument('--precision', default='double', choices=['double', 'mixed', 'mixed_fp32'])
+    ap.add_argument('--workers', type=int, default=4)
+    ap.add_argument('--max-batch', type=int, default=64)
+    ap.add_argument('--budget-gb', type=float, default=120.0)
+    ap.add_argument('--orders', default='5,8,11,15', help='half-orders drawn from (comma list)')
+    ap.add_argument('--max-layers', type=int, default=6)
+    ap.add_argument('--seed', type=int, default=5)
+    args = ap.parse_args()
+    orders = [(int(v), int(v)) for v in args.orders.split(',')]
+    reqs = _stream(args.requests, args.rate, args.seed, orders, args.max_layers)
+    backend = GpuBackend(args.workers, int(args.budget_gb * 2 ** 30), args.precision)
+    server = Server(backend, args.workers, args.max_batch)
+    _, stats = server.run(reqs)
+    stats.update(precision=args.precision, rate=args.rate, workers=args.workers, orders=args.orders,
+                 max_layers=args.max_layers, gpu_launches=backend.launches())
+    print(json.dumps(stats))
+
+
+if __name__ == '__main__':
+    main()

@@ -92,10 +92,10 @@ ORDER_CHOICES = ((5, 5), (8, 8), (11, 11), (15, 15))
 EPS_CHOICES = (1.0, 2.25, 12.25, -20 + 1.5j)
 
 
-def serving_request(rng, idx):
-    orders = ORDER_CHOICES[int(rng.integers(0, len(ORDER_CHOICES)))]
-    L = int(rng.integers(1, 7))
-    side = int((64, 128, 256)[int(rng.integers(0, 3))])
+def serving_request(rng, idx, orders_choices=ORDER_CHOICES, sides=(64, 128, 256), max_layers=6):
+    orders = orders_choices[int(rng.integers(0, len(orders_choices)))]
+    L = int(rng.integers(1, max_layers + 1))
+    side = int(sides[int(rng.integers(0, len(sides)))])
     layers = []
     for _ in range(L):
         hi = EPS_CHOICES[int(rng.integers(0, len(EPS_CHOICES)))]
