@@ -164,3 +164,22 @@ def test_layer_modes_double_float_eigenpairs():
     wn, Wn = w[0].cpu().numpy(), W[0].cpu().numpy()
     res = np.linalg.norm(om2 @ Wn - Wn * wn[None, :]) / (np.linalg.norm(om2) * np.linalg.norm(Wn))
     assert res < 1e-12, res
+
+
+def test_double_float_form_survives_the_fp32_exponent_range():
+    """Requests that once overflowed or underflowed the double-float (FP32-exponent) form: nearly
+    converged bulges of ~1e-25, metal layers, near-degenerate modes. The mixed result must be
+    finite and equal to the FP64 one to 1e-9."""
+    E = _engine()
+    from wavebit_gb300.serving import _stream, _pol_pair
+    reqs = _stream(128, 4.0, 5, [(5, 5), (8, 8)], 4)
+    for r in (reqs[56], reqs[60], reqs[62], reqs[69]):
+        conv = E.assemble(torch.as_tensor(r.eps, device='cuda'), *r.orders)
+        L = r.eps.shape[0]
+        inp = E.BatchInputs([list(range(L))], [r.thickness], [r.wavelength], [r.period], [r.theta], [r.phi],
+                            [r.eps_top], [r.eps_bot], [_pol_pair(r.pol)])
+        Rd, Td, sd = E.solve_batch(conv, inp, precision='double')
+        Rm, Tm, sm = E.solve_batch(conv, inp, precision='mixed')
+        torch.cuda.synchronize()
+        assert int(sd.item()) & ~8 == 0 and int(sm.item()) & ~8 == 0, (r.id, int(sm.item()))
+        assert float((Rd - Rm).abs().max()) <= 1e-9 and float((Td - Tm).abs().max()) <= 1e-9, r.id

@@ -107,7 +107,8 @@ def test_each_result_is_the_same_alone_and_in_the_mix():
     assert st['completed'] == 24
     for r in reqs[:8]:
         alone, _ = Server(GpuBackend(1, 4 << 30), n_workers=1, max_batch=1).run(
-            [Request(r.id, r.eps, r.thickness, r.orders, r.period, r.wavelength, r.theta, r.phi, r.pol)],
+            [Request(r.id, r.eps, r.thickness, r.orders, r.period, r.wavelength, r.theta, r.phi, r.pol,
+                     r.eps_top, r.eps_bot)],
             realtime=False)
         a, m = alone[r.id], mixed[r.id]
         scale = max(np.abs(a.R).max(), np.abs(a.T).max())

@@ -218,20 +218,25 @@ __global__ void __launch_bounds__(EIG_THREADS) unghr_kernel(Cx<R>* __restrict__ 
 template <class R> struct Rot { Cx<R> t1, v2; R t2, beta; bool identity; };
 template <class R> __device__ __forceinline__ Rot<R> chase_reflector(Cx<R> alpha, R x) {
   Rot<R> r;
-  if (x == R(0.0) && alpha.y == R(0.0)) {
+  // scaled by m = max(|Re a|, |Im a|, |x|) so that squares stay in range (the double-float form
+  // has FP32's exponent range, where a nearly converged bulge of 1e-25 would square to zero)
+  const R m = rmax(rmax(rabs(alpha.x), rabs(alpha.y)), rabs(x));
+  if ((x == R(0.0) && alpha.y == R(0.0)) || !(m > RealT<R>::tiny())) {
     r.identity = true; r.t1 = cxzero<R>(); r.v2 = cxzero<R>(); r.t2 = R(0.0); r.beta = alpha.x;
     return r;
   }
-  R nrm = rsqrt_(alpha.x * alpha.x + alpha.y * alpha.y + x * x);
-  R beta = (alpha.x >= R(0.0)) ? -nrm : nrm;
-  R ib = R(1.0) / beta;
-  Cx<R> d = cxmk<R>(alpha.x - beta, alpha.y);
+  const R im = R(1.0) / m;
+  const R ax = alpha.x * im, ay = alpha.y * im, xs = x * im;
+  R nrm = rsqrt_(ax * ax + ay * ay + xs * xs);
+  R bs = (ax >= R(0.0)) ? -nrm : nrm;                         // beta / m
+  R ib = R(1.0) / bs;
+  Cx<R> d = cxmk<R>(ax - bs, ay);                              // (alpha - beta) / m
   R idd = R(1.0) / (d.x * d.x + d.y * d.y);
   r.identity = false;
-  r.beta = beta;
-  r.t1 = cxmk<R>((beta - alpha.x) * ib, -(alpha.y * ib));
-  r.v2 = cxmk<R>(x * d.x * idd, -(x * d.y * idd));          // x / (alpha - beta)
-  r.t2 = -(x * ib);                                          // Re(t1 v2) = -x / beta
+  r.beta = bs * m;
+  r.t1 = cxmk<R>((bs - ax) * ib, -(ay * ib));
+  r.v2 = cxmk<R>(xs * d.x * idd, -(xs * d.y * idd));            // x / (alpha - beta)
+  r.t2 = -(xs * ib);                                           // Re(t1 v2) = -x / beta
   return r;
 }
 
@@ -262,7 +267,8 @@ __global__ void __launch_bounds__(EIG_THREADS) hseqr_kernel(Cx<R>* __restrict__ 
     for (int r = 1; r < n; ++r) {
       C_ sd = h(r, r - 1);
       R a = cxabs(sd);
-      if (a > R(0.0) && sd.y != R(0.0)) d = d * (sd * (R(1.0) / a));
+      // a subdiagonal below the safe range keeps a unit phase (its imaginary part is dropped)
+      if (a > RealT<R>::tiny() && sd.y != R(0.0)) d = d * (sd * (R(1.0) / a));
       sphase[r] = d;
     }
   }
@@ -385,9 +391,13 @@ __global__ void __launch_bounds__(EIG_THREADS) hseqr_kernel(Cx<R>* __restrict__ 
         s_done = 0;
         if (sd.y != R(0.0)) {
           R a = cxabs(sd);
-          h(i, i - 1) = cxmk<R>(a, R(0.0));
-          s_sc = sd * (R(1.0) / a);
-          s_done = 1;
+          if (a > RealT<R>::tiny()) {
+            h(i, i - 1) = cxmk<R>(a, R(0.0));
+            s_sc = sd * (R(1.0) / a);
+            s_done = 1;
+          } else {
+            h(i, i - 1) = cxmk<R>(sd.x, R(0.0));      // below the safe range: negligible
+          }
         }
       }
       __syncthreads();
@@ -436,6 +446,11 @@ __global__ void __launch_bounds__(256) trevc_kernel(const Cx<R>* __restrict__ Ta
     x[r] = v;
   }
   __syncwarp();
+  // back-substitution with rescaling: whenever a component exceeds `big`, the whole column (the
+  // solved part and the remaining right-hand side) is scaled down, since an eigenvector is only
+  // defined up to scale. This keeps the double-float form (FP32 exponent range) finite where
+  // nearly equal eigenvalues make the triangular solve grow.
+  const R big = RealT<R>::big();
   for (int j = k - 1; j >= 0; --j) {
     C_ xj = cxzero<R>();
     if (lane == (j & 31)) {
@@ -446,6 +461,14 @@ __global__ void __launch_bounds__(256) trevc_kernel(const Cx<R>* __restrict__ Ta
     }
     xj.x = shfl_idx(xj.x, j & 31);
     xj.y = shfl_idx(xj.y, j & 31);
+    R mag = cxabs1(xj);
+    if (mag > big) {
+      const R sc = R(1.0) / mag;
+      __syncwarp();
+      for (int r = lane; r <= k; r += 32) x[r] = x[r] * sc;
+      xj = xj * sc;
+      __syncwarp();
+    }
     const C_* tc = T + (long long)j * ldt;
     for (int r = lane; r < j; r += 32) x[r] = x[r] - xj * tc[r];
     __syncwarp();

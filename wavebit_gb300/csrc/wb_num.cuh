@@ -87,15 +87,18 @@ template <class R> struct RealT;
 template <> struct RealT<double> {
   WB_NHD static constexpr double eps() { return 2.220446049250313e-16; }
   WB_NHD static constexpr double tiny() { return 2.2250738585072014e-308; }
+  WB_NHD static constexpr double big() { return 1e100; }     // rescaling bound, far below overflow
 };
 template <> struct RealT<float> {
   WB_NHD static constexpr float eps() { return 1.1920928955078125e-07f; }
   WB_NHD static constexpr float tiny() { return 1.1754943508222875e-38f; }
+  WB_NHD static constexpr float big() { return 1e18f; }
 };
 template <> struct RealT<df64> {
   // unit roundoff of the double-word format ~ 2^-47; smallest safe value keeps hi normal
   static WB_ND df64 eps() { return df64(7.105427357601002e-15f, 0.f); }
   static WB_ND df64 tiny() { return df64(1.1754943508222875e-38f * 1024.f, 0.f); }
+  static WB_ND df64 big() { return df64(1e18f, 0.f); }
 };
 
 WB_NHD double rabs(double a) { return fabs(a); }
@@ -162,7 +165,7 @@ template <class R> WB_ND R cxabs2(Cx<R> a) { return a.x * a.x + a.y * a.y; }
 template <class R> WB_ND R cxabs(Cx<R> a) {
   R ax = rabs(a.x), ay = rabs(a.y);
   R m = rmax(ax, ay);
-  if (m == R(0.0)) return R(0.0);
+  if (!(m > RealT<R>::tiny())) return m;     // zero or below the safe range: |a| ~ max part
   R s = R(1.0) / m;
   R u = ax * s, v = ay * s;
   return m * rsqrt_(u * u + v * v);
@@ -180,6 +183,7 @@ template <class R> WB_ND Cx<R> cxsqrt(Cx<R> z) {
   R x = z.x, y = z.y;
   if (x == R(0.0) && y == R(0.0)) return cxmk<R>(R(0.0), y);
   R t = rsqrt_(R(0.5) * (rabs(x) + cxabs(z)));
+  if (!(t > R(0.0))) return cxmk<R>(R(0.0), R(0.0));       // below the representable range
   if (x >= R(0.0)) return cxmk<R>(t, y / (R(2.0) * t));
   R ay = rabs(y);
   return cxmk<R>(ay / (R(2.0) * t), y < R(0.0) ? -t : t);

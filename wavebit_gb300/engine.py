@@ -19,10 +19,14 @@ def _stream():
 
 
 def _c128(x, device):
+    if isinstance(x, (list, tuple)):
+        x = np.asarray(x, dtype=np.complex128)
     return torch.as_tensor(x, dtype=torch.complex128, device=device).contiguous()
 
 
 def _f64(x, device):
+    if isinstance(x, (list, tuple)):
+        x = np.asarray(x, dtype=np.float64)
     return torch.as_tensor(x, dtype=torch.float64, device=device).contiguous()
 
 

@@ -241,7 +241,9 @@ class Server:
         wall = now()
         lat = np.array([r.latency for r in results.values() if r.error is None])
         ok = len(lat)
-        stats = {'requests': len(reqs), 'completed': ok, 'errors': len(reqs) - ok, 'wall_s': wall,
+        errs = collections.Counter(r.status for r in results.values() if r.error is not None)
+        stats = {'requests': len(reqs), 'completed': ok, 'errors': len(reqs) - ok,
+                 'error_status_counts': {str(k): v for k, v in sorted(errs.items())}, 'wall_s': wall,
                  'throughput_rps': ok / wall if wall > 0 else 0.0, 'batches': busy_batches,
                  'p50_latency_s': float(np.percentile(lat, 50)) if ok else None,
                  'p99_latency_s': float(np.percentile(lat, 99)) if ok else None}
