@@ -149,6 +149,57 @@ def test_mixed_precision_within_tolerance(precision, tol):
     assert worst <= tol, worst
 
 
+@pytest.mark.parametrize('precision', ['double', 'mixed'])
+def test_layer_modes_every_pair_of_a_multi_wave_batch(precision):
+    """Pairs that start in later waves of CTAs (six pairs per SM) are eigenpairs like the first
+    wave's: a CTA whose warps read a value another thread had already overwritten (the
+    Householder alpha in the Hessenberg reduction) broke exactly those pairs."""
+    E = _engine()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    rng = np.random.default_rng(11)
+    eps = np.stack([_rast(rng, 24, 24) for _ in range(3)])
+    hu = hv = 4
+    conv = E.assemble(torch.as_tensor(eps, device='cuda'), hu, hv)
+    kx, ky = O.separable_kxy(910.0, (1000.0, 1000.0), O.incident_kxy(0.0, 0.0, 1.0), hu, hv)
+    kxg, kyg = O.order_grid(kx, ky)
+    P = 6 * sms
+    layer = [p % 3 for p in range(P)]
+    w, q, W, V, st = E.layer_modes(conv, layer, np.tile(kxg.real, (P, 1)), np.tile(kyg.real, (P, 1)),
+                                   precision=precision)
+    torch.cuda.synchronize()
+    assert not (st.cpu().numpy() & 6).any()
+    res = torch.zeros(P, dtype=torch.float64, device='cuda')
+    for l in range(3):
+        om2, _ = O.layer_operator(kxg, kyg, *(s[l].cpu().numpy() for s in (conv.epx, conv.epy, conv.epz_i)))
+        A = torch.as_tensor(om2, device='cuda')
+        idx = torch.arange(l, P, 3, device='cuda')
+        res[idx] = (A[None] @ W[idx] - W[idx] * w[idx][:, None, :]).abs().amax(dim=(1, 2)) / A.abs().max()
+    bad = torch.nonzero(res > 1e-11).flatten().cpu().numpy()
+    assert bad.size == 0, (bad[:10], float(res.max()))
+
+
+def test_solve_batch_is_invariant_to_batch_position():
+    """A batch of identical solves spanning several CTA waves returns the oracle's answer in every
+    slot, bit for bit the same."""
+    E = _engine()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    rng = np.random.default_rng(12)
+    eps = np.stack([_rast(rng, 24, 24), _rast(rng, 24, 24)])
+    hu = hv = 3
+    th = np.array([180.0, 260.0])
+    B = 3 * sms
+    conv = E.assemble(torch.as_tensor(eps, device='cuda'), hu, hv)
+    inp = E.BatchInputs([[0, 1]] * B, [th] * B, [905.0] * B, [[1000.0, 1000.0]] * B, [0.1] * B, [0.3] * B,
+                        [1.0] * B, [2.25] * B, [[1.0, 0.0]] * B)
+    R, T, st = E.solve_batch(conv, inp, precision='double')
+    torch.cuda.synchronize()
+    assert not (st.cpu().numpy() & ~8).any()
+    R, T = R.cpu().numpy(), T.cpu().numpy()
+    assert np.array_equal(R, np.broadcast_to(R[:1], R.shape)) and np.array_equal(T, np.broadcast_to(T[:1], T.shape))
+    o = O.solve_stack(eps, th, 905.0, (1000.0, 1000.0), hu, hv, 0.1, 0.3, 1.0, 2.25, (1.0, 0.0))
+    assert np.abs(R[0] - o['R']).max() <= 1e-10 and np.abs(T[0] - o['T']).max() <= 1e-10
+
+
 def test_layer_modes_double_float_eigenpairs():
     """The double-float eigen-solve returns FP64-class eigenpairs."""
     E = _engine()

@@ -127,11 +127,12 @@ __global__ void __launch_bounds__(EIG_THREADS) gehrd_kernel(Cx<R>* __restrict__ 
     }
     if (tid == 0) {
       sv[0] = cxone<R>();
-      col[k + 1] = cxmk<R>(r.beta, R(0.0));
       tau[k] = r.tau;
       s_tau = r.tau;
     }
     __syncthreads();
+    // every thread has read alpha = A(k+1, k) by now; column k is not touched again in this step
+    if (tid == 0) col[k + 1] = cxmk<R>(r.beta, R(0.0));
     const C_ t = s_tau;
     // right: y = A[:, k+1:n] v ; A[:, k+1:n] -= t y v^H  (all rows)
     for (int i = tid; i < n; i += blockDim.x) {
