@@ -43,8 +43,11 @@ extern "C" {
                               (rcwa/_engine/solve_2d.py:2463-2482); the result is flagged */
 
 #define WB_PRECISION_FP64 0        /* IEEE FP64 throughout */
-#define WB_PRECISION_MIXED 1       /* eigen-solve and cascade in double-float (2 x FP32) arithmetic */
-#define WB_PRECISION_MIXED_FP32 2  /* double-float eigen-solve, FP32 cascade */
+#define WB_PRECISION_MIXED 1       /* double-float (2 x FP32) eigen-solve; FP32 cascade whose
+                                      amplitudes are refined against the double-float interface
+                                      equations (FP64-class results) */
+#define WB_PRECISION_MIXED_FP32 2  /* double-float eigen-solve, unrefined FP32 cascade (~1e-5) */
+#define WB_PRECISION_MIXED_DF64 3  /* double-float eigen-solve and cascade */
 
 typedef struct { double re, im; } wb_complex;
 typedef struct wb_handle wb_handle;

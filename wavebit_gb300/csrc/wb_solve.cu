@@ -599,15 +599,16 @@ void stage_b(cudaStream_t s, int P, int N, const cplx* conv, const int* pair_lay
 // ------------------------------------------------------------------- stage C driver
 // Bottom-up reflections, top-down incidence pass and efficiencies, in precision RC.
 // bW, bV: (P, n, n) LU-factored bigW / bigV with pivots; X: FP64 (P, n).
+// Bottom-up half of the cascade: R_L = diag(t11), then R_l for l = L-1 .. 0, leaving in Mk the
+// LU factors of every layer's M and, when Ak is given, those of every layer's A (the matrix
+// whose solve yields R_l); otherwise A lives in S1 only for the duration of its layer.
 template <class RC>
-void stage_c(cudaStream_t s, Arena& ar, int Bc, int L, int N, Cx<RC>* bW, Cx<RC>* bV, const int* pivW,
-             const int* pivV, const cplx* X, const PortVectors& pv, const SolveDesc& d, int first,
-             const SolveOut& out, int32_t* st, Cx<RC>* Mk, int* pivM, Cx<RC>* Rk, Cx<RC>* S1, Cx<RC>* S2,
-             Cx<RC>* S3, int* pivS, Cx<RC>* Cin, Cx<RC>* g, Cx<RC>* h, Cx<RC>* r1, Cx<RC>* r2, Cx<RC>* cref) {
+void cascade_factor(cudaStream_t s, int Bc, int L, int N, Cx<RC>* bW, Cx<RC>* bV, const int* pivW, const int* pivV,
+                    const cplx* X, const PortVectors& pv, int32_t* st, Cx<RC>* Mk, int* pivM, Cx<RC>* Rk,
+                    Cx<RC>* S1, Cx<RC>* S2, Cx<RC>* S3, int* pivS, Cx<RC>* Ak, int* pivA) {
   const int n = 2 * N;
   const long long n2 = (long long)n * n;
   const long long lay_bs = (long long)L * n2, lay_ps = (long long)L * n, r_bs = (long long)(L + 1) * n2;
-  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
   diag_matrix_kernel<RC><<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, pv.t11, Rk + (long long)L * n2, r_bs);
   note_launch();
   const dim3 tgrid((n + 31) / 32, (n + 31) / 32, Bc), tblk(32, 8);
@@ -627,10 +628,25 @@ void stage_c(cudaStream_t s, Arena& ar, int Bc, int L, int N, Cx<RC>* bW, Cx<RC>
     getrs<RC>(s, Bc, n, bWl, n, lay_bs, pW, lay_ps, S2, n, n, n2, 1);            // X1^T
     getrs<RC>(s, Bc, n, bVl, n, lay_bs, pV, lay_ps, S3, n, n, n2, 1);            // X2^T
     Cx<RC>* Rl = Rk + (long long)l * n2;
-    ab2_kernel<RC><<<tgrid, tblk, 0, s>>>(n, S2, S3, n2, pv.wg, pv.vg, S1, n2, Rl, r_bs); note_launch();
-    getrf<RC>(s, Bc, n, S1, n, n2, pivS, n, st, 1);
-    getrs<RC>(s, Bc, n, S1, n, n2, pivS, n, Rl, n, n, r_bs, 0);                 // R_l
+    Cx<RC>* A = Ak ? Ak + (long long)l * n2 : S1;
+    int* pA = Ak ? pivA + (long long)l * n : pivS;
+    const long long a_bs = Ak ? lay_bs : n2, pa_bs = Ak ? lay_ps : n;
+    ab2_kernel<RC><<<tgrid, tblk, 0, s>>>(n, S2, S3, n2, pv.wg, pv.vg, A, a_bs, Rl, r_bs); note_launch();
+    getrf<RC>(s, Bc, n, A, n, a_bs, pA, pa_bs, st, 1);
+    getrs<RC>(s, Bc, n, A, n, a_bs, pA, pa_bs, Rl, n, n, r_bs, 0);              // R_l
   }
+}
+
+template <class RC>
+void stage_c(cudaStream_t s, Arena& ar, int Bc, int L, int N, Cx<RC>* bW, Cx<RC>* bV, const int* pivW,
+             const int* pivV, const cplx* X, const PortVectors& pv, const SolveDesc& d, int first,
+             const SolveOut& out, int32_t* st, Cx<RC>* Mk, int* pivM, Cx<RC>* Rk, Cx<RC>* S1, Cx<RC>* S2,
+             Cx<RC>* S3, int* pivS, Cx<RC>* Cin, Cx<RC>* g, Cx<RC>* h, Cx<RC>* r1, Cx<RC>* r2, Cx<RC>* cref) {
+  const int n = 2 * N;
+  const long long n2 = (long long)n * n;
+  const long long lay_bs = (long long)L * n2, lay_ps = (long long)L * n, r_bs = (long long)(L + 1) * n2;
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  cascade_factor<RC>(s, Bc, L, N, bW, bV, pivW, pivV, X, pv, st, Mk, pivM, Rk, S1, S2, S3, pivS, nullptr, nullptr);
   const long long v3 = (long long)n * 3;
   incident_kernel<RC><<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, N, d.pol + 2 * first, pv.nt, Cin, v3); note_launch();
   top_kernel<RC><<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, Rk, r_bs, pv.r22, S1, n2); note_launch();
@@ -662,7 +678,406 @@ void stage_c(cudaStream_t s, Arena& ar, int Bc, int L, int N, Cx<RC>* bW, Cx<RC>
   note_launch();
 }
 
+// --------------------------------------------------- cascade with FP64-class refinement
+// The mixed form factors the cascade in FP32 (cascade_factor<float>) and then solves the
+// interface equations of the whole stack by defect correction: the residual of the exact
+// equations is evaluated in double-float with the double-float modes of stage B, and the FP32
+// factors solve for the correction. Unknowns per solve and incidence column: the gap amplitudes
+// g_l (down) and h_l (up) above layer l (l = 0..L, L = the gap above the substrate) and the modal
+// amplitudes c+_l (down, at the top of layer l) and c-_l (up, at its bottom). Equations:
+//   top     g_0 - r21 C - r22 h_0                      = 0
+//   E1      W (c+ + X c-)  - wg (g_l + h_l)            = 0        (tangential E, top of layer l)
+//   E2      V (c+ - X c-)  - vg (g_l - h_l)            = 0        (tangential H, top)
+//   E3      W (X c+ + c-)  - wg (g_l+1 + h_l+1)        = 0        (tangential E, bottom)
+//   E4      V (X c+ - c-)  - vg (g_l+1 - h_l+1)        = 0        (tangential H, bottom)
+//   bottom  h_L - t11 g_L                              = 0
+// with c_ref = r11 C + r12 h_0 and c_trn = t21 g_L read off the solution (scattering.py:907-994
+// reads the same two blocks). Eliminating layer by layer from the bottom with right-hand sides
+// f1..f4 on E1..E4 gives h_l = R_l g_l + s_l with the cascade's R_l and
+//   a3 = W^-1 (wg s' + f3),  a4 = V^-1 (-vg s' + f4)
+//   sigma = ((a3 - a4) - rho_b (a3 + a4)) / 2,   rho_b = N M^-1
+//   s_l = A^-1 (2 X sigma - (W^-1 f1 - V^-1 f2) + X rho_b X (W^-1 f1 + V^-1 f2))
+// and from the top g_0 = G0^-1 (r22 s_0 + f_top), then per layer
+//   c+ = (W^-1 (wg (g + h) + f1) + V^-1 (vg (g - h) + f2)) / 2
+//   g' = M^-1 (2 X c+ - (a3 + a4)),   c- = rho_b X c+ + sigma.
+// Without sources this is the cascade's own top-down pass. N y = W^-1 wg (y + R' y) -
+// V^-1 vg (y - R' y) is applied from R' and the factors of W and V.
+//
+// Vector layouts: per-solve blocks of k columns of length n (column-major, batch stride given);
+// per (solve, layer) arrays (Bc, L, 3, n); gap arrays (Bc, L+1, 3, n).
+
+// WB = [wg s' + f3 | f1], VB = [-vg s' + f4 | f2]
+template <class R>
+__global__ void bu_rhs_kernel(int Bc, int n, const Cx<R>* __restrict__ sn, long long s_bs, const Cx<R>* __restrict__ f1,
+                              const Cx<R>* __restrict__ f2, const Cx<R>* __restrict__ f3, const Cx<R>* __restrict__ f4,
+                              long long f_bs, const cplx* __restrict__ wg, const cplx* __restrict__ vg,
+                              Cx<R>* __restrict__ WB, Cx<R>* __restrict__ VB) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)Bc * n * 3) return;
+  const long long b = idx / (3LL * n);
+  const int rem = (int)(idx % (3LL * n)), i = rem % n;
+  const Cx<R> sv = sn[b * s_bs + rem];
+  const long long o = b * 6LL * n;
+  WB[o + rem] = ld<R>(wg + b * n + i) * sv + f3[b * f_bs + rem];
+  WB[o + 3LL * n + rem] = f1[b * f_bs + rem];
+  VB[o + rem] = f4[b * f_bs + rem] - ld<R>(vg + b * n + i) * sv;
+  VB[o + 3LL * n + rem] = f2[b * f_bs + rem];
+}
+
+// from WB = [a3 | W^-1 f1], VB = [a4 | V^-1 f2]: Y = [a3 + a4 | X (W^-1 f1 + V^-1 f2)],
+// asum = a3 + a4, sig = a3 - a4 (completed later), D = W^-1 f1 - V^-1 f2
+template <class R>
+__global__ void bu_y_kernel(int Bc, int n, const Cx<R>* __restrict__ WB, const Cx<R>* __restrict__ VB,
+                            const cplx* __restrict__ X, long long x_bs, Cx<R>* __restrict__ Y,
+                            Cx<R>* __restrict__ asum, Cx<R>* __restrict__ sig, long long f_bs, Cx<R>* __restrict__ D) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)Bc * n * 3) return;
+  const long long b = idx / (3LL * n);
+  const int rem = (int)(idx % (3LL * n)), i = rem % n;
+  const long long o = b * 6LL * n;
+  const Cx<R> a3 = WB[o + rem], a4 = VB[o + rem];
+  const Cx<R> w1 = WB[o + 3LL * n + rem], v2 = VB[o + 3LL * n + rem];
+  const Cx<R> x = ld<R>(X + b * x_bs + i);
+  Y[o + rem] = a3 + a4;
+  Y[o + 3LL * n + rem] = x * (w1 + v2);
+  asum[b * f_bs + rem] = a3 + a4;
+  sig[b * f_bs + rem] = a3 - a4;
+  D[b * 3LL * n + rem] = w1 - v2;
+}
+
+// U1 = wg (Z + Rz), U2 = vg (Z - Rz), k columns, batch stride zs
+template <class R>
+__global__ void nz_kernel(int Bc, int n, int k, const Cx<R>* __restrict__ Z, long long zs, const Cx<R>* __restrict__ Rz,
+                          const cplx* __restrict__ wg, const cplx* __restrict__ vg, Cx<R>* __restrict__ U1,
+                          Cx<R>* __restrict__ U2) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)Bc * n * k) return;
+  const long long b = idx / ((long long)k * n);
+  const int rem = (int)(idx % ((long long)k * n)), i = rem % n;
+  const Cx<R> z = Z[b * zs + rem], r = Rz[b * (long long)k * n + rem];
+  U1[b * (long long)k * n + rem] = ld<R>(wg + b * n + i) * (z + r);
+  U2[b * (long long)k * n + rem] = ld<R>(vg + b * n + i) * (z - r);
+}
+
+// NZ = U1 - U2 = rho_b Y:  sigma = (sig - NZ[:, :3]) / 2 ;  rhs = 2 X sigma - D + X NZ[:, 3:]
+template <class R>
+__global__ void bu_src_kernel(int Bc, int n, const Cx<R>* __restrict__ U1, const Cx<R>* __restrict__ U2,
+                              const cplx* __restrict__ X, long long x_bs, Cx<R>* __restrict__ sig, long long f_bs,
+                              const Cx<R>* __restrict__ D, Cx<R>* __restrict__ rhs, long long r_bs) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)Bc * n * 3) return;
+  const long long b = idx / (3LL * n);
+  const int rem = (int)(idx % (3LL * n)), i = rem % n;
+  const long long o = b * 6LL * n;
+  const Cx<R> nz0 = U1[o + rem] - U2[o + rem];
+  const Cx<R> nz1 = U1[o + 3LL * n + rem] - U2[o + 3LL * n + rem];
+  const Cx<R> x = ld<R>(X + b * x_bs + i);
+  const Cx<R> sg = (sig[b * f_bs + rem] - nz0) * R(0.5);
+  sig[b * f_bs + rem] = sg;
+  rhs[b * r_bs + rem] = x * (sg * R(2.0)) - D[b * 3LL * n + rem] + x * nz1;
+}
+
+// out = d * a + c  (n x 3 per solve; d per-solve diagonal, FP64)
+template <class R>
+__global__ void diag_axpy3_kernel(int Bc, int n, const cplx* __restrict__ d, const Cx<R>* __restrict__ a, long long a_bs,
+                                  const Cx<R>* __restrict__ c, long long c_bs, Cx<R>* __restrict__ out, long long o_bs) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)Bc * n * 3) return;
+  const long long b = idx / (3LL * n);
+  const int rem = (int)(idx % (3LL * n)), i = rem % n;
+  out[b * o_bs + rem] = ld<R>(d + b * n + i) * a[b * a_bs + rem] + c[b * c_bs + rem];
+}
+
+// WB = wg (g + h) + f1, VB = vg (g - h) + f2  (3 columns at stride 6n)
+template <class R>
+__global__ void td_rhs_kernel(int Bc, int n, const Cx<R>* __restrict__ g, const Cx<R>* __restrict__ h, long long g_bs,
+                              const Cx<R>* __restrict__ f1, const Cx<R>* __restrict__ f2, long long f_bs,
+                              const cplx* __restrict__ wg, const cplx* __restrict__ vg, Cx<R>* __restrict__ WB,
+                              Cx<R>* __restrict__ VB) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)Bc * n * 3) return;
+  const long long b = idx / (3LL * n);
+  const int rem = (int)(idx % (3LL * n)), i = rem % n;
+  const Cx<R> gg = g[b * g_bs + rem], hh = h[b * g_bs + rem];
+  WB[b * 6LL * n + rem] = ld<R>(wg + b * n + i) * (gg + hh) + f1[b * f_bs + rem];
+  VB[b * 6LL * n + rem] = ld<R>(vg + b * n + i) * (gg - hh) + f2[b * f_bs + rem];
+}
+
+// c+ = (WB + VB) / 2 ; Y = [X c+ | 2 X c+ - asum]
+template <class R>
+__global__ void td_cp_kernel(int Bc, int n, const Cx<R>* __restrict__ WB, const Cx<R>* __restrict__ VB,
+                             const cplx* __restrict__ X, long long x_bs, const Cx<R>* __restrict__ asum,
+                             Cx<R>* __restrict__ cp, long long f_bs, Cx<R>* __restrict__ Y) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)Bc * n * 3) return;
+  const long long b = idx / (3LL * n);
+  const int rem = (int)(idx % (3LL * n)), i = rem % n;
+  const Cx<R> c = (WB[b * 6LL * n + rem] + VB[b * 6LL * n + rem]) * R(0.5);
+  cp[b * f_bs + rem] = c;
+  const Cx<R> xc = ld<R>(X + b * x_bs + i) * c;
+  Y[b * 6LL * n + rem] = xc;
+  Y[b * 6LL * n + 3LL * n + rem] = xc * R(2.0) - asum[b * f_bs + rem];
+}
+
+// c- = U1 - U2 + sigma ; g_next = Y[:, 3:]
+template <class R>
+__global__ void td_cm_kernel(int Bc, int n, const Cx<R>* __restrict__ U1, const Cx<R>* __restrict__ U2,
+                             const Cx<R>* __restrict__ sig, Cx<R>* __restrict__ cm, long long f_bs,
+                             const Cx<R>* __restrict__ Y, Cx<R>* __restrict__ gn, long long g_bs) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)Bc * n * 3) return;
+  const long long b = idx / (3LL * n);
+  const int rem = (int)(idx % (3LL * n));
+  cm[b * f_bs + rem] = U1[b * 3LL * n + rem] - U2[b * 3LL * n + rem] + sig[b * f_bs + rem];
+  gn[b * g_bs + rem] = Y[b * 6LL * n + 3LL * n + rem];
+}
+
+// dst += src over `count` complex entries (FP32 corrections into the double-float state)
+template <class RS, class RD>
+__global__ void accumulate_kernel(long long count, const Cx<RS>* __restrict__ src, Cx<RD>* __restrict__ dst) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const Cx<RS> a = src[i];
+  Cx<RD> d = dst[i];
+  d.x = d.x + RD((double)a.x);
+  d.y = d.y + RD((double)a.y);
+  dst[i] = d;
+}
+
+// per (solve, layer) pair: UW = [c+ + X c- | X c+ + c-], UV = [c+ - X c- | X c+ - c-]
+template <class R>
+__global__ void res_u_kernel(int P, int n, const Cx<R>* __restrict__ cp, const Cx<R>* __restrict__ cm,
+                             const cplx* __restrict__ X, Cx<R>* __restrict__ UW, Cx<R>* __restrict__ UV) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)P * n * 3) return;
+  const long long p = idx / (3LL * n);
+  const int rem = (int)(idx % (3LL * n)), i = rem % n;
+  const Cx<R> a = cp[p * 3LL * n + rem], c = cm[p * 3LL * n + rem];
+  const Cx<R> x = ld<R>(X + p * n + i);
+  const Cx<R> xa = x * a, xc = x * c;
+  UW[p * 6LL * n + rem] = a + xc;
+  UW[p * 6LL * n + 3LL * n + rem] = xa + c;
+  UV[p * 6LL * n + rem] = a - xc;
+  UV[p * 6LL * n + 3LL * n + rem] = xa - c;
+}
+
+// negated residuals of E1..E4 as FP32 right-hand sides (YW = W UW, YV = V UV)
+template <class R>
+__global__ void res_f_kernel(int P, int L, int n, const Cx<R>* __restrict__ YW, const Cx<R>* __restrict__ YV,
+                             const Cx<R>* __restrict__ g, const Cx<R>* __restrict__ h, const cplx* __restrict__ wg,
+                             const cplx* __restrict__ vg, Cx<float>* __restrict__ f1, Cx<float>* __restrict__ f2,
+                             Cx<float>* __restrict__ f3, Cx<float>* __restrict__ f4) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)P * n * 3) return;
+  const long long p = idx / (3LL * n);
+  const int rem = (int)(idx % (3LL * n)), i = rem % n;
+  const long long b = p / L, l = p % L;
+  const long long gt = (b * (L + 1) + l) * 3LL * n + rem, gb = gt + 3LL * n;
+  const Cx<R> w = ld<R>(wg + b * n + i), v = ld<R>(vg + b * n + i);
+  const Cx<R> g0 = g[gt], h0 = h[gt], g1 = g[gb], h1 = h[gb];
+  const Cx<R> e1 = YW[p * 6LL * n + rem] - w * (g0 + h0);
+  const Cx<R> e3 = YW[p * 6LL * n + 3LL * n + rem] - w * (g1 + h1);
+  const Cx<R> e2 = YV[p * 6LL * n + rem] - v * (g0 - h0);
+  const Cx<R> e4 = YV[p * 6LL * n + 3LL * n + rem] - v * (g1 - h1);
+  auto neg32 = [](Cx<R> e) { return cxmk<float>((float)(-rto(e.x)), (float)(-rto(e.y))); };
+  f1[p * 3LL * n + rem] = neg32(e1);
+  f2[p * 3LL * n + rem] = neg32(e2);
+  f3[p * 3LL * n + rem] = neg32(e3);
+  f4[p * 3LL * n + rem] = neg32(e4);
+}
+
+// negated residuals of the top and bottom port equations
+template <class R>
+__global__ void res_tb_kernel(int Bc, int L, int n, const Cx<R>* __restrict__ g, const Cx<R>* __restrict__ h,
+                              const Cx<R>* __restrict__ Cin, const cplx* __restrict__ r21, const cplx* __restrict__ r22,
+                              const cplx* __restrict__ t11, Cx<float>* __restrict__ ft, Cx<float>* __restrict__ fb) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)Bc * n * 3) return;
+  const long long b = idx / (3LL * n);
+  const int rem = (int)(idx % (3LL * n)), i = rem % n;
+  const long long top = b * (L + 1) * 3LL * n + rem, bot = top + (long long)L * 3 * n;
+  const Cx<R> et = g[top] - ld<R>(r21 + b * n + i) * Cin[b * 3LL * n + rem] - ld<R>(r22 + b * n + i) * h[top];
+  const Cx<R> eb = h[bot] - ld<R>(t11 + b * n + i) * g[bot];
+  ft[b * 3LL * n + rem] = cxmk<float>((float)(-rto(et.x)), (float)(-rto(et.y)));
+  fb[b * 3LL * n + rem] = cxmk<float>((float)(-rto(eb.x)), (float)(-rto(eb.y)));
+}
+
+// Work arrays of the refinement (FP32 unless noted), carved from the arena.
+struct RefineBufs {
+  using F = Cx<float>;
+  using D = Cx<df64>;
+  F *f1, *f2, *f3, *f4;           // (Bc, L, 3, n) right-hand sides of E1..E4
+  F *ft, *fb;                     // (Bc, 3, n)
+  F *sv, *asum, *sig;             // s: (Bc, L+1, 3, n); asum, sig: (Bc, L, 3, n)
+  F *dg, *dh, *dcp, *dcm;         // corrections
+  F *WB, *VB, *Y, *Rz, *U1, *U2;  // (Bc, 6, n) scratch
+  F *Dv;                          // (Bc, 3, n)
+  D *g, *h, *cp, *cm;             // double-float state
+  D *UW, *UV, *YW, *YV;           // (P, 6, n) residual products
+  D *Cin, *cref, *ctrn;           // (Bc, 3, n)
+  bool carve(Arena& ar, int Bc, int L, int n) {
+    const size_t P = (size_t)Bc * L, v = 3 * (size_t)n, G = (size_t)Bc * (L + 1);
+    f1 = ar.get<F>(P * v); f2 = ar.get<F>(P * v); f3 = ar.get<F>(P * v); f4 = ar.get<F>(P * v);
+    ft = ar.get<F>(Bc * v); fb = ar.get<F>(Bc * v);
+    sv = ar.get<F>(G * v); asum = ar.get<F>(P * v); sig = ar.get<F>(P * v);
+    dg = ar.get<F>(G * v); dh = ar.get<F>(G * v); dcp = ar.get<F>(P * v); dcm = ar.get<F>(P * v);
+    WB = ar.get<F>(2 * Bc * v); VB = ar.get<F>(2 * Bc * v); Y = ar.get<F>(2 * Bc * v);
+    Rz = ar.get<F>(2 * Bc * v); U1 = ar.get<F>(2 * Bc * v); U2 = ar.get<F>(2 * Bc * v);
+    Dv = ar.get<F>(Bc * v);
+    g = ar.get<D>(G * v); h = ar.get<D>(G * v); cp = ar.get<D>(P * v); cm = ar.get<D>(P * v);
+    UW = ar.get<D>(2 * P * v); UV = ar.get<D>(2 * P * v); YW = ar.get<D>(2 * P * v); YV = ar.get<D>(2 * P * v);
+    Cin = ar.get<D>(Bc * v); cref = ar.get<D>(Bc * v); ctrn = ar.get<D>(Bc * v);
+    return ar.ok();
+  }
+  static size_t bytes(int Bc, int L, int n) {
+    const size_t P = (size_t)Bc * L, v = 3 * (size_t)n, G = (size_t)Bc * (L + 1);
+    size_t b = 0;
+    auto A = [&](size_t x) { b += (x + 255) & ~(size_t)255; };
+    for (int k = 0; k < 4; ++k) A(8 * P * v);
+    A(8 * Bc * v); A(8 * Bc * v);
+    A(8 * G * v); A(8 * P * v); A(8 * P * v);
+    A(8 * G * v); A(8 * G * v); A(8 * P * v); A(8 * P * v);
+    for (int k = 0; k < 6; ++k) A(8 * 2 * Bc * v);
+    A(8 * Bc * v);
+    A(16 * G * v); A(16 * G * v); A(16 * P * v); A(16 * P * v);
+    for (int k = 0; k < 4; ++k) A(16 * 2 * P * v);
+    for (int k = 0; k < 3; ++k) A(16 * Bc * v);
+    return b;
+  }
+};
+
+// One FP32 solve of the interface equations with right-hand sides rb.f*, from the factors left by
+// cascade_factor<float> (bW, bV, Mk, Ak with pivots; Rk; G0 in S1 with pivS). Writes the
+// solution to rb.dg, rb.dh, rb.dcp, rb.dcm.
+static void cascade_sources(cudaStream_t s, int Bc, int L, int n, const Cx<float>* bW, const Cx<float>* bV,
+                            const int* pivW, const int* pivV, const Cx<float>* Mk, const int* pivM,
+                            const Cx<float>* Ak, const int* pivA, const Cx<float>* Rk, const Cx<float>* G0,
+                            const int* pivG, const cplx* X, const PortVectors& pv, RefineBufs& rb) {
+  using F = Cx<float>;
+  const long long n2 = (long long)n * n, v3 = 3LL * n, v6 = 6LL * n;
+  const long long lay_bs = (long long)L * n2, lay_ps = (long long)L * n, r_bs = (long long)(L + 1) * n2;
+  const long long f_bs = (long long)L * v3, g_bs = (long long)(L + 1) * v3;
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  const unsigned nb3 = nblk((long long)Bc * v3, 256), nb6 = nblk((long long)Bc * v6, 256);
+  // bottom: h_L = t11 g_L + s_L with s_L = f_bottom
+  cudaMemcpy2DAsync(rb.sv + (long long)L * v3, g_bs * sizeof(F), rb.fb, v3 * sizeof(F), v3 * sizeof(F), Bc,
+                    cudaMemcpyDeviceToDevice, s);
+  for (int l = L - 1; l >= 0; --l) {
+    const F* Wl = bW + (long long)l * n2;  const int* pW = pivW + (long long)l * n;
+    const F* Vl = bV + (long long)l * n2;  const int* pV = pivV + (long long)l * n;
+    const F* Ml = Mk + (long long)l * n2;  const int* pM = pivM + (long long)l * n;
+    const F* Al = Ak + (long long)l * n2;  const int* pA = pivA + (long long)l * n;
+    const F* Rn = Rk + (long long)(l + 1) * n2;
+    const long long fo = (long long)l * v3;
+    bu_rhs_kernel<float><<<nb3, 256, 0, s>>>(Bc, n, rb.sv + (long long)(l + 1) * v3, g_bs, rb.f1 + fo, rb.f2 + fo,
+                                             rb.f3 + fo, rb.f4 + fo, f_bs, pv.wg, pv.vg, rb.WB, rb.VB);
+    note_launch();
+    getrs<float>(s, Bc, n, Wl, n, lay_bs, pW, lay_ps, rb.WB, 6, n, v6, 0);
+    getrs<float>(s, Bc, n, Vl, n, lay_bs, pV, lay_ps, rb.VB, 6, n, v6, 0);
+    bu_y_kernel<float><<<nb3, 256, 0, s>>>(Bc, n, rb.WB, rb.VB, X + (long long)l * n, lay_ps, rb.Y, rb.asum + fo,
+                                           rb.sig + fo, f_bs, rb.Dv);
+    note_launch();
+    getrs<float>(s, Bc, n, Ml, n, lay_bs, pM, lay_ps, rb.Y, 6, n, v6, 0);           // Z = M^-1 Y
+    gemm<float>(s, Bc, n, 6, n, one, Rn, 1, n, r_bs, rb.Y, 1, n, v6, zero, rb.Rz, 1, n, v6);
+    nz_kernel<float><<<nb6, 256, 0, s>>>(Bc, n, 6, rb.Y, v6, rb.Rz, pv.wg, pv.vg, rb.U1, rb.U2); note_launch();
+    getrs<float>(s, Bc, n, Wl, n, lay_bs, pW, lay_ps, rb.U1, 6, n, v6, 0);
+    getrs<float>(s, Bc, n, Vl, n, lay_bs, pV, lay_ps, rb.U2, 6, n, v6, 0);
+    bu_src_kernel<float><<<nb3, 256, 0, s>>>(Bc, n, rb.U1, rb.U2, X + (long long)l * n, lay_ps, rb.sig + fo, f_bs,
+                                             rb.Dv, rb.sv + (long long)l * v3, g_bs);
+    note_launch();
+    getrs<float>(s, Bc, n, Al, n, lay_bs, pA, lay_ps, rb.sv + (long long)l * v3, 3, n, g_bs, 0);   // s_l
+  }
+  // top: g_0 = G0^-1 (r22 s_0 + f_top)
+  diag_axpy3_kernel<float><<<nb3, 256, 0, s>>>(Bc, n, pv.r22, rb.sv, g_bs, rb.ft, v3, rb.dg, g_bs); note_launch();
+  getrs<float>(s, Bc, n, G0, n, n2, pivG, n, rb.dg, 3, n, g_bs, 0);
+  // h_l = s_l + R_l g_l for every l < L is formed layer by layer below
+  for (int l = 0; l < L; ++l) {
+    const F* Wl = bW + (long long)l * n2;  const int* pW = pivW + (long long)l * n;
+    const F* Vl = bV + (long long)l * n2;  const int* pV = pivV + (long long)l * n;
+    const F* Ml = Mk + (long long)l * n2;  const int* pM = pivM + (long long)l * n;
+    const long long fo = (long long)l * v3, go = (long long)l * v3;
+    cudaMemcpy2DAsync(rb.dh + go, g_bs * sizeof(F), rb.sv + go, g_bs * sizeof(F), v3 * sizeof(F), Bc,
+                      cudaMemcpyDeviceToDevice, s);
+    gemm<float>(s, Bc, n, 3, n, one, Rk + (long long)l * n2, 1, n, r_bs, rb.dg + go, 1, n, g_bs, one, rb.dh + go, 1, n,
+                g_bs);                                                                   // h_l
+    td_rhs_kernel<float><<<nb3, 256, 0, s>>>(Bc, n, rb.dg + go, rb.dh + go, g_bs, rb.f1 + fo, rb.f2 + fo, f_bs,
+                                             pv.wg, pv.vg, rb.WB, rb.VB);
+    note_launch();
+    getrs<float>(s, Bc, n, Wl, n, lay_bs, pW, lay_ps, rb.WB, 3, n, v6, 0);
+    getrs<float>(s, Bc, n, Vl, n, lay_bs, pV, lay_ps, rb.VB, 3, n, v6, 0);
+    td_cp_kernel<float><<<nb3, 256, 0, s>>>(Bc, n, rb.WB, rb.VB, X + (long long)l * n, lay_ps, rb.asum + fo,
+                                            rb.dcp + fo, f_bs, rb.Y);
+    note_launch();
+    getrs<float>(s, Bc, n, Ml, n, lay_bs, pM, lay_ps, rb.Y, 6, n, v6, 0);           // [M^-1 X c+ | g_l+1]
+    gemm<float>(s, Bc, n, 3, n, one, Rk + (long long)(l + 1) * n2, 1, n, r_bs, rb.Y, 1, n, v6, zero, rb.Rz, 1, n, v3);
+    nz_kernel<float><<<nb3, 256, 0, s>>>(Bc, n, 3, rb.Y, v6, rb.Rz, pv.wg, pv.vg, rb.U1, rb.U2); note_launch();
+    getrs<float>(s, Bc, n, Wl, n, lay_bs, pW, lay_ps, rb.U1, 3, n, v3, 0);
+    getrs<float>(s, Bc, n, Vl, n, lay_bs, pV, lay_ps, rb.U2, 3, n, v3, 0);
+    td_cm_kernel<float><<<nb3, 256, 0, s>>>(Bc, n, rb.U1, rb.U2, rb.sig + fo, rb.dcm + fo, f_bs, rb.Y,
+                                            rb.dg + go + v3, g_bs);
+    note_launch();
+  }
+  // h_L = t11 g_L + s_L
+  diag_axpy3_kernel<float><<<nb3, 256, 0, s>>>(Bc, n, pv.t11, rb.dg + (long long)L * v3, g_bs,
+                                               rb.sv + (long long)L * v3, g_bs, rb.dh + (long long)L * v3, g_bs);
+  note_launch();
+}
+
+// Stage C of the mixed form: FP32 factorisation, then `passes` solves of the interface equations
+// (the first from a zero state), each against the double-float residual of the previous state.
+// bWd / bVd: the double-float bigW / bigV of stage B (unfactored); bW / bV: their FP32 LU.
+void stage_c_refined(cudaStream_t s, int Bc, int L, int N, const Cx<df64>* bWd, const Cx<df64>* bVd,
+                     Cx<float>* bW, Cx<float>* bV, const int* pivW, const int* pivV, const cplx* X,
+                     const PortVectors& pv, const SolveDesc& d, int first, const SolveOut& out, int32_t* st,
+                     Cx<float>* Mk, int* pivM, Cx<float>* Ak, int* pivA, Cx<float>* Rk, Cx<float>* S1,
+                     Cx<float>* S2, Cx<float>* S3, int* pivS, RefineBufs& rb, int passes) {
+  using D = Cx<df64>;
+  const int n = 2 * N, P = Bc * L;
+  const long long n2 = (long long)n * n, v3 = 3LL * n, v6 = 6LL * n;
+  const long long r_bs = (long long)(L + 1) * n2, g_bs = (long long)(L + 1) * v3;
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  cascade_factor<float>(s, Bc, L, N, bW, bV, pivW, pivV, X, pv, st, Mk, pivM, Rk, S1, S2, S3, pivS, Ak, pivA);
+  top_kernel<float><<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, Rk, r_bs, pv.r22, S1, n2); note_launch();
+  getrf<float>(s, Bc, n, S1, n, n2, pivS, n, st, 1);
+  incident_kernel<df64><<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, N, d.pol + 2 * first, pv.nt, rb.Cin, v3);
+  note_launch();
+  const size_t gsz = sizeof(D) * (size_t)Bc * g_bs, csz = sizeof(D) * (size_t)P * v3;
+  cudaMemsetAsync(rb.g, 0, gsz, s); cudaMemsetAsync(rb.h, 0, gsz, s);
+  cudaMemsetAsync(rb.cp, 0, csz, s); cudaMemsetAsync(rb.cm, 0, csz, s);
+  const unsigned nbp = nblk((long long)P * v3, 256), nbb = nblk((long long)Bc * v3, 256);
+  for (int it = 0; it < passes; ++it) {
+    // residual of the current double-float state
+    res_u_kernel<df64><<<nbp, 256, 0, s>>>(P, n, rb.cp, rb.cm, X, rb.UW, rb.UV); note_launch();
+    gemm<df64>(s, P, n, 6, n, one, bWd, 1, n, n2, rb.UW, 1, n, v6, zero, rb.YW, 1, n, v6);
+    gemm<df64>(s, P, n, 6, n, one, bVd, 1, n, n2, rb.UV, 1, n, v6, zero, rb.YV, 1, n, v6);
+    res_f_kernel<df64><<<nbp, 256, 0, s>>>(P, L, n, rb.YW, rb.YV, rb.g, rb.h, pv.wg, pv.vg, rb.f1, rb.f2, rb.f3, rb.f4);
+    note_launch();
+    res_tb_kernel<df64><<<nbb, 256, 0, s>>>(Bc, L, n, rb.g, rb.h, rb.Cin, pv.r21, pv.r22, pv.t11, rb.ft, rb.fb);
+    note_launch();
+    // FP32 correction, accumulated into the state
+    cascade_sources(s, Bc, L, n, bW, bV, pivW, pivV, Mk, pivM, Ak, pivA, Rk, S1, pivS, X, pv, rb);
+    const long long gc = (long long)Bc * g_bs, cc = (long long)P * v3;
+    accumulate_kernel<float, df64><<<nblk(gc, 256), 256, 0, s>>>(gc, rb.dg, rb.g); note_launch();
+    accumulate_kernel<float, df64><<<nblk(gc, 256), 256, 0, s>>>(gc, rb.dh, rb.h); note_launch();
+    accumulate_kernel<float, df64><<<nblk(cc, 256), 256, 0, s>>>(cc, rb.dcp, rb.cp); note_launch();
+    accumulate_kernel<float, df64><<<nblk(cc, 256), 256, 0, s>>>(cc, rb.dcm, rb.cm); note_launch();
+  }
+  // c_ref = r11 C + r12 h_0, c_trn = t21 g_L, then the efficiencies
+  dscale3_kernel<df64><<<nbb, 256, 0, s>>>(Bc, n, pv.r11, rb.Cin, v3, pv.r12, rb.h, g_bs, rb.cref, v3); note_launch();
+  dscale3_kernel<df64><<<nbb, 256, 0, s>>>(Bc, n, pv.t21, rb.g + (long long)L * v3, g_bs, nullptr, nullptr, 0, rb.ctrn, v3);
+  note_launch();
+  efficiency_kernel<df64><<<nblk((long long)Bc * N * 3, 256), 256, 0, s>>>(
+      Bc, N, rb.cref, rb.ctrn, v3, pv, d.eps_top + first, d.eps_bot + first, d.pol + 2 * first,
+      out.R + (long long)first * 3 * N, out.T + (long long)first * 3 * N,
+      out.amps ? out.amps + (long long)first * 12 * N : nullptr, st);
+  note_launch();
+}
+
 // ------------------------------------------------------------------------- orchestration
+// Solves of the interface equations in the mixed form: the FP32 solve from a zero state and
+// one refinement against the double-float residual.
+constexpr int kRefinePasses = 2;
+
 // Workspace of one chunk of `chunk` solves with L layers of N orders (n = 2N). All matrices are
 // allocated at 16 bytes per complex entry (complex128 or complex df64); the FP32 cascade of the
 // mixed form takes its own 8-byte copies.
@@ -678,16 +1093,23 @@ size_t solve_chunk_bytes(int N, int L, int chunk, int precision) {
   A(16 * P * n2); A(16 * P * n2); A(16 * P * n2);                  // OM, Zb, Xv
   for (int k = 0; k < 5; ++k) A(16 * P * n);                        // wr, tau, w, q, X
   A(sizeof(int) * P * n); A(sizeof(int) * P * n); A(sizeof(int) * P * n);
-  const size_t ec = (precision == 2) ? 8 : 16;                     // stage C element size
-  if (precision == 2) { A(ec * P * n2); A(ec * P * n2); A(ec * P * n2); }   // FP32 bigW, bigV, Mk
+  const bool fp32c = (precision == 1 || precision == 2);           // FP32 cascade
+  const size_t ec = fp32c ? 8 : 16;                                // stage C element size
+  if (fp32c) { A(ec * P * n2); A(ec * P * n2); A(ec * P * n2); }   // FP32 bigW, bigV, Mk
   A(ec * (P + chunk) * n2);
   A(ec * chunk * n2); A(ec * chunk * n2); A(ec * chunk * n2);
   A(sizeof(int) * chunk * n);
-  for (int k = 0; k < 6; ++k) A(ec * chunk * n * 3);
+  if (precision == 1) {                                            // per-layer A factors, refinement
+    A(ec * P * n2); A(sizeof(int) * P * n);
+    b += RefineBufs::bytes(chunk, L, (int)n);
+  } else {
+    for (int k = 0; k < 6; ++k) A(ec * chunk * n * 3);
+  }
   return b;
 }
 
-// precision: 0 plain FP64; 1 mixed (df64 stage B and C); 2 mixed (df64 stage B, FP32 stage C)
+// precision: 0 plain FP64; 1 mixed (df64 stage B, FP32 cascade refined against the df64
+// interface equations); 2 df64 stage B with the unrefined FP32 cascade; 3 df64 stage B and C
 int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int count, const SolveOut& out,
                 int precision) {
   const int N = (2 * d.hu + 1) * (2 * d.hv + 1), n = 2 * N, L = d.n_layers;
@@ -749,7 +1171,7 @@ int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int co
     Cx<R>* OM = (Cx<R>*)OMr; Cx<R>* Zb = (Cx<R>*)Zbr; Cx<R>* Xv = (Cx<R>*)Xvr;
     stage_b<R>(s, P, N, d.conv, pair_layer, pair_solve, pair_thick, wl, pv.kx, pv.ky, OM, Zb, Xv, (Cx<R>*)wr,
                (Cx<R>*)taur, w, q, X, pv.c, pv.s, st, L, true);
-    if (precision == 1) {
+    if (precision == 3) {
       getrf<R>(s, P, n, OM, n, n2, pivW, n, st, L);
       getrf<R>(s, P, n, Zb, n, n2, pivV, n, st, L);
       Cx<R>* Rk = ar.get<Cx<R>>((size_t)(P + Bc) * n2);
@@ -771,13 +1193,23 @@ int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int co
     Cx<RC>* S1 = ar.get<Cx<RC>>((size_t)Bc * n2); Cx<RC>* S2 = ar.get<Cx<RC>>((size_t)Bc * n2);
     Cx<RC>* S3 = ar.get<Cx<RC>>((size_t)Bc * n2);
     int* pivS = ar.get<int>((size_t)Bc * n);
-    Cx<RC>* v[6];
-    for (int k = 0; k < 6; ++k) v[k] = ar.get<Cx<RC>>((size_t)Bc * n * 3);
     if (!ar.ok()) return -1;
     convert<R, RC>(s, OM, bW, (long long)P * n2);
     convert<R, RC>(s, Zb, bV, (long long)P * n2);
     getrf<RC>(s, P, n, bW, n, n2, pivW, n, st, L);
     getrf<RC>(s, P, n, bV, n, n2, pivV, n, st, L);
+    if (precision == 1) {
+      Cx<RC>* Ak = ar.get<Cx<RC>>((size_t)P * n2);
+      int* pivA = ar.get<int>((size_t)P * n);
+      RefineBufs rb;
+      if (!rb.carve(ar, Bc, L, n) || !ar.ok()) return -1;
+      stage_c_refined(s, Bc, L, N, OM, Zb, bW, bV, pivW, pivV, X, pv, d, first, out, st, Mk, pivM, Ak, pivA, Rk,
+                      S1, S2, S3, pivS, rb, kRefinePasses);
+      return 0;
+    }
+    Cx<RC>* v[6];
+    for (int k = 0; k < 6; ++k) v[k] = ar.get<Cx<RC>>((size_t)Bc * n * 3);
+    if (!ar.ok()) return -1;
     stage_c<RC>(s, ar, Bc, L, N, bW, bV, pivW, pivV, X, pv, d, first, out, st, Mk, pivM, Rk, S1, S2, S3, pivS,
                 v[0], v[1], v[2], v[3], v[4], v[5]);
   }
