@@ -146,6 +146,16 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def hbm_peak():
+    """Measured HBM copy bandwidth of the GB300s (GB/s), or the 6.8 TB/s fallback."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'MEASURED_PEAKS.json')
+    try:
+        with open(path) as f:
+            return float(json.load(f)['hbm_gbs'])
+    except (OSError, KeyError, ValueError):
+        return 6800.0
+
+
 def fp64_peak(torch, dev):
     """cuBLAS DGEMM 4096^3 rate measured now (the FP64 roofline denominator)."""
     a = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
@@ -166,7 +176,7 @@ def main():
     ap.add_argument('--steps', type=int, default=3)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
-    ap.add_argument('--precision', default='double', choices=['double', 'mixed', 'mixed_fp32'])
+    ap.add_argument('--precision', default='double', choices=['double', 'mixed', 'mixed_fp32', 'mixed_df64'])
     ap.add_argument('--workload', default='crossed_sweep', choices=['crossed_sweep', 'mixed_sweep'])
     ap.add_argument('--solves', type=int, default=128)
     ap.add_argument('--ref-sample', type=int, default=4)
@@ -259,14 +269,13 @@ def main():
     # sweep's P = B*L (solve, layer) pairs, on the launching stream
     roof = None
     if rank == 0:
-        from oracle import rcwa_oracle as O  # noqa: F401  (only for the kx grid helpers below)
+        from wavebit_gb300.adjoint import ports
         P = B * L
         kxs, kys = [], []
         for b in range(B):
-            kx, ky = O.separable_kxy(float(wl[b]), cfg['period'], (0.0, 0.0), hu, hv)
-            kxg, kyg = O.order_grid(kx, ky)
+            pv = ports(float(wl[b]), cfg['period'], float(thetas[b]), 0.0, cfg['eps_top'], cfg['eps_bot'], hu, hv, 'cpu')
             for _ in range(L):
-                kxs.append(kxg.real); kys.append(kyg.real)
+                kxs.append(pv['kx'].numpy()); kys.append(pv['ky'].numpy())
         kxs, kys = np.array(kxs), np.array(kys)
         pl = np.tile(np.arange(L), B)
         E.layer_modes(conv, pl, kxs, kys, handle=handle)   # warm
@@ -287,6 +296,35 @@ def main():
                 'flops_per_launch': flops, 'launch_ms': tb * 1e3, 'traffic': None,
                 'whole_step': {'achieved': (280 * L + 192) * n ** 3 * B / (t / args.steps) / 1e12,
                                'unit': 'TFLOP/s', 'flops_convention': '(280 L + 192) n^3 per solve'}}
+
+    # stage A (convolution-matrix assembly of the stack's layers): HBM bytes per layer are the
+    # raster read plus the three N x N slots written
+    stage_a = None
+    if rank == 0:
+        eps_dev = torch.as_tensor(eps_host, device=dev)
+        E.assemble(eps_dev, hu, hv, handle=handle)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 5
+        e0.record(stream)
+        for _ in range(reps):
+            E.assemble(eps_dev, hu, hv, handle=handle)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ta = e0.elapsed_time(e1) / 1e3 / reps
+        ny, nx = eps_host.shape[1:]
+        nbytes = L * (16 * ny * nx + 3 * 16 * N * N)
+        hbm = hbm_peak()
+        stage_a = {'layers': L, 'ms': ta * 1e3, 'bytes': nbytes, 'achieved_GBps': nbytes / ta / 1e9,
+                   'hbm_peak_GBps': hbm, 'frac': nbytes / ta / 1e9 / hbm if hbm else None,
+                   'note': 'latency bound (direct DFT, Toeplitz inverses and two N x N inverses per layer); '
+                           'runs once per stack and is cached across the sweep'}
+
+    # energy balance |1 - sum R - sum T| for lossless stacks (no absorbing layer)
+    energy = None
+    if rank == 0 and not np.any(np.imag(eps_host)):
+        Rs, Ts = out[0].view(B, 3, -1).sum(-1), out[1].view(B, 3, -1).sum(-1)
+        energy = float((1.0 - Rs - Ts).abs().max())
 
     # end to end through the C ABI with host buffers (copies in, stage A, solve, copies out)
     e2e = None
@@ -312,7 +350,7 @@ def main():
                 'data': 'synthetic', 'config': _config(args.precision, 'gb300', B, args.workload), 'e2e': e2e,
                 'gpu_launches': int(launches), 'roofline': roof, 'clocks': clk,
                 'status_nonzero': int((st & ~8).astype(bool).sum()), 'grazing_flags': int(((st & 8) != 0).sum()),
-                'mixed_vs_fp64': mixed_vs_fp64}
+                'mixed_vs_fp64': mixed_vs_fp64, 'stage_a': stage_a, 'energy_balance_max': energy}
         if not args.no_cpu_baseline and world == 1:
             line['cpu_baseline'] = cpu_baseline(cfg, args.ref_sample)
         print(json.dumps(line), flush=True)
