@@ -176,7 +176,7 @@ def main():
     ap.add_argument('--steps', type=int, default=3)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
-    ap.add_argument('--precision', default='double', choices=['double', 'mixed', 'mixed_fp32', 'mixed_df64'])
+    ap.add_argument('--precision', default='double', choices=['double', 'mixed', 'mixed_fp32', 'mixed_df64', 'mixed_df64_eig'])
     ap.add_argument('--workload', default='crossed_sweep', choices=['crossed_sweep', 'mixed_sweep'])
     ap.add_argument('--solves', type=int, default=128)
     ap.add_argument('--ref-sample', type=int, default=4)

@@ -43,11 +43,13 @@ extern "C" {
                               (rcwa/_engine/solve_2d.py:2463-2482); the result is flagged */
 
 #define WB_PRECISION_FP64 0        /* IEEE FP64 throughout */
-#define WB_PRECISION_MIXED 1       /* double-float (2 x FP32) eigen-solve; FP32 cascade whose
-                                      amplitudes are refined against the double-float interface
-                                      equations (FP64-class results) */
-#define WB_PRECISION_MIXED_FP32 2  /* double-float eigen-solve, unrefined FP32 cascade (~1e-5) */
+#define WB_PRECISION_MIXED 1       /* FP32 eigen-solve brought to FP64 accuracy by Newton steps
+                                      against the FP64 operator; FP32 cascade whose amplitudes are
+                                      refined against the double-float interface equations */
+#define WB_PRECISION_MIXED_FP32 2  /* double-float (2 x FP32) eigen-solve, unrefined FP32 cascade
+                                      (~1e-5) */
 #define WB_PRECISION_MIXED_DF64 3  /* double-float eigen-solve and cascade */
+#define WB_PRECISION_MIXED_DF64_EIG 4  /* double-float eigen-solve, refined FP32 cascade */
 
 typedef struct { double re, im; } wb_complex;
 typedef struct wb_handle wb_handle;
@@ -85,7 +87,8 @@ int wb_assemble_li(wb_handle* h, const wb_complex* eps, int L, int ny, int nx, i
 /* Stage B: eigenmodes of n_pairs layers. conv: device (n_conv, 3, N, N) slots epx, epy, epz_i;
  * pair_layer: device (n_pairs) index into conv; kx, ky: device (n_pairs, N) normalised order
  * wavevectors. Outputs (device): w (n_pairs, 2N) eigenvalues of Omega^2, q (n_pairs, 2N),
- * W and V (n_pairs, 2N, 2N) column-major, status (n_pairs). precision: WB_PRECISION_*.
+ * W and V (n_pairs, 2N, 2N) column-major, status (n_pairs). precision: WB_PRECISION_FP64 for
+ * the FP64 eigen-solve, any other WB_PRECISION_* for the double-float one.
  * Reference: rcwa/_engine/solve_2d.py:2303-2460 (layer_modes_2d, no exceptional-point
  * rebuilds), _common/conventions.py:186-249 (mode_q), _common/backend.py:1767-1812 (eig). */
 int wb_layer_modes(wb_handle* h, int n_pairs, int hu, int hv, const wb_complex* conv,

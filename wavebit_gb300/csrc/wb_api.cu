@@ -148,7 +148,7 @@ int wb_layer_modes(wb_handle* h, int n_pairs, int hu, int hv, const wb_complex* 
   if (!h || !conv || !pair_layer || !kx || !ky || !w || !q || !W || !V)
     return fail(WB_E_INVALID, "wb_layer_modes: NULL argument");
   if (n_pairs <= 0 || !valid_orders(hu, hv)) return fail(WB_E_INVALID, "wb_layer_modes: bad sizes");
-  if (precision < WB_PRECISION_FP64 || precision > WB_PRECISION_MIXED_DF64)
+  if (precision < WB_PRECISION_FP64 || precision > WB_PRECISION_MIXED_DF64_EIG)
     return fail(WB_E_INVALID, "wb_layer_modes: precision %d", precision);
   cudaSetDevice(h->device);
   const int N = (2 * hu + 1) * (2 * hv + 1), n = 2 * N;
@@ -171,7 +171,7 @@ int wb_solve_batch(wb_handle* h, int B, int L, int hu, int hv, const wb_complex*
       !eps_bot || !pol || !R || !T || !status)
     return fail(WB_E_INVALID, "wb_solve_batch: NULL argument");
   if (B <= 0 || L <= 0 || !valid_orders(hu, hv)) return fail(WB_E_INVALID, "wb_solve_batch: bad sizes B=%d L=%d", B, L);
-  if (precision < WB_PRECISION_FP64 || precision > WB_PRECISION_MIXED_DF64)
+  if (precision < WB_PRECISION_FP64 || precision > WB_PRECISION_MIXED_DF64_EIG)
     return fail(WB_E_INVALID, "wb_solve_batch: precision %d", precision);
   cudaSetDevice(h->device);
   const int N = (2 * hu + 1) * (2 * hv + 1);

@@ -596,6 +596,351 @@ void stage_b(cudaStream_t s, int P, int N, const cplx* conv, const int* pair_lay
   }
 }
 
+// dst += src over `count` complex entries (FP32 corrections into a wider state)
+template <class RS, class RD>
+__global__ void accumulate_kernel(long long count, const Cx<RS>* __restrict__ src, Cx<RD>* __restrict__ dst) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const Cx<RS> a = src[i];
+  Cx<RD> d = dst[i];
+  d.x = d.x + RD((double)a.x);
+  d.y = d.y + RD((double)a.y);
+  dst[i] = d;
+}
+
+// complex128 -> complex double-float in place (both 16 bytes per entry)
+__global__ void to_df64_kernel(long long count, cplx* __restrict__ buf) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const cplx v = buf[i];
+  Cx<df64> o;
+  o.x = df64(v.x); o.y = df64(v.y);
+  reinterpret_cast<Cx<df64>*>(buf)[i] = o;
+}
+
+// -------------------------------------- stage B of the mixed form: FP32 Schur + Newton steps
+// The eigenpairs are computed in FP32 (the stage_b pipeline on floats) and brought to FP64
+// accuracy by Newton steps on the FP64 operator. With W, Lambda the current pairs:
+//   R = Omega^2 W - W Lambda                       (FP64 GEMM)
+//   G = W^-1 R                                     (FP32 LU of W rounded to FP32)
+//   d_i = lambda_i + G_ii
+//   E_ij = G_ij / (d_j - d_i) for i, j in different groups, 0 otherwise
+//   W <- W + W E (FP32 product added to the FP64 W); lambda_i <- d_i
+// where groups are the connected components of the strong couplings |G_ij| > kCouple |d_j - d_i|
+// (near-degenerate modes, for which the first-order formula does not hold). The block
+// Lambda + G restricted to each group is diagonalised exactly in FP64 (the stage-B eigen
+// pipeline on 32 x 32 blocks padded with distant eigenvalues) and the group's columns of W are
+// rotated by its eigenvectors. Each step squares the error; two take FP32 eigenpairs to
+// FP64-class ones (|dR,T| ~1e-11 against the FP64 form at (12,12)).
+constexpr int kGroupMax = 32;          // largest group diagonalised exactly
+constexpr int kGroupSlotsPerPair = 32; // group slots per (solve, layer) pair
+constexpr double kCouple = 0.02;
+constexpr int kNewtonSteps = 2;
+
+struct GroupBufs {
+  int cap = 0;
+  int* count = nullptr;     // (1) slots used
+  int* pair = nullptr;      // (cap)
+  int* size = nullptr;      // (cap)
+  int* members = nullptr;   // (cap, 32)
+  double* offmax = nullptr; // (cap) largest off-diagonal |B_ab| / scale of the pair
+  cplx* A = nullptr;        // (cap, 32, 32) padded blocks -> Schur form -> eigenvectors
+  cplx* Z = nullptr;        // (cap, 32, 32) Schur vectors
+  cplx* X = nullptr;        // (cap, 32, 32) eigenvectors of the Schur form
+  cplx* w = nullptr;        // (cap, 32)
+  cplx* tau = nullptr;      // (cap, 32)
+  bool carve(Arena& ar, int cap_) {
+    cap = cap_;
+    const size_t c = (size_t)cap, b2 = (size_t)kGroupMax * kGroupMax;
+    count = ar.get<int>(1); pair = ar.get<int>(c); size = ar.get<int>(c); members = ar.get<int>(c * kGroupMax);
+    offmax = ar.get<double>(c);
+    A = ar.get<cplx>(c * b2); Z = ar.get<cplx>(c * b2); X = ar.get<cplx>(c * b2);
+    w = ar.get<cplx>(c * kGroupMax); tau = ar.get<cplx>(c * kGroupMax);
+    return ar.ok();
+  }
+  static size_t bytes(int cap_) {
+    const size_t c = (size_t)cap_, b2 = (size_t)kGroupMax * kGroupMax;
+    size_t b = 0;
+    auto A_ = [&](size_t x) { b += (x + 255) & ~(size_t)255; };
+    A_(4); A_(4 * c); A_(4 * c); A_(4 * c * kGroupMax); A_(8 * c);
+    A_(16 * c * b2); A_(16 * c * b2); A_(16 * c * b2); A_(16 * c * kGroupMax); A_(16 * c * kGroupMax);
+    return b;
+  }
+};
+
+__global__ void widen_kernel(long long count, const Cx<float>* __restrict__ src, cplx* __restrict__ dst) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < count) dst[i] = cmk((double)src[i].x, (double)src[i].y);
+}
+
+// R32 = FP32(AW - W diag(lambda))
+__global__ void resid32_kernel(long long total, int n, long long n2, const cplx* __restrict__ AW, const cplx* __restrict__ W,
+                               const cplx* __restrict__ lam, Cx<float>* __restrict__ R) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= total) return;
+  const long long p = idx / n2, rem = idx % n2;
+  const int j = (int)(rem / n);
+  const cplx r = csub(AW[idx], cmul(W[idx], lam[p * n + j]));
+  R[idx] = cxmk<float>((float)r.x, (float)r.y);
+}
+
+// every slot a diagonal 32 x 32 block with distinct entries, so unused slots converge at once
+__global__ void group_init_kernel(int cap, cplx* __restrict__ A, int* __restrict__ count) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx == 0) *count = 0;
+  if (idx >= (long long)cap * kGroupMax * kGroupMax) return;
+  const int rem = (int)(idx % (kGroupMax * kGroupMax)), a = rem % kGroupMax, b = rem / kGroupMax;
+  A[idx] = (a == b) ? cmk(1.0 + a, 0.0) : cmk(0.0, 0.0);
+}
+
+// One CTA per pair: d, the groups (lock-free union-find over the strong couplings, links always
+// from the larger root index to the smaller, retries bounded), the group blocks into slots, E and
+// the new lambda. A pair whose groups do not fit (more than kGroupMax members, slots exhausted,
+// union retries exhausted) is flagged WB_ST_NOCONV.
+__global__ void __launch_bounds__(256) group_kernel(int n, const Cx<float>* __restrict__ Gall, cplx* __restrict__ lam_all,
+                                                    Cx<float>* __restrict__ Eall, GroupBufs gb, int32_t* __restrict__ status,
+                                                    int st_div) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cplx* d = reinterpret_cast<cplx*>(smraw);
+  int* parent = reinterpret_cast<int*>(d + n);
+  int* label = parent + n;
+  int* cnt = label + n;
+  int* slot = cnt + n;
+  int* fill = slot + n;
+  __shared__ int s_fail;
+  __shared__ double s_red[32];
+  const int p = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const long long n2 = (long long)n * n;
+  const Cx<float>* G = Gall + p * n2;
+  Cx<float>* E = Eall + p * n2;
+  cplx* lam = lam_all + (long long)p * n;
+  if (tid == 0) s_fail = 0;
+  double mx = 0.0;
+  for (int i = tid; i < n; i += blockDim.x) {
+    const Cx<float> g = G[i + (long long)i * n];
+    const cplx v = cadd(lam[i], cmk((double)g.x, (double)g.y));
+    d[i] = v; parent[i] = i; cnt[i] = 0; slot[i] = -1; fill[i] = 0;
+    mx = fmax(mx, cabsv(v));
+  }
+  for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  if (lane == 0) s_red[warp] = mx;
+  __syncthreads();
+  double scale = 0.0;
+  for (int k = 0; k < nw; ++k) scale = fmax(scale, s_red[k]);
+  volatile int* vp = parent;
+  for (long long e = tid; e < n2; e += blockDim.x) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    if (i == j) continue;
+    const Cx<float> g = G[e];
+    const double ga = hypot((double)g.x, (double)g.y);
+    if (!(ga > kCouple * cabsv(csub(d[j], d[i])))) continue;
+    int a = i, b = j;
+    bool linked = false;
+    for (int tries = 0; tries < 64 + 4 * n && !linked; ++tries) {
+      int ra = a, rb = b;
+      for (int h = 0; h < n && vp[ra] != ra; ++h) ra = vp[ra];
+      for (int h = 0; h < n && vp[rb] != rb; ++h) rb = vp[rb];
+      if (ra == rb) { linked = true; break; }
+      if (ra > rb) { const int t = ra; ra = rb; rb = t; }
+      if (atomicCAS(&parent[rb], rb, ra) == rb) linked = true;
+    }
+    if (!linked) s_fail = 1;
+  }
+  __syncthreads();
+  for (int i = tid; i < n; i += blockDim.x) {
+    int r = i;
+    for (int h = 0; h < n && vp[r] != r; ++h) r = vp[r];
+    label[i] = r;
+    atomicAdd(&cnt[r], 1);
+  }
+  __syncthreads();
+  for (int r = tid; r < n; r += blockDim.x) {
+    if (label[r] != r || cnt[r] < 2) continue;
+    const int sl = atomicAdd(gb.count, 1);
+    if (sl < gb.cap && cnt[r] <= kGroupMax) {
+      slot[r] = sl; gb.pair[sl] = p; gb.size[sl] = cnt[r];
+    } else {
+      s_fail = 1;
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < n; i += blockDim.x) {
+    const int r = label[i];
+    if (slot[r] < 0) continue;
+    const int pos = atomicAdd(&fill[r], 1);
+    gb.members[(long long)slot[r] * kGroupMax + pos] = i;
+  }
+  __syncthreads();
+  // group blocks: B = diag(lambda) + G on the members, padded with distinct distant eigenvalues
+  for (int r = warp; r < n; r += nw) {
+    const int sl = slot[r];
+    if (sl < 0) continue;
+    const int sz = cnt[r];
+    const int* mem = gb.members + (long long)sl * kGroupMax;
+    cplx* B = gb.A + (long long)sl * kGroupMax * kGroupMax;
+    double off = 0.0;
+    for (int e = lane; e < kGroupMax * kGroupMax; e += 32) {
+      const int a = e % kGroupMax, b = e / kGroupMax;
+      cplx v = cmk(0.0, 0.0);
+      if (a < sz && b < sz) {
+        const Cx<float> g = G[mem[a] + (long long)mem[b] * n];
+        v = cmk((double)g.x, (double)g.y);
+        if (a == b) v = cadd(v, lam[mem[a]]);
+        else off = fmax(off, cabsv(v));
+      } else if (a == b) {
+        v = cmk((3.0 + a) * (scale + 1.0), 0.0);
+      }
+      B[e] = v;
+    }
+    for (int o = 16; o > 0; o >>= 1) off = fmax(off, __shfl_xor_sync(0xffffffffu, off, o));
+    if (lane == 0) gb.offmax[sl] = off / (scale > 0.0 ? scale : 1.0);
+  }
+  // first-order corrections between groups, and the new eigenvalues
+  for (long long e = tid; e < n2; e += blockDim.x) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    Cx<float> v = cxzero<float>();
+    if (i != j && label[i] != label[j]) {
+      const cplx dd = csub(d[j], d[i]);
+      if (dd.x != 0.0 || dd.y != 0.0) {
+        const Cx<float> g = G[e];
+        const cplx q = cdiv(cmk((double)g.x, (double)g.y), dd);
+        v = cxmk<float>((float)q.x, (float)q.y);
+      }
+    }
+    E[e] = v;
+  }
+  __syncthreads();
+  for (int i = tid; i < n; i += blockDim.x) lam[i] = d[i];
+  if (tid == 0 && s_fail) wb_flag(status + p / st_div, WB_ST_NOCONV);
+}
+
+// One CTA per used slot: rotate the group's columns of W by the block's eigenvectors and set
+// its eigenvalues. Eigenvectors of the padded block are told apart by their weight on the
+// group's own coordinates (the padding eigenvalues are far away, so the two sets separate).
+__global__ void __launch_bounds__(256) group_apply_kernel(int n, long long n2, GroupBufs gb, cplx* __restrict__ W_all,
+                                                          cplx* __restrict__ lam_all, int32_t* __restrict__ status,
+                                                          int st_div) {
+  __shared__ int sel[kGroupMax];
+  __shared__ int s_nsel;
+  __shared__ cplx S[kGroupMax * kGroupMax];
+  const int sl = blockIdx.x;
+  const int used = min(*gb.count, gb.cap);
+  if (sl >= used) return;
+  const int p = gb.pair[sl], sz = gb.size[sl], tid = threadIdx.x;
+  const int* mem = gb.members + (long long)sl * kGroupMax;
+  const cplx* V = gb.A + (long long)sl * kGroupMax * kGroupMax;    // normalised eigenvectors
+  const cplx* wv = gb.w + (long long)sl * kGroupMax;
+  if (tid < 32) {
+    double mass = 0.0;
+    for (int a = 0; a < sz; ++a) { const cplx v = V[a + tid * kGroupMax]; mass += v.x * v.x + v.y * v.y; }
+    const bool take = mass > 0.5 && isfinite(mass) && isfinite(wv[tid].x) && isfinite(wv[tid].y);
+    const unsigned m = __ballot_sync(0xffffffffu, take);
+    if (take) sel[__popc(m & ((1u << tid) - 1u))] = tid;
+    if (tid == 0) s_nsel = __popc(m);
+  }
+  __syncthreads();
+  if (s_nsel != sz) {
+    if (tid == 0) wb_flag(status + p / st_div, WB_ST_NOCONV);
+    return;
+  }
+  for (int e = tid; e < sz * sz; e += blockDim.x) {
+    const int a = e % sz, b = e / sz;
+    S[a + b * kGroupMax] = V[a + sel[b] * kGroupMax];
+  }
+  __syncthreads();
+  cplx* W = W_all + p * n2;
+  for (int r = tid; r < n; r += blockDim.x) {
+    cplx row[kGroupMax];
+    for (int a = 0; a < sz; ++a) row[a] = W[r + (long long)mem[a] * n];
+    for (int b = 0; b < sz; ++b) {
+      cplx acc = cmk(0.0, 0.0);
+      for (int a = 0; a < sz; ++a) acc = cadd(acc, cmul(row[a], S[a + b * kGroupMax]));
+      W[r + (long long)mem[b] * n] = acc;
+    }
+  }
+  if (tid < sz) lam_all[(long long)p * n + mem[tid]] = wv[sel[tid]];
+}
+
+// Work buffers of stage_b_newton. The FP32 buffers are the cascade's own (free until stage C).
+struct NewtonBufs {
+  Cx<float> *F1, *F2, *F3, *F4;   // (P, n, n): Omega^2/T/W32/LU(W), Z/W in FP32, X/E, G/W E
+  Cx<float> *wr, *tau;            // (P, n)
+  int* piv;                       // (P, n)
+  cplx* lam;                      // (P, n)
+};
+
+// Outputs as stage_b<df64>: bigW in Wd and bigV in Vd as double-float, w/q/X in FP64.
+// Wd, Vd, Om: (P, n, n) complex128-sized buffers (FP64 W, Omega^2 W, Omega^2 during the steps).
+void stage_b_newton(cudaStream_t s, int P, int N, const cplx* conv, const int* pair_layer, const int* pair_solve,
+                    const double* pair_thick, const double* wavelength, const double* kx, const double* ky,
+                    cplx* Wd, cplx* Vd, cplx* Om, NewtonBufs& nb, GroupBufs& gb, cplx* w, cplx* q, cplx* X,
+                    const double* c, const double* sn, int32_t* st, int st_div) {
+  const int n = 2 * N;
+  const long long n2 = (long long)n * n, NN = (long long)N * N, tot = (long long)P * n2;
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  using F = Cx<float>;
+  // FP32 eigenpairs
+  {
+    dim3 gr((N + 63) / 64, (N + 63) / 64, P * 4);
+    omega2_kernel<float><<<gr, 256, 0, s>>>(N, conv, 3 * NN, pair_layer, pair_solve, kx, ky, nb.F1, n2); note_launch();
+  }
+  geev_schur<float>(s, P, n, nb.F1, n, n2, nb.F2, n, n2, nb.wr, nb.tau, st, st_div);
+  trevc<float>(s, P, n, nb.F1, n, n2, nb.F3, n, n2);
+  gemm<float>(s, P, n, n, n, one, nb.F2, 1, n, n2, nb.F3, 1, n, n2, zero, nb.F1, 1, n, n2);
+  normalize_columns<float>(s, P, n, nb.F1, n, n2);
+  widen_kernel<<<nblk(tot, 256), 256, 0, s>>>(tot, nb.F1, Wd); note_launch();
+  widen_kernel<<<nblk((long long)P * n, 256), 256, 0, s>>>((long long)P * n, nb.wr, nb.lam); note_launch();
+  // FP64 operator
+  {
+    dim3 gr((N + 63) / 64, (N + 63) / 64, P * 4);
+    omega2_kernel<double><<<gr, 256, 0, s>>>(N, conv, 3 * NN, pair_layer, pair_solve, kx, ky, (Cx<double>*)Om, n2);
+    note_launch();
+  }
+  const size_t gsm = (size_t)n * (sizeof(cplx) + 5 * sizeof(int));
+  cudaFuncSetAttribute(group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm);
+  for (int it = 0; it < kNewtonSteps; ++it) {
+    if (it > 0) convert<double, float>(s, (const Cx<double>*)Wd, nb.F1, tot);
+    cudaMemcpyAsync(nb.F2, nb.F1, sizeof(F) * tot, cudaMemcpyDeviceToDevice, s);   // W in FP32 for W E
+    getrf<float>(s, P, n, nb.F1, n, n2, nb.piv, n, st, st_div);                    // LU of W in FP32
+    gemm<double>(s, P, n, n, n, one, (const Cx<double>*)Om, 1, n, n2, (const Cx<double>*)Wd, 1, n, n2, zero,
+                 (Cx<double>*)Vd, 1, n, n2);                                        // Omega^2 W
+    resid32_kernel<<<nblk(tot, 256), 256, 0, s>>>(tot, n, n2, Vd, Wd, nb.lam, nb.F4); note_launch();
+    getrs<float>(s, P, n, nb.F1, n, n2, nb.piv, n, nb.F4, n, n, n2, 0);            // G = W32^-1 R
+    group_init_kernel<<<nblk((long long)gb.cap * kGroupMax * kGroupMax, 256), 256, 0, s>>>(gb.cap, gb.A, gb.count);
+    note_launch();
+    group_kernel<<<P, 256, gsm, s>>>(n, nb.F4, nb.lam, nb.F3, gb, st, st_div); note_launch();
+    gemm<float>(s, P, n, n, n, one, nb.F2, 1, n, n2, nb.F3, 1, n, n2, zero, nb.F4, 1, n, n2);   // W E
+    accumulate_kernel<float, double><<<nblk(tot, 256), 256, 0, s>>>(tot, nb.F4, (Cx<double>*)Wd); note_launch();
+    // exact diagonalisation of the groups
+    Cx<double>* A = (Cx<double>*)gb.A;
+    Cx<double>* Zs = (Cx<double>*)gb.Z;
+    Cx<double>* Xs = (Cx<double>*)gb.X;
+    const long long b2 = (long long)kGroupMax * kGroupMax;
+    geev_schur<double>(s, gb.cap, kGroupMax, A, kGroupMax, b2, Zs, kGroupMax, b2, (Cx<double>*)gb.w,
+                       (Cx<double>*)gb.tau, nullptr, 1);
+    trevc<double>(s, gb.cap, kGroupMax, A, kGroupMax, b2, Xs, kGroupMax, b2);
+    gemm<double>(s, gb.cap, kGroupMax, kGroupMax, kGroupMax, one, Zs, 1, kGroupMax, b2, Xs, 1, kGroupMax, b2, zero,
+                 A, 1, kGroupMax, b2);
+    normalize_columns<double>(s, gb.cap, kGroupMax, A, kGroupMax, b2);
+    group_apply_kernel<<<gb.cap, 256, 0, s>>>(n, n2, gb, Wd, nb.lam, st, st_div); note_launch();
+    normalize_columns<double>(s, P, n, (Cx<double>*)Wd, n, n2);
+  }
+  // q, X, V and the s/p rotation in FP64, then the double-float form the cascade reads
+  modeq_kernel<double><<<P, 256, 0, s>>>(P, n, (const Cx<double>*)nb.lam, pair_solve, pair_thick, wavelength, w, q, X, st);
+  note_launch();
+  {
+    dim3 gr((N + 63) / 64, (n + 63) / 64, P * 2);
+    vmodes_kernel<double><<<gr, 256, 0, s>>>(N, conv, 3 * NN, pair_layer, pair_solve, kx, ky, (const Cx<double>*)Wd, q,
+                                             (Cx<double>*)Vd, n2);
+    note_launch();
+  }
+  sp_rotate_kernel<double><<<nblk((long long)P * N * n, 256), 256, 0, s>>>(P, N, pair_solve, c, sn, (Cx<double>*)Wd,
+                                                                          (Cx<double>*)Vd, n2);
+  note_launch();
+  to_df64_kernel<<<nblk(tot, 256), 256, 0, s>>>(tot, Wd); note_launch();
+  to_df64_kernel<<<nblk(tot, 256), 256, 0, s>>>(tot, Vd); note_launch();
+}
+
 // ------------------------------------------------------------------- stage C driver
 // Bottom-up reflections, top-down incidence pass and efficiencies, in precision RC.
 // bW, bV: (P, n, n) LU-factored bigW / bigV with pivots; X: FP64 (P, n).
@@ -830,18 +1175,6 @@ __global__ void td_cm_kernel(int Bc, int n, const Cx<R>* __restrict__ U1, const 
   const int rem = (int)(idx % (3LL * n));
   cm[b * f_bs + rem] = U1[b * 3LL * n + rem] - U2[b * 3LL * n + rem] + sig[b * f_bs + rem];
   gn[b * g_bs + rem] = Y[b * 6LL * n + 3LL * n + rem];
-}
-
-// dst += src over `count` complex entries (FP32 corrections into the double-float state)
-template <class RS, class RD>
-__global__ void accumulate_kernel(long long count, const Cx<RS>* __restrict__ src, Cx<RD>* __restrict__ dst) {
-  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= count) return;
-  const Cx<RS> a = src[i];
-  Cx<RD> d = dst[i];
-  d.x = d.x + RD((double)a.x);
-  d.y = d.y + RD((double)a.y);
-  dst[i] = d;
 }
 
 // per (solve, layer) pair: UW = [c+ + X c- | X c+ + c-], UV = [c+ - X c- | X c+ - c-]
@@ -1093,23 +1426,26 @@ size_t solve_chunk_bytes(int N, int L, int chunk, int precision) {
   A(16 * P * n2); A(16 * P * n2); A(16 * P * n2);                  // OM, Zb, Xv
   for (int k = 0; k < 5; ++k) A(16 * P * n);                        // wr, tau, w, q, X
   A(sizeof(int) * P * n); A(sizeof(int) * P * n); A(sizeof(int) * P * n);
-  const bool fp32c = (precision == 1 || precision == 2);           // FP32 cascade
+  const bool fp32c = (precision == 1 || precision == 2 || precision == 4);   // FP32 cascade
   const size_t ec = fp32c ? 8 : 16;                                // stage C element size
   if (fp32c) { A(ec * P * n2); A(ec * P * n2); A(ec * P * n2); }   // FP32 bigW, bigV, Mk
   A(ec * (P + chunk) * n2);
   A(ec * chunk * n2); A(ec * chunk * n2); A(ec * chunk * n2);
   A(sizeof(int) * chunk * n);
-  if (precision == 1) {                                            // per-layer A factors, refinement
+  if (precision == 1 || precision == 4) {                          // per-layer A factors, refinement
     A(ec * P * n2); A(sizeof(int) * P * n);
     b += RefineBufs::bytes(chunk, L, (int)n);
+    if (precision == 1) { A(16 * P * n); b += GroupBufs::bytes(kGroupSlotsPerPair * (int)P); }
   } else {
     for (int k = 0; k < 6; ++k) A(ec * chunk * n * 3);
   }
   return b;
 }
 
-// precision: 0 plain FP64; 1 mixed (df64 stage B, FP32 cascade refined against the df64
-// interface equations); 2 df64 stage B with the unrefined FP32 cascade; 3 df64 stage B and C
+// precision: 0 plain FP64; 1 mixed (FP32 eigen-solve with Newton steps against the FP64
+// operator, FP32 cascade refined against the double-float interface equations); 2 df64 stage B
+// with the unrefined FP32 cascade; 3 df64 stage B and C; 4 df64 stage B with the refined FP32
+// cascade
 int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int count, const SolveOut& out,
                 int precision) {
   const int N = (2 * d.hu + 1) * (2 * d.hv + 1), n = 2 * N, L = d.n_layers;
@@ -1165,6 +1501,35 @@ int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int co
                v[0], v[1], v[2], v[3], v[4], v[5]);
     return 0;
   }
+  if (precision == 1) {
+    // FP32 eigen-solve refined by Newton steps, FP32 cascade refined against the interface equations
+    using RC = float;
+    Cx<RC>* bW = ar.get<Cx<RC>>((size_t)P * n2);
+    Cx<RC>* bV = ar.get<Cx<RC>>((size_t)P * n2);
+    Cx<RC>* Mk = ar.get<Cx<RC>>((size_t)P * n2);
+    Cx<RC>* Rk = ar.get<Cx<RC>>((size_t)(P + Bc) * n2);
+    Cx<RC>* S1 = ar.get<Cx<RC>>((size_t)Bc * n2); Cx<RC>* S2 = ar.get<Cx<RC>>((size_t)Bc * n2);
+    Cx<RC>* S3 = ar.get<Cx<RC>>((size_t)Bc * n2);
+    int* pivS = ar.get<int>((size_t)Bc * n);
+    Cx<RC>* Ak = ar.get<Cx<RC>>((size_t)P * n2);
+    int* pivA = ar.get<int>((size_t)P * n);
+    RefineBufs rb;
+    if (!rb.carve(ar, Bc, L, n)) return -1;
+    cplx* lam = ar.get<cplx>((size_t)P * n);
+    GroupBufs gb;
+    if (!gb.carve(ar, kGroupSlotsPerPair * P) || !ar.ok()) return -1;
+    NewtonBufs nb{bW, bV, Mk, Rk, (Cx<float>*)wr, (Cx<float>*)taur, pivW, lam};
+    stage_b_newton(s, P, N, d.conv, pair_layer, pair_solve, pair_thick, wl, pv.kx, pv.ky, (cplx*)OMr, (cplx*)Zbr,
+                   (cplx*)Xvr, nb, gb, w, q, X, pv.c, pv.s, st, L);
+    Cx<df64>* OM = (Cx<df64>*)OMr; Cx<df64>* Zb = (Cx<df64>*)Zbr;
+    convert<df64, RC>(s, OM, bW, (long long)P * n2);
+    convert<df64, RC>(s, Zb, bV, (long long)P * n2);
+    getrf<RC>(s, P, n, bW, n, n2, pivW, n, st, L);
+    getrf<RC>(s, P, n, bV, n, n2, pivV, n, st, L);
+    stage_c_refined(s, Bc, L, N, OM, Zb, bW, bV, pivW, pivV, X, pv, d, first, out, st, Mk, pivM, Ak, pivA, Rk,
+                    S1, S2, S3, pivS, rb, kRefinePasses);
+    return 0;
+  }
   // mixed: stage B in df64
   {
     using R = df64;
@@ -1198,7 +1563,7 @@ int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int co
     convert<R, RC>(s, Zb, bV, (long long)P * n2);
     getrf<RC>(s, P, n, bW, n, n2, pivW, n, st, L);
     getrf<RC>(s, P, n, bV, n, n2, pivV, n, st, L);
-    if (precision == 1) {
+    if (precision == 4) {
       Cx<RC>* Ak = ar.get<Cx<RC>>((size_t)P * n2);
       int* pivA = ar.get<int>((size_t)P * n);
       RefineBufs rb;

@@ -266,7 +266,7 @@ def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument('--requests', type=int, default=256)
     ap.add_argument('--rate', type=float, default=20.0, help='Poisson arrival rate, requests/s')
-    ap.add_argument('--precision', default='double', choices=['double', 'mixed', 'mixed_fp32', 'mixed_df64'])
+    ap.add_argument('--precision', default='double', choices=['double', 'mixed', 'mixed_fp32', 'mixed_df64', 'mixed_df64_eig'])
     ap.add_argument('--workers', type=int, default=4)
     ap.add_argument('--max-batch', type=int, default=64)
     ap.add_argument('--budget-gb', type=float, default=120.0)
