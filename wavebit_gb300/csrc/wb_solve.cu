@@ -633,13 +633,16 @@ __global__ void to_df64_kernel(long long count, cplx* __restrict__ buf) {
 // rotated by its eigenvectors. Each step squares the error; two take FP32 eigenpairs to
 // FP64-class ones (|dR,T| ~1e-11 against the FP64 form at (12,12)).
 constexpr int kGroupMax = 32;          // largest group diagonalised exactly
-constexpr int kGroupSlotsPerPair = 32; // group slots per (solve, layer) pair
 constexpr double kCouple = 0.02;
 constexpr int kNewtonSteps = 2;
+constexpr double kScalarGroup = 1e-10;  // a group whose block is scalar to this (relative) keeps its basis
+constexpr double kParallel = 0.99;      // |cos| between eigenvectors above which a group keeps its basis
 
+// Group storage: 2-member groups (the TE/TM pairs of every order of a uniform layer, say) are
+// solved in closed form from a compact pool; larger groups go to padded 32 x 32 slots.
 struct GroupBufs {
-  int cap = 0;
-  int* count = nullptr;     // (1) slots used
+  int cap = 0, cap2 = 0;
+  int* count = nullptr;     // (2) slots used: [0] large groups, [1] 2-member groups
   int* pair = nullptr;      // (cap)
   int* size = nullptr;      // (cap)
   int* members = nullptr;   // (cap, 32)
@@ -649,21 +652,29 @@ struct GroupBufs {
   cplx* X = nullptr;        // (cap, 32, 32) eigenvectors of the Schur form
   cplx* w = nullptr;        // (cap, 32)
   cplx* tau = nullptr;      // (cap, 32)
-  bool carve(Arena& ar, int cap_) {
-    cap = cap_;
-    const size_t c = (size_t)cap, b2 = (size_t)kGroupMax * kGroupMax;
-    count = ar.get<int>(1); pair = ar.get<int>(c); size = ar.get<int>(c); members = ar.get<int>(c * kGroupMax);
+  int* pair2 = nullptr;     // (cap2)
+  int* mem2 = nullptr;      // (cap2, 2)
+  cplx* B2 = nullptr;       // (cap2, 4) blocks, column-major
+  double* scale2 = nullptr; // (cap2) scale of the pair
+  static int caps(int P, int n, int& cap2) { cap2 = P * (n / 2); return 16 * P + 1024; }
+  bool carve(Arena& ar, int P, int n) {
+    cap = caps(P, n, cap2);
+    const size_t c = (size_t)cap, b2 = (size_t)kGroupMax * kGroupMax, c2 = (size_t)cap2;
+    count = ar.get<int>(2); pair = ar.get<int>(c); size = ar.get<int>(c); members = ar.get<int>(c * kGroupMax);
     offmax = ar.get<double>(c);
     A = ar.get<cplx>(c * b2); Z = ar.get<cplx>(c * b2); X = ar.get<cplx>(c * b2);
     w = ar.get<cplx>(c * kGroupMax); tau = ar.get<cplx>(c * kGroupMax);
+    pair2 = ar.get<int>(c2); mem2 = ar.get<int>(2 * c2); B2 = ar.get<cplx>(4 * c2); scale2 = ar.get<double>(c2);
     return ar.ok();
   }
-  static size_t bytes(int cap_) {
-    const size_t c = (size_t)cap_, b2 = (size_t)kGroupMax * kGroupMax;
+  static size_t bytes(int P, int n) {
+    int c2i;
+    const size_t c = (size_t)caps(P, n, c2i), b2 = (size_t)kGroupMax * kGroupMax, c2 = (size_t)c2i;
     size_t b = 0;
     auto A_ = [&](size_t x) { b += (x + 255) & ~(size_t)255; };
-    A_(4); A_(4 * c); A_(4 * c); A_(4 * c * kGroupMax); A_(8 * c);
+    A_(8); A_(4 * c); A_(4 * c); A_(4 * c * kGroupMax); A_(8 * c);
     A_(16 * c * b2); A_(16 * c * b2); A_(16 * c * b2); A_(16 * c * kGroupMax); A_(16 * c * kGroupMax);
+    A_(4 * c2); A_(8 * c2); A_(64 * c2); A_(8 * c2);
     return b;
   }
 };
@@ -687,7 +698,7 @@ __global__ void resid32_kernel(long long total, int n, long long n2, const cplx*
 // every slot a diagonal 32 x 32 block with distinct entries, so unused slots converge at once
 __global__ void group_init_kernel(int cap, cplx* __restrict__ A, int* __restrict__ count) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (idx == 0) *count = 0;
+  if (idx == 0) { count[0] = 0; count[1] = 0; }
   if (idx >= (long long)cap * kGroupMax * kGroupMax) return;
   const int rem = (int)(idx % (kGroupMax * kGroupMax)), a = rem % kGroupMax, b = rem / kGroupMax;
   A[idx] = (a == b) ? cmk(1.0 + a, 0.0) : cmk(0.0, 0.0);
@@ -754,9 +765,16 @@ __global__ void __launch_bounds__(256) group_kernel(int n, const Cx<float>* __re
     atomicAdd(&cnt[r], 1);
   }
   __syncthreads();
+  // slots: -1 none; 2-member groups in the compact pool as -2 - index; larger ones padded
   for (int r = tid; r < n; r += blockDim.x) {
     if (label[r] != r || cnt[r] < 2) continue;
-    const int sl = atomicAdd(gb.count, 1);
+    if (cnt[r] == 2) {
+      const int sl = atomicAdd(&gb.count[1], 1);
+      if (sl < gb.cap2) { slot[r] = -2 - sl; gb.pair2[sl] = p; gb.scale2[sl] = scale; }
+      else s_fail = 1;
+      continue;
+    }
+    const int sl = atomicAdd(&gb.count[0], 1);
     if (sl < gb.cap && cnt[r] <= kGroupMax) {
       slot[r] = sl; gb.pair[sl] = p; gb.size[sl] = cnt[r];
     } else {
@@ -766,11 +784,24 @@ __global__ void __launch_bounds__(256) group_kernel(int n, const Cx<float>* __re
   __syncthreads();
   for (int i = tid; i < n; i += blockDim.x) {
     const int r = label[i];
-    if (slot[r] < 0) continue;
+    if (slot[r] == -1) continue;
     const int pos = atomicAdd(&fill[r], 1);
-    gb.members[(long long)slot[r] * kGroupMax + pos] = i;
+    if (slot[r] <= -2) gb.mem2[2LL * (-2 - slot[r]) + pos] = i;
+    else gb.members[(long long)slot[r] * kGroupMax + pos] = i;
   }
   __syncthreads();
+  for (int r = tid; r < n; r += blockDim.x) {
+    if (slot[r] > -2) continue;
+    const long long sl = -2 - slot[r];
+    const int a = gb.mem2[2 * sl], b = gb.mem2[2 * sl + 1];
+    const Cx<float> gaa = G[a + (long long)a * n], gba = G[b + (long long)a * n];
+    const Cx<float> gab = G[a + (long long)b * n], gbb = G[b + (long long)b * n];
+    cplx* B = gb.B2 + 4 * sl;
+    B[0] = cadd(lam[a], cmk((double)gaa.x, (double)gaa.y));
+    B[1] = cmk((double)gba.x, (double)gba.y);
+    B[2] = cmk((double)gab.x, (double)gab.y);
+    B[3] = cadd(lam[b], cmk((double)gbb.x, (double)gbb.y));
+  }
   // group blocks: B = diag(lambda) + G on the members, padded with distinct distant eigenvalues
   for (int r = warp; r < n; r += nw) {
     const int sl = slot[r];
@@ -824,8 +855,9 @@ __global__ void __launch_bounds__(256) group_apply_kernel(int n, long long n2, G
   __shared__ int s_nsel;
   __shared__ cplx S[kGroupMax * kGroupMax];
   const int sl = blockIdx.x;
-  const int used = min(*gb.count, gb.cap);
+  const int used = min(gb.count[0], gb.cap);
   if (sl >= used) return;
+  if (gb.offmax[sl] <= kScalarGroup) return;               // degenerate group: any basis is an eigenbasis
   const int p = gb.pair[sl], sz = gb.size[sl], tid = threadIdx.x;
   const int* mem = gb.members + (long long)sl * kGroupMax;
   const cplx* V = gb.A + (long long)sl * kGroupMax * kGroupMax;    // normalised eigenvectors
@@ -848,6 +880,25 @@ __global__ void __launch_bounds__(256) group_apply_kernel(int n, long long n2, G
     S[a + b * kGroupMax] = V[a + sel[b] * kGroupMax];
   }
   __syncthreads();
+  // an eigenvector set that is nearly dependent (a defective or noise-dominated block) would
+  // make W singular: keep the group's basis then
+  __shared__ int s_par;
+  if (tid == 0) s_par = 0;
+  __syncthreads();
+  for (int e = tid; e < sz * sz; e += blockDim.x) {
+    const int a = e % sz, b = e / sz;
+    if (a >= b) continue;
+    double na = 0.0, nb2 = 0.0;
+    cplx dot = cmk(0.0, 0.0);
+    for (int k = 0; k < sz; ++k) {
+      const cplx u = S[k + a * kGroupMax], v = S[k + b * kGroupMax];
+      na += u.x * u.x + u.y * u.y; nb2 += v.x * v.x + v.y * v.y;
+      dot = cadd(dot, cmul(cconj(u), v));
+    }
+    if (cabsv(dot) > kParallel * sqrt(na * nb2)) s_par = 1;
+  }
+  __syncthreads();
+  if (s_par) return;
   cplx* W = W_all + p * n2;
   for (int r = tid; r < n; r += blockDim.x) {
     cplx row[kGroupMax];
@@ -859,6 +910,44 @@ __global__ void __launch_bounds__(256) group_apply_kernel(int n, long long n2, G
     }
   }
   if (tid < sz) lam_all[(long long)p * n + mem[tid]] = wv[sel[tid]];
+}
+
+// One warp per 2-member group: B = [[a, b], [c, d]] has eigenvalues m +- r, m = (a + d)/2,
+// r = sqrt(((a - d)/2)^2 + b c), with the sign of r chosen so that s = (a - d)/2 + r is the larger
+// root difference; eigenvectors (s, c) and (b, -s) need no cancelling subtraction.
+__global__ void group2_apply_kernel(int n, long long n2, GroupBufs gb, cplx* __restrict__ W_all,
+                                    cplx* __restrict__ lam_all) {
+  const long long gw = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int used = min(gb.count[1], gb.cap2);
+  if (gw >= used) return;
+  const int p = gb.pair2[gw];
+  const int i = gb.mem2[2 * gw], j = gb.mem2[2 * gw + 1];
+  const cplx* B = gb.B2 + 4 * gw;
+  const cplx a = B[0], c = B[1], b = B[2], d = B[3];
+  const double sc = gb.scale2[gw] > 0.0 ? gb.scale2[gw] : 1.0;
+  const cplx m = cscale(cadd(a, d), 0.5), dl = cscale(csub(a, d), 0.5);
+  if (fmax(fmax(cabsv(b), cabsv(c)), cabsv(dl)) <= kScalarGroup * sc) return;   // degenerate: keep the basis
+  cplx r = csqrt_p(cadd(cmul(dl, dl), cmul(b, c)));
+  if (cabsv(cadd(dl, r)) < cabsv(csub(dl, r))) r = cneg(r);
+  const cplx sv = cadd(dl, r);
+  // v1 = (s, c) for m + r, v2 = (b, -s) for m - r
+  const double n1 = sqrt(cabs2(sv) + cabs2(c)), n2v = sqrt(cabs2(b) + cabs2(sv));
+  if (!(n1 > 0.0) || !(n2v > 0.0)) return;
+  const cplx v11 = cscale(sv, 1.0 / n1), v21 = cscale(c, 1.0 / n1);
+  const cplx v12 = cscale(b, 1.0 / n2v), v22 = cscale(cneg(sv), 1.0 / n2v);
+  const cplx dot = cadd(cmul(cconj(v11), v12), cmul(cconj(v21), v22));
+  if (!(cabsv(dot) <= kParallel)) return;                    // nearly defective: keep the basis
+  cplx* W = W_all + p * n2;
+  for (int row = lane; row < n; row += 32) {
+    const cplx wi = W[row + (long long)i * n], wj = W[row + (long long)j * n];
+    W[row + (long long)i * n] = cadd(cmul(wi, v11), cmul(wj, v21));
+    W[row + (long long)j * n] = cadd(cmul(wi, v12), cmul(wj, v22));
+  }
+  if (lane == 0) {
+    lam_all[(long long)p * n + i] = cadd(m, r);
+    lam_all[(long long)p * n + j] = csub(m, r);
+  }
 }
 
 // Work buffers of stage_b_newton. The FP32 buffers are the cascade's own (free until stage C).
@@ -923,6 +1012,7 @@ void stage_b_newton(cudaStream_t s, int P, int N, const cplx* conv, const int* p
                  A, 1, kGroupMax, b2);
     normalize_columns<double>(s, gb.cap, kGroupMax, A, kGroupMax, b2);
     group_apply_kernel<<<gb.cap, 256, 0, s>>>(n, n2, gb, Wd, nb.lam, st, st_div); note_launch();
+    group2_apply_kernel<<<nblk(32LL * gb.cap2, 256), 256, 0, s>>>(n, n2, gb, Wd, nb.lam); note_launch();
     normalize_columns<double>(s, P, n, (Cx<double>*)Wd, n, n2);
   }
   // q, X, V and the s/p rotation in FP64, then the double-float form the cascade reads
@@ -1435,7 +1525,7 @@ size_t solve_chunk_bytes(int N, int L, int chunk, int precision) {
   if (precision == 1 || precision == 4) {                          // per-layer A factors, refinement
     A(ec * P * n2); A(sizeof(int) * P * n);
     b += RefineBufs::bytes(chunk, L, (int)n);
-    if (precision == 1) { A(16 * P * n); b += GroupBufs::bytes(kGroupSlotsPerPair * (int)P); }
+    if (precision == 1) { A(16 * P * n); b += GroupBufs::bytes((int)P, (int)n); }
   } else {
     for (int k = 0; k < 6; ++k) A(ec * chunk * n * 3);
   }
@@ -1517,7 +1607,7 @@ int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int co
     if (!rb.carve(ar, Bc, L, n)) return -1;
     cplx* lam = ar.get<cplx>((size_t)P * n);
     GroupBufs gb;
-    if (!gb.carve(ar, kGroupSlotsPerPair * P) || !ar.ok()) return -1;
+    if (!gb.carve(ar, P, n) || !ar.ok()) return -1;
     NewtonBufs nb{bW, bV, Mk, Rk, (Cx<float>*)wr, (Cx<float>*)taur, pivW, lam};
     stage_b_newton(s, P, N, d.conv, pair_layer, pair_solve, pair_thick, wl, pv.kx, pv.ky, (cplx*)OMr, (cplx*)Zbr,
                    (cplx*)Xvr, nb, gb, w, q, X, pv.c, pv.s, st, L);
