@@ -28,6 +28,11 @@ void gemm(cudaStream_t s, int batch, int m, int n, int k, double2 alpha,
           const Cx<R>* B, long long b_rs, long long b_cs, long long b_bs,
           double2 beta, Cx<R>* C, long long c_rs, long long c_cs, long long c_bs);
 template <class R>
+void gemm_idx(cudaStream_t s, int batch, int m, int n, int k, double2 alpha,
+              const Cx<R>* A, long long a_rs, long long a_cs, long long a_bs, const int* a_idx,
+              const Cx<R>* B, long long b_rs, long long b_cs, long long b_bs,
+              double2 beta, Cx<R>* C, long long c_rs, long long c_cs, long long c_bs);
+template <class R>
 void getrf(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a_bs, int* ipiv, long long piv_bs,
            int32_t* status, int st_div);
 template <class R>

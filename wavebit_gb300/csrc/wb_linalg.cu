@@ -24,12 +24,13 @@ __global__ void __launch_bounds__(256) gemm_kernel(
     int m, int n, int k, double2 alpha_d,
     const Cx<R>* __restrict__ A, long long a_rs, long long a_cs, long long a_bs,
     const Cx<R>* __restrict__ B, long long b_rs, long long b_cs, long long b_bs,
-    double2 beta_d, Cx<R>* __restrict__ C, long long c_rs, long long c_cs, long long c_bs) {
+    double2 beta_d, Cx<R>* __restrict__ C, long long c_rs, long long c_cs, long long c_bs,
+    const int* __restrict__ a_idx) {
   using C_ = Cx<R>;
   __shared__ C_ sA[GK][GT + 1];
   __shared__ C_ sB[GK][GT + 1];
   const int bz = blockIdx.z;
-  A += bz * a_bs; B += bz * b_bs; C += bz * c_bs;
+  A += (a_idx ? (long long)a_idx[bz] : (long long)bz) * a_bs; B += bz * b_bs; C += bz * c_bs;
   const int row0 = blockIdx.x * GT, col0 = blockIdx.y * GT;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   C_ acc[4][4];
@@ -85,15 +86,84 @@ __global__ void __launch_bounds__(256) gemm_kernel(
   }
 }
 
+// Narrow products (C with at most 8 columns: right-hand-side blocks, residual products). One
+// output row per thread: every A element is loaded once, coalesced down its column, and used for
+// all NC columns of B, which sit in shared memory. The square-tile kernel above would spend most
+// of its 64-column tile on zeros here.
+constexpr int NW_ROWS = 128;
+template <class R, int NC>
+__global__ void __launch_bounds__(NW_ROWS) gemm_narrow_kernel(
+    int m, int nc, int k, double2 alpha_d, const Cx<R>* __restrict__ A, long long lda, long long a_bs,
+    const Cx<R>* __restrict__ B, long long ldb, long long b_bs, double2 beta_d, Cx<R>* __restrict__ C,
+    long long ldc, long long c_bs) {
+  using C_ = Cx<R>;
+  __shared__ C_ sB[32][NC];
+  const long long bz = blockIdx.y;
+  A += bz * a_bs; B += bz * b_bs; C += bz * c_bs;
+  const int row = blockIdx.x * NW_ROWS + threadIdx.x;
+  C_ acc[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) acc[c] = cxzero<R>();
+  for (int k0 = 0; k0 < k; k0 += 32) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * NC; e += NW_ROWS) {
+      const int kk = e % 32, c = e / 32;
+      sB[kk][c] = (k0 + kk < k && c < nc) ? B[(k0 + kk) + (long long)c * ldb] : cxzero<R>();
+    }
+    __syncthreads();
+    if (row < m) {
+      const int kend = min(32, k - k0);
+      for (int kk = 0; kk < kend; ++kk) {
+        const C_ a = A[row + (long long)(k0 + kk) * lda];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) acc[c] = cxfma(a, sB[kk][c], acc[c]);
+      }
+    }
+  }
+  if (row >= m) return;
+  const C_ alpha = cxfrom<R>(alpha_d), beta = cxfrom<R>(beta_d);
+  const bool zero_beta = (beta_d.x == 0.0 && beta_d.y == 0.0);
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    if (c >= nc) break;
+    C_* p = C + row + (long long)c * ldc;
+    *p = zero_beta ? alpha * acc[c] : alpha * acc[c] + beta * *p;
+  }
+}
+
 template <class R>
 void gemm(cudaStream_t s, int batch, int m, int n, int k, double2 alpha,
           const Cx<R>* A, long long a_rs, long long a_cs, long long a_bs,
           const Cx<R>* B, long long b_rs, long long b_cs, long long b_bs,
           double2 beta, Cx<R>* C, long long c_rs, long long c_cs, long long c_bs) {
   if (batch <= 0 || m <= 0 || n <= 0) return;
+  if (n <= 8 && k > 0 && a_rs == 1 && b_rs == 1 && c_rs == 1) {
+    dim3 g((m + NW_ROWS - 1) / NW_ROWS, batch);
+    if (n <= 3)
+      gemm_narrow_kernel<R, 3><<<g, NW_ROWS, 0, s>>>(m, n, k, alpha, A, a_cs, a_bs, B, b_cs, b_bs, beta, C, c_cs, c_bs);
+    else if (n <= 6)
+      gemm_narrow_kernel<R, 6><<<g, NW_ROWS, 0, s>>>(m, n, k, alpha, A, a_cs, a_bs, B, b_cs, b_bs, beta, C, c_cs, c_bs);
+    else
+      gemm_narrow_kernel<R, 8><<<g, NW_ROWS, 0, s>>>(m, n, k, alpha, A, a_cs, a_bs, B, b_cs, b_bs, beta, C, c_cs, c_bs);
+    note_launch();
+    return;
+  }
   dim3 grid((m + GT - 1) / GT, (n + GT - 1) / GT, batch);
   gemm_kernel<R><<<grid, 256, 0, s>>>(m, n, k, alpha, A, a_rs, a_cs, a_bs, B, b_rs, b_cs, b_bs, beta, C, c_rs,
-                                      c_cs, c_bs); note_launch();
+                                      c_cs, c_bs, nullptr); note_launch();
+}
+
+// As gemm, with the A operand of batch entry z at A + a_idx[z] * a_bs (a table of operands
+// shared by several entries, e.g. one convolution slot per layer for every solve).
+template <class R>
+void gemm_idx(cudaStream_t s, int batch, int m, int n, int k, double2 alpha,
+              const Cx<R>* A, long long a_rs, long long a_cs, long long a_bs, const int* a_idx,
+              const Cx<R>* B, long long b_rs, long long b_cs, long long b_bs,
+              double2 beta, Cx<R>* C, long long c_rs, long long c_cs, long long c_bs) {
+  if (batch <= 0 || m <= 0 || n <= 0) return;
+  dim3 grid((m + GT - 1) / GT, (n + GT - 1) / GT, batch);
+  gemm_kernel<R><<<grid, 256, 0, s>>>(m, n, k, alpha, A, a_rs, a_cs, a_bs, B, b_rs, b_cs, b_bs, beta, C, c_rs,
+                                      c_cs, c_bs, a_idx); note_launch();
 }
 
 // ----------------------------------------------------------------------- LU factorisation
@@ -446,6 +516,9 @@ void zset_identity(cudaStream_t s, int batch, int n, cplx* A, int lda, long long
   template void gemm<R>(cudaStream_t, int, int, int, int, double2, const Cx<R>*, long long, long long,     \
                         long long, const Cx<R>*, long long, long long, long long, double2, Cx<R>*,         \
                         long long, long long, long long);                                                 \
+  template void gemm_idx<R>(cudaStream_t, int, int, int, int, double2, const Cx<R>*, long long, long long, \
+                            long long, const int*, const Cx<R>*, long long, long long, long long, double2,  \
+                            Cx<R>*, long long, long long, long long);                                     \
   template void getrf<R>(cudaStream_t, int, int, Cx<R>*, int, long long, int*, long long, int32_t*, int); \
   template void getrs<R>(cudaStream_t, int, int, const Cx<R>*, int, long long, const int*, long long,      \
                          Cx<R>*, int, int, long long, int);                                               \

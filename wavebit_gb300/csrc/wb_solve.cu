@@ -621,7 +621,7 @@ __global__ void to_df64_kernel(long long count, cplx* __restrict__ buf) {
 // -------------------------------------- stage B of the mixed form: FP32 Schur + Newton steps
 // The eigenpairs are computed in FP32 (the stage_b pipeline on floats) and brought to FP64
 // accuracy by Newton steps on the FP64 operator. With W, Lambda the current pairs:
-//   R = Omega^2 W - W Lambda                       (FP64 GEMM)
+//   R = Omega^2 W - W Lambda                       (FP64 products from the slots)
 //   G = W^-1 R                                     (FP32 LU of W rounded to FP32)
 //   d_i = lambda_i + G_ii
 //   E_ij = G_ij / (d_j - d_i) for i, j in different groups, 0 otherwise
@@ -684,15 +684,45 @@ __global__ void widen_kernel(long long count, const Cx<float>* __restrict__ src,
   if (i < count) dst[i] = cmk((double)src[i].x, (double)src[i].y);
 }
 
-// R32 = FP32(AW - W diag(lambda))
-__global__ void resid32_kernel(long long total, int n, long long n2, const cplx* __restrict__ AW, const cplx* __restrict__ W,
-                               const cplx* __restrict__ lam, Cx<float>* __restrict__ R) {
+// Omega^2 W without forming Omega^2 (solve_2d.py:2377-2418 with epxy = epyx = 0): with
+// T = epx W_top, U = epy W_bot and Y = epz_i (Kx T + Ky U),
+//   (Omega^2 W)_top = Kx Y - T + Ky^2 W_top - Kx Ky W_bot
+//   (Omega^2 W)_bot = Ky Y - U - Kx Ky W_top + Kx^2 W_bot
+// (three N x N by N x n products per pair instead of four to form Omega^2 and one n x n product).
+__global__ void omw_s_kernel(long long total, int N, int n, const int* __restrict__ pair_solve,
+                             const double* __restrict__ kx, const double* __restrict__ ky, const cplx* __restrict__ T,
+                             const cplx* __restrict__ U, cplx* __restrict__ S) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= total) return;
+  const long long Nn = (long long)N * n;
+  const long long p = idx / Nn;
+  const int i = (int)((idx % Nn) % N);
+  const long long o = (long long)pair_solve[p] * N + i;
+  S[idx] = cadd(cscale(T[idx], kx[o]), cscale(U[idx], ky[o]));
+}
+
+// R32 = FP32(Omega^2 W - W diag(lambda)) from T, U, Y of omw_s_kernel's products
+__global__ void omw_resid_kernel(long long total, int N, int n, const int* __restrict__ pair_solve,
+                                 const double* __restrict__ kx, const double* __restrict__ ky,
+                                 const cplx* __restrict__ T, const cplx* __restrict__ U, const cplx* __restrict__ Y,
+                                 const cplx* __restrict__ W, const cplx* __restrict__ lam, Cx<float>* __restrict__ R) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= total) return;
+  const long long n2 = (long long)n * n, Nn = (long long)N * n;
   const long long p = idx / n2, rem = idx % n2;
-  const int j = (int)(rem / n);
-  const cplx r = csub(AW[idx], cmul(W[idx], lam[p * n + j]));
-  R[idx] = cxmk<float>((float)r.x, (float)r.y);
+  const int r = (int)(rem % n), j = (int)(rem / n);
+  const bool top = r < N;
+  const int i = top ? r : r - N;
+  const long long o = (long long)pair_solve[p] * N + i;
+  const double a = kx[o], b = ky[o];
+  const cplx* Wp = W + p * n2;
+  const cplx wt = Wp[i + (long long)j * n], wb = Wp[N + i + (long long)j * n];
+  const long long h = p * Nn + i + (long long)j * N;
+  cplx aw;
+  if (top) aw = cadd(csub(cscale(Y[h], a), T[h]), csub(cscale(wt, b * b), cscale(wb, a * b)));
+  else aw = cadd(csub(cscale(Y[h], b), U[h]), csub(cscale(wb, a * a), cscale(wt, a * b)));
+  const cplx res = csub(aw, cmul(Wp[r + (long long)j * n], lam[p * n + j]));
+  R[idx] = cxmk<float>((float)res.x, (float)res.y);
 }
 
 // every slot a diagonal 32 x 32 block with distinct entries, so unused slots converge at once
@@ -959,7 +989,7 @@ struct NewtonBufs {
 };
 
 // Outputs as stage_b<df64>: bigW in Wd and bigV in Vd as double-float, w/q/X in FP64.
-// Wd, Vd, Om: (P, n, n) complex128-sized buffers (FP64 W, Omega^2 W, Omega^2 during the steps).
+// Wd, Vd, Om: (P, n, n) complex128-sized buffers (FP64 W; scratch of the Omega^2 W products).
 void stage_b_newton(cudaStream_t s, int P, int N, const cplx* conv, const int* pair_layer, const int* pair_solve,
                     const double* pair_thick, const double* wavelength, const double* kx, const double* ky,
                     cplx* Wd, cplx* Vd, cplx* Om, NewtonBufs& nb, GroupBufs& gb, cplx* w, cplx* q, cplx* X,
@@ -979,21 +1009,29 @@ void stage_b_newton(cudaStream_t s, int P, int N, const cplx* conv, const int* p
   normalize_columns<float>(s, P, n, nb.F1, n, n2);
   widen_kernel<<<nblk(tot, 256), 256, 0, s>>>(tot, nb.F1, Wd); note_launch();
   widen_kernel<<<nblk((long long)P * n, 256), 256, 0, s>>>((long long)P * n, nb.wr, nb.lam); note_launch();
-  // FP64 operator
-  {
-    dim3 gr((N + 63) / 64, (N + 63) / 64, P * 4);
-    omega2_kernel<double><<<gr, 256, 0, s>>>(N, conv, 3 * NN, pair_layer, pair_solve, kx, ky, (Cx<double>*)Om, n2);
-    note_launch();
-  }
+  // scratch for Omega^2 W: T, U in Om; S in F3 (as complex128); Y in Vd
+  const long long Nn = (long long)N * n, totN = (long long)P * Nn;
+  Cx<double>* Tm = (Cx<double>*)Om;
+  Cx<double>* Um = Tm + totN;
+  Cx<double>* Sm = (Cx<double>*)nb.F3;
+  Cx<double>* Ym = (Cx<double>*)Vd;
+  const Cx<double>* cv = (const Cx<double>*)conv;
   const size_t gsm = (size_t)n * (sizeof(cplx) + 5 * sizeof(int));
   cudaFuncSetAttribute(group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm);
   for (int it = 0; it < kNewtonSteps; ++it) {
     if (it > 0) convert<double, float>(s, (const Cx<double>*)Wd, nb.F1, tot);
     cudaMemcpyAsync(nb.F2, nb.F1, sizeof(F) * tot, cudaMemcpyDeviceToDevice, s);   // W in FP32 for W E
     getrf<float>(s, P, n, nb.F1, n, n2, nb.piv, n, st, st_div);                    // LU of W in FP32
-    gemm<double>(s, P, n, n, n, one, (const Cx<double>*)Om, 1, n, n2, (const Cx<double>*)Wd, 1, n, n2, zero,
-                 (Cx<double>*)Vd, 1, n, n2);                                        // Omega^2 W
-    resid32_kernel<<<nblk(tot, 256), 256, 0, s>>>(tot, n, n2, Vd, Wd, nb.lam, nb.F4); note_launch();
+    const Cx<double>* Wc = (const Cx<double>*)Wd;
+    gemm_idx<double>(s, P, N, n, N, one, cv, 1, N, 3 * NN, pair_layer, Wc, 1, n, n2, zero, Tm, 1, N, Nn);
+    gemm_idx<double>(s, P, N, n, N, one, cv + NN, 1, N, 3 * NN, pair_layer, Wc + N, 1, n, n2, zero, Um, 1, N, Nn);
+    omw_s_kernel<<<nblk(totN, 256), 256, 0, s>>>(totN, N, n, pair_solve, kx, ky, (const cplx*)Tm, (const cplx*)Um,
+                                                 (cplx*)Sm);
+    note_launch();
+    gemm_idx<double>(s, P, N, n, N, one, cv + 2 * NN, 1, N, 3 * NN, pair_layer, Sm, 1, N, Nn, zero, Ym, 1, N, Nn);
+    omw_resid_kernel<<<nblk(tot, 256), 256, 0, s>>>(tot, N, n, pair_solve, kx, ky, (const cplx*)Tm, (const cplx*)Um,
+                                                    (const cplx*)Ym, Wd, nb.lam, nb.F4);
+    note_launch();
     getrs<float>(s, P, n, nb.F1, n, n2, nb.piv, n, nb.F4, n, n, n2, 0);            // G = W32^-1 R
     group_init_kernel<<<nblk((long long)gb.cap * kGroupMax * kGroupMax, 256), 256, 0, s>>>(gb.cap, gb.A, gb.count);
     note_launch();
