@@ -86,6 +86,29 @@ def test_a_poisoned_request_fails_alone():
     assert all(res[r.id].error is None for r in mates)
 
 
+class FallbackBackend(FakeBackend):
+    """Fails the listed requests' first attempt (status 2); their retry, run in the fallback
+    precision, succeeds."""
+    fallback_precision = 'mixed_df64_eig'
+
+    def results(self, tok):
+        ids = np.array([r.id for r in tok['reqs']], float)
+        st = np.array([2 if (r.id in self.poisoned and not r.retry) else 0 for r in tok['reqs']], np.int32)
+        return ids[:, None], 1 - ids[:, None], st
+
+
+def test_a_failed_mixed_solve_is_solved_again_in_the_fallback_precision():
+    clock = FakeClock()
+    be = FallbackBackend(clock, limit=4, poisoned={5, 17})
+    res, st = Server(be, n_workers=2, max_batch=8, clock=clock, idle_sleep=0).run(_reqs(30))
+    assert st['completed'] == 30 and st['errors'] == 0 and st['fallbacks'] == 2
+    for rid in (5, 17):
+        assert res[rid].error is None and float(res[rid].R[0]) == rid
+    # a retry runs in a batch of retries only
+    for tok in be.batches:
+        assert len({r.retry for r in tok['reqs']}) == 1
+
+
 def test_requests_that_cannot_fit_are_refused_not_queued():
     clock = FakeClock()
     be = FakeBackend(clock, refuse={((2, 2), 2)})

@@ -300,6 +300,22 @@ class Prepared:
                                  handle=self.handle)
         R, T, status = out[:3]
         st = status.cpu().numpy()
+        fallback = np.nonzero(st & ~_lib.WB_ST_GRAZING)[0] if self.precision == 'mixed' else np.zeros(0, int)
+        if fallback.size:
+            # solves the mixed form could not finish (a near-degenerate group too large for its
+            # Newton step, say) are solved again with the double-float eigen-solve
+            idx = torch.as_tensor(fallback, device=R.device)
+            sub = engine.BatchInputs(np.tile(np.arange(L), (len(fallback), 1)),
+                                     np.tile(r['thickness'], (len(fallback), 1)), np.asarray(wl)[fallback],
+                                     np.tile(r['period'], (len(fallback), 1)), np.full(len(fallback), r['theta']),
+                                     np.full(len(fallback), r['phi']), np.full(len(fallback), r['eps_top']),
+                                     np.full(len(fallback), r['eps_bot']), np.tile(r['pol'], (len(fallback), 1)))
+            out2 = engine.solve_batch(conv, sub, precision='mixed_df64_eig', amplitudes=amplitudes,
+                                      handle=self.handle)
+            R[idx], T[idx], status[idx] = out2[0], out2[1], out2[2]
+            if amplitudes:
+                out[3][idx] = out2[3]
+            st = status.cpu().numpy()
         bad = st & ~_lib.WB_ST_GRAZING
         if np.any(bad & _lib.WB_ST_SINGULAR):
             raise NumericalError('a factorization met an exact zero pivot', code='rcwa.singular')
@@ -307,7 +323,8 @@ class Prepared:
             raise NumericalError('the solve produced non-finite results', code='rcwa.nonfinite')
         diag = {'solve_path': ('2d',) * B, 'effective_wavelengths': tuple(wl),
                 'grazing': tuple(bool(s & _lib.WB_ST_GRAZING) for s in st),
-                'status': st, 'precision': self.precision}
+                'status': st, 'precision': self.precision,
+                'fallback_solves': tuple(int(i) for i in fallback)}
         return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]), status, wl, diag,
                       out[3] if amplitudes else None)
 

@@ -34,7 +34,7 @@ Result = collections.namedtuple('Result', 'id R T status error latency')
 
 class Request:
     __slots__ = ('id', 'eps', 'thickness', 'orders', 'period', 'wavelength', 'theta', 'phi', 'pol',
-                 'eps_top', 'eps_bot', 'arrival', 'start', 'layer_keys')
+                 'eps_top', 'eps_bot', 'arrival', 'start', 'layer_keys', 'retry')
 
     def __init__(self, id, eps, thickness, orders, period, wavelength, theta, phi, pol, eps_top=1.0,
                  eps_bot=1.0, arrival=0.0):
@@ -52,6 +52,7 @@ class Request:
         self.arrival = float(arrival)
         self.start = None
         self.layer_keys = None
+        self.retry = False
 
     @property
     def bucket(self):
@@ -81,6 +82,10 @@ class GpuBackend:
         self.device = torch.device('cuda', device)
         torch.cuda.set_device(self.device)
         self.precision = precision
+        # a mixed-form solve that reports a failure (a group of near-degenerate modes too large
+        # for the Newton step, an FP32 QR that did not converge) is solved again with the
+        # double-float eigen-solve
+        self.fallback_precision = 'mixed_df64_eig' if precision == 'mixed' else None
         self.per_worker = int(hbm_budget // (n_workers + 1))          # one share for the conv cache
         self.cache_budget = int(hbm_budget - n_workers * self.per_worker)
         self.handles = [_lib.Handle(device, self.per_worker) for _ in range(n_workers)]
@@ -147,7 +152,8 @@ class GpuBackend:
                                      [r.period for r in reqs], [r.theta for r in reqs], [r.phi for r in reqs],
                                      [r.eps_top for r in reqs], [r.eps_bot for r in reqs],
                                      [_pol_pair(r.pol) for r in reqs], device=self.device)
-            R, T, st = engine.solve_batch(conv, inp, precision=self.precision, handle=self.handles[worker])
+            prec = self.fallback_precision if reqs[0].retry and self.fallback_precision else self.precision
+            R, T, st = engine.solve_batch(conv, inp, precision=prec, handle=self.handles[worker])
             Rh = torch.empty(R.shape, dtype=R.dtype, pin_memory=True)
             Th = torch.empty(T.shape, dtype=T.dtype, pin_memory=True)
             sh = torch.empty(st.shape, dtype=st.dtype, pin_memory=True)
@@ -191,6 +197,8 @@ class Server:
         nxt = 0
         t0 = self.clock()
         busy_batches = 0
+        fallbacks = 0
+        can_retry = getattr(self.backend, 'fallback_precision', None) is not None
 
         def now():
             return self.clock() - t0
@@ -214,6 +222,13 @@ class Server:
                     tdone = now()
                     for i, r in enumerate(batch):
                         err = None if (int(st[i]) & ~8) == 0 else f'solve status {int(st[i])}'
+                        if err and can_retry and not r.retry:
+                            # once more in the fallback precision, in a bucket of its own; its
+                            # arrival time puts it at the head of the queue
+                            r.retry = True
+                            fallbacks += 1
+                            waiting.setdefault(r.bucket + ('fallback',), collections.deque()).append(r)
+                            continue
                         lat = tdone - (r.arrival if realtime else 0.0)
                         results[r.id] = Result(r.id, None if err else Rr[i], None if err else Tr[i],
                                                int(st[i]), err, lat)
@@ -244,7 +259,7 @@ class Server:
         errs = collections.Counter(r.status for r in results.values() if r.error is not None)
         stats = {'requests': len(reqs), 'completed': ok, 'errors': len(reqs) - ok,
                  'error_status_counts': {str(k): v for k, v in sorted(errs.items())}, 'wall_s': wall,
-                 'throughput_rps': ok / wall if wall > 0 else 0.0, 'batches': busy_batches,
+                 'throughput_rps': ok / wall if wall > 0 else 0.0, 'batches': busy_batches, 'fallbacks': fallbacks,
                  'p50_latency_s': float(np.percentile(lat, 50)) if ok else None,
                  'p99_latency_s': float(np.percentile(lat, 99)) if ok else None}
         return results, stats
