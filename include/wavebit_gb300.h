@@ -113,6 +113,20 @@ int wb_solve_batch(wb_handle* h, int B, int L, int hu, int hv, const wb_complex*
                    double* R, double* T, wb_complex* amps, int32_t* status, int precision,
                    void* stream);
 
+/* Stage C alone: the S-matrix cascade and the efficiencies of B solves from given modes, e.g.
+ * eigenpairs kept on the device from earlier wb_layer_modes calls. Every array is a device pointer.
+ *   W, V (B*L, 2N, 2N) column-major and q (B*L, 2N) of the (solve, layer) pairs p = b*L + l, as
+ *   wb_layer_modes returns them (computed with the order wavevectors of the same wavelength,
+ *   period and angles); thickness (B, L); the other arrays as in wb_solve_batch.
+ * precision: WB_PRECISION_FP64 (FP64 cascade) or WB_PRECISION_MIXED (FP32 cascade refined against
+ * the given modes). Reference: rcwa/_engine/scattering.py:116-200, 1272-1293 (_ab_matrices,
+ * _s_layer, redheffer_star, the SMM cascade) and :907-994; solve_2d.py:2584-2616 (sp_modes_2d). */
+int wb_smm_solve(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* W, const wb_complex* V,
+                 const wb_complex* q, const double* thickness, const double* wavelength, const double* period,
+                 const double* theta, const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,
+                 const wb_complex* pol, double* R, double* T, wb_complex* amps, int32_t* status, int precision,
+                 void* stream);
+
 /* The same solve from HOST buffers: rasters in, efficiencies out. Copies inputs to the
  * device, assembles the L layers (stage A), solves the B problems, copies R, T and status
  * back and synchronises. eps: host (L, ny, nx); the other arrays as in wb_solve_batch but in

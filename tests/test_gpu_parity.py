@@ -237,3 +237,31 @@ def test_double_float_form_survives_the_fp32_exponent_range():
         torch.cuda.synchronize()
         assert int(sd.item()) & ~8 == 0 and int(sm.item()) & ~8 == 0, (r.id, int(sm.item()))
         assert float((Rd - Rm).abs().max()) <= 1e-9 and float((Td - Tm).abs().max()) <= 1e-9, r.id
+
+
+@pytest.mark.parametrize('precision,tol', [('double', 1e-12), ('mixed', 1e-9)])
+def test_smm_solve_from_layer_modes_matches_the_fused_solve(precision, tol):
+    """Stage C alone (wb_smm_solve) on the modes of wb_layer_modes gives the fused solve's
+    efficiencies: the seam through which eigenpairs kept on the device are reused."""
+    E = _engine()
+    from wavebit_gb300.adjoint import ports
+    rng = np.random.default_rng(31)
+    eps = np.stack([_rast(rng, 20, 20), _rast(rng, 20, 20), np.full((20, 20), 2.25 + 0.05j)])
+    hu, hv, B, L = 3, 4, 5, 3
+    wl = np.linspace(500, 900, B)
+    th = np.array([120.0, 240.0, 60.0])
+    period = (800.0, 900.0)
+    conv = E.assemble(torch.as_tensor(eps, device='cuda'), hu, hv)
+    inp = E.BatchInputs(np.tile(np.arange(L), (B, 1)), np.tile(th, (B, 1)), wl, np.tile(period, (B, 1)),
+                        np.full(B, 0.3), np.full(B, 0.5), np.ones(B), np.full(B, 2.25), np.tile([0.6, 0.8], (B, 1)))
+    R0, T0, st0 = E.solve_batch(conv, inp, precision='double')
+    kx, ky = [], []
+    for b in range(B):
+        pv = ports(float(wl[b]), period, 0.3, 0.5, 1.0, 2.25, hu, hv, 'cpu')
+        for _ in range(L):
+            kx.append(pv['kx'].numpy()); ky.append(pv['ky'].numpy())
+    w, q, W, V, st = E.layer_modes(conv, np.tile(np.arange(L), B), np.array(kx), np.array(ky))
+    R, T, st2 = E.smm_solve(W, V, q, inp, hu, hv, precision=precision)
+    torch.cuda.synchronize()
+    assert not (st2.cpu().numpy() & ~8).any()
+    assert float((R - R0).abs().max()) <= tol and float((T - T0).abs().max()) <= tol

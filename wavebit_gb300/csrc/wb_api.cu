@@ -194,6 +194,36 @@ int wb_solve_batch(wb_handle* h, int B, int L, int hu, int hv, const wb_complex*
   return cuda_check("wb_solve_batch");
 }
 
+int wb_smm_solve(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* W, const wb_complex* V,
+                 const wb_complex* q, const double* thickness, const double* wavelength, const double* period,
+                 const double* theta, const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,
+                 const wb_complex* pol, double* R, double* T, wb_complex* amps, int32_t* status, int precision,
+                 void* stream) {
+  if (!h || !W || !V || !q || !thickness || !wavelength || !period || !theta || !phi || !eps_top || !eps_bot ||
+      !pol || !R || !T || !status)
+    return fail(WB_E_INVALID, "wb_smm_solve: NULL argument");
+  if (B <= 0 || L <= 0 || !valid_orders(hu, hv)) return fail(WB_E_INVALID, "wb_smm_solve: bad sizes B=%d L=%d", B, L);
+  if (precision != WB_PRECISION_FP64 && precision != WB_PRECISION_MIXED)
+    return fail(WB_E_INVALID, "wb_smm_solve: precision %d (FP64 or MIXED)", precision);
+  cudaSetDevice(h->device);
+  const int N = (2 * hu + 1) * (2 * hv + 1);
+  int chunk = B;
+  while (chunk > 1 && wb::smm_chunk_bytes(N, L, chunk, precision) > h->budget) chunk = (chunk + 1) / 2;
+  int rc = reserve(h, wb::smm_chunk_bytes(N, L, chunk, precision));
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaMemsetAsync(status, 0, sizeof(int32_t) * B, s);
+  wb::SolveDesc d{B, L, hu, hv, nullptr, nullptr, thickness, wavelength, period, theta, phi, (const cplx*)eps_top,
+                  (const cplx*)eps_bot, (const cplx*)pol};
+  wb::SolveOut o{R, T, (cplx*)amps, status};
+  for (int first = 0; first < B; first += chunk) {
+    int count = std::min(chunk, B - first);
+    if (wb::smm_chunk(s, h->arena, d, (const cplx*)W, (const cplx*)V, (const cplx*)q, first, count, o, precision) != 0)
+      return fail(WB_E_NOMEM, "wb_smm_solve: arena exhausted for a chunk of %d", count);
+  }
+  return cuda_check("wb_smm_solve");
+}
+
 int wb_solve_host(wb_handle* h, int B, int L, int ny, int nx, int hu, int hv,
                   const wb_complex* eps, const int32_t* layer_index, const double* thickness,
                   const double* wavelength, const double* period, const double* theta,

@@ -63,5 +63,8 @@ void layer_modes(cudaStream_t s, Arena& ar, int n_pairs, int N, const cplx* conv
 void regroup_slots(cudaStream_t s, int L, int N, const cplx* planes, cplx* out);
 int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int count, const SolveOut& out,
                 int precision);
+size_t smm_chunk_bytes(int N, int L, int chunk, int precision);
+int smm_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* W, const cplx* V, const cplx* q,
+              int first, int count, const SolveOut& out, int precision);
 
 }  // namespace wb

@@ -562,7 +562,7 @@ __global__ void pairs_kernel(int B, int L, const int* __restrict__ layer_index, 
                              int* __restrict__ pair_layer, int* __restrict__ pair_solve, double* __restrict__ pair_thick) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= B * L) return;
-  pair_layer[p] = layer_index[p];
+  pair_layer[p] = layer_index ? layer_index[p] : 0;
   pair_solve[p] = p / L;
   pair_thick[p] = thick[p];
 }
@@ -1706,6 +1706,104 @@ int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int co
     stage_c<RC>(s, ar, Bc, L, N, bW, bV, pivW, pivV, X, pv, d, first, out, st, Mk, pivM, Rk, S1, S2, S3, pivS,
                 v[0], v[1], v[2], v[3], v[4], v[5]);
   }
+  return 0;
+}
+
+// ----------------------------------------------------- stage C door (wb_smm_solve)
+// The cascade and the efficiencies of B solves from given modes: W, V (P, n, n) and q (P, n) of
+// every (solve, layer) pair as wb_layer_modes returns them (before the s/p rotation).
+__global__ void xq_kernel(int P, int n, const cplx* __restrict__ q, const int* __restrict__ pair_solve,
+                          const double* __restrict__ thick, const double* __restrict__ wavelength,
+                          cplx* __restrict__ X) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)P * n) return;
+  const long long p = idx / n;
+  const double k0 = 2.0 * 3.141592653589793 / wavelength[pair_solve[p]];
+  X[idx] = cexp_(cscale(q[idx], -k0 * thick[p]));
+}
+
+size_t smm_chunk_bytes(int N, int L, int chunk, int precision) {
+  return solve_chunk_bytes(N, L, chunk, precision == 0 ? 0 : 4);
+}
+
+// precision: 0 FP64 cascade; otherwise the FP32 cascade refined against the modes (double-float)
+int smm_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* Wm, const cplx* Vm, const cplx* qm,
+              int first, int count, const SolveOut& out, int precision) {
+  const int N = (2 * d.hu + 1) * (2 * d.hv + 1), n = 2 * N, L = d.n_layers;
+  const long long n2 = (long long)n * n;
+  const int Bc = count, P = Bc * L;
+  int32_t* st = out.status + first;
+  ar.reset();
+  PortVectors pv;
+  pv.kx = ar.get<double>((size_t)Bc * N); pv.ky = ar.get<double>((size_t)Bc * N);
+  pv.c = ar.get<double>((size_t)Bc * N); pv.s = ar.get<double>((size_t)Bc * N);
+  pv.kz_top = ar.get<cplx>((size_t)Bc * N); pv.kz_bot = ar.get<cplx>((size_t)Bc * N);
+  pv.wg = ar.get<cplx>((size_t)Bc * n); pv.vg = ar.get<cplx>((size_t)Bc * n);
+  pv.r11 = ar.get<cplx>((size_t)Bc * n); pv.r12 = ar.get<cplx>((size_t)Bc * n);
+  pv.r21 = ar.get<cplx>((size_t)Bc * n); pv.r22 = ar.get<cplx>((size_t)Bc * n);
+  pv.t11 = ar.get<cplx>((size_t)Bc * n); pv.t21 = ar.get<cplx>((size_t)Bc * n);
+  pv.nt = ar.get<cplx>(Bc); pv.nb = ar.get<cplx>(Bc);
+  int* pair_layer = ar.get<int>(P);
+  int* pair_solve = ar.get<int>(P);
+  double* pair_thick = ar.get<double>(P);
+  cplx* OM = ar.get<cplx>((size_t)P * n2);
+  cplx* Zb = ar.get<cplx>((size_t)P * n2);
+  cplx* Xv = ar.get<cplx>((size_t)P * n2);
+  cplx* X = ar.get<cplx>((size_t)P * n);
+  int* pivW = ar.get<int>((size_t)P * n);
+  int* pivV = ar.get<int>((size_t)P * n);
+  int* pivM = ar.get<int>((size_t)P * n);
+  if (!ar.ok()) return -1;
+  ports_kernel<<<Bc, 128, 0, s>>>(Bc, d.hu, d.hv, d.wavelength + first, d.period + 2 * first, d.theta + first,
+                                  d.phi + first, d.eps_top + first, d.eps_bot + first, pv); note_launch();
+  pairs_kernel<<<nblk(P, 128), 128, 0, s>>>(Bc, L, nullptr, d.thickness + (long long)first * L, pair_layer,
+                                            pair_solve, pair_thick);
+  note_launch();
+  const long long off = (long long)first * L;
+  cudaMemcpyAsync(OM, Wm + off * n2, sizeof(cplx) * P * n2, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(Zb, Vm + off * n2, sizeof(cplx) * P * n2, cudaMemcpyDeviceToDevice, s);
+  xq_kernel<<<nblk((long long)P * n, 256), 256, 0, s>>>(P, n, qm + off * n, pair_solve, pair_thick, d.wavelength + first, X);
+  note_launch();
+  sp_rotate_kernel<double><<<nblk((long long)P * N * n, 256), 256, 0, s>>>(P, N, pair_solve, pv.c, pv.s,
+                                                                          (Cx<double>*)OM, (Cx<double>*)Zb, n2);
+  note_launch();
+  if (precision == 0) {
+    using R = double;
+    getrf<R>(s, P, n, (Cx<R>*)OM, n, n2, pivW, n, st, L);
+    getrf<R>(s, P, n, (Cx<R>*)Zb, n, n2, pivV, n, st, L);
+    Cx<R>* Rk = ar.get<Cx<R>>((size_t)(P + Bc) * n2);
+    Cx<R>* S1 = ar.get<Cx<R>>((size_t)Bc * n2); Cx<R>* S2 = ar.get<Cx<R>>((size_t)Bc * n2);
+    Cx<R>* S3 = ar.get<Cx<R>>((size_t)Bc * n2);
+    int* pivS = ar.get<int>((size_t)Bc * n);
+    Cx<R>* v[6];
+    for (int k = 0; k < 6; ++k) v[k] = ar.get<Cx<R>>((size_t)Bc * n * 3);
+    if (!ar.ok()) return -1;
+    stage_c<R>(s, ar, Bc, L, N, (Cx<R>*)OM, (Cx<R>*)Zb, pivW, pivV, X, pv, d, first, out, st, (Cx<R>*)Xv, pivM, Rk,
+               S1, S2, S3, pivS, v[0], v[1], v[2], v[3], v[4], v[5]);
+    return 0;
+  }
+  using RC = float;
+  const long long tot = (long long)P * n2;
+  to_df64_kernel<<<nblk(tot, 256), 256, 0, s>>>(tot, OM); note_launch();
+  to_df64_kernel<<<nblk(tot, 256), 256, 0, s>>>(tot, Zb); note_launch();
+  Cx<RC>* bW = ar.get<Cx<RC>>((size_t)P * n2);
+  Cx<RC>* bV = ar.get<Cx<RC>>((size_t)P * n2);
+  Cx<RC>* Mk = ar.get<Cx<RC>>((size_t)P * n2);
+  Cx<RC>* Rk = ar.get<Cx<RC>>((size_t)(P + Bc) * n2);
+  Cx<RC>* S1 = ar.get<Cx<RC>>((size_t)Bc * n2); Cx<RC>* S2 = ar.get<Cx<RC>>((size_t)Bc * n2);
+  Cx<RC>* S3 = ar.get<Cx<RC>>((size_t)Bc * n2);
+  int* pivS = ar.get<int>((size_t)Bc * n);
+  Cx<RC>* Ak = ar.get<Cx<RC>>((size_t)P * n2);
+  int* pivA = ar.get<int>((size_t)P * n);
+  RefineBufs rb;
+  if (!rb.carve(ar, Bc, L, n) || !ar.ok()) return -1;
+  Cx<df64>* OMd = (Cx<df64>*)OM; Cx<df64>* Zbd = (Cx<df64>*)Zb;
+  convert<df64, RC>(s, OMd, bW, tot);
+  convert<df64, RC>(s, Zbd, bV, tot);
+  getrf<RC>(s, P, n, bW, n, n2, pivW, n, st, L);
+  getrf<RC>(s, P, n, bV, n, n2, pivV, n, st, L);
+  stage_c_refined(s, Bc, L, N, OMd, Zbd, bW, bV, pivW, pivV, X, pv, d, first, out, st, Mk, pivM, Ak, pivA, Rk,
+                  S1, S2, S3, pivS, rb, kRefinePasses);
   return 0;
 }
 

@@ -147,6 +147,31 @@ def solve_batch(conv, inp, precision='double', amplitudes=False, handle=None, ou
     return res + ((amps,) if amplitudes else ())
 
 
+def smm_solve(W, V, q, inp, hu, hv, precision='double', amplitudes=False, handle=None):
+    """Stage C from given modes (wb_smm_solve). ``W, V`` (B*L, n, n) and ``q`` (B*L, n) in the
+    natural orientation :func:`layer_modes` returns, pair ``p = b*L + l``; ``inp`` the batch's
+    per-solve parameters (its ``layer_index`` is not used). Returns ``(R, T, status[, amps])``."""
+    dev = W.device
+    N = n_orders(hu, hv)
+    B, L = inp.B, inp.L
+    Wc = W.transpose(-1, -2).contiguous()          # back to the column-major buffers of the ABI
+    Vc = V.transpose(-1, -2).contiguous()
+    qc = q.contiguous()
+    R = torch.empty((B, 3, N), dtype=torch.float64, device=dev)
+    T = torch.empty_like(R)
+    status = torch.zeros(B, dtype=torch.int32, device=dev)
+    amps = torch.empty((B, 3, 4, N), dtype=torch.complex128, device=dev) if amplitudes else None
+    h = handle or _lib.handle(dev.index or 0)
+    _lib.check(h.lib.wb_smm_solve(
+        h.h, B, L, hu, hv, Wc.data_ptr(), Vc.data_ptr(), qc.data_ptr(), inp.thickness.data_ptr(),
+        inp.wavelength.data_ptr(), inp.period.data_ptr(), inp.theta.data_ptr(), inp.phi.data_ptr(),
+        inp.eps_top.data_ptr(), inp.eps_bot.data_ptr(), inp.pol.data_ptr(), R.data_ptr(), T.data_ptr(),
+        amps.data_ptr() if amps is not None else None, status.data_ptr(), _lib.PRECISION[precision], _stream()))
+    nu, nv = 2 * hu + 1, 2 * hv + 1
+    res = (R.view(B, 3, nv, nu), T.view(B, 3, nv, nu), status)
+    return res + ((amps,) if amplitudes else ())
+
+
 def solve_host(eps, layer_index, thickness, wavelength, period, theta, phi, eps_top, eps_bot, pol,
                hu, hv, precision='double', handle=None):
     """Whole solve from host (NumPy) buffers through ``wb_solve_host``."""
