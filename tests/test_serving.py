@@ -136,3 +136,21 @@ def test_each_result_is_the_same_alone_and_in_the_mix():
         a, m = alone[r.id], mixed[r.id]
         scale = max(np.abs(a.R).max(), np.abs(a.T).max())
         assert np.abs(a.R - m.R).max() <= 1e-12 * scale and np.abs(a.T - m.T).max() <= 1e-12 * scale
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('precision,tol', [('double', 1e-12), ('mixed', 1e-9)])
+def test_resident_eigenpairs_are_reused_and_give_the_same_results(precision, tol):
+    torch = pytest.importorskip('torch')
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from wavebit_gb300.serving import GpuBackend, _stream, _repeat
+    reqs = _repeat(_stream(12, rate=400.0, seed=13, orders=[(2, 2), (3, 3)], max_layers=3, sides=(32,)), 2, 400.0)
+    ref, st0 = Server(GpuBackend(2, 6 << 30, 'double'), n_workers=2, max_batch=8).run(reqs)
+    be = GpuBackend(2, 6 << 30, precision, eig_cache=True)
+    got, st = Server(be, n_workers=2, max_batch=8).run(reqs)
+    assert st['completed'] == len(reqs) and st0['completed'] == len(reqs)
+    assert be.eig_hits > 0 and be.eig_misses > 0
+    for r in reqs:
+        a, m = ref[r.id], got[r.id]
+        assert np.abs(a.R - m.R).max() <= tol and np.abs(a.T - m.T).max() <= tol, r.id

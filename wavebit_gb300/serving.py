@@ -13,8 +13,12 @@ and the workers' batches overlap on the device.
   fit even alone is refused with an error result (it never blocks the queue).
 * Resident convolution matrices: stage A runs once per distinct raster (keyed by its bytes and
   the orders) and the result stays on the device in an LRU cache charged to the budget.
+* Resident eigenpairs (``--eig-cache``): the per-layer modes of every (layer, wavelength,
+  k-parallel) stay on the device; a batch runs the eigen-solve only for pairs not seen before and
+  then stage C alone (``wb_smm_solve``).
 * A request whose solve reports a non-zero status (singular, non-convergent, non-finite) gets an
-  error result; the other requests of its batch keep theirs.
+  error result; the other requests of its batch keep theirs. In the mixed form it is first solved
+  once more with the double-float eigen-solve.
 
 The solver is a small interface (``GpuBackend`` here; the CPU tests pass a fake one), so the
 scheduling logic is tested without a GPU. ``python -m wavebit_gb300.serving`` replays a seeded
@@ -75,7 +79,7 @@ def _pol_pair(pol):
 class GpuBackend:
     """libwbgpu.so behind the serving loop: one handle and one CUDA stream per worker."""
 
-    def __init__(self, n_workers, hbm_budget, precision='double', device=0):
+    def __init__(self, n_workers, hbm_budget, precision='double', device=0, eig_cache=False):
         import torch
         from . import _lib, engine
         self.torch, self.lib, self.engine = torch, _lib, engine
@@ -94,6 +98,17 @@ class GpuBackend:
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(n_workers)]
         self.cache = collections.OrderedDict()      # key -> ((3, N, N) tensor, ready event)
         self.cache_bytes = 0
+        # per-layer eigenpairs kept on the device, keyed by (layer, wavelength, k-parallel): the
+        # raster and orders, the wavelength, and period, angles and superstrate (which fix the
+        # order wavevectors). A batch whose pairs are all present skips the eigen-solve and runs
+        # stage C alone (wb_smm_solve). Charged to half of the cache share.
+        self.eig_modes = {'double': 'double', 'mixed': 'mixed'}.get(precision) if eig_cache else None
+        self.eig = collections.OrderedDict()        # key -> (q, W, V, ready event)
+        self.eig_bytes = 0
+        if self.eig_modes:
+            self.eig_budget = self.cache_budget // 2
+            self.cache_budget -= self.eig_budget
+        self.eig_hits = self.eig_misses = 0
         self.launches0 = sum(h.launches() for h in self.handles)
 
     # ---- admission
@@ -131,6 +146,51 @@ class GpuBackend:
                 self.cache_bytes -= old.numel() * 16
         return keys
 
+    # ---- resident eigenpairs
+    def _pair_key(self, layer_key, r):
+        return (layer_key, r.wavelength, r.theta, r.phi, r.period, r.eps_top)
+
+    def modes_for(self, reqs, keys_all, conv, index, worker):
+        """(q, W, V) stacked over the batch's (solve, layer) pairs, computing the missing ones."""
+        torch, engine = self.torch, self.engine
+        from .adjoint import ports
+        hu, hv = reqs[0].orders
+        stream = self.streams[worker]
+        pkeys = [[self._pair_key(k, r) for k in ks] for r, ks in zip(reqs, keys_all)]
+        missing = list(dict.fromkeys(pk for row in pkeys for pk in row if pk not in self.eig))
+        self.eig_hits += sum(1 for row in pkeys for pk in row if pk in self.eig)
+        self.eig_misses += len(missing)
+        if missing:
+            where = {}
+            for r, ks, row in zip(reqs, keys_all, pkeys):
+                for k, pk in zip(ks, row):
+                    where.setdefault(pk, (r, k))
+            kx, ky, pl = [], [], []
+            for pk in missing:
+                r, k = where[pk]
+                pv = ports(r.wavelength, r.period, r.theta, r.phi, r.eps_top, r.eps_bot, hu, hv, self.device)
+                kx.append(pv['kx']); ky.append(pv['ky']); pl.append(index[k])
+            w, q, W, V, st = engine.layer_modes(conv, pl, torch.stack(kx), torch.stack(ky),
+                                                precision=self.eig_modes, handle=self.handles[worker])
+            ev = torch.cuda.Event()
+            for i, pk in enumerate(missing):
+                entry = (q[i].clone(), W[i].clone(), V[i].clone())
+                self.eig[pk] = entry + (ev,)
+                self.eig_bytes += sum(t.numel() * 16 for t in entry)
+            ev.record(stream)
+            while self.eig_bytes > self.eig_budget and len(self.eig) > len(missing):
+                _, old = self.eig.popitem(last=False)
+                self.eig_bytes -= sum(t.numel() * 16 for t in old[:3])
+        flat = [pk for row in pkeys for pk in row]
+        for pk in dict.fromkeys(flat):
+            q, W, V, ev = self.eig[pk]
+            self.eig.move_to_end(pk)
+            stream.wait_event(ev)
+            for t in (q, W, V):
+                t.record_stream(stream)
+        return (torch.stack([self.eig[pk][0] for pk in flat]), torch.stack([self.eig[pk][1] for pk in flat]),
+                torch.stack([self.eig[pk][2] for pk in flat]))
+
     # ---- one batch
     def launch(self, worker, reqs):
         torch, engine = self.torch, self.engine
@@ -153,7 +213,12 @@ class GpuBackend:
                                      [r.eps_top for r in reqs], [r.eps_bot for r in reqs],
                                      [_pol_pair(r.pol) for r in reqs], device=self.device)
             prec = self.fallback_precision if reqs[0].retry and self.fallback_precision else self.precision
-            R, T, st = engine.solve_batch(conv, inp, precision=prec, handle=self.handles[worker])
+            if self.eig_modes and not reqs[0].retry:
+                q, W, V = self.modes_for(reqs, keys_all, conv, index, worker)
+                R, T, st = engine.smm_solve(W, V, q, inp, hu, hv, precision=self.precision,
+                                            handle=self.handles[worker])
+            else:
+                R, T, st = engine.solve_batch(conv, inp, precision=prec, handle=self.handles[worker])
             Rh = torch.empty(R.shape, dtype=R.dtype, pin_memory=True)
             Th = torch.empty(T.shape, dtype=T.dtype, pin_memory=True)
             sh = torch.empty(st.shape, dtype=st.dtype, pin_memory=True)
@@ -277,6 +342,18 @@ def _stream(n, rate, seed, orders=None, max_layers=6, sides=(64, 128, 256)):
     return out
 
 
+def _repeat(reqs, times, rate):
+    """The stream replayed `times` times back to back, with new ids and later arrivals."""
+    out = []
+    span = (reqs[-1].arrival if reqs else 0.0) + 1.0 / rate
+    for k in range(times):
+        for r in reqs:
+            c = Request(k * len(reqs) + r.id, r.eps, r.thickness, r.orders, r.period, r.wavelength, r.theta, r.phi,
+                        r.pol, r.eps_top, r.eps_bot, r.arrival + k * span)
+            out.append(c)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument('--requests', type=int, default=256)
@@ -288,14 +365,20 @@ def main():
     ap.add_argument('--orders', default='5,8,11,15', help='half-orders drawn from (comma list)')
     ap.add_argument('--max-layers', type=int, default=6)
     ap.add_argument('--seed', type=int, default=5)
+    ap.add_argument('--eig-cache', action='store_true', help='keep per-layer eigenpairs on the device')
+    ap.add_argument('--repeat', type=int, default=1,
+                    help='replay each request this many times (as new requests), e.g. to exercise the caches')
     args = ap.parse_args()
     orders = [(int(v), int(v)) for v in args.orders.split(',')]
     reqs = _stream(args.requests, args.rate, args.seed, orders, args.max_layers)
-    backend = GpuBackend(args.workers, int(args.budget_gb * 2 ** 30), args.precision)
+    if args.repeat > 1:
+        reqs = _repeat(reqs, args.repeat, args.rate)
+    backend = GpuBackend(args.workers, int(args.budget_gb * 2 ** 30), args.precision, eig_cache=args.eig_cache)
     server = Server(backend, args.workers, args.max_batch)
     _, stats = server.run(reqs)
     stats.update(precision=args.precision, rate=args.rate, workers=args.workers, orders=args.orders,
-                 max_layers=args.max_layers, gpu_launches=backend.launches())
+                 max_layers=args.max_layers, gpu_launches=backend.launches(), eig_cache=args.eig_cache,
+                 eig_hits=backend.eig_hits, eig_misses=backend.eig_misses, repeat=args.repeat)
     print(json.dumps(stats))
 
 
