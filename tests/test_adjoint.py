@@ -90,3 +90,18 @@ def test_autograd_function_matches_solve_and_grad_cpu():
     assert abs(float(loss) - ref[0]) < 1e-12
     assert torch.allclose(e.grad, ref[3], rtol=0, atol=1e-14)
     assert torch.allclose(t.grad, ref[4], rtol=0, atol=1e-14)
+
+
+def test_chunked_stage_b_gives_the_same_gradient_cpu():
+    """A budget that admits one wavelength's eigenpairs at a time (recomputed per chunk, never all
+    resident) gives the same loss and gradients as the unchunked pass."""
+    eps, th = _case(4)
+    kw = dict(KW, wavelengths=[600.0, 650.0, 710.0])
+    wR, wT = _weights(9, B=3, seed=4)
+    full = _loss(eps, th, 'torch', weights_R=wR, weights_T=wT, **kw)
+    n = 18
+    one = _loss(eps, th, 'torch', weights_R=wR, weights_T=wT, hbm_budget=8 * 16 * n * n * eps.shape[0], **kw)
+    assert AD._chunk_size(eps.shape[0], n, 8 * 16 * n * n * eps.shape[0], 'cpu') == 1
+    assert abs(full[0] - one[0]) <= 1e-12 * abs(full[0])
+    for a, b in zip(full[1:], one[1:]):
+        assert float((a - b).abs().max()) <= 1e-12 * max(1.0, float(a.abs().max()))

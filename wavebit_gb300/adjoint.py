@@ -408,14 +408,31 @@ def _stage_b_batch(impl, conv, pvs, L, hu, hv, cs=None):
     return torch.stack(ws), torch.stack(Ws)
 
 
+def _chunk_size(L, n, budget, device):
+    """Wavelengths per stage-B chunk: the eigenpairs and the reverse pass's per-layer temporaries
+    (about 8 complex n x n matrices per layer) of one chunk fit `budget` bytes (default: a quarter
+    of the free device memory; unbounded on the CPU)."""
+    per = 8 * 16 * n * n * L
+    if budget is None:
+        if torch.device(device).type != 'cuda':
+            return None
+        budget = torch.cuda.mem_get_info(torch.device(device))[0] // 4
+    return max(1, int(budget // per))
+
+
 def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weights_T, theta=0.0, phi=0.0,
-                   eps_top=1.0, eps_bot=1.0, pol=(0.0, 1.0), impl='gb300', device=None, grad=True):
+                   eps_top=1.0, eps_bot=1.0, pol=(0.0, 1.0), impl='gb300', device=None, grad=True,
+                   hbm_budget=None):
     """Loss = sum_b sum_i (weights_R[b, i] R[b, i] + weights_T[b, i] T[b, i]) over the given
     polarization's per-order efficiencies, and its gradients with respect to the raster
     permittivities (real part; shape of ``eps``) and the thicknesses.
 
     eps: (L, ny, nx) entry face first; thickness (L,); wavelengths (B,).
     Returns (loss, R (B, N), T (B, N), d_loss/d_eps (L, ny, nx) real, d_loss/d_thickness (L,)).
+
+    The eigenpairs are computed for a chunk of wavelengths at a time, sized by ``hbm_budget``
+    (bytes), and dropped after the chunk's forward and reverse passes: however many wavelengths,
+    no more than one chunk's modes are resident.
     """
     device = device or ('cuda' if impl == 'gb300' else 'cpu')
     eps = torch.as_tensor(eps, dtype=torch.complex128, device=device)
@@ -432,18 +449,22 @@ def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weigh
         conv = [sa[0] for sa in saved_a]
     wls = [float(v) for v in np.atleast_1d(wavelengths)]
     pvs = [ports(lam, period, theta, phi, eps_top, eps_bot, hu, hv, device) for lam in wls]
-    w_all, W_all = _stage_b_batch(impl, conv, pvs, L, hu, hv, cs)
+    chunk = _chunk_size(L, n, hbm_budget, device) or len(wls)
+    w_all = W_all = None
     g_conv = [[torch.zeros(N, N, dtype=torch.complex128, device=device) for _ in range(3)] for _ in range(L)]
     g_th = torch.zeros(L, dtype=torch.float64, device=device)
     loss = 0.0
     Rs, Ts = [], []
     for b, lam in enumerate(wls):
+        if b % chunk == 0:
+            w_all = W_all = None
+            w_all, W_all = _stage_b_batch(impl, conv, pvs[b:b + chunk], L, hu, hv, cs)
         pv = pvs[b]
         k0 = 2 * PI / lam
         bW, bV, Xs, per_layer = [], [], [], []
         for l in range(L):
             om2, omr, so = layer_operator_torch(pv['kx'], pv['ky'], *conv[l])
-            w, W = w_all[b * L + l], W_all[b * L + l]
+            w, W = w_all[(b % chunk) * L + l], W_all[(b % chunk) * L + l]
             q = mode_q_torch(w)
             V = (omr @ W) / q[None, :]
             c, s = pv['c'], pv['s']
