@@ -22,11 +22,12 @@ from . import _lib, engine
 
 class WavebitError(Exception):
     """Base error with a machine-readable ``code`` (errors.py:18-66 of the reference)."""
-    default_code = 'wavebit.error'
+    default_code = 'input.invalid'
 
     def __init__(self, message, *, code=None, path=None):
         self.code = code or self.default_code
         self.path = path
+        self.message = message
         super().__init__(f'{path}: {message}' if path else message)
 
 
@@ -36,6 +37,11 @@ class ValidationError(WavebitError, ValueError):
 
 class UnsupportedFeatureError(ValidationError):
     default_code = 'feature.unsupported'
+
+
+class IncompatibleProblemError(ValidationError):
+    """A live problem violates a prepared calculation's reuse contract (errors.py:56-58)."""
+    default_code = 'problem.incompatible'
 
 
 class NumericalError(WavebitError):
@@ -289,10 +295,15 @@ class Prepared:
         conv = self.conv
         if problem is not None and not _same_rasters(r['rasters'], self.resolved['rasters']):
             conv = _assemble_layers(r['rasters'], *r['orders'], self.handle)
+        L = len(r['rasters'])
+        return self._solve(r, conv, np.tile(np.arange(L), (len(r['wavelengths']), 1)), amplitudes)
+
+    def _solve(self, r, conv, layer_index, amplitudes=False):
+        """Solve every wavelength of ``r`` with the layers ``layer_index[b]`` of ``conv``."""
         hu, hv = r['orders']
         wl = r['wavelengths']
         B, L = len(wl), len(r['rasters'])
-        inp = engine.BatchInputs(np.tile(np.arange(L), (B, 1)), np.tile(r['thickness'], (B, 1)), wl,
+        inp = engine.BatchInputs(layer_index, np.tile(r['thickness'], (B, 1)), wl,
                                  np.tile(r['period'], (B, 1)), np.full(B, r['theta']),
                                  np.full(B, r['phi']), np.full(B, r['eps_top']),
                                  np.full(B, r['eps_bot']), np.tile(r['pol'], (B, 1)))
@@ -305,7 +316,7 @@ class Prepared:
             # solves the mixed form could not finish (a near-degenerate group too large for its
             # Newton step, say) are solved again with the double-float eigen-solve
             idx = torch.as_tensor(fallback, device=R.device)
-            sub = engine.BatchInputs(np.tile(np.arange(L), (len(fallback), 1)),
+            sub = engine.BatchInputs(np.asarray(layer_index)[fallback],
                                      np.tile(r['thickness'], (len(fallback), 1)), np.asarray(wl)[fallback],
                                      np.tile(r['period'], (len(fallback), 1)), np.full(len(fallback), r['theta']),
                                      np.full(len(fallback), r['phi']), np.full(len(fallback), r['eps_top']),
@@ -365,3 +376,6 @@ def run(problem, *, numerics=None, backend='gb300', device='cuda', precision='do
     """``prepare(...).run()`` (_lifecycle.py:801-803)."""
     return prepare(problem, numerics=numerics, backend=backend, device=device,
                    precision=precision).run(amplitudes=amplitudes)
+
+
+from . import operators  # noqa: E402  (rcwa.operators.assemble / solve, as in the reference)
