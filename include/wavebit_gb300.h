@@ -137,8 +137,13 @@ int wb_solve_host(wb_handle* h, int B, int L, int ny, int nx, int hu, int hv,
                   const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,
                   const wb_complex* pol, double* R, double* T, int32_t* status, int precision);
 
-/* Bytes of arena one chunk of `chunk` solves with L layers and N orders needs. */
+/* Bytes of arena one chunk of `chunk` solves with L layers and N orders needs (FP64 form). */
 size_t wb_solve_workspace_bytes(int hu, int hv, int L, int chunk);
+
+/* The same for any WB_PRECISION_* form (the mixed forms keep FP32 copies, group slots and
+ * refinement vectors beside the FP64-sized buffers); 0 for invalid arguments. Admission code
+ * (the reference's rcwa.check estimates, _lifecycle.py:422-457) sizes batches with it. */
+size_t wb_workspace_bytes(int hu, int hv, int L, int chunk, int precision);
 
 /* Stage A without any allocation, for callers that may not allocate device memory (code running
  * inside another component's CUDA-graph capture, servers and plugins whose host owns the device

@@ -72,3 +72,28 @@ def test_workspace_estimate_grows_with_the_chunk(lib):
     b = lib.wb_solve_workspace_bytes(7, 7, 4, 32)
     assert 0 < a < b
     assert lib.wb_solve_workspace_bytes(-1, 7, 4, 16) == 0
+
+
+def test_workspace_estimate_per_form(lib):
+    """The FP64 form matches wb_solve_workspace_bytes; the mixed forms need more (FP32 copies,
+    group slots, refinement vectors); bad precisions give 0."""
+    from wavebit_gb300 import _lib
+    fp64 = lib.wb_workspace_bytes(7, 7, 4, 16, _lib.PRECISION['double'])
+    assert fp64 == lib.wb_solve_workspace_bytes(7, 7, 4, 16)
+    for name in ('mixed', 'mixed_fp32', 'mixed_df64_eig'):
+        assert lib.wb_workspace_bytes(7, 7, 4, 16, _lib.PRECISION[name]) > fp64, name
+    assert lib.wb_workspace_bytes(7, 7, 4, 16, 99) == 0 and lib.wb_workspace_bytes(7, 7, 4, 16, -1) == 0
+
+
+def test_smm_solve_refuses_bad_arguments_before_any_device_work(lib):
+    """wb_smm_solve checks pointers, sizes and the precision on the host (no GPU calls): NULL
+    arguments, empty batches and forms other than FP64 / MIXED are WB_E_INVALID."""
+    from wavebit_gb300 import _lib
+    fake = ctypes.create_string_buffer(64)             # a non-NULL address, never dereferenced here
+    p = ctypes.addressof(fake)
+    args = lambda B, prec, h=p: (h, B, 2, 1, 1) + (p,) * 15 + (prec, None)
+    assert lib.wb_smm_solve(*args(4, 0, None)) == _lib.WB_E_INVALID
+    assert 'NULL' in _lib.last_error()
+    assert lib.wb_smm_solve(*args(0, 0)) == _lib.WB_E_INVALID
+    assert lib.wb_smm_solve(*args(4, _lib.PRECISION['mixed_df64'])) == _lib.WB_E_INVALID
+    assert 'precision' in _lib.last_error()

@@ -35,6 +35,7 @@ SIGNATURES = {
     'wb_solve_host': (_i, [_vp, _i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                            _vp, _vp, _vp, _vp, _i]),
     'wb_solve_workspace_bytes': (_sz, [_i, _i, _i, _i]),
+    'wb_workspace_bytes': (_sz, [_i, _i, _i, _i, _i]),
     'wb_kernel_launches': (_ll, [_vp]),
     'wb_assemble_li_noalloc': (_i, [_vp, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     'wb_assemble_li_noalloc_limit': (_sz, []),

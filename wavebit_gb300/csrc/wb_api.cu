@@ -141,6 +141,13 @@ size_t wb_solve_workspace_bytes(int hu, int hv, int L, int chunk) {
   return wb::solve_chunk_bytes((2 * hu + 1) * (2 * hv + 1), L, chunk, WB_PRECISION_FP64);
 }
 
+size_t wb_workspace_bytes(int hu, int hv, int L, int chunk, int precision) {
+  if (!valid_orders(hu, hv) || L <= 0 || chunk <= 0 || precision < WB_PRECISION_FP64 ||
+      precision > WB_PRECISION_MIXED_DF64_EIG)
+    return 0;
+  return wb::solve_chunk_bytes((2 * hu + 1) * (2 * hv + 1), L, chunk, precision);
+}
+
 int wb_layer_modes(wb_handle* h, int n_pairs, int hu, int hv, const wb_complex* conv,
                    const int32_t* pair_layer, const double* kx, const double* ky, wb_complex* w,
                    wb_complex* q, wb_complex* W, wb_complex* V, int32_t* status, int precision,

@@ -242,7 +242,7 @@ def check(problem, *, numerics=None, backend='gb300', device='cuda', precision='
     N = engine.n_orders(hu, hv)
     L = len(r['rasters'])
     chunk = max(1, min(len(r['wavelengths']), 128))
-    ws = int(_lib.load().wb_solve_workspace_bytes(hu, hv, L, chunk))
+    ws = int(_lib.load().wb_workspace_bytes(hu, hv, L, chunk, _lib.PRECISION.get(precision, 0)))
     est = {'retained_spatial_modes': N,
            'one_dense_material_matrix_bytes': 16 * N * N,
            'one_first_order_matrix_bytes': 16 * (2 * N) ** 2,

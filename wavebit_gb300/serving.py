@@ -9,7 +9,7 @@ that arrive while others are on the GPU are admitted as soon as a worker and mem
 and the workers' batches overlap on the device.
 
 * Admission: a bucket's batch limit is the largest batch whose workspace
-  (``wb_solve_workspace_bytes``) fits one worker's share of the budget; a request that cannot
+  (``wb_workspace_bytes`` of the serving precision) fits one worker's share of the budget; a request that cannot
   fit even alone is refused with an error result (it never blocks the queue).
 * Resident convolution matrices: stage A runs once per distinct raster (keyed by its bytes and
   the orders) and the result stays on the device in an LRU cache charged to the budget.
@@ -116,7 +116,8 @@ class GpuBackend:
         hu, hv = orders
         b = limit
         while b >= 1:
-            if int(self.lib.load().wb_solve_workspace_bytes(hu, hv, L, b)) <= self.per_worker:
+            if int(self.lib.load().wb_workspace_bytes(hu, hv, L, b, self.lib.PRECISION[self.precision])) \
+                    <= self.per_worker:
                 return b
             b //= 2
         return 0
