@@ -8,13 +8,21 @@
 // (scattering.py:163-200, :1272-1293) and reads R and T off the final S11 / S21
 // (scattering.py:907-994). Only those two blocks, applied to three incidence columns, are
 // ever read, so the stars are evaluated bottom-up keeping the one block the next star needs:
-// the reflection R_k seen from the gap above layer k,
-//     R_k = (S_layer_k * R_{k+1})_11
-//         = (A - rho_t B)^-1 (rho_t A - B),  rho_t = X rho_b X,  rho_b = (B + A R)(A + B R)^-1
-// with A, B the gap/layer interface pair of _ab_matrices (scattering.py:116-125) and
-// X = diag(exp(-k0 q d)). The transmitted amplitudes follow from one top-down pass with three
-// right-hand sides. This is the same star algebra (equal in exact arithmetic; the tests hold
-// it to the reference within 1e-10) at ~60 n^3 FP64 flops per layer instead of ~180 n^3.
+// the reflection R_l seen from the gap above layer l,
+//     P1 = bigW^-1 W_g (I + R_l+1),  P2 = bigV^-1 V_g (I - R_l+1),  M = P1 + P2,  N = P1 - P2
+//     rho_b = N M^-1,  rho_t = X rho_b X,  X1 = (I - rho_t) bigW^-1,  X2 = (I + rho_t) bigV^-1
+//     R_l = A^-1 B,  A = X1 W_g + X2 V_g,  B = -X1 W_g + X2 V_g
+// with W_g, V_g the gap modes (scattering.py:128-160) and X = diag(exp(-k0 q d)). The transmitted
+// amplitudes follow from one top-down pass with three right-hand sides. This is the same star
+// algebra (equal in exact arithmetic; the tests hold it to the reference within 1e-10) at
+// ~53 n^3 FP64 flops per layer instead of ~180 n^3.
+//
+// The mixed form (precision 1) runs stage B as an FP32 eigen-solve brought to FP64 accuracy by
+// Newton steps against the FP64 operator (stage_b_newton), and stage C as the FP32 cascade whose
+// amplitudes are refined against the stack's interface equations in double-float
+// (stage_c_refined). Sections below, in order: ports, Omega^2, q/X, V, the cascade's elementwise
+// kernels, the stage-B drivers, the cascade drivers, orchestration (solve_chunk), and the doors of
+// wb_smm_solve and wb_layer_modes.
 #include <vector>
 #include <algorithm>
 #include "wb_common.cuh"
