@@ -80,3 +80,67 @@ def test_numerics_outside_the_path_are_unsupported(field, value):
     num = rcwa.Numerics(orders=(1, 1), **{field: value})
     with pytest.raises(rcwa.UnsupportedFeatureError):
         rcwa._resolve(_problem(), num)
+
+
+class _FakeInputs:
+    def __init__(self, li, th, wl, per, theta, phi, et, eb, pol, device=None):
+        self.wl, self.theta = np.asarray(wl, float), np.asarray(theta, float)
+        self.B = len(self.wl)
+
+
+def _fake_solver(rule):
+    """A stand-in for engine.solve_batch: R carries the wavelength, T the angle each solve used,
+    and ``rule(wl, theta)`` decides its status word."""
+    import torch
+
+    def solve(conv, inp, precision='double', amplitudes=False, handle=None):
+        R = torch.tensor(inp.wl, dtype=torch.float64).reshape(-1, 1, 1, 1).repeat(1, 3, 1, 1)
+        T = torch.tensor(inp.theta, dtype=torch.float64).reshape(-1, 1, 1, 1).repeat(1, 3, 1, 1)
+        st = torch.tensor([rule(w, t) for w, t in zip(inp.wl, inp.theta)], dtype=torch.int32)
+        return R, T, st
+    return solve
+
+
+def _prepared(detuning):
+    p = rcwa.Prepared.__new__(rcwa.Prepared)
+    p.numerics, p.precision, p.handle = rcwa.Numerics(orders=(0, 0), detuning=detuning), 'double', None
+    r = dict(wavelengths=np.array([600.0, 700.0, 800.0]), rasters=[np.ones((1, 1))], thickness=np.array([100.0]),
+             period=(500.0, 500.0), theta=0.3, phi=0.0, eps_top=1.0, eps_bot=1.0, pol=(1.0, 0.0), orders=(0, 0))
+    return p, r
+
+
+def test_auto_detune_ladder_moves_the_wavelength_then_the_angle(monkeypatch):
+    from wavebit_gb300 import _lib
+    g = _lib.WB_ST_GRAZING
+    # 700 grazes exactly; 800 grazes until both the wavelength and the angle have moved
+    rule = lambda w, t: g if (w == 700.0 or (w in (800.0, 800.0 * (1 + 1e-12)) and t == 0.3)) else 0
+    monkeypatch.setattr(rcwa.engine, 'BatchInputs', _FakeInputs)
+    monkeypatch.setattr(rcwa.engine, 'solve_batch', _fake_solver(rule))
+    p, r = _prepared(True)
+    with pytest.warns(rcwa.AutoDetuneWarning):
+        res = p._solve(r, None, np.zeros((3, 1), int))
+    eff = res.diagnostics['effective_wavelengths']
+    assert eff == (600.0, 700.0 * (1 + 1e-12), 800.0 * (1 + 1e-12))
+    assert res.diagnostics['detuned'] == {1: ('wavelength',), 2: ('wavelength', 'theta')}
+    assert not any(res.diagnostics['grazing'])
+    assert float(res.R[2].max()) == 800.0 * (1 + 1e-12) and float(res.T[2].max()) == 0.3 * (1 + 1e-12)
+
+
+def test_a_grazing_mode_without_detuning_warns(monkeypatch):
+    from wavebit_gb300 import _lib
+    monkeypatch.setattr(rcwa.engine, 'BatchInputs', _FakeInputs)
+    monkeypatch.setattr(rcwa.engine, 'solve_batch', _fake_solver(lambda w, t: _lib.WB_ST_GRAZING if w == 700.0 else 0))
+    p, r = _prepared(None)
+    with pytest.warns(rcwa.RayleighPointWarning):
+        res = p._solve(r, None, np.zeros((3, 1), int))
+    assert res.diagnostics['grazing'] == (False, True, False) and res.diagnostics['detuned'] == {}
+
+
+def test_a_failed_solve_is_a_numerical_error_with_the_reference_code(monkeypatch):
+    from wavebit_gb300 import _lib
+    monkeypatch.setattr(rcwa.engine, 'BatchInputs', _FakeInputs)
+    monkeypatch.setattr(rcwa.engine, 'solve_batch', _fake_solver(lambda w, t: _lib.WB_ST_SINGULAR if w == 600.0 else 0))
+    p, r = _prepared(None)
+    with pytest.raises(rcwa.NumericalError) as e:
+        p._solve(r, None, np.zeros((3, 1), int))
+    assert e.value.code == 'rcwa.singular'

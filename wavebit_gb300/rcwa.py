@@ -11,6 +11,7 @@ Everything numerical runs in libwbgpu.so; there is no CPU path.
 """
 from dataclasses import dataclass, field
 import math
+import warnings
 
 import numpy as np
 import torch
@@ -46,6 +47,18 @@ class IncompatibleProblemError(ValidationError):
 
 class NumericalError(WavebitError):
     default_code = 'numerical.failure'
+
+
+class RayleighPointWarning(UserWarning):
+    """A layer eigenmode sits numerically on its light line (backend.py:1151 of the reference)."""
+
+
+class AutoDetuneWarning(UserWarning):
+    """The auto-detune ladder moved a wavelength or angle (backend.py:1253 of the reference)."""
+
+
+# relative step of an auto-detune retry (engine.py:141-147 of the reference)
+_AUTO_DETUNE_REL = 1e-12
 
 # ------------------------------------------------------------- declarations (mirror)
 
@@ -298,46 +311,92 @@ class Prepared:
         L = len(r['rasters'])
         return self._solve(r, conv, np.tile(np.arange(L), (len(r['wavelengths']), 1)), amplitudes)
 
+    def _batch(self, r, conv, layer_index, idx, wl, theta, precision, amplitudes):
+        """One wb_solve_batch over the wavelengths ``idx`` (with their own, possibly detuned,
+        wavelength and theta)."""
+        k = len(idx)
+        inp = engine.BatchInputs(np.asarray(layer_index)[idx], np.tile(r['thickness'], (k, 1)), wl[idx],
+                                 np.tile(r['period'], (k, 1)), theta[idx], np.full(k, r['phi']),
+                                 np.full(k, r['eps_top']), np.full(k, r['eps_bot']), np.tile(r['pol'], (k, 1)))
+        return engine.solve_batch(conv, inp, precision=precision, amplitudes=amplitudes, handle=self.handle)
+
     def _solve(self, r, conv, layer_index, amplitudes=False):
         """Solve every wavelength of ``r`` with the layers ``layer_index[b]`` of ``conv``."""
-        hu, hv = r['orders']
-        wl = r['wavelengths']
-        B, L = len(wl), len(r['rasters'])
-        inp = engine.BatchInputs(layer_index, np.tile(r['thickness'], (B, 1)), wl,
-                                 np.tile(r['period'], (B, 1)), np.full(B, r['theta']),
-                                 np.full(B, r['phi']), np.full(B, r['eps_top']),
-                                 np.full(B, r['eps_bot']), np.tile(r['pol'], (B, 1)))
-        out = engine.solve_batch(conv, inp, precision=self.precision, amplitudes=amplitudes,
-                                 handle=self.handle)
+        B = len(r['wavelengths'])
+        wl = np.asarray(r['wavelengths'], dtype=np.float64).copy()
+        th = np.full(B, float(r['theta']))
+        out = list(self._batch(r, conv, layer_index, np.arange(B), wl, th, self.precision, amplitudes))
         R, T, status = out[:3]
+
+        def merge(idx, res):
+            t = torch.as_tensor(idx, device=R.device)
+            R[t], T[t], status[t] = res[0], res[1], res[2]
+            if amplitudes:
+                out[3][t] = res[3]
+
         st = status.cpu().numpy()
         fallback = np.nonzero(st & ~_lib.WB_ST_GRAZING)[0] if self.precision == 'mixed' else np.zeros(0, int)
         if fallback.size:
             # solves the mixed form could not finish (a near-degenerate group too large for its
             # Newton step, say) are solved again with the double-float eigen-solve
-            idx = torch.as_tensor(fallback, device=R.device)
-            sub = engine.BatchInputs(np.asarray(layer_index)[fallback],
-                                     np.tile(r['thickness'], (len(fallback), 1)), np.asarray(wl)[fallback],
-                                     np.tile(r['period'], (len(fallback), 1)), np.full(len(fallback), r['theta']),
-                                     np.full(len(fallback), r['phi']), np.full(len(fallback), r['eps_top']),
-                                     np.full(len(fallback), r['eps_bot']), np.tile(r['pol'], (len(fallback), 1)))
-            out2 = engine.solve_batch(conv, sub, precision='mixed_df64_eig', amplitudes=amplitudes,
-                                      handle=self.handle)
-            R[idx], T[idx], status[idx] = out2[0], out2[1], out2[2]
-            if amplitudes:
-                out[3][idx] = out2[3]
+            merge(fallback, self._batch(r, conv, layer_index, fallback, wl, th, 'mixed_df64_eig', amplitudes))
             st = status.cpu().numpy()
+        moved = self._detune(r, conv, layer_index, wl, th, st, merge, amplitudes)
+        st = status.cpu().numpy()
+        grazing = np.nonzero(st & _lib.WB_ST_GRAZING)[0]
+        if grazing.size:
+            warnings.warn(f'a layer mode sits on its cutoff at {grazing.size} wavelength(s); the GB300 path does '
+                          'not rebuild exceptional points, so those results may be inaccurate. '
+                          'rcwa.Numerics(detuning=True) retries them slightly detuned.', RayleighPointWarning,
+                          stacklevel=3)
         bad = st & ~_lib.WB_ST_GRAZING
         if np.any(bad & _lib.WB_ST_SINGULAR):
             raise NumericalError('a factorization met an exact zero pivot', code='rcwa.singular')
         if np.any(bad & (_lib.WB_ST_NONFINITE | _lib.WB_ST_NOCONV)):
             raise NumericalError('the solve produced non-finite results', code='rcwa.nonfinite')
-        diag = {'solve_path': ('2d',) * B, 'effective_wavelengths': tuple(wl),
+        diag = {'solve_path': ('2d',) * B, 'effective_wavelengths': tuple(float(v) for v in wl),
                 'grazing': tuple(bool(s & _lib.WB_ST_GRAZING) for s in st),
                 'status': st, 'precision': self.precision,
-                'fallback_solves': tuple(int(i) for i in fallback)}
-        return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]), status, wl, diag,
-                      out[3] if amplitudes else None)
+                'fallback_solves': tuple(int(i) for i in fallback), 'detuned': moved}
+        return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]), status, tuple(r['wavelengths']),
+                      diag, out[3] if amplitudes else None)
+
+    def _detune(self, r, conv, layer_index, wl, th, st, merge, amplitudes):
+        """The reference's auto-detune ladder (engine.py:6382-6480), opt-in through
+        ``Numerics(detuning=True | step)``: wavelengths with a grazing layer mode or a failed
+        solve are solved again at wavelength * (1 + step), then, where the condition stays and
+        theta != 0, with theta * (1 + step) as well. A rung that fails keeps the previous values;
+        the detuned values are kept (``wl``, ``th`` updated in place). Returns {index: knobs}."""
+        det = getattr(_numerics_or_default(self.numerics), 'detuning', None)
+        if not det:
+            return {}
+        step = _AUTO_DETUNE_REL if det is True else float(det)
+        remaining = np.nonzero(st != 0)[0]
+        moved = {}
+        knobs = ['wavelength'] + (['theta'] if float(r['theta']) != 0.0 else [])
+        for knob in knobs:
+            if not remaining.size:
+                break
+            arr = wl if knob == 'wavelength' else th
+            saved = arr[remaining].copy()
+            arr[remaining] = saved * (1 + step)
+            res = self._batch(r, conv, layer_index, remaining, wl, th, self.precision, amplitudes)
+            s2 = res[2].cpu().numpy()
+            ok = (s2 & ~_lib.WB_ST_GRAZING) == 0           # the rung solved (grazing or not)
+            arr[remaining[~ok]] = saved[~ok]                # a failed rung keeps the previous values
+            if ok.any():
+                sel = np.nonzero(ok)[0]
+                merge(remaining[sel], tuple(x[torch.as_tensor(sel, device=x.device)] if x is not None else None
+                                           for x in res))
+                for i in remaining[sel]:
+                    moved.setdefault(int(i), []).append(knob)
+            remaining = remaining[~ok | ((s2 & _lib.WB_ST_GRAZING) != 0)]
+        if moved:
+            warnings.warn(f'auto_detune: {len(moved)} wavelength(s) had a mode on its cutoff or a failed solve; '
+                          f're-solved with {", ".join(sorted({k for v in moved.values() for k in v}))} * (1 + {step:g}). '
+                          'The results keep those values (Result.diagnostics["effective_wavelengths"]).',
+                          AutoDetuneWarning, stacklevel=4)
+        return {i: tuple(v) for i, v in moved.items()}
 
 
 def _same_rasters(a, b):
