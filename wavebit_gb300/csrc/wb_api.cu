@@ -10,6 +10,7 @@
 #include "wb_common.cuh"
 #include "wb_kernels.h"
 #include "wb_internal.h"
+#include "wb_trace.h"
 
 struct wb_handle {
   int device = 0;
@@ -124,6 +125,7 @@ int wb_build_indices(int hu, int hv, int32_t* labels_u, int32_t* labels_v, int32
 
 int wb_assemble_li(wb_handle* h, const wb_complex* eps, int L, int ny, int nx, int hu, int hv,
                    wb_complex* epx, wb_complex* epy, wb_complex* epz_i, int32_t* status, void* stream) {
+  wb::TraceRange trace_("wb:assemble_li");
   if (!h || !eps || !epx || !epy || !epz_i) return fail(WB_E_INVALID, "wb_assemble_li: NULL argument");
   if (L <= 0 || ny <= 0 || nx <= 0 || !valid_orders(hu, hv))
     return fail(WB_E_INVALID, "wb_assemble_li: bad sizes L=%d ny=%d nx=%d orders=(%d,%d)", L, ny, nx, hu, hv);
@@ -152,6 +154,7 @@ int wb_layer_modes(wb_handle* h, int n_pairs, int hu, int hv, const wb_complex* 
                    const int32_t* pair_layer, const double* kx, const double* ky, wb_complex* w,
                    wb_complex* q, wb_complex* W, wb_complex* V, int32_t* status, int precision,
                    void* stream) {
+  wb::TraceRange trace_("wb:layer_modes");
   if (!h || !conv || !pair_layer || !kx || !ky || !w || !q || !W || !V)
     return fail(WB_E_INVALID, "wb_layer_modes: NULL argument");
   if (n_pairs <= 0 || !valid_orders(hu, hv)) return fail(WB_E_INVALID, "wb_layer_modes: bad sizes");
@@ -174,6 +177,7 @@ int wb_solve_batch(wb_handle* h, int B, int L, int hu, int hv, const wb_complex*
                    const wb_complex* eps_top, const wb_complex* eps_bot, const wb_complex* pol,
                    double* R, double* T, wb_complex* amps, int32_t* status, int precision,
                    void* stream) {
+  wb::TraceRange trace_("wb:solve_batch");
   if (!h || !conv || !layer_index || !thickness || !wavelength || !period || !theta || !phi || !eps_top ||
       !eps_bot || !pol || !R || !T || !status)
     return fail(WB_E_INVALID, "wb_solve_batch: NULL argument");
@@ -206,6 +210,7 @@ int wb_smm_solve(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* W
                  const double* theta, const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,
                  const wb_complex* pol, double* R, double* T, wb_complex* amps, int32_t* status, int precision,
                  void* stream) {
+  wb::TraceRange trace_("wb:smm_solve");
   if (!h || !W || !V || !q || !thickness || !wavelength || !period || !theta || !phi || !eps_top || !eps_bot ||
       !pol || !R || !T || !status)
     return fail(WB_E_INVALID, "wb_smm_solve: NULL argument");
@@ -236,6 +241,7 @@ int wb_solve_host(wb_handle* h, int B, int L, int ny, int nx, int hu, int hv,
                   const double* wavelength, const double* period, const double* theta,
                   const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,
                   const wb_complex* pol, double* R, double* T, int32_t* status, int precision) {
+  wb::TraceRange trace_("wb:solve_host");
   if (!h || !eps || !layer_index || !thickness || !wavelength || !period || !theta || !phi || !eps_top ||
       !eps_bot || !pol || !R || !T || !status)
     return fail(WB_E_INVALID, "wb_solve_host: NULL argument");

@@ -29,6 +29,7 @@
 #include "wb_kernels.h"
 #include "wb_internal.h"
 #include "wb_num.cuh"
+#include "wb_trace.h"
 #include <type_traits>
 
 namespace wb {
@@ -583,6 +584,7 @@ void stage_b(cudaStream_t s, int P, int N, const cplx* conv, const int* pair_lay
              const double* pair_thick, const double* wavelength, const double* kx, const double* ky,
              Cx<RB>* OM, Cx<RB>* Zb, Cx<RB>* Xv, Cx<RB>* wr, Cx<RB>* tau, cplx* w, cplx* q, cplx* X,
              const double* c, const double* sn, int32_t* st, int st_div, bool rotate) {
+  TraceRange trace_("wb:stage_b");
   const int n = 2 * N;
   const long long n2 = (long long)n * n, NN = (long long)N * N;
   {
@@ -1002,6 +1004,7 @@ void stage_b_newton(cudaStream_t s, int P, int N, const cplx* conv, const int* p
                     const double* pair_thick, const double* wavelength, const double* kx, const double* ky,
                     cplx* Wd, cplx* Vd, cplx* Om, NewtonBufs& nb, GroupBufs& gb, cplx* w, cplx* q, cplx* X,
                     const double* c, const double* sn, int32_t* st, int st_div) {
+  TraceRange trace_("wb:stage_b.newton");
   const int n = 2 * N;
   const long long n2 = (long long)n * n, NN = (long long)N * N, tot = (long long)P * n2;
   const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
@@ -1123,6 +1126,7 @@ void stage_c(cudaStream_t s, Arena& ar, int Bc, int L, int N, Cx<RC>* bW, Cx<RC>
              const int* pivV, const cplx* X, const PortVectors& pv, const SolveDesc& d, int first,
              const SolveOut& out, int32_t* st, Cx<RC>* Mk, int* pivM, Cx<RC>* Rk, Cx<RC>* S1, Cx<RC>* S2,
              Cx<RC>* S3, int* pivS, Cx<RC>* Cin, Cx<RC>* g, Cx<RC>* h, Cx<RC>* r1, Cx<RC>* r2, Cx<RC>* cref) {
+  TraceRange trace_("wb:stage_c");
   const int n = 2 * N;
   const long long n2 = (long long)n * n;
   const long long lay_bs = (long long)L * n2, lay_ps = (long long)L * n, r_bs = (long long)(L + 1) * n2;
@@ -1422,6 +1426,7 @@ static void cascade_sources(cudaStream_t s, int Bc, int L, int n, const Cx<float
                             const int* pivW, const int* pivV, const Cx<float>* Mk, const int* pivM,
                             const Cx<float>* Ak, const int* pivA, const Cx<float>* Rk, const Cx<float>* G0,
                             const int* pivG, const cplx* X, const PortVectors& pv, RefineBufs& rb) {
+  TraceRange trace_("wb:stage_c.sources");
   using F = Cx<float>;
   const long long n2 = (long long)n * n, v3 = 3LL * n, v6 = 6LL * n;
   const long long lay_bs = (long long)L * n2, lay_ps = (long long)L * n, r_bs = (long long)(L + 1) * n2;
@@ -1500,6 +1505,7 @@ void stage_c_refined(cudaStream_t s, int Bc, int L, int N, const Cx<df64>* bWd, 
                      const PortVectors& pv, const SolveDesc& d, int first, const SolveOut& out, int32_t* st,
                      Cx<float>* Mk, int* pivM, Cx<float>* Ak, int* pivA, Cx<float>* Rk, Cx<float>* S1,
                      Cx<float>* S2, Cx<float>* S3, int* pivS, RefineBufs& rb, int passes) {
+  TraceRange trace_("wb:stage_c.refined");
   using D = Cx<df64>;
   const int n = 2 * N, P = Bc * L;
   const long long n2 = (long long)n * n, v3 = 3LL * n, v6 = 6LL * n;
