@@ -28,7 +28,7 @@ extern "C" {
 #endif
 
 #define WB_OK 0
-#define WB_E_INVALID 1     /* bad argument (reference: ValidationError, code 'rcwa.invalid') */
+#define WB_E_INVALID 1     /* bad argument (reference: ValidationError, code 'input.invalid') */
 #define WB_E_NOMEM 2       /* the request does not fit the handle's HBM budget */
 #define WB_E_SINGULAR 3    /* an exact zero pivot (reference: NumericalError 'rcwa.singular') */
 #define WB_E_NOCONV 4      /* the eigenvalue iteration hit its cap (LAPACK zgeev info > 0) */
@@ -54,7 +54,8 @@ extern "C" {
 typedef struct { double re, im; } wb_complex;
 typedef struct wb_handle wb_handle;
 
-/* Version of this ABI (major * 100 + minor). */
+/* Version of this ABI (major * 100 + minor): 2.0 = the precision codes above (WB_PRECISION_MIXED
+ * is the FP32 eigen-solve with Newton steps), wb_smm_solve and wb_workspace_bytes. */
 int wb_version(void);
 
 /* Message of the calling thread's last failure, NUL-terminated, truncated to len. */

@@ -33,6 +33,10 @@ def test_every_declared_symbol_is_exported(lib):
         assert hasattr(lib, name), name
 
 
+def test_abi_version(lib):
+    assert lib.wb_version() == 200
+
+
 def test_binding_table_covers_the_header():
     from wavebit_gb300 import _lib
     assert set(_declared()) == set(_lib.SIGNATURES)
