@@ -161,7 +161,8 @@ int wb_assemble_li_noalloc(const wb_complex* eps, int L, int ny, int nx, int hu,
                            void* stream);
 size_t wb_assemble_li_noalloc_limit(void);
 
-/* Number of kernels the library launched on this handle since creation (for accounting). */
+/* Number of kernels the library has launched in this process since it was loaded, over all
+ * handles (for accounting: take differences around a region). The handle is not consulted. */
 long long wb_kernel_launches(wb_handle* h);
 
 #ifdef __cplusplus

@@ -109,7 +109,7 @@ class GpuBackend:
             self.eig_budget = self.cache_budget // 2
             self.cache_budget -= self.eig_budget
         self.eig_hits = self.eig_misses = 0
-        self.launches0 = sum(h.launches() for h in self.handles)
+        self.launches0 = self.handles[0].launches()     # the library's count is process-wide
 
     # ---- admission
     def max_batch(self, orders, L, limit):
@@ -235,7 +235,7 @@ class GpuBackend:
         return token['R'].numpy()[:, 0], token['T'].numpy()[:, 0], token['status'].numpy()
 
     def launches(self):
-        return sum(h.launches() for h in self.handles) - self.launches0
+        return self.handles[0].launches() - self.launches0
 
 
 class Server:
