@@ -119,36 +119,101 @@ def raster_series(a, h):
 # ------------------------------------------------------------------ stage A3: Li's nested rules
 
 
-def conv_matrix(grid, hu, hv):
-    """Direct rule both ways, BTTB layout rows ``i = n*n_u + m`` (factorization.py:504-520)."""
+def conv_matrix(grid, hu, hv, su=None, sv=None):
+    """Direct rule both ways, BTTB layout rows ``i = n*n_u + m`` (factorization.py:504-520).
+    ``su`` / ``sv`` are the series along u / v (default: the raster staircase series)."""
+    su = su or (lambda a: raster_series(a, hu))
+    sv = sv or (lambda a: raster_series(a, hv))
     n_u, n_v = 2 * hu + 1, 2 * hv + 1
-    by_column = raster_series(grid.T, hv)                 # [j_u, k_v]
-    coeffs = raster_series(by_column.T, hu)               # [k_v, k_u]
+    by_column = sv(grid.T)                                # [j_u, k_v]
+    coeffs = su(by_column.T)                              # [k_v, k_u]
     blocks = np.take(np.take(coeffs, toeplitz_positions(hv), axis=0),
                      toeplitz_positions(hu), axis=1)
     out = blocks.reshape(n_v, n_v, n_u, n_u).transpose(0, 2, 1, 3)
     return out.reshape(n_v * n_u, n_v * n_u)
 
 
-def nested_rule_v_inner(grid, hu, hv, invert_outer):
+def nested_rule_v_inner(grid, hu, hv, invert_outer, su=None, sv=None):
     """``T_u([T_v(g)]^-1)``, optionally inverted (factorization.py:523-567, ``inner='v'``)."""
+    su = su or (lambda a: raster_series(a, hu))
+    sv = sv or (lambda a: raster_series(a, hv))
     n_u, n_v = 2 * hu + 1, 2 * hv + 1
-    lines = raster_series(grid.T, hv)                     # [j_u, k_v]
+    lines = sv(grid.T)                                    # [j_u, k_v]
     inner = np.linalg.inv(np.take(lines, toeplitz_positions(hv), axis=1)
                           .reshape(lines.shape[0], n_v, n_v))
     entries = inner.reshape(lines.shape[0], n_v * n_v).T  # [(n, n'), j_u]
-    outer = np.take(raster_series(entries, hu), toeplitz_positions(hu), axis=1)
+    outer = np.take(su(entries), toeplitz_positions(hu), axis=1)
     out = outer.reshape(n_v, n_v, n_u, n_u).transpose(0, 2, 1, 3).reshape(n_v * n_u, n_v * n_u)
     return np.linalg.inv(out) if invert_outer else out
 
 
-def li_conv(eps, hu, hv):
+def li_conv(eps, hu, hv, su=None, sv=None):
     """One layer's ``(epx, epy, epz_i)`` under fixed nesting (factorization.py:600-671)."""
     eps = np.asarray(eps, dtype=np.complex128)
-    epx = nested_rule_v_inner(eps, hu, hv, invert_outer=True)
-    epy = nested_rule_v_inner(1.0 / eps, hu, hv, invert_outer=False)
-    epz_i = np.linalg.inv(conv_matrix(eps, hu, hv))
+    epx = nested_rule_v_inner(eps, hu, hv, invert_outer=True, su=su, sv=sv)
+    epy = nested_rule_v_inner(1.0 / eps, hu, hv, invert_outer=False, su=su, sv=sv)
+    epz_i = np.linalg.inv(conv_matrix(eps, hu, hv, su=su, sv=sv))
     return epx, epy, epz_i
+
+
+# ------------------------------------------------------ stage A: integrated coefficients
+
+
+def compression_indices(cell):
+    """Last row / column of each run of identical neighbours, and the right-hand edges they
+    place on the unit cell (factorization.py:3005-3045). Columns are compared first; rows are
+    compared on the column-reduced raster."""
+    cell = np.asarray(cell)
+    n_row, n_col = cell.shape
+    col_idx = np.flatnonzero(np.any(cell[:, :-1] != cell[:, 1:], axis=0)).tolist() + [n_col - 1]
+    reduced = cell[:, col_idx]
+    row_idx = np.flatnonzero(np.any(reduced[:-1, :] != reduced[1:, :], axis=1)).tolist() + [n_row - 1]
+    x = (np.asarray(col_idx, dtype=np.float64) + 1.0) / n_col
+    y = (np.asarray(row_idx, dtype=np.float64) + 1.0) / n_row
+    return row_idx, col_idx, x, y
+
+
+def segment_bounds(edges):
+    """``(left, width)`` of the segments ending at ``edges`` on the unit cell
+    (factorization.py:443-454)."""
+    right = np.asarray(edges, dtype=np.float64).reshape(-1)
+    right = right / right[-1]
+    left = np.concatenate([[0.0], right[:-1]])
+    return left, right - left
+
+
+def segment_series(left, width, h):
+    """Orders ``-2h..2h`` of a profile constant on segments ``[left_j, left_j + width_j)``, in the
+    jump form ``c_k = sum_j (a_j - a_{j-1}) exp(-2 pi i k left_j) / (2 pi i k)``,
+    ``c_0 = sum_j a_j width_j`` (factorization.py:457-501)."""
+    orders = np.arange(-2 * h, 2 * h + 1)
+    scale = np.array([0j if o == 0 else 1.0 / (2j * math.pi * o) for o in orders])
+    weights = np.exp(-2j * math.pi * (left[:, None] * orders[None, :]))
+
+    def series(a):
+        a = np.asarray(a, dtype=np.complex128)
+        jumps = a - np.roll(a, 1, axis=-1)
+        ac = jumps @ (weights * scale[None, :])
+        dc = (a @ width.astype(np.complex128))[..., None]
+        return np.where(orders == 0, dc, ac)
+    return series
+
+
+def li_conv_integrated(eps, hu, hv):
+    """One layer's ``(epx, epy, epz_i)`` with integrated (closed-form segment) coefficients on
+    the compressed raster (factorization.py:674-686, :3135-3206)."""
+    eps = np.asarray(eps, dtype=np.complex128)
+    row_idx, col_idx, x, y = compression_indices(eps)
+    comp = eps[np.ix_(row_idx, col_idx)]
+    su = segment_series(*segment_bounds(x), hu)
+    sv = segment_series(*segment_bounds(y), hv)
+    return li_conv(comp, hu, hv, su=su, sv=sv)
+
+
+def to_conv_mat_raster_integrated(structure, hu, hv):
+    """Per-layer integrated slots stacked ``(L, N, N)`` (factorization.py:3181-3206)."""
+    out = [li_conv_integrated(e, hu, hv) for e in structure]
+    return tuple(np.stack([o[i] for o in out]) for i in range(3))
 
 
 def to_conv_mat_raster_sampled(structure, hu, hv):

@@ -10,6 +10,8 @@ It writes
   ``rcwa.run`` (NumPy backend, SMM, sampled Li, fixed nesting): per-order R and T for ``'s'``
   and ``'p'`` incidence, and each layer's centre-frame convolution matrices from
   ``rcwa.operators.assemble``;
+* ``ref_integrated.npz`` -- the same scenes (but the largest) with the integrated (closed-form
+  segment) coefficients, ``fourier_coefficients='integrated'``;
 * ``legacy_cases.npz`` -- the efficiencies that the reference's own frozen legacy golden file
   (``tests/fixtures/legacy_rcwa/golden_legacy.npz``) holds for its 1D, conical and 2D sampled-Li
   cases, with the inputs those cases are defined by (``tests/fixtures/legacy_rcwa/gen_goldens.py``).
@@ -79,7 +81,7 @@ def ref_cases():
     return cases
 
 
-def run_ref(case, pol):
+def run_ref(case, pol, coefficients=None):
     from wavebit import Material, Units, rcwa
     from wavebit.rcwa import operators
     st = case['structure'][::-1]          # public stacks list layers bottom to top
@@ -91,7 +93,7 @@ def run_ref(case, pol):
                          bottom=Material(epsilon=case['eps_bot']), layers=layers),
         excitation=rcwa.Excitation(wavelength=case['wavelength'], sources=(
             rcwa.PlaneWave(polarization=pol, theta=case['theta'], phi=case['phi']),)))
-    num = rcwa.Numerics(orders=case['orders'])
+    num = rcwa.Numerics(orders=case['orders'], fourier_coefficients=coefficients)
     res = rcwa.run(prob, numerics=num)
     ops = operators.assemble(prob, numerics=num)
     conv = ops.epsilon[0]
@@ -119,6 +121,30 @@ def make_ref_cases():
     out['names'] = np.array(names)
     np.savez_compressed(os.path.join(HERE, 'ref_cases.npz'), **out)
     print('ref_cases.npz:', len(names), 'cases')
+
+
+def make_integrated_cases():
+    """The same scenes with the integrated (closed-form segment) coefficients."""
+    out = {}
+    names = []
+    for case in ref_cases():
+        if case['name'] == 'crossed_5':       # the largest scene; the others cover the path
+            continue
+        n = case['name']
+        names.append(n)
+        for key in ('structure', 'thickness', 'wavelength', 'period', 'orders', 'theta', 'phi',
+                    'eps_top', 'eps_bot'):
+            out[f'{n}__{key}'] = np.asarray(case[key])
+        for pol in ('s', 'p'):
+            R, T, conv = run_ref(case, pol, coefficients='integrated')
+            out[f'{n}__R_{pol}'] = R
+            out[f'{n}__T_{pol}'] = T
+        if conv[0].shape[-1] <= 50:
+            for slot, arr in zip(('epx', 'epy', 'epz_i'), conv):
+                out[f'{n}__{slot}'] = arr[::-1]
+    out['names'] = np.array(names)
+    np.savez_compressed(os.path.join(HERE, 'ref_integrated.npz'), **out)
+    print('ref_integrated.npz:', len(names), 'cases')
 
 
 def make_legacy_cases():
@@ -158,4 +184,5 @@ def make_legacy_cases():
 if __name__ == '__main__':
     sys.path.insert(0, os.path.join(REF, 'src'))
     make_ref_cases()
+    make_integrated_cases()
     make_legacy_cases()

@@ -119,3 +119,49 @@ def test_lossless_energy_balance():
                         1.0, 2.25, 'p')
     for col in range(3):
         assert abs(out['R'][col].sum() + out['T'][col].sum() - 1) < 1e-12
+
+
+INTEGRATED_NAMES = list(np.load(os.path.join(GOLDEN, 'ref_integrated.npz'))['names'])
+
+
+def _integrated():
+    return np.load(os.path.join(GOLDEN, 'ref_integrated.npz'))
+
+
+@pytest.mark.parametrize('name', INTEGRATED_NAMES)
+def test_integrated_conv_matrices_match_reference_assemble(name):
+    """Integrated (closed-form segment) slots against ``rcwa.operators.assemble`` with
+    ``fourier_coefficients='integrated'`` (centre frame)."""
+    c = _case(_integrated(), name)
+    if 'epx' not in c:
+        pytest.skip('no stored slots for this case')
+    hu, hv = (int(v) for v in c['orders'])
+    mine = O.to_conv_mat_raster_integrated(c['structure'], hu, hv)
+    for m, theirs in zip(mine, (c['epx'], c['epy'], c['epz_i'])):
+        for i in range(m.shape[0]):
+            got = O.swap_fourier_origin(m[i], hu, hv)
+            assert np.abs(got - theirs[i]).max() <= 1e-12 * np.abs(theirs[i]).max(), (name, i)
+
+
+@pytest.mark.parametrize('name', INTEGRATED_NAMES)
+def test_integrated_solve_matches_reference_run(name):
+    """Per-order R and T of the oracle's solve on integrated slots against the reference's own
+    ``rcwa.run`` with ``fourier_coefficients='integrated'``, for s and p."""
+    c = _case(_integrated(), name)
+    hu, hv = (int(v) for v in c['orders'])
+    conv = O.to_conv_mat_raster_integrated(c['structure'], hu, hv)
+    for pol in ('s', 'p'):
+        o = O.solve_stack(c['structure'], c['thickness'], float(c['wavelength']), tuple(c['period']), hu, hv,
+                          float(c['theta']), float(c['phi']), complex(c['eps_top']), complex(c['eps_bot']), pol,
+                          conv=conv)
+        scale = max(np.abs(c[f'R_{pol}']).max(), np.abs(c[f'T_{pol}']).max())
+        assert np.abs(o['R'][0] - c[f'R_{pol}']).max() <= 1e-12 * scale, (name, pol)
+        assert np.abs(o['T'][0] - c[f'T_{pol}']).max() <= 1e-12 * scale, (name, pol)
+
+
+def test_integrated_coefficients_keep_a_uniform_layer_exact():
+    """The jump form gives a uniform layer exactly eps * I (factorization.py:457-501)."""
+    epx, epy, epz_i = O.li_conv_integrated(np.full((7, 5), 6.25 + 0.5j), 3, 2)
+    N = 35
+    assert np.array_equal(epx, (6.25 + 0.5j) * np.eye(N)) or np.abs(epx - (6.25 + 0.5j) * np.eye(N)).max() < 1e-15
+    assert np.abs(epz_i - np.eye(N) / (6.25 + 0.5j)).max() < 1e-15
