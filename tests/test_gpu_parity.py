@@ -220,10 +220,12 @@ def test_layer_modes_double_float_eigenpairs():
     assert res < 1e-12, res
 
 
-def test_double_float_form_survives_the_fp32_exponent_range():
-    """Requests that once overflowed or underflowed the double-float (FP32-exponent) form: nearly
-    converged bulges of ~1e-25, metal layers, near-degenerate modes. The mixed result must be
-    finite and equal to the FP64 one to 1e-9."""
+@pytest.mark.parametrize('precision', ['mixed', 'mixed_df64_eig'])
+def test_double_float_form_survives_the_fp32_exponent_range(precision):
+    """Requests that once overflowed or underflowed the double-float (FP32-exponent) eigen-solve:
+    nearly converged bulges of ~1e-25, metal layers, near-degenerate modes; the same requests
+    through the FP32 + Newton eigen-solve. The result must be finite and equal to the FP64 one
+    to 1e-9."""
     E = _engine()
     from wavebit_gb300.serving import _stream, _pol_pair
     reqs = _stream(128, 4.0, 5, [(5, 5), (8, 8)], 4)
@@ -233,7 +235,7 @@ def test_double_float_form_survives_the_fp32_exponent_range():
         inp = E.BatchInputs([list(range(L))], [r.thickness], [r.wavelength], [r.period], [r.theta], [r.phi],
                             [r.eps_top], [r.eps_bot], [_pol_pair(r.pol)])
         Rd, Td, sd = E.solve_batch(conv, inp, precision='double')
-        Rm, Tm, sm = E.solve_batch(conv, inp, precision='mixed')
+        Rm, Tm, sm = E.solve_batch(conv, inp, precision=precision)
         torch.cuda.synchronize()
         assert int(sd.item()) & ~8 == 0 and int(sm.item()) & ~8 == 0, (r.id, int(sm.item()))
         assert float((Rd - Rm).abs().max()) <= 1e-9 and float((Td - Tm).abs().max()) <= 1e-9, r.id
