@@ -412,6 +412,17 @@ def sp_result(S, kx, ky, kz_top, kz_bot, n_top, n_bot, eps_top, eps_bot, inciden
     return R, T, eff, amps
 
 
+def exported_scattering(S, hu, hv):
+    """The stack's ``S`` as the reference publishes it (``Outputs(scattering=True)``,
+    scattering.py:482-605): the four blocks at the half-space ports with s amplitudes first and
+    the p port variables after, each order referenced at the cell centre -- ``C S C`` of the
+    corner-frame cascade, ``C = diag((-1)^(m+n))`` on both polarization halves."""
+    m = order_labels(hu)[None, :] + order_labels(hv)[:, None]
+    d = np.where(m.reshape(-1) % 2 == 0, 1.0, -1.0)
+    c = np.concatenate([d, d])
+    return tuple(c[:, None] * blk * c[None, :] for blk in S)
+
+
 def solve_stack(structure, thickness, wavelength, period, hu, hv, theta=0.0, phi=0.0,
                 eps_top=1.0, eps_bot=1.0, polarization='s', conv=None, keep=False):
     """One SMM solve of a raster stack (scattering.py:1185-1456; engine.py:7836-7880).

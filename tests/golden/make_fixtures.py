@@ -12,6 +12,8 @@ It writes
   ``rcwa.operators.assemble``;
 * ``ref_integrated.npz`` -- the same scenes (but the largest) with the integrated (closed-form
   segment) coefficients, ``fourier_coefficients='integrated'``;
+* ``ref_scattering.npz`` -- the stack's exported scattering matrix (``Outputs(scattering=True)``)
+  of five of those scenes;
 * ``legacy_cases.npz`` -- the efficiencies that the reference's own frozen legacy golden file
   (``tests/fixtures/legacy_rcwa/golden_legacy.npz``) holds for its 1D, conical and 2D sampled-Li
   cases, with the inputs those cases are defined by (``tests/fixtures/legacy_rcwa/gen_goldens.py``).
@@ -147,6 +149,39 @@ def make_integrated_cases():
     print('ref_integrated.npz:', len(names), 'cases')
 
 
+def make_scattering_cases():
+    """The stack's scattering matrix (Outputs(scattering=True), scattering.py:482-560) of a few
+    small scenes: S11, S12, S21, S22 at the half-space ports, about the cell centre."""
+    from wavebit import Material, Units, rcwa
+    out = {}
+    names = []
+    for case in ref_cases():
+        if case['name'] not in ('grating_1d', 'crossed_0', 'crossed_1', 'crossed_4', 'symmetric_pillar'):
+            continue
+        n = case['name']
+        names.append(n)
+        for key in ('structure', 'thickness', 'wavelength', 'period', 'orders', 'theta', 'phi',
+                    'eps_top', 'eps_bot'):
+            out[f'{n}__{key}'] = np.asarray(case[key])
+        st = case['structure'][::-1]
+        th = list(case['thickness'])[::-1]
+        layers = tuple(rcwa.Layer(thickness=float(t), epsilon=np.asarray(e)) for e, t in zip(st, th))
+        prob = rcwa.Problem(
+            units=Units(length='nm'),
+            stack=rcwa.Stack(period=case['period'], top=Material(epsilon=case['eps_top']),
+                             bottom=Material(epsilon=case['eps_bot']), layers=layers),
+            excitation=rcwa.Excitation(wavelength=case['wavelength'], sources=(
+                rcwa.PlaneWave(polarization='s', theta=case['theta'], phi=case['phi']),)),
+            outputs=rcwa.Outputs(scattering=True))
+        res = rcwa.run(prob, numerics=rcwa.Numerics(orders=case['orders']))
+        sm = res.scattering[0]
+        for blk in ('S11', 'S12', 'S21', 'S22'):
+            out[f'{n}__{blk}'] = np.asarray(getattr(sm, blk))
+    out['names'] = np.array(names)
+    np.savez_compressed(os.path.join(HERE, 'ref_scattering.npz'), **out)
+    print('ref_scattering.npz:', len(names), 'cases')
+
+
 def make_legacy_cases():
     """Efficiencies from the reference's frozen legacy golden file, with their inputs."""
     gold = np.load(os.path.join(REF, 'tests/fixtures/legacy_rcwa/golden_legacy.npz'))
@@ -185,4 +220,5 @@ if __name__ == '__main__':
     sys.path.insert(0, os.path.join(REF, 'src'))
     make_ref_cases()
     make_integrated_cases()
+    make_scattering_cases()
     make_legacy_cases()

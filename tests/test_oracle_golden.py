@@ -165,3 +165,28 @@ def test_integrated_coefficients_keep_a_uniform_layer_exact():
     N = 35
     assert np.array_equal(epx, (6.25 + 0.5j) * np.eye(N)) or np.abs(epx - (6.25 + 0.5j) * np.eye(N)).max() < 1e-15
     assert np.abs(epz_i - np.eye(N) / (6.25 + 0.5j)).max() < 1e-15
+
+
+SCATTERING_NAMES = list(np.load(os.path.join(GOLDEN, 'ref_scattering.npz'))['names'])
+
+
+@pytest.mark.parametrize('name', SCATTERING_NAMES)
+def test_exported_scattering_matrix_matches_reference(name):
+    """The four blocks of the stack's S at the half-space ports, about the cell centre, against
+    the reference's ``result.scattering`` (``Outputs(scattering=True)``, scattering.py:482-605)."""
+    c = _case(np.load(os.path.join(GOLDEN, 'ref_scattering.npz')), name)
+    hu, hv = (int(v) for v in c['orders'])
+    out = O.solve_stack(c['structure'], c['thickness'], float(c['wavelength']), tuple(c['period']), hu, hv,
+                        float(c['theta']), float(c['phi']), complex(c['eps_top']), complex(c['eps_bot']), 's')
+    mine = O.exported_scattering(out['S'], hu, hv)
+    for blk, m in zip(('S11', 'S12', 'S21', 'S22'), mine):
+        theirs = c[blk]
+        assert np.abs(m - theirs).max() <= 1e-12 * max(1.0, np.abs(theirs).max()), (name, blk)
+    # the readings the reference documents for the s block: S11 delta = r_s and S21 delta = t_s,
+    # both referenced at the cell centre (the solve's own amplitudes are about the corner)
+    N = (2 * hu + 1) * (2 * hv + 1)
+    m = O.order_labels(hu)[None, :] + O.order_labels(hv)[:, None]
+    d = np.where(m.reshape(-1) % 2 == 0, 1.0, -1.0)
+    r_s, t_s = out['amps'][0][1].reshape(-1), out['amps'][2][1].reshape(-1)
+    assert np.abs(mine[0][:N, N // 2] - d * r_s).max() <= 1e-13
+    assert np.abs(mine[2][:N, N // 2] - d * t_s).max() <= 1e-13
