@@ -85,6 +85,17 @@ int wb_build_indices(int hu, int hv, int32_t* labels_u, int32_t* labels_v, int32
 int wb_assemble_li(wb_handle* h, const wb_complex* eps, int L, int ny, int nx, int hu, int hv,
                    wb_complex* epx, wb_complex* epy, wb_complex* epz_i, int32_t* status, void* stream);
 
+/* Stage A with integrated (closed-form segment) coefficients, Li fixed nesting. eps: device
+ * (L, ny, nx) compressed cells, each pixel standing for one block of equal neighbours of the
+ * raster; x_edges: device (L, nx) right edges of the column blocks on the unit cell, y_edges:
+ * device (L, ny) those of the row blocks, increasing, the last one 1 (the record
+ * compression_indices returns). Outputs as wb_assemble_li. Reference:
+ * rcwa/_engine/factorization.py:3181-3206 (to_conv_mat_raster_integrated), :443-501
+ * (_segment_bounds, _segment_series), :3005-3045 (compression_indices). */
+int wb_assemble_li_integrated(wb_handle* h, const wb_complex* eps, int L, int ny, int nx, const double* x_edges,
+                              const double* y_edges, int hu, int hv, wb_complex* epx, wb_complex* epy,
+                              wb_complex* epz_i, int32_t* status, void* stream);
+
 /* Stage B: eigenmodes of n_pairs layers. conv: device (n_conv, 3, N, N) slots epx, epy, epz_i;
  * pair_layer: device (n_pairs) index into conv; kx, ky: device (n_pairs, N) normalised order
  * wavevectors. Outputs (device): w (n_pairs, 2N) eigenvalues of Omega^2, q (n_pairs, 2N),

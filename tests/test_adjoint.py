@@ -87,7 +87,7 @@ def test_autograd_function_matches_solve_and_grad_cpu():
     loss = AD.efficiency_loss(e, t, wR, wT, **spec)
     loss.backward()
     ref = _loss(eps, th, 'torch', weights_R=wR, weights_T=wT, **KW)
-    assert abs(float(loss) - ref[0]) < 1e-12
+    assert abs(float(loss.detach()) - ref[0]) < 1e-12
     assert torch.allclose(e.grad, ref[3], rtol=0, atol=1e-14)
     assert torch.allclose(t.grad, ref[4], rtol=0, atol=1e-14)
 

@@ -74,12 +74,54 @@ def test_bad_orders_are_refused(numerics, path):
     assert e.value.path == path
 
 
-@pytest.mark.parametrize('field,value', [('algorithm', 'etm'), ('fourier_coefficients', 'integrated'),
-                                         ('factorization', 'nvf'), ('li_nesting', 'alternating')])
+@pytest.mark.parametrize('field,value', [('algorithm', 'etm'), ('fourier_coefficients', 'shape'),
+                                         ('factorization', 'nvf'), ('factorization', 'laurent'),
+                                         ('li_nesting', 'alternating')])
 def test_numerics_outside_the_path_are_unsupported(field, value):
     num = rcwa.Numerics(orders=(1, 1), **{field: value})
     with pytest.raises(rcwa.UnsupportedFeatureError):
         rcwa._resolve(_problem(), num)
+
+
+@pytest.mark.parametrize('value', ['sampled', 'integrated', 'INTEGRATED', None])
+def test_both_coefficient_rules_are_admitted(value):
+    num = rcwa.Numerics(orders=(1, 1), fourier_coefficients=value)
+    rcwa._resolve(_problem(), num)
+    assert rcwa._integrated(num) == (value is not None and value.lower() == 'integrated')
+
+
+@pytest.mark.parametrize('value', [True, 0, -1e-12, float('nan'), float('inf'), '1e-12'])
+def test_detuning_is_a_positive_relative_step(value):
+    """numerics.py:127-131 of the reference: None or a positive finite float / int."""
+    with pytest.raises(rcwa.ValidationError) as e:
+        rcwa._resolve(_problem(), rcwa.Numerics(orders=(1, 1), detuning=value))
+    assert e.value.code == 'numerics.detuning' and e.value.path == 'numerics.detuning'
+
+
+def test_a_detuning_step_is_admitted():
+    rcwa._resolve(_problem(), rcwa.Numerics(orders=(1, 1), detuning=1e-12))
+    rcwa._resolve(_problem(), rcwa.Numerics(orders=(1, 1), detuning=1))
+
+
+def test_compression_matches_the_oracle_record():
+    """The host compression of the integrated path against the oracle's restatement of
+    compression_indices, on rasters with runs, isolated pixels and uniform layers."""
+    from oracle import rcwa_oracle as O
+    rng = np.random.default_rng(7)
+    cells = [np.full((5, 7), 2.25 + 0j), np.array([[1.0, 12.25]]), np.ones((1, 1))]
+    for _ in range(30):
+        ny, nx = rng.integers(1, 25, size=2)
+        base = np.where(rng.random((rng.integers(1, 5), rng.integers(1, 5))) < 0.5, 12.25, 1.0 + 0.5j)
+        ry = np.sort(rng.integers(0, ny, size=base.shape[0] - 1))
+        rx = np.sort(rng.integers(0, nx, size=base.shape[1] - 1))
+        cells.append(base[np.searchsorted(ry, np.arange(ny), side='right')][:, np.searchsorted(rx, np.arange(nx), side='right')])
+    cells.append(rng.standard_normal((9, 4)) + 0j)          # nothing to compress
+    for cell in cells:
+        comp, x, y = rcwa.compression(cell)
+        ri, ci, ox, oy = O.compression_indices(cell)
+        assert np.array_equal(comp, cell[np.ix_(ri, ci)])
+        assert np.array_equal(x, ox) and np.array_equal(y, oy)       # bit-identical edges
+        assert x[-1] == 1.0 and y[-1] == 1.0
 
 
 class _FakeInputs:
@@ -116,7 +158,7 @@ def test_auto_detune_ladder_moves_the_wavelength_then_the_angle(monkeypatch):
     rule = lambda w, t: g if (w == 700.0 or (w in (800.0, 800.0 * (1 + 1e-12)) and t == 0.3)) else 0
     monkeypatch.setattr(rcwa.engine, 'BatchInputs', _FakeInputs)
     monkeypatch.setattr(rcwa.engine, 'solve_batch', _fake_solver(rule))
-    p, r = _prepared(True)
+    p, r = _prepared(rcwa._AUTO_DETUNE_REL)
     with pytest.warns(rcwa.AutoDetuneWarning):
         res = p._solve(r, None, np.zeros((3, 1), int))
     eff = res.diagnostics['effective_wavelengths']

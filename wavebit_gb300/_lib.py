@@ -27,6 +27,7 @@ SIGNATURES = {
     'wb_reserve': (_i, [_vp, _sz]),
     'wb_build_indices': (_i, [_i, _i, _vp, _vp, _vp, _vp]),
     'wb_assemble_li': (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
+    'wb_assemble_li_integrated': (_i, [_vp, _vp, _i, _i, _i, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     'wb_layer_modes': (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     'wb_solve_batch': (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                             _vp, _vp, _vp, _vp, _i, _vp]),

@@ -138,6 +138,24 @@ int wb_assemble_li(wb_handle* h, const wb_complex* eps, int L, int ny, int nx, i
   return cuda_check("wb_assemble_li");
 }
 
+int wb_assemble_li_integrated(wb_handle* h, const wb_complex* eps, int L, int ny, int nx, const double* x_edges,
+                              const double* y_edges, int hu, int hv, wb_complex* epx, wb_complex* epy,
+                              wb_complex* epz_i, int32_t* status, void* stream) {
+  wb::TraceRange trace_("wb:assemble_li_integrated");
+  if (!h || !eps || !x_edges || !y_edges || !epx || !epy || !epz_i)
+    return fail(WB_E_INVALID, "wb_assemble_li_integrated: NULL argument");
+  if (L <= 0 || ny <= 0 || nx <= 0 || !valid_orders(hu, hv))
+    return fail(WB_E_INVALID, "wb_assemble_li_integrated: bad sizes L=%d ny=%d nx=%d orders=(%d,%d)", L, ny, nx,
+                hu, hv);
+  cudaSetDevice(h->device);
+  size_t need = wb::assemble_workspace_bytes(L, ny, nx, hu, hv);
+  int rc = reserve(h, need);
+  if (rc) return rc;
+  wb::assemble_li((cudaStream_t)stream, (const cplx*)eps, L, ny, nx, hu, hv, (cplx*)epx, (cplx*)epy, (cplx*)epz_i,
+                  h->buf, status, x_edges, y_edges);
+  return cuda_check("wb_assemble_li_integrated");
+}
+
 size_t wb_solve_workspace_bytes(int hu, int hv, int L, int chunk) {
   if (!valid_orders(hu, hv) || L <= 0 || chunk <= 0) return 0;
   return wb::solve_chunk_bytes((2 * hu + 1) * (2 * hv + 1), L, chunk, WB_PRECISION_FP64);

@@ -6,10 +6,14 @@
 //   BTTB rows i = n * n_u + m, entry (i, i') = c_{(n-n'), (m-m')}  (_conv_matrix :504-520)
 // Only orders -2h..2h of each line are needed, so each coefficient is a direct DFT sum over
 // the line's pixels (with exact integer argument reduction) rather than a full FFT.
+// Integrated coefficients (to_conv_mat_raster_integrated, factorization.py:3181-3206) run the
+// same pipeline on a compressed raster, with the closed-form segment series (wb_series.cuh) in
+// place of the staircase series; the compression itself is done once on the host.
 // The work is a few tens of MFLOP per 256x256 layer and is cached per layer: it is
 // HBM/latency-bound and tiny next to stages B and C.
 #include "wb_common.cuh"
 #include "wb_kernels.h"
+#include "wb_series.cuh"
 
 namespace wb {
 
@@ -52,6 +56,35 @@ __global__ void series_kernel(const cplx* __restrict__ in, long long n_lines, in
     acc = cadd(acc, a0);
   }
   out[line * nk + kk] = acc;
+}
+
+// The integrated counterpart of series_kernel: the same line addressing, and per line the
+// right edges of its segments, edges[((line / lines_per_seg) % n_seg_rows) * npts + j].
+__global__ void segment_series_kernel(const cplx* __restrict__ in, long long n_lines, int lines_per_group,
+                                      long long group_stride, long long line_stride, long long pt_stride,
+                                      int npts, int h, int reciprocal, const double* __restrict__ edges,
+                                      long long lines_per_seg, int n_seg_rows, cplx* __restrict__ out) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= n_lines * (4 * h + 1)) return;
+  segment_series_at(idx, in, lines_per_group, group_stride, line_stride, pt_stride, npts, h, reciprocal, edges,
+                    lines_per_seg, n_seg_rows, out);
+}
+
+// One series launch: the staircase series when `edges` is NULL, else the segment series with
+// `lines_per_seg` consecutive lines sharing a row of edges (rows cycle over n_seg_rows layers).
+static void launch_series(cudaStream_t s, const cplx* in, long long lines, int lines_per_group,
+                          long long group_stride, long long line_stride, long long pt_stride, int npts, int h,
+                          int reciprocal, const double* edges, long long lines_per_seg, int n_seg_rows,
+                          cplx* out) {
+  const long long th = lines * (4 * h + 1);
+  const unsigned blocks = (unsigned)((th + 127) / 128);
+  if (edges)
+    segment_series_kernel<<<blocks, 128, 0, s>>>(in, lines, lines_per_group, group_stride, line_stride, pt_stride,
+                                                 npts, h, reciprocal, edges, lines_per_seg, n_seg_rows, out);
+  else
+    series_kernel<<<blocks, 128, 0, s>>>(in, lines, lines_per_group, group_stride, line_stride, pt_stride, npts,
+                                         h, reciprocal, out);
+  note_launch();
 }
 
 // Inverse of the (2h+1)^2 Toeplitz matrix T[r][c] = coef[r - c + 2h] of each line, by
@@ -145,7 +178,8 @@ size_t assemble_workspace_bytes(int L, int ny, int nx, int hu, int hv) {
 }
 
 void assemble_li(cudaStream_t s, const cplx* eps, int L, int ny, int nx, int hu, int hv,
-                 cplx* epx, cplx* epy, cplx* epz_i, void* ws, int32_t* status) {
+                 cplx* epx, cplx* epy, cplx* epz_i, void* ws, int32_t* status, const double* x_edges,
+                 const double* y_edges) {
   const int nu = 2 * hu + 1, nv = 2 * hv + 1, N = nu * nv, nku = 4 * hu + 1, nkv = 4 * hv + 1;
   char* p = static_cast<char*>(ws);
   cplx* cv = reinterpret_cast<cplx*>(p); p += align256(sizeof(cplx) * L * 2 * nx * nkv);
@@ -155,32 +189,22 @@ void assemble_li(cudaStream_t s, const cplx* eps, int L, int ny, int nx, int hu,
   cplx* pre = reinterpret_cast<cplx*>(p); p += align256(sizeof(cplx) * 2 * L * N * N);
   int* ipiv = reinterpret_cast<int*>(p);
   const long long plane = (long long)ny * nx;
-  // 1. series along v of every column, for eps (groups 0..L-1) and 1/eps (groups L..2L-1)
-  for (int rec = 0; rec < 2; ++rec) {
-    long long lines = (long long)L * nx;
-    long long th = lines * nkv;
-    series_kernel<<<(unsigned)((th + 127) / 128), 128, 0, s>>>(eps, lines, nx, plane, 1, nx, ny, hv, rec,
-                                                              cv + (long long)rec * L * nx * nkv); note_launch();
-  }
+  // 1. series along v of every column, for eps (groups 0..L-1) and 1/eps (groups L..2L-1);
+  //    line = layer * nx + x
+  for (int rec = 0; rec < 2; ++rec)
+    launch_series(s, eps, (long long)L * nx, nx, plane, 1, nx, ny, hv, rec, y_edges, nx, L,
+                  cv + (long long)rec * L * nx * nkv);
   // 2. inner Toeplitz inverses, groups (rec, layer): 2L groups of nx lines
   {
     size_t sm = sizeof(cplx) * nv * 2 * nv;
     toeplitz_inverse_kernel<<<2 * L * nx, 128, sm, s>>>(cv, nx, hv, inner, status); note_launch();
   }
-  // 3. series along u of every inner-inverse entry: 2L * nv^2 lines of nx points
-  {
-    long long lines = 2LL * L * nv * nv;
-    long long th = lines * nku;
-    series_kernel<<<(unsigned)((th + 127) / 128), 128, 0, s>>>(inner, lines, 1, nx, 0, 1, nx, hu, 0, cu); note_launch();
-  }
-  // 4. direct rule: series along u of the eps column series (lines (layer, kv), points x)
-  {
-    long long lines = (long long)L * nkv;
-    long long th = lines * nku;
-    // cv for eps is laid out [(layer * nx + x) * nkv + kv]: line (layer, kv) has stride nkv per x
-    series_kernel<<<(unsigned)((th + 127) / 128), 128, 0, s>>>(cv, lines, nkv, (long long)nx * nkv, 1, nkv,
-                                                              nx, hu, 0, c2); note_launch();
-  }
+  // 3. series along u of every inner-inverse entry: 2L * nv^2 lines of nx points;
+  //    line = ((rec * L + layer) * nv + r) * nv + c
+  launch_series(s, inner, 2LL * L * nv * nv, 1, nx, 0, 1, nx, hu, 0, x_edges, (long long)nv * nv, L, cu);
+  // 4. direct rule: series along u of the eps column series (lines (layer, kv), points x).
+  //    cv for eps is laid out [(layer * nx + x) * nkv + kv]: line (layer, kv) has stride nkv per x
+  launch_series(s, cv, (long long)L * nkv, nkv, (long long)nx * nkv, 1, nkv, nx, hu, 0, x_edges, nkv, L, c2);
   // 5. BTTB layouts: pre[0:L] = T_u([T_v(eps)]^-1), epy = T_u([T_v(1/eps)]^-1), pre[L:2L] = T_uv(eps)
   {
     long long th = (long long)L * N * N;

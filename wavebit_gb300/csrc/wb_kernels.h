@@ -61,8 +61,11 @@ void normalize_columns(cudaStream_t s, int batch, int n, Cx<R>* W, int ldw, long
 
 // ---- stage A: convolution matrices (wb_assemble.cu)
 // eps: (L, ny, nx) row-major raster; outputs (L, N, N) column-major; scratch from `ws`.
+// x_edges (L, nx) and y_edges (L, ny), both NULL for sampled coefficients: the right edges of
+// the column / row segments of compressed rasters, for integrated coefficients.
 size_t assemble_workspace_bytes(int L, int ny, int nx, int hu, int hv);
 void assemble_li(cudaStream_t s, const cplx* eps, int L, int ny, int nx, int hu, int hv,
-                 cplx* epx, cplx* epy, cplx* epz_i, void* ws, int32_t* status);
+                 cplx* epx, cplx* epy, cplx* epz_i, void* ws, int32_t* status,
+                 const double* x_edges = nullptr, const double* y_edges = nullptr);
 
 }  // namespace wb

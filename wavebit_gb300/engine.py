@@ -66,17 +66,33 @@ class ConvStack:
         return cls(buf.to(torch.complex128), hu, hv)
 
 
-def assemble(eps, hu, hv, handle=None):
-    """Stage A: Li-rule convolution matrices of ``eps`` (L, ny, nx) (wb_assemble_li)."""
+def assemble(eps, hu, hv, handle=None, edges=None):
+    """Stage A: Li-rule convolution matrices of ``eps`` (L, ny, nx) (wb_assemble_li).
+
+    ``edges = (x_edges (L, nx), y_edges (L, ny))`` makes ``eps`` compressed cells with those
+    block edges on the unit cell and the coefficients integrated (wb_assemble_li_integrated)."""
+    L, ny, nx = (int(v) for v in eps.shape)
+    if edges is not None:
+        x_edges, y_edges = (np.asarray(e, dtype=np.float64) for e in edges)
+        if x_edges.shape != (L, nx) or y_edges.shape != (L, ny):
+            raise ValueError(f'edges must be ({L}, {nx}) and ({L}, {ny})')
+        for e in (x_edges, y_edges):
+            if not (np.all(np.diff(e, axis=1) > 0) and np.all(e[:, 0] > 0) and np.all(e[:, -1] == 1.0)):
+                raise ValueError('block edges must increase from above 0 to exactly 1 along each row')
     eps = _c128(eps, 'cuda')
-    L, ny, nx = eps.shape
     N = n_orders(hu, hv)
     h = handle or _lib.handle(eps.device.index or 0)
     planes = torch.empty((3, L, N, N), dtype=torch.complex128, device=eps.device)
     status = torch.zeros(1, dtype=torch.int32, device=eps.device)
-    _lib.check(h.lib.wb_assemble_li(h.h, eps.data_ptr(), L, ny, nx, hu, hv, planes[0].data_ptr(),
-                                    planes[1].data_ptr(), planes[2].data_ptr(), status.data_ptr(),
-                                    _stream()))
+    if edges is None:
+        _lib.check(h.lib.wb_assemble_li(h.h, eps.data_ptr(), L, ny, nx, hu, hv, planes[0].data_ptr(),
+                                        planes[1].data_ptr(), planes[2].data_ptr(), status.data_ptr(),
+                                        _stream()))
+    else:
+        xe, ye = _f64(x_edges, eps.device), _f64(y_edges, eps.device)
+        _lib.check(h.lib.wb_assemble_li_integrated(h.h, eps.data_ptr(), L, ny, nx, xe.data_ptr(), ye.data_ptr(),
+                                                   hu, hv, planes[0].data_ptr(), planes[1].data_ptr(),
+                                                   planes[2].data_ptr(), status.data_ptr(), _stream()))
     return ConvStack(planes.transpose(0, 1).contiguous(), hu, hv, status)
 
 

@@ -149,19 +149,28 @@ def _numerics_orders(numerics):
     orders = tuple(int(v) for v in getattr(numerics, 'orders', (0, 0)))
     if len(orders) != 2 or min(orders) < 0:
         raise ValidationError('orders must be a pair of nonnegative integers', path='numerics.orders')
-    for name, allowed in (('algorithm', ('smm',)), ('fourier_coefficients', (None, 'sampled')),
+    for name, allowed in (('algorithm', ('smm',)), ('fourier_coefficients', (None, 'sampled', 'integrated')),
                           ('factorization', (None, 'li')), ('li_nesting', (None, 'fixed'))):
         val = getattr(numerics, name, None)
+        val = getattr(val, 'value', val)                # the reference's enums carry the name
         if isinstance(val, str):
             val = val.lower()
         if val not in allowed:
             raise UnsupportedFeatureError(
-                f'numerics.{name}={val!r}: the GB300 path implements {allowed[-1]!r} only',
+                f'numerics.{name}={val!r}: the GB300 path implements {", ".join(map(repr, allowed[1:]))} only',
                 path=f'numerics.{name}')
-    if getattr(numerics, 'detuning', None) is not None:
-        raise UnsupportedFeatureError('detuning is not implemented on the GB300 path',
-                                      path='numerics.detuning')
+    det = getattr(numerics, 'detuning', None)
+    if det is not None and (type(det) not in (float, int) or not math.isfinite(det) or det <= 0):
+        raise ValidationError('detuning is None (exact requested problem) or a positive relative step.',
+                              code='numerics.detuning', path='numerics.detuning')
     return orders
+
+
+def _integrated(numerics):
+    """Whether the Li slots take integrated (closed-form segment) coefficients."""
+    val = getattr(numerics, 'fourier_coefficients', None)
+    val = getattr(val, 'value', val)
+    return isinstance(val, str) and val.lower() == 'integrated'
 
 
 def _resolve(problem, numerics):
@@ -266,7 +275,8 @@ def check(problem, *, numerics=None, backend='gb300', device='cuda', precision='
         est['device_free_bytes'] = int(free)
         est['admissible'] = ws <= free
     resolved = {'order_window': ((0, hu), (0, hv)), 'wavelength_count': len(r['wavelengths']),
-                'layer_count': L, 'fourier_coefficients': 'sampled', 'factorization': 'li',
+                'layer_count': L, 'fourier_coefficients': 'integrated' if _integrated(numerics) else 'sampled',
+                'factorization': 'li',
                 'algorithm': 'smm', 'solve_path': '2d', 'backend': backend, 'device': device,
                 'precision': precision}
     return CheckReport(issues=(), estimates=est, resolved=resolved)
@@ -301,13 +311,14 @@ class Prepared:
         r = _resolve(problem, numerics)
         self.resolved = r
         hu, hv = r['orders']
-        self.conv = _assemble_layers(r['rasters'], hu, hv, handle)
+        self.integrated = _integrated(numerics)
+        self.conv = _assemble_layers(r['rasters'], hu, hv, handle, self.integrated)
 
     def run(self, problem=None, *, amplitudes=False):
         r = self.resolved if problem is None else _resolve(problem, self.numerics)
         conv = self.conv
         if problem is not None and not _same_rasters(r['rasters'], self.resolved['rasters']):
-            conv = _assemble_layers(r['rasters'], *r['orders'], self.handle)
+            conv = _assemble_layers(r['rasters'], *r['orders'], self.handle, self.integrated)
         L = len(r['rasters'])
         return self._solve(r, conv, np.tile(np.arange(L), (len(r['wavelengths']), 1)), amplitudes)
 
@@ -347,7 +358,7 @@ class Prepared:
         if grazing.size:
             warnings.warn(f'a layer mode sits on its cutoff at {grazing.size} wavelength(s); the GB300 path does '
                           'not rebuild exceptional points, so those results may be inaccurate. '
-                          'rcwa.Numerics(detuning=True) retries them slightly detuned.', RayleighPointWarning,
+                          'rcwa.Numerics(detuning=1e-12) retries them slightly detuned.', RayleighPointWarning,
                           stacklevel=3)
         bad = st & ~_lib.WB_ST_GRAZING
         if np.any(bad & _lib.WB_ST_SINGULAR):
@@ -363,14 +374,14 @@ class Prepared:
 
     def _detune(self, r, conv, layer_index, wl, th, st, merge, amplitudes):
         """The reference's auto-detune ladder (engine.py:6382-6480), opt-in through
-        ``Numerics(detuning=True | step)``: wavelengths with a grazing layer mode or a failed
+        ``Numerics(detuning=step)``, a positive relative step: wavelengths with a grazing layer mode or a failed
         solve are solved again at wavelength * (1 + step), then, where the condition stays and
         theta != 0, with theta * (1 + step) as well. A rung that fails keeps the previous values;
         the detuned values are kept (``wl``, ``th`` updated in place). Returns {index: knobs}."""
         det = getattr(_numerics_or_default(self.numerics), 'detuning', None)
         if not det:
             return {}
-        step = _AUTO_DETUNE_REL if det is True else float(det)
+        step = float(det)
         remaining = np.nonzero(st != 0)[0]
         moved = {}
         knobs = ['wavelength'] + (['theta'] if float(r['theta']) != 0.0 else [])
@@ -403,16 +414,37 @@ def _same_rasters(a, b):
     return len(a) == len(b) and all(x.shape == y.shape and np.array_equal(x, y) for x, y in zip(a, b))
 
 
-def _assemble_layers(rasters, hu, hv, handle):
-    """Stage A for every layer; rasters of different shapes are assembled separately."""
+def compression(cell):
+    """A raster reduced to one pixel per block of equal neighbours, with the right edges of the
+    column and row blocks on the unit cell: ``(cell, x_edges, y_edges)``
+    (compression_indices, factorization.py:3005-3045). A column block ends where any row
+    changes between neighbouring columns; a row block where the column-reduced rows change."""
+    cell = np.asarray(cell)
+    ny, nx = cell.shape
+    cols = np.append(np.nonzero((cell[:, 1:] != cell[:, :-1]).any(axis=0))[0], nx - 1)
+    reduced = cell[:, cols]
+    rows = np.append(np.nonzero((reduced[1:] != reduced[:-1]).any(axis=1))[0], ny - 1)
+    return (reduced[rows], (cols.astype(np.float64) + 1.0) / nx, (rows.astype(np.float64) + 1.0) / ny)
+
+
+def _assemble_layers(rasters, hu, hv, handle, integrated=False):
+    """Stage A for every layer; consecutive layers of one shape are assembled together. With
+    ``integrated`` each raster is compressed first (on the host, once per prepare) and shapes
+    are those of the compressed cells."""
+    if integrated:
+        comp = [compression(e) for e in rasters]
+        cells = [c[0] for c in comp]
+    else:
+        cells = rasters
     bufs = []
     i = 0
-    while i < len(rasters):
+    while i < len(cells):
         j = i
-        while j < len(rasters) and rasters[j].shape == rasters[i].shape:
+        while j < len(cells) and cells[j].shape == cells[i].shape:
             j += 1
-        eps = torch.as_tensor(np.stack(rasters[i:j]), device='cuda')
-        bufs.append(engine.assemble(eps, hu, hv, handle=handle).buf)
+        eps = torch.as_tensor(np.stack(cells[i:j]), device='cuda')
+        edges = (np.stack([c[1] for c in comp[i:j]]), np.stack([c[2] for c in comp[i:j]])) if integrated else None
+        bufs.append(engine.assemble(eps, hu, hv, handle=handle, edges=edges).buf)
         i = j
     return engine.ConvStack(torch.cat(bufs, dim=0), hu, hv)
 

@@ -79,13 +79,17 @@ def _pol_pair(pol):
 class GpuBackend:
     """libwbgpu.so behind the serving loop: one handle and one CUDA stream per worker."""
 
-    def __init__(self, n_workers, hbm_budget, precision='double', device=0, eig_cache=False):
+    def __init__(self, n_workers, hbm_budget, precision='double', device=0, eig_cache=False, coefficients='sampled'):
         import torch
         from . import _lib, engine
         self.torch, self.lib, self.engine = torch, _lib, engine
         self.device = torch.device('cuda', device)
         torch.cuda.set_device(self.device)
         self.precision = precision
+        if coefficients not in ('sampled', 'integrated'):
+            raise ValueError("coefficients must be 'sampled' or 'integrated'")
+        # integrated (closed-form segment) coefficients assemble each raster's compressed cell
+        self.coefficients = coefficients
         # a mixed-form solve that reports a failure (a group of near-degenerate modes too large
         # for the Newton step, an FP32 QR that did not converge) is solved again with the
         # double-float eigen-solve
@@ -129,14 +133,20 @@ class GpuBackend:
         keys = []
         for l in range(req.eps.shape[0]):
             raster = req.eps[l]
-            key = (hashlib.blake2b(raster.tobytes(), digest_size=16).hexdigest(), raster.shape, hu, hv)
+            key = (hashlib.blake2b(raster.tobytes(), digest_size=16).hexdigest(), raster.shape, hu, hv,
+                   self.coefficients)
             keys.append(key)
             if key in self.cache:
                 self.cache.move_to_end(key)
                 continue
+            edges = None
+            if self.coefficients == 'integrated':
+                from .rcwa import compression
+                raster, x_edges, y_edges = compression(raster)
+                edges = (x_edges[None], y_edges[None])
             with torch.cuda.stream(self.streams[worker]):
                 cs = self.engine.assemble(torch.as_tensor(raster[None], device=self.device), hu, hv,
-                                          handle=self.handles[worker])
+                                          handle=self.handles[worker], edges=edges)
                 ev = torch.cuda.Event()
                 ev.record(self.streams[worker])
             t = cs.buf[0]
@@ -367,6 +377,8 @@ def main():
     ap.add_argument('--max-layers', type=int, default=6)
     ap.add_argument('--seed', type=int, default=5)
     ap.add_argument('--eig-cache', action='store_true', help='keep per-layer eigenpairs on the device')
+    ap.add_argument('--coefficients', default='sampled', choices=['sampled', 'integrated'],
+                    help='Li coefficients: sampled staircase or integrated segments of the compressed raster')
     ap.add_argument('--repeat', type=int, default=1,
                     help='replay each request this many times (as new requests), e.g. to exercise the caches')
     args = ap.parse_args()
@@ -374,12 +386,14 @@ def main():
     reqs = _stream(args.requests, args.rate, args.seed, orders, args.max_layers)
     if args.repeat > 1:
         reqs = _repeat(reqs, args.repeat, args.rate)
-    backend = GpuBackend(args.workers, int(args.budget_gb * 2 ** 30), args.precision, eig_cache=args.eig_cache)
+    backend = GpuBackend(args.workers, int(args.budget_gb * 2 ** 30), args.precision, eig_cache=args.eig_cache,
+                         coefficients=args.coefficients)
     server = Server(backend, args.workers, args.max_batch)
     _, stats = server.run(reqs)
     stats.update(precision=args.precision, rate=args.rate, workers=args.workers, orders=args.orders,
                  max_layers=args.max_layers, gpu_launches=backend.launches(), eig_cache=args.eig_cache,
-                 eig_hits=backend.eig_hits, eig_misses=backend.eig_misses, repeat=args.repeat)
+                 eig_hits=backend.eig_hits, eig_misses=backend.eig_misses, repeat=args.repeat,
+                 coefficients=args.coefficients)
     print(json.dumps(stats))
 
 
