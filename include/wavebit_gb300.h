@@ -139,6 +139,21 @@ int wb_smm_solve(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* W
                  const wb_complex* pol, double* R, double* T, wb_complex* amps, int32_t* status, int precision,
                  void* stream);
 
+/* The stack's scattering matrix at its two half-space ports, as the reference publishes it
+ * (Outputs(scattering=True), result.scattering), from given modes (FP64). Inputs as wb_smm_solve
+ * without pol. Outputs (device, each (B, 2N, 2N) column-major): S11 reflection back into the
+ * superstrate, S12 transmission from the substrate into the superstrate, S21 transmission from
+ * the superstrate into the substrate, S22 reflection back into the substrate. Rows and columns
+ * are the s amplitudes of the N orders followed by the p port variables (the p wave's magnetic
+ * field: S11 applied to a unit s column is r_s, to a unit p column -r_p), every order referenced
+ * at the cell centre. Reference: rcwa/_engine/scattering.py:482-605 (ScatteringMatrix,
+ * _scattering_matrix), :1272-1293 (the cascade that forms it). */
+int wb_scattering_matrix(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* W, const wb_complex* V,
+                         const wb_complex* q, const double* thickness, const double* wavelength, const double* period,
+                         const double* theta, const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,
+                         wb_complex* S11, wb_complex* S12, wb_complex* S21, wb_complex* S22, int32_t* status,
+                         void* stream);
+
 /* The same solve from HOST buffers: rasters in, efficiencies out. Copies inputs to the
  * device, assembles the L layers (stage A), solves the B problems, copies R, T and status
  * back and synchronises. eps: host (L, ny, nx); the other arrays as in wb_solve_batch but in

@@ -101,3 +101,18 @@ def test_smm_solve_refuses_bad_arguments_before_any_device_work(lib):
     assert lib.wb_smm_solve(*args(0, 0)) == _lib.WB_E_INVALID
     assert lib.wb_smm_solve(*args(4, _lib.PRECISION['mixed_df64'])) == _lib.WB_E_INVALID
     assert 'precision' in _lib.last_error()
+
+
+def test_scattering_matrix_refuses_bad_arguments_before_any_device_work(lib):
+    """wb_scattering_matrix checks pointers and sizes on the host: NULL arguments, empty batches
+    and bad orders are WB_E_INVALID with a message."""
+    from wavebit_gb300 import _lib
+    fake = ctypes.create_string_buffer(64)
+    p = ctypes.addressof(fake)
+    args = lambda B, hu=1, h=p, out=p: (h, B, 2, hu, 1) + (p,) * 10 + (out, p, p, p, p, None)
+    assert lib.wb_scattering_matrix(*args(4, h=None)) == _lib.WB_E_INVALID
+    assert 'NULL' in _lib.last_error()
+    assert lib.wb_scattering_matrix(*args(4, out=None)) == _lib.WB_E_INVALID
+    assert lib.wb_scattering_matrix(*args(0)) == _lib.WB_E_INVALID
+    assert lib.wb_scattering_matrix(*args(4, hu=-1)) == _lib.WB_E_INVALID
+    assert 'wb_scattering_matrix' in _lib.last_error()

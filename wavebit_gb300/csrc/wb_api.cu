@@ -254,6 +254,36 @@ int wb_smm_solve(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* W
   return cuda_check("wb_smm_solve");
 }
 
+int wb_scattering_matrix(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* W, const wb_complex* V,
+                         const wb_complex* q, const double* thickness, const double* wavelength, const double* period,
+                         const double* theta, const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,
+                         wb_complex* S11, wb_complex* S12, wb_complex* S21, wb_complex* S22, int32_t* status,
+                         void* stream) {
+  wb::TraceRange trace_("wb:scattering_matrix");
+  if (!h || !W || !V || !q || !thickness || !wavelength || !period || !theta || !phi || !eps_top || !eps_bot ||
+      !S11 || !S12 || !S21 || !S22 || !status)
+    return fail(WB_E_INVALID, "wb_scattering_matrix: NULL argument");
+  if (B <= 0 || L <= 0 || !valid_orders(hu, hv))
+    return fail(WB_E_INVALID, "wb_scattering_matrix: bad sizes B=%d L=%d", B, L);
+  cudaSetDevice(h->device);
+  const int N = (2 * hu + 1) * (2 * hv + 1);
+  int chunk = B;
+  while (chunk > 1 && wb::scattering_chunk_bytes(N, L, chunk) > h->budget) chunk = (chunk + 1) / 2;
+  int rc = reserve(h, wb::scattering_chunk_bytes(N, L, chunk));
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaMemsetAsync(status, 0, sizeof(int32_t) * B, s);
+  wb::SolveDesc d{B, L, hu, hv, nullptr, nullptr, thickness, wavelength, period, theta, phi, (const cplx*)eps_top,
+                  (const cplx*)eps_bot, nullptr};
+  for (int first = 0; first < B; first += chunk) {
+    int count = std::min(chunk, B - first);
+    if (wb::scattering_chunk(s, h->arena, d, (const cplx*)W, (const cplx*)V, (const cplx*)q, first, count,
+                             (cplx*)S11, (cplx*)S12, (cplx*)S21, (cplx*)S22, status) != 0)
+      return fail(WB_E_NOMEM, "wb_scattering_matrix: arena exhausted for a chunk of %d", count);
+  }
+  return cuda_check("wb_scattering_matrix");
+}
+
 int wb_solve_host(wb_handle* h, int B, int L, int ny, int nx, int hu, int hv,
                   const wb_complex* eps, const int32_t* layer_index, const double* thickness,
                   const double* wavelength, const double* period, const double* theta,

@@ -63,6 +63,11 @@ void layer_modes(cudaStream_t s, Arena& ar, int n_pairs, int N, const cplx* conv
 void regroup_slots(cudaStream_t s, int L, int N, const cplx* planes, cplx* out);
 int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int count, const SolveOut& out,
                 int precision);
+// The stack's scattering matrix at the half-space ports from given modes (wb_scattering_matrix):
+// S11..S22 (B, n, n) column-major, centre frame.
+size_t scattering_chunk_bytes(int N, int L, int chunk);
+int scattering_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* W, const cplx* V, const cplx* q,
+                     int first, int count, cplx* S11, cplx* S12, cplx* S21, cplx* S22, int32_t* status);
 size_t smm_chunk_bytes(int N, int L, int chunk, int precision);
 int smm_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* W, const cplx* V, const cplx* q,
               int first, int count, const SolveOut& out, int precision);

@@ -40,17 +40,19 @@ long long launch_count() { return (long long)__atomic_load_n(&g_launches, __ATOM
 
 // --------------------------------------------------------------------------- ports
 // Per solve: order wavevectors, per-order s/p frame, half-space kz, gap waves and the diagonal
-// S blocks of the superstrate->gap and gap->substrate interfaces.
+// S blocks of the superstrate->gap and gap->substrate interfaces. The incident wavevector is
+// fixed by theta and phi in eps_inc (NULL: the superstrate); the mirrored stack of the
+// scattering-matrix export keeps the original one while its half-spaces are swapped.
 __global__ void ports_kernel(int B, int hu, int hv, const double* __restrict__ wavelength,
                              const double* __restrict__ period, const double* __restrict__ theta,
                              const double* __restrict__ phi, const cplx* __restrict__ eps_top,
-                             const cplx* __restrict__ eps_bot, PortVectors pv) {
+                             const cplx* __restrict__ eps_bot, const cplx* __restrict__ eps_inc, PortVectors pv) {
   const int b = blockIdx.x;
   const int nu = 2 * hu + 1, nv = 2 * hv + 1, N = nu * nv, n = 2 * N;
   const double lam = wavelength[b];
   const cplx et = eps_top[b], eb = eps_bot[b];
-  // lossless superstrate: N_phase = sqrt(Re eps), k_inc = N sin(theta) (cos phi, sin phi)
-  const double index = sqrt(et.x);
+  // lossless incidence medium: N_phase = sqrt(Re eps), k_inc = N sin(theta) (cos phi, sin phi)
+  const double index = sqrt((eps_inc ? eps_inc[b] : et).x);
   const double st = sin(theta[b]);
   const double ph = phi[b];
   const double kix = index * st * cos(ph), kiy = index * st * sin(ph);
@@ -1620,7 +1622,7 @@ int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int co
   int* pivM = ar.get<int>((size_t)P * n);
   if (!ar.ok()) return -1;
   ports_kernel<<<Bc, 128, 0, s>>>(Bc, d.hu, d.hv, d.wavelength + first, d.period + 2 * first, d.theta + first,
-                                  d.phi + first, d.eps_top + first, d.eps_bot + first, pv); note_launch();
+                                  d.phi + first, d.eps_top + first, d.eps_bot + first, nullptr, pv); note_launch();
   pairs_kernel<<<nblk(P, 128), 128, 0, s>>>(Bc, L, d.layer_index + (long long)first * L,
                                             d.thickness + (long long)first * L, pair_layer, pair_solve, pair_thick);
   note_launch();
@@ -1769,7 +1771,7 @@ int smm_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* Wm, con
   int* pivM = ar.get<int>((size_t)P * n);
   if (!ar.ok()) return -1;
   ports_kernel<<<Bc, 128, 0, s>>>(Bc, d.hu, d.hv, d.wavelength + first, d.period + 2 * first, d.theta + first,
-                                  d.phi + first, d.eps_top + first, d.eps_bot + first, pv); note_launch();
+                                  d.phi + first, d.eps_top + first, d.eps_bot + first, nullptr, pv); note_launch();
   pairs_kernel<<<nblk(P, 128), 128, 0, s>>>(Bc, L, nullptr, d.thickness + (long long)first * L, pair_layer,
                                             pair_solve, pair_thick);
   note_launch();
@@ -1818,6 +1820,225 @@ int smm_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* Wm, con
   getrf<RC>(s, P, n, bV, n, n2, pivV, n, st, L);
   stage_c_refined(s, Bc, L, N, OMd, Zbd, bW, bV, pivW, pivV, X, pv, d, first, out, st, Mk, pivM, Ak, pivA, Rk,
                   S1, S2, S3, pivS, rb, kRefinePasses);
+  return 0;
+}
+
+// ------------------------------------------ scattering-matrix export (wb_scattering_matrix)
+// The four blocks of the stack's S at the half-space ports, as the reference publishes them
+// (Outputs(scattering=True), scattering.py:482-605). The cascade lit in every port column from
+// the superstrate gives S11 (the reflected columns) and S21 (the transmitted ones); the mirrored
+// stack -- layers in reverse order, half-spaces swapped, the same order wavevectors -- gives S22
+// and S12 the same way. Under z -> -z tangential E keeps its sign and tangential H changes it,
+// which is the relation between a layer's down- and up-going (W, V) columns, so the rotated,
+// factored modes of each layer serve both orientations unchanged. The blocks leave in the
+// centre frame, C S C with C = diag((-1)^(m+n)) on both polarization halves.
+
+// out = diag(d) in (+ diag(e) in2 when e): k columns of length n per batch
+__global__ void dscale_cols_kernel(int B, int n, int k, const cplx* __restrict__ d, const cplx* __restrict__ in,
+                                   long long in_bs, const cplx* __restrict__ e, const cplx* __restrict__ in2,
+                                   long long in2_bs, cplx* __restrict__ out, long long out_bs) {
+  const long long nk = (long long)n * k;
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * nk) return;
+  const long long b = idx / nk, rem = idx % nk;
+  const int i = (int)(rem % n);
+  cplx v = cmul(d[b * n + i], in[b * in_bs + rem]);
+  if (e) v = cadd(v, cmul(e[b * n + i], in2[b * in2_bs + rem]));
+  out[b * out_bs + rem] = v;
+}
+
+// rhs1 = wg o (g + h), rhs2 = vg o (g - h)
+__global__ void gh_cols_kernel(int B, int n, int k, const cplx* __restrict__ g, const cplx* __restrict__ h,
+                               const cplx* __restrict__ wg, const cplx* __restrict__ vg, cplx* __restrict__ r1,
+                               cplx* __restrict__ r2, long long bs) {
+  const long long nk = (long long)n * k;
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * nk) return;
+  const long long b = idx / nk, rem = idx % nk;
+  const int i = (int)(rem % n);
+  const cplx gg = g[b * bs + rem], hh = h[b * bs + rem];
+  r1[b * bs + rem] = cmul(wg[b * n + i], cadd(gg, hh));
+  r2[b * bs + rem] = cmul(vg[b * n + i], csub(gg, hh));
+}
+
+// g = X o (r1 + r2)  (2 c+ at the bottom of the layer)
+__global__ void ct_cols_kernel(int B, int n, int k, const cplx* __restrict__ r1, const cplx* __restrict__ r2,
+                               const cplx* __restrict__ X, long long x_ps, cplx* __restrict__ g, long long bs) {
+  const long long nk = (long long)n * k;
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * nk) return;
+  const long long b = idx / nk, rem = idx % nk;
+  const int i = (int)(rem % n);
+  g[b * bs + rem] = cmul(X[b * x_ps + i], cadd(r1[b * bs + rem], r2[b * bs + rem]));
+}
+
+// out[b] = C in[b] C for column-major n x n blocks (n = 2N), C_i = (-1)^(m+n) of order i % N
+__global__ void centre_frame_kernel(int B, int hu, int hv, const cplx* __restrict__ in, long long in_bs,
+                                    cplx* __restrict__ out) {
+  const int nu = 2 * hu + 1, N = nu * (2 * hv + 1), n = 2 * N;
+  const long long n2 = (long long)n * n;
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * n2) return;
+  const long long b = idx / n2, rem = idx % n2;
+  const int i = (int)(rem % n) % N, j = (int)(rem / n) % N;
+  // (u - hu) + (v - hv) has the parity of u + v + hu + hv
+  const int par = (i % nu + i / nu + j % nu + j / nu) & 1;
+  const cplx v = in[b * in_bs + rem];
+  out[b * n2 + rem] = par ? cneg(v) : v;
+}
+
+// Top-down pass of the cascade for the k columns of Cin (Bc, n, k), after cascade_factor: the
+// reflected columns cref = r11 C + r12 h_0 and the transmitted ctrn = t21 g_L, in the
+// half-space port variables (stage_c's three-column pass for any k, FP64).
+static void cascade_columns(cudaStream_t s, int Bc, int L, int n, const cplx* bW, const cplx* bV, const int* pivW,
+                            const int* pivV, const cplx* X, const PortVectors& pv, int32_t* st, const cplx* Mk,
+                            const int* pivM, const cplx* Rk, cplx* G0, int* pivS, const cplx* Cin, int k, cplx* g,
+                            cplx* h, cplx* r1, cplx* r2, cplx* cref, cplx* ctrn) {
+  typedef Cx<double> C;
+  const long long n2 = (long long)n * n, lay_bs = (long long)L * n2, lay_ps = (long long)L * n;
+  const long long r_bs = (long long)(L + 1) * n2, vk = (long long)n * k;
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  const unsigned gk = nblk((long long)Bc * vk, 256);
+  top_kernel<double><<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, (const C*)Rk, r_bs, pv.r22, (C*)G0, n2);
+  note_launch();
+  getrf<double>(s, Bc, n, (C*)G0, n, n2, pivS, n, st, 1);
+  dscale_cols_kernel<<<gk, 256, 0, s>>>(Bc, n, k, pv.r21, Cin, vk, nullptr, nullptr, 0, g, vk); note_launch();
+  getrs<double>(s, Bc, n, (const C*)G0, n, n2, pivS, n, (C*)g, k, n, vk, 0);                      // g_0
+  gemm<double>(s, Bc, n, k, n, one, (const C*)Rk, 1, n, r_bs, (const C*)g, 1, n, vk, zero, (C*)h, 1, n, vk);
+  dscale_cols_kernel<<<gk, 256, 0, s>>>(Bc, n, k, pv.r11, Cin, vk, pv.r12, h, vk, cref, vk); note_launch();
+  for (int l = 0; l < L; ++l) {
+    if (l > 0)
+      gemm<double>(s, Bc, n, k, n, one, (const C*)(Rk + l * n2), 1, n, r_bs, (const C*)g, 1, n, vk, zero, (C*)h, 1,
+                   n, vk);                                                                        // h_l = R_l g_l
+    gh_cols_kernel<<<gk, 256, 0, s>>>(Bc, n, k, g, h, pv.wg, pv.vg, r1, r2, vk); note_launch();
+    getrs<double>(s, Bc, n, (const C*)(bW + l * n2), n, lay_bs, pivW + (long long)l * n, lay_ps, (C*)r1, k, n, vk, 0);
+    getrs<double>(s, Bc, n, (const C*)(bV + l * n2), n, lay_bs, pivV + (long long)l * n, lay_ps, (C*)r2, k, n, vk, 0);
+    ct_cols_kernel<<<gk, 256, 0, s>>>(Bc, n, k, r1, r2, X + (long long)l * n, lay_ps, g, vk); note_launch();
+    getrs<double>(s, Bc, n, (const C*)(Mk + l * n2), n, lay_bs, pivM + (long long)l * n, lay_ps, (C*)g, k, n, vk,
+                  0);                                                                             // g_{l+1}
+  }
+  dscale_cols_kernel<<<gk, 256, 0, s>>>(Bc, n, k, pv.t21, g, vk, nullptr, nullptr, 0, ctrn, vk); note_launch();
+}
+
+// dst = src with the layers of every solve in reverse order (blocks of `per` elements per layer)
+template <class T>
+__global__ void mirror_layers_kernel(long long total, int L, long long per, const T* __restrict__ src,
+                                     T* __restrict__ dst) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= total) return;
+  const long long lp = (long long)L * per;
+  const long long b = idx / lp, rem = idx % lp;
+  const int l = (int)(rem / per);
+  dst[idx] = src[b * lp + (long long)(L - 1 - l) * per + rem % per];
+}
+
+template <class T>
+static void mirror_layers(cudaStream_t s, int Bc, int L, long long per, const T* src, T* dst) {
+  const long long total = (long long)Bc * L * per;
+  mirror_layers_kernel<T><<<nblk(total, 256), 256, 0, s>>>(total, L, per, src, dst); note_launch();
+}
+
+namespace {
+struct ByteCount {
+  size_t b = 0;
+  template <class T> T* get(size_t count) { b += (count * sizeof(T) + 255) & ~(size_t)255; return nullptr; }
+  bool ok() const { return true; }
+};
+}  // namespace
+
+// Scratch of one export chunk; the same carve sizes it (ByteCount) and lays it out (Arena).
+struct ScatterBufs {
+  PortVectors pv[2];                        // [0] lit from the superstrate, [1] the mirrored stack
+  int *pair_layer, *pair_solve;
+  double* pair_thick;
+  cplx *OM[2], *Zb[2], *X[2];               // factored bigW / bigV and X per (solve, layer), both orders
+  int *pivW[2], *pivV[2];
+  cplx *Mk, *Rk, *S1, *S2, *S3, *Cin, *g, *h, *r1, *r2, *cref, *ctrn;
+  int *pivM, *pivS;
+  template <class A> bool carve(A& ar, int Bc, int L, int N) {
+    const size_t n = 2 * (size_t)N, n2 = n * n, P = (size_t)Bc * L;
+    for (PortVectors& v : pv) {
+      v.kx = ar.template get<double>((size_t)Bc * N); v.ky = ar.template get<double>((size_t)Bc * N);
+      v.c = ar.template get<double>((size_t)Bc * N); v.s = ar.template get<double>((size_t)Bc * N);
+      v.kz_top = ar.template get<cplx>((size_t)Bc * N); v.kz_bot = ar.template get<cplx>((size_t)Bc * N);
+      v.wg = ar.template get<cplx>(Bc * n); v.vg = ar.template get<cplx>(Bc * n);
+      v.r11 = ar.template get<cplx>(Bc * n); v.r12 = ar.template get<cplx>(Bc * n);
+      v.r21 = ar.template get<cplx>(Bc * n); v.r22 = ar.template get<cplx>(Bc * n);
+      v.t11 = ar.template get<cplx>(Bc * n); v.t21 = ar.template get<cplx>(Bc * n);
+      v.nt = ar.template get<cplx>(Bc); v.nb = ar.template get<cplx>(Bc);
+    }
+    pair_layer = ar.template get<int>(P); pair_solve = ar.template get<int>(P);
+    pair_thick = ar.template get<double>(P);
+    for (int o = 0; o < 2; ++o) {
+      OM[o] = ar.template get<cplx>(P * n2); Zb[o] = ar.template get<cplx>(P * n2);
+      X[o] = ar.template get<cplx>(P * n);
+      pivW[o] = ar.template get<int>(P * n); pivV[o] = ar.template get<int>(P * n);
+    }
+    Mk = ar.template get<cplx>(P * n2); pivM = ar.template get<int>(P * n);
+    Rk = ar.template get<cplx>((P + Bc) * n2);
+    S1 = ar.template get<cplx>(Bc * n2); S2 = ar.template get<cplx>(Bc * n2); S3 = ar.template get<cplx>(Bc * n2);
+    pivS = ar.template get<int>(Bc * n);
+    Cin = ar.template get<cplx>(Bc * n2); g = ar.template get<cplx>(Bc * n2); h = ar.template get<cplx>(Bc * n2);
+    r1 = ar.template get<cplx>(Bc * n2); r2 = ar.template get<cplx>(Bc * n2);
+    cref = ar.template get<cplx>(Bc * n2); ctrn = ar.template get<cplx>(Bc * n2);
+    return ar.ok();
+  }
+};
+
+size_t scattering_chunk_bytes(int N, int L, int chunk) {
+  ByteCount c;
+  ScatterBufs sb;
+  sb.carve(c, chunk, L, N);
+  return c.b;
+}
+
+int scattering_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* Wm, const cplx* Vm, const cplx* qm,
+                     int first, int count, cplx* S11, cplx* S12, cplx* S21, cplx* S22, int32_t* status) {
+  const int N = (2 * d.hu + 1) * (2 * d.hv + 1), n = 2 * N, L = d.n_layers;
+  const long long n2 = (long long)n * n;
+  const int Bc = count, P = Bc * L;
+  int32_t* st = status + first;
+  ar.reset();
+  ScatterBufs sb;
+  if (!sb.carve(ar, Bc, L, N)) return -1;
+  const cplx *et = d.eps_top + first, *eb = d.eps_bot + first;
+  ports_kernel<<<Bc, 128, 0, s>>>(Bc, d.hu, d.hv, d.wavelength + first, d.period + 2 * first, d.theta + first,
+                                  d.phi + first, et, eb, nullptr, sb.pv[0]); note_launch();
+  ports_kernel<<<Bc, 128, 0, s>>>(Bc, d.hu, d.hv, d.wavelength + first, d.period + 2 * first, d.theta + first,
+                                  d.phi + first, eb, et, et, sb.pv[1]); note_launch();
+  pairs_kernel<<<nblk(P, 128), 128, 0, s>>>(Bc, L, nullptr, d.thickness + (long long)first * L, sb.pair_layer,
+                                            sb.pair_solve, sb.pair_thick);
+  note_launch();
+  const long long off = (long long)first * L;
+  cudaMemcpyAsync(sb.OM[0], Wm + off * n2, sizeof(cplx) * P * n2, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(sb.Zb[0], Vm + off * n2, sizeof(cplx) * P * n2, cudaMemcpyDeviceToDevice, s);
+  xq_kernel<<<nblk((long long)P * n, 256), 256, 0, s>>>(P, n, qm + off * n, sb.pair_solve, sb.pair_thick,
+                                                        d.wavelength + first, sb.X[0]);
+  note_launch();
+  sp_rotate_kernel<double><<<nblk((long long)P * N * n, 256), 256, 0, s>>>(
+      P, N, sb.pair_solve, sb.pv[0].c, sb.pv[0].s, (Cx<double>*)sb.OM[0], (Cx<double>*)sb.Zb[0], n2);
+  note_launch();
+  getrf<double>(s, P, n, (Cx<double>*)sb.OM[0], n, n2, sb.pivW[0], n, st, L);
+  getrf<double>(s, P, n, (Cx<double>*)sb.Zb[0], n, n2, sb.pivV[0], n, st, L);
+  // the mirrored stack's layer l is layer L-1-l: the same factors, X and pivots, reordered
+  mirror_layers(s, Bc, L, n2, sb.OM[0], sb.OM[1]);
+  mirror_layers(s, Bc, L, n2, sb.Zb[0], sb.Zb[1]);
+  mirror_layers(s, Bc, L, (long long)n, sb.X[0], sb.X[1]);
+  mirror_layers(s, Bc, L, (long long)n, sb.pivW[0], sb.pivW[1]);
+  mirror_layers(s, Bc, L, (long long)n, sb.pivV[0], sb.pivV[1]);
+  typedef Cx<double> C;
+  for (int o = 0; o < 2; ++o) {
+    cascade_factor<double>(s, Bc, L, N, (C*)sb.OM[o], (C*)sb.Zb[o], sb.pivW[o], sb.pivV[o], sb.X[o], sb.pv[o], st,
+                           (C*)sb.Mk, sb.pivM, (C*)sb.Rk, (C*)sb.S1, (C*)sb.S2, (C*)sb.S3, sb.pivS, nullptr, nullptr);
+    zset_identity(s, Bc, n, sb.Cin, n, n2);
+    cascade_columns(s, Bc, L, n, sb.OM[o], sb.Zb[o], sb.pivW[o], sb.pivV[o], sb.X[o], sb.pv[o], st, sb.Mk, sb.pivM,
+                    sb.Rk, sb.S1, sb.pivS, sb.Cin, n, sb.g, sb.h, sb.r1, sb.r2, sb.cref, sb.ctrn);
+    const unsigned gb = nblk((long long)Bc * n2, 256);
+    centre_frame_kernel<<<gb, 256, 0, s>>>(Bc, d.hu, d.hv, sb.cref, n2, (o ? S22 : S11) + (long long)first * n2);
+    note_launch();
+    centre_frame_kernel<<<gb, 256, 0, s>>>(Bc, d.hu, d.hv, sb.ctrn, n2, (o ? S12 : S21) + (long long)first * n2);
+    note_launch();
+  }
   return 0;
 }
 

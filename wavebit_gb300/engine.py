@@ -188,6 +188,29 @@ def smm_solve(W, V, q, inp, hu, hv, precision='double', amplitudes=False, handle
     return res + ((amps,) if amplitudes else ())
 
 
+def scattering_matrix(W, V, q, inp, hu, hv, handle=None):
+    """The stack's scattering matrix at its half-space ports from given modes
+    (wb_scattering_matrix). ``W, V, q`` and ``inp`` as for :func:`smm_solve`. Returns
+    ``(S11, S12, S21, S22, status)``: each block ``(B, 2N, 2N)`` in natural orientation, s
+    amplitudes then p port variables, about the cell centre."""
+    dev = W.device
+    n = 2 * n_orders(hu, hv)
+    B, L = inp.B, inp.L
+    Wc = W.transpose(-1, -2).contiguous()
+    Vc = V.transpose(-1, -2).contiguous()
+    qc = q.contiguous()
+    S = torch.empty((4, B, n, n), dtype=torch.complex128, device=dev)
+    status = torch.zeros(B, dtype=torch.int32, device=dev)
+    h = handle or _lib.handle(dev.index or 0)
+    _lib.check(h.lib.wb_scattering_matrix(
+        h.h, B, L, hu, hv, Wc.data_ptr(), Vc.data_ptr(), qc.data_ptr(), inp.thickness.data_ptr(),
+        inp.wavelength.data_ptr(), inp.period.data_ptr(), inp.theta.data_ptr(), inp.phi.data_ptr(),
+        inp.eps_top.data_ptr(), inp.eps_bot.data_ptr(), S[0].data_ptr(), S[1].data_ptr(), S[2].data_ptr(),
+        S[3].data_ptr(), status.data_ptr(), _stream()))
+    S = S.transpose(-1, -2)
+    return S[0], S[1], S[2], S[3], status
+
+
 def solve_host(eps, layer_index, thickness, wavelength, period, theta, phi, eps_top, eps_bot, pol,
                hu, hv, precision='double', handle=None):
     """Whole solve from host (NumPy) buffers through ``wb_solve_host``."""

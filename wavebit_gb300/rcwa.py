@@ -12,6 +12,7 @@ Everything numerical runs in libwbgpu.so; there is no CPU path.
 from dataclasses import dataclass, field
 import math
 import warnings
+from typing import NamedTuple
 
 import numpy as np
 import torch
@@ -113,10 +114,91 @@ class Excitation:
 
 
 @dataclass(frozen=True)
+class Outputs:
+    """What a run keeps beyond R and T (the reference's ``rcwa.Outputs``): ``scattering`` keeps
+    the stack's scattering matrix of every wavelength (``Result.scattering``)."""
+    scattering: bool = False
+
+
+@dataclass(frozen=True)
 class Problem:
     stack: Stack
     excitation: Excitation
     units: Units = field(default_factory=Units)
+    outputs: Outputs = field(default_factory=Outputs)
+
+
+class Port(NamedTuple):
+    """The basis one end of a :class:`ScatteringMatrix` counts (scattering.py:379-425 of the
+    reference): the retained orders' in-plane wavevectors over k0 (one per order, ``i = n*n_u +
+    m``), the half-space the port opens into, and the channel (``'sp'``: N s amplitudes over N p
+    port variables)."""
+    kx_over_k0: object
+    ky_over_k0: object
+    refractive_index: object
+    mu: object
+    channel: str
+
+
+def _port_disagreement(a, b, tol=1e-12):
+    """Why ports ``a`` and ``b`` are not the same basis, or ``None`` (scattering.py:655-700)."""
+    if a.channel != b.channel:
+        return f'they count different polarizations: {a.channel!r} against {b.channel!r}'
+
+    def differ(x, y):
+        if (x is None) != (y is None):
+            return True
+        if x is None:
+            return False
+        xa, ya = np.asarray(x), np.asarray(y)
+        return xa.shape != ya.shape or bool(np.max(np.abs(xa - ya)) > tol)
+
+    if differ(a.kx_over_k0, b.kx_over_k0) or differ(a.ky_over_k0, b.ky_over_k0):
+        return ('their retained orders are different in-plane wavevectors; for lossless media choose '
+                'theta_b = arcsin(sin(theta_a) * n_a / n_b) so that both pieces share k_par')
+    if differ(a.refractive_index, b.refractive_index) or differ(a.mu, b.mu):
+        return 'they open into different half-spaces; both pieces have to name the same joint medium'
+    return None
+
+
+def redheffer_star(S_a, S_b):
+    """``S_a * S_b`` of two block 4-tuples (scattering.py:191-200 of the reference)."""
+    a11, a12, a21, a22 = S_a
+    b11, b12, b21, b22 = S_b
+    I = torch.eye(a11.shape[-1], dtype=a11.dtype, device=a11.device)
+    D_i = torch.linalg.inv(I - b11 @ a22)
+    F_i = torch.linalg.inv(I - a22 @ b11)
+    return (a11 + a12 @ D_i @ b11 @ a21, a12 @ D_i @ b12, b21 @ F_i @ a21, b22 + b21 @ F_i @ a22 @ b12)
+
+
+class ScatteringMatrix(NamedTuple):
+    """The stack's scattering matrix at its two half-space ports (scattering.py:482-605 of the
+    reference), torch tensors of side 2N: rows and columns are the N s amplitudes followed by the
+    N p port variables (the p wave's magnetic field, so ``S11`` of a unit p column is ``-r_p``),
+    every order referenced at the cell centre. ``S11`` reflects back into the incidence medium,
+    ``S21`` transmits into the far half-space, ``S12`` / ``S22`` are the same for light arriving
+    from the far side."""
+    S11: object
+    S12: object
+    S21: object
+    S22: object
+    entry_port: Port
+    exit_port: Port
+
+    @property
+    def blocks(self):
+        return (self.S11, self.S12, self.S21, self.S22)
+
+    def cascade(self, beyond):
+        """This stack followed by ``beyond`` (the piece the light reaches next), refused when the
+        two ports where they meet are not the same basis (scattering.py:552-604)."""
+        if not isinstance(beyond, ScatteringMatrix):
+            raise TypeError(f'cascade() takes a ScatteringMatrix, got {type(beyond).__name__}')
+        why = _port_disagreement(self.exit_port, beyond.entry_port)
+        if why is not None:
+            raise ValueError(f'cascade() cannot join these two: {why}')
+        return ScatteringMatrix(*redheffer_star(self.blocks, beyond.blocks), entry_port=self.entry_port,
+                                exit_port=beyond.exit_port)
 
 
 @dataclass(frozen=True)
@@ -166,6 +248,10 @@ def _numerics_orders(numerics):
     return orders
 
 
+def _wants_scattering(problem):
+    return bool(getattr(getattr(problem, 'outputs', None), 'scattering', False))
+
+
 def _integrated(numerics):
     """Whether the Li slots take integrated (closed-form segment) coefficients."""
     val = getattr(numerics, 'fourier_coefficients', None)
@@ -182,6 +268,9 @@ def _resolve(problem, numerics):
     period = tuple(float(p) for p in stack.period)
     if len(period) == 1:
         period = (period[0], period[0])
+    if getattr(getattr(problem, 'outputs', None), 'fields', False):
+        raise UnsupportedFeatureError('field reconstruction is outside the GB300 raster path',
+                                      path='outputs.fields')
     layers = tuple(stack.layers)
     if not layers:
         raise ValidationError('the stack has no layers', path='stack.layers')
@@ -285,7 +374,7 @@ def check(problem, *, numerics=None, backend='gb300', device='cuda', precision='
 class Result:
     """R and T with the reference's ``(wavelength, order_v, order_u)`` axes, on the device."""
 
-    def __init__(self, R, T, R_sp, T_sp, status, wavelengths, diagnostics, amplitudes=None):
+    def __init__(self, R, T, R_sp, T_sp, status, wavelengths, diagnostics, amplitudes=None, scattering=None):
         self.R, self.T = R, T
         self.outputs = {'incident': {'R': R, 'T': T},
                         's_inc': {'R': R_sp[0], 'T': T_sp[0]},
@@ -294,6 +383,15 @@ class Result:
         self.wavelengths = wavelengths
         self.diagnostics = diagnostics
         self.amplitudes = amplitudes
+        self._scattering = scattering
+
+    @property
+    def scattering(self):
+        """One :class:`ScatteringMatrix` per wavelength (results.py:137-141 of the reference)."""
+        if self._scattering is None:
+            raise UnsupportedFeatureError('Request Outputs(scattering=True) with the SMM algorithm before running.',
+                                          code='outputs.unavailable', path='outputs.scattering')
+        return self._scattering
 
     @property
     def absorption(self):
@@ -320,7 +418,8 @@ class Prepared:
         if problem is not None and not _same_rasters(r['rasters'], self.resolved['rasters']):
             conv = _assemble_layers(r['rasters'], *r['orders'], self.handle, self.integrated)
         L = len(r['rasters'])
-        return self._solve(r, conv, np.tile(np.arange(L), (len(r['wavelengths']), 1)), amplitudes)
+        scattering = _wants_scattering(self.problem if problem is None else problem)
+        return self._solve(r, conv, np.tile(np.arange(L), (len(r['wavelengths']), 1)), amplitudes, scattering)
 
     def _batch(self, r, conv, layer_index, idx, wl, theta, precision, amplitudes):
         """One wb_solve_batch over the wavelengths ``idx`` (with their own, possibly detuned,
@@ -331,8 +430,10 @@ class Prepared:
                                  np.full(k, r['eps_top']), np.full(k, r['eps_bot']), np.tile(r['pol'], (k, 1)))
         return engine.solve_batch(conv, inp, precision=precision, amplitudes=amplitudes, handle=self.handle)
 
-    def _solve(self, r, conv, layer_index, amplitudes=False):
-        """Solve every wavelength of ``r`` with the layers ``layer_index[b]`` of ``conv``."""
+    def _solve(self, r, conv, layer_index, amplitudes=False, scattering=False):
+        """Solve every wavelength of ``r`` with the layers ``layer_index[b]`` of ``conv``; with
+        ``scattering`` also keep the stack's scattering matrix of each (at the same, possibly
+        detuned, wavelength and angle)."""
         B = len(r['wavelengths'])
         wl = np.asarray(r['wavelengths'], dtype=np.float64).copy()
         th = np.full(B, float(r['theta']))
@@ -369,8 +470,47 @@ class Prepared:
                 'grazing': tuple(bool(s & _lib.WB_ST_GRAZING) for s in st),
                 'status': st, 'precision': self.precision,
                 'fallback_solves': tuple(int(i) for i in fallback), 'detuned': moved}
+        S = self._scattering(r, conv, np.asarray(layer_index), wl, th) if scattering else None
         return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]), status, tuple(r['wavelengths']),
-                      diag, out[3] if amplitudes else None)
+                      diag, out[3] if amplitudes else None, S)
+
+    def _scattering(self, r, conv, layer_index, wl, th, budget=2 << 30):
+        """The stack's scattering matrix per wavelength (Outputs(scattering=True)): the FP64 modes
+        of every (wavelength, layer) pair (wb_layer_modes), then wb_scattering_matrix, a chunk of
+        wavelengths at a time so that at most ``budget`` bytes of modes and blocks are held."""
+        from .adjoint import ports
+        hu, hv = r['orders']
+        B, L = layer_index.shape
+        n = 2 * engine.n_orders(hu, hv)
+        dev = conv.buf.device
+        chunk = max(1, int(budget // ((2 * L + 4) * n * n * 16)))
+        n_top, n_bot = complex(np.sqrt(complex(r['eps_top']))), complex(np.sqrt(complex(r['eps_bot'])))
+        out = []
+        for lo in range(0, B, chunk):
+            idx = np.arange(lo, min(B, lo + chunk))
+            pvs = [ports(float(wl[b]), r['period'], float(th[b]), r['phi'], r['eps_top'], r['eps_bot'], hu, hv, dev)
+                   for b in idx]
+            kx = torch.stack([p['kx'] for p in pvs]).repeat_interleave(L, 0)
+            ky = torch.stack([p['ky'] for p in pvs]).repeat_interleave(L, 0)
+            _, q, W, V, st_modes = engine.layer_modes(conv, layer_index[idx].reshape(-1), kx, ky, precision='double',
+                                                      handle=self.handle)
+            k = len(idx)
+            inp = engine.BatchInputs(layer_index[idx], np.tile(r['thickness'], (k, 1)), wl[idx],
+                                     np.tile(r['period'], (k, 1)), th[idx], np.full(k, r['phi']),
+                                     np.full(k, r['eps_top']), np.full(k, r['eps_bot']), np.tile(r['pol'], (k, 1)))
+            S11, S12, S21, S22, st = engine.scattering_matrix(W, V, q, inp, hu, hv, handle=self.handle)
+            bad = (st.cpu().numpy() | st_modes.cpu().numpy().reshape(k, L).max(axis=1)) & ~_lib.WB_ST_GRAZING
+            if np.any(bad & _lib.WB_ST_SINGULAR):
+                raise NumericalError('a factorization of the scattering matrix met an exact zero pivot',
+                                     code='rcwa.singular')
+            if np.any(bad):
+                raise NumericalError('the scattering matrix is not finite', code='rcwa.nonfinite')
+            for i, b in enumerate(idx):
+                kxo, kyo = pvs[i]['kx'].cpu().numpy(), pvs[i]['ky'].cpu().numpy()
+                out.append(ScatteringMatrix(S11[i], S12[i], S21[i], S22[i],
+                                            entry_port=Port(kxo, kyo, n_top, 1.0, 'sp'),
+                                            exit_port=Port(kxo, kyo, n_bot, 1.0, 'sp')))
+        return tuple(out)
 
     def _detune(self, r, conv, layer_index, wl, th, st, merge, amplitudes):
         """The reference's auto-detune ladder (engine.py:6382-6480), opt-in through
