@@ -479,3 +479,142 @@ def solve_stack(structure, thickness, wavelength, period, hu, hv, theta=0.0, phi
     if keep:
         out['layers'] = layers
     return out
+
+# ------------------------------------------------------------ fields (Outputs(fields=True))
+
+_Z0 = 1.0 / (8.8541878188e-12 * 299792458.0)     # free-space impedance, units.py:7-9
+_TOP_FACE = 1.0                                  # scattering.py:225-232
+
+
+def below_reflections(S_layers, S_trn):
+    """``(gamma, F)``: the reflection below each split plane and each layer's gap-to-gap map,
+    bottom-up (scattering.py:236-267)."""
+    n = len(S_layers)
+    I = np.eye(S_trn[0].shape[0], dtype=np.complex128)
+    gamma, F = [None] * (n + 1), [None] * n
+    gamma[n] = S_trn[0]
+    for p in range(n - 1, -1, -1):
+        s11, s12, s21, s22 = S_layers[p]
+        below = gamma[p + 1]
+        F[p] = np.linalg.solve(I - s22 @ below, s21)
+        gamma[p] = s11 + s12 @ (below @ F[p])
+    return gamma, F
+
+
+def field_state(S_ref, S_trn, S_layers, AB, roots, c_inc):
+    """Each layer's ``(+, -)`` mode amplitudes, ``+`` at its top face and ``-`` at its bottom,
+    read off the gap amplitudes of the cascade (scattering.py:270-350); a mode with
+    ``|k0 q d| < 1`` takes its ``-`` from the top face (modal_gradient.two_face, value only)."""
+    I = np.eye(S_trn[0].shape[0], dtype=np.complex128)
+    gamma, F = below_reflections(S_layers, S_trn)
+    g = np.linalg.solve(I - S_ref[3] @ gamma[0], S_ref[2] @ c_inc)
+    out = []
+    for p, ((A, B), (q, k0_d)) in enumerate(zip(AB, roots)):
+        g_next = F[p] @ g
+        up_top = gamma[p] @ g
+        plus = 0.5 * (A @ g + B @ up_top)
+        minus_top = 0.5 * (B @ g + A @ up_top)
+        minus_bottom = 0.5 * (B @ g_next + A @ (gamma[p + 1] @ g_next))
+        keep = (np.abs(q * k0_d) < _TOP_FACE)[:, None]
+        with np.errstate(over='ignore', invalid='ignore'):
+            carried = np.exp(k0_d * q)[:, None] * minus_top
+        out.append((plus, np.where(keep, carried, minus_bottom)))
+        g = g_next
+    return out
+
+
+def layer_field_coefficients(W, V, q, d, k0, epz_i, kxg, kyg, plus, minus, z):
+    """Per-order ``(Sx, Sy, -Sz, i Ux, i Uy, -i Uz)`` at depths ``z`` below a layer's top face,
+    in the propagation frame (fields.py:630-790, 2D layout, ``U = i H``)."""
+    N = kxg.shape[0]
+    z = np.asarray(z, dtype=np.float64)[:, None]
+    fwd = np.exp(-k0 * q[None, :] * z)                  # (nz, n)
+    bwd = np.exp(k0 * q[None, :] * (z - d))
+    ap = fwd * plus[None, :]
+    am = bwd * minus[None, :]
+    a1p, a2p, a1m, a2m = ap[:, :N], ap[:, N:], am[:, :N], am[:, N:]
+    W11, W12, W21, W22 = W[:N, :N], W[:N, N:], W[N:, :N], W[N:, N:]
+    V11, V12, V21, V22 = V[:N, :N], V[:N, N:], V[N:, :N], V[N:, N:]
+    s1, s2, d1, d2 = a1p + a1m, a2p + a2m, -a1p + a1m, -a2p + a2m
+    Sx = s1 @ W11.T + s2 @ W12.T
+    Sy = s1 @ W21.T + s2 @ W22.T
+    Ux = d1 @ V11.T + d2 @ V12.T
+    Uy = d1 @ V21.T + d2 @ V22.T
+    Sz = 1j * (kxg[None, :] * Uy - kyg[None, :] * Ux) @ epz_i.T
+    Uz = 1j * (kxg[None, :] * Sy - kyg[None, :] * Sx)
+    return np.stack([Sx, Sy, -Sz, 1j * Ux, 1j * Uy, -1j * Uz], axis=-1)   # (nz, N, 6)
+
+
+def field_phasors(structure, thickness, wavelength, period, hu, hv, theta, phi, eps_top, eps_bot,
+                  polarization, amplitude, x, y, z, conv=None):
+    """Collocated ``(Ex, Ey, Ez, Hx, Hy, Hz)`` at the points ``x`` (from the cell centre),
+    ``y`` and ``z`` (upward from the stack's bottom face; a face belongs to the layer above it),
+    shape ``(nz, ny, nx, 6)``, E in V/m per V/m of ``amplitude`` and H in A/m
+    (results.py:148-229, field_result.py:332-700, fields.py:630-790). Layers are listed entry
+    (top) face first, as :func:`solve_stack` takes them."""
+    structure = np.asarray(structure, dtype=np.complex128)
+    thickness = np.asarray(thickness, dtype=np.float64)
+    L = structure.shape[0]
+    if conv is None:
+        conv = to_conv_mat_raster_sampled(structure, hu, hv)
+    epx_all, epy_all, epz_i_all = conv
+    k_inc = incident_kxy(theta, phi, eps_top)
+    kx, ky = separable_kxy(wavelength, period, k_inc, hu, hv)
+    kxg, kyg = order_grid(kx, ky)
+    N = kxg.shape[0]
+    k0 = 2 * _PI / wavelength
+    eps_top, eps_bot = np.complex128(eps_top), np.complex128(eps_bot)
+    n_top = np.sqrt(eps_top)
+    k_par_sq = kxg ** 2 + kyg ** 2
+    kz_top, kz_bot = boundary_kz(eps_top, k_par_sq), boundary_kz(eps_bot, k_par_sq)
+    yg = gap_waves(kxg, kyg)
+    I, O = np.eye(N, dtype=np.complex128), np.zeros((N, N), np.complex128)
+    W_top = np.block([[I, O], [O, -1j * np.diag(kz_top) / eps_top]])
+    V_top = np.block([[-1j * np.diag(kz_top), O], [O, I]])
+    W_bot = np.block([[I, O], [O, -1j * np.diag(kz_bot) / eps_bot]])
+    V_bot = np.block([[-1j * np.diag(kz_bot), O], [O, I]])
+    W_gap = np.block([[I, O], [O, -1j * np.diag(yg)]])
+    V_gap = np.block([[-1j * np.diag(yg), O], [O, I]])
+    varphi = order_azimuth(kyg.reshape(ky.shape[0], kx.shape[0]), kxg.reshape(ky.shape[0], kx.shape[0]), phi)
+    c, s = np.cos(varphi), np.sin(varphi)
+    S_ref = s_reflection(W_top, V_top, W_gap, V_gap)
+    S_trn = s_transmission(W_bot, V_bot, W_gap, V_gap)
+    modes, S_layers, AB, roots = [], [], [], []
+    for i in range(L):
+        W, V, q, w, _ = layer_modes_2d(kxg, kyg, epx_all[i], epy_all[i], epz_i_all[i])
+        big_W, big_V = sp_modes_2d(W, V, c, s, N)
+        X = np.diag(np.exp(-k0 * thickness[i] * q))
+        A, B = ab_matrices(big_W, big_V, W_gap, V_gap)
+        S_layers.append(s_layer(A, B, X))
+        AB.append((A, B))
+        roots.append((q, k0 * thickness[i]))
+        modes.append((W, V, q))
+    a_s, a_p = polarization_pair(polarization)
+    delta = np.zeros((N, 1), np.complex128)
+    delta[N // 2] = 1.0
+    c_inc = np.concatenate([a_s * delta, -1j * n_top * a_p * delta], axis=0)
+    amps = field_state(S_ref, S_trn, S_layers, AB, roots, c_inc)
+    # public heights -> (layer in propagation order, depth below its top face)
+    z = np.asarray(z, dtype=np.float64).reshape(-1)
+    ds = thickness[::-1]                                  # bottom layer first
+    edges = np.concatenate([[0.0], np.cumsum(ds)])
+    owner = np.minimum((z[:, None] >= edges[None, 1:]).sum(axis=1), L - 1)
+    coef = np.zeros((z.shape[0], N, 6), np.complex128)
+    for j in range(L):
+        sel = np.flatnonzero(owner == j)
+        if not sel.size:
+            continue
+        p = L - 1 - j
+        depth = ds[j] - (z[sel] - edges[j])
+        W, V, q = modes[p]
+        plus, minus = amps[p]
+        coef[sel] = layer_field_coefficients(W, V, q, thickness[p], k0, epz_i_all[p], kxg, kyg,
+                                             plus[:, 0], minus[:, 0], depth)
+    coef = coef * np.array([1, 1, -1, -1, -1, 1])[None, None, :]          # mirror into the scene frame
+    m = order_labels(hu)[None, :] + order_labels(hv)[:, None]
+    coef = coef * np.where(m.reshape(-1) % 2 == 0, 1.0, -1.0)[None, :, None]   # corner -> centre
+    xs = np.asarray(x, dtype=np.float64)
+    ys = np.asarray(y, dtype=np.float64)
+    phase = np.exp(1j * k0 * (xs[None, :, None] * kxg[None, None, :] + ys[:, None, None] * kyg[None, None, :]))
+    out = np.einsum('yxo,zoc->zyxc', phase, coef)
+    return amplitude * out * np.array([1, 1, 1, 1 / _Z0, 1 / _Z0, 1 / _Z0])

@@ -14,6 +14,8 @@ It writes
   segment) coefficients, ``fourier_coefficients='integrated'``;
 * ``ref_scattering.npz`` -- the stack's exported scattering matrix (``Outputs(scattering=True)``)
   of five of those scenes;
+* ``ref_fields.npz`` -- collocated field phasors (``Outputs(fields=True)``, ``result.field``) of
+  five of those scenes at explicit points, s and p incidence;
 * ``legacy_cases.npz`` -- the efficiencies that the reference's own frozen legacy golden file
   (``tests/fixtures/legacy_rcwa/golden_legacy.npz``) holds for its 1D, conical and 2D sampled-Li
   cases, with the inputs those cases are defined by (``tests/fixtures/legacy_rcwa/gen_goldens.py``).
@@ -182,6 +184,49 @@ def make_scattering_cases():
     print('ref_scattering.npz:', len(names), 'cases')
 
 
+def make_field_cases():
+    """Collocated field phasors (``Outputs(fields=True)``, ``result.field(x=, y=, z=)``,
+    results.py:148-229) of a few small scenes at explicit points: interior heights, an internal
+    face and both outer faces; ``x``, ``y`` from the cell centre."""
+    from wavebit import Material, Units, rcwa
+    out = {}
+    names = []
+    for case in ref_cases():
+        if case['name'] not in ('grating_1d', 'crossed_0', 'crossed_1', 'crossed_4', 'symmetric_pillar'):
+            continue
+        n = case['name']
+        names.append(n)
+        for key in ('structure', 'thickness', 'wavelength', 'period', 'orders', 'theta', 'phi',
+                    'eps_top', 'eps_bot'):
+            out[f'{n}__{key}'] = np.asarray(case[key])
+        st = case['structure'][::-1]
+        th = np.asarray(case['thickness'], dtype=float)[::-1]
+        total = float(th.sum())
+        layers = tuple(rcwa.Layer(thickness=float(t), epsilon=np.asarray(e)) for e, t in zip(st, th))
+        px, py = (float(v) for v in case['period'])
+        x = np.array([-0.31 * px, 0.0, 0.12 * px, 0.45 * px])
+        y = np.array([-0.27 * py, 0.08 * py, 0.5 * py])
+        faces = np.concatenate([[0.0], np.cumsum(th)])
+        z = np.unique(np.concatenate([faces, faces[:-1] + 0.37 * th, faces[:-1] + 0.81 * th]))
+        for pol, amp in (('s', 1.0), ('p', 2.5)):
+            prob = rcwa.Problem(
+                units=Units(length='nm'),
+                stack=rcwa.Stack(period=case['period'], top=Material(epsilon=case['eps_top']),
+                                 bottom=Material(epsilon=case['eps_bot']), layers=layers),
+                excitation=rcwa.Excitation(wavelength=case['wavelength'], sources=(
+                    rcwa.PlaneWave(polarization=pol, theta=case['theta'], phi=case['phi'], amplitude=amp),)),
+                outputs=rcwa.Outputs(fields=True))
+            res = rcwa.run(prob, numerics=rcwa.Numerics(orders=case['orders']))
+            f = res.field(x=x, y=y, z=z)
+            out[f'{n}__field_{pol}'] = np.asarray(f.values)
+            out[f'{n}__amplitude_{pol}'] = np.asarray(amp)
+        out[f'{n}__x'], out[f'{n}__y'], out[f'{n}__z'] = x, y, z
+        out[f'{n}__total'] = np.asarray(total)
+    out['names'] = np.array(names)
+    np.savez_compressed(os.path.join(HERE, 'ref_fields.npz'), **out)
+    print('ref_fields.npz:', len(names), 'cases')
+
+
 def make_legacy_cases():
     """Efficiencies from the reference's frozen legacy golden file, with their inputs."""
     gold = np.load(os.path.join(REF, 'tests/fixtures/legacy_rcwa/golden_legacy.npz'))
@@ -221,4 +266,5 @@ if __name__ == '__main__':
     make_ref_cases()
     make_integrated_cases()
     make_scattering_cases()
+    make_field_cases()
     make_legacy_cases()

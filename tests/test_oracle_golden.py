@@ -190,3 +190,24 @@ def test_exported_scattering_matrix_matches_reference(name):
     r_s, t_s = out['amps'][0][1].reshape(-1), out['amps'][2][1].reshape(-1)
     assert np.abs(mine[0][:N, N // 2] - d * r_s).max() <= 1e-13
     assert np.abs(mine[2][:N, N // 2] - d * t_s).max() <= 1e-13
+
+
+FIELD_NAMES = list(np.load(os.path.join(GOLDEN, 'ref_fields.npz'))['names'])
+
+
+@pytest.mark.parametrize('name', FIELD_NAMES)
+def test_field_phasors_match_reference(name):
+    """Collocated (Ex, Ey, Ez, Hx, Hy, Hz) at explicit points -- interior heights, internal faces
+    (read in the layer above) and both outer faces -- against the reference's
+    ``result.field(x=, y=, z=)`` (results.py:148-229), s and p incidence with a source amplitude.
+    E and H are each held to 1e-12 of their own largest magnitude."""
+    c = _case(np.load(os.path.join(GOLDEN, 'ref_fields.npz')), name)
+    hu, hv = (int(v) for v in c['orders'])
+    for pol in ('s', 'p'):
+        got = O.field_phasors(c['structure'], c['thickness'], float(c['wavelength']), tuple(c['period']), hu, hv,
+                              float(c['theta']), float(c['phi']), complex(c['eps_top']), complex(c['eps_bot']), pol,
+                              float(c[f'amplitude_{pol}']), c['x'], c['y'], c['z'])
+        want = c[f'field_{pol}'][0]
+        for part in (slice(0, 3), slice(3, 6)):
+            scale = np.abs(want[..., part]).max()
+            assert np.abs(got[..., part] - want[..., part]).max() <= 1e-12 * scale, (name, pol, part)
