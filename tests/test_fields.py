@@ -1,0 +1,149 @@
+"""Field reconstruction (``Outputs(fields=True)``, ``Result.field``): the device-agnostic state
+and synthesis of ``wavebit_gb300.fields`` on the CPU with the oracle's modes, and the whole
+lifecycle on a GPU with the kernels' modes, both against the reference's ``result.field``."""
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip('torch')
+
+from oracle import rcwa_oracle as O
+from wavebit_gb300 import fields as F
+from wavebit_gb300 import rcwa
+from wavebit_gb300.adjoint import ports
+
+GOLDEN = os.path.join(os.path.dirname(__file__), 'golden')
+NAMES = list(np.load(os.path.join(GOLDEN, 'ref_fields.npz'))['names'])
+
+
+def _case(name):
+    d = np.load(os.path.join(GOLDEN, 'ref_fields.npz'))
+    return {k.split('__', 1)[1]: d[k] for k in d.files if k.startswith(name + '__')}
+
+
+def _check(got, want, tol, label):
+    for part in (slice(0, 3), slice(3, 6)):
+        scale = np.abs(want[..., part]).max()
+        assert np.abs(got[..., part] - want[..., part]).max() <= tol * scale, (label, part)
+
+
+@pytest.mark.parametrize('name', NAMES)
+def test_state_and_synthesis_match_the_reference_on_the_cpu(name):
+    """build_state + synthesize on CPU tensors, fed the oracle's Cartesian modes and slots."""
+    c = _case(name)
+    hu, hv = (int(v) for v in c['orders'])
+    st = np.asarray(c['structure'], complex)
+    th = np.asarray(c['thickness'], float)
+    wl, per = float(c['wavelength']), tuple(float(p) for p in c['period'])
+    pv = ports(wl, per, float(c['theta']), float(c['phi']), complex(c['eps_top']), complex(c['eps_bot']), hu, hv, 'cpu')
+    kxg, kyg = pv['kx'].numpy(), pv['ky'].numpy()
+    conv = O.to_conv_mat_raster_sampled(st, hu, hv)
+    modes, epz = [], []
+    for i in range(st.shape[0]):
+        W, V, q, _, _ = O.layer_modes_2d(kxg + 0j, kyg + 0j, conv[0][i], conv[1][i], conv[2][i])
+        modes.append(tuple(torch.as_tensor(a) for a in (W, V, q)))
+        epz.append(torch.as_tensor(conv[2][i]))
+    for pol in ('s', 'p'):
+        state = F.build_state(modes, epz, th, wl, pv, O.polarization_pair(pol), hu, hv)
+        z, owner, depth = F.height_points(c['z'], th)
+        got = F.synthesize(state, owner, depth, c['x'], c['y'], float(c[f'amplitude_{pol}'])).numpy()
+        _check(got, c[f'field_{pol}'][0], 1e-12, (name, pol))
+
+
+def test_height_rules():
+    """Faces belong to the layer above; counts give every layer both of its faces."""
+    th = np.array([30.0, 50.0, 20.0])                     # top layer first; bottom layer is 20 thick
+    owner, depth = F.heights(th, [0.0, 20.0, 70.0, 100.0, 45.0])
+    assert owner.tolist() == [2, 1, 0, 0, 1]
+    assert np.allclose(depth, [20.0, 50.0, 30.0, 0.0, 25.0])
+    z, owner, depth = F.height_points(3, th)
+    assert np.allclose(z, [0, 10, 20, 20, 45, 70, 70, 85, 100])
+    assert owner.tolist() == [2, 2, 2, 1, 1, 1, 0, 0, 0]
+    assert np.allclose(depth, [20, 10, 0, 50, 25, 0, 30, 15, 0])
+    with pytest.raises(ValueError):
+        F.heights(th, [-1.0])
+    with pytest.raises(ValueError):
+        F.heights(th, [100.5])
+    assert np.allclose(F.axis_points(3, 500.0, 'x'), [-250.0, 0.0, 250.0])
+
+
+def test_a_result_without_fields_refuses_to_sample():
+    res = rcwa.Result(None, None, (None, None), (None, None), None, (), {})
+    with pytest.raises(rcwa.UnsupportedFeatureError) as e:
+        res.field(x=[0.0], y=[0.0], z=[0.0])
+    assert e.value.code == 'outputs.unavailable' and e.value.path == 'outputs.fields'
+
+
+def _problem(c, pol):
+    st, th = np.asarray(c['structure'], complex), np.asarray(c['thickness'], float)
+    layers = tuple(rcwa.Layer(thickness=float(t), epsilon=e) for e, t in zip(st[::-1], th[::-1]))
+    return rcwa.Problem(units=rcwa.Units('nm'),
+                        stack=rcwa.Stack(period=tuple(float(p) for p in c['period']),
+                                         top=rcwa.Material(epsilon=complex(c['eps_top'])),
+                                         bottom=rcwa.Material(epsilon=complex(c['eps_bot'])), layers=layers),
+                        excitation=rcwa.Excitation(wavelength=float(c['wavelength']), sources=(
+                            rcwa.PlaneWave(polarization=pol, theta=float(c['theta']), phi=float(c['phi']),
+                                           amplitude=float(c[f'amplitude_{pol}'])),)),
+                        outputs=rcwa.Outputs(fields=True))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('name', NAMES)
+def test_lifecycle_fields_match_the_reference(name):
+    """rcwa.run(..., Outputs(fields=True)).field(x=, y=, z=) with the kernels' modes, within
+    1e-10 of the reference's own phasors (E and H each against their largest magnitude)."""
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    c = _case(name)
+    hu, hv = (int(v) for v in c['orders'])
+    for pol in ('s', 'p'):
+        res = rcwa.run(_problem(c, pol), numerics=rcwa.Numerics(orders=(hu, hv)))
+        f = res.field(x=c['x'], y=c['y'], z=c['z'])
+        assert f.values.shape == (1, len(c['z']), len(c['y']), len(c['x']), 6)
+        assert f.values.device.type == 'cuda' and f.components == F.COMPONENTS
+        _check(f.values[0].cpu().numpy(), c[f'field_{pol}'][0], 1e-10, (name, pol))
+
+
+def _oracle_layer_modes(conv, pair_layer, kx, ky, precision='double', handle=None):
+    """A CPU stand-in for engine.layer_modes: the oracle's eigen-solve of each pair's layer."""
+    out = [[], [], [], []]
+    for p, l in enumerate(np.asarray(pair_layer).reshape(-1)):
+        kxg, kyg = kx[p].numpy() + 0j, ky[p].numpy() + 0j
+        W, V, q, w, _ = O.layer_modes_2d(kxg, kyg, *(conv.slot(k)[int(l)].numpy() for k in range(3)))
+        for lst, a in zip(out, (w, q, W, V)):
+            lst.append(torch.as_tensor(a))
+    w, q, W, V = (torch.stack(x) for x in out)
+    return w, q, W, V, torch.zeros(len(out[0]), dtype=torch.int32)
+
+
+@pytest.mark.parametrize('name', ['crossed_0', 'symmetric_pillar'])
+def test_lifecycle_field_states_on_the_cpu(name, monkeypatch):
+    """Prepared._field_states and Result.field with the stage-B kernel replaced by the oracle on
+    the CPU: the per-(wavelength, layer) bookkeeping, slots, heights and source amplitude."""
+    from wavebit_gb300 import engine
+    c = _case(name)
+    hu, hv = (int(v) for v in c['orders'])
+    st = np.asarray(c['structure'], complex)
+    conv_np = O.to_conv_mat_raster_sampled(st, hu, hv)
+    conv = engine.ConvStack.from_matrices(*(torch.as_tensor(a) for a in conv_np), hu, hv)
+    monkeypatch.setattr(engine, 'layer_modes', _oracle_layer_modes)
+    for pol in ('s', 'p'):
+        r = rcwa._resolve(_problem(c, pol), rcwa.Numerics(orders=(hu, hv)))
+        p = rcwa.Prepared.__new__(rcwa.Prepared)
+        p.handle = None
+        L = st.shape[0]
+        wl = np.asarray(r['wavelengths'], dtype=np.float64)
+        th = np.full(len(wl), r['theta'])
+        states = p._field_states(r, conv, np.tile(np.arange(L), (len(wl), 1)), wl, th)
+        res = rcwa.Result(None, None, (None, None), (None, None), None, tuple(wl), {}, None, None, states,
+                          (np.asarray(r['thickness']), r['period'], r['amplitude']))
+        f = res.field(x=c['x'], y=c['y'], z=c['z'])
+        _check(f.values[0].numpy(), c[f'field_{pol}'][0], 1e-12, (name, pol))
+        with pytest.raises(rcwa.ValidationError) as e:
+            res.field(x=c['x'], y=c['y'], z=[-5.0])
+        assert e.value.code == 'field.coordinates'
+        with pytest.raises(rcwa.UnsupportedFeatureError):
+            res.field(x=c['x'], y=c['y'], z=c['z'], reconstruction='lalanne')
+        counts = res.field(x=3, y=2, z=2)
+        assert counts.values.shape == (1, 2 * L, 2, 3, 6)

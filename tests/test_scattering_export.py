@@ -76,15 +76,12 @@ def test_the_matrix_is_only_there_when_requested():
     assert e.value.code == 'outputs.unavailable' and e.value.path == 'outputs.scattering'
 
 
-def test_field_outputs_are_refused():
-    class _Out:
-        fields = True
-        scattering = False
+def test_both_outputs_resolve():
     p = rcwa.Problem(stack=rcwa.Stack(layers=(rcwa.Layer(thickness=10.0, epsilon=2.0),), period=(500., 500.)),
-                     excitation=rcwa.Excitation(600.0, (rcwa.PlaneWave(polarization='s'),)), outputs=_Out())
-    with pytest.raises(rcwa.UnsupportedFeatureError) as e:
-        rcwa._resolve(p, rcwa.Numerics())
-    assert e.value.path == 'outputs.fields'
+                     excitation=rcwa.Excitation(600.0, (rcwa.PlaneWave(polarization='s', amplitude=3.0),)),
+                     outputs=rcwa.Outputs(fields=True, scattering=True))
+    r = rcwa._resolve(p, rcwa.Numerics())
+    assert r['amplitude'] == 3.0 and rcwa._wants_fields(p) and rcwa._wants_scattering(p)
 
 
 def _problem(c, **kw):

@@ -1,0 +1,221 @@
+"""Field reconstruction inside the stack (``Outputs(fields=True)``, ``Result.field``).
+
+The reference keeps, per wavelength, every layer's ``(+, -)`` mode amplitudes of the incident
+column, read off the S-matrix cascade (rcwa/_engine/scattering.py:236-350), and sums the
+collocated phasors from them on request (rcwa/results.py:148-229,
+rcwa/_engine/field_result.py:332-700, rcwa/_engine/fields.py:630-790). Here the modes are the
+stage-B kernels' (wb_layer_modes, FP64); the amplitudes come from the cascade's own recursion
+(:func:`wavebit_gb300.adjoint.cascade_forward`) and the synthesis is batched matrix products,
+all on the device that holds the modes. ``'plain'`` reconstruction only.
+
+Conventions (the reference's): ``x`` and ``y`` are measured from the cell centre, ``z`` upward
+from the stack's bottom face, a face belongs to the layer above it; values are
+``(wavelength, z, y, x, 6)`` for ``(Ex, Ey, Ez, Hx, Hy, Hz)``, E in V/m for a source of
+``amplitude`` V/m and H in A/m, time convention ``exp(-i omega t)``.
+"""
+import math
+from typing import NamedTuple
+
+import numpy as np
+import torch
+
+from .adjoint import cascade_forward
+
+#: free-space impedance 1 / (epsilon0 c0) (units.py:7-9 of the reference)
+Z0 = 1.0 / (8.8541878188e-12 * 299792458.0)
+#: a mode's ``-`` amplitude is read off the layer's top face below this ``|k0 q d|``
+#: (scattering.py:225-232, modal_gradient.two_face)
+TOP_FACE = 1.0
+#: (Ex, Ey, Ez, Hx, Hy, Hz) parity between the propagation frame (z into the stack from the
+#: lit face) and the public frame (z up from the bottom): E is polar, H axial (fields.py:114-118)
+MIRROR = (1.0, 1.0, -1.0, -1.0, -1.0, 1.0)
+COMPONENTS = ('Ex', 'Ey', 'Ez', 'Hx', 'Hy', 'Hz')
+
+
+class LayerState(NamedTuple):
+    """One layer of one wavelength: Cartesian modes (natural orientation), roots, thickness,
+    the inverse-zz convolution slot (cell corner) and the incident column's amplitudes."""
+    W: torch.Tensor
+    V: torch.Tensor
+    q: torch.Tensor
+    d: float
+    epz_i: torch.Tensor
+    plus: torch.Tensor
+    minus: torch.Tensor
+
+
+class FieldState(NamedTuple):
+    """What one wavelength keeps for :meth:`Result.field`; layers entry (top) face first."""
+    k0: float
+    kx: torch.Tensor          # (N,) per-order kx / k0
+    ky: torch.Tensor
+    odd: torch.Tensor         # (N,) True where (-1)^(m+n) = -1 (corner -> centre sign)
+    layers: tuple
+
+
+class FieldSamples(NamedTuple):
+    """Collocated phasors and the points they were taken at (results.py:214-229)."""
+    coordinates: dict
+    values: torch.Tensor
+    components: tuple
+    sampling: str
+    metadata: dict
+
+
+def sp_rotate(W, V, c, s):
+    """The s/p rotation of a layer's Cartesian modes (solve_2d.py:2584-2616), as the kernels'
+    sp_rotate_kernel and :func:`wavebit_gb300.adjoint.solve_and_grad` apply it."""
+    N = c.shape[0]
+    W1, W2, V1, V2 = W[:N], W[N:], V[:N], V[N:]
+    bw = torch.cat([c[:, None] * W2 - s[:, None] * W1, c[:, None] * W1 + s[:, None] * W2], 0)
+    bv = torch.cat([c[:, None] * V1 + s[:, None] * V2, c[:, None] * V2 - s[:, None] * V1], 0)
+    return bw, bv
+
+
+def layer_amplitudes(modes, thickness, k0, pv, C):
+    """Every layer's ``(+, -)`` amplitudes for the incidence columns ``C`` (n, k): ``+`` at the
+    layer's top face, ``-`` at its bottom face (scattering.py:270-350). ``modes`` is a list of
+    ``(W, V, q)`` (Cartesian, entry face first), ``pv`` the port vectors of
+    :func:`wavebit_gb300.adjoint.ports`.
+
+    With ``g``, ``h = R g`` the gap amplitudes above a layer and ``bW``, ``bV`` its rotated modes,
+    the layer's amplitudes at that face are ``(b1 + b2)/2`` down and ``(b1 - b2)/2`` up,
+    ``b1 = bW^-1 wg (g + h)``, ``b2 = bV^-1 vg (g - h)``; the ``-`` amplitude is read at the bottom
+    face from the gap below, except for a mode with ``|k0 q d| < 1``, whose two amplitudes
+    nearly cancel in the field and which takes its top-face value carried down by
+    ``exp(k0 q d)`` (modal_gradient.two_face)."""
+    bW, bV, Xs = [], [], []
+    for (W, V, q), d in zip(modes, thickness):
+        bw, bv = sp_rotate(W, V, pv['c'], pv['s'])
+        bW.append(bw); bV.append(bv)
+        Xs.append(torch.exp(-k0 * float(d) * q))
+    _, _, sv = cascade_forward(bW, bV, Xs, pv, C)
+    wg, vg = pv['wg'][:, None], pv['vg'][:, None]
+    out = []
+    for l, ((W, V, q), d) in enumerate(zip(modes, thickness)):
+        b1, b2 = sv['td'][l]['b1'], sv['td'][l]['b2']
+        plus = 0.5 * (b1 + b2)
+        minus_top = 0.5 * (b1 - b2)
+        gn = sv['g'][l + 1]
+        hn = sv['Rk'][l + 1] @ gn
+        minus_bottom = 0.5 * (torch.linalg.solve(bW[l], wg * (gn + hn)) - torch.linalg.solve(bV[l], vg * (gn - hn)))
+        kd = k0 * float(d)
+        keep = (torch.abs(q * kd) < TOP_FACE)[:, None]
+        carried = torch.exp(torch.where(keep[:, 0], kd * q, torch.zeros_like(q)))[:, None] * minus_top
+        out.append((plus, torch.where(keep, carried, minus_bottom)))
+    return out
+
+
+def layer_coefficients(layer, k0, kx, ky, depth):
+    """Per-order ``(Sx, Sy, -Sz, i Ux, i Uy, -i Uz)`` of the incident column at ``depth`` (nz,)
+    below the layer's top face, in the propagation frame (fields.py:630-790, ``U = i H``):
+    ``Sx, Sy = W (a+ + a-)``, ``Ux, Uy = V (a- - a+)`` with ``a+ = exp(-k0 q z) c+`` and
+    ``a- = exp(k0 q (z - d)) c-``; ``Sz = i epz_i (Kx Uy - Ky Ux)``, ``Uz = i (Kx Sy - Ky Sx)``."""
+    N = kx.shape[0]
+    z = depth[:, None]
+    q = layer.q[None, :]
+    ap = torch.exp(-k0 * q * z) * layer.plus[None, :]
+    am = torch.exp(k0 * q * (z - layer.d)) * layer.minus[None, :]
+    S = (ap + am) @ layer.W.T                                # (nz, n): Sx | Sy
+    U = (am - ap) @ layer.V.T                                #           Ux | Uy
+    Sx, Sy, Ux, Uy = S[:, :N], S[:, N:], U[:, :N], U[:, N:]
+    Sz = 1j * (kx[None, :] * Uy - ky[None, :] * Ux) @ layer.epz_i.T
+    Uz = 1j * (kx[None, :] * Sy - ky[None, :] * Sx)
+    return torch.stack([Sx, Sy, -Sz, 1j * Ux, 1j * Uy, -1j * Uz], dim=-1)   # (nz, N, 6)
+
+
+def heights(thickness_top_first, z):
+    """Public heights -> ``(owner, depth)``: the layer (entry face first) holding each height and
+    the depth below that layer's top face. Heights run upward from the bottom face; a face
+    belongs to the layer above it; the outer faces are inside (field_result.py:375-398)."""
+    ds = np.asarray(thickness_top_first, dtype=np.float64)[::-1]       # bottom layer first
+    L = ds.shape[0]
+    edges = np.concatenate([[0.0], np.cumsum(ds)])
+    z = np.asarray(z, dtype=np.float64).reshape(-1)
+    if not np.all(np.isfinite(z)):
+        raise ValueError('z must hold finite heights')
+    if z.size and (z.min() < 0.0 or z.max() > edges[-1]):
+        raise ValueError(f'z coordinates must lie inside the stack, 0 to {edges[-1]:g} measured upward from '
+                         f'its bottom; got {z.min():g} to {z.max():g}')
+    j = np.minimum((z[:, None] >= edges[None, 1:]).sum(axis=1), L - 1)
+    return L - 1 - j, ds[j] - (z - edges[j])
+
+
+def synthesize(state, owner, depth, x, y, amplitude):
+    """``(nz, ny, nx, 6)`` phasors of one wavelength at the heights ``(owner, depth)`` and the
+    centre-origin points ``x`` (nx,), ``y`` (ny,) (field_result.py:109-122, 640-690)."""
+    dev = state.kx.device
+    nz, N = owner.shape[0], state.kx.shape[0]
+    coef = torch.zeros((nz, N, 6), dtype=torch.complex128, device=dev)
+    for p, layer in enumerate(state.layers):
+        sel = np.flatnonzero(owner == p)
+        if sel.size:
+            idx = torch.as_tensor(sel, device=dev)
+            d = torch.as_tensor(depth[sel], dtype=torch.float64, device=dev)
+            coef[idx] = layer_coefficients(layer, state.k0, state.kx, state.ky, d)
+    coef = coef * torch.as_tensor(MIRROR, dtype=torch.complex128, device=dev)
+    coef = torch.where(state.odd[None, :, None], -coef, coef)
+    xs = torch.as_tensor(x, dtype=torch.float64, device=dev)
+    ys = torch.as_tensor(y, dtype=torch.float64, device=dev)
+    arg = state.k0 * (xs[None, :, None] * state.kx[None, None, :] + ys[:, None, None] * state.ky[None, None, :])
+    phase = torch.exp(1j * arg).reshape(-1, N)                         # (ny*nx, N)
+    out = torch.einsum('po,zoc->zpc', phase, coef).reshape(nz, ys.shape[0], xs.shape[0], 6)
+    scale = torch.as_tensor([1, 1, 1, 1 / Z0, 1 / Z0, 1 / Z0], dtype=torch.complex128, device=dev)
+    return complex(amplitude) * out * scale
+
+
+def axis_points(spec, extent, name):
+    """A count spans ``[-extent/2, extent/2]`` inclusive; explicit coordinates are taken as
+    given (field_result.py:85-106)."""
+    if isinstance(spec, (int, np.integer)) and not isinstance(spec, bool):
+        if spec < 1:
+            raise ValueError(f'{name} must be a positive integer count')
+        return np.linspace(-0.5, 0.5, int(spec)) * extent
+    arr = np.asarray(spec, dtype=np.float64)
+    if arr.ndim != 1 or not arr.shape[0] or not np.all(np.isfinite(arr)):
+        raise ValueError(f'{name} must be a positive integer count or a nonempty 1-D array of finite coordinates')
+    return arr
+
+
+def height_points(spec, thickness_top_first):
+    """Heights for a ``z`` request: explicit heights as given, with owners by face rule; a
+    count gives every layer its own ``count`` heights from its bottom face to its top face, so
+    an internal face appears twice, the lower layer's first (field_result.py:375-398)."""
+    if isinstance(spec, (int, np.integer)) and not isinstance(spec, bool):
+        if spec < 1:
+            raise ValueError('z must be a positive integer count')
+        ds = np.asarray(thickness_top_first, dtype=np.float64)[::-1]
+        L = ds.shape[0]
+        edges = np.concatenate([[0.0], np.cumsum(ds)])
+        frac = np.linspace(0.0, 1.0, int(spec))
+        z = np.concatenate([edges[j] + frac * ds[j] for j in range(L)])
+        j = np.repeat(np.arange(L), int(spec))
+        return z, L - 1 - j, ds[j] - (z - edges[j])
+    z = np.asarray(spec, dtype=np.float64).reshape(-1)
+    if z.ndim != 1 or not z.shape[0]:
+        raise ValueError('z must be a positive integer count or a nonempty 1-D array of heights')
+    owner, depth = heights(thickness_top_first, z)
+    return z, owner, depth
+
+
+def order_parity(hu, hv, device):
+    """``(-1)^(m+n) = -1`` over the flattened orders ``i = n*n_u + m``: the sign between a
+    coefficient about the cell corner and the same about its centre (field_result.py:672-679)."""
+    m = np.arange(-hu, hu + 1)[None, :] + np.arange(-hv, hv + 1)[:, None]
+    return torch.as_tensor(m.reshape(-1) % 2 == 1, device=device)
+
+
+def build_state(modes, epz_i, thickness, wavelength, pv, pol, hu, hv):
+    """The :class:`FieldState` of one wavelength from its layers' ``(W, V, q)`` (Cartesian,
+    entry face first), their corner-frame ``epz_i`` slots and the port vectors ``pv``; ``pol``
+    is the source's ``(a_s, a_p)``."""
+    dev = pv['kx'].device
+    k0 = 2 * math.pi / float(wavelength)
+    N = pv['kx'].shape[0]
+    C = torch.zeros((2 * N, 1), dtype=torch.complex128, device=dev)
+    C[N // 2, 0] = complex(pol[0])
+    C[N + N // 2, 0] = -1j * complex(pv['nt']) * complex(pol[1])
+    amps = layer_amplitudes(modes, thickness, k0, pv, C)
+    layers = tuple(LayerState(W, V, q, float(d), e, plus[:, 0], minus[:, 0])
+                   for (W, V, q), d, e, (plus, minus) in zip(modes, thickness, epz_i, amps))
+    return FieldState(k0, pv['kx'], pv['ky'], order_parity(hu, hv, dev), layers)

@@ -116,7 +116,9 @@ class Excitation:
 @dataclass(frozen=True)
 class Outputs:
     """What a run keeps beyond R and T (the reference's ``rcwa.Outputs``): ``scattering`` keeps
-    the stack's scattering matrix of every wavelength (``Result.scattering``)."""
+    the stack's scattering matrix of every wavelength (``Result.scattering``), ``fields`` the
+    layers' mode amplitudes that ``Result.field`` samples."""
+    fields: bool = False
     scattering: bool = False
 
 
@@ -252,6 +254,10 @@ def _wants_scattering(problem):
     return bool(getattr(getattr(problem, 'outputs', None), 'scattering', False))
 
 
+def _wants_fields(problem):
+    return bool(getattr(getattr(problem, 'outputs', None), 'fields', False))
+
+
 def _integrated(numerics):
     """Whether the Li slots take integrated (closed-form segment) coefficients."""
     val = getattr(numerics, 'fourier_coefficients', None)
@@ -268,9 +274,6 @@ def _resolve(problem, numerics):
     period = tuple(float(p) for p in stack.period)
     if len(period) == 1:
         period = (period[0], period[0])
-    if getattr(getattr(problem, 'outputs', None), 'fields', False):
-        raise UnsupportedFeatureError('field reconstruction is outside the GB300 raster path',
-                                      path='outputs.fields')
     layers = tuple(stack.layers)
     if not layers:
         raise ValidationError('the stack has no layers', path='stack.layers')
@@ -328,9 +331,13 @@ def _resolve(problem, numerics):
         a_s, a_p = (complex(v) for v in pol)
         nrm = math.sqrt(abs(a_s) ** 2 + abs(a_p) ** 2)
         a_s, a_p = a_s / nrm, a_p / nrm
+    amplitude = complex(np.asarray(getattr(src, 'amplitude', 1.0)).reshape(()))
+    if not np.isfinite(amplitude):
+        raise ValidationError('the source amplitude must be finite', path='excitation.sources[0].amplitude')
     orders = _numerics_orders(_numerics_or_default(numerics))
     return dict(rasters=rasters, thickness=np.array(thick), period=period, eps_top=eps_top,
-                eps_bot=eps_bot, wavelengths=wl, theta=theta, phi=phi, pol=(a_s, a_p), orders=orders)
+                eps_bot=eps_bot, wavelengths=wl, theta=theta, phi=phi, pol=(a_s, a_p), orders=orders,
+                amplitude=amplitude)
 
 
 def _numerics_or_default(numerics):
@@ -374,7 +381,8 @@ def check(problem, *, numerics=None, backend='gb300', device='cuda', precision='
 class Result:
     """R and T with the reference's ``(wavelength, order_v, order_u)`` axes, on the device."""
 
-    def __init__(self, R, T, R_sp, T_sp, status, wavelengths, diagnostics, amplitudes=None, scattering=None):
+    def __init__(self, R, T, R_sp, T_sp, status, wavelengths, diagnostics, amplitudes=None, scattering=None,
+                 field_states=None, field_geometry=None):
         self.R, self.T = R, T
         self.outputs = {'incident': {'R': R, 'T': T},
                         's_inc': {'R': R_sp[0], 'T': T_sp[0]},
@@ -384,6 +392,36 @@ class Result:
         self.diagnostics = diagnostics
         self.amplitudes = amplitudes
         self._scattering = scattering
+        self._field_states = field_states
+        self._field_geometry = field_geometry
+
+    def field(self, *, x, y, z, reconstruction='plain'):
+        """Collocated complex phasors at explicit points or counts (results.py:148-229 of the
+        reference): values ``(wavelength, z, y, x, 6)`` for ``(Ex, Ey, Ez, Hx, Hy, Hz)``, E in
+        V/m and H in A/m; ``x``, ``y`` from the cell centre, ``z`` upward from the stack's bottom
+        face (a face belongs to the layer above it). ``reconstruction='plain'`` only."""
+        from . import fields as F
+        if not self._field_states:
+            raise UnsupportedFeatureError('This result did not retain field reconstruction state. Request '
+                                          'Outputs(fields=True).', code='outputs.unavailable', path='outputs.fields')
+        if reconstruction in ('lalanne', 'split', 'splitw'):
+            raise UnsupportedFeatureError(f'reconstruction={reconstruction!r} is outside the GB300 raster path; '
+                                          "use 'plain'", code='field.reconstruction', path='reconstruction')
+        if reconstruction != 'plain':
+            raise ValidationError(f"reconstruction must be 'plain', 'lalanne', 'split' or 'splitw', not "
+                                  f'{reconstruction!r}.', code='field.reconstruction', path='reconstruction')
+        thickness, period, amplitude = self._field_geometry
+        try:
+            xs = F.axis_points(x, period[0], 'x')
+            ys = F.axis_points(y, period[1], 'y')
+            zs, owner, depth = F.height_points(z, thickness)
+        except ValueError as e:
+            raise ValidationError(str(e), code='field.coordinates', path='x/y/z') from e
+        values = torch.stack([F.synthesize(st, owner, depth, xs, ys, amplitude) for st in self._field_states])
+        return F.FieldSamples(coordinates={'x': xs, 'y': ys, 'z': zs, 'wavelength': self.wavelengths},
+                              values=values, components=F.COMPONENTS, sampling='collocated Cartesian phasor',
+                              metadata={'axis_order': ('wavelength', 'z', 'y', 'x', 'component'),
+                                        'time_convention': 'exp(-i*omega*t)'})
 
     @property
     def scattering(self):
@@ -418,8 +456,9 @@ class Prepared:
         if problem is not None and not _same_rasters(r['rasters'], self.resolved['rasters']):
             conv = _assemble_layers(r['rasters'], *r['orders'], self.handle, self.integrated)
         L = len(r['rasters'])
-        scattering = _wants_scattering(self.problem if problem is None else problem)
-        return self._solve(r, conv, np.tile(np.arange(L), (len(r['wavelengths']), 1)), amplitudes, scattering)
+        asked = self.problem if problem is None else problem
+        return self._solve(r, conv, np.tile(np.arange(L), (len(r['wavelengths']), 1)), amplitudes,
+                           _wants_scattering(asked), _wants_fields(asked))
 
     def _batch(self, r, conv, layer_index, idx, wl, theta, precision, amplitudes):
         """One wb_solve_batch over the wavelengths ``idx`` (with their own, possibly detuned,
@@ -430,7 +469,7 @@ class Prepared:
                                  np.full(k, r['eps_top']), np.full(k, r['eps_bot']), np.tile(r['pol'], (k, 1)))
         return engine.solve_batch(conv, inp, precision=precision, amplitudes=amplitudes, handle=self.handle)
 
-    def _solve(self, r, conv, layer_index, amplitudes=False, scattering=False):
+    def _solve(self, r, conv, layer_index, amplitudes=False, scattering=False, fields=False):
         """Solve every wavelength of ``r`` with the layers ``layer_index[b]`` of ``conv``; with
         ``scattering`` also keep the stack's scattering matrix of each (at the same, possibly
         detuned, wavelength and angle)."""
@@ -471,35 +510,66 @@ class Prepared:
                 'status': st, 'precision': self.precision,
                 'fallback_solves': tuple(int(i) for i in fallback), 'detuned': moved}
         S = self._scattering(r, conv, np.asarray(layer_index), wl, th) if scattering else None
+        states = self._field_states(r, conv, np.asarray(layer_index), wl, th) if fields else None
         return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]), status, tuple(r['wavelengths']),
-                      diag, out[3] if amplitudes else None, S)
+                      diag, out[3] if amplitudes else None, S, states,
+                      (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0)))
 
-    def _scattering(self, r, conv, layer_index, wl, th, budget=2 << 30):
-        """The stack's scattering matrix per wavelength (Outputs(scattering=True)): the FP64 modes
-        of every (wavelength, layer) pair (wb_layer_modes), then wb_scattering_matrix, a chunk of
-        wavelengths at a time so that at most ``budget`` bytes of modes and blocks are held."""
+    def _mode_chunks(self, r, conv, layer_index, wl, th, per_wl_bytes, budget=2 << 30):
+        """FP64 modes of every (wavelength, layer) pair (wb_layer_modes), a chunk of wavelengths
+        at a time: yields ``(idx, pvs, q, W, V)`` with W, V Cartesian in natural orientation."""
         from .adjoint import ports
         hu, hv = r['orders']
         B, L = layer_index.shape
-        n = 2 * engine.n_orders(hu, hv)
         dev = conv.buf.device
-        chunk = max(1, int(budget // ((2 * L + 4) * n * n * 16)))
-        n_top, n_bot = complex(np.sqrt(complex(r['eps_top']))), complex(np.sqrt(complex(r['eps_bot'])))
-        out = []
+        chunk = max(1, int(budget // per_wl_bytes))
         for lo in range(0, B, chunk):
             idx = np.arange(lo, min(B, lo + chunk))
             pvs = [ports(float(wl[b]), r['period'], float(th[b]), r['phi'], r['eps_top'], r['eps_bot'], hu, hv, dev)
                    for b in idx]
             kx = torch.stack([p['kx'] for p in pvs]).repeat_interleave(L, 0)
             ky = torch.stack([p['ky'] for p in pvs]).repeat_interleave(L, 0)
-            _, q, W, V, st_modes = engine.layer_modes(conv, layer_index[idx].reshape(-1), kx, ky, precision='double',
-                                                      handle=self.handle)
+            _, q, W, V, st = engine.layer_modes(conv, layer_index[idx].reshape(-1), kx, ky, precision='double',
+                                                handle=self.handle)
+            bad = st.cpu().numpy() & ~_lib.WB_ST_GRAZING
+            if np.any(bad & _lib.WB_ST_SINGULAR):
+                raise NumericalError('a layer factorization met an exact zero pivot', code='rcwa.singular')
+            if np.any(bad):
+                raise NumericalError('the layer eigen-solve did not converge', code='rcwa.nonfinite')
+            yield idx, pvs, q, W, V
+
+    def _field_states(self, r, conv, layer_index, wl, th):
+        """Per wavelength, every layer's modes and the incident column's ``(+, -)`` amplitudes
+        (Outputs(fields=True)), computed on the device from FP64 modes; the states stay resident
+        (2 (2N)^2 complex per layer and wavelength) for ``Result.field``."""
+        from . import fields as F
+        hu, hv = r['orders']
+        B, L = layer_index.shape
+        n = 2 * engine.n_orders(hu, hv)
+        states = []
+        for idx, pvs, q, W, V in self._mode_chunks(r, conv, layer_index, wl, th, (2 * L + 2) * n * n * 16):
+            for i, b in enumerate(idx):
+                modes = [(W[i * L + l], V[i * L + l], q[i * L + l]) for l in range(L)]
+                epz = [conv.slot(2)[int(layer_index[b][l])] for l in range(L)]
+                states.append(F.build_state(modes, epz, r['thickness'], wl[b], pvs[i], r['pol'], hu, hv))
+        return tuple(states)
+
+    def _scattering(self, r, conv, layer_index, wl, th):
+        """The stack's scattering matrix per wavelength (Outputs(scattering=True)): the FP64 modes
+        of every (wavelength, layer) pair, then wb_scattering_matrix, a chunk of wavelengths at a
+        time so that about 2 GiB of modes and blocks are held at once."""
+        hu, hv = r['orders']
+        B, L = layer_index.shape
+        n = 2 * engine.n_orders(hu, hv)
+        n_top, n_bot = complex(np.sqrt(complex(r['eps_top']))), complex(np.sqrt(complex(r['eps_bot'])))
+        out = []
+        for idx, pvs, q, W, V in self._mode_chunks(r, conv, layer_index, wl, th, (2 * L + 4) * n * n * 16):
             k = len(idx)
             inp = engine.BatchInputs(layer_index[idx], np.tile(r['thickness'], (k, 1)), wl[idx],
                                      np.tile(r['period'], (k, 1)), th[idx], np.full(k, r['phi']),
                                      np.full(k, r['eps_top']), np.full(k, r['eps_bot']), np.tile(r['pol'], (k, 1)))
             S11, S12, S21, S22, st = engine.scattering_matrix(W, V, q, inp, hu, hv, handle=self.handle)
-            bad = (st.cpu().numpy() | st_modes.cpu().numpy().reshape(k, L).max(axis=1)) & ~_lib.WB_ST_GRAZING
+            bad = st.cpu().numpy() & ~_lib.WB_ST_GRAZING
             if np.any(bad & _lib.WB_ST_SINGULAR):
                 raise NumericalError('a factorization of the scattering matrix met an exact zero pivot',
                                      code='rcwa.singular')
