@@ -618,3 +618,86 @@ def field_phasors(structure, thickness, wavelength, period, hu, hv, theta, phi, 
     phase = np.exp(1j * k0 * (xs[None, :, None] * kxg[None, None, :] + ys[:, None, None] * kyg[None, None, :]))
     out = np.einsum('yxo,zoc->zyxc', phase, coef)
     return amplitude * out * np.array([1, 1, 1, 1 / _Z0, 1 / _Z0, 1 / _Z0])
+
+# --------------------------------------------------- the ETM connecting algorithm (cross-check)
+
+
+def etm_stack(structure, thickness, wavelength, period, hu, hv, theta=0.0, phi=0.0, eps_top=1.0, eps_bot=1.0,
+              polarization='s', conv=None):
+    """One enhanced-transmittance-matrix solve (solve_2d.py:2619-2843, solve_1d.py:1389-1520):
+    from the substrate up, ``a = (W^-1 F + V^-1 G)/2``, ``b = (W^-1 F - V^-1 G)/2``,
+    ``Y = X b a^-1 X``, ``F = W (I + Y)``, ``G = V (I - Y)``, ``T = T a^-1 X``; then one block
+    solve of the superstrate's boundary equations for ``R_s``, ``R_p`` and ``T_1``,
+    ``(T_s, T_p) = T T_1``. Real in-plane wavevectors and passive layers, where the ETM's
+    labels (conventions.py:252-300) are :func:`mode_q`'s and the max-volume relabelling is off;
+    every layer in the plain (non-run) form of ``_run_ab``. Returns ``R``, ``T`` as
+    :func:`solve_stack` does (given polarization, pure s, pure p)."""
+    structure = np.asarray(structure, dtype=np.complex128)
+    L = structure.shape[0]
+    if conv is None:
+        conv = to_conv_mat_raster_sampled(structure, hu, hv)
+    epx_all, epy_all, epz_i_all = conv
+    k_inc = incident_kxy(theta, phi, eps_top)
+    kx, ky = separable_kxy(wavelength, period, k_inc, hu, hv)
+    kxg, kyg = order_grid(kx, ky)
+    N = kxg.shape[0]
+    n_v, n_u = ky.shape[0], kx.shape[0]
+    k0 = 2 * _PI / wavelength
+    eps_top, eps_bot = np.complex128(eps_top), np.complex128(eps_bot)
+    n_top = np.sqrt(eps_top)
+    k_par_sq = kxg ** 2 + kyg ** 2
+    kz_top, kz_bot = boundary_kz(eps_top, k_par_sq), boundary_kz(eps_bot, k_par_sq)
+    varphi = order_azimuth(kyg.reshape(n_v, n_u), kxg.reshape(n_v, n_u), phi)
+    c, s = np.cos(varphi), np.sin(varphi)
+    I, O = np.eye(N, dtype=np.complex128), np.zeros((N, N), np.complex128)
+    I2 = np.eye(2 * N, dtype=np.complex128)
+    F = np.block([[I, O], [O, -1j * np.diag(kz_bot) / eps_bot]])
+    G = np.block([[-1j * np.diag(kz_bot), O], [O, I]])
+    T = I2.copy()
+    for i in range(L - 1, -1, -1):
+        W, V, q, w, _ = layer_modes_2d(kxg, kyg, epx_all[i], epy_all[i], epz_i_all[i])
+        big_W, big_V = sp_modes_2d(W, V, c, s, N)
+        Wi_F = np.linalg.solve(big_W, F)
+        Vi_G = np.linalg.solve(big_V, G)
+        a, b = 0.5 * (Wi_F + Vi_G), 0.5 * (Wi_F - Vi_G)
+        a_i = np.linalg.inv(a)
+        X = np.diag(np.exp(-k0 * thickness[i] * q))
+        Y = X @ b @ a_i @ X
+        F, G = big_W @ (I2 + Y), big_V @ (I2 - Y)
+        T = T @ a_i @ X
+    kz_inc = kz_top[N // 2]
+    Kt = np.diag(kz_top)
+    final_A = np.block([[I, O, -F[:N, :N], -F[:N, N:]],
+                        [O, 1j * Kt / eps_top, -F[N:, :N], -F[N:, N:]],
+                        [1j * Kt, O, -G[:N, :N], -G[:N, N:]],
+                        [O, I, -G[N:, :N], -G[N:, N:]]])
+    delta = np.zeros((N, 1), np.complex128)
+    delta[N // 2] = 1.0
+    h_p, e_p = n_top, n_top * kz_inc / eps_top
+
+    def column(a_s, a_p):
+        return np.concatenate([-a_s * delta, a_p * e_p * delta, 1j * a_s * kz_inc * delta, 1j * h_p * a_p * delta])
+
+    inc = polarization_pair(polarization)
+    cols = np.concatenate([column(*inc), column(np.sin(np.complex128(_HALF_PI)), np.cos(np.complex128(_HALF_PI))),
+                           column(np.sin(np.complex128(0.0)), np.cos(np.complex128(0.0)))], axis=1)
+    x = np.linalg.solve(final_A, cols)
+    Rs, Rp = x[:N], x[N:2 * N]
+    Tt = T @ x[2 * N:]
+    Ts, Tp = Tt[:N], Tt[N:]
+
+    def as_orders(M):
+        return M.T.reshape(3, n_v, n_u)
+
+    s_power = np.real(kz_inc)
+    p_power = abs(n_top) ** 2 * np.real(kz_inc / eps_top)
+    a_s, a_p = inc
+    denom = np.array([abs(a_s) ** 2 * s_power + abs(a_p) ** 2 * p_power, s_power, p_power]).reshape(3, 1, 1)
+    kzt, kzb = kz_top.reshape(n_v, n_u), kz_bot.reshape(n_v, n_u)
+
+    def wave_power(amp, adm):
+        return np.real(amp * np.conj(amp)) * np.real(adm)
+
+    R = (wave_power(as_orders(Rs), kzt) + wave_power(as_orders(Rp), kzt / eps_top)) / denom
+    Tr = (wave_power(as_orders(Ts), kzb) + wave_power(as_orders(Tp), kzb / eps_bot)) / denom
+    return dict(R=R, T=Tr)

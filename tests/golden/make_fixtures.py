@@ -16,6 +16,8 @@ It writes
   of five of those scenes;
 * ``ref_fields.npz`` -- collocated field phasors (``Outputs(fields=True)``, ``result.field``) of
   five of those scenes at explicit points, s and p incidence;
+* ``ref_etm.npz`` -- per-order R/T of the reference's ETM connecting algorithm on the scenes of
+  ``ref_cases.npz``;
 * ``legacy_cases.npz`` -- the efficiencies that the reference's own frozen legacy golden file
   (``tests/fixtures/legacy_rcwa/golden_legacy.npz``) holds for its 1D, conical and 2D sampled-Li
   cases, with the inputs those cases are defined by (``tests/fixtures/legacy_rcwa/gen_goldens.py``).
@@ -85,7 +87,7 @@ def ref_cases():
     return cases
 
 
-def run_ref(case, pol, coefficients=None):
+def run_ref(case, pol, coefficients=None, algorithm='smm'):
     from wavebit import Material, Units, rcwa
     from wavebit.rcwa import operators
     st = case['structure'][::-1]          # public stacks list layers bottom to top
@@ -97,9 +99,9 @@ def run_ref(case, pol, coefficients=None):
                          bottom=Material(epsilon=case['eps_bot']), layers=layers),
         excitation=rcwa.Excitation(wavelength=case['wavelength'], sources=(
             rcwa.PlaneWave(polarization=pol, theta=case['theta'], phi=case['phi']),)))
-    num = rcwa.Numerics(orders=case['orders'], fourier_coefficients=coefficients)
+    num = rcwa.Numerics(orders=case['orders'], fourier_coefficients=coefficients, algorithm=algorithm)
     res = rcwa.run(prob, numerics=num)
-    ops = operators.assemble(prob, numerics=num)
+    ops = operators.assemble(prob, numerics=rcwa.Numerics(orders=case['orders'], fourier_coefficients=coefficients))
     conv = ops.epsilon[0]
     return np.asarray(res.R)[0], np.asarray(res.T)[0], [np.asarray(c) for c in conv[:3]]
 
@@ -227,6 +229,26 @@ def make_field_cases():
     print('ref_fields.npz:', len(names), 'cases')
 
 
+def make_etm_cases():
+    """Per-order R and T of the reference's ETM connecting algorithm (``Numerics(algorithm='etm')``,
+    solve_2d.py:2619-2843) on the reference scenes, s and p incidence."""
+    out = {}
+    names = []
+    for case in ref_cases():
+        n = case['name']
+        names.append(n)
+        for key in ('structure', 'thickness', 'wavelength', 'period', 'orders', 'theta', 'phi',
+                    'eps_top', 'eps_bot'):
+            out[f'{n}__{key}'] = np.asarray(case[key])
+        for pol in ('s', 'p'):
+            R, T, _ = run_ref(case, pol, algorithm='etm')
+            out[f'{n}__R_{pol}'] = R
+            out[f'{n}__T_{pol}'] = T
+    out['names'] = np.array(names)
+    np.savez_compressed(os.path.join(HERE, 'ref_etm.npz'), **out)
+    print('ref_etm.npz:', len(names), 'cases')
+
+
 def make_legacy_cases():
     """Efficiencies from the reference's frozen legacy golden file, with their inputs."""
     gold = np.load(os.path.join(REF, 'tests/fixtures/legacy_rcwa/golden_legacy.npz'))
@@ -267,4 +289,5 @@ if __name__ == '__main__':
     make_integrated_cases()
     make_scattering_cases()
     make_field_cases()
+    make_etm_cases()
     make_legacy_cases()

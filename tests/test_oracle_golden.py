@@ -211,3 +211,23 @@ def test_field_phasors_match_reference(name):
         for part in (slice(0, 3), slice(3, 6)):
             scale = np.abs(want[..., part]).max()
             assert np.abs(got[..., part] - want[..., part]).max() <= 1e-12 * scale, (name, pol, part)
+
+
+ETM_NAMES = list(np.load(os.path.join(GOLDEN, 'ref_etm.npz'))['names'])
+
+
+@pytest.mark.parametrize('name', ETM_NAMES)
+def test_etm_matches_the_reference_etm_and_the_smm(name):
+    """The oracle's ETM connecting algorithm against the reference's
+    ``Numerics(algorithm='etm')`` run, and against the oracle's own SMM solve: the two connecting
+    algorithms answer one question (solve_2d.py:2619-2843, scattering.py:1185-1456)."""
+    c = _case(np.load(os.path.join(GOLDEN, 'ref_etm.npz')), name)
+    hu, hv = (int(v) for v in c['orders'])
+    args = (c['structure'], c['thickness'], float(c['wavelength']), tuple(c['period']), hu, hv,
+            float(c['theta']), float(c['phi']), complex(c['eps_top']), complex(c['eps_bot']), 's')
+    etm, smm = O.etm_stack(*args), O.solve_stack(*args)
+    for col, pol in ((1, 's'), (2, 'p')):
+        scale = max(np.abs(c[f'R_{pol}']).max(), np.abs(c[f'T_{pol}']).max())
+        for key in ('R', 'T'):
+            assert np.abs(etm[key][col] - c[f'{key}_{pol}']).max() <= 1e-12 * scale, (name, pol, key)
+            assert np.abs(etm[key][col] - smm[key][col]).max() <= 1e-12 * scale, (name, pol, key)
