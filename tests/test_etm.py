@@ -1,0 +1,108 @@
+"""The ETM connecting algorithm (``Numerics(algorithm='etm')``): the device-agnostic recursion of
+``wavebit_gb300.etm`` on the CPU with the oracle's modes, the lifecycle bookkeeping on the CPU
+with the stage-B kernel replaced by the oracle, and the whole path on a GPU -- each against the
+reference's own ETM runs and the SMM."""
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip('torch')
+
+from oracle import rcwa_oracle as O
+from wavebit_gb300 import etm as E
+from wavebit_gb300 import rcwa
+from wavebit_gb300.adjoint import ports
+
+GOLDEN = os.path.join(os.path.dirname(__file__), 'golden')
+NAMES = list(np.load(os.path.join(GOLDEN, 'ref_etm.npz'))['names'])
+
+
+def _case(name):
+    d = np.load(os.path.join(GOLDEN, 'ref_etm.npz'))
+    return {k.split('__', 1)[1]: d[k] for k in d.files if k.startswith(name + '__')}
+
+
+def _check(R, T, c, tol, label):
+    for col, pol in ((1, 's'), (2, 'p')):
+        scale = max(np.abs(c[f'R_{pol}']).max(), np.abs(c[f'T_{pol}']).max())
+        assert np.abs(R[col] - c[f'R_{pol}']).max() <= tol * scale, (label, pol)
+        assert np.abs(T[col] - c[f'T_{pol}']).max() <= tol * scale, (label, pol)
+
+
+@pytest.mark.parametrize('name', NAMES)
+def test_etm_recursion_matches_the_reference_on_the_cpu(name):
+    c = _case(name)
+    hu, hv = (int(v) for v in c['orders'])
+    st = np.asarray(c['structure'], complex)
+    wl = float(c['wavelength'])
+    pv = ports(wl, tuple(float(p) for p in c['period']), float(c['theta']), float(c['phi']),
+               complex(c['eps_top']), complex(c['eps_bot']), hu, hv, 'cpu')
+    conv = O.to_conv_mat_raster_sampled(st, hu, hv)
+    modes = []
+    for i in range(st.shape[0]):
+        W, V, q, _, _ = O.layer_modes_2d(pv['kx'].numpy() + 0j, pv['ky'].numpy() + 0j, conv[0][i], conv[1][i], conv[2][i])
+        modes.append(tuple(torch.as_tensor(a) for a in (W, V, q)))
+    R, T = E.etm_solve(modes, np.asarray(c['thickness'], float), 2 * np.pi / wl, pv, O.polarization_pair('s'),
+                       2 * hu + 1, 2 * hv + 1)
+    _check(R.numpy(), T.numpy(), c, 1e-12, name)
+
+
+def _problem(c, **kw):
+    st, th = np.asarray(c['structure'], complex), np.asarray(c['thickness'], float)
+    layers = tuple(rcwa.Layer(thickness=float(t), epsilon=e) for e, t in zip(st[::-1], th[::-1]))
+    return rcwa.Problem(units=rcwa.Units('nm'),
+                        stack=rcwa.Stack(period=tuple(float(p) for p in c['period']),
+                                         top=rcwa.Material(epsilon=complex(c['eps_top'])),
+                                         bottom=rcwa.Material(epsilon=complex(c['eps_bot'])), layers=layers),
+                        excitation=rcwa.Excitation(wavelength=float(c['wavelength']), sources=(
+                            rcwa.PlaneWave(polarization='s', theta=float(c['theta']), phi=float(c['phi'])),)),
+                        **kw)
+
+
+def test_etm_refuses_a_scattering_matrix():
+    """The ETM never forms a both-sides operator (scattering.py:482-495; _lifecycle.py:130-132)."""
+    c = _case(NAMES[0])
+    p = _problem(c, outputs=rcwa.Outputs(scattering=True))
+    with pytest.raises(rcwa.UnsupportedFeatureError) as e:
+        rcwa._resolve(p, rcwa.Numerics(orders=(1, 1), algorithm='etm'))
+    assert e.value.code == 'rcwa.scattering_algorithm'
+
+
+@pytest.mark.parametrize('name', ['crossed_1', 'symmetric_pillar'])
+def test_lifecycle_etm_on_the_cpu(name, monkeypatch):
+    """Prepared._solve_etm with the stage-B kernel replaced by the oracle on the CPU."""
+    from wavebit_gb300 import engine
+    from test_fields import _oracle_layer_modes
+    c = _case(name)
+    hu, hv = (int(v) for v in c['orders'])
+    st = np.asarray(c['structure'], complex)
+    conv_np = O.to_conv_mat_raster_sampled(st, hu, hv)
+    conv = engine.ConvStack.from_matrices(*(torch.as_tensor(a) for a in conv_np), hu, hv)
+    monkeypatch.setattr(engine, 'layer_modes', _oracle_layer_modes)
+    num = rcwa.Numerics(orders=(hu, hv), algorithm='etm')
+    r = rcwa._resolve(_problem(c), num)
+    p = rcwa.Prepared.__new__(rcwa.Prepared)
+    p.handle, p.numerics, p.precision = None, num, 'double'
+    res = p._solve_etm(r, conv, np.tile(np.arange(st.shape[0]), (1, 1)))
+    assert res.diagnostics['algorithm'] == 'etm'
+    _check(np.stack([res.R[0].numpy(), res.outputs['s_inc']['R'][0].numpy(), res.outputs['p_inc']['R'][0].numpy()]),
+           np.stack([res.T[0].numpy(), res.outputs['s_inc']['T'][0].numpy(), res.outputs['p_inc']['T'][0].numpy()]),
+           c, 1e-12, name)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('name', NAMES)
+def test_lifecycle_etm_matches_the_reference_on_the_gpu(name):
+    """rcwa.run(..., Numerics(algorithm='etm')) with the kernels' modes against the reference's
+    ETM runs, and against this package's own SMM run of the same problem."""
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    c = _case(name)
+    hu, hv = (int(v) for v in c['orders'])
+    etm = rcwa.run(_problem(c), numerics=rcwa.Numerics(orders=(hu, hv), algorithm='etm'))
+    smm = rcwa.run(_problem(c), numerics=rcwa.Numerics(orders=(hu, hv)))
+    R = np.stack([etm.R[0].cpu().numpy()] + [etm.outputs[k]['R'][0].cpu().numpy() for k in ('s_inc', 'p_inc')])
+    T = np.stack([etm.T[0].cpu().numpy()] + [etm.outputs[k]['T'][0].cpu().numpy() for k in ('s_inc', 'p_inc')])
+    _check(R, T, c, 1e-10, name)
+    assert np.abs(etm.R.cpu().numpy() - smm.R.cpu().numpy()).max() <= 1e-10

@@ -74,7 +74,7 @@ def test_bad_orders_are_refused(numerics, path):
     assert e.value.path == path
 
 
-@pytest.mark.parametrize('field,value', [('algorithm', 'etm'), ('fourier_coefficients', 'shape'),
+@pytest.mark.parametrize('field,value', [('algorithm', 'fdtd'), ('fourier_coefficients', 'shape'),
                                          ('factorization', 'nvf'), ('factorization', 'laurent'),
                                          ('li_nesting', 'alternating')])
 def test_numerics_outside_the_path_are_unsupported(field, value):

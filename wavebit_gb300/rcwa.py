@@ -233,7 +233,7 @@ def _numerics_orders(numerics):
     orders = tuple(int(v) for v in getattr(numerics, 'orders', (0, 0)))
     if len(orders) != 2 or min(orders) < 0:
         raise ValidationError('orders must be a pair of nonnegative integers', path='numerics.orders')
-    for name, allowed in (('algorithm', ('smm',)), ('fourier_coefficients', (None, 'sampled', 'integrated')),
+    for name, allowed in (('algorithm', (None, 'smm', 'etm')), ('fourier_coefficients', (None, 'sampled', 'integrated')),
                           ('factorization', (None, 'li')), ('li_nesting', (None, 'fixed'))):
         val = getattr(numerics, name, None)
         val = getattr(val, 'value', val)                # the reference's enums carry the name
@@ -256,6 +256,13 @@ def _wants_scattering(problem):
 
 def _wants_fields(problem):
     return bool(getattr(getattr(problem, 'outputs', None), 'fields', False))
+
+
+def _algorithm(numerics):
+    """``'smm'`` or ``'etm'`` (the connecting algorithm of ``Numerics``)."""
+    val = getattr(numerics, 'algorithm', None)
+    val = getattr(val, 'value', val)
+    return 'etm' if isinstance(val, str) and val.lower() == 'etm' else 'smm'
 
 
 def _integrated(numerics):
@@ -331,6 +338,9 @@ def _resolve(problem, numerics):
         a_s, a_p = (complex(v) for v in pol)
         nrm = math.sqrt(abs(a_s) ** 2 + abs(a_p) ** 2)
         a_s, a_p = a_s / nrm, a_p / nrm
+    if _wants_scattering(problem) and _algorithm(numerics) == 'etm':
+        raise UnsupportedFeatureError('Scattering matrices require algorithm="smm".',
+                                      code='rcwa.scattering_algorithm', path='outputs.scattering')
     amplitude = complex(np.asarray(getattr(src, 'amplitude', 1.0)).reshape(()))
     if not np.isfinite(amplitude):
         raise ValidationError('the source amplitude must be finite', path='excitation.sources[0].amplitude')
@@ -373,7 +383,7 @@ def check(problem, *, numerics=None, backend='gb300', device='cuda', precision='
     resolved = {'order_window': ((0, hu), (0, hv)), 'wavelength_count': len(r['wavelengths']),
                 'layer_count': L, 'fourier_coefficients': 'integrated' if _integrated(numerics) else 'sampled',
                 'factorization': 'li',
-                'algorithm': 'smm', 'solve_path': '2d', 'backend': backend, 'device': device,
+                'algorithm': _algorithm(numerics), 'solve_path': '2d', 'backend': backend, 'device': device,
                 'precision': precision}
     return CheckReport(issues=(), estimates=est, resolved=resolved)
 
@@ -457,8 +467,10 @@ class Prepared:
             conv = _assemble_layers(r['rasters'], *r['orders'], self.handle, self.integrated)
         L = len(r['rasters'])
         asked = self.problem if problem is None else problem
-        return self._solve(r, conv, np.tile(np.arange(L), (len(r['wavelengths']), 1)), amplitudes,
-                           _wants_scattering(asked), _wants_fields(asked))
+        layer_index = np.tile(np.arange(L), (len(r['wavelengths']), 1))
+        if _algorithm(self.numerics) == 'etm':
+            return self._solve_etm(r, conv, layer_index, _wants_fields(asked))
+        return self._solve(r, conv, layer_index, amplitudes, _wants_scattering(asked), _wants_fields(asked))
 
     def _batch(self, r, conv, layer_index, idx, wl, theta, precision, amplitudes):
         """One wb_solve_batch over the wavelengths ``idx`` (with their own, possibly detuned,
@@ -513,6 +525,33 @@ class Prepared:
         states = self._field_states(r, conv, np.asarray(layer_index), wl, th) if fields else None
         return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]), status, tuple(r['wavelengths']),
                       diag, out[3] if amplitudes else None, S, states,
+                      (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0)))
+
+    def _solve_etm(self, r, conv, layer_index, fields=False):
+        """``Numerics(algorithm='etm')``: the ETM recursion over the FP64 modes of every
+        (wavelength, layer) pair (:mod:`wavebit_gb300.etm`), a cross-check of the cascade on the
+        same modes. Fields, when asked for, are read off the cascade's state as with the SMM."""
+        from .etm import etm_solve
+        hu, hv = r['orders']
+        B, L = layer_index.shape
+        n = 2 * engine.n_orders(hu, hv)
+        wl = np.asarray(r['wavelengths'], dtype=np.float64).copy()
+        th = np.full(B, float(r['theta']))
+        Rs, Ts = [None] * B, [None] * B
+        for idx, pvs, q, W, V in self._mode_chunks(r, conv, layer_index, wl, th, (2 * L + 4) * n * n * 16):
+            for i, b in enumerate(idx):
+                modes = [(W[i * L + l], V[i * L + l], q[i * L + l]) for l in range(L)]
+                Rs[b], Ts[b] = etm_solve(modes, r['thickness'], 2 * math.pi / float(wl[b]), pvs[i], r['pol'],
+                                         2 * hu + 1, 2 * hv + 1)
+        R, T = torch.stack(Rs), torch.stack(Ts)
+        if not (bool(torch.isfinite(R).all()) and bool(torch.isfinite(T).all())):
+            raise NumericalError('the ETM solve produced non-finite results', code='rcwa.nonfinite')
+        st = np.zeros(B, dtype=np.int32)
+        diag = {'solve_path': ('2d',) * B, 'algorithm': 'etm', 'effective_wavelengths': tuple(float(v) for v in wl),
+                'grazing': (False,) * B, 'status': st, 'precision': 'double', 'fallback_solves': (), 'detuned': {}}
+        states = self._field_states(r, conv, layer_index, wl, th) if fields else None
+        return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]),
+                      torch.as_tensor(st, device=R.device), tuple(r['wavelengths']), diag, None, None, states,
                       (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0)))
 
     def _mode_chunks(self, r, conv, layer_index, wl, th, per_wl_bytes, budget=2 << 30):
