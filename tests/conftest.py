@@ -8,3 +8,14 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line('markers', 'gpu: needs a CUDA GPU (runs through the C-ABI library)')
+
+
+#: Modules collected after every other one, in their own (alphabetical) order: the ETM and field
+#: paths, which sit on top of the parity-tested stages, so that under ``-x`` a failure there
+#: cannot keep the stage-level parity suites from reporting; and the allocation-free entry point,
+#: whose fixed scratch is shared by the whole process, at the very end.
+_LAST = ('test_etm.py', 'test_fields.py', 'test_zz_no_alloc.py')
+
+
+def pytest_collection_modifyitems(session, config, items):
+    items.sort(key=lambda item: os.path.basename(str(item.fspath)) in _LAST)
