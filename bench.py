@@ -40,6 +40,24 @@ def _dist():
     return world, rank, local
 
 
+def max_over_ranks(t, world, dist=None, device='cpu'):
+    """The slowest rank's time (all_reduce MAX; one value per rank, FP64). Every rank times the
+    same region between the same two barriers, and the job's throughput is set by the rank that
+    took longest."""
+    if world <= 1:
+        return float(t)
+    import torch
+    tt = torch.tensor([float(t)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def whole_job_rate(world, units_per_rank, steps, t_max):
+    """Units per second of the whole job: every rank solves its own ``units_per_rank`` per step
+    (replicas, weak scaling), all of them within the slowest rank's ``t_max``."""
+    return world * units_per_rank * steps / t_max
+
+
 def _config(precision, impl, B, workload='crossed_sweep'):
     if workload == 'crossed_sweep':
         desc = ('crossed_sweep: 3x 256^2 binary rasters + 50 nm eps=-20+1.5j layer, period 1000 nm, '
@@ -272,11 +290,8 @@ def main():
                          'mixed_value': B / tmx, 'mixed_ms_per_step': tmx * 1e3, 'speedup': t64 / tmx,
                          'mixed_form': 'mixed' if args.precision == 'double' else args.precision,
                          'max_abs_dRT': d, 'target': 1e-6, 'within_target': d <= 1e-6}
-    if world > 1:
-        tt = torch.tensor([t], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
-    value = world * B * args.steps / t
+    t = max_over_ranks(t, world, dist, dev)
+    value = whole_job_rate(world, B, args.steps, t)
     st = out[2].cpu().numpy()
 
     # stage-B (eigen-solve pipeline) timing for the roofline: one wb_layer_modes launch over the
