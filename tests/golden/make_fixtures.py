@@ -18,6 +18,8 @@ It writes
   five of those scenes at explicit points, s and p incidence;
 * ``ref_etm.npz`` -- per-order R/T of the reference's ETM connecting algorithm on the scenes of
   ``ref_cases.npz``;
+* ``reticolo_cases.npz`` -- RETICOLO's per-order efficiencies of twelve 1D gratings (the
+  reference's ``tests/references/golden_reticolo.npz``) with their inputs;
 * ``legacy_cases.npz`` -- the efficiencies that the reference's own frozen legacy golden file
   (``tests/fixtures/legacy_rcwa/golden_legacy.npz``) holds for its 1D, conical and 2D sampled-Li
   cases, with the inputs those cases are defined by (``tests/fixtures/legacy_rcwa/gen_goldens.py``).
@@ -283,6 +285,50 @@ def make_legacy_cases():
     print('legacy_cases.npz:', len(cases), 'cases')
 
 
+def make_reticolo_cases():
+    """RETICOLO's per-order efficiencies of twelve 1D binary gratings (the reference's
+    tests/references/golden_reticolo.npz, read by test_reticolo_golden.py), with their inputs as
+    that test spells them (restated top layer first, permittivities; TE/TM are the s/p columns at
+    phi = 0, the conical cases take psi). RETICOLO reports the propagating orders only: ``idx_*``
+    are their positions in the order vector -h..h."""
+    gold = np.load(os.path.join(REF, 'tests/references/golden_reticolo.npz'))
+    half = [[[9.0] * 5 + [1.0] * 5]]
+    quarter = [[[12.25] * 3 + [1.0] * 9]]
+    # the test hands the factory `_TWO_LAYER[::-1]` with thickness [0.22, 0.15], layers listed from
+    # the bottom up: top first, that is the eps-9 layer (0.15) over the eps-4.84 layer (0.22)
+    two = [[[9.0] * 6 + [1.0] * 6], [[4.840000000000001] * 8 + [1.0] * 4]]
+    base = dict(theta=0.0, phi=0.0, top=1.0, bot=2.25, h=10, period=0.7, wavelength=0.9, structure=half,
+                thickness=[0.15])
+    cases = {
+        'te_normal': dict(base, pol='s'),
+        'te_oblique': dict(base, pol='s', theta=0.2),
+        'tm_normal': dict(base, pol='p'),
+        'tm_oblique': dict(base, pol='p', theta=0.2),
+        'te_quarter': dict(base, pol='s', theta=0.15, h=12, period=0.8, wavelength=0.7, structure=quarter,
+                           thickness=[0.25]),
+        'tm_quarter': dict(base, pol='p', theta=0.15, h=12, period=0.8, wavelength=0.7, structure=quarter,
+                           thickness=[0.25]),
+        'te_two_layer': dict(base, pol='s', theta=0.25, bot=4.0, wavelength=0.85, structure=two,
+                             thickness=[0.15, 0.22]),
+        'tm_two_layer': dict(base, pol='p', theta=0.25, bot=4.0, wavelength=0.85, structure=two,
+                             thickness=[0.15, 0.22]),
+        'te_high_order': dict(base, pol='s', theta=0.2, h=30),
+        'tm_high_order': dict(base, pol='p', theta=0.2, h=30),
+        'conical_te': dict(base, pol='s', theta=0.2, phi=0.3),
+        'conical_tm': dict(base, pol='p', theta=0.2, phi=0.3),
+    }
+    out = {}
+    for name, kw in cases.items():
+        for key, val in kw.items():
+            out[f'{name}__{key}'] = np.asarray(val)
+        for side in ('ri', 'ti'):
+            out[f'{name}__idx_{side}'] = np.asarray(gold[f'{name}__idx_{side}'])
+            out[f'{name}__de_{side}'] = np.asarray(gold[f'{name}__de_{side}'])
+    out['names'] = np.array(list(cases))
+    np.savez_compressed(os.path.join(HERE, 'reticolo_cases.npz'), **out)
+    print('reticolo_cases.npz:', len(cases), 'cases')
+
+
 if __name__ == '__main__':
     sys.path.insert(0, os.path.join(REF, 'src'))
     make_ref_cases()
@@ -291,3 +337,4 @@ if __name__ == '__main__':
     make_field_cases()
     make_etm_cases()
     make_legacy_cases()
+    make_reticolo_cases()

@@ -231,3 +231,26 @@ def test_etm_matches_the_reference_etm_and_the_smm(name):
         for key in ('R', 'T'):
             assert np.abs(etm[key][col] - c[f'{key}_{pol}']).max() <= 1e-12 * scale, (name, pol, key)
             assert np.abs(etm[key][col] - smm[key][col]).max() <= 1e-12 * scale, (name, pol, key)
+
+
+RETICOLO_NAMES = list(np.load(os.path.join(GOLDEN, 'reticolo_cases.npz'))['names'])
+
+
+def _reticolo_solve(c):
+    h, per = int(c['h']), float(c['period'])
+    o = O.solve_stack(np.asarray(c['structure'], complex), c['thickness'], float(c['wavelength']), (per, per), h, 0,
+                      float(c['theta']), float(c['phi']), complex(c['top']), complex(c['bot']), str(c['pol']))
+    return o['R'][0].ravel(), o['T'][0].ravel()
+
+
+@pytest.mark.parametrize('name', RETICOLO_NAMES)
+def test_oracle_matches_reticolo_orders(name):
+    """Per-order efficiencies of twelve 1D gratings (TE/TM, oblique, quarter duty cycle, two
+    layers, orders 30, conical) against RETICOLO (tests/references/test_reticolo_golden.py:115-135
+    of the reference, atol 1e-11); every order RETICOLO did not report carries no power."""
+    c = _case(np.load(os.path.join(GOLDEN, 'reticolo_cases.npz')), name)
+    R, T = _reticolo_solve(c)
+    for side, arr in (('ri', R), ('ti', T)):
+        idx = c[f'idx_{side}']
+        assert np.abs(arr[idx] - c[f'de_{side}']).max() < 1e-11, (name, side)
+        assert np.abs(np.delete(arr, idx)).max(initial=0.0) < 1e-14, (name, side)
