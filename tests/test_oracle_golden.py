@@ -254,3 +254,53 @@ def test_oracle_matches_reticolo_orders(name):
         idx = c[f'idx_{side}']
         assert np.abs(arr[idx] - c[f'de_{side}']).max() < 1e-11, (name, side)
         assert np.abs(np.delete(arr, idx)).max(initial=0.0) < 1e-14, (name, side)
+
+
+def _airy(eps1, eps2, eps3, kx, k0d, pol):
+    """Specular R, T of a uniform slab by the thin-film (Airy) formulas, exp(-i w t):
+    kz = sqrt(eps - kx^2) with Im kz >= 0; the p channel uses the admittance kz/eps."""
+    kz = [np.sqrt(complex(e) - kx ** 2) for e in (eps1, eps2, eps3)]
+    kz = [k if k.imag > 0 or (k.imag == 0 and k.real >= 0) else -k for k in kz]
+    y = kz if pol == 's' else [k / e for k, e in zip(kz, (eps1, eps2, eps3))]
+    r12, r23 = (y[0] - y[1]) / (y[0] + y[1]), (y[1] - y[2]) / (y[1] + y[2])
+    t12, t23 = 2 * y[0] / (y[0] + y[1]), 2 * y[1] / (y[1] + y[2])
+    ph = np.exp(1j * kz[1] * k0d)
+    den = 1 + r12 * r23 * ph ** 2
+    r, t = (r12 + r23 * ph ** 2) / den, t12 * t23 * ph / den
+    if pol == 'p':       # t above transmits the H field; power goes with the admittance kz/eps
+        return abs(r) ** 2, (y[2].real / y[0].real) * abs(t) ** 2
+    return abs(r) ** 2, (kz[2].real / kz[0].real) * abs(t) ** 2
+
+
+@pytest.mark.parametrize('eps2', [6.25, 2.1 + 0.4j, -8.0 + 1.2j])
+@pytest.mark.parametrize('pol', ['s', 'p'])
+def test_uniform_slab_is_the_airy_formula(eps2, pol):
+    """A uniform layer at oblique incidence through the full 2D path (orders (2, 2)): the specular
+    efficiencies are the thin-film formulas and every other order is empty
+    (test_lossy_media.py, test_uniform_interfaces.py of the reference)."""
+    eps1, eps3, theta, wl, d = 1.44, 2.25, 0.4, 633.0, 170.0
+    st = np.full((1, 4, 4), eps2, dtype=complex)
+    out = O.solve_stack(st, np.array([d]), wl, (400.0, 450.0), 2, 2, theta, 0.0, eps1, eps3, pol)
+    kx = np.sqrt(eps1) * np.sin(theta)
+    R, T = _airy(eps1, eps2, eps3, kx, 2 * np.pi / wl * d, pol)
+    spec = (2, 2)
+    assert abs(out['R'][0][spec] - R) < 1e-12 and abs(out['T'][0][spec] - T) < 1e-12
+    for M in (out['R'][0], out['T'][0]):
+        rest = M.copy()
+        rest[spec] = 0.0
+        assert np.abs(rest).max() < 1e-14
+
+
+@pytest.mark.parametrize('pol', ['s', 'p'])
+def test_a_y_invariant_grating_solves_alike_at_any_hv(pol):
+    """1D == 2D on a y-invariant stack at phi = 0 (test_equivalence.py:79-102 of the reference):
+    the ky = 0 row at orders (h, 2) is the (h, 0) solution, and the other rows are empty."""
+    rng = np.random.default_rng(12)
+    row = np.where(rng.random(16) < 0.45, 12.25 + 0.1j, 1.0)
+    st = np.stack([np.tile(row, (6, 1)), np.tile(row[::-1], (6, 1))]).astype(complex)
+    th = np.array([140.0, 90.0])
+    a = O.solve_stack(st, th, 700.0, (800.0, 500.0), 6, 0, 0.3, 0.0, 1.0, 2.25, pol)
+    b = O.solve_stack(st, th, 700.0, (800.0, 500.0), 6, 2, 0.3, 0.0, 1.0, 2.25, pol)
+    for key in ('R', 'T'):
+        assert np.abs(b[key][0][2] - a[key][0][0]).max() < 1e-12
+        assert np.abs(np.delete(b[key][0], 2, axis=0)).max() < 1e-14
