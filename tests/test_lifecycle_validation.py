@@ -186,3 +186,26 @@ def test_a_failed_solve_is_a_numerical_error_with_the_reference_code(monkeypatch
     with pytest.raises(rcwa.NumericalError) as e:
         p._solve(r, None, np.zeros((3, 1), int))
     assert e.value.code == 'rcwa.singular'
+
+
+def test_check_reports_the_resolved_numerics_and_outputs_without_a_gpu():
+    """rcwa.check resolves and estimates on the host (_lifecycle.py:380-420 of the reference):
+    the coefficient rule, the connecting algorithm, what the outputs keep and what it costs."""
+    p = _problem()
+    p = rcwa.Problem(stack=p.stack, excitation=p.excitation, units=p.units,
+                     outputs=rcwa.Outputs(fields=True, scattering=False))
+    rep = rcwa.check(p, numerics=rcwa.Numerics(orders=(3, 2), fourier_coefficients='integrated',
+                                               algorithm='etm'))
+    res = rep.resolved
+    assert res['fourier_coefficients'] == 'integrated' and res['algorithm'] == 'etm'
+    assert res['retained_fields'] is True and res['retained_scattering'] is False
+    assert res['length_units'] == 'nm' and res['layer_count'] == 2
+    N = 7 * 5
+    assert rep.estimates['retained_spatial_modes'] == N
+    assert rep.estimates['retained_field_bytes'] == 16 * 1 * 2 * (2 * (2 * N) ** 2 + 4 * N)
+    assert rep.estimates['retained_scattering_bytes'] == 0
+    assert rep.estimates['device_workspace_bytes'] > 0
+    with pytest.raises(rcwa.UnsupportedFeatureError) as e:
+        rcwa.check(rcwa.Problem(stack=p.stack, excitation=p.excitation, outputs=rcwa.Outputs(scattering=True)),
+                   numerics=rcwa.Numerics(orders=(1, 1), algorithm='etm'))
+    assert e.value.code == 'rcwa.scattering_algorithm'

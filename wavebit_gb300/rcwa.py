@@ -371,9 +371,13 @@ def check(problem, *, numerics=None, backend='gb300', device='cuda', precision='
     L = len(r['rasters'])
     chunk = max(1, min(len(r['wavelengths']), 128))
     ws = int(_lib.load().wb_workspace_bytes(hu, hv, L, chunk, _lib.PRECISION.get(precision, 0)))
+    n_wl = len(r['wavelengths'])
     est = {'retained_spatial_modes': N,
            'one_dense_material_matrix_bytes': 16 * N * N,
            'one_first_order_matrix_bytes': 16 * (2 * N) ** 2,
+           # what Outputs keeps resident on the device after the run
+           'retained_field_bytes': 16 * n_wl * L * (2 * (2 * N) ** 2 + 4 * N) if _wants_fields(problem) else 0,
+           'retained_scattering_bytes': 16 * n_wl * 4 * (2 * N) ** 2 if _wants_scattering(problem) else 0,
            'device_workspace_bytes': ws,
            'device_chunk': chunk}
     if torch.cuda.is_available():
@@ -384,7 +388,9 @@ def check(problem, *, numerics=None, backend='gb300', device='cuda', precision='
                 'layer_count': L, 'fourier_coefficients': 'integrated' if _integrated(numerics) else 'sampled',
                 'factorization': 'li',
                 'algorithm': _algorithm(numerics), 'solve_path': '2d', 'backend': backend, 'device': device,
-                'precision': precision}
+                'precision': precision, 'retained_fields': _wants_fields(problem),
+                'retained_scattering': _wants_scattering(problem),
+                'length_units': getattr(getattr(problem, 'units', None), 'length', None)}
     return CheckReport(issues=(), estimates=est, resolved=resolved)
 
 
