@@ -57,6 +57,13 @@ def test_polarization_pairs_are_normalised():
     (dict(source=rcwa.PlaneWave(kx=0.1)), rcwa.UnsupportedFeatureError, 'feature.unsupported',
      'excitation.sources[0]'),
     (dict(source=rcwa.PlaneWave(theta=2.0)), rcwa.ValidationError, 'input.invalid', 'excitation.sources[0].theta'),
+    (dict(source=rcwa.PlaneWave(phi=float('nan'))), rcwa.ValidationError, 'input.invalid', 'excitation.sources[0].phi'),
+    (dict(source=rcwa.PlaneWave(polarization='x')), rcwa.ValidationError, 'input.invalid',
+     'excitation.sources[0].polarization'),
+    (dict(source=rcwa.PlaneWave(polarization=(0.0, 0.0))), rcwa.ValidationError, 'input.invalid',
+     'excitation.sources[0].polarization'),
+    (dict(wavelength=float('inf')), rcwa.ValidationError, 'input.invalid', 'excitation.wavelength'),
+    (dict(wavelength=()), rcwa.ValidationError, 'input.invalid', 'excitation.wavelength'),
 ])
 def test_refusals_carry_the_reference_classes_and_codes(kw, error, code, path):
     with pytest.raises(error) as e:

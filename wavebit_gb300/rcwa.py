@@ -1,13 +1,15 @@
 """The ``rcwa.check -> prepare -> run`` lifecycle of the reference, as a GB300 backend.
 
 Mirrors ``wavebit.rcwa`` (rcwa/_lifecycle.py:422 ``check``, :737 ``prepare``, :698
-``Prepared.run``, :801 ``run``) for raster stacks under the default numerics (SMM, sampled
-Li coefficients, fixed nesting). It accepts the reference's own declaration objects
-(``wavebit.rcwa.Problem`` and friends) unchanged, by their attributes, or the small mirror
-dataclasses defined here when the reference is not installed. Results come back as torch
+``Prepared.run``, :801 ``run``) for raster stacks under Li's fixed nesting, with sampled or
+integrated coefficients, the SMM or (as a cross-check) the ETM connecting algorithm, and the
+optional outputs ``scattering`` and ``fields``. It accepts the reference's own declaration
+objects (``wavebit.rcwa.Problem`` and friends) unchanged, by their attributes, or the small
+mirror dataclasses defined here when the reference is not installed. Results come back as torch
 tensors on the device with the reference's ``(wavelength, order_v, order_u)`` axes.
 
-Everything numerical runs in libwbgpu.so; there is no CPU path.
+Stages A, B and C run in libwbgpu.so; the field amplitudes and the ETM recursion run as torch
+linear algebra on the same device, over the library's modes. There is no CPU path.
 """
 from dataclasses import dataclass, field
 import math
@@ -316,8 +318,8 @@ def _resolve(problem, numerics):
                                       path='stack.top')
     exc = problem.excitation
     wl = np.atleast_1d(np.asarray(exc.wavelength, dtype=np.float64)).reshape(-1)
-    if not np.all(wl > 0):
-        raise ValidationError('wavelengths must be positive', path='excitation.wavelength')
+    if not (wl.size and np.all(np.isfinite(wl)) and np.all(wl > 0)):
+        raise ValidationError('wavelengths must be finite and positive', path='excitation.wavelength')
     sources = tuple(exc.sources)
     if len(sources) != 1:
         raise UnsupportedFeatureError('one PlaneWave source per problem on the GB300 path',
@@ -329,14 +331,20 @@ def _resolve(problem, numerics):
     phi = float(np.real(0.0 if src.phi is None else src.phi))
     if not abs(theta) < math.pi / 2:
         raise ValidationError('theta must be a real angle below pi/2', path='excitation.sources[0].theta')
+    if not math.isfinite(phi):
+        raise ValidationError('phi must be a finite angle', path='excitation.sources[0].phi')
     pol = src.polarization
     if isinstance(pol, str):
         if pol not in ('s', 'p'):
-            raise ValidationError("polarization must be 's', 'p' or an (s, p) pair")
+            raise ValidationError("polarization must be 's', 'p' or an (s, p) pair",
+                                  path='excitation.sources[0].polarization')
         a_s, a_p = (complex(1.0, 0.0), complex(math.cos(math.pi / 2))) if pol == 's' else (0j, 1 + 0j)
     else:
         a_s, a_p = (complex(v) for v in pol)
         nrm = math.sqrt(abs(a_s) ** 2 + abs(a_p) ** 2)
+        if not (nrm > 0 and math.isfinite(nrm)):
+            raise ValidationError('an (s, p) polarization pair must be finite and not both zero',
+                                  path='excitation.sources[0].polarization')
         a_s, a_p = a_s / nrm, a_p / nrm
     if _wants_scattering(problem) and _algorithm(numerics) == 'etm':
         raise UnsupportedFeatureError('Scattering matrices require algorithm="smm".',
