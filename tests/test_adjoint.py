@@ -105,3 +105,48 @@ def test_chunked_stage_b_gives_the_same_gradient_cpu():
     assert abs(full[0] - one[0]) <= 1e-12 * abs(full[0])
     for a, b in zip(full[1:], one[1:]):
         assert float((a - b).abs().max()) <= 1e-12 * max(1.0, float(a.abs().max()))
+
+
+@pytest.mark.parametrize('case', ['oblique_crossed', 'normal_degenerate'])
+def test_wavelength_gradient_matches_finite_differences_cpu(case):
+    """d loss / d wavelength by the forward tangent (wavelength_tangent) against a central
+    difference, including normal incidence on a symmetric cell, whose eigenvalues are exactly
+    degenerate (the broadened gaps) and whose specular order sits on the kx = 0 branch."""
+    if case == 'oblique_crossed':
+        eps, th = _case(4)
+        kw = dict(KW, wavelengths=[620.0, 710.0])
+        wR, wT = _weights(9, B=2, seed=2)
+    else:
+        eps = np.ones((1, 8, 8), complex)
+        eps[0, 2:6, 2:6] = 9.0
+        th = np.array([150.0])
+        kw = dict(KW, wavelengths=[655.0], theta=0.0, phi=0.0, pol=(1.0, 0.0), period=(700.0, 700.0), hu=2, hv=2)
+        wR, wT = _weights(25, B=1, seed=3)
+    out = AD.solve_and_grad(eps, th, impl='torch', device='cpu', weights_R=wR, weights_T=wT, grad_wavelength=True,
+                            **kw)
+    assert len(out) == 6
+    for b, lam in enumerate(kw['wavelengths']):
+        h = 1e-3
+
+        def f(x):
+            wl = list(kw['wavelengths'])
+            wl[b] = x
+            return AD.solve_and_grad(eps, th, impl='torch', device='cpu', weights_R=wR, weights_T=wT, grad=False,
+                                     **dict(kw, wavelengths=wl))[0]
+        fd = (f(lam + h) - f(lam - h)) / (2 * h)
+        assert abs(float(out[5][b]) - fd) <= 1e-6 * abs(fd), (case, b)
+
+
+def test_autograd_function_carries_the_wavelength_gradient_cpu():
+    eps, th = _case(6, L=1)
+    wR, wT = _weights(9, B=2, seed=5)
+    e = torch.tensor(eps.real, requires_grad=True)
+    t = torch.tensor(th, requires_grad=True)
+    wl = torch.tensor(KW['wavelengths'], dtype=torch.float64, requires_grad=True)
+    spec = dict(KW, impl='torch', wavelengths=wl)
+    loss = AD.efficiency_loss(e, t, wR, wT, **spec)
+    loss.backward()
+    ref = AD.solve_and_grad(eps, th, impl='torch', device='cpu', weights_R=wR, weights_T=wT, grad_wavelength=True,
+                            **KW)
+    assert torch.allclose(wl.grad, ref[5], rtol=0, atol=1e-14)
+    assert torch.allclose(e.grad, ref[3], rtol=0, atol=1e-14)

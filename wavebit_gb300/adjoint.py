@@ -385,6 +385,100 @@ def efficiencies(cref, ctrn, wr, wt, N):
     return a[:N] + a[N:], b[:N] + b[N:]
 
 
+# ------------------------------------------------------------ d loss / d wavelength
+
+_PV_KEYS = ('kx', 'ky', 'c', 's', 'kzt', 'kzb', 'wg', 'vg', 'r11', 'r12', 'r21', 'r22', 't11', 't21')
+
+
+def _rotate(W, V, c, s, N):
+    """The s/p rotation of a layer's Cartesian modes (sp_rotate_kernel)."""
+    W1, W2, V1, V2 = W[:N], W[N:], V[:N], V[N:]
+    bw = torch.cat([c[:, None] * W2 - s[:, None] * W1, c[:, None] * W1 + s[:, None] * W2], 0)
+    bv = torch.cat([c[:, None] * V1 + s[:, None] * V2, c[:, None] * V2 - s[:, None] * V1], 0)
+    return bw, bv
+
+
+def eig_tangent(w, W, dA):
+    """Tangents of the eigenvalues and (scale-free) eigenvectors of A along dA: with
+    E = W^-1 dA W, dw = diag(E) and dW = W C, C_ij = E_ij / (w_j - w_i) off the diagonal, the
+    reciprocal gap broadened as in :func:`eig_adjoint` (whose F is this one's conjugate)."""
+    n = w.shape[0]
+    E = torch.linalg.solve(W, dA @ W)
+    d = w[None, :] - w[:, None]
+    scale = w.abs().max().clamp_min(1e-300)
+    eps = (n * 2.220446049250313e-16 * scale) ** 2
+    G = d.conj() / (d.abs() ** 2 + eps)
+    G.fill_diagonal_(0)
+    return torch.diagonal(E).clone(), W @ (G * E)
+
+
+def wavelength_tangent(*args):
+    """:func:`_wavelength_tangent`, quiet about torch's own deprecation notices from inside
+    ``torch.func``."""
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore', DeprecationWarning)
+        return _wavelength_tangent(*args)
+
+
+def _wavelength_tangent(lam, period, theta, phi, eps_top, eps_bot, hu, hv, conv, thickness, per_layer, pol,
+                        wR, wT, device):
+    """``d loss / d wavelength`` of one solve by a forward tangent: the wavelength moves k0
+    (``d k0 = -k0 / lam``) and every order's in-plane wavevector (``d kx = u / Lx``,
+    ``d ky = v / Ly``), hence the ports, each layer's operator, its eigenpairs (:func:`eig_tangent`),
+    ``q``, ``V``, the s/p rotation and ``X = exp(-k0 d q)``, and through the cascade the
+    efficiencies. The pure-torch pieces are differentiated exactly by ``torch.func.jvp``."""
+    from torch.func import jvp
+    N = (2 * hu + 1) * (2 * hv + 1)
+    n = 2 * N
+    lam_t = torch.tensor(float(lam), dtype=torch.float64, device=device)
+    one = torch.ones((), dtype=torch.float64, device=device)
+
+    def port_vectors(l):
+        pv = ports(l, period, theta, phi, eps_top, eps_bot, hu, hv, device)
+        return tuple(pv[k] for k in _PV_KEYS)
+
+    pv_vals, pv_tans = jvp(port_vectors, (lam_t,), (one,))
+    pv0 = ports(float(lam), period, theta, phi, eps_top, eps_bot, hu, hv, device)
+    k0 = 2 * PI / float(lam)
+    dk0 = -k0 / float(lam)
+    kx, ky = pv_vals[0], pv_vals[1]
+    dkx, dky = pv_tans[0], pv_tans[1]
+    c, s, dc, ds = pv_vals[2], pv_vals[3], pv_tans[2], pv_tans[3]
+    bWs, bVs, Xs, dbWs, dbVs, dXs = [], [], [], [], [], []
+    for l, p in enumerate(per_layer):
+        epx, epy, epz = conv[l]
+        (om2, omr, _), (dom2, domr, _) = jvp(lambda a, b: layer_operator_torch(a, b, epx, epy, epz), (kx, ky),
+                                             (dkx, dky))
+        w, W, q = p['w'], p['W'], p['q']
+        dw, dW = eig_tangent(w, W, dom2)
+        dq = dw / (2.0 * q)
+        V = (omr @ W) / q[None, :]
+        dV = (domr @ W + omr @ dW) / q[None, :] - (omr @ W) * (dq / q ** 2)[None, :]
+        (bw, bv), (dbw, dbv) = jvp(lambda W_, V_, c_, s_: _rotate(W_, V_, c_, s_, N), (W, V, c, s), (dW, dV, dc, ds))
+        d = float(thickness[l])
+        X = torch.exp(-k0 * d * q)
+        dX = X * (-d) * (dk0 * q + k0 * dq)
+        bWs.append(bw); bVs.append(bv); Xs.append(X)
+        dbWs.append(dbw); dbVs.append(dbv); dXs.append(dX)
+    C = _incidence(pv0, pol, N, device)
+    wR_t = torch.as_tensor(wR, dtype=torch.float64, device=device)
+    wT_t = torch.as_tensor(wT, dtype=torch.float64, device=device)
+
+    def loss_of(bWl, bVl, Xl, pvt):
+        pv = dict(pv0)
+        pv.update(zip(_PV_KEYS, pvt))
+        cref, ctrn, _ = cascade_forward(list(bWl), list(bVl), list(Xl), pv, C)
+        wr, wt = _efficiency_weights(pv, pol, N)
+        a = (cref[:, 0] * cref[:, 0].conj()).real * wr
+        b = (ctrn[:, 0] * ctrn[:, 0].conj()).real * wt
+        return (wR_t * (a[:N] + a[N:])).sum() + (wT_t * (b[:N] + b[N:])).sum()
+
+    _, dloss = jvp(loss_of, (tuple(bWs), tuple(bVs), tuple(Xs), tuple(pv_vals)),
+                   (tuple(dbWs), tuple(dbVs), tuple(dXs), tuple(pv_tans)))
+    return float(dloss)
+
+
 def _stage_b_batch(impl, conv, pvs, L, hu, hv, cs=None):
     """Eigenpairs of every (wavelength, layer) pair: one wb_layer_modes launch on the CUDA
     kernels (gb300) or torch.linalg.eig (torch reference). Returns w (P, n), W (P, n, n)."""
@@ -422,7 +516,7 @@ def _chunk_size(L, n, budget, device):
 
 def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weights_T, theta=0.0, phi=0.0,
                    eps_top=1.0, eps_bot=1.0, pol=(0.0, 1.0), impl='gb300', device=None, grad=True,
-                   hbm_budget=None):
+                   hbm_budget=None, grad_wavelength=False):
     """Loss = sum_b sum_i (weights_R[b, i] R[b, i] + weights_T[b, i] T[b, i]) over the given
     polarization's per-order efficiencies, and its gradients with respect to the raster
     permittivities (real part; shape of ``eps``) and the thicknesses.
@@ -433,6 +527,9 @@ def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weigh
     The eigenpairs are computed for a chunk of wavelengths at a time, sized by ``hbm_budget``
     (bytes), and dropped after the chunk's forward and reverse passes: however many wavelengths,
     no more than one chunk's modes are resident.
+
+    With ``grad_wavelength`` a sixth value is returned: ``d loss / d wavelength`` (B,), each
+    wavelength's own term by a forward tangent (:func:`wavelength_tangent`).
     """
     device = device or ('cuda' if impl == 'gb300' else 'cpu')
     eps = torch.as_tensor(eps, dtype=torch.complex128, device=device)
@@ -455,6 +552,7 @@ def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weigh
     g_th = torch.zeros(L, dtype=torch.float64, device=device)
     loss = 0.0
     Rs, Ts = [], []
+    g_wl = []
     for b, lam in enumerate(wls):
         if b % chunk == 0:
             w_all = W_all = None
@@ -482,6 +580,9 @@ def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weigh
         wT = torch.as_tensor(weights_T[b], dtype=torch.float64, device=device)
         loss += float((wR * Rb).sum() + (wT * Tb).sum())
         Rs.append(Rb); Ts.append(Tb)
+        if grad_wavelength:
+            g_wl.append(wavelength_tangent(lam, period, theta, phi, eps_top, eps_bot, hu, hv, conv, thickness,
+                                           per_layer, pol, weights_R[b], weights_T[b], device))
         if not grad:
             continue
         # reverse: efficiencies -> amplitudes (d|a|^2 = 2 Re(conj(a) da))
@@ -512,38 +613,50 @@ def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weigh
             gom2 = eig_adjoint(n, p['w'], p['W'], gw, gW)
             gx, gy, gz = layer_operator_adjoint(gom2, gomr, p['so'])
             g_conv[l][0] += gx; g_conv[l][1] += gy; g_conv[l][2] += gz
+    extra = (torch.tensor(g_wl, dtype=torch.float64, device=device),) if grad_wavelength else ()
     if not grad:
-        return loss, torch.stack(Rs), torch.stack(Ts), None, None
+        return (loss, torch.stack(Rs), torch.stack(Ts), None, None) + extra
     g_eps = torch.stack([li_conv_adjoint(g_conv[l], hu, hv, saved_a[l][1]) for l in range(L)])
-    return loss, torch.stack(Rs), torch.stack(Ts), g_eps.real, g_th
+    return (loss, torch.stack(Rs), torch.stack(Ts), g_eps.real, g_th) + extra
 
 
 class EfficiencyLoss(torch.autograd.Function):
     """``loss = sum(weights_R * R + weights_T * T)`` of a raster stack as a differentiable
-    function of the (real) raster permittivities and the layer thicknesses.
+    function of the (real) raster permittivities, the layer thicknesses and the wavelengths.
 
     The forward runs stages A and B on the CUDA kernels and evaluates the hand-written reverse
-    pass at once (one solve per wavelength; nothing but the two gradients is kept for
-    ``backward``, so no per-layer eigenpairs stay resident between the passes).
+    pass at once (one solve per wavelength; nothing but the gradients is kept for ``backward``,
+    so no per-layer eigenpairs stay resident between the passes). The wavelength gradient (a
+    forward tangent per wavelength) is computed only when ``wavelengths`` requires it.
     """
 
     @staticmethod
-    def forward(ctx, eps, thickness, weights_R, weights_T, spec):
-        loss, R, T, g_eps, g_th = solve_and_grad(
-            eps.detach().to(torch.complex128), thickness.detach().cpu().numpy(), spec['wavelengths'],
+    def forward(ctx, eps, thickness, wavelengths, weights_R, weights_T, spec):
+        want_wl = bool(ctx.needs_input_grad[2])
+        out = solve_and_grad(
+            eps.detach().to(torch.complex128), thickness.detach().cpu().numpy(),
+            [float(v) for v in wavelengths.detach().cpu().reshape(-1)],
             spec['period'], spec['hu'], spec['hv'], weights_R.detach().cpu().numpy(),
             weights_T.detach().cpu().numpy(), theta=spec.get('theta', 0.0), phi=spec.get('phi', 0.0),
             eps_top=spec.get('eps_top', 1.0), eps_bot=spec.get('eps_bot', 1.0), pol=spec.get('pol', (0.0, 1.0)),
-            impl=spec.get('impl', 'gb300'), device=eps.device)
-        ctx.save_for_backward(g_eps.to(eps.dtype), g_th.to(thickness.dtype).to(thickness.device))
+            impl=spec.get('impl', 'gb300'), device=eps.device, grad_wavelength=want_wl)
+        loss, g_eps, g_th = out[0], out[3], out[4]
+        g_wl = out[5].to(wavelengths.dtype).to(wavelengths.device).reshape(wavelengths.shape) if want_wl \
+            else torch.zeros_like(wavelengths)
+        ctx.save_for_backward(g_eps.to(eps.dtype), g_th.to(thickness.dtype).to(thickness.device), g_wl)
+        ctx.want_wl = want_wl
         return torch.as_tensor(loss, dtype=torch.float64, device=eps.device)
 
     @staticmethod
     def backward(ctx, grad):
-        g_eps, g_th = ctx.saved_tensors
-        return grad * g_eps, grad * g_th, None, None, None
+        g_eps, g_th, g_wl = ctx.saved_tensors
+        return grad * g_eps, grad * g_th, (grad * g_wl if ctx.want_wl else None), None, None, None
 
 
 def efficiency_loss(eps, thickness, weights_R, weights_T, **spec):
-    """Functional form of :class:`EfficiencyLoss`."""
-    return EfficiencyLoss.apply(eps, thickness, torch.as_tensor(weights_R), torch.as_tensor(weights_T), spec)
+    """Functional form of :class:`EfficiencyLoss`; ``spec['wavelengths']`` may be a tensor that
+    requires grad."""
+    spec = dict(spec)
+    wl = spec.pop('wavelengths')
+    wl = wl if torch.is_tensor(wl) else torch.as_tensor(np.atleast_1d(wl), dtype=torch.float64)
+    return EfficiencyLoss.apply(eps, thickness, wl, torch.as_tensor(weights_R), torch.as_tensor(weights_T), spec)
