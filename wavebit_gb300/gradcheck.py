@@ -3,7 +3,10 @@ continuous raster, orders (9, 9), 32 wavelengths over 1000-1600 nm, p incidence,
 sum_lambda T(0,0)): times one forward+reverse pass and compares the pixel and thickness
 gradients with central finite differences (step 1e-6 on 16 seeded pixels) of the same forward.
 
-    python -m wavebit_gb300.gradcheck [--wavelengths 32] [--pixels 16] [--orders 9]
+    python -m wavebit_gb300.gradcheck [--wavelengths 32] [--pixels 16] [--orders 9] [--wavelength]
+
+``--wavelength`` also checks d loss / d wavelength of the first wavelength (its forward tangent)
+against a central difference of 1e-3 nm.
 """
 import argparse
 import json
@@ -22,6 +25,7 @@ def main():
     ap.add_argument('--pixels', type=int, default=16)
     ap.add_argument('--orders', type=int, default=9)
     ap.add_argument('--side', type=int, default=128)
+    ap.add_argument('--wavelength', action='store_true', help='check d loss / d wavelength too')
     args = ap.parse_args()
     cfg = WL.adjoint_layer(side=args.side, n_wavelengths=args.wavelengths)
     h = args.orders
@@ -64,6 +68,20 @@ def main():
            'max_rel_err_pixels': worst, 'thickness_grad': float(g_th[0]), 'thickness_fd': fd_t,
            'thickness_rel_err': abs(fd_t - float(g_th[0])) / max(abs(fd_t), 1e-300),
            'samples': [dict(y=r[0], x=r[1], fd=r[2], adjoint=r[3]) for r in rows[:4]]}
+    if args.wavelength:
+        t0 = time.perf_counter()
+        g_wl = AD.solve_and_grad(eps, th, weights_R=wR, weights_T=wT, grad=False, grad_wavelength=True, **kw)[5]
+        torch.cuda.synchronize()
+        h_wl = 1e-3
+        wl0 = list(cfg['wavelengths'])
+
+        def at(lam):
+            return AD.solve_and_grad(eps, th, weights_R=wR, weights_T=wT, grad=False,
+                                     **dict(kw, wavelengths=[lam] + wl0[1:]))[0]
+        fd_wl = (at(wl0[0] + h_wl) - at(wl0[0] - h_wl)) / (2 * h_wl)
+        out.update(wavelength_grad=float(g_wl[0]), wavelength_fd=fd_wl,
+                   wavelength_rel_err=abs(fd_wl - float(g_wl[0])) / max(abs(fd_wl), 1e-300),
+                   wavelength_grad_seconds=time.perf_counter() - t0)
     print(json.dumps(out))
 
 
