@@ -150,3 +150,22 @@ def test_autograd_function_carries_the_wavelength_gradient_cpu():
                             **KW)
     assert torch.allclose(wl.grad, ref[5], rtol=0, atol=1e-14)
     assert torch.allclose(e.grad, ref[3], rtol=0, atol=1e-14)
+
+
+def test_integrated_coefficients_take_the_same_pass_cpu():
+    """Over one segment per pixel the integrated series is the sampled one, so a differentiated
+    raster with fourier_coefficients='integrated' has the oracle's integrated solve as its loss."""
+    from oracle import rcwa_oracle as O
+    eps, th = _case(7, L=1)
+    wR, wT = _weights(9)
+    a = _loss(eps, th, 'torch', weights_R=wR, weights_T=wT, fourier_coefficients='integrated', **KW)
+    b = _loss(eps, th, 'torch', weights_R=wR, weights_T=wT, **KW)
+    assert a[0] == b[0] and torch.equal(a[3], b[3])
+    conv = O.to_conv_mat_raster_integrated(eps, 1, 1)
+    ref = 0.0
+    for bi, lam in enumerate(KW['wavelengths']):
+        o = O.solve_stack(eps, th, lam, KW['period'], 1, 1, KW['theta'], KW['phi'], 1.0, 2.25, KW['pol'], conv=conv)
+        ref += float((wR[bi] * o['R'][0].reshape(-1)).sum() + (wT[bi] * o['T'][0].reshape(-1)).sum())
+    assert abs(a[0] - ref) < 1e-12
+    with pytest.raises(ValueError):
+        _loss(eps, th, 'torch', weights_R=wR, weights_T=wT, fourier_coefficients='laurent', **KW)

@@ -516,7 +516,7 @@ def _chunk_size(L, n, budget, device):
 
 def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weights_T, theta=0.0, phi=0.0,
                    eps_top=1.0, eps_bot=1.0, pol=(0.0, 1.0), impl='gb300', device=None, grad=True,
-                   hbm_budget=None, grad_wavelength=False):
+                   hbm_budget=None, grad_wavelength=False, fourier_coefficients=None):
     """Loss = sum_b sum_i (weights_R[b, i] R[b, i] + weights_T[b, i] T[b, i]) over the given
     polarization's per-order efficiencies, and its gradients with respect to the raster
     permittivities (real part; shape of ``eps``) and the thicknesses.
@@ -530,7 +530,14 @@ def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weigh
 
     With ``grad_wavelength`` a sixth value is returned: ``d loss / d wavelength`` (B,), each
     wavelength's own term by a forward tangent (:func:`wavelength_tangent`).
+
+    ``fourier_coefficients`` may be ``'sampled'`` or ``'integrated'``: a differentiated raster
+    keeps every pixel edge (factorization.py:3135-3150 of the reference), and over one segment
+    per pixel the closed-form segment series is the exact staircase series the sampled rule
+    computes, so both take the same pass.
     """
+    if fourier_coefficients not in (None, 'sampled', 'integrated'):
+        raise ValueError("fourier_coefficients must be 'sampled' or 'integrated'")
     device = device or ('cuda' if impl == 'gb300' else 'cpu')
     eps = torch.as_tensor(eps, dtype=torch.complex128, device=device)
     L = eps.shape[0]
@@ -639,7 +646,8 @@ class EfficiencyLoss(torch.autograd.Function):
             spec['period'], spec['hu'], spec['hv'], weights_R.detach().cpu().numpy(),
             weights_T.detach().cpu().numpy(), theta=spec.get('theta', 0.0), phi=spec.get('phi', 0.0),
             eps_top=spec.get('eps_top', 1.0), eps_bot=spec.get('eps_bot', 1.0), pol=spec.get('pol', (0.0, 1.0)),
-            impl=spec.get('impl', 'gb300'), device=eps.device, grad_wavelength=want_wl)
+            impl=spec.get('impl', 'gb300'), device=eps.device, grad_wavelength=want_wl,
+            fourier_coefficients=spec.get('fourier_coefficients'))
         loss, g_eps, g_th = out[0], out[3], out[4]
         g_wl = out[5].to(wavelengths.dtype).to(wavelengths.device).reshape(wavelengths.shape) if want_wl \
             else torch.zeros_like(wavelengths)
