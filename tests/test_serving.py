@@ -86,6 +86,24 @@ def test_a_poisoned_request_fails_alone():
     assert all(res[r.id].error is None for r in mates)
 
 
+class RaisingBackend(FakeBackend):
+    """Raises from launch whenever a listed request is in the batch (an input the library refuses)."""
+
+    def launch(self, worker, reqs):
+        if any(r.id in self.poisoned for r in reqs):
+            raise RuntimeError('wb_solve_batch: refused')
+        return super().launch(worker, reqs)
+
+
+def test_a_batch_whose_launch_raises_is_taken_apart():
+    clock = FakeClock()
+    be = RaisingBackend(clock, limit=8, poisoned={7})
+    res, st = Server(be, n_workers=2, max_batch=8, clock=clock, idle_sleep=0).run(_reqs(24))
+    assert res[7].error is not None and res[7].status == -2 and 'refused' in res[7].error
+    assert st['errors'] == 1 and st['completed'] == 23
+    assert all(res[i].error is None and res[i].R[0] == i for i in range(24) if i != 7)
+
+
 class FallbackBackend(FakeBackend):
     """Fails the listed requests' first attempt (status 2); their retry, run in the fallback
     precision, succeeds."""

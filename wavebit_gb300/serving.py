@@ -18,7 +18,8 @@ and the workers' batches overlap on the device.
   then stage C alone (``wb_smm_solve``).
 * A request whose solve reports a non-zero status (singular, non-convergent, non-finite) gets an
   error result; the other requests of its batch keep theirs. In the mixed form it is first solved
-  once more with the double-float eigen-solve.
+  once more with the double-float eigen-solve. A batch whose launch raises is taken apart and its
+  requests launched one at a time, so the one at fault gets the error result (status -2) alone.
 
 The solver is a small interface (``GpuBackend`` here; the CPU tests pass a fake one), so the
 scheduling logic is tested without a GPU. ``python -m wavebit_gb300.serving`` replays a seeded
@@ -319,9 +320,22 @@ class Server:
                         del waiting[b]
                     for r in take:
                         r.start = now()
-                    inflight[w] = (self.backend.launch(w, take), take)
-                    busy_batches += 1
                     progressed = True
+                    try:
+                        token = self.backend.launch(w, take)
+                    except Exception as e:
+                        # a batch the backend refuses: its requests go again one per batch, so
+                        # that the one at fault fails alone and the others are served
+                        if len(take) > 1:
+                            for r in take:
+                                waiting.setdefault(r.bucket + ('alone', r.id), collections.deque()).append(r)
+                        else:
+                            r = take[0]
+                            results[r.id] = Result(r.id, None, None, -2, f'launch failed: {e}',
+                                                   now() - (r.arrival if realtime else 0.0))
+                        continue
+                    inflight[w] = (token, take)
+                    busy_batches += 1
             if not progressed:
                 if realtime and nxt < len(reqs) and not waiting and all(f is None for f in inflight):
                     gap = reqs[nxt].arrival - now()
