@@ -216,3 +216,20 @@ def test_check_reports_the_resolved_numerics_and_outputs_without_a_gpu():
         rcwa.check(rcwa.Problem(stack=p.stack, excitation=p.excitation, outputs=rcwa.Outputs(scattering=True)),
                    numerics=rcwa.Numerics(orders=(1, 1), algorithm='etm'))
     assert e.value.code == 'rcwa.scattering_algorithm'
+
+
+def test_solve_batch_refuses_layer_indices_outside_the_convolution_stack():
+    """The kernels index the convolution stack with layer_index: a batch that would read past it
+    is refused on the host, before any device work (engine.solve_batch)."""
+    import torch
+    conv = rcwa.engine.ConvStack(torch.zeros((2, 3, 9, 9), dtype=torch.complex128), 1, 1)
+    for bad in ([[0, 2]], [[-1, 0]]):
+        inp = rcwa.engine.BatchInputs(bad, [[10.0, 10.0]], [600.0], [[500.0, 500.0]], [0.0], [0.0], [1.0], [1.0],
+                                      [[1.0, 0.0]], device='cpu')
+        with pytest.raises(ValueError, match='layer_index'):
+            rcwa.engine.solve_batch(conv, inp)
+    ok = rcwa.engine.BatchInputs([[0, 1]], [[10.0, 10.0]], [600.0], [[500.0, 500.0]], [0.0], [0.0], [1.0], [1.0],
+                                 [[1.0, 0.0]], device='cpu')
+    assert ok.index_range == (0, 1)
+    with pytest.raises(ValueError, match='pair_layer'):
+        rcwa.engine.layer_modes(conv, [0, 2], np.zeros((2, 9)), np.zeros((2, 9)))

@@ -102,6 +102,11 @@ def layer_modes(conv, pair_layer, kx, ky, precision='double', handle=None):
     hu, hv = conv.hu, conv.hv
     N = n_orders(hu, hv)
     n = 2 * N
+    if not (torch.is_tensor(pair_layer) and pair_layer.is_cuda):
+        pl = np.asarray(pair_layer.cpu() if torch.is_tensor(pair_layer) else pair_layer)
+        if pl.size and (int(pl.min()) < 0 or int(pl.max()) >= conv.n_layers):
+            raise ValueError(f'pair_layer spans {int(pl.min())}..{int(pl.max())}; the convolution stack holds '
+                             f'{conv.n_layers} layers')
     pair_layer = torch.as_tensor(pair_layer, dtype=torch.int32, device=dev).contiguous()
     P = pair_layer.shape[0]
     kx = _f64(kx, dev).reshape(P, N)
@@ -124,6 +129,13 @@ class BatchInputs:
 
     def __init__(self, layer_index, thickness, wavelength, period, theta, phi, eps_top, eps_bot, pol,
                  device='cuda'):
+        # the range of the indices, read on the host while they are host data: the kernels index
+        # the convolution stack with them, so solve_batch refuses a batch that would read past it
+        if torch.is_tensor(layer_index) and layer_index.is_cuda:
+            self.index_range = None
+        else:
+            li = np.asarray(layer_index.cpu() if torch.is_tensor(layer_index) else layer_index)
+            self.index_range = (int(li.min()), int(li.max())) if li.size else None
         self.layer_index = torch.as_tensor(layer_index, dtype=torch.int32, device=device).contiguous()
         B, L = self.layer_index.shape
         self.B, self.L = B, L
@@ -144,6 +156,9 @@ def solve_batch(conv, inp, precision='double', amplitudes=False, handle=None, ou
     hu, hv = conv.hu, conv.hv
     N = n_orders(hu, hv)
     B, L = inp.B, inp.L
+    rng = getattr(inp, 'index_range', None)
+    if rng is not None and (rng[0] < 0 or rng[1] >= conv.n_layers):
+        raise ValueError(f'layer_index spans {rng[0]}..{rng[1]}; the convolution stack holds {conv.n_layers} layers')
     if out is None:
         R = torch.empty((B, 3, N), dtype=torch.float64, device=dev)
         T = torch.empty_like(R)
