@@ -97,8 +97,9 @@ int wb_assemble_li_integrated(wb_handle* h, const wb_complex* eps, int L, int ny
                               wb_complex* epz_i, int32_t* status, void* stream);
 
 /* Stage B: eigenmodes of n_pairs layers. conv: device (n_conv, 3, N, N) slots epx, epy, epz_i;
- * pair_layer: device (n_pairs) index into conv; kx, ky: device (n_pairs, N) normalised order
- * wavevectors. Outputs (device): w (n_pairs, 2N) eigenvalues of Omega^2, q (n_pairs, 2N),
+ * pair_layer: device (n_pairs) index into conv, each in [0, n_conv) (device data: the library
+ * cannot read it before the kernels do, so the caller keeps it in range); kx, ky: device
+ * (n_pairs, N) normalised order wavevectors. Outputs (device): w (n_pairs, 2N) eigenvalues of Omega^2, q (n_pairs, 2N),
  * W and V (n_pairs, 2N, 2N) column-major, status (n_pairs). precision: WB_PRECISION_FP64 for
  * the FP64 eigen-solve, any other WB_PRECISION_* for the double-float one.
  * Reference: rcwa/_engine/solve_2d.py:2303-2460 (layer_modes_2d, no exceptional-point
@@ -110,7 +111,8 @@ int wb_layer_modes(wb_handle* h, int n_pairs, int hu, int hv, const wb_complex* 
 
 /* One batch of whole solves (stages B and C). Every array is a device pointer.
  *   conv        (n_conv, 3, N, N) from wb_assemble_li, any layers of any stacks
- *   layer_index (B, L) into conv, entry face first;  thickness (B, L), in wavelength units
+ *   layer_index (B, L) into conv, entry face first, each in [0, n_conv) (not checked on the
+ *               device: the caller keeps it in range);  thickness (B, L), in wavelength units
  *   wavelength (B); period (B, 2); theta, phi (B) radians (real; lossless superstrate)
  *   eps_top, eps_bot (B); pol (B, 2) = (a_s, a_p), unit norm
  * Outputs: R, T (B, 3, N) per-order efficiencies for [given polarization, pure s, pure p];
