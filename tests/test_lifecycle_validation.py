@@ -233,3 +233,9 @@ def test_solve_batch_refuses_layer_indices_outside_the_convolution_stack():
     assert ok.index_range == (0, 1)
     with pytest.raises(ValueError, match='pair_layer'):
         rcwa.engine.layer_modes(conv, [0, 2], np.zeros((2, 9)), np.zeros((2, 9)))
+    # given modes must cover every (solve, layer) pair the kernels read
+    W = torch.zeros((1, 18, 18), dtype=torch.complex128)
+    q = torch.zeros((1, 18), dtype=torch.complex128)
+    for fn in (rcwa.engine.smm_solve, rcwa.engine.scattering_matrix):
+        with pytest.raises(ValueError, match='modes must be'):
+            fn(W, W, q, ok, 1, 1)

@@ -178,10 +178,20 @@ def solve_batch(conv, inp, precision='double', amplitudes=False, handle=None, ou
     return res + ((amps,) if amplitudes else ())
 
 
+def _check_modes(W, V, q, inp, hu, hv):
+    """The kernels read B*L pairs of (2N, 2N) modes and (2N,) roots: refuse anything smaller."""
+    n = 2 * n_orders(hu, hv)
+    P = inp.B * inp.L
+    if tuple(W.shape) != (P, n, n) or tuple(V.shape) != (P, n, n) or tuple(q.shape) != (P, n):
+        raise ValueError(f'modes must be W, V ({P}, {n}, {n}) and q ({P}, {n}) for {inp.B} solves of {inp.L} '
+                         f'layers at orders ({hu}, {hv}); got {tuple(W.shape)}, {tuple(V.shape)}, {tuple(q.shape)}')
+
+
 def smm_solve(W, V, q, inp, hu, hv, precision='double', amplitudes=False, handle=None):
     """Stage C from given modes (wb_smm_solve). ``W, V`` (B*L, n, n) and ``q`` (B*L, n) in the
     natural orientation :func:`layer_modes` returns, pair ``p = b*L + l``; ``inp`` the batch's
     per-solve parameters (its ``layer_index`` is not used). Returns ``(R, T, status[, amps])``."""
+    _check_modes(W, V, q, inp, hu, hv)
     dev = W.device
     N = n_orders(hu, hv)
     B, L = inp.B, inp.L
@@ -208,6 +218,7 @@ def scattering_matrix(W, V, q, inp, hu, hv, handle=None):
     (wb_scattering_matrix). ``W, V, q`` and ``inp`` as for :func:`smm_solve`. Returns
     ``(S11, S12, S21, S22, status)``: each block ``(B, 2N, 2N)`` in natural orientation, s
     amplitudes then p port variables, about the cell centre."""
+    _check_modes(W, V, q, inp, hu, hv)
     dev = W.device
     n = 2 * n_orders(hu, hv)
     B, L = inp.B, inp.L
