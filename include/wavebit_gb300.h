@@ -55,7 +55,8 @@ typedef struct { double re, im; } wb_complex;
 typedef struct wb_handle wb_handle;
 
 /* Version of this ABI (major * 100 + minor): 2.0 = the precision codes above (WB_PRECISION_MIXED
- * is the FP32 eigen-solve with Newton steps), wb_smm_solve and wb_workspace_bytes. */
+ * is the FP32 eigen-solve with Newton steps), wb_smm_solve and wb_workspace_bytes; 2.1 adds
+ * wb_assemble_li_integrated and wb_scattering_matrix. */
 int wb_version(void);
 
 /* Message of the calling thread's last failure, NUL-terminated, truncated to len. */

@@ -34,7 +34,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_abi_version(lib):
-    assert lib.wb_version() == 200
+    assert lib.wb_version() == 201
 
 
 def test_binding_table_covers_the_header():

@@ -72,7 +72,7 @@ int noalloc_fail(const char* msg) { g_err = msg; return WB_E_INVALID; }
 
 extern "C" {
 
-int wb_version(void) { return 200; }
+int wb_version(void) { return 201; }
 
 int wb_last_error(char* buf, size_t len) {
   if (!buf || len == 0) return WB_E_INVALID;
