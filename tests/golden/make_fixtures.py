@@ -18,6 +18,8 @@ It writes
   five of those scenes at explicit points, s and p incidence;
 * ``ref_etm.npz`` -- per-order R/T of the reference's ETM connecting algorithm on the scenes of
   ``ref_cases.npz``;
+* ``ref_halfspace.npz`` -- per-order R/T of the reference's own run on scenes with a lossy or
+  metallic substrate, total internal reflection and a denser superstrate;
 * ``reticolo_cases.npz`` -- RETICOLO's per-order efficiencies of twelve 1D gratings (the
   reference's ``tests/references/golden_reticolo.npz``) with their inputs;
 * ``legacy_cases.npz`` -- the efficiencies that the reference's own frozen legacy golden file
@@ -285,6 +287,42 @@ def make_legacy_cases():
     print('legacy_cases.npz:', len(cases), 'cases')
 
 
+def halfspace_cases():
+    """Scenes whose half-spaces take the other branches of the boundary kz: a lossy and a metallic
+    substrate, total internal reflection under a denser superstrate (theta beyond the critical
+    angle into eps 1), and a denser superstrate at an ordinary angle."""
+    rng = np.random.default_rng(20261204)
+    base = dict(thickness=[180., 90.], wavelength=720., period=(900., 800.), orders=(3, 2))
+
+    def stack():
+        return np.stack([_rast(rng, 12, 14, values=(12.25, 2.25, 4.0 + 0.3j)), np.full((12, 14), 2.1 + 0j)])
+    return [
+        dict(base, name='lossy_substrate', structure=stack(), theta=0.3, phi=0.4, eps_top=1.0, eps_bot=2.1 + 0.3j),
+        dict(base, name='metal_substrate', structure=stack(), theta=0.2, phi=1.2, eps_top=1.0, eps_bot=-20.0 + 1.5j),
+        dict(base, name='tir', structure=stack(), theta=0.8, phi=0.5, eps_top=2.25, eps_bot=1.0),
+        dict(base, name='dense_superstrate', structure=stack(), theta=0.35, phi=2.2, eps_top=2.25, eps_bot=1.44),
+    ]
+
+
+def make_halfspace_cases():
+    """Per-order R/T of the reference's own run on :func:`halfspace_cases`, s and p."""
+    out = {}
+    names = []
+    for case in halfspace_cases():
+        n = case['name']
+        names.append(n)
+        for key in ('structure', 'thickness', 'wavelength', 'period', 'orders', 'theta', 'phi',
+                    'eps_top', 'eps_bot'):
+            out[f'{n}__{key}'] = np.asarray(case[key])
+        for pol in ('s', 'p'):
+            R, T, _ = run_ref(case, pol)
+            out[f'{n}__R_{pol}'] = R
+            out[f'{n}__T_{pol}'] = T
+    out['names'] = np.array(names)
+    np.savez_compressed(os.path.join(HERE, 'ref_halfspace.npz'), **out)
+    print('ref_halfspace.npz:', len(names), 'cases')
+
+
 def make_reticolo_cases():
     """RETICOLO's per-order efficiencies of twelve 1D binary gratings (the reference's
     tests/references/golden_reticolo.npz, read by test_reticolo_golden.py), with their inputs as
@@ -336,5 +374,6 @@ if __name__ == '__main__':
     make_scattering_cases()
     make_field_cases()
     make_etm_cases()
+    make_halfspace_cases()
     make_legacy_cases()
     make_reticolo_cases()

@@ -304,3 +304,21 @@ def test_a_y_invariant_grating_solves_alike_at_any_hv(pol):
     for key in ('R', 'T'):
         assert np.abs(b[key][0][2] - a[key][0][0]).max() < 1e-12
         assert np.abs(np.delete(b[key][0], 2, axis=0)).max() < 1e-14
+
+
+HALFSPACE_NAMES = list(np.load(os.path.join(GOLDEN, 'ref_halfspace.npz'))['names'])
+
+
+@pytest.mark.parametrize('name', HALFSPACE_NAMES)
+def test_oracle_matches_reference_half_space_branches(name):
+    """A lossy and a metallic substrate, total internal reflection under a denser superstrate and
+    a denser superstrate at an ordinary angle: per-order R/T against the reference's own run
+    (the boundary kz on Maystre's cut, conventions.py:655-760), s and p, 1e-12."""
+    c = _case(np.load(os.path.join(GOLDEN, 'ref_halfspace.npz')), name)
+    hu, hv = (int(v) for v in c['orders'])
+    o = O.solve_stack(c['structure'], c['thickness'], float(c['wavelength']), tuple(c['period']), hu, hv,
+                      float(c['theta']), float(c['phi']), complex(c['eps_top']), complex(c['eps_bot']), 's')
+    for col, pol in ((1, 's'), (2, 'p')):
+        scale = max(np.abs(c[f'R_{pol}']).max(), np.abs(c[f'T_{pol}']).max())
+        assert np.abs(o['R'][col] - c[f'R_{pol}']).max() <= 1e-12 * scale, (name, pol)
+        assert np.abs(o['T'][col] - c[f'T_{pol}']).max() <= 1e-12 * scale, (name, pol)
