@@ -19,7 +19,8 @@ It writes
 * ``ref_etm.npz`` -- per-order R/T of the reference's ETM connecting algorithm on the scenes of
   ``ref_cases.npz``;
 * ``ref_halfspace.npz`` -- per-order R/T of the reference's own run on scenes with a lossy or
-  metallic substrate, total internal reflection and a denser superstrate;
+  metallic substrate, total internal reflection, a denser superstrate, and normal incidence at
+  an azimuth with cos(phi) < 0;
 * ``reticolo_cases.npz`` -- RETICOLO's per-order efficiencies of twelve 1D gratings (the
   reference's ``tests/references/golden_reticolo.npz``) with their inputs;
 * ``legacy_cases.npz`` -- the efficiencies that the reference's own frozen legacy golden file
@@ -288,9 +289,10 @@ def make_legacy_cases():
 
 
 def halfspace_cases():
-    """Scenes whose half-spaces take the other branches of the boundary kz: a lossy and a metallic
-    substrate, total internal reflection under a denser superstrate (theta beyond the critical
-    angle into eps 1), and a denser superstrate at an ordinary angle."""
+    """Scenes on the other branches of the boundary kz -- a lossy and a metallic substrate, total
+    internal reflection under a denser superstrate (theta beyond the critical angle into eps 1), a
+    denser superstrate at an ordinary angle -- and of the order azimuth: normal incidence with
+    cos(phi) < 0, where the specular order's s/p frame is atan(sin phi / cos phi) + pi."""
     rng = np.random.default_rng(20261204)
     base = dict(thickness=[180., 90.], wavelength=720., period=(900., 800.), orders=(3, 2))
 
@@ -301,6 +303,7 @@ def halfspace_cases():
         dict(base, name='metal_substrate', structure=stack(), theta=0.2, phi=1.2, eps_top=1.0, eps_bot=-20.0 + 1.5j),
         dict(base, name='tir', structure=stack(), theta=0.8, phi=0.5, eps_top=2.25, eps_bot=1.0),
         dict(base, name='dense_superstrate', structure=stack(), theta=0.35, phi=2.2, eps_top=2.25, eps_bot=1.44),
+        dict(base, name='normal_rotated', structure=stack(), theta=0.0, phi=2.5, eps_top=1.0, eps_bot=2.25),
     ]
 
 
