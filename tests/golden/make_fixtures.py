@@ -21,6 +21,7 @@ It writes
 * ``ref_halfspace.npz`` -- per-order R/T of the reference's own run on scenes with a lossy or
   metallic substrate, total internal reflection, a denser superstrate, and normal incidence at
   an azimuth with cos(phi) < 0;
+* ``ref_bare.npz`` -- per-order R/T of the reference's own run on stacks with no layers;
 * ``reticolo_cases.npz`` -- RETICOLO's per-order efficiencies of twelve 1D gratings (the
   reference's ``tests/references/golden_reticolo.npz``) with their inputs;
 * ``legacy_cases.npz`` -- the efficiencies that the reference's own frozen legacy golden file
@@ -326,6 +327,27 @@ def make_halfspace_cases():
     print('ref_halfspace.npz:', len(names), 'cases')
 
 
+def make_bare_cases():
+    """Stacks with no layers: the reference solves the bare interface between its half-spaces
+    (results.py:180-189) -- per-order R/T of its own run, s and p."""
+    out = {}
+    scenes = [dict(name='bare_oblique', eps_top=1.0, eps_bot=2.25, theta=0.4, phi=0.3),
+              dict(name='bare_lossy', eps_top=2.25, eps_bot=-8.0 + 1.2j, theta=0.25, phi=1.1)]
+    for sc in scenes:
+        case = dict(sc, structure=np.zeros((0, 1, 1), complex), thickness=[], wavelength=633.0,
+                    period=(500.0, 600.0), orders=(2, 1))
+        n = sc['name']
+        for key in ('wavelength', 'period', 'orders', 'theta', 'phi', 'eps_top', 'eps_bot'):
+            out[f'{n}__{key}'] = np.asarray(case[key])
+        for pol in ('s', 'p'):
+            R, T, _ = run_ref(case, pol)
+            out[f'{n}__R_{pol}'] = R
+            out[f'{n}__T_{pol}'] = T
+    out['names'] = np.array([sc['name'] for sc in scenes])
+    np.savez_compressed(os.path.join(HERE, 'ref_bare.npz'), **out)
+    print('ref_bare.npz:', len(scenes), 'cases')
+
+
 def make_reticolo_cases():
     """RETICOLO's per-order efficiencies of twelve 1D binary gratings (the reference's
     tests/references/golden_reticolo.npz, read by test_reticolo_golden.py), with their inputs as
@@ -378,5 +400,6 @@ if __name__ == '__main__':
     make_field_cases()
     make_etm_cases()
     make_halfspace_cases()
+    make_bare_cases()
     make_legacy_cases()
     make_reticolo_cases()

@@ -39,7 +39,6 @@ def test_polarization_pairs_are_normalised():
 
 @pytest.mark.parametrize('kw,error,code,path', [
     (dict(lattice=((1, 0), (0.5, 1))), rcwa.UnsupportedFeatureError, 'feature.unsupported', 'stack.lattice'),
-    (dict(layers=()), rcwa.ValidationError, 'input.invalid', 'stack.layers'),
     (dict(layers=(rcwa.Layer(thickness=50.0, epsilon=2.0, regions=('disc',)),)), rcwa.UnsupportedFeatureError,
      'feature.unsupported', 'stack.layers[0]'),
     (dict(layers=(rcwa.Layer(thickness=50.0, epsilon=2.0, mu=2.0),)), rcwa.UnsupportedFeatureError,
@@ -239,3 +238,16 @@ def test_solve_batch_refuses_layer_indices_outside_the_convolution_stack():
     for fn in (rcwa.engine.smm_solve, rcwa.engine.scattering_matrix):
         with pytest.raises(ValueError, match='modes must be'):
             fn(W, W, q, ok, 1, 1)
+
+
+def test_a_stack_with_no_layers_is_the_bare_interface():
+    """The reference solves a stack with no layers through one zero-thickness layer of the top
+    medium (results.py:180-189); the mirror resolves it the same way."""
+    r = rcwa._resolve(_problem(layers=()), rcwa.Numerics(orders=(1, 1)))
+    assert r['bare_interface'] and r['thickness'].tolist() == [0.0]
+    assert r['rasters'][0].shape == (1, 1) and r['rasters'][0][0, 0] == r['eps_top']
+    res = rcwa.Result(None, None, (None, None), (None, None), None, (600.0,), {}, None, None, (object(),),
+                      (r['thickness'], r['period'], 1.0, True))
+    with pytest.raises(rcwa.ValidationError) as e:
+        res.field(x=[0.0], y=[0.0], z=[0.0])
+    assert e.value.code == 'field.coordinates'

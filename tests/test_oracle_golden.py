@@ -322,3 +322,21 @@ def test_oracle_matches_reference_half_space_branches(name):
         scale = max(np.abs(c[f'R_{pol}']).max(), np.abs(c[f'T_{pol}']).max())
         assert np.abs(o['R'][col] - c[f'R_{pol}']).max() <= 1e-12 * scale, (name, pol)
         assert np.abs(o['T'][col] - c[f'T_{pol}']).max() <= 1e-12 * scale, (name, pol)
+
+
+BARE_NAMES = list(np.load(os.path.join(GOLDEN, 'ref_bare.npz'))['names'])
+
+
+@pytest.mark.parametrize('name', BARE_NAMES)
+def test_bare_interface_is_a_zero_thickness_layer_of_the_top_medium(name):
+    """A stack with no layers against the reference's own run: the oracle through one
+    zero-thickness layer of the superstrate, as the lifecycle resolves it (results.py:180-189)."""
+    c = _case(np.load(os.path.join(GOLDEN, 'ref_bare.npz')), name)
+    hu, hv = (int(v) for v in c['orders'])
+    et = complex(c['eps_top'])
+    o = O.solve_stack(np.full((1, 1, 1), et), np.array([0.0]), float(c['wavelength']), tuple(c['period']), hu, hv,
+                      float(c['theta']), float(c['phi']), et, complex(c['eps_bot']), 's')
+    for col, pol in ((1, 's'), (2, 'p')):
+        scale = max(np.abs(c[f'R_{pol}']).max(), np.abs(c[f'T_{pol}']).max())
+        assert np.abs(o['R'][col] - c[f'R_{pol}']).max() <= 1e-12 * scale, (name, pol)
+        assert np.abs(o['T'][col] - c[f'T_{pol}']).max() <= 1e-12 * scale, (name, pol)

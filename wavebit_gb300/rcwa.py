@@ -284,8 +284,6 @@ def _resolve(problem, numerics):
     if len(period) == 1:
         period = (period[0], period[0])
     layers = tuple(stack.layers)
-    if not layers:
-        raise ValidationError('the stack has no layers', path='stack.layers')
     rasters, thick = [], []
     for i, layer in enumerate(layers):
         if getattr(layer, 'regions', ()):
@@ -313,6 +311,11 @@ def _resolve(problem, numerics):
     rasters, thick = rasters[::-1], thick[::-1]
     eps_top = _scalar_eps(stack.top, 'stack.top')
     eps_bot = _scalar_eps(stack.bottom, 'stack.bottom')
+    bare = not layers
+    if bare:
+        # the bare interface between the half-spaces, solved as the reference solves it: through
+        # one zero-thickness layer of the top medium (results.py:180-189)
+        rasters, thick = [np.full((1, 1), eps_top, dtype=np.complex128)], [0.0]
     if eps_top.imag != 0 or eps_top.real <= 0:
         raise UnsupportedFeatureError('the lit superstrate must be lossless with Re(eps) > 0',
                                       path='stack.top')
@@ -355,7 +358,7 @@ def _resolve(problem, numerics):
     orders = _numerics_orders(_numerics_or_default(numerics))
     return dict(rasters=rasters, thickness=np.array(thick), period=period, eps_top=eps_top,
                 eps_bot=eps_bot, wavelengths=wl, theta=theta, phi=phi, pol=(a_s, a_p), orders=orders,
-                amplitude=amplitude)
+                amplitude=amplitude, bare_interface=bare)
 
 
 def _numerics_or_default(numerics):
@@ -434,7 +437,11 @@ class Result:
         if reconstruction != 'plain':
             raise ValidationError(f"reconstruction must be 'plain', 'lalanne', 'split' or 'splitw', not "
                                   f'{reconstruction!r}.', code='field.reconstruction', path='reconstruction')
-        thickness, period, amplitude = self._field_geometry
+        thickness, period, amplitude = self._field_geometry[:3]
+        if len(self._field_geometry) > 3 and self._field_geometry[3]:
+            raise ValidationError('This stack has no layers, so field() has nothing to sample: it reconstructs '
+                                  'inside finite layers only, and here z = 0 is the interface between the two '
+                                  'half-spaces. Add a layer to sample inside it.', code='field.coordinates', path='z')
         try:
             xs = F.axis_points(x, period[0], 'x')
             ys = F.axis_points(y, period[1], 'y')
@@ -539,7 +546,8 @@ class Prepared:
         states = self._field_states(r, conv, np.asarray(layer_index), wl, th) if fields else None
         return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]), status, tuple(r['wavelengths']),
                       diag, out[3] if amplitudes else None, S, states,
-                      (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0)))
+                      (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0),
+                       r.get('bare_interface', False)))
 
     def _solve_etm(self, r, conv, layer_index, fields=False):
         """``Numerics(algorithm='etm')``: the ETM recursion over the FP64 modes of every
@@ -566,7 +574,8 @@ class Prepared:
         states = self._field_states(r, conv, layer_index, wl, th) if fields else None
         return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]),
                       torch.as_tensor(st, device=R.device), tuple(r['wavelengths']), diag, None, None, states,
-                      (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0)))
+                      (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0),
+                       r.get('bare_interface', False)))
 
     def _mode_chunks(self, r, conv, layer_index, wl, th, per_wl_bytes, budget=2 << 30):
         """FP64 modes of every (wavelength, layer) pair (wb_layer_modes), a chunk of wavelengths
