@@ -72,6 +72,10 @@ int wb_destroy(wb_handle* h);
  * later call on the handle allocates. Serving loops call it once per worker at start-up. */
 int wb_reserve(wb_handle* h, size_t bytes);
 
+/* Order windows: every entry point takes orders (hu, hv) with 0 <= hv <= 42 and
+ * N = (2hu+1)(2hv+1) <= 3228 (the largest windows the kernels hold on chip) and refuses others
+ * with WB_E_INVALID; wb_workspace_bytes returns 0 for them. */
+
 /* Bit-exact harmonic tables: labels_u[2hu+1] = -hu..hu, labels_v likewise; toeplitz_u
  * [(2hu+1)^2] = r - c + 2hu row-major, toeplitz_v likewise. Host memory, no handle needed.
  * Reference: rcwa/_engine/engine.py:953-993 (_separable_kxy order labels),

@@ -60,6 +60,16 @@ def test_invalid_orders_are_refused_with_a_message(lib):
     assert 'orders' in _lib.last_error()
 
 
+def test_order_windows_end_where_the_kernels_on_chip_buffers_do(lib):
+    from wavebit_gb300 import _lib
+    for hu, hv in ((0, 43), (28, 28), (1614, 0)):
+        assert lib.wb_build_indices(hu, hv, None, None, None, None) == _lib.WB_E_INVALID, (hu, hv)
+        assert 'hv <= 42' in _lib.last_error()
+        assert lib.wb_workspace_bytes(hu, hv, 1, 1, 0) == 0
+    for hu, hv in ((27, 27), (1613, 0), (18, 42)):
+        assert lib.wb_workspace_bytes(hu, hv, 1, 1, 0) > 0, (hu, hv)
+
+
 def test_create_without_a_gpu_fails_cleanly(lib):
     import torch
     if torch.cuda.is_available():

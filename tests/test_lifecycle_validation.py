@@ -73,6 +73,8 @@ def test_refusals_carry_the_reference_classes_and_codes(kw, error, code, path):
 @pytest.mark.parametrize('numerics,path', [
     (rcwa.Numerics(orders=(-1, 2)), 'numerics.orders'),
     (rcwa.Numerics(orders=(2,)), 'numerics.orders'),
+    (rcwa.Numerics(orders=(28, 28)), 'numerics.orders'),
+    (rcwa.Numerics(orders=(0, 43)), 'numerics.orders'),
 ])
 def test_bad_orders_are_refused(numerics, path):
     with pytest.raises(rcwa.ValidationError) as e:

@@ -63,7 +63,7 @@ int reserve(wb_handle* h, size_t bytes) {
   return WB_OK;
 }
 
-bool valid_orders(int hu, int hv) { return hu >= 0 && hv >= 0 && hu <= 64 && hv <= 64; }
+bool valid_orders(int hu, int hv) { return wb::orders_fit(hu, hv); }
 }  // namespace
 
 namespace wb {
@@ -114,7 +114,8 @@ int wb_reserve(wb_handle* h, size_t bytes) {
 
 int wb_build_indices(int hu, int hv, int32_t* labels_u, int32_t* labels_v, int32_t* toeplitz_u,
                      int32_t* toeplitz_v) {
-  if (!valid_orders(hu, hv)) return fail(WB_E_INVALID, "orders (%d, %d) out of range", hu, hv);
+  if (!valid_orders(hu, hv))
+    return fail(WB_E_INVALID, "orders (%d, %d) out of range: 0 <= hv <= 42 and (2hu+1)(2hv+1) <= 3228", hu, hv);
   const int nu = 2 * hu + 1, nv = 2 * hv + 1;
   if (labels_u) for (int i = 0; i < nu; ++i) labels_u[i] = i - hu;
   if (labels_v) for (int i = 0; i < nv; ++i) labels_v[i] = i - hv;

@@ -197,6 +197,9 @@ void assemble_li(cudaStream_t s, const cplx* eps, int L, int ny, int nx, int hu,
   // 2. inner Toeplitz inverses, groups (rec, layer): 2L groups of nx lines
   {
     size_t sm = sizeof(cplx) * nv * 2 * nv;
+    // past the default 48 KB a block has to opt in (hv <= 42 keeps the tile within 227 KB)
+    if (sm > 48 * 1024)
+      cudaFuncSetAttribute(toeplitz_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     toeplitz_inverse_kernel<<<2 * L * nx, 128, sm, s>>>(cv, nx, hv, inner, status); note_launch();
   }
   // 3. series along u of every inner-inverse entry: 2L * nv^2 lines of nx points;

@@ -59,6 +59,15 @@ void trevc(cudaStream_t s, int batch, int n, const Cx<R>* T, int ldt, long long 
 template <class R>
 void normalize_columns(cudaStream_t s, int batch, int n, Cx<R>* W, int ldw, long long w_bs);
 
+// ---- order windows
+// The largest windows the kernels hold on chip: stage A inverts an (2hv+1)^2 Toeplitz matrix
+// beside its identity in one block's shared memory (32 (2hv+1)^2 bytes <= 227 KB: hv <= 42), and
+// the eigen-solve keeps vectors of n = 2N complex values in shared memory (36 n bytes for the
+// mixed form's group step: N <= 3228).
+inline bool orders_fit(int hu, int hv) {
+  return hu >= 0 && hv >= 0 && hv <= 42 && hu <= 1613 && (2LL * hu + 1) * (2LL * hv + 1) <= 3228;
+}
+
 // ---- stage A: convolution matrices (wb_assemble.cu)
 // eps: (L, ny, nx) row-major raster; outputs (L, N, N) column-major; scratch from `ws`.
 // x_edges (L, nx) and y_edges (L, ny), both NULL for sampled coefficients: the right edges of

@@ -73,7 +73,7 @@ extern "C" int wb_assemble_li_noalloc(const wb_complex* eps, int L, int ny, int 
                                       void* stream) {
   char msg[256];
   if (!eps || !epx || !epy || !epz_i) return wb::noalloc_fail("wb_assemble_li_noalloc: NULL argument"), WB_E_INVALID;
-  if (L <= 0 || ny <= 0 || nx <= 0 || hu < 0 || hv < 0 || hu > 64 || hv > 64) {
+  if (L <= 0 || ny <= 0 || nx <= 0 || !wb::orders_fit(hu, hv)) {
     snprintf(msg, sizeof(msg), "wb_assemble_li_noalloc: bad sizes L=%d ny=%d nx=%d orders=(%d,%d)", L, ny, nx, hu, hv);
     wb::noalloc_fail(msg);
     return WB_E_INVALID;

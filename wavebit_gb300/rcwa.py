@@ -235,6 +235,9 @@ def _numerics_orders(numerics):
     orders = tuple(int(v) for v in getattr(numerics, 'orders', (0, 0)))
     if len(orders) != 2 or min(orders) < 0:
         raise ValidationError('orders must be a pair of nonnegative integers', path='numerics.orders')
+    if _lib.load().wb_workspace_bytes(orders[0], orders[1], 1, 1, 0) == 0:
+        raise ValidationError(f'orders {orders} exceed the windows the GB300 kernels hold on chip: '
+                              '0 <= hv <= 42 and (2hu+1)(2hv+1) <= 3228', path='numerics.orders')
     for name, allowed in (('algorithm', (None, 'smm', 'etm')), ('fourier_coefficients', (None, 'sampled', 'integrated')),
                           ('factorization', (None, 'li')), ('li_nesting', (None, 'fixed'))):
         val = getattr(numerics, name, None)
