@@ -253,3 +253,28 @@ def test_a_stack_with_no_layers_is_the_bare_interface():
     with pytest.raises(rcwa.ValidationError) as e:
         res.field(x=[0.0], y=[0.0], z=[0.0])
     assert e.value.code == 'field.coordinates'
+
+
+def test_a_prepared_run_refuses_a_changed_layout_and_takes_new_values():
+    """Prepared.run(problem) keeps the reference's reuse contract (_adapt.py:633-640): values are
+    live, the declaration layout is not (code prepared.structure)."""
+    base = _problem()
+    p = rcwa.Prepared.__new__(rcwa.Prepared)
+    p.problem, p.numerics = base, rcwa.Numerics(orders=(1, 1))
+    p.resolved = rcwa._resolve(base, p.numerics)
+    # new values in the same layout: accepted
+    moved = _problem(wavelength=700.0, layers=(rcwa.Layer(thickness=150.0, epsilon=np.array([[1.0, 9.0], [9.0, 1.0]])),
+                                               rcwa.Layer(thickness=60.0, epsilon=3.1)))
+    p._check_layout(moved, rcwa._resolve(moved, p.numerics))
+    for changed, path in ((_problem(layers=(rcwa.Layer(thickness=80.0, epsilon=2.25),)), 'stack.layers'),
+                          (_problem(layers=(rcwa.Layer(thickness=120.0, epsilon=np.ones((3, 2))),
+                                            rcwa.Layer(thickness=80.0, epsilon=2.25))), 'stack.layers'),
+                          (_problem(wavelength=(600.0, 640.0)), 'excitation')):
+        with pytest.raises(rcwa.IncompatibleProblemError) as e:
+            p._check_layout(changed, rcwa._resolve(changed, p.numerics))
+        assert e.value.code == 'prepared.structure' and e.value.path == path
+    asked = rcwa.Problem(stack=base.stack, excitation=base.excitation, units=base.units,
+                         outputs=rcwa.Outputs(fields=True))
+    with pytest.raises(rcwa.IncompatibleProblemError) as e:
+        p._check_layout(asked, rcwa._resolve(asked, p.numerics))
+    assert e.value.path == 'outputs'

@@ -484,8 +484,28 @@ class Prepared:
         self.integrated = _integrated(numerics)
         self.conv = _assemble_layers(r['rasters'], hu, hv, handle, self.integrated)
 
+    @staticmethod
+    def _layout(problem, r):
+        """What a preparation fixes (_adapt.py:633-640 of the reference): the layer count and
+        raster shapes, the number of wavelengths and sources, and the requested outputs; the
+        values in them stay live."""
+        return ((len(r['rasters']), tuple(e.shape for e in r['rasters'])),
+                (len(r['wavelengths']), len(tuple(problem.excitation.sources))),
+                (_wants_fields(problem), _wants_scattering(problem)))
+
+    def _check_layout(self, problem, r):
+        old = self._layout(self.problem, self.resolved)
+        new = self._layout(problem, r)
+        if new != old:
+            path = ('stack.layers' if new[0] != old[0] else 'excitation' if new[1] != old[1] else 'outputs')
+            raise IncompatibleProblemError('The problem declaration layout changed. Prepare it again (layer/source '
+                                           'counts, raster shapes, outputs and spectral shape are structural).',
+                                           code='prepared.structure', path=path)
+
     def run(self, problem=None, *, amplitudes=False):
         r = self.resolved if problem is None else _resolve(problem, self.numerics)
+        if problem is not None:
+            self._check_layout(problem, r)
         conv = self.conv
         if problem is not None and not _same_rasters(r['rasters'], self.resolved['rasters']):
             conv = _assemble_layers(r['rasters'], *r['orders'], self.handle, self.integrated)
