@@ -213,10 +213,12 @@ def test_check_reports_the_resolved_numerics_and_outputs_without_a_gpu():
     assert rep.estimates['retained_field_bytes'] == 16 * 1 * 2 * (2 * (2 * N) ** 2 + 4 * N)
     assert rep.estimates['retained_scattering_bytes'] == 0
     assert rep.estimates['device_workspace_bytes'] > 0
-    with pytest.raises(rcwa.UnsupportedFeatureError) as e:
-        rcwa.check(rcwa.Problem(stack=p.stack, excitation=p.excitation, outputs=rcwa.Outputs(scattering=True)),
-                   numerics=rcwa.Numerics(orders=(1, 1), algorithm='etm'))
-    assert e.value.code == 'rcwa.scattering_algorithm'
+    # as in the reference, check reports a refusal as an issue instead of raising it
+    rep = rcwa.check(rcwa.Problem(stack=p.stack, excitation=p.excitation, outputs=rcwa.Outputs(scattering=True)),
+                     numerics=rcwa.Numerics(orders=(1, 1), algorithm='etm'))
+    assert len(rep.issues) == 1 and rep.issues[0].code == 'rcwa.scattering_algorithm'
+    assert rep.issues[0].path == 'outputs.scattering' and rep.issues[0].severity == 'error'
+    assert rcwa.check(_problem(wavelength=-1.0)).issues[0].code == 'input.invalid'
 
 
 def test_solve_batch_refuses_layer_indices_outside_the_convolution_stack():
@@ -278,3 +280,14 @@ def test_a_prepared_run_refuses_a_changed_layout_and_takes_new_values():
     with pytest.raises(rcwa.IncompatibleProblemError) as e:
         p._check_layout(asked, rcwa._resolve(asked, p.numerics))
     assert e.value.path == 'outputs'
+
+
+def test_validate_reports_instead_of_raising():
+    base = _problem()
+    p = rcwa.Prepared.__new__(rcwa.Prepared)
+    p.problem, p.numerics, p.precision = base, rcwa.Numerics(orders=(1, 1)), 'double'
+    p.resolved = rcwa._resolve(base, p.numerics)
+    ok = p.validate(base)
+    assert ok.issues == () and ok.resolved['layer_count'] == 2
+    bad = p.validate(_problem(layers=(rcwa.Layer(thickness=80.0, epsilon=2.25),)))
+    assert bad.issues[0].code == 'prepared.structure' and bad.issues[0].path == 'stack.layers'

@@ -24,14 +24,27 @@ from . import _lib, engine
 # ------------------------------------------------------------------------------- errors
 
 
+@dataclass(frozen=True)
+class Issue:
+    """One structured finding (errors.py:9-15 of the reference)."""
+    code: str
+    path: str
+    message: str
+    expected: object = None
+    actual: object = None
+    severity: str = 'error'
+
+
 class WavebitError(Exception):
-    """Base error with a machine-readable ``code`` (errors.py:18-66 of the reference)."""
+    """Base error with a machine-readable ``code`` and its ``Issue`` (errors.py:18-66 of the
+    reference)."""
     default_code = 'input.invalid'
 
     def __init__(self, message, *, code=None, path=None):
         self.code = code or self.default_code
         self.path = path
         self.message = message
+        self.issue = Issue(code=self.code, path=path or 'problem', message=message)
         super().__init__(f'{path}: {message}' if path else message)
 
 
@@ -372,13 +385,30 @@ def _numerics_or_default(numerics):
 
 @dataclass
 class CheckReport:
-    issues: tuple
-    estimates: dict
-    resolved: dict
+    issues: tuple = ()
+    estimates: dict = field(default_factory=dict)
+    resolved: dict = field(default_factory=dict)
+
+
+def _issue(error, path='problem'):
+    """The Issue a refusal reports (_lifecycle.py:63-69 of the reference)."""
+    if isinstance(error, WavebitError):
+        return error.issue
+    if isinstance(error, NotImplementedError):
+        return UnsupportedFeatureError(str(error), code='rcwa.unsupported', path=path).issue
+    return ValidationError(str(error), code='rcwa.invalid', path=path).issue
 
 
 def check(problem, *, numerics=None, backend='gb300', device='cuda', precision='double'):
-    """Admission without a solve (_lifecycle.py:422-457): report keys plus GB300 estimates."""
+    """Admission without a solve (_lifecycle.py:422-457): the report keys plus GB300 estimates, or
+    -- as in the reference -- a report whose ``issues`` hold the refusal instead of raising it."""
+    try:
+        return _check(problem, numerics, backend, device, precision)
+    except (ValidationError, TypeError, ValueError, NotImplementedError) as error:
+        return CheckReport(issues=(_issue(error),))
+
+
+def _check(problem, numerics, backend, device, precision):
     r = _resolve(problem, numerics)
     hu, hv = r['orders']
     N = engine.n_orders(hu, hv)
@@ -492,6 +522,16 @@ class Prepared:
         return ((len(r['rasters']), tuple(e.shape for e in r['rasters'])),
                 (len(r['wavelengths']), len(tuple(problem.excitation.sources))),
                 (_wants_fields(problem), _wants_scattering(problem)))
+
+    def validate(self, problem):
+        """Whether a concrete problem can reuse this preparation (_lifecycle.py:678-698 of the
+        reference): its check report, or a report whose ``issues`` say why not."""
+        try:
+            r = _resolve(problem, self.numerics)
+            self._check_layout(problem, r)
+        except (ValidationError, TypeError, ValueError, NotImplementedError) as error:
+            return CheckReport(issues=(_issue(error),))
+        return check(problem, numerics=self.numerics, precision=self.precision)
 
     def _check_layout(self, problem, r):
         old = self._layout(self.problem, self.resolved)
