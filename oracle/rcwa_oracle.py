@@ -423,6 +423,15 @@ def exported_scattering(S, hu, hv):
     return tuple(c[:, None] * blk * c[None, :] for blk in S)
 
 
+def amplitude_ratios(amps, hu, hv):
+    """The published amplitude ratios (results.py:357-390): the Fresnel amplitudes of
+    :func:`sp_result` (r_s, r_p, t_s, t_p, each ``(3, n_v, n_u)``) referenced at the cell centre,
+    order (m, n) times ``(-1)^(m+n)``."""
+    m = order_labels(hu)[None, :] + order_labels(hv)[:, None]
+    d = np.where(m % 2 == 0, 1.0, -1.0)
+    return tuple(d[None] * a for a in amps)
+
+
 def solve_stack(structure, thickness, wavelength, period, hu, hv, theta=0.0, phi=0.0,
                 eps_top=1.0, eps_bot=1.0, polarization='s', conv=None, keep=False):
     """One SMM solve of a raster stack (scattering.py:1185-1456; engine.py:7836-7880).

@@ -21,6 +21,8 @@ It writes
 * ``ref_halfspace.npz`` -- per-order R/T of the reference's own run on scenes with a lossy or
   metallic substrate, total internal reflection, a denser superstrate, and normal incidence at
   an azimuth with cos(phi) < 0;
+* ``ref_amplitudes.npz`` -- the reference's published amplitude ratios of the reference scenes
+  (p and mixed incidence);
 * ``ref_bare.npz`` -- per-order R/T of the reference's own run on stacks with no layers;
 * ``reticolo_cases.npz`` -- RETICOLO's per-order efficiencies of twelve 1D gratings (the
   reference's ``tests/references/golden_reticolo.npz``) with their inputs;
@@ -327,6 +329,39 @@ def make_halfspace_cases():
     print('ref_halfspace.npz:', len(names), 'cases')
 
 
+def make_amplitude_cases():
+    """The reference's published amplitude ratios (outputs['reflected'|'transmitted']
+    .amplitude_ratio_s/_p, results.py:357-390) of the reference scenes under p-polarised and
+    mixed (s, p) incidence."""
+    from wavebit import Material, Units, rcwa
+    out = {}
+    names = []
+    for case in ref_cases():
+        n = case['name']
+        names.append(n)
+        for key in ('structure', 'thickness', 'wavelength', 'period', 'orders', 'theta', 'phi',
+                    'eps_top', 'eps_bot'):
+            out[f'{n}__{key}'] = np.asarray(case[key])
+        st = case['structure'][::-1]
+        th = list(case['thickness'])[::-1]
+        layers = tuple(rcwa.Layer(thickness=float(t), epsilon=np.asarray(e)) for e, t in zip(st, th))
+        for tag, pol in (('p', 'p'), ('mix', (0.6, 0.8j))):
+            prob = rcwa.Problem(
+                units=Units(length='nm'),
+                stack=rcwa.Stack(period=case['period'], top=Material(epsilon=case['eps_top']),
+                                 bottom=Material(epsilon=case['eps_bot']), layers=layers),
+                excitation=rcwa.Excitation(wavelength=case['wavelength'], sources=(
+                    rcwa.PlaneWave(polarization=pol, theta=case['theta'], phi=case['phi']),)))
+            res = rcwa.run(prob, numerics=rcwa.Numerics(orders=case['orders']))
+            for port in ('reflected', 'transmitted'):
+                o = res.outputs[port]
+                out[f'{n}__{tag}_{port}_s'] = np.asarray(o.amplitude_ratio_s)[0]
+                out[f'{n}__{tag}_{port}_p'] = np.asarray(o.amplitude_ratio_p)[0]
+    out['names'] = np.array(names)
+    np.savez_compressed(os.path.join(HERE, 'ref_amplitudes.npz'), **out)
+    print('ref_amplitudes.npz:', len(names), 'cases')
+
+
 def make_bare_cases():
     """Stacks with no layers: the reference solves the bare interface between its half-spaces
     (results.py:180-189) -- per-order R/T of its own run, s and p."""
@@ -401,5 +436,6 @@ if __name__ == '__main__':
     make_etm_cases()
     make_halfspace_cases()
     make_bare_cases()
+    make_amplitude_cases()
     make_legacy_cases()
     make_reticolo_cases()

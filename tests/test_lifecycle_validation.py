@@ -291,3 +291,30 @@ def test_validate_reports_instead_of_raising():
     assert ok.issues == () and ok.resolved['layer_count'] == 2
     bad = p.validate(_problem(layers=(rcwa.Layer(thickness=80.0, epsilon=2.25),)))
     assert bad.issues[0].code == 'prepared.structure' and bad.issues[0].path == 'stack.layers'
+
+
+def test_diffraction_orders_carry_the_reference_amplitude_ratios():
+    """outputs['reflected'|'transmitted'] from amplitudes laid out as the efficiency kernel writes
+    them (B, 3 columns, (r_s, r_p, t_s, t_p), N, about the corner), here the oracle's, against the
+    reference's own published ratios (mixed (0.6, 0.8i) incidence)."""
+    import os
+    import torch
+    from oracle import rcwa_oracle as O
+    d = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'ref_amplitudes.npz'))
+    for name in ('crossed_1', 'crossed_2'):
+        c = {k.split('__', 1)[1]: d[k] for k in d.files if k.startswith(name + '__')}
+        hu, hv = (int(v) for v in c['orders'])
+        o = O.solve_stack(c['structure'], c['thickness'], float(c['wavelength']), tuple(c['period']), hu, hv,
+                          float(c['theta']), float(c['phi']), complex(c['eps_top']), complex(c['eps_bot']),
+                          (0.6, 0.8j))
+        amps = torch.as_tensor(np.stack([np.stack([a[col].reshape(-1) for a in o['amps']]) for col in range(3)]))[None]
+        R = torch.as_tensor(o['R'][0])[None]
+        T = torch.as_tensor(o['T'][0])[None]
+        refl, trans = rcwa._diffraction_orders(R, T, amps, (float(c['wavelength']),), hu, hv)
+        assert refl.orders_u.tolist() == list(range(-hu, hu + 1)) and torch.equal(refl.efficiency, R)
+        for got, key in ((refl.amplitude_ratio_s, 'reflected_s'), (refl.amplitude_ratio_p, 'reflected_p'),
+                         (trans.amplitude_ratio_s, 'transmitted_s'), (trans.amplitude_ratio_p, 'transmitted_p')):
+            want = c[f'mix_{key}']
+            assert np.abs(got[0].numpy() - want).max() <= 1e-12 * max(1.0, np.abs(want).max()), (name, key)
+    none = rcwa._diffraction_orders(R, T, None, (600.0,), hu, hv)
+    assert none[0].amplitude_ratio_s is None and none[1].efficiency is T

@@ -340,3 +340,21 @@ def test_bare_interface_is_a_zero_thickness_layer_of_the_top_medium(name):
         scale = max(np.abs(c[f'R_{pol}']).max(), np.abs(c[f'T_{pol}']).max())
         assert np.abs(o['R'][col] - c[f'R_{pol}']).max() <= 1e-12 * scale, (name, pol)
         assert np.abs(o['T'][col] - c[f'T_{pol}']).max() <= 1e-12 * scale, (name, pol)
+
+
+AMPLITUDE_NAMES = list(np.load(os.path.join(GOLDEN, 'ref_amplitudes.npz'))['names'])
+
+
+@pytest.mark.parametrize('name', AMPLITUDE_NAMES)
+def test_amplitude_ratios_match_the_reference(name):
+    """outputs['reflected'|'transmitted'].amplitude_ratio_s/_p of the reference's own run, p and
+    mixed (0.6, 0.8i) incidence: the oracle's Fresnel amplitudes about the cell centre."""
+    c = _case(np.load(os.path.join(GOLDEN, 'ref_amplitudes.npz')), name)
+    hu, hv = (int(v) for v in c['orders'])
+    for tag, pol in (('p', 'p'), ('mix', (0.6, 0.8j))):
+        o = O.solve_stack(c['structure'], c['thickness'], float(c['wavelength']), tuple(c['period']), hu, hv,
+                          float(c['theta']), float(c['phi']), complex(c['eps_top']), complex(c['eps_bot']), pol)
+        rs, rp, ts, tp = O.amplitude_ratios(o['amps'], hu, hv)
+        for key, mine in (('reflected_s', rs), ('reflected_p', rp), ('transmitted_s', ts), ('transmitted_p', tp)):
+            theirs = c[f'{tag}_{key}']
+            assert np.abs(mine[0] - theirs).max() <= 1e-12 * max(1.0, np.abs(theirs).max()), (name, tag, key)

@@ -438,15 +438,49 @@ def _check(problem, numerics, backend, device, precision):
     return CheckReport(issues=(), estimates=est, resolved=resolved)
 
 
+class DiffractionOrders(NamedTuple):
+    """One port's diffraction orders (results.py:373-392 of the reference): the efficiency of
+    every order ``(wavelength, order_v, order_u)`` and, when the run kept amplitudes, the Fresnel
+    amplitude ratios of its s and p waves referenced at the cell centre."""
+    wavelengths: tuple
+    orders_u: object
+    orders_v: object
+    efficiency: object
+    amplitude_ratio_s: object = None
+    amplitude_ratio_p: object = None
+
+
+def _diffraction_orders(R, T, amplitudes, wavelengths, hu, hv):
+    """``outputs['reflected']`` and ``outputs['transmitted']`` of the given polarization. The
+    kernels' amplitudes (B, 3, 4, N: column, (r_s, r_p, t_s, t_p), order) are about the cell
+    corner; order (m, n) about the centre is ``(-1)^(m+n)`` times it."""
+    ou, ov = np.arange(-hu, hu + 1), np.arange(-hv, hv + 1)
+    ratios = [None] * 4
+    if amplitudes is not None:
+        m = ou[None, :] + ov[:, None]
+        sign = torch.as_tensor(np.where(m % 2 == 0, 1.0, -1.0), dtype=torch.complex128, device=amplitudes.device)
+        B = amplitudes.shape[0]
+        ratios = [amplitudes[:, 0, k].reshape(B, 2 * hv + 1, 2 * hu + 1) * sign for k in range(4)]
+    return (DiffractionOrders(wavelengths, ou, ov, R, ratios[0], ratios[1]),
+            DiffractionOrders(wavelengths, ou, ov, T, ratios[2], ratios[3]))
+
+
 class Result:
-    """R and T with the reference's ``(wavelength, order_v, order_u)`` axes, on the device."""
+    """R and T with the reference's ``(wavelength, order_v, order_u)`` axes, on the device.
+
+    ``outputs`` holds the reference's ``'reflected'`` / ``'transmitted'`` diffraction orders of
+    the given polarization, and the per-polarization efficiencies of the three incidence columns
+    (``'incident'``, ``'s_inc'``, ``'p_inc'``)."""
 
     def __init__(self, R, T, R_sp, T_sp, status, wavelengths, diagnostics, amplitudes=None, scattering=None,
-                 field_states=None, field_geometry=None):
+                 field_states=None, field_geometry=None, orders=None):
         self.R, self.T = R, T
         self.outputs = {'incident': {'R': R, 'T': T},
                         's_inc': {'R': R_sp[0], 'T': T_sp[0]},
                         'p_inc': {'R': R_sp[1], 'T': T_sp[1]}}
+        if orders is not None:
+            self.outputs['reflected'], self.outputs['transmitted'] = _diffraction_orders(
+                R, T, amplitudes, wavelengths, *orders)
         self.status = status
         self.wavelengths = wavelengths
         self.diagnostics = diagnostics
@@ -610,7 +644,7 @@ class Prepared:
         return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]), status, tuple(r['wavelengths']),
                       diag, out[3] if amplitudes else None, S, states,
                       (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0),
-                       r.get('bare_interface', False)))
+                       r.get('bare_interface', False)), orders=r['orders'])
 
     def _solve_etm(self, r, conv, layer_index, fields=False):
         """``Numerics(algorithm='etm')``: the ETM recursion over the FP64 modes of every
@@ -638,7 +672,7 @@ class Prepared:
         return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]),
                       torch.as_tensor(st, device=R.device), tuple(r['wavelengths']), diag, None, None, states,
                       (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0),
-                       r.get('bare_interface', False)))
+                       r.get('bare_interface', False)), orders=r['orders'])
 
     def _mode_chunks(self, r, conv, layer_index, wl, th, per_wl_bytes, budget=2 << 30):
         """FP64 modes of every (wavelength, layer) pair (wb_layer_modes), a chunk of wavelengths
