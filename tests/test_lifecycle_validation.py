@@ -318,3 +318,15 @@ def test_diffraction_orders_carry_the_reference_amplitude_ratios():
             assert np.abs(got[0].numpy() - want).max() <= 1e-12 * max(1.0, np.abs(want).max()), (name, key)
     none = rcwa._diffraction_orders(R, T, None, (600.0,), hu, hv)
     assert none[0].amplitude_ratio_s is None and none[1].efficiency is T
+
+
+def test_result_reports_power_entering_absorption_and_validity():
+    import torch
+    R = torch.tensor([[[0.1, 0.2]], [[0.3, 0.0]]], dtype=torch.float64)
+    T = torch.tensor([[[0.5, 0.1]], [[0.6, 0.05]]], dtype=torch.float64)
+    res = rcwa.Result(R, T, (R, R), (T, T), None, (600.0, 700.0), {}, orders=(0, 0))
+    assert torch.allclose(res.outputs['power_entering'], torch.tensor([0.7, 0.7], dtype=torch.float64))
+    assert torch.allclose(res.outputs['absorption'], torch.tensor([0.1, 0.05], dtype=torch.float64))
+    assert torch.allclose(res.absorption, res.outputs['absorption'])
+    assert res.validity['checks']['numerical_finite'] is True
+    assert res.validity['convergence']['status'] == 'not assessed'

@@ -481,6 +481,18 @@ class Result:
         if orders is not None:
             self.outputs['reflected'], self.outputs['transmitted'] = _diffraction_orders(
                 R, T, amplitudes, wavelengths, *orders)
+        if torch.is_tensor(R) and torch.is_tensor(T):
+            # real in-plane wavevectors and a lossless superstrate: the net flux into the stack is
+            # the incident one less the reflected orders' (results.py:375-380)
+            sr, st_ = R.sum(dim=(-2, -1)), T.sum(dim=(-2, -1))
+            self.outputs['power_entering'] = 1.0 - sr
+            self.outputs['absorption'] = 1.0 - sr - st_
+            finite = bool(torch.isfinite(R).all()) and bool(torch.isfinite(T).all())
+        else:
+            finite = None
+        # finiteness is numerical validity, not a statement of convergence in the orders
+        self.validity = {'checks': {'numerical_finite': finite},
+                         'convergence': {'status': 'not assessed', 'requires': 'independent refinement study'}}
         self.status = status
         self.wavelengths = wavelengths
         self.diagnostics = diagnostics
