@@ -330,3 +330,16 @@ def test_result_reports_power_entering_absorption_and_validity():
     assert torch.allclose(res.absorption, res.outputs['absorption'])
     assert res.validity['checks']['numerical_finite'] is True
     assert res.validity['convergence']['status'] == 'not assessed'
+
+
+def test_sample_structure_returns_the_raster_the_solve_reads():
+    p = _problem()
+    np.testing.assert_array_equal(rcwa.sample_structure(p, layer=0), np.full((1, 1), 2.25 + 0j))
+    np.testing.assert_array_equal(rcwa.sample_structure(p, layer=1), np.array([[1.0, 12.25], [12.25, 1.0]]))
+    for kw, code in ((dict(layer=2), 'structure.layer'), (dict(samples=0), 'structure.samples'),
+                     (dict(quantity='chi'), 'structure.quantity'), (dict(wavelength_index=3), 'structure.wavelength')):
+        with pytest.raises(rcwa.ValidationError) as e:
+            rcwa.sample_structure(p, **kw)
+        assert e.value.code == code
+    with pytest.raises(rcwa.UnsupportedFeatureError):
+        rcwa.sample_structure(p, quantity='mu')

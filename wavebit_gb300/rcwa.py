@@ -844,6 +844,36 @@ def prepare(problem, *, numerics=None, backend='gb300', device='cuda', precision
     return Prepared(problem, numerics, precision, handle)
 
 
+def sample_structure(problem, *, layer=0, samples=512, wavelength_index=0, quantity='epsilon', component=None):
+    """One layer's relative permittivity as the solve reads it, without a solve
+    (_structure.py:19-100 of the reference): a raster layer keeps its own resolution, axes
+    ``(y, x)``, row zero the negative-y edge; ``layer`` counts from the bottom. Region and
+    profiled layers, permeability and tensor components are outside the raster path."""
+    layers = tuple(problem.stack.layers)
+    if type(layer) is not int or not 0 <= layer < len(layers):
+        raise ValidationError('layer must index a finite layer from zero.', code='structure.layer', path='layer')
+    if type(samples) is not int or samples < 1:
+        raise ValidationError('samples must be a positive integer.', code='structure.samples', path='samples')
+    if quantity not in ('epsilon', 'mu'):
+        raise ValidationError("quantity must be 'epsilon' or 'mu'.", code='structure.quantity', path='quantity')
+    wl = np.atleast_1d(np.asarray(problem.excitation.wavelength, dtype=np.float64)).reshape(-1)
+    if type(wavelength_index) is not int or not 0 <= wavelength_index < len(wl):
+        raise ValidationError('wavelength_index must index the excitation spectrum from zero.',
+                              code='structure.wavelength', path='wavelength_index')
+    if quantity == 'mu' or component is not None:
+        raise UnsupportedFeatureError('permeability and tensor components are outside the GB300 raster path',
+                                      path='quantity' if quantity == 'mu' else 'component')
+    selected = layers[layer]
+    if getattr(selected, 'regions', ()):
+        raise UnsupportedFeatureError('region (shape) layers are outside the GB300 raster path',
+                                      path=f'stack.layers[{layer}]')
+    eps = selected.epsilon
+    if eps is None:
+        eps = _scalar_eps(selected.background, f'stack.layers[{layer}].background')
+    eps = np.array(eps.detach().cpu().numpy() if hasattr(eps, 'detach') else eps, dtype=np.complex128)
+    return eps.reshape(1, 1) if eps.ndim == 0 else eps.reshape(1, -1) if eps.ndim == 1 else eps
+
+
 def run(problem, *, numerics=None, backend='gb300', device='cuda', precision='double', amplitudes=False):
     """``prepare(...).run()`` (_lifecycle.py:801-803)."""
     return prepare(problem, numerics=numerics, backend=backend, device=device,
