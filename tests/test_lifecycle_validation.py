@@ -334,8 +334,9 @@ def test_result_reports_power_entering_absorption_and_validity():
 
 def test_sample_structure_returns_the_raster_the_solve_reads():
     p = _problem()
-    np.testing.assert_array_equal(rcwa.sample_structure(p, layer=0), np.full((1, 1), 2.25 + 0j))
-    np.testing.assert_array_equal(rcwa.sample_structure(p, layer=1), np.array([[1.0, 12.25], [12.25, 1.0]]))
+    # the public stack lists layers from the bottom: layer 0 is the raster, layer 1 the uniform one
+    np.testing.assert_array_equal(rcwa.sample_structure(p, layer=0), np.array([[1.0, 12.25], [12.25, 1.0]]))
+    np.testing.assert_array_equal(rcwa.sample_structure(p, layer=1), np.full((1, 1), 2.25 + 0j))
     for kw, code in ((dict(layer=2), 'structure.layer'), (dict(samples=0), 'structure.samples'),
                      (dict(quantity='chi'), 'structure.quantity'), (dict(wavelength_index=3), 'structure.wavelength')):
         with pytest.raises(rcwa.ValidationError) as e:
