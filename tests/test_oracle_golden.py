@@ -358,3 +358,13 @@ def test_amplitude_ratios_match_the_reference(name):
         for key, mine in (('reflected_s', rs), ('reflected_p', rp), ('transmitted_s', ts), ('transmitted_p', tp)):
             theirs = c[f'{tag}_{key}']
             assert np.abs(mine[0] - theirs).max() <= 1e-12 * max(1.0, np.abs(theirs).max()), (name, tag, key)
+
+
+def test_quickstart_totals():
+    """The reference README's quickstart (one 300 nm layer [[1, 1, 12.25, 12.25]], period 700 nm,
+    eps_sub 2.25, orders (10, 0), normal s incidence at 900 nm): total R and T as the reference
+    prints them, R = 0.2053316282584904 and T = 0.7946683717415131."""
+    out = O.solve_stack(np.array([[[1.0, 1.0, 12.25, 12.25]]]), np.array([300.0]), 900.0, (700.0, 700.0), 10, 0,
+                        0.0, 0.0, 1.0, 2.25, 's')
+    assert abs(out['R'][0].sum() - 0.2053316282584904) < 1e-13
+    assert abs(out['T'][0].sum() - 0.7946683717415131) < 1e-13
