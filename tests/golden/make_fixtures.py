@@ -15,7 +15,8 @@ It writes
 * ``ref_scattering.npz`` -- the stack's exported scattering matrix (``Outputs(scattering=True)``)
   of five of those scenes;
 * ``ref_fields.npz`` -- collocated field phasors (``Outputs(fields=True)``, ``result.field``) of
-  five of those scenes at explicit points, s and p incidence;
+  five of those scenes and two of ``ref_halfspace.npz`` (total internal reflection, a metallic
+  substrate) at explicit points, s and p incidence;
 * ``ref_etm.npz`` -- per-order R/T of the reference's ETM connecting algorithm on the scenes of
   ``ref_cases.npz``;
 * ``ref_halfspace.npz`` -- per-order R/T of the reference's own run on scenes with a lossy or
@@ -201,9 +202,10 @@ def make_field_cases():
     from wavebit import Material, Units, rcwa
     out = {}
     names = []
-    for case in ref_cases():
-        if case['name'] not in ('grating_1d', 'crossed_0', 'crossed_1', 'crossed_4', 'symmetric_pillar'):
-            continue
+    scenes = [c for c in ref_cases() if c['name'] in ('grating_1d', 'crossed_0', 'crossed_1', 'crossed_4',
+                                                         'symmetric_pillar')]
+    scenes += [c for c in halfspace_cases() if c['name'] in ('tir', 'metal_substrate')]
+    for case in scenes:
         n = case['name']
         names.append(n)
         for key in ('structure', 'thickness', 'wavelength', 'period', 'orders', 'theta', 'phi',
