@@ -18,7 +18,7 @@ It writes
   five of those scenes and two of ``ref_halfspace.npz`` (total internal reflection, a metallic
   substrate) at explicit points, s and p incidence;
 * ``ref_etm.npz`` -- per-order R/T of the reference's ETM connecting algorithm on the scenes of
-  ``ref_cases.npz``;
+  ``ref_cases.npz`` and ``ref_halfspace.npz``;
 * ``ref_halfspace.npz`` -- per-order R/T of the reference's own run on scenes with a lossy or
   metallic substrate, total internal reflection, a denser superstrate, and normal incidence at
   an azimuth with cos(phi) < 0;
@@ -168,9 +168,9 @@ def make_scattering_cases():
     from wavebit import Material, Units, rcwa
     out = {}
     names = []
-    for case in ref_cases():
-        if case['name'] not in ('grating_1d', 'crossed_0', 'crossed_1', 'crossed_4', 'symmetric_pillar'):
-            continue
+    scenes = [c for c in ref_cases() if c['name'] in ('grating_1d', 'crossed_0', 'crossed_1', 'crossed_4',
+                                                         'symmetric_pillar')] + halfspace_cases()
+    for case in scenes:
         n = case['name']
         names.append(n)
         for key in ('structure', 'thickness', 'wavelength', 'period', 'orders', 'theta', 'phi',
@@ -244,7 +244,7 @@ def make_etm_cases():
     solve_2d.py:2619-2843) on the reference scenes, s and p incidence."""
     out = {}
     names = []
-    for case in ref_cases():
+    for case in ref_cases() + halfspace_cases():
         n = case['name']
         names.append(n)
         for key in ('structure', 'thickness', 'wavelength', 'period', 'orders', 'theta', 'phi',
