@@ -84,6 +84,50 @@ def test_both_outputs_resolve():
     assert r['amplitude'] == 3.0 and rcwa._wants_fields(p) and rcwa._wants_scattering(p)
 
 
+def _stack_S(structure, thickness, wl, period, hu, hv, kinc, phi, eps_top, eps_bot):
+    """The oracle cascade of solve_stack with the incident transverse wavevector given rather than
+    derived from theta: the form the device's mirrored stack takes (its k_par fixed by the lit side)."""
+    conv = O.to_conv_mat_raster_sampled(np.asarray(structure, complex), hu, hv)
+    kx, ky = O.separable_kxy(wl, period, kinc, hu, hv)
+    kxg, kyg = O.order_grid(kx, ky)
+    N = kxg.shape[0]; k0 = 2 * np.pi / wl
+    et, eb = np.complex128(eps_top), np.complex128(eps_bot)
+    kpar = kxg ** 2 + kyg ** 2
+    kzt, kzb = O.boundary_kz(et, kpar), O.boundary_kz(eb, kpar)
+    y = O.gap_waves(kxg, kyg)
+    I, Z = np.eye(N, dtype=complex), np.zeros((N, N), complex)
+    Wt = np.block([[I, Z], [Z, -1j * np.diag(kzt) / et]]); Vt = np.block([[-1j * np.diag(kzt), Z], [Z, I]])
+    Wb = np.block([[I, Z], [Z, -1j * np.diag(kzb) / eb]]); Vb = np.block([[-1j * np.diag(kzb), Z], [Z, I]])
+    Wg = np.block([[I, Z], [Z, -1j * np.diag(y)]]); Vg = np.block([[-1j * np.diag(y), Z], [Z, I]])
+    vphi = O.order_azimuth(kyg.reshape(ky.shape[0], kx.shape[0]), kxg.reshape(ky.shape[0], kx.shape[0]), phi)
+    c, s = np.cos(vphi), np.sin(vphi)
+    S = O.s_reflection(Wt, Vt, Wg, Vg)
+    for i in range(len(structure)):
+        W, V, q, w, _ = O.layer_modes_2d(kxg, kyg, conv[0][i], conv[1][i], conv[2][i])
+        bW, bV = O.sp_modes_2d(W, V, c, s, N)
+        A, B = O.ab_matrices(bW, bV, Wg, Vg)
+        S = O.redheffer_star(S, O.s_layer(A, B, np.diag(np.exp(-k0 * thickness[i] * q))))
+    return O.redheffer_star(S, O.s_transmission(Wb, Vb, Wg, Vg))
+
+
+
+@pytest.mark.parametrize('name', NAMES)
+def test_the_mirrored_stack_gives_the_far_side_blocks(name):
+    """The construction wb_scattering_matrix uses for S22 and S12: the stack with its layers in
+    reverse order and its half-spaces swapped, at the same transverse wavevector, lit from the
+    former substrate -- its S11 and S21 are the stack's S22 and S12 (here against the reference's
+    own blocks, complex and evanescent half-spaces included)."""
+    c = _case(name)
+    hu, hv = (int(v) for v in c['orders'])
+    et, eb = complex(c['eps_top']), complex(c['eps_bot'])
+    kinc = O.incident_kxy(float(c['theta']), float(c['phi']), et)
+    mir = O.exported_scattering(_stack_S(c['structure'][::-1], c['thickness'][::-1], float(c['wavelength']),
+                                         tuple(c['period']), hu, hv, kinc, float(c['phi']), eb, et), hu, hv)
+    for got, key in ((mir[0], 'S22'), (mir[2], 'S12')):
+        want = c[key]
+        assert np.abs(got - want).max() <= 1e-12 * max(1.0, np.abs(want).max()), (name, key)
+
+
 def _problem(c, **kw):
     st, th = np.asarray(c['structure'], complex), np.asarray(c['thickness'], float)
     layers = tuple(rcwa.Layer(thickness=float(t), epsilon=e) for e, t in zip(st[::-1], th[::-1]))
