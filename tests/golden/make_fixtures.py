@@ -22,8 +22,8 @@ It writes
 * ``ref_halfspace.npz`` -- per-order R/T of the reference's own run on scenes with a lossy or
   metallic substrate, total internal reflection, a denser superstrate, and normal incidence at
   an azimuth with cos(phi) < 0;
-* ``ref_amplitudes.npz`` -- the reference's published amplitude ratios of the reference scenes
-  (p and mixed incidence);
+* ``ref_amplitudes.npz`` -- the reference's published amplitude ratios of the scenes of
+  ``ref_cases.npz`` and ``ref_halfspace.npz`` (p and mixed incidence);
 * ``ref_bare.npz`` -- per-order R/T of the reference's own run on stacks with no layers;
 * ``reticolo_cases.npz`` -- RETICOLO's per-order efficiencies of twelve 1D gratings (the
   reference's ``tests/references/golden_reticolo.npz``) with their inputs;
@@ -338,7 +338,7 @@ def make_amplitude_cases():
     from wavebit import Material, Units, rcwa
     out = {}
     names = []
-    for case in ref_cases():
+    for case in ref_cases() + halfspace_cases():
         n = case['name']
         names.append(n)
         for key in ('structure', 'thickness', 'wavelength', 'period', 'orders', 'theta', 'phi',
