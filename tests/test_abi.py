@@ -126,3 +126,35 @@ def test_scattering_matrix_refuses_bad_arguments_before_any_device_work(lib):
     assert lib.wb_scattering_matrix(*args(0)) == _lib.WB_E_INVALID
     assert lib.wb_scattering_matrix(*args(4, hu=-1)) == _lib.WB_E_INVALID
     assert 'wb_scattering_matrix' in _lib.last_error()
+
+
+def test_header_is_plain_c_and_a_c_program_links(lib, tmp_path):
+    """The boundary is a C ABI: the public header compiles as strict C99 (no C++ or torch types)
+    and a C program links libwbgpu.so and calls its host-only entry points."""
+    import shutil
+    import subprocess
+    from wavebit_gb300 import _lib
+    gcc = shutil.which('gcc')
+    if gcc is None:
+        pytest.skip('gcc is not available')
+    src = tmp_path / 'main.c'
+    src.write_text('''
+#include <stdio.h>
+#include "wavebit_gb300.h"
+int main(void) {
+  int32_t lu[5], lv[3], tu[25], tv[9];
+  int rc = wb_build_indices(2, 1, lu, lv, tu, tv);
+  printf("%d %d %d %d %zu\\n", wb_version(), rc, lu[0], tv[8], wb_workspace_bytes(2, 1, 1, 1, WB_PRECISION_FP64));
+  return rc;
+}
+''')
+    exe = tmp_path / 'main'
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    cc = subprocess.run([gcc, '-std=c99', '-Wall', '-Wextra', '-Werror', '-pedantic', '-I', os.path.join(ROOT, 'include'),
+                         '-o', str(exe), str(src), '-L', libdir, '-lwbgpu', f'-Wl,-rpath,{libdir}'],
+                        capture_output=True, text=True)
+    assert cc.returncode == 0, cc.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert run.returncode == 0, run.stderr
+    version, rc, first, last, ws = run.stdout.split()
+    assert (int(version), int(rc), int(first), int(last)) == (201, 0, -2, 2) and int(ws) > 0
