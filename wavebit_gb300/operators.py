@@ -20,7 +20,11 @@ import torch
 from . import engine
 from . import rcwa as _rcwa
 
-__all__ = ['ConvMatrices', 'Operators', 'assemble', 'solve']
+__all__ = ['ConvMatrices', 'Operators', 'Port', 'ScatteringMatrix', 'assemble', 'solve']
+
+# the scattering-matrix types, which the reference's operators module re-exports (operators.py:14-21)
+Port = _rcwa.Port
+ScatteringMatrix = _rcwa.ScatteringMatrix
 
 
 class ConvMatrices(NamedTuple):
