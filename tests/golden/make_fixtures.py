@@ -232,6 +232,10 @@ def make_field_cases():
             f = res.field(x=x, y=y, z=z)
             out[f'{n}__field_{pol}'] = np.asarray(f.values)
             out[f'{n}__amplitude_{pol}'] = np.asarray(amp)
+            # counts: a centred grid in x and y, each layer's own heights face to face in z
+            fc = res.field(x=3, y=2, z=3)
+            out[f'{n}__field_counts_{pol}'] = np.asarray(fc.values)
+            out[f'{n}__counts_z_{pol}'] = np.asarray(fc.coordinates['z'])
         out[f'{n}__x'], out[f'{n}__y'], out[f'{n}__z'] = x, y, z
         out[f'{n}__total'] = np.asarray(total)
     out['names'] = np.array(names)

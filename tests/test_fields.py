@@ -147,3 +147,29 @@ def test_lifecycle_field_states_on_the_cpu(name, monkeypatch):
             res.field(x=c['x'], y=c['y'], z=c['z'], reconstruction='lalanne')
         counts = res.field(x=3, y=2, z=2)
         assert counts.values.shape == (1, 2 * L, 2, 3, 6)
+
+
+@pytest.mark.parametrize('name', NAMES)
+def test_count_sampling_matches_the_reference_on_the_cpu(name):
+    """x=3, y=2, z=3: a centred grid across the cell and every layer's own heights from its bottom
+    face to its top face (an internal face twice, the lower layer's first), field_result.py:85-106,
+    375-398 -- the heights and the phasors against the reference's."""
+    c = _case(name)
+    hu, hv = (int(v) for v in c['orders'])
+    st = np.asarray(c['structure'], complex)
+    th = np.asarray(c['thickness'], float)
+    wl, per = float(c['wavelength']), tuple(float(p) for p in c['period'])
+    pv = ports(wl, per, float(c['theta']), float(c['phi']), complex(c['eps_top']), complex(c['eps_bot']), hu, hv, 'cpu')
+    conv = O.to_conv_mat_raster_sampled(st, hu, hv)
+    modes, epz = [], []
+    for i in range(st.shape[0]):
+        W, V, q, _, _ = O.layer_modes_2d(pv['kx'].numpy() + 0j, pv['ky'].numpy() + 0j, conv[0][i], conv[1][i], conv[2][i])
+        modes.append(tuple(torch.as_tensor(a) for a in (W, V, q)))
+        epz.append(torch.as_tensor(conv[2][i]))
+    for pol in ('s', 'p'):
+        state = F.build_state(modes, epz, th, wl, pv, O.polarization_pair(pol), hu, hv)
+        z, owner, depth = F.height_points(3, th)
+        assert np.allclose(z, c[f'counts_z_{pol}'], rtol=0, atol=1e-9)
+        got = F.synthesize(state, owner, depth, F.axis_points(3, per[0], 'x'), F.axis_points(2, per[1], 'y'),
+                           float(c[f'amplitude_{pol}'])).numpy()
+        _check(got, c[f'field_counts_{pol}'][0], 1e-12, (name, pol))
