@@ -236,6 +236,11 @@ def make_field_cases():
             fc = res.field(x=3, y=2, z=3)
             out[f'{n}__field_counts_{pol}'] = np.asarray(fc.values)
             out[f'{n}__counts_z_{pol}'] = np.asarray(fc.coordinates['z'])
+            # the half-spaces' waves on the two faces (results.py:231-265)
+            for side in ('top', 'bottom'):
+                for part in ('incoming', 'outgoing', 'total'):
+                    b = res.boundary_fields(side=side, x=x, y=y, part=part)
+                    out[f'{n}__boundary_{side}_{part}_{pol}'] = np.asarray(b.values)
         out[f'{n}__x'], out[f'{n}__y'], out[f'{n}__z'] = x, y, z
         out[f'{n}__total'] = np.asarray(total)
     out['names'] = np.array(names)

@@ -173,3 +173,31 @@ def test_count_sampling_matches_the_reference_on_the_cpu(name):
         got = F.synthesize(state, owner, depth, F.axis_points(3, per[0], 'x'), F.axis_points(2, per[1], 'y'),
                            float(c[f'amplitude_{pol}'])).numpy()
         _check(got, c[f'field_counts_{pol}'][0], 1e-12, (name, pol))
+
+
+@pytest.mark.parametrize('name', NAMES)
+def test_boundary_fields_match_the_reference_on_the_cpu(name):
+    """The half-spaces' waves on both faces (incoming, outgoing, total) from the field state built
+    on the CPU with the oracle's modes, against the reference's result.boundary_fields."""
+    c = _case(name)
+    hu, hv = (int(v) for v in c['orders'])
+    st = np.asarray(c['structure'], complex)
+    th = np.asarray(c['thickness'], float)
+    wl, per = float(c['wavelength']), tuple(float(p) for p in c['period'])
+    pv = ports(wl, per, float(c['theta']), float(c['phi']), complex(c['eps_top']), complex(c['eps_bot']), hu, hv, 'cpu')
+    conv = O.to_conv_mat_raster_sampled(st, hu, hv)
+    modes, epz = [], []
+    for i in range(st.shape[0]):
+        W, V, q, _, _ = O.layer_modes_2d(pv['kx'].numpy() + 0j, pv['ky'].numpy() + 0j, conv[0][i], conv[1][i], conv[2][i])
+        modes.append(tuple(torch.as_tensor(a) for a in (W, V, q)))
+        epz.append(torch.as_tensor(conv[2][i]))
+    for pol in ('s', 'p'):
+        state = F.build_state(modes, epz, th, wl, pv, O.polarization_pair(pol), hu, hv)
+        for side in ('top', 'bottom'):
+            for part in ('incoming', 'outgoing', 'total'):
+                got = F.expand_boundary(state, side, part, c['x'], c['y'], float(c[f'amplitude_{pol}'])).numpy()
+                want = c[f'boundary_{side}_{part}_{pol}'][0]
+                if np.abs(want).max() == 0:
+                    assert np.abs(got).max() == 0, (name, pol, side, part)
+                else:
+                    _check(got, want, 1e-12, (name, pol, side, part))

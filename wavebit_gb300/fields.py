@@ -45,12 +45,15 @@ class LayerState(NamedTuple):
 
 
 class FieldState(NamedTuple):
-    """What one wavelength keeps for :meth:`Result.field`; layers entry (top) face first."""
+    """What one wavelength keeps for :meth:`Result.field` and :meth:`Result.boundary_fields`;
+    layers entry (top) face first; ``boundary`` maps each face to its (incoming, outgoing)
+    six-component spectra (N, 6)."""
     k0: float
     kx: torch.Tensor          # (N,) per-order kx / k0
     ky: torch.Tensor
     odd: torch.Tensor         # (N,) True where (-1)^(m+n) = -1 (corner -> centre sign)
     layers: tuple
+    boundary: dict = None
 
 
 class FieldSamples(NamedTuple):
@@ -89,7 +92,7 @@ def layer_amplitudes(modes, thickness, k0, pv, C):
         bw, bv = sp_rotate(W, V, pv['c'], pv['s'])
         bW.append(bw); bV.append(bv)
         Xs.append(torch.exp(-k0 * float(d) * q))
-    _, _, sv = cascade_forward(bW, bV, Xs, pv, C)
+    cref, ctrn, sv = cascade_forward(bW, bV, Xs, pv, C)
     wg, vg = pv['wg'][:, None], pv['vg'][:, None]
     out = []
     for l, ((W, V, q), d) in enumerate(zip(modes, thickness)):
@@ -103,7 +106,59 @@ def layer_amplitudes(modes, thickness, k0, pv, C):
         keep = (torch.abs(q * kd) < TOP_FACE)[:, None]
         carried = torch.exp(torch.where(keep[:, 0], kd * q, torch.zeros_like(q)))[:, None] * minus_top
         out.append((plus, torch.where(keep, carried, minus_bottom)))
-    return out
+    return out, cref, ctrn
+
+
+def boundary_spectra(pv, cref, ctrn, pol, odd):
+    """Each face's (incoming, outgoing) six-component spectra of the incident column, (N, 6) per
+    order (field_result.py:700-800, ordinary_spectra / ordinary_state): on the lit (top) face the
+    incident wave and the reflected orders, on the far face nothing and the transmitted orders.
+    Every order's s and p waves take the Cartesian basis ``e_s = (-s, c, 0)``,
+    ``e_p = (-kz c, -kz s, d rho) / n``, ``H = k x e`` (k = (kx, ky, d kz), d = -1 down, +1 up,
+    rho = kx c + ky s) of the half-space it lives in; the coefficients are the Fresnel amplitude
+    ratios about the cell centre (the reflected p one with the opposite sign to that basis)."""
+    N = pv['kx'].shape[0]
+    dev = pv['kx'].device
+    C = torch.complex128
+    gx, gy = pv['kx'].to(C), pv['ky'].to(C)
+    c, s = pv['c'].to(C), pv['s'].to(C)
+    n_top, n_bot = complex(pv['nt']), complex(pv['nb'])
+    sign = torch.where(odd, -1.0, 1.0).to(C)
+    r_s = cref[:N, 0] * sign
+    r_p = (-cref[N:, 0]) / (-1j * n_top) * sign
+    t_s = ctrn[:N, 0] * sign
+    t_p = ctrn[N:, 0] / (-1j * n_bot) * sign
+    zero = torch.zeros_like(gx)
+    rho = gx * c + gy * s
+
+    def basis(n, kz, d):
+        es = torch.stack([-s, c, zero], -1)
+        ep = torch.stack([-kz * c / n, -kz * s / n, d * rho / n], -1)
+        k = torch.stack([gx, gy, d * kz], -1)
+        return (torch.cat([es, torch.linalg.cross(k, es)], -1), torch.cat([ep, torch.linalg.cross(k, ep)], -1))
+
+    inc_s, inc_p = basis(n_top, pv['kzt'], -1.0)
+    ref_s, ref_p = basis(n_top, pv['kzt'], 1.0)
+    trn_s, trn_p = basis(n_bot, pv['kzb'], -1.0)
+    delta = torch.zeros(N, dtype=C, device=dev)
+    delta[N // 2] = 1.0
+    incoming = delta[:, None] * (complex(pol[0]) * inc_s + complex(pol[1]) * inc_p)
+    reflected = r_s[:, None] * ref_s - r_p[:, None] * ref_p
+    transmitted = t_s[:, None] * trn_s + t_p[:, None] * trn_p
+    return {'top': (incoming, reflected), 'bottom': (torch.zeros_like(transmitted), transmitted)}
+
+
+def expand_boundary(state, side, part, x, y, amplitude):
+    """``(ny, nx, 6)`` phasors of one face's waves at the centre-origin points (field_result.py:109-122)."""
+    incoming, outgoing = state.boundary[side]
+    coef = incoming if part == 'incoming' else outgoing if part == 'outgoing' else incoming + outgoing
+    dev = state.kx.device
+    xs = torch.as_tensor(x, dtype=torch.float64, device=dev)
+    ys = torch.as_tensor(y, dtype=torch.float64, device=dev)
+    arg = state.k0 * (xs[None, :, None] * state.kx[None, None, :] + ys[:, None, None] * state.ky[None, None, :])
+    out = torch.exp(1j * arg) @ coef                                    # (ny, nx, 6)
+    scale = torch.as_tensor([1, 1, 1, 1 / Z0, 1 / Z0, 1 / Z0], dtype=torch.complex128, device=dev)
+    return complex(amplitude) * out * scale
 
 
 def layer_coefficients(layer, k0, kx, ky, depth):
@@ -215,7 +270,8 @@ def build_state(modes, epz_i, thickness, wavelength, pv, pol, hu, hv):
     C = torch.zeros((2 * N, 1), dtype=torch.complex128, device=dev)
     C[N // 2, 0] = complex(pol[0])
     C[N + N // 2, 0] = -1j * complex(pv['nt']) * complex(pol[1])
-    amps = layer_amplitudes(modes, thickness, k0, pv, C)
+    amps, cref, ctrn = layer_amplitudes(modes, thickness, k0, pv, C)
     layers = tuple(LayerState(W, V, q, float(d), e, plus[:, 0], minus[:, 0])
                    for (W, V, q), d, e, (plus, minus) in zip(modes, thickness, epz_i, amps))
-    return FieldState(k0, pv['kx'], pv['ky'], order_parity(hu, hv, dev), layers)
+    odd = order_parity(hu, hv, dev)
+    return FieldState(k0, pv['kx'], pv['ky'], odd, layers, boundary_spectra(pv, cref, ctrn, pol, odd))

@@ -533,6 +533,30 @@ class Result:
                               metadata={'axis_order': ('wavelength', 'z', 'y', 'x', 'component'),
                                         'time_convention': 'exp(-i*omega*t)'})
 
+    def boundary_fields(self, *, side, x, y, part='total'):
+        """Collocated phasors of the half-spaces' waves on the top or bottom face (results.py:231-265
+        of the reference): ``part`` ``'incoming'``, ``'outgoing'`` or ``'total'``; values
+        ``(wavelength, y, x, 6)``, E in V/m and H in A/m; ``x``, ``y`` from the cell centre."""
+        from . import fields as F
+        if not self._field_states:
+            raise UnsupportedFeatureError('This result did not retain field reconstruction state. Request '
+                                          'Outputs(fields=True).', code='outputs.unavailable', path='outputs.fields')
+        for name, value, allowed in (('side', side, ('top', 'bottom')),
+                                     ('part', part, ('incoming', 'outgoing', 'total'))):
+            if not isinstance(value, str) or value not in allowed:
+                raise ValidationError(f'{name} is one of {", ".join(map(repr, allowed))}; got {value!r}.',
+                                      code=f'field.{name}', path=name)
+        period, amplitude = self._field_geometry[1], self._field_geometry[2]
+        try:
+            xs = F.axis_points(x, period[0], 'x')
+            ys = F.axis_points(y, period[1], 'y')
+        except ValueError as e:
+            raise ValidationError(str(e), code='field.coordinates', path='x/y') from e
+        values = torch.stack([F.expand_boundary(st, side, part, xs, ys, amplitude) for st in self._field_states])
+        return F.FieldSamples(coordinates={'x': xs, 'y': ys, 'wavelength': self.wavelengths}, values=values,
+                              components=F.COMPONENTS, sampling='collocated boundary phasor',
+                              metadata={'side': side, 'part': part, 'axis_order': ('wavelength', 'y', 'x', 'component')})
+
     @property
     def scattering(self):
         """One :class:`ScatteringMatrix` per wavelength (results.py:137-141 of the reference)."""
