@@ -103,6 +103,10 @@ def test_lifecycle_fields_match_the_reference(name):
         assert f.values.shape == (1, len(c['z']), len(c['y']), len(c['x']), 6)
         assert f.values.device.type == 'cuda' and f.components == F.COMPONENTS
         _check(f.values[0].cpu().numpy(), c[f'field_{pol}'][0], 1e-10, (name, pol))
+        for side in ('top', 'bottom'):
+            want = c[f'boundary_{side}_total_{pol}'][0]
+            got = res.boundary_fields(side=side, x=c['x'], y=c['y']).values[0].cpu().numpy()
+            _check(got, want, 1e-10, (name, pol, side))
 
 
 def _oracle_layer_modes(conv, pair_layer, kx, ky, precision='double', handle=None):
@@ -147,6 +151,12 @@ def test_lifecycle_field_states_on_the_cpu(name, monkeypatch):
             res.field(x=c['x'], y=c['y'], z=c['z'], reconstruction='lalanne')
         counts = res.field(x=3, y=2, z=2)
         assert counts.values.shape == (1, 2 * L, 2, 3, 6)
+        b = res.boundary_fields(side='top', x=c['x'], y=c['y'], part='outgoing')
+        _check(b.values[0].numpy(), c[f'boundary_top_outgoing_{pol}'][0], 1e-12, (name, pol, 'boundary'))
+        assert b.metadata['side'] == 'top' and b.values.shape == (1, len(c['y']), len(c['x']), 6)
+        with pytest.raises(rcwa.ValidationError) as e:
+            res.boundary_fields(side='left', x=c['x'], y=c['y'])
+        assert e.value.code == 'field.side'
 
 
 @pytest.mark.parametrize('name', NAMES)
