@@ -236,6 +236,9 @@ def make_field_cases():
             fc = res.field(x=3, y=2, z=3)
             out[f'{n}__field_counts_{pol}'] = np.asarray(fc.values)
             out[f'{n}__counts_z_{pol}'] = np.asarray(fc.coordinates['z'])
+            # Lalanne's rule: E_x, E_y of patterned layers from the D series line by line
+            fl = res.field(x=x, y=y, z=z, reconstruction='lalanne')
+            out[f'{n}__field_lalanne_{pol}'] = np.asarray(fl.values)
             # the half-spaces' waves on the two faces (results.py:231-265)
             for side in ('top', 'bottom'):
                 for part in ('incoming', 'outgoing', 'total'):

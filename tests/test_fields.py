@@ -103,6 +103,8 @@ def test_lifecycle_fields_match_the_reference(name):
         assert f.values.shape == (1, len(c['z']), len(c['y']), len(c['x']), 6)
         assert f.values.device.type == 'cuda' and f.components == F.COMPONENTS
         _check(f.values[0].cpu().numpy(), c[f'field_{pol}'][0], 1e-10, (name, pol))
+        fl = res.field(x=c['x'], y=c['y'], z=c['z'], reconstruction='lalanne')
+        _check(fl.values[0].cpu().numpy(), c[f'field_lalanne_{pol}'][0], 1e-10, (name, pol, 'lalanne'))
         for side in ('top', 'bottom'):
             want = c[f'boundary_{side}_total_{pol}'][0]
             got = res.boundary_fields(side=side, x=c['x'], y=c['y']).values[0].cpu().numpy()
@@ -141,14 +143,21 @@ def test_lifecycle_field_states_on_the_cpu(name, monkeypatch):
         th = np.full(len(wl), r['theta'])
         states = p._field_states(r, conv, np.tile(np.arange(L), (len(wl), 1)), wl, th)
         res = rcwa.Result(None, None, (None, None), (None, None), None, tuple(wl), {}, None, None, states,
-                          (np.asarray(r['thickness']), r['period'], r['amplitude']))
+                          (np.asarray(r['thickness']), r['period'], r['amplitude'], False, (hu, hv)))
         f = res.field(x=c['x'], y=c['y'], z=c['z'])
         _check(f.values[0].numpy(), c[f'field_{pol}'][0], 1e-12, (name, pol))
         with pytest.raises(rcwa.ValidationError) as e:
             res.field(x=c['x'], y=c['y'], z=[-5.0])
         assert e.value.code == 'field.coordinates'
-        with pytest.raises(rcwa.UnsupportedFeatureError):
-            res.field(x=c['x'], y=c['y'], z=c['z'], reconstruction='lalanne')
+        fl = res.field(x=c['x'], y=c['y'], z=c['z'], reconstruction='lalanne')
+        _check(fl.values[0].numpy(), c[f'field_lalanne_{pol}'][0], 1e-12, (name, pol, 'lalanne'))
+        assert fl.metadata['reconstruction'] == 'lalanne'
+        with pytest.raises(rcwa.UnsupportedFeatureError) as e:
+            res.field(x=c['x'], y=c['y'], z=c['z'], reconstruction='splitw')
+        assert e.value.code == 'field.reconstruction'
+        with pytest.raises(rcwa.ValidationError) as e:
+            res.field(x=c['x'], y=c['y'], z=c['z'], reconstruction='li')
+        assert e.value.code == 'field.reconstruction'
         counts = res.field(x=3, y=2, z=2)
         assert counts.values.shape == (1, 2 * L, 2, 3, 6)
         b = res.boundary_fields(side='top', x=c['x'], y=c['y'], part='outgoing')
@@ -211,3 +220,27 @@ def test_boundary_fields_match_the_reference_on_the_cpu(name):
                     assert np.abs(got).max() == 0, (name, pol, side, part)
                 else:
                     _check(got, want, 1e-12, (name, pol, side, part))
+
+
+@pytest.mark.parametrize('name', NAMES)
+def test_lalanne_rule_matches_the_reference_on_the_cpu(name):
+    """reconstruction='lalanne' (E_x, E_y of patterned layers from the D series line by line,
+    P. Lalanne and M. P. Jurek 1998) on the CPU with the oracle's modes, against the reference's."""
+    c = _case(name)
+    hu, hv = (int(v) for v in c['orders'])
+    st = np.asarray(c['structure'], complex)
+    th = np.asarray(c['thickness'], float)
+    wl, per = float(c['wavelength']), tuple(float(p) for p in c['period'])
+    pv = ports(wl, per, float(c['theta']), float(c['phi']), complex(c['eps_top']), complex(c['eps_bot']), hu, hv, 'cpu')
+    conv = O.to_conv_mat_raster_sampled(st, hu, hv)
+    modes, epz = [], []
+    for i in range(st.shape[0]):
+        W, V, q, _, _ = O.layer_modes_2d(pv['kx'].numpy() + 0j, pv['ky'].numpy() + 0j, conv[0][i], conv[1][i], conv[2][i])
+        modes.append(tuple(torch.as_tensor(a) for a in (W, V, q)))
+        epz.append(torch.as_tensor(conv[2][i]))
+    for pol in ('s', 'p'):
+        state = F.build_state(modes, epz, th, wl, pv, O.polarization_pair(pol), hu, hv, rasters=list(st))
+        z, owner, depth = F.height_points(c['z'], th)
+        got = F.synthesize(state, owner, depth, c['x'], c['y'], float(c[f'amplitude_{pol}']), 'lalanne', per,
+                           (hu, hv)).numpy()
+        _check(got, c[f'field_lalanne_{pol}'][0], 1e-11, (name, pol))

@@ -34,7 +34,8 @@ COMPONENTS = ('Ex', 'Ey', 'Ez', 'Hx', 'Hy', 'Hz')
 
 class LayerState(NamedTuple):
     """One layer of one wavelength: Cartesian modes (natural orientation), roots, thickness,
-    the inverse-zz convolution slot (cell corner) and the incident column's amplitudes."""
+    the inverse-zz convolution slot (cell corner), the incident column's amplitudes and the
+    layer's raster ``(ny, nx)`` (for Lalanne's rule; ``None`` when not kept)."""
     W: torch.Tensor
     V: torch.Tensor
     q: torch.Tensor
@@ -42,6 +43,7 @@ class LayerState(NamedTuple):
     epz_i: torch.Tensor
     plus: torch.Tensor
     minus: torch.Tensor
+    raster: object = None
 
 
 class FieldState(NamedTuple):
@@ -179,6 +181,73 @@ def layer_coefficients(layer, k0, kx, ky, depth):
     return torch.stack([Sx, Sy, -Sz, 1j * Ux, 1j * Uy, -1j * Uz], dim=-1)   # (nz, N, 6)
 
 
+# ------------------------------------------------------------------ Lalanne's rule (2D)
+
+def staircase_series(lines, h):
+    """Orders ``-2h..2h`` of each line (rows of ``lines``) as an exact staircase over equal pixels
+    about the cell corner -- the series stage A's series_kernel evaluates (factorization.py:
+    289-440): the DFT of ``(a - a0)/n`` at ``k mod n``, times ``sinc(k/n) exp(-i pi k/n)``, plus
+    ``a0`` at order 0."""
+    lines = np.asarray(lines, dtype=np.complex128)
+    n = lines.shape[-1]
+    k = np.arange(-2 * h, 2 * h + 1)
+    a0 = lines[:, :1]
+    spec = np.fft.fft((lines - a0) / n, axis=-1) if n > 1 else np.zeros_like(lines)
+    t = k / n
+    with np.errstate(invalid='ignore', divide='ignore'):
+        sinc = np.where(k == 0, 1.0, np.sin(np.pi * t) / (np.pi * t))
+    out = spec[:, k % n] * (sinc * np.exp(-1j * np.pi * t))[None, :]
+    out[:, 2 * h] += a0[:, 0]
+    return out
+
+
+def line_rules(lines, h):
+    """Li's inverse rule ``[T(1/a)]^-1`` of each line, ``(m, 2h+1, 2h+1)``, ``T[r, c] = c_{r-c}``
+    (factorization.py:570-592): it takes the Fourier coefficients of the field normal to the
+    line's walls to those of its displacement."""
+    c = staircase_series(1.0 / np.asarray(lines, dtype=np.complex128), h)
+    r = np.arange(2 * h + 1)
+    return np.linalg.inv(c[:, r[:, None] - r[None, :] + 2 * h])
+
+
+def sample_pixels(corner_points, period, n_pixels):
+    """The raster pixel under each sample (corner-origin coordinates), periodically; a sample
+    on a wall belongs to the pixel on its positive side (lalanne.py:298-318)."""
+    frac = np.asarray(corner_points, dtype=np.float64) / float(period)
+    return np.floor(frac * n_pixels + 1e-9).astype(int) % n_pixels
+
+
+def lalanne_pair(coef, raster, hu, hv, k0, kx_u, ky_v, x, y, period, phase, odd):
+    """``E_x`` and ``E_y`` ``(nz, ny, nx)`` of a patterned layer by Lalanne's rule
+    (fields.py:1068-1110, field_result.py:610-650 of the reference): in the kernels' corner frame
+    (the centre sign of ``coef`` undone), the ``E_x`` series is summed over the y orders, turned
+    into the ``D_x`` series by the inverse rule of the raster row under each y sample, summed over
+    x and divided by ``eps`` at the sample; ``E_y`` likewise along the columns; ``phase`` puts the
+    incident wave's phase at the cell centre back."""
+    dev = coef.device
+    nu, nv = 2 * hu + 1, 2 * hv + 1
+    ny, nx = raster.shape
+    xc = np.asarray(x, dtype=np.float64) + 0.5 * period[0]
+    yc = np.asarray(y, dtype=np.float64) + 0.5 * period[1]
+    cols = sample_pixels(xc, period[0], nx)
+    rows = sample_pixels(yc, period[1], ny)
+    ops_x = torch.as_tensor(line_rules(raster[rows], hu), device=dev)              # (n_y, nu, nu)
+    ops_y = torch.as_tensor(line_rules(raster[:, cols].T, hv), device=dev)         # (n_x, nv, nv)
+    eps = torch.as_tensor(raster[np.ix_(rows, cols)], device=dev)                 # (n_y, n_x)
+    kernel = torch.where(odd[None, :, None], -coef, coef)
+    gx = kernel[..., 0].reshape(-1, nv, nu)
+    gy = kernel[..., 1].reshape(-1, nv, nu)
+    px = torch.exp(1j * k0 * torch.as_tensor(xc, device=dev)[:, None] * kx_u[None, :])   # (n_x, nu)
+    py = torch.exp(1j * k0 * torch.as_tensor(yc, device=dev)[:, None] * ky_v[None, :])   # (n_y, nv)
+    ex_rows = torch.einsum('jv,zvu->zju', py, gx)
+    dx = torch.einsum('jab,zjb->zja', ops_x, ex_rows)
+    ex = torch.einsum('zju,iu->zji', dx, px) / eps
+    ey_cols = torch.einsum('zvu,iu->ziv', gy, px)
+    dy = torch.einsum('iab,zib->zia', ops_y, ey_cols)
+    ey = torch.einsum('ziv,jv->zji', dy, py) / eps
+    return ex * phase, ey * phase
+
+
 def heights(thickness_top_first, z):
     """Public heights -> ``(owner, depth)``: the layer (entry face first) holding each height and
     the depth below that layer's top face. Heights run upward from the bottom face; a face
@@ -196,9 +265,11 @@ def heights(thickness_top_first, z):
     return L - 1 - j, ds[j] - (z - edges[j])
 
 
-def synthesize(state, owner, depth, x, y, amplitude):
+def synthesize(state, owner, depth, x, y, amplitude, reconstruction='plain', period=None, orders=None):
     """``(nz, ny, nx, 6)`` phasors of one wavelength at the heights ``(owner, depth)`` and the
-    centre-origin points ``x`` (nx,), ``y`` (ny,) (field_result.py:109-122, 640-690)."""
+    centre-origin points ``x`` (nx,), ``y`` (ny,) (field_result.py:109-122, 640-690).
+    ``reconstruction='lalanne'`` rebuilds ``E_x`` and ``E_y`` in patterned layers by Lalanne's rule
+    (needs the ``period`` and the ``orders`` ``(hu, hv)``)."""
     dev = state.kx.device
     nz, N = owner.shape[0], state.kx.shape[0]
     coef = torch.zeros((nz, N, 6), dtype=torch.complex128, device=dev)
@@ -215,6 +286,20 @@ def synthesize(state, owner, depth, x, y, amplitude):
     arg = state.k0 * (xs[None, :, None] * state.kx[None, None, :] + ys[:, None, None] * state.ky[None, None, :])
     phase = torch.exp(1j * arg).reshape(-1, N)                         # (ny*nx, N)
     out = torch.einsum('po,zoc->zpc', phase, coef).reshape(nz, ys.shape[0], xs.shape[0], 6)
+    if reconstruction == 'lalanne':
+        hu, hv = orders
+        nu = 2 * hu + 1
+        kx_u, ky_v = state.kx[:nu], state.ky[::nu]
+        spec = N // 2
+        centre_phase = torch.exp(-1j * state.k0 * (state.kx[spec] * 0.5 * period[0] + state.ky[spec] * 0.5 * period[1]))
+        for p, layer in enumerate(state.layers):
+            r = layer.raster
+            sel = np.flatnonzero(owner == p)
+            if r is None or not sel.size or np.all(r == r.flat[0]):
+                continue                          # a uniform layer keeps the Fourier sum
+            idx = torch.as_tensor(sel, device=dev)
+            ex, ey = lalanne_pair(coef[idx], r, hu, hv, state.k0, kx_u, ky_v, x, y, period, centre_phase, state.odd)
+            out[idx, :, :, 0], out[idx, :, :, 1] = ex, ey
     scale = torch.as_tensor([1, 1, 1, 1 / Z0, 1 / Z0, 1 / Z0], dtype=torch.complex128, device=dev)
     return complex(amplitude) * out * scale
 
@@ -260,7 +345,7 @@ def order_parity(hu, hv, device):
     return torch.as_tensor(m.reshape(-1) % 2 == 1, device=device)
 
 
-def build_state(modes, epz_i, thickness, wavelength, pv, pol, hu, hv):
+def build_state(modes, epz_i, thickness, wavelength, pv, pol, hu, hv, rasters=None):
     """The :class:`FieldState` of one wavelength from its layers' ``(W, V, q)`` (Cartesian,
     entry face first), their corner-frame ``epz_i`` slots and the port vectors ``pv``; ``pol``
     is the source's ``(a_s, a_p)``."""
@@ -271,7 +356,8 @@ def build_state(modes, epz_i, thickness, wavelength, pv, pol, hu, hv):
     C[N // 2, 0] = complex(pol[0])
     C[N + N // 2, 0] = -1j * complex(pv['nt']) * complex(pol[1])
     amps, cref, ctrn = layer_amplitudes(modes, thickness, k0, pv, C)
-    layers = tuple(LayerState(W, V, q, float(d), e, plus[:, 0], minus[:, 0])
-                   for (W, V, q), d, e, (plus, minus) in zip(modes, thickness, epz_i, amps))
+    rasters = rasters if rasters is not None else [None] * len(modes)
+    layers = tuple(LayerState(W, V, q, float(d), e, plus[:, 0], minus[:, 0], r)
+                   for (W, V, q), d, e, (plus, minus), r in zip(modes, thickness, epz_i, amps, rasters))
     odd = order_parity(hu, hv, dev)
     return FieldState(k0, pv['kx'], pv['ky'], odd, layers, boundary_spectra(pv, cref, ctrn, pol, odd))

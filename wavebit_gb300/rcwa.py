@@ -505,15 +505,18 @@ class Result:
         """Collocated complex phasors at explicit points or counts (results.py:148-229 of the
         reference): values ``(wavelength, z, y, x, 6)`` for ``(Ex, Ey, Ez, Hx, Hy, Hz)``, E in
         V/m and H in A/m; ``x``, ``y`` from the cell centre, ``z`` upward from the stack's bottom
-        face (a face belongs to the layer above it). ``reconstruction='plain'`` only."""
+        face (a face belongs to the layer above it). ``reconstruction`` is ``'plain'`` (the modes'
+        Fourier sums) or ``'lalanne'`` (``E_x``, ``E_y`` of patterned layers from the displacement
+        series line by line, field_result.py:610-650)."""
         from . import fields as F
         if not self._field_states:
             raise UnsupportedFeatureError('This result did not retain field reconstruction state. Request '
                                           'Outputs(fields=True).', code='outputs.unavailable', path='outputs.fields')
-        if reconstruction in ('lalanne', 'split', 'splitw'):
+        if reconstruction in ('split', 'splitw'):
             raise UnsupportedFeatureError(f'reconstruction={reconstruction!r} is outside the GB300 raster path; '
-                                          "use 'plain'", code='field.reconstruction', path='reconstruction')
-        if reconstruction != 'plain':
+                                          "use 'plain' or 'lalanne'", code='field.reconstruction',
+                                          path='reconstruction')
+        if reconstruction not in ('plain', 'lalanne'):
             raise ValidationError(f"reconstruction must be 'plain', 'lalanne', 'split' or 'splitw', not "
                                   f'{reconstruction!r}.', code='field.reconstruction', path='reconstruction')
         thickness, period, amplitude = self._field_geometry[:3]
@@ -527,11 +530,13 @@ class Result:
             zs, owner, depth = F.height_points(z, thickness)
         except ValueError as e:
             raise ValidationError(str(e), code='field.coordinates', path='x/y/z') from e
-        values = torch.stack([F.synthesize(st, owner, depth, xs, ys, amplitude) for st in self._field_states])
+        orders = self._field_geometry[4] if len(self._field_geometry) > 4 else None
+        values = torch.stack([F.synthesize(st, owner, depth, xs, ys, amplitude, reconstruction, period, orders)
+                              for st in self._field_states])
         return F.FieldSamples(coordinates={'x': xs, 'y': ys, 'z': zs, 'wavelength': self.wavelengths},
                               values=values, components=F.COMPONENTS, sampling='collocated Cartesian phasor',
                               metadata={'axis_order': ('wavelength', 'z', 'y', 'x', 'component'),
-                                        'time_convention': 'exp(-i*omega*t)'})
+                                        'time_convention': 'exp(-i*omega*t)', 'reconstruction': reconstruction})
 
     def boundary_fields(self, *, side, x, y, part='total'):
         """Collocated phasors of the half-spaces' waves on the top or bottom face (results.py:231-265
@@ -680,7 +685,7 @@ class Prepared:
         return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]), status, tuple(r['wavelengths']),
                       diag, out[3] if amplitudes else None, S, states,
                       (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0),
-                       r.get('bare_interface', False)), orders=r['orders'])
+                       r.get('bare_interface', False), tuple(r['orders'])), orders=r['orders'])
 
     def _solve_etm(self, r, conv, layer_index, fields=False):
         """``Numerics(algorithm='etm')``: the ETM recursion over the FP64 modes of every
@@ -708,7 +713,7 @@ class Prepared:
         return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]),
                       torch.as_tensor(st, device=R.device), tuple(r['wavelengths']), diag, None, None, states,
                       (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0),
-                       r.get('bare_interface', False)), orders=r['orders'])
+                       r.get('bare_interface', False), tuple(r['orders'])), orders=r['orders'])
 
     def _mode_chunks(self, r, conv, layer_index, wl, th, per_wl_bytes, budget=2 << 30):
         """FP64 modes of every (wavelength, layer) pair (wb_layer_modes), a chunk of wavelengths
@@ -746,7 +751,8 @@ class Prepared:
             for i, b in enumerate(idx):
                 modes = [(W[i * L + l], V[i * L + l], q[i * L + l]) for l in range(L)]
                 epz = [conv.slot(2)[int(layer_index[b][l])] for l in range(L)]
-                states.append(F.build_state(modes, epz, r['thickness'], wl[b], pvs[i], r['pol'], hu, hv))
+                rasters = [r['rasters'][int(layer_index[b][l])] for l in range(L)]
+                states.append(F.build_state(modes, epz, r['thickness'], wl[b], pvs[i], r['pol'], hu, hv, rasters))
         return tuple(states)
 
     def _scattering(self, r, conv, layer_index, wl, th):
