@@ -239,6 +239,9 @@ def make_field_cases():
             # Lalanne's rule: E_x, E_y of patterned layers from the D series line by line
             fl = res.field(x=x, y=y, z=z, reconstruction='lalanne')
             out[f'{n}__field_lalanne_{pol}'] = np.asarray(fl.values)
+            # and at counts, whose x samples sit on the cell's two edges
+            out[f'{n}__field_counts_lalanne_{pol}'] = np.asarray(
+                res.field(x=3, y=2, z=3, reconstruction='lalanne').values)
             # the half-spaces' waves on the two faces (results.py:231-265)
             for side in ('top', 'bottom'):
                 for part in ('incoming', 'outgoing', 'total'):

@@ -244,3 +244,9 @@ def test_lalanne_rule_matches_the_reference_on_the_cpu(name):
         got = F.synthesize(state, owner, depth, c['x'], c['y'], float(c[f'amplitude_{pol}']), 'lalanne', per,
                            (hu, hv)).numpy()
         _check(got, c[f'field_lalanne_{pol}'][0], 1e-11, (name, pol))
+        # counts put x samples on both cell edges, and every internal face in both layers
+        xs, ys = F.axis_points(3, per[0], 'x'), F.axis_points(2, per[1], 'y')
+        _, owner, depth = F.height_points(3, th)
+        got = F.synthesize(state, owner, depth, xs, ys, float(c[f'amplitude_{pol}']), 'lalanne', per,
+                           (hu, hv)).numpy()
+        _check(got, c[f'field_counts_lalanne_{pol}'][0], 1e-11, (name, pol, 'counts'))
