@@ -374,6 +374,25 @@ def make_amplitude_cases():
                 o = res.outputs[port]
                 out[f'{n}__{tag}_{port}_s'] = np.asarray(o.amplitude_ratio_s)[0]
                 out[f'{n}__{tag}_{port}_p'] = np.asarray(o.amplitude_ratio_p)[0]
+            # the other per-order readings, with a 2.5 V/m source in micrometres (power scales
+            # with |amplitude|^2 and the cell measure with the length unit)
+            prob_um = rcwa.Problem(
+                units=Units(length='um'),
+                stack=rcwa.Stack(period=tuple(p / 1000 for p in case['period']),
+                                 top=Material(epsilon=case['eps_top']), bottom=Material(epsilon=case['eps_bot']),
+                                 layers=tuple(rcwa.Layer(thickness=float(t) / 1000, epsilon=np.asarray(e))
+                                              for e, t in zip(st, th))),
+                excitation=rcwa.Excitation(wavelength=case['wavelength'] / 1000, sources=(
+                    rcwa.PlaneWave(polarization=pol, theta=case['theta'], phi=case['phi'], amplitude=2.5),)))
+            res = rcwa.run(prob_um, numerics=rcwa.Numerics(orders=case['orders']))
+            for port in ('reflected', 'transmitted'):
+                o = res.outputs[port]
+                for key in ('amplitude_ratio_xyz', 'power', 'k_parallel', 'k_normal', 'efficiency'):
+                    out[f'{n}__{tag}_{port}_{key}'] = np.asarray(getattr(o, key))[0]
+                out[f'{n}__{tag}_{port}_plane'] = np.asarray(o.reference['plane'])
+                out[f'{n}__{tag}_{port}_cell_measure'] = np.asarray(o.reference['cell_measure'])
+                out[f'{n}__{tag}_{port}_incident_power'] = np.asarray(o.reference['incident_power'])
+                out[f'{n}__{tag}_{port}_epsilon'] = np.asarray(o.reference['epsilon'])
     out['names'] = np.array(names)
     np.savez_compressed(os.path.join(HERE, 'ref_amplitudes.npz'), **out)
     print('ref_amplitudes.npz:', len(names), 'cases')

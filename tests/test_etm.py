@@ -48,6 +48,31 @@ def test_etm_recursion_matches_the_reference_on_the_cpu(name):
     _check(R.numpy(), T.numpy(), c, 1e-12, name)
 
 
+@pytest.mark.parametrize('name', ['crossed_1', 'crossed_4', 'metal_substrate', 'tir'])
+def test_etm_amplitudes_are_the_smm_fresnel_amplitudes(name):
+    """etm_solve(amplitudes=True): the final matching's unknowns, as the efficiency kernel's
+    Fresnel amplitudes (r_s, r_p, t_s, t_p about the cell corner), equal the oracle's SMM ones
+    under mixed incidence; the pure-s and pure-p columns too."""
+    c = _case(name)
+    hu, hv = (int(v) for v in c['orders'])
+    st, th = np.asarray(c['structure'], complex), np.asarray(c['thickness'], float)
+    wl, per = float(c['wavelength']), tuple(float(p) for p in c['period'])
+    pol = (0.6, 0.8j)
+    o = O.solve_stack(st, th, wl, per, hu, hv, float(c['theta']), float(c['phi']), complex(c['eps_top']),
+                      complex(c['eps_bot']), pol)
+    pv = ports(wl, per, float(c['theta']), float(c['phi']), complex(c['eps_top']), complex(c['eps_bot']), hu, hv, 'cpu')
+    conv = O.to_conv_mat_raster_sampled(st, hu, hv)
+    modes = []
+    for i in range(st.shape[0]):
+        W, V, q, _, _ = O.layer_modes_2d(pv['kx'].numpy() + 0j, pv['ky'].numpy() + 0j, conv[0][i], conv[1][i], conv[2][i])
+        modes.append(tuple(torch.as_tensor(a) for a in (W, V, q)))
+    _, _, amps = E.etm_solve(modes, th, 2 * np.pi / wl, pv, O.polarization_pair(pol), 2 * hu + 1, 2 * hv + 1,
+                             amplitudes=True)
+    want = np.stack([np.stack([a[col].reshape(-1) for a in o['amps']]) for col in range(3)])
+    assert amps.shape == want.shape
+    assert np.abs(amps.numpy() - want).max() <= 1e-12 * np.abs(want).max(), name
+
+
 def _problem(c, **kw):
     st, th = np.asarray(c['structure'], complex), np.asarray(c['thickness'], float)
     layers = tuple(rcwa.Layer(thickness=float(t), epsilon=e) for e, t in zip(st[::-1], th[::-1]))
@@ -89,6 +114,12 @@ def test_lifecycle_etm_on_the_cpu(name, monkeypatch):
     _check(np.stack([res.R[0].numpy(), res.outputs['s_inc']['R'][0].numpy(), res.outputs['p_inc']['R'][0].numpy()]),
            np.stack([res.T[0].numpy(), res.outputs['s_inc']['T'][0].numpy(), res.outputs['p_inc']['T'][0].numpy()]),
            c, 1e-12, name)
+    # the lifecycle's per-order readings: powers add up to the efficiencies times the incident power
+    refl, trans = res.reflection, res.transmission
+    p_inc = float(refl.reference['incident_power'][0])
+    assert refl.reference['length_units'] == 'nm' and refl.k_normal.shape == refl.efficiency.shape
+    assert float(refl.power.sum()) == pytest.approx(float(res.R.sum()) * p_inc, rel=1e-10)
+    assert float(trans.power.sum()) == pytest.approx(float(res.T.sum()) * p_inc, rel=1e-10)
 
 
 @pytest.mark.gpu
@@ -106,3 +137,8 @@ def test_lifecycle_etm_matches_the_reference_on_the_gpu(name):
     T = np.stack([etm.T[0].cpu().numpy()] + [etm.outputs[k]['T'][0].cpu().numpy() for k in ('s_inc', 'p_inc')])
     _check(R, T, c, 1e-10, name)
     assert np.abs(etm.R.cpu().numpy() - smm.R.cpu().numpy()).max() <= 1e-10
+    for port in ('reflected', 'transmitted'):
+        for key in ('amplitude_ratio_s', 'amplitude_ratio_p', 'power'):
+            a, b = getattr(etm.outputs[port], key), getattr(smm.outputs[port], key)
+            scale = torch.abs(b).max().item() if key == 'power' else max(1.0, torch.abs(b).max().item())
+            assert torch.abs(a - b).max().item() <= 1e-9 * scale, (name, port, key)

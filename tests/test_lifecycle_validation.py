@@ -344,3 +344,66 @@ def test_sample_structure_returns_the_raster_the_solve_reads():
         assert e.value.code == code
     with pytest.raises(rcwa.UnsupportedFeatureError):
         rcwa.sample_structure(p, quantity='mu')
+
+
+def _amplitude_case(name):
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'ref_amplitudes.npz'))
+    return {k.split('__', 1)[1]: d[k] for k in d.files if k.startswith(name + '__')}
+
+
+@pytest.mark.parametrize('name', ['grating_1d', 'crossed_1', 'crossed_3', 'symmetric_pillar', 'lossy_substrate',
+                                  'metal_substrate', 'tir', 'dense_superstrate', 'normal_rotated'])
+def test_order_readings_match_the_reference(name):
+    """outputs['reflected'|'transmitted'] beyond the ratios -- amplitude_ratio_xyz, power (W),
+    k_parallel, k_normal, and the reference's plane, cell measure, medium and incident power --
+    from the oracle's amplitudes, against the reference's own run in micrometres with a 2.5 V/m
+    source (results.py:292-420)."""
+    import torch
+    from oracle import rcwa_oracle as O
+    c = _amplitude_case(name)
+    hu, hv = (int(v) for v in c['orders'])
+    um = 1e-3
+    wl, per = float(c['wavelength']) * um, tuple(float(p) * um for p in c['period'])
+    th = np.asarray(c['thickness'], float) * um
+    for tag, pol in (('p', 'p'), ('mix', (0.6, 0.8j))):
+        o = O.solve_stack(c['structure'], th, wl, per, hu, hv, float(c['theta']), float(c['phi']),
+                          complex(c['eps_top']), complex(c['eps_bot']), pol)
+        amps = torch.as_tensor(np.stack([np.stack([a[col].reshape(-1) for a in o['amps']]) for col in range(3)]))[None]
+        R, T = torch.as_tensor(o['R'][0])[None], torch.as_tensor(o['T'][0])[None]
+        ports = dict(wavelengths=[wl], thetas=[float(c['theta'])], phi=float(c['phi']), period=per,
+                     eps_top=complex(c['eps_top']), eps_bot=complex(c['eps_bot']), pol=O.polarization_pair(pol),
+                     amplitude=2.5, length='um', top_plane=float(th.sum()))
+        refl, trans = rcwa._diffraction_orders(R, T, amps, (wl,), hu, hv, ports=ports)
+        p_inc = float(c[f'{tag}_reflected_incident_power'][0])
+        assert abs(float(refl.reference['incident_power'][0]) - p_inc) <= 1e-13 * p_inc, (name, tag)
+        for port, got in (('reflected', refl), ('transmitted', trans)):
+            key = f'{tag}_{port}'
+            for field_, tol in (('amplitude_ratio_xyz', 1e-11), ('k_parallel', 1e-13), ('k_normal', 1e-13)):
+                want = c[f'{key}_{field_}']
+                diff = np.abs(getattr(got, field_)[0].numpy() - want).max()
+                assert diff <= tol * max(1.0, np.abs(want).max()), (name, key, field_, diff)
+            assert np.abs(got.power[0].numpy() - c[f'{key}_power']).max() <= 1e-11 * p_inc, (name, key)
+            assert np.abs(got.efficiency[0].numpy() - c[f'{key}_efficiency']).max() <= 1e-11, (name, key)
+            assert got.reference['plane'][0] == pytest.approx(float(c[f'{key}_plane'][0]), rel=1e-14, abs=1e-18)
+            assert got.reference['cell_measure'][0] == pytest.approx(float(c[f'{key}_cell_measure'][0]), rel=1e-14)
+            assert got.reference['epsilon'][0] == complex(c[f'{key}_epsilon'][0])
+            # the CW field is the ratio times the source, and one order reads the same arrays
+            assert torch.equal(got.field_xyz, got.amplitude_ratio_xyz * 2.5)
+            one = got.order(0, 0)
+            assert one.k_normal.shape == (1,) and torch.equal(one.power, got.power[:, hv, hu])
+        # the outgoing powers add up to the efficiencies times the incident power
+        total = float(refl.power.sum() + trans.power.sum())
+        assert total == pytest.approx(float(R.sum() + T.sum()) * p_inc, rel=1e-9, abs=1e-12 * p_inc)
+
+
+def test_units_and_order_lookup_refusals():
+    import torch
+    with pytest.raises(rcwa.ValidationError) as e:
+        rcwa.Units(length='inch')
+    assert e.value.code == 'units.length'
+    R = torch.zeros((1, 3, 5), dtype=torch.float64)
+    refl, _ = rcwa._diffraction_orders(R, R, None, (1.0,), 2, 1)
+    with pytest.raises(KeyError):
+        refl.order(3, 0)
+    assert refl.order(-2, 1).efficiency.shape == (1,) and refl.field_s is None

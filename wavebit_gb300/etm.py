@@ -27,11 +27,13 @@ def _diag(v):
     return torch.diag_embed(v)
 
 
-def etm_solve(modes, thickness, k0, pv, pol, n_u, n_v):
+def etm_solve(modes, thickness, k0, pv, pol, n_u, n_v, amplitudes=False):
     """Per-order efficiencies ``(R, T)``, each ``(3, n_v, n_u)`` for the given polarization,
     pure s and pure p, of one wavelength. ``modes``: ``(W, V, q)`` per layer, Cartesian, entry
     face first; ``pv``: the port vectors of :func:`wavebit_gb300.adjoint.ports`; ``pol``:
-    ``(a_s, a_p)``."""
+    ``(a_s, a_p)``. With ``amplitudes`` also the Fresnel amplitudes ``(3, 4, N)`` in the
+    efficiency kernel's layout (column; r_s, r_p, t_s, t_p; order, about the cell corner): the
+    final matching's p unknowns are ``-i n`` times the Fresnel p ratios."""
     kzt, kzb = pv['kzt'], pv['kzb']
     et, eb = complex(pv['et']), complex(pv['eb'])
     n_top = complex(pv['nt'])
@@ -87,4 +89,8 @@ def etm_solve(modes, thickness, k0, pv, pol, n_u, n_v):
 
     R = (power(Rs, kzt) + power(Rp, kzt / et)) / denom
     Tr = (power(Ts, kzb) + power(Tp, kzb / eb)) / denom
-    return R.reshape(3, n_v, n_u), Tr.reshape(3, n_v, n_u)
+    if not amplitudes:
+        return R.reshape(3, n_v, n_u), Tr.reshape(3, n_v, n_u)
+    n_bot = complex(pv['nb'])
+    amps = torch.stack([Rs, Rp / (-1j * n_top), Ts, Tp / (-1j * n_bot)]).permute(2, 0, 1)
+    return R.reshape(3, n_v, n_u), Tr.reshape(3, n_v, n_u), amps

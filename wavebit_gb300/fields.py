@@ -111,25 +111,16 @@ def layer_amplitudes(modes, thickness, k0, pv, C):
     return out, cref, ctrn
 
 
-def boundary_spectra(pv, cref, ctrn, pol, odd):
-    """Each face's (incoming, outgoing) six-component spectra of the incident column, (N, 6) per
-    order (field_result.py:700-800, ordinary_spectra / ordinary_state): on the lit (top) face the
-    incident wave and the reflected orders, on the far face nothing and the transmitted orders.
-    Every order's s and p waves take the Cartesian basis ``e_s = (-s, c, 0)``,
-    ``e_p = (-kz c, -kz s, d rho) / n``, ``H = k x e`` (k = (kx, ky, d kz), d = -1 down, +1 up,
-    rho = kx c + ky s) of the half-space it lives in; the coefficients are the Fresnel amplitude
-    ratios about the cell centre (the reflected p one with the opposite sign to that basis)."""
-    N = pv['kx'].shape[0]
-    dev = pv['kx'].device
+def order_waves(kx, ky, c, s, kzt, kzb, n_top, n_bot, ratios, pol):
+    """Per order, the incoming wave and the reflected and transmitted ones, six components each
+    ``(E, k x E)`` (field_result.py:700-800, ordinary_spectra): every order's s and p waves in the
+    Cartesian basis ``e_s = (-s, c, 0)``, ``e_p = (-kz c, -kz s, d rho) / n``, ``H = k x e``
+    (``k = (kx, ky, d kz)``, ``d = -1`` down, ``+1`` up, ``rho = kx c + ky s``) of the half-space it
+    lives in, weighted by the Fresnel ratios ``(r_s, r_p, t_s, t_p)`` about the cell centre (the
+    reflected p one with the opposite sign to that basis). Every argument but the two indices
+    and ``pol`` may carry leading batch axes; returns three ``(..., N, 6)`` tensors."""
     C = torch.complex128
-    gx, gy = pv['kx'].to(C), pv['ky'].to(C)
-    c, s = pv['c'].to(C), pv['s'].to(C)
-    n_top, n_bot = complex(pv['nt']), complex(pv['nb'])
-    sign = torch.where(odd, -1.0, 1.0).to(C)
-    r_s = cref[:N, 0] * sign
-    r_p = (-cref[N:, 0]) / (-1j * n_top) * sign
-    t_s = ctrn[:N, 0] * sign
-    t_p = ctrn[N:, 0] / (-1j * n_bot) * sign
+    gx, gy, c, s = (t.to(C) for t in (kx, ky, c, s))
     zero = torch.zeros_like(gx)
     rho = gx * c + gy * s
 
@@ -139,14 +130,75 @@ def boundary_spectra(pv, cref, ctrn, pol, odd):
         k = torch.stack([gx, gy, d * kz], -1)
         return (torch.cat([es, torch.linalg.cross(k, es)], -1), torch.cat([ep, torch.linalg.cross(k, ep)], -1))
 
-    inc_s, inc_p = basis(n_top, pv['kzt'], -1.0)
-    ref_s, ref_p = basis(n_top, pv['kzt'], 1.0)
-    trn_s, trn_p = basis(n_bot, pv['kzb'], -1.0)
-    delta = torch.zeros(N, dtype=C, device=dev)
+    inc_s, inc_p = basis(complex(n_top), kzt, -1.0)
+    ref_s, ref_p = basis(complex(n_top), kzt, 1.0)
+    trn_s, trn_p = basis(complex(n_bot), kzb, -1.0)
+    r_s, r_p, t_s, t_p = ratios
+    N = gx.shape[-1]
+    delta = torch.zeros(N, dtype=C, device=gx.device)
     delta[N // 2] = 1.0
     incoming = delta[:, None] * (complex(pol[0]) * inc_s + complex(pol[1]) * inc_p)
-    reflected = r_s[:, None] * ref_s - r_p[:, None] * ref_p
-    transmitted = t_s[:, None] * trn_s + t_p[:, None] * trn_p
+    reflected = r_s[..., None] * ref_s - r_p[..., None] * ref_p
+    transmitted = t_s[..., None] * trn_s + t_p[..., None] * trn_p
+    return incoming, reflected, transmitted
+
+
+def order_table(wavelengths, thetas, phi, period, eps_top, eps_bot, hu, hv, device):
+    """Every retained order's normalised in-plane wavevector ``(kx, ky)``, its s/p frame angle
+    ``(c, s) = (cos, sin)`` and its normal component ``kz`` in the superstrate and the substrate,
+    each ``(B, N)`` over ``B`` solves: what the ports kernel forms per solve
+    (conventions.py:1118-1147, solve_2d.py:76-98), for all solves at once."""
+    import math
+    C = torch.complex128
+    wl = torch.as_tensor(np.asarray(wavelengths, dtype=np.float64), device=device)[:, None]
+    th = torch.as_tensor(np.asarray(thetas, dtype=np.float64), device=device)[:, None]
+    nu = 2 * hu + 1
+    N = nu * (2 * hv + 1)
+    index = math.sqrt(float(np.real(eps_top)))
+    kix = index * torch.sin(th) * math.cos(phi)
+    kiy = index * torch.sin(th) * math.sin(phi)
+    u = (torch.arange(N, device=device) % nu - hu).double()
+    v = (torch.arange(N, device=device) // nu - hv).double()
+    kx = kix + u * (wl / period[0])
+    ky = kiy + v * (wl / period[1])
+    one = torch.ones_like(kx)
+    spec = math.atan(math.sin(phi) / math.cos(phi)) + (math.pi if math.cos(phi) < 0 else 0.0)
+    vphi = torch.where(kx == 0,
+                       torch.where(ky == 0, spec * one, torch.where(ky < 0, -math.pi / 2 * one, math.pi / 2 * one)
+                                   - kx / torch.where(ky == 0, one, ky)),
+                       torch.atan(ky / torch.where(kx == 0, one, kx)) + math.pi * (kx < 0).double())
+    kpar = (kx * kx + ky * ky).to(C)
+
+    def kz(eps):
+        z = torch.sqrt(complex(eps) - kpar)
+        return torch.where((z.real + z.imag) < 0, -z, z)
+    return kx, ky, torch.cos(vphi), torch.sin(vphi), kz(eps_top), kz(eps_bot)
+
+
+def wave_power(waves, sign, area, amplitude):
+    """The time-averaged power of each wave through a face of ``area`` (m^2), counted along
+    ``sign`` times +z: ``sign/2 Re(E_x conj(Z0 H_y) - E_y conj(Z0 H_x)) / Z0 * area * |amplitude|^2``
+    (results.py:279-282)."""
+    return (sign * 0.5 / Z0 * (waves[..., 0] * waves[..., 4].conj() - waves[..., 1] * waves[..., 3].conj()).real
+            * area * abs(amplitude) ** 2)
+
+
+def boundary_spectra(pv, cref, ctrn, pol, odd):
+    """Each face's (incoming, outgoing) six-component spectra of the incident column, (N, 6) per
+    order (field_result.py:700-800, ordinary_spectra / ordinary_state): on the lit (top) face the
+    incident wave and the reflected orders, on the far face nothing and the transmitted orders.
+    Every order's s and p waves take the Cartesian basis ``e_s = (-s, c, 0)``,
+    ``e_p = (-kz c, -kz s, d rho) / n``, ``H = k x e`` (k = (kx, ky, d kz), d = -1 down, +1 up,
+    rho = kx c + ky s) of the half-space it lives in; the coefficients are the Fresnel amplitude
+    ratios about the cell centre (the reflected p one with the opposite sign to that basis)."""
+    N = pv['kx'].shape[0]
+    C = torch.complex128
+    n_top, n_bot = complex(pv['nt']), complex(pv['nb'])
+    sign = torch.where(odd, -1.0, 1.0).to(C)
+    ratios = (cref[:N, 0] * sign, (-cref[N:, 0]) / (-1j * n_top) * sign,
+              ctrn[:N, 0] * sign, ctrn[N:, 0] / (-1j * n_bot) * sign)
+    incoming, reflected, transmitted = order_waves(pv['kx'], pv['ky'], pv['c'], pv['s'], pv['kzt'], pv['kzb'],
+                                                   n_top, n_bot, ratios, pol)
     return {'top': (incoming, reflected), 'bottom': (torch.zeros_like(transmitted), transmitted)}
 
 

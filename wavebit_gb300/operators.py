@@ -133,7 +133,7 @@ def solve(problem, operators):
             stacks.append(engine.ConvStack.from_matrices(*slots, hu, hv))
         layer_index[w] = which[key] * L + np.arange(L)
     conv = stacks[0] if len(stacks) == 1 else engine.ConvStack(torch.cat([c.buf for c in stacks]), hu, hv)
-    res = prepared._solve(r, conv, layer_index, scattering=_rcwa._wants_scattering(problem),
+    res = prepared._solve(r, conv, layer_index, amplitudes=True, scattering=_rcwa._wants_scattering(problem),
                           fields=_rcwa._wants_fields(problem))
     res.diagnostics['explicit_operators'] = True
     return res

@@ -79,9 +79,23 @@ _AUTO_DETUNE_REL = 1e-12
 # ------------------------------------------------------------- declarations (mirror)
 
 
+#: metres in one length unit (units.py:10)
+_LENGTH_METRES = {'m': 1.0, 'mm': 1e-3, 'um': 1e-6, 'nm': 1e-9}
+
+
 @dataclass(frozen=True)
 class Units:
+    """The length unit of every length in the problem (units.py:10-26): ``'m'``, ``'mm'``,
+    ``'um'`` or ``'nm'``."""
     length: str = 'm'
+
+    def __post_init__(self):
+        if not isinstance(self.length, str) or self.length not in _LENGTH_METRES:
+            raise ValidationError("length must be 'm', 'mm', 'um', or 'nm'", code='units.length', path='units.length')
+
+    @property
+    def length_unit_meters(self):
+        return _LENGTH_METRES[self.length]
 
 
 @dataclass(frozen=True)
@@ -292,6 +306,9 @@ def _integrated(numerics):
 
 def _resolve(problem, numerics):
     """Problem -> flat arrays in kernel order (entry layer first)."""
+    length = getattr(getattr(problem, 'units', None), 'length', 'm')
+    if not isinstance(length, str) or length not in _LENGTH_METRES:
+        raise ValidationError("length must be 'm', 'mm', 'um', or 'nm'", code='units.length', path='units.length')
     stack = problem.stack
     if getattr(stack, 'lattice', None) is not None:
         raise UnsupportedFeatureError('oblique lattices are outside the GB300 raster path',
@@ -374,7 +391,7 @@ def _resolve(problem, numerics):
     orders = _numerics_orders(_numerics_or_default(numerics))
     return dict(rasters=rasters, thickness=np.array(thick), period=period, eps_top=eps_top,
                 eps_bot=eps_bot, wavelengths=wl, theta=theta, phi=phi, pol=(a_s, a_p), orders=orders,
-                amplitude=amplitude, bare_interface=bare)
+                amplitude=amplitude, bare_interface=bare, length=length)
 
 
 def _numerics_or_default(numerics):
@@ -438,31 +455,125 @@ def _check(problem, numerics, backend, device, precision):
     return CheckReport(issues=(), estimates=est, resolved=resolved)
 
 
+def _incident_scaled(ratio, reference):
+    field_ = (reference or {}).get('incident_field')
+    return None if ratio is None or field_ is None else ratio * field_
+
+
+class DiffractionOrder(NamedTuple):
+    """One order of :class:`DiffractionOrders` (contracts.py:149-175): each array with the
+    wavelength axis only (``k_parallel`` and ``amplitude_ratio_xyz`` with their trailing axis)."""
+    wavelengths: tuple
+    order_u: int
+    order_v: int
+    efficiency: object = None
+    amplitude_ratio_s: object = None
+    amplitude_ratio_p: object = None
+    power: object = None
+    amplitude_ratio_xyz: object = None
+    k_parallel: object = None
+    k_normal: object = None
+    reference: dict = None
+    metadata: dict = None
+
+    field_s = property(lambda self: _incident_scaled(self.amplitude_ratio_s, self.reference))
+    field_p = property(lambda self: _incident_scaled(self.amplitude_ratio_p, self.reference))
+    field_xyz = property(lambda self: _incident_scaled(self.amplitude_ratio_xyz, self.reference))
+
+
 class DiffractionOrders(NamedTuple):
-    """One port's diffraction orders (results.py:373-392 of the reference): the efficiency of
-    every order ``(wavelength, order_v, order_u)`` and, when the run kept amplitudes, the Fresnel
-    amplitude ratios of its s and p waves referenced at the cell centre."""
+    """One port's diffraction orders (results.py:373-392, contracts.py:288-345 of the reference),
+    arrays ``(wavelength, order_v, order_u)``: ``efficiency``; the Fresnel amplitude ratios of each
+    order's s and p waves and of its Cartesian E (``amplitude_ratio_xyz``, trailing xyz axis),
+    referenced at the port's plane and the cell centre; ``power``, each order's outgoing power
+    in W; ``k_parallel`` (trailing (kx, ky) axis) and ``k_normal``, the order's wavevector in
+    rad per length unit, ``k_normal`` signed along z (negative for a wave leaving through the
+    bottom). ``reference`` names the port, its plane, medium, cell measure and the incident
+    normalisation with their units; ``metadata`` the run's flags. The amplitude-derived arrays
+    are None when the run did not keep amplitudes."""
     wavelengths: tuple
     orders_u: object
     orders_v: object
     efficiency: object
     amplitude_ratio_s: object = None
     amplitude_ratio_p: object = None
+    power: object = None
+    amplitude_ratio_xyz: object = None
+    k_parallel: object = None
+    k_normal: object = None
+    reference: dict = None
+    metadata: dict = None
+
+    field_s = property(lambda self: _incident_scaled(self.amplitude_ratio_s, self.reference))
+    field_p = property(lambda self: _incident_scaled(self.amplitude_ratio_p, self.reference))
+    field_xyz = property(lambda self: _incident_scaled(self.amplitude_ratio_xyz, self.reference))
+
+    def order(self, m, n=0):
+        """Order ``(m, n)`` as one :class:`DiffractionOrder` (contracts.py:259-267); KeyError when
+        the order is not retained."""
+        labels_u, labels_v = [int(v) for v in self.orders_u], [int(v) for v in self.orders_v]
+        if int(m) not in labels_u or int(n) not in labels_v:
+            raise KeyError((m, n))
+        i, j = labels_u.index(int(m)), labels_v.index(int(n))
+        pick = lambda a: None if a is None else a[:, j, i]
+        return DiffractionOrder(self.wavelengths, int(m), int(n), pick(self.efficiency), pick(self.amplitude_ratio_s),
+                                pick(self.amplitude_ratio_p), pick(self.power), pick(self.amplitude_ratio_xyz),
+                                pick(self.k_parallel), pick(self.k_normal), self.reference, self.metadata)
 
 
-def _diffraction_orders(R, T, amplitudes, wavelengths, hu, hv):
+def _diffraction_orders(R, T, amplitudes, wavelengths, hu, hv, ports=None):
     """``outputs['reflected']`` and ``outputs['transmitted']`` of the given polarization. The
     kernels' amplitudes (B, 3, 4, N: column, (r_s, r_p, t_s, t_p), order) are about the cell
-    corner; order (m, n) about the centre is ``(-1)^(m+n)`` times it."""
+    corner; order (m, n) about the centre is ``(-1)^(m+n)`` times it. ``ports`` (the solves'
+    effective wavelengths and angles, the media, the cell, the source and the length unit) adds
+    the wavevectors, the Cartesian ratios and the powers (results.py:292-420)."""
+    from . import fields as F
     ou, ov = np.arange(-hu, hu + 1), np.arange(-hv, hv + 1)
+    nu, nv = 2 * hu + 1, 2 * hv + 1
     ratios = [None] * 4
     if amplitudes is not None:
         m = ou[None, :] + ov[:, None]
         sign = torch.as_tensor(np.where(m % 2 == 0, 1.0, -1.0), dtype=torch.complex128, device=amplitudes.device)
         B = amplitudes.shape[0]
-        ratios = [amplitudes[:, 0, k].reshape(B, 2 * hv + 1, 2 * hu + 1) * sign for k in range(4)]
-    return (DiffractionOrders(wavelengths, ou, ov, R, ratios[0], ratios[1]),
-            DiffractionOrders(wavelengths, ou, ov, T, ratios[2], ratios[3]))
+        ratios = [amplitudes[:, 0, k].reshape(B, nv, nu) * sign for k in range(4)]
+    if ports is None:
+        return (DiffractionOrders(wavelengths, ou, ov, R, ratios[0], ratios[1]),
+                DiffractionOrders(wavelengths, ou, ov, T, ratios[2], ratios[3]))
+    p = ports
+    dev = R.device
+    wl = np.asarray(p['wavelengths'], dtype=np.float64)
+    B = wl.shape[0]
+    kx, ky, c, s, kzt, kzb = F.order_table(wl, p['thetas'], p['phi'], p['period'], p['eps_top'], p['eps_bot'],
+                                           hu, hv, dev)
+    k0 = torch.as_tensor(2 * math.pi / wl, device=dev)[:, None]
+    k_par = (torch.stack([kx, ky], -1) * k0[..., None]).to(torch.complex128).reshape(B, nv, nu, 2)
+    area = abs(p['period'][0] * p['period'][1]) * _LENGTH_METRES[p['length']] ** 2
+    amp = complex(p['amplitude'])
+    xyz, power, incident = [None, None], [None, None], None
+    if amplitudes is not None:
+        flat = [r.reshape(B, -1) for r in ratios]
+        n_top, n_bot = np.sqrt(complex(p['eps_top'])), np.sqrt(complex(p['eps_bot']))
+        inc, refl, trn = F.order_waves(kx, ky, c, s, kzt, kzb, n_top, n_bot, flat, p['pol'])
+        xyz = [w[..., :3].reshape(B, nv, nu, 3) for w in (refl, trn)]
+        power = [F.wave_power(w, sg, area, amp).reshape(B, nv, nu) for w, sg in ((refl, 1.0), (trn, -1.0))]
+        incident = F.wave_power(inc, -1.0, area, amp).sum(-1)
+    defined = torch.ones(B, dtype=torch.bool, device=dev)
+    metadata = {'power_defined': defined, 'efficiency_defined': defined, 'propagation': 'continuum',
+                'polarization_frame': "each order's outgoing s/p frame", 'time_convention': 'exp(-i*omega*t)'}
+    out = []
+    for k, (wave, port, kz, sign, eps, plane) in enumerate((
+            ('reflected', 'top', kzt, 1.0, p['eps_top'], float(p['top_plane'])),
+            ('transmitted', 'bottom', kzb, -1.0, p['eps_bot'], 0.0))):
+        reference = {'port': port, 'wave': wave, 'plane': (plane,) * B, 'length_units': p['length'],
+                     'lateral_origin': (0.0, 0.0), 'outward_normal': (0.0, 0.0, sign), 'incident_port': 'top',
+                     'incident_field': amp, 'incident_field_units': 'V/m', 'incident_power': incident,
+                     'incident_power_units': 'W', 'cell_measure': (area,) * B, 'cell_measure_units': 'm^2',
+                     'invariant_axes': (), 'epsilon': (complex(eps),) * B, 'mu': (1.0,) * B,
+                     'amplitude_ratio_units': '1', 'power_units': 'W', 'wavevector_units': 'rad/' + p['length']}
+        out.append(DiffractionOrders(tuple(float(v) for v in wl), ou, ov, R if k == 0 else T, ratios[2 * k],
+                                     ratios[2 * k + 1], power[k], xyz[k], k_par,
+                                     (sign * k0 * kz).reshape(B, nv, nu), reference, metadata))
+    return tuple(out)
 
 
 class Result:
@@ -473,14 +584,14 @@ class Result:
     (``'incident'``, ``'s_inc'``, ``'p_inc'``)."""
 
     def __init__(self, R, T, R_sp, T_sp, status, wavelengths, diagnostics, amplitudes=None, scattering=None,
-                 field_states=None, field_geometry=None, orders=None):
+                 field_states=None, field_geometry=None, orders=None, ports=None):
         self.R, self.T = R, T
         self.outputs = {'incident': {'R': R, 'T': T},
                         's_inc': {'R': R_sp[0], 'T': T_sp[0]},
                         'p_inc': {'R': R_sp[1], 'T': T_sp[1]}}
         if orders is not None:
             self.outputs['reflected'], self.outputs['transmitted'] = _diffraction_orders(
-                R, T, amplitudes, wavelengths, *orders)
+                R, T, amplitudes, wavelengths, *orders, ports=ports)
         if torch.is_tensor(R) and torch.is_tensor(T):
             # real in-plane wavevectors and a lossless superstrate: the net flux into the stack is
             # the incident one less the reflected orders' (results.py:375-380)
@@ -574,6 +685,16 @@ class Result:
     def absorption(self):
         return 1.0 - self.R.sum(dim=(-2, -1)) - self.T.sum(dim=(-2, -1))
 
+    @property
+    def reflection(self):
+        """``outputs['reflected']`` (results.py:128-130)."""
+        return self.outputs['reflected']
+
+    @property
+    def transmission(self):
+        """``outputs['transmitted']`` (results.py:132-134)."""
+        return self.outputs['transmitted']
+
 
 class Prepared:
     """Stage A done once and kept on the device (_lifecycle.py:698-733 ``Prepared.run``)."""
@@ -617,7 +738,11 @@ class Prepared:
                                            'counts, raster shapes, outputs and spectral shape are structural).',
                                            code='prepared.structure', path=path)
 
-    def run(self, problem=None, *, amplitudes=False):
+    def run(self, problem=None, *, amplitudes=True):
+        """Solve ``problem`` (or the prepared one) on the kept convolution matrices
+        (_lifecycle.py:698-733). ``amplitudes`` keeps the kernels' Fresnel amplitudes, which the
+        amplitude ratios, Cartesian ratios and per-order powers of ``outputs['reflected']`` and
+        ``outputs['transmitted']`` read; the reference always answers them (``answers='amplitude'``)."""
         r = self.resolved if problem is None else _resolve(problem, self.numerics)
         if problem is not None:
             self._check_layout(problem, r)
@@ -685,7 +810,8 @@ class Prepared:
         return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]), status, tuple(r['wavelengths']),
                       diag, out[3] if amplitudes else None, S, states,
                       (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0),
-                       r.get('bare_interface', False), tuple(r['orders'])), orders=r['orders'])
+                       r.get('bare_interface', False), tuple(r['orders'])), orders=r['orders'],
+                      ports=_ports_context(r, wl, th))
 
     def _solve_etm(self, r, conv, layer_index, fields=False):
         """``Numerics(algorithm='etm')``: the ETM recursion over the FP64 modes of every
@@ -697,13 +823,13 @@ class Prepared:
         n = 2 * engine.n_orders(hu, hv)
         wl = np.asarray(r['wavelengths'], dtype=np.float64).copy()
         th = np.full(B, float(r['theta']))
-        Rs, Ts = [None] * B, [None] * B
+        Rs, Ts, As = [None] * B, [None] * B, [None] * B
         for idx, pvs, q, W, V in self._mode_chunks(r, conv, layer_index, wl, th, (2 * L + 4) * n * n * 16):
             for i, b in enumerate(idx):
                 modes = [(W[i * L + l], V[i * L + l], q[i * L + l]) for l in range(L)]
-                Rs[b], Ts[b] = etm_solve(modes, r['thickness'], 2 * math.pi / float(wl[b]), pvs[i], r['pol'],
-                                         2 * hu + 1, 2 * hv + 1)
-        R, T = torch.stack(Rs), torch.stack(Ts)
+                Rs[b], Ts[b], As[b] = etm_solve(modes, r['thickness'], 2 * math.pi / float(wl[b]), pvs[i],
+                                                r['pol'], 2 * hu + 1, 2 * hv + 1, amplitudes=True)
+        R, T, amps = torch.stack(Rs), torch.stack(Ts), torch.stack(As)
         if not (bool(torch.isfinite(R).all()) and bool(torch.isfinite(T).all())):
             raise NumericalError('the ETM solve produced non-finite results', code='rcwa.nonfinite')
         st = np.zeros(B, dtype=np.int32)
@@ -711,9 +837,10 @@ class Prepared:
                 'grazing': (False,) * B, 'status': st, 'precision': 'double', 'fallback_solves': (), 'detuned': {}}
         states = self._field_states(r, conv, layer_index, wl, th) if fields else None
         return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]),
-                      torch.as_tensor(st, device=R.device), tuple(r['wavelengths']), diag, None, None, states,
+                      torch.as_tensor(st, device=R.device), tuple(r['wavelengths']), diag, amps, None, states,
                       (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0),
-                       r.get('bare_interface', False), tuple(r['orders'])), orders=r['orders'])
+                       r.get('bare_interface', False), tuple(r['orders'])), orders=r['orders'],
+                      ports=_ports_context(r, wl, th))
 
     def _mode_chunks(self, r, conv, layer_index, wl, th, per_wl_bytes, budget=2 << 30):
         """FP64 modes of every (wavelength, layer) pair (wb_layer_modes), a chunk of wavelengths
@@ -821,6 +948,15 @@ class Prepared:
         return {i: tuple(v) for i, v in moved.items()}
 
 
+def _ports_context(r, wl, th):
+    """What the diffraction-order readings need beside R, T and the amplitudes: the solves'
+    effective wavelengths and angles, the media, the cell, the source and the length unit."""
+    return dict(wavelengths=np.asarray(wl, dtype=np.float64), thetas=np.asarray(th, dtype=np.float64),
+                phi=float(r['phi']), period=tuple(r['period']), eps_top=r['eps_top'], eps_bot=r['eps_bot'],
+                pol=r['pol'], amplitude=r.get('amplitude', 1.0), length=r.get('length', 'm'),
+                top_plane=float(np.sum(r['thickness'])))
+
+
 def _same_rasters(a, b):
     return len(a) == len(b) and all(x.shape == y.shape and np.array_equal(x, y) for x, y in zip(a, b))
 
@@ -904,7 +1040,7 @@ def sample_structure(problem, *, layer=0, samples=512, wavelength_index=0, quant
     return eps.reshape(1, 1) if eps.ndim == 0 else eps.reshape(1, -1) if eps.ndim == 1 else eps
 
 
-def run(problem, *, numerics=None, backend='gb300', device='cuda', precision='double', amplitudes=False):
+def run(problem, *, numerics=None, backend='gb300', device='cuda', precision='double', amplitudes=True):
     """``prepare(...).run()`` (_lifecycle.py:801-803)."""
     return prepare(problem, numerics=numerics, backend=backend, device=device,
                    precision=precision).run(amplitudes=amplitudes)
