@@ -118,6 +118,9 @@ def test_lifecycle_etm_on_the_cpu(name, monkeypatch):
     refl, trans = res.reflection, res.transmission
     p_inc = float(refl.reference['incident_power'][0])
     assert refl.reference['length_units'] == 'nm' and refl.k_normal.shape == refl.efficiency.shape
+    assert res.provenance['solver'] == 'rcwa' and res.provenance['length_units'] == 'nm'
+    assert res.provenance['requested_wavelengths'] == res.wavelengths
+    assert res.diagnostics['effective_theta'] == (float(c['theta']),) and bool(res.diagnostics['efficiency_defined'].all())
     assert float(refl.power.sum()) == pytest.approx(float(res.R.sum()) * p_inc, rel=1e-10)
     assert float(trans.power.sum()) == pytest.approx(float(res.T.sum()) * p_inc, rel=1e-10)
 

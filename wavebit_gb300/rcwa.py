@@ -584,7 +584,7 @@ class Result:
     (``'incident'``, ``'s_inc'``, ``'p_inc'``)."""
 
     def __init__(self, R, T, R_sp, T_sp, status, wavelengths, diagnostics, amplitudes=None, scattering=None,
-                 field_states=None, field_geometry=None, orders=None, ports=None):
+                 field_states=None, field_geometry=None, orders=None, ports=None, provenance=None):
         self.R, self.T = R, T
         self.outputs = {'incident': {'R': R, 'T': T},
                         's_inc': {'R': R_sp[0], 'T': T_sp[0]},
@@ -607,6 +607,7 @@ class Result:
         self.status = status
         self.wavelengths = wavelengths
         self.diagnostics = diagnostics
+        self.provenance = dict(provenance or {})
         self.amplitudes = amplitudes
         self._scattering = scattering
         self._field_states = field_states
@@ -802,16 +803,18 @@ class Prepared:
         if np.any(bad & (_lib.WB_ST_NONFINITE | _lib.WB_ST_NOCONV)):
             raise NumericalError('the solve produced non-finite results', code='rcwa.nonfinite')
         diag = {'solve_path': ('2d',) * B, 'effective_wavelengths': tuple(float(v) for v in wl),
+                'effective_theta': tuple(float(v) for v in th),
                 'grazing': tuple(bool(s & _lib.WB_ST_GRAZING) for s in st),
                 'status': st, 'precision': self.precision,
-                'fallback_solves': tuple(int(i) for i in fallback), 'detuned': moved}
+                'fallback_solves': tuple(int(i) for i in fallback), 'detuned': moved,
+                **_defined_flags(B, R.device, self.numerics)}
         S = self._scattering(r, conv, np.asarray(layer_index), wl, th) if scattering else None
         states = self._field_states(r, conv, np.asarray(layer_index), wl, th) if fields else None
-        return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]), status, tuple(r['wavelengths']),
+        return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]), status, tuple(float(v) for v in wl),
                       diag, out[3] if amplitudes else None, S, states,
                       (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0),
                        r.get('bare_interface', False), tuple(r['orders'])), orders=r['orders'],
-                      ports=_ports_context(r, wl, th))
+                      ports=_ports_context(r, wl, th), provenance=_provenance(r, self.numerics, self.precision))
 
     def _solve_etm(self, r, conv, layer_index, fields=False):
         """``Numerics(algorithm='etm')``: the ETM recursion over the FP64 modes of every
@@ -834,13 +837,15 @@ class Prepared:
             raise NumericalError('the ETM solve produced non-finite results', code='rcwa.nonfinite')
         st = np.zeros(B, dtype=np.int32)
         diag = {'solve_path': ('2d',) * B, 'algorithm': 'etm', 'effective_wavelengths': tuple(float(v) for v in wl),
-                'grazing': (False,) * B, 'status': st, 'precision': 'double', 'fallback_solves': (), 'detuned': {}}
+                'effective_theta': tuple(float(v) for v in th),
+                'grazing': (False,) * B, 'status': st, 'precision': 'double', 'fallback_solves': (), 'detuned': {},
+                **_defined_flags(B, R.device, self.numerics)}
         states = self._field_states(r, conv, layer_index, wl, th) if fields else None
         return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]),
-                      torch.as_tensor(st, device=R.device), tuple(r['wavelengths']), diag, amps, None, states,
+                      torch.as_tensor(st, device=R.device), tuple(float(v) for v in wl), diag, amps, None, states,
                       (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0),
                        r.get('bare_interface', False), tuple(r['orders'])), orders=r['orders'],
-                      ports=_ports_context(r, wl, th))
+                      ports=_ports_context(r, wl, th), provenance=_provenance(r, self.numerics, 'double'))
 
     def _mode_chunks(self, r, conv, layer_index, wl, th, per_wl_bytes, budget=2 << 30):
         """FP64 modes of every (wavelength, layer) pair (wb_layer_modes), a chunk of wavelengths
@@ -946,6 +951,30 @@ class Prepared:
                           'The results keep those values (Result.diagnostics["effective_wavelengths"]).',
                           AutoDetuneWarning, stacklevel=4)
         return {i: tuple(v) for i, v in moved.items()}
+
+
+def _defined_flags(B, device, numerics):
+    """The diagnostics' power and efficiency flags (results.py:474-478): on this path (real
+    in-plane wavevectors from a lossless superstrate) every solve has both."""
+    ones = torch.ones(B, dtype=torch.bool, device=device)
+    return {'port_power_defined': ones, 'efficiency_defined': ones,
+            'detuning_relative_step': getattr(_numerics_or_default(numerics), 'detuning', None),
+            'half_space_merge': None}
+
+
+def _provenance(r, numerics, precision):
+    """What produced a result (results.py:479-484): solver, versions, units, numerics, frames."""
+    from . import __version__
+    try:
+        library = int(_lib.load().wb_version())
+    except ImportError:               # no library: nothing ran on the device, only the version is unknown
+        library = None
+    return {'solver': 'rcwa', 'backend': 'gb300', 'code_version': __version__,
+            'library_version': library, 'length_units': r.get('length', 'm'),
+            'units': Units(r.get('length', 'm')), 'numerics': numerics, 'precision': precision,
+            'coordinate_frame': '+z up; bottom interface z=0; layers bottom-to-top',
+            'time_convention': 'exp(-i*omega*t)', 'source_normalization': 'electric amplitude V/m',
+            'requested_wavelengths': tuple(float(v) for v in r['wavelengths'])}
 
 
 def _ports_context(r, wl, th):
