@@ -250,3 +250,18 @@ def test_lalanne_rule_matches_the_reference_on_the_cpu(name):
         got = F.synthesize(state, owner, depth, xs, ys, float(c[f'amplitude_{pol}']), 'lalanne', per,
                            (hu, hv)).numpy()
         _check(got, c[f'field_counts_lalanne_{pol}'][0], 1e-11, (name, pol, 'counts'))
+
+
+def test_coordinate_rules_follow_the_reference():
+    """Counts are positive integers; explicit coordinates are nonempty 1-D finite real arrays
+    (a torch tensor too), and a complex value with an imaginary part is refused rather than
+    truncated (results.py:47-69)."""
+    assert np.array_equal(F.axis_points(torch.tensor([0.5, -1.0]), 2.0, 'x'), [0.5, -1.0])
+    assert np.array_equal(F.axis_points(np.array([1 + 0j, 2 + 0j]), 2.0, 'x'), [1.0, 2.0])
+    assert np.allclose(F.axis_points(3, 2.0, 'x'), [-1.0, 0.0, 1.0])
+    for bad in ([1 + 1e-3j], [[0.0, 1.0]], [], [np.nan], ['a'], 0, True):
+        with pytest.raises(ValueError):
+            F.axis_points(bad, 2.0, 'x')
+    for bad in ([[0.1, 0.2]], [0.1 + 1j]):
+        with pytest.raises(ValueError):
+            F.height_points(bad, np.array([1.0]))

@@ -356,6 +356,24 @@ def synthesize(state, owner, depth, x, y, amplitude, reconstruction='plain', per
     return complex(amplitude) * out * scale
 
 
+def explicit_coordinates(spec, name):
+    """A nonempty one-dimensional array of finite real coordinates (numbers, or a torch tensor on
+    any device), as float64 on the host; anything else is refused, a complex value with a
+    nonzero imaginary part included (results.py:47-69)."""
+    if hasattr(spec, 'detach'):
+        spec = spec.detach().cpu().numpy()
+    try:
+        arr = np.asarray(spec)
+        usable = (arr.dtype.kind in 'biufc' and arr.ndim == 1 and arr.size > 0
+                  and bool(np.all(np.isfinite(arr))) and not np.any(np.imag(arr)))
+    except (TypeError, ValueError):
+        usable = False
+    if not usable:
+        raise ValueError(f'{name} must be a positive integer count or a nonempty one-dimensional array of '
+                         'finite real coordinates')
+    return np.real(arr).astype(np.float64)
+
+
 def axis_points(spec, extent, name):
     """A count spans ``[-extent/2, extent/2]`` inclusive; explicit coordinates are taken as
     given (field_result.py:85-106)."""
@@ -363,10 +381,7 @@ def axis_points(spec, extent, name):
         if spec < 1:
             raise ValueError(f'{name} must be a positive integer count')
         return np.linspace(-0.5, 0.5, int(spec)) * extent
-    arr = np.asarray(spec, dtype=np.float64)
-    if arr.ndim != 1 or not arr.shape[0] or not np.all(np.isfinite(arr)):
-        raise ValueError(f'{name} must be a positive integer count or a nonempty 1-D array of finite coordinates')
-    return arr
+    return explicit_coordinates(spec, name)
 
 
 def height_points(spec, thickness_top_first):
@@ -383,9 +398,7 @@ def height_points(spec, thickness_top_first):
         z = np.concatenate([edges[j] + frac * ds[j] for j in range(L)])
         j = np.repeat(np.arange(L), int(spec))
         return z, L - 1 - j, ds[j] - (z - edges[j])
-    z = np.asarray(spec, dtype=np.float64).reshape(-1)
-    if z.ndim != 1 or not z.shape[0]:
-        raise ValueError('z must be a positive integer count or a nonempty 1-D array of heights')
+    z = explicit_coordinates(spec, 'z')
     owner, depth = heights(thickness_top_first, z)
     return z, owner, depth
 
