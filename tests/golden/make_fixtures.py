@@ -398,6 +398,67 @@ def make_amplitude_cases():
     print('ref_amplitudes.npz:', len(names), 'cases')
 
 
+def make_backside_cases():
+    """The reference's own run of scenes lit from below (``PlaneWave(side='bottom')``: the angles
+    in the substrate, R back into it, T into the superstrate): per-order R and T, the amplitude
+    ratios and the other per-order readings, fields at explicit points and the boundary fields,
+    s and mixed incidence with a 2.5 V/m source."""
+    from wavebit import Material, Units, rcwa
+    out = {}
+    names = []
+    scenes = [c for c in ref_cases() if c['name'] in ('grating_1d', 'crossed_1', 'crossed_4', 'symmetric_pillar')]
+    scenes += [c for c in halfspace_cases() if c['name'] in ('tir', 'dense_superstrate', 'normal_rotated')]
+    for case in scenes:
+        n = case['name']
+        names.append(n)
+        for key in ('structure', 'thickness', 'wavelength', 'period', 'orders', 'theta', 'phi',
+                    'eps_top', 'eps_bot'):
+            out[f'{n}__{key}'] = np.asarray(case[key])
+        st = case['structure'][::-1]
+        th = np.asarray(case['thickness'], dtype=float)[::-1]
+        layers = tuple(rcwa.Layer(thickness=float(t), epsilon=np.asarray(e)) for e, t in zip(st, th))
+        px, py = (float(v) for v in case['period'])
+        x = np.array([-0.31 * px, 0.0, 0.45 * px])
+        y = np.array([-0.27 * py, 0.5 * py])
+        faces = np.concatenate([[0.0], np.cumsum(th)])
+        z = np.unique(np.concatenate([faces, faces[:-1] + 0.37 * th]))
+        for tag, pol in (('s', 's'), ('mix', (0.6, 0.8j))):
+            prob = rcwa.Problem(
+                units=Units(length='nm'),
+                stack=rcwa.Stack(period=case['period'], top=Material(epsilon=case['eps_top']),
+                                 bottom=Material(epsilon=case['eps_bot']), layers=layers),
+                excitation=rcwa.Excitation(wavelength=case['wavelength'], sources=(
+                    rcwa.PlaneWave(side='bottom', polarization=pol, theta=case['theta'], phi=case['phi'],
+                                   amplitude=2.5),)),
+                outputs=rcwa.Outputs(fields=True, scattering=True))
+            res = rcwa.run(prob, numerics=rcwa.Numerics(orders=case['orders']))
+            if tag == 's':
+                # the scattering matrix is incidence-relative: S11 reflects back into the substrate
+                S = res.scattering[0]
+                for blk in ('S11', 'S12', 'S21', 'S22'):
+                    out[f'{n}__{blk}'] = np.asarray(getattr(S, blk))
+                out[f'{n}__entry_index'] = np.asarray(S.entry_port.refractive_index)
+            out[f'{n}__R_{tag}'] = np.asarray(res.R)[0]
+            out[f'{n}__T_{tag}'] = np.asarray(res.T)[0]
+            for port in ('reflected', 'transmitted'):
+                o = res.outputs[port]
+                for key in ('amplitude_ratio_s', 'amplitude_ratio_p', 'amplitude_ratio_xyz', 'power', 'k_parallel',
+                            'k_normal'):
+                    out[f'{n}__{tag}_{port}_{key}'] = np.asarray(getattr(o, key))[0]
+                out[f'{n}__{tag}_{port}_plane'] = np.asarray(o.reference['plane'])
+                out[f'{n}__{tag}_{port}_port'] = np.asarray(o.reference['port'])
+                out[f'{n}__{tag}_{port}_incident_power'] = np.asarray(o.reference['incident_power'])
+            out[f'{n}__field_{tag}'] = np.asarray(res.field(x=x, y=y, z=z).values)
+            for side in ('top', 'bottom'):
+                for part in ('incoming', 'outgoing'):
+                    b = res.boundary_fields(side=side, x=x, y=y, part=part)
+                    out[f'{n}__boundary_{side}_{part}_{tag}'] = np.asarray(b.values)
+        out[f'{n}__x'], out[f'{n}__y'], out[f'{n}__z'] = x, y, z
+    out['names'] = np.array(names)
+    np.savez_compressed(os.path.join(HERE, 'ref_backside.npz'), **out)
+    print('ref_backside.npz:', len(names), 'cases')
+
+
 def make_bare_cases():
     """Stacks with no layers: the reference solves the bare interface between its half-spaces
     (results.py:180-189) -- per-order R/T of its own run, s and p."""
@@ -458,6 +519,9 @@ def make_reticolo_cases():
         for side in ('ri', 'ti'):
             out[f'{name}__idx_{side}'] = np.asarray(gold[f'{name}__idx_{side}'])
             out[f'{name}__de_{side}'] = np.asarray(gold[f'{name}__de_{side}'])
+            # the same scene lit from below at the same in-plane wavevector (RETICOLO's inc_bottom):
+            # reflection back into the substrate, transmission into the superstrate
+            out[f'{name}__de_{side}_bot'] = np.asarray(gold[f'{name}__de_{side}_bot'])
     out['names'] = np.array(list(cases))
     np.savez_compressed(os.path.join(HERE, 'reticolo_cases.npz'), **out)
     print('reticolo_cases.npz:', len(cases), 'cases')
@@ -472,6 +536,7 @@ if __name__ == '__main__':
     make_etm_cases()
     make_halfspace_cases()
     make_bare_cases()
+    make_backside_cases()
     make_amplitude_cases()
     make_legacy_cases()
     make_reticolo_cases()

@@ -51,8 +51,9 @@ def test_polarization_pairs_are_normalised():
     (dict(bottom=rcwa.Material(2.0, mu=3.0)), rcwa.UnsupportedFeatureError, 'feature.unsupported', 'stack.bottom'),
     (dict(top=rcwa.Material(lambda wl: 2.0)), rcwa.UnsupportedFeatureError, 'feature.unsupported', 'stack.top'),
     (dict(wavelength=-5.0), rcwa.ValidationError, 'input.invalid', 'excitation.wavelength'),
-    (dict(source=rcwa.PlaneWave(side='bottom')), rcwa.UnsupportedFeatureError, 'feature.unsupported',
-     'excitation.sources[0]'),
+    (dict(source=rcwa.PlaneWave(side='left')), rcwa.ValidationError, 'source.side', 'source.side'),
+    (dict(source=rcwa.PlaneWave(side='bottom'), bottom=rcwa.Material(-5.0 + 0.2j)), rcwa.UnsupportedFeatureError,
+     'feature.unsupported', 'stack.bottom'),
     (dict(source=rcwa.PlaneWave(kx=0.1)), rcwa.UnsupportedFeatureError, 'feature.unsupported',
      'excitation.sources[0]'),
     (dict(source=rcwa.PlaneWave(theta=2.0)), rcwa.ValidationError, 'input.invalid', 'excitation.sources[0].theta'),

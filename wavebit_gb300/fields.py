@@ -67,6 +67,13 @@ class FieldSamples(NamedTuple):
     metadata: dict
 
 
+def z_mirror(device):
+    """The six components' signs under z -> -z: E is a polar vector (E_z turns), H an axial
+    one (H_x and H_y turn). A scene lit from below is solved as its mirror image lit from above,
+    and its fields are that solve's, mirrored back."""
+    return torch.as_tensor([1, 1, -1, -1, -1, 1], dtype=torch.complex128, device=device)
+
+
 def sp_rotate(W, V, c, s):
     """The s/p rotation of a layer's Cartesian modes (solve_2d.py:2584-2616), as the kernels'
     sp_rotate_kernel and :func:`wavebit_gb300.adjoint.solve_and_grad` apply it."""

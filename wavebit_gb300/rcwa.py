@@ -344,14 +344,24 @@ def _resolve(problem, numerics):
     rasters, thick = rasters[::-1], thick[::-1]
     eps_top = _scalar_eps(stack.top, 'stack.top')
     eps_bot = _scalar_eps(stack.bottom, 'stack.bottom')
+    sources = tuple(problem.excitation.sources)
+    side = getattr(sources[0], 'side', 'top') if len(sources) == 1 else 'top'
+    if side not in ('top', 'bottom'):
+        raise ValidationError("side must be 'top' or 'bottom'.", code='source.side', path='source.side')
+    if side == 'bottom':
+        # lit from below: exactly the z-mirrored scene lit from above (the reference's
+        # incidence_side contract): the public bottom-first layers are the entry face first and the
+        # half-spaces trade places; results are mapped back to the scene's frame afterwards
+        rasters, thick = rasters[::-1], thick[::-1]
+        eps_top, eps_bot = eps_bot, eps_top
     bare = not layers
     if bare:
         # the bare interface between the half-spaces, solved as the reference solves it: through
         # one zero-thickness layer of the top medium (results.py:180-189)
         rasters, thick = [np.full((1, 1), eps_top, dtype=np.complex128)], [0.0]
     if eps_top.imag != 0 or eps_top.real <= 0:
-        raise UnsupportedFeatureError('the lit superstrate must be lossless with Re(eps) > 0',
-                                      path='stack.top')
+        raise UnsupportedFeatureError('the lit half-space must be lossless with Re(eps) > 0',
+                                      path='stack.top' if side == 'top' else 'stack.bottom')
     exc = problem.excitation
     wl = np.atleast_1d(np.asarray(exc.wavelength, dtype=np.float64)).reshape(-1)
     if not (wl.size and np.all(np.isfinite(wl)) and np.all(wl > 0)):
@@ -361,8 +371,8 @@ def _resolve(problem, numerics):
         raise UnsupportedFeatureError('one PlaneWave source per problem on the GB300 path',
                                       path='excitation.sources')
     src = sources[0]
-    if getattr(src, 'side', 'top') != 'top' or getattr(src, 'kx', None) is not None or getattr(src, 'ky', None) is not None:
-        raise UnsupportedFeatureError('top-side incidence given by theta/phi only', path='excitation.sources[0]')
+    if getattr(src, 'kx', None) is not None or getattr(src, 'ky', None) is not None:
+        raise UnsupportedFeatureError('incidence given by theta/phi only', path='excitation.sources[0]')
     theta = float(np.real(0.0 if src.theta is None else src.theta))
     phi = float(np.real(0.0 if src.phi is None else src.phi))
     if not abs(theta) < math.pi / 2:
@@ -391,7 +401,7 @@ def _resolve(problem, numerics):
     orders = _numerics_orders(_numerics_or_default(numerics))
     return dict(rasters=rasters, thickness=np.array(thick), period=period, eps_top=eps_top,
                 eps_bot=eps_bot, wavelengths=wl, theta=theta, phi=phi, pol=(a_s, a_p), orders=orders,
-                amplitude=amplitude, bare_interface=bare, length=length)
+                amplitude=amplitude, bare_interface=bare, length=length, side=side)
 
 
 def _numerics_or_default(numerics):
@@ -560,12 +570,19 @@ def _diffraction_orders(R, T, amplitudes, wavelengths, hu, hv, ports=None):
     defined = torch.ones(B, dtype=torch.bool, device=dev)
     metadata = {'power_defined': defined, 'efficiency_defined': defined, 'propagation': 'continuum',
                 'polarization_frame': "each order's outgoing s/p frame", 'time_convention': 'exp(-i*omega*t)'}
+    # lit from below, the solve ran on the z-mirrored scene: its reflected wave leaves through
+    # the scene's bottom, its transmitted one through the top, and E_z changes sign
+    lit, far = ('bottom', 'top') if p.get('side', 'top') == 'bottom' else ('top', 'bottom')
+    if lit == 'bottom' and xyz[0] is not None:
+        flip = torch.as_tensor([1.0, 1.0, -1.0], dtype=torch.complex128, device=dev)
+        xyz = [a * flip for a in xyz]
+    planes, normals = {'top': float(p['top_plane']), 'bottom': 0.0}, {'top': 1.0, 'bottom': -1.0}
     out = []
-    for k, (wave, port, kz, sign, eps, plane) in enumerate((
-            ('reflected', 'top', kzt, 1.0, p['eps_top'], float(p['top_plane'])),
-            ('transmitted', 'bottom', kzb, -1.0, p['eps_bot'], 0.0))):
+    for k, (wave, port, kz, eps) in enumerate((('reflected', lit, kzt, p['eps_top']),
+                                               ('transmitted', far, kzb, p['eps_bot']))):
+        sign, plane = normals[port], planes[port]
         reference = {'port': port, 'wave': wave, 'plane': (plane,) * B, 'length_units': p['length'],
-                     'lateral_origin': (0.0, 0.0), 'outward_normal': (0.0, 0.0, sign), 'incident_port': 'top',
+                     'lateral_origin': (0.0, 0.0), 'outward_normal': (0.0, 0.0, sign), 'incident_port': lit,
                      'incident_field': amp, 'incident_field_units': 'V/m', 'incident_power': incident,
                      'incident_power_units': 'W', 'cell_measure': (area,) * B, 'cell_measure_units': 'm^2',
                      'invariant_axes': (), 'epsilon': (complex(eps),) * B, 'mu': (1.0,) * B,
@@ -636,15 +653,24 @@ class Result:
             raise ValidationError('This stack has no layers, so field() has nothing to sample: it reconstructs '
                                   'inside finite layers only, and here z = 0 is the interface between the two '
                                   'half-spaces. Add a layer to sample inside it.', code='field.coordinates', path='z')
+        lit_below = self._lit_side() == 'bottom'
         try:
             xs = F.axis_points(x, period[0], 'x')
             ys = F.axis_points(y, period[1], 'y')
-            zs, owner, depth = F.height_points(z, thickness)
+            # heights and face ownership in the scene's frame; lit from below the state is that
+            # of the z-mirrored scene, whose layer p is the scene's (L-1-p), depth measured upward
+            scene = thickness[::-1] if lit_below else thickness
+            zs, owner, depth = F.height_points(z, scene)
         except ValueError as e:
             raise ValidationError(str(e), code='field.coordinates', path='x/y/z') from e
+        if lit_below:
+            depth = np.asarray(scene, dtype=np.float64)[owner] - depth
+            owner = len(scene) - 1 - owner
         orders = self._field_geometry[4] if len(self._field_geometry) > 4 else None
         values = torch.stack([F.synthesize(st, owner, depth, xs, ys, amplitude, reconstruction, period, orders)
                               for st in self._field_states])
+        if lit_below:
+            values = values * F.z_mirror(values.device)
         return F.FieldSamples(coordinates={'x': xs, 'y': ys, 'z': zs, 'wavelength': self.wavelengths},
                               values=values, components=F.COMPONENTS, sampling='collocated Cartesian phasor',
                               metadata={'axis_order': ('wavelength', 'z', 'y', 'x', 'component'),
@@ -669,7 +695,11 @@ class Result:
             ys = F.axis_points(y, period[1], 'y')
         except ValueError as e:
             raise ValidationError(str(e), code='field.coordinates', path='x/y') from e
-        values = torch.stack([F.expand_boundary(st, side, part, xs, ys, amplitude) for st in self._field_states])
+        lit_below = self._lit_side() == 'bottom'
+        face = {'top': 'bottom', 'bottom': 'top'}[side] if lit_below else side
+        values = torch.stack([F.expand_boundary(st, face, part, xs, ys, amplitude) for st in self._field_states])
+        if lit_below:
+            values = values * F.z_mirror(values.device)
         return F.FieldSamples(coordinates={'x': xs, 'y': ys, 'wavelength': self.wavelengths}, values=values,
                               components=F.COMPONENTS, sampling='collocated boundary phasor',
                               metadata={'side': side, 'part': part, 'axis_order': ('wavelength', 'y', 'x', 'component')})
@@ -685,6 +715,10 @@ class Result:
     @property
     def absorption(self):
         return 1.0 - self.R.sum(dim=(-2, -1)) - self.T.sum(dim=(-2, -1))
+
+    def _lit_side(self):
+        g = self._field_geometry
+        return g[5] if g is not None and len(g) > 5 else 'top'
 
     @property
     def reflection(self):
@@ -813,7 +847,7 @@ class Prepared:
         return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]), status, tuple(float(v) for v in wl),
                       diag, out[3] if amplitudes else None, S, states,
                       (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0),
-                       r.get('bare_interface', False), tuple(r['orders'])), orders=r['orders'],
+                       r.get('bare_interface', False), tuple(r['orders']), r.get('side', 'top')), orders=r['orders'],
                       ports=_ports_context(r, wl, th), provenance=_provenance(r, self.numerics, self.precision))
 
     def _solve_etm(self, r, conv, layer_index, fields=False):
@@ -844,7 +878,7 @@ class Prepared:
         return Result(R[:, 0], T[:, 0], (R[:, 1], R[:, 2]), (T[:, 1], T[:, 2]),
                       torch.as_tensor(st, device=R.device), tuple(float(v) for v in wl), diag, amps, None, states,
                       (np.asarray(r['thickness'], dtype=np.float64), r['period'], r.get('amplitude', 1.0),
-                       r.get('bare_interface', False), tuple(r['orders'])), orders=r['orders'],
+                       r.get('bare_interface', False), tuple(r['orders']), r.get('side', 'top')), orders=r['orders'],
                       ports=_ports_context(r, wl, th), provenance=_provenance(r, self.numerics, 'double'))
 
     def _mode_chunks(self, r, conv, layer_index, wl, th, per_wl_bytes, budget=2 << 30):
@@ -983,7 +1017,7 @@ def _ports_context(r, wl, th):
     return dict(wavelengths=np.asarray(wl, dtype=np.float64), thetas=np.asarray(th, dtype=np.float64),
                 phi=float(r['phi']), period=tuple(r['period']), eps_top=r['eps_top'], eps_bot=r['eps_bot'],
                 pol=r['pol'], amplitude=r.get('amplitude', 1.0), length=r.get('length', 'm'),
-                top_plane=float(np.sum(r['thickness'])))
+                top_plane=float(np.sum(r['thickness'])), side=r.get('side', 'top'))
 
 
 def _same_rasters(a, b):
