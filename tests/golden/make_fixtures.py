@@ -459,6 +459,49 @@ def make_backside_cases():
     print('ref_backside.npz:', len(names), 'cases')
 
 
+def make_direct_cases():
+    """The reference's own run with the incidence given as a wavevector
+    (``PlaneWave(kx=, ky=)``, rad per length unit, fixed across two wavelengths so the angle
+    changes with the wavelength), lit from either side, and at exactly normal incidence: per-order
+    R and T and the amplitude ratios, s and mixed incidence."""
+    from wavebit import Material, Units, rcwa
+    out = {}
+    names = []
+    plans = [('crossed_1', 'top', 0.003, -0.002), ('crossed_4', 'top', -0.0041, 0.0007),
+             ('symmetric_pillar', 'top', 0.0, 0.0), ('tir', 'bottom', 0.0025, 0.001),
+             ('grating_1d', 'bottom', -0.002, 0.0)]
+    cases = {c['name']: c for c in ref_cases() + halfspace_cases()}
+    for n, side, kx, ky in plans:
+        case = cases[n]
+        names.append(n)
+        for key in ('structure', 'thickness', 'period', 'orders', 'eps_top', 'eps_bot'):
+            out[f'{n}__{key}'] = np.asarray(case[key])
+        wls = np.array([0.92, 1.07]) * float(case['wavelength'])
+        out[f'{n}__wavelengths'], out[f'{n}__kx'], out[f'{n}__ky'] = wls, np.asarray(kx), np.asarray(ky)
+        out[f'{n}__side'] = np.asarray(side)
+        st = case['structure'][::-1]
+        th = np.asarray(case['thickness'], dtype=float)[::-1]
+        layers = tuple(rcwa.Layer(thickness=float(t), epsilon=np.asarray(e)) for e, t in zip(st, th))
+        for tag, pol in (('s', 's'), ('mix', (0.6, 0.8j))):
+            prob = rcwa.Problem(
+                units=Units(length='nm'),
+                stack=rcwa.Stack(period=case['period'], top=Material(epsilon=case['eps_top']),
+                                 bottom=Material(epsilon=case['eps_bot']), layers=layers),
+                excitation=rcwa.Excitation(wavelength=wls, sources=(
+                    rcwa.PlaneWave(side=side, polarization=pol, kx=kx, ky=ky),)))
+            res = rcwa.run(prob, numerics=rcwa.Numerics(orders=case['orders']))
+            out[f'{n}__R_{tag}'] = np.asarray(res.R)
+            out[f'{n}__T_{tag}'] = np.asarray(res.T)
+            for port in ('reflected', 'transmitted'):
+                o = res.outputs[port]
+                for comp in ('s', 'p'):
+                    out[f'{n}__{tag}_{port}_{comp}'] = np.asarray(getattr(o, f'amplitude_ratio_{comp}'))
+                out[f'{n}__{tag}_{port}_k_parallel'] = np.asarray(o.k_parallel)
+    out['names'] = np.array(names)
+    np.savez_compressed(os.path.join(HERE, 'ref_direct.npz'), **out)
+    print('ref_direct.npz:', len(names), 'cases')
+
+
 def make_bare_cases():
     """Stacks with no layers: the reference solves the bare interface between its half-spaces
     (results.py:180-189) -- per-order R/T of its own run, s and p."""
@@ -537,6 +580,7 @@ if __name__ == '__main__':
     make_halfspace_cases()
     make_bare_cases()
     make_backside_cases()
+    make_direct_cases()
     make_amplitude_cases()
     make_legacy_cases()
     make_reticolo_cases()

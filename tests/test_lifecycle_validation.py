@@ -156,7 +156,8 @@ def _prepared(detuning):
     p = rcwa.Prepared.__new__(rcwa.Prepared)
     p.numerics, p.precision, p.handle = rcwa.Numerics(orders=(0, 0), detuning=detuning), 'double', None
     r = dict(wavelengths=np.array([600.0, 700.0, 800.0]), rasters=[np.ones((1, 1))], thickness=np.array([100.0]),
-             period=(500.0, 500.0), theta=0.3, phi=0.0, eps_top=1.0, eps_bot=1.0, pol=(1.0, 0.0), orders=(0, 0))
+             period=(500.0, 500.0), theta=0.3, thetas=np.full(3, 0.3), phi=0.0, eps_top=1.0, eps_bot=1.0,
+             pol=(1.0, 0.0), orders=(0, 0))
     return p, r
 
 

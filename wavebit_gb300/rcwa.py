@@ -371,14 +371,18 @@ def _resolve(problem, numerics):
         raise UnsupportedFeatureError('one PlaneWave source per problem on the GB300 path',
                                       path='excitation.sources')
     src = sources[0]
-    if getattr(src, 'kx', None) is not None or getattr(src, 'ky', None) is not None:
-        raise UnsupportedFeatureError('incidence given by theta/phi only', path='excitation.sources[0]')
-    theta = float(np.real(0.0 if src.theta is None else src.theta))
-    phi = float(np.real(0.0 if src.phi is None else src.phi))
-    if not abs(theta) < math.pi / 2:
-        raise ValidationError('theta must be a real angle below pi/2', path='excitation.sources[0].theta')
-    if not math.isfinite(phi):
-        raise ValidationError('phi must be a finite angle', path='excitation.sources[0].phi')
+    direct = getattr(src, 'kx', None) is not None or getattr(src, 'ky', None) is not None
+    if direct:
+        thetas, phi = _direct_incidence(src, wl, eps_top)
+        theta = float(thetas[0])
+    else:
+        theta = float(np.real(0.0 if src.theta is None else src.theta))
+        phi = float(np.real(0.0 if src.phi is None else src.phi))
+        if not abs(theta) < math.pi / 2:
+            raise ValidationError('theta must be a real angle below pi/2', path='excitation.sources[0].theta')
+        if not math.isfinite(phi):
+            raise ValidationError('phi must be a finite angle', path='excitation.sources[0].phi')
+        thetas = np.full(wl.shape[0], theta)
     pol = src.polarization
     if isinstance(pol, str):
         if pol not in ('s', 'p'):
@@ -400,8 +404,32 @@ def _resolve(problem, numerics):
         raise ValidationError('the source amplitude must be finite', path='excitation.sources[0].amplitude')
     orders = _numerics_orders(_numerics_or_default(numerics))
     return dict(rasters=rasters, thickness=np.array(thick), period=period, eps_top=eps_top,
-                eps_bot=eps_bot, wavelengths=wl, theta=theta, phi=phi, pol=(a_s, a_p), orders=orders,
+                eps_bot=eps_bot, wavelengths=wl, theta=theta, thetas=thetas, phi=phi, pol=(a_s, a_p), orders=orders,
                 amplitude=amplitude, bare_interface=bare, length=length, side=side)
+
+
+def _direct_incidence(src, wl, eps_inc):
+    """``PlaneWave(kx=, ky=)``: physical wavenumbers (rad per length unit), taken as given at every
+    wavelength (engine.py:2750-2758): ``k_par / k0 = (kx, ky) * wavelength / (2 pi)``. The
+    kernels take that wavevector as the polar angle in the lit medium of index ``n`` and the
+    azimuth, ``sin(theta) = |k_par| / (k0 n)`` (one angle per wavelength) and
+    ``phi = atan2(ky, kx)`` (0 at normal incidence, where the s/p frame takes ``phi = 0``, as
+    the reference's frame azimuth does for a direct wavevector)."""
+    if getattr(src, 'theta', None) is not None or getattr(src, 'phi', None) is not None:
+        raise ValidationError('Use theta/phi or kx/ky, not both.', code='source.direction_ambiguous', path='source')
+    k = []
+    for name in ('kx', 'ky'):
+        v = getattr(src, name, None)
+        v = 0.0 if v is None else complex(np.asarray(v).reshape(()))
+        if not (np.isfinite(v) and v.imag == 0):
+            raise ValidationError(f'{name} must be a finite real wavenumber', path=f'excitation.sources[0].{name}')
+        k.append(v.real)
+    kpar = math.hypot(*k) * wl / (2 * math.pi)
+    n = math.sqrt(eps_inc.real)
+    if np.any(kpar >= n):
+        raise UnsupportedFeatureError('an incident wavevector at or past the lit medium\'s light line (evanescent '
+                                      'incidence) is outside the GB300 raster path', path='excitation.sources[0]')
+    return np.arcsin(kpar / n), (math.atan2(k[1], k[0]) if k[0] or k[1] else 0.0)
 
 
 def _numerics_or_default(numerics):
@@ -806,7 +834,7 @@ class Prepared:
         detuned, wavelength and angle)."""
         B = len(r['wavelengths'])
         wl = np.asarray(r['wavelengths'], dtype=np.float64).copy()
-        th = np.full(B, float(r['theta']))
+        th = np.asarray(r['thetas'], dtype=np.float64).copy()
         out = list(self._batch(r, conv, layer_index, np.arange(B), wl, th, self.precision, amplitudes))
         R, T, status = out[:3]
 
@@ -859,7 +887,7 @@ class Prepared:
         B, L = layer_index.shape
         n = 2 * engine.n_orders(hu, hv)
         wl = np.asarray(r['wavelengths'], dtype=np.float64).copy()
-        th = np.full(B, float(r['theta']))
+        th = np.asarray(r['thetas'], dtype=np.float64).copy()
         Rs, Ts, As = [None] * B, [None] * B, [None] * B
         for idx, pvs, q, W, V in self._mode_chunks(r, conv, layer_index, wl, th, (2 * L + 4) * n * n * 16):
             for i, b in enumerate(idx):
@@ -961,7 +989,7 @@ class Prepared:
         step = float(det)
         remaining = np.nonzero(st != 0)[0]
         moved = {}
-        knobs = ['wavelength'] + (['theta'] if float(r['theta']) != 0.0 else [])
+        knobs = ['wavelength'] + (['theta'] if np.any(np.asarray(r['thetas']) != 0.0) else [])
         for knob in knobs:
             if not remaining.size:
                 break
