@@ -11,12 +11,12 @@ def pytest_configure(config):
 
 
 #: Modules collected after every other one, in their own (alphabetical) order: incidence from
-#: below and by wavevector, the ETM and field paths, which sit on top of the parity-tested stages, the amplitude ratios, the half-space
+#: below and by wavevector, the ETM and field paths, gain films, which sit on top of the parity-tested stages, the amplitude ratios, the half-space
 #: branches, the RETICOLO orders, the wavelength gradient and the serving loop's integrated
 #: coefficients, so that under ``-x`` a failure there cannot keep the stage-level parity suites
 #: from reporting; and the allocation-free entry point, whose fixed scratch is shared by the
 #: whole process, at the end.
-_LAST = ('test_backside.py', 'test_direct_incidence.py', 'test_etm.py', 'test_fields.py', 'test_gpu_amplitudes.py', 'test_gpu_halfspace.py',
+_LAST = ('test_backside.py', 'test_direct_incidence.py', 'test_etm.py', 'test_fields.py', 'test_gain_film.py', 'test_gpu_amplitudes.py', 'test_gpu_halfspace.py',
          'test_gpu_reticolo.py', 'test_gpu_wavelength_gradient.py', 'test_serving_integrated.py',
          'test_zz_no_alloc.py')
 

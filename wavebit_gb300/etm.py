@@ -12,7 +12,8 @@ From the substrate up, per layer with rotated modes ``W``, ``V`` and ``X = exp(-
 seeded with the substrate's ``F``, ``G`` and ``T = I``; one block solve of the superstrate's
 boundary equations then gives ``R_s``, ``R_p`` and ``T_1``, and ``(T_s, T_p) = T T_1``. Real
 in-plane wavevectors and passive layers, where the ETM's mode labels are ``mode_q``'s
-(conventions.py:252-300) and every layer takes the plain form of ``_run_ab``.
+(conventions.py:252-300) and every layer takes the plain form of ``_run_ab``; a finite gain
+film too, whose answer does not depend on how its modes are labelled.
 """
 import math
 
