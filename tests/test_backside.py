@@ -174,3 +174,22 @@ def test_lifecycle_from_below_on_the_gpu(name):
         want = c[blk]
         assert np.abs(getattr(S, blk).cpu().numpy() - want).max() <= 1e-10 * max(1.0, np.abs(want).max()), (name, blk)
     assert S.entry_port.refractive_index == pytest.approx(np.sqrt(complex(c['eps_bot'])), rel=1e-15)
+
+
+def test_a_preparation_takes_the_same_scene_lit_from_the_other_side():
+    """Which side the source lights is not structural: the layout a preparation fixes is read in
+    the scene's own layer order, so a stack of rasters of different shapes lit from below keeps
+    the layout of the same stack lit from above; a changed raster shape is still refused."""
+    st = (rcwa.Layer(thickness=50.0, epsilon=np.ones((2, 3)) * 2.0), rcwa.Layer(thickness=60.0, epsilon=np.ones((4, 5))))
+
+    def problem(side, layers=st):
+        return rcwa.Problem(stack=rcwa.Stack(period=(400.0, 500.0), top=rcwa.Material(1.0),
+                                             bottom=rcwa.Material(2.25), layers=layers),
+                            excitation=rcwa.Excitation(wavelength=600.0, sources=(
+                                rcwa.PlaneWave(side=side, theta=0.2),)))
+    num = rcwa.Numerics(orders=(1, 1))
+    top, bottom = problem('top'), problem('bottom')
+    layout = rcwa.Prepared._layout
+    assert layout(top, rcwa._resolve(top, num)) == layout(bottom, rcwa._resolve(bottom, num))
+    other = problem('bottom', (st[0], rcwa.Layer(thickness=60.0, epsilon=np.ones((4, 4)))))
+    assert layout(other, rcwa._resolve(other, num)) != layout(top, rcwa._resolve(top, num))

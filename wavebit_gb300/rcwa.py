@@ -777,8 +777,10 @@ class Prepared:
     def _layout(problem, r):
         """What a preparation fixes (_adapt.py:633-640 of the reference): the layer count and
         raster shapes, the number of wavelengths and sources, and the requested outputs; the
-        values in them stay live."""
-        return ((len(r['rasters']), tuple(e.shape for e in r['rasters'])),
+        values in them stay live. Shapes are read in the scene's own layer order, whichever side
+        the source lights."""
+        rasters = r['rasters'][::-1] if r.get('side', 'top') == 'bottom' else r['rasters']
+        return ((len(rasters), tuple(e.shape for e in rasters)),
                 (len(r['wavelengths']), len(tuple(problem.excitation.sources))),
                 (_wants_fields(problem), _wants_scattering(problem)))
 
