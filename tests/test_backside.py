@@ -193,3 +193,34 @@ def test_a_preparation_takes_the_same_scene_lit_from_the_other_side():
     assert layout(top, rcwa._resolve(top, num)) == layout(bottom, rcwa._resolve(bottom, num))
     other = problem('bottom', (st[0], rcwa.Layer(thickness=60.0, epsilon=np.ones((4, 4)))))
     assert layout(other, rcwa._resolve(other, num)) != layout(top, rcwa._resolve(top, num))
+
+
+def test_the_operator_contract_is_the_scene_not_the_lit_side():
+    from wavebit_gb300 import operators
+    c = _case('crossed_1')
+    top = _problem(c, 's', fields=False)
+    bottom = rcwa.Problem(units=top.units, stack=top.stack, excitation=rcwa.Excitation(
+        wavelength=top.excitation.wavelength, sources=(rcwa.PlaneWave(side='top', theta=0.1),)))
+    num = rcwa.Numerics(orders=(1, 1))
+    assert operators._contract(top, num) == operators._contract(bottom, num)
+
+
+@pytest.mark.gpu
+def test_operators_keep_the_scenes_layer_order_from_below():
+    """rcwa.operators.assemble lists the layers top first whichever side is lit, and solve with
+    those operators is rcwa.run of the bottom-lit problem."""
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from wavebit_gb300 import operators
+    c = _case('crossed_4')
+    hu, hv = (int(v) for v in c['orders'])
+    num = rcwa.Numerics(orders=(hu, hv))
+    lit_below = _problem(c, 's', fields=False)
+    lit_above = rcwa.Problem(units=lit_below.units, stack=lit_below.stack, excitation=rcwa.Excitation(
+        wavelength=lit_below.excitation.wavelength, sources=(rcwa.PlaneWave(side='top', theta=0.1),)))
+    ops_b, ops_t = operators.assemble(lit_below, numerics=num), operators.assemble(lit_above, numerics=num)
+    for a, b in zip(ops_b.epsilon[0][:3], ops_t.epsilon[0][:3]):
+        assert torch.equal(a, b)
+    got = operators.solve(lit_below, ops_b)
+    want = rcwa.run(lit_below, numerics=num)
+    assert torch.abs(got.R - want.R).max().item() <= 1e-12 and torch.abs(got.T - want.T).max().item() <= 1e-12

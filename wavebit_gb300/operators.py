@@ -70,8 +70,17 @@ def _contract(problem, numerics):
     """The physical inputs the operators were built for: rasters, thicknesses, period, half
     spaces, wavelengths and the order window."""
     r = _rcwa._resolve(problem, numerics)
-    return (tuple((e.shape, e.tobytes()) for e in r['rasters']), r['thickness'].tobytes(), r['period'],
-            complex(r['eps_top']), complex(r['eps_bot']), r['wavelengths'].tobytes(), r['orders'])
+    rasters, thick, top, bot = r['rasters'], r['thickness'], r['eps_top'], r['eps_bot']
+    if _lit_below(r):                      # the scene's own order and half-spaces, whichever side is lit
+        rasters, thick, top, bot = rasters[::-1], thick[::-1], bot, top
+    return (tuple((e.shape, e.tobytes()) for e in rasters), np.ascontiguousarray(thick).tobytes(), r['period'],
+            complex(top), complex(bot), r['wavelengths'].tobytes(), r['orders'])
+
+
+def _lit_below(r):
+    """Lit from below, the resolved layers are the z-mirrored scene's (entry face first); the
+    operators keep the scene's own top-first order either way."""
+    return r.get('side', 'top') == 'bottom'
 
 
 def assemble(problem, *, numerics=None, backend='gb300', device='cuda', precision='double'):
@@ -81,12 +90,14 @@ def assemble(problem, *, numerics=None, backend='gb300', device='cuda', precisio
     hu, hv = r['orders']
     conv = prepared.conv
     cm = ConvMatrices(*(_swap_frame(conv.slot(k), hu, hv) for k in range(3)))
+    if _lit_below(r):
+        cm = ConvMatrices(*(a.flip(0) for a in cm[:3]), None, None)
     n_wl = len(r['wavelengths'])
     return Operators(epsilon=(cm,) * n_wl, mu=(None,) * n_wl, wavelengths=tuple(float(w) for w in r['wavelengths']),
                      numerics=numerics, execution={'backend': backend, 'device': device, 'precision': precision},
                      metadata={'fourier_origin': 'cell center (0,0)',
                                'slot_order': ('xx', 'yy', 'inverse_zz', 'xy', 'yx'),
-                               'layer_order': 'entry face (top) first',
+                               'layer_order': 'top layer first',
                                'physical_contract': 'stack and vacuum wavelengths fixed; replace arrays '
                                                     'explicitly for a different constitutive operator'},
                      _prepared=prepared, _physical_contract=_contract(problem, numerics))
@@ -131,7 +142,7 @@ def solve(problem, operators):
                 slots.append(_swap_frame(t, hu, hv))
             which[key] = len(stacks)
             stacks.append(engine.ConvStack.from_matrices(*slots, hu, hv))
-        layer_index[w] = which[key] * L + np.arange(L)
+        layer_index[w] = which[key] * L + (np.arange(L)[::-1] if _lit_below(r) else np.arange(L))
     conv = stacks[0] if len(stacks) == 1 else engine.ConvStack(torch.cat([c.buf for c in stacks]), hu, hv)
     res = prepared._solve(r, conv, layer_index, amplitudes=True, scattering=_rcwa._wants_scattering(problem),
                           fields=_rcwa._wants_fields(problem))
