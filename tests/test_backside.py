@@ -198,11 +198,11 @@ def test_a_preparation_takes_the_same_scene_lit_from_the_other_side():
 def test_the_operator_contract_is_the_scene_not_the_lit_side():
     from wavebit_gb300 import operators
     c = _case('crossed_1')
-    top = _problem(c, 's', fields=False)
-    bottom = rcwa.Problem(units=top.units, stack=top.stack, excitation=rcwa.Excitation(
-        wavelength=top.excitation.wavelength, sources=(rcwa.PlaneWave(side='top', theta=0.1),)))
+    lit_below = _problem(c, 's', fields=False)
+    lit_above = rcwa.Problem(units=lit_below.units, stack=lit_below.stack, excitation=rcwa.Excitation(
+        wavelength=lit_below.excitation.wavelength, sources=(rcwa.PlaneWave(side='top', theta=0.1),)))
     num = rcwa.Numerics(orders=(1, 1))
-    assert operators._contract(top, num) == operators._contract(bottom, num)
+    assert operators._contract(lit_below, num) == operators._contract(lit_above, num)
 
 
 @pytest.mark.gpu
