@@ -449,6 +449,7 @@ def make_backside_cases():
                 out[f'{n}__{tag}_{port}_port'] = np.asarray(o.reference['port'])
                 out[f'{n}__{tag}_{port}_incident_power'] = np.asarray(o.reference['incident_power'])
             out[f'{n}__field_{tag}'] = np.asarray(res.field(x=x, y=y, z=z).values)
+            out[f'{n}__field_lalanne_{tag}'] = np.asarray(res.field(x=x, y=y, z=z, reconstruction='lalanne').values)
             for side in ('top', 'bottom'):
                 for part in ('incoming', 'outgoing'):
                     b = res.boundary_fields(side=side, x=x, y=y, part=part)

@@ -68,6 +68,8 @@ def _check_result(res, c, tag, tol, name):
         assert np.abs(dev_np(o.power[0]) - c[f'{key}_power']).max() <= tol * p_inc, (name, key, 'power')
     f = res.field(x=c['x'], y=c['y'], z=c['z'])
     _check_fields(dev_np(f.values[0]), c[f'field_{tag}'][0], tol, (name, tag, 'field'))
+    f = res.field(x=c['x'], y=c['y'], z=c['z'], reconstruction='lalanne')
+    _check_fields(dev_np(f.values[0]), c[f'field_lalanne_{tag}'][0], 10 * tol, (name, tag, 'lalanne'))
     for side in ('top', 'bottom'):
         for part in ('incoming', 'outgoing'):
             b = res.boundary_fields(side=side, x=c['x'], y=c['y'], part=part)
