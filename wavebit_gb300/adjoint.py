@@ -521,7 +521,9 @@ def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weigh
     polarization's per-order efficiencies, and its gradients with respect to the raster
     permittivities (real part; shape of ``eps``) and the thicknesses.
 
-    eps: (L, ny, nx) entry face first; thickness (L,); wavelengths (B,).
+    eps: (L, ny, nx) entry face first; thickness (L,); wavelengths (B,). ``eps_top`` is the lit
+    half-space: a scene lit from below is its z-mirror lit from above, so pass its layers
+    bottom-first with the half-spaces swapped (the gradients come back in that order).
     Returns (loss, R (B, N), T (B, N), d_loss/d_eps (L, ny, nx) real, d_loss/d_thickness (L,)).
 
     The eigenpairs are computed for a chunk of wavelengths at a time, sized by ``hbm_budget``
