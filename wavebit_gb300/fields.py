@@ -131,11 +131,16 @@ def order_waves(kx, ky, c, s, kzt, kzb, n_top, n_bot, ratios, pol):
     zero = torch.zeros_like(gx)
     rho = gx * c + gy * s
 
+    def cross(a, b):
+        a0, a1, a2 = a.unbind(-1)
+        b0, b1, b2 = b.unbind(-1)
+        return torch.stack([a1 * b2 - a2 * b1, a2 * b0 - a0 * b2, a0 * b1 - a1 * b0], -1)
+
     def basis(n, kz, d):
         es = torch.stack([-s, c, zero], -1)
         ep = torch.stack([-kz * c / n, -kz * s / n, d * rho / n], -1)
         k = torch.stack([gx, gy, d * kz], -1)
-        return (torch.cat([es, torch.linalg.cross(k, es)], -1), torch.cat([ep, torch.linalg.cross(k, ep)], -1))
+        return torch.cat([es, cross(k, es)], -1), torch.cat([ep, cross(k, ep)], -1)
 
     inc_s, inc_p = basis(complex(n_top), kzt, -1.0)
     ref_s, ref_p = basis(complex(n_top), kzt, 1.0)
