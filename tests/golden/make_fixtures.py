@@ -13,20 +13,28 @@ It writes
 * ``ref_integrated.npz`` -- the same scenes (but the largest) with the integrated (closed-form
   segment) coefficients, ``fourier_coefficients='integrated'``;
 * ``ref_scattering.npz`` -- the stack's exported scattering matrix (``Outputs(scattering=True)``)
-  of five of those scenes;
+  of five of those scenes and the five of ``ref_halfspace.npz``;
 * ``ref_fields.npz`` -- collocated field phasors (``Outputs(fields=True)``, ``result.field``) of
   five of those scenes and two of ``ref_halfspace.npz`` (total internal reflection, a metallic
-  substrate) at explicit points, s and p incidence;
+  substrate) at explicit points and counts, plain and Lalanne reconstruction, and the boundary
+  fields on both faces, s and p incidence;
 * ``ref_etm.npz`` -- per-order R/T of the reference's ETM connecting algorithm on the scenes of
   ``ref_cases.npz`` and ``ref_halfspace.npz``;
 * ``ref_halfspace.npz`` -- per-order R/T of the reference's own run on scenes with a lossy or
   metallic substrate, total internal reflection, a denser superstrate, and normal incidence at
   an azimuth with cos(phi) < 0;
 * ``ref_amplitudes.npz`` -- the reference's published amplitude ratios of the scenes of
-  ``ref_cases.npz`` and ``ref_halfspace.npz`` (p and mixed incidence);
+  ``ref_cases.npz`` and ``ref_halfspace.npz`` (p and mixed incidence), and the other per-order
+  readings (Cartesian ratios, powers, wavevectors, port references) of a run in micrometres with
+  a 2.5 V/m source;
+* ``ref_backside.npz`` -- scenes lit from below (``PlaneWave(side='bottom')``): R, T, every
+  per-order reading, fields, boundary fields and the incidence-relative scattering matrix;
+* ``ref_direct.npz`` -- runs with the incidence given as a wavevector (``PlaneWave(kx=, ky=)``)
+  over two wavelengths, from either side;
 * ``ref_bare.npz`` -- per-order R/T of the reference's own run on stacks with no layers;
 * ``reticolo_cases.npz`` -- RETICOLO's per-order efficiencies of twelve 1D gratings (the
-  reference's ``tests/references/golden_reticolo.npz``) with their inputs;
+  reference's ``tests/references/golden_reticolo.npz``), lit from above and from below, with
+  their inputs;
 * ``legacy_cases.npz`` -- the efficiencies that the reference's own frozen legacy golden file
   (``tests/fixtures/legacy_rcwa/golden_legacy.npz``) holds for its 1D, conical and 2D sampled-Li
   cases, with the inputs those cases are defined by (``tests/fixtures/legacy_rcwa/gen_goldens.py``).
