@@ -409,3 +409,14 @@ def test_units_and_order_lookup_refusals():
     with pytest.raises(KeyError):
         refl.order(3, 0)
     assert refl.order(-2, 1).efficiency.shape == (1,) and refl.field_s is None
+
+
+def test_numerics_the_path_does_not_implement_are_refused_not_ignored():
+    """The second-order layer operator is what the kernels solve; a merge tolerance changes the
+    problem. Both defaults pass, other values are refused with the option's path."""
+    rcwa._numerics_orders(rcwa.Numerics(orders=(1, 1), formulation='second_order', half_space_merge_tolerance=0.0))
+    for kw, path in ((dict(formulation='first_order'), 'numerics.formulation'),
+                     (dict(half_space_merge_tolerance=1e-6), 'numerics.half_space_merge_tolerance')):
+        with pytest.raises(rcwa.UnsupportedFeatureError) as e:
+            rcwa._numerics_orders(rcwa.Numerics(orders=(1, 1), **kw))
+        assert e.value.path == path

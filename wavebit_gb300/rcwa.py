@@ -241,6 +241,8 @@ class Numerics:
     li_nesting: object = None
     detuning: object = None
     exceptional_points: str = 'rebuild'
+    formulation: str = 'auto'
+    half_space_merge_tolerance: float = 0.0
 
 # ------------------------------------------------------------------------ resolution
 
@@ -275,6 +277,16 @@ def _numerics_orders(numerics):
             raise UnsupportedFeatureError(
                 f'numerics.{name}={val!r}: the GB300 path implements {", ".join(map(repr, allowed[1:]))} only',
                 path=f'numerics.{name}')
+    # the layer operator here is the second-order one (Omega^2, solve_2d.py:2377-2418), and a
+    # tolerance that snaps nearly equal media into a half-space changes the problem
+    form = getattr(getattr(numerics, 'formulation', 'auto'), 'value', getattr(numerics, 'formulation', 'auto'))
+    if form not in (None, 'auto', 'second_order'):
+        raise UnsupportedFeatureError(f'numerics.formulation={form!r}: the GB300 path solves the second-order '
+                                      "layer operator ('auto' or 'second_order')", path='numerics.formulation')
+    tol = getattr(numerics, 'half_space_merge_tolerance', 0.0)
+    if tol not in (None, 0, 0.0):
+        raise UnsupportedFeatureError('numerics.half_space_merge_tolerance: the GB300 path solves the stack as '
+                                      'declared (tolerance 0)', path='numerics.half_space_merge_tolerance')
     det = getattr(numerics, 'detuning', None)
     if det is not None and (type(det) not in (float, int) or not math.isfinite(det) or det <= 0):
         raise ValidationError('detuning is None (exact requested problem) or a positive relative step.',
