@@ -420,3 +420,42 @@ def test_numerics_the_path_does_not_implement_are_refused_not_ignored():
         with pytest.raises(rcwa.UnsupportedFeatureError) as e:
             rcwa._numerics_orders(rcwa.Numerics(orders=(1, 1), **kw))
         assert e.value.path == path
+
+
+def test_other_illuminations_are_refused_not_read_as_a_plane_wave():
+    """An incident-order set, a Gaussian beam and a dipole carry angle fields like a plane wave;
+    they are refused by what defines them rather than solved as their central wave."""
+    from dataclasses import dataclass
+
+    @dataclass(frozen=True)
+    class IncidentOrders:
+        weights: tuple
+        side: str = 'top'
+        polarization: object = 's'
+        amplitude: object = 1.0
+        theta: object = 0.1
+        phi: object = None
+        kx: object = None
+        ky: object = None
+
+    @dataclass(frozen=True)
+    class GaussianBeam:
+        waist: object = 2.0
+        side: str = 'top'
+        polarization: object = 's'
+        theta: object = None
+        phi: object = None
+        kx: object = None
+        ky: object = None
+
+    @dataclass(frozen=True)
+    class ElectricDipole:
+        position: tuple = (0.0, 0.0, 10.0)
+        moment: tuple = (1.0, 0.0, 0.0)
+
+    for src in (IncidentOrders(weights=(((0, 0), 1.0), ((1, 0), 0.5))), GaussianBeam(), ElectricDipole()):
+        prob = rcwa.Problem(stack=rcwa.Stack(period=(500.0, 500.0), layers=(rcwa.Layer(thickness=50.0, epsilon=2.0),)),
+                            excitation=rcwa.Excitation(wavelength=600.0, sources=(src,)))
+        with pytest.raises(rcwa.UnsupportedFeatureError) as e:
+            rcwa._resolve(prob, rcwa.Numerics(orders=(1, 1)))
+        assert e.value.path == 'excitation.sources[0]'

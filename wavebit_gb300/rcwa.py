@@ -383,6 +383,12 @@ def _resolve(problem, numerics):
         raise UnsupportedFeatureError('one PlaneWave source per problem on the GB300 path',
                                       path='excitation.sources')
     src = sources[0]
+    # a coherent order set, a beam or a dipole reads like a plane wave by its angle fields but is
+    # another illumination; it is refused by what defines it, never solved as its central wave
+    for marker, kind in (('weights', 'incident orders'), ('waist', 'a Gaussian beam'), ('moment', 'a dipole')):
+        if hasattr(src, marker):
+            raise UnsupportedFeatureError(f'{kind} as a source is outside the GB300 path (one plane wave per problem)',
+                                          path='excitation.sources[0]')
     direct = getattr(src, 'kx', None) is not None or getattr(src, 'ky', None) is not None
     if direct:
         thetas, phi = _direct_incidence(src, wl, eps_top)
