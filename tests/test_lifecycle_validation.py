@@ -459,3 +459,20 @@ def test_other_illuminations_are_refused_not_read_as_a_plane_wave():
         with pytest.raises(rcwa.UnsupportedFeatureError) as e:
             rcwa._resolve(prob, rcwa.Numerics(orders=(1, 1)))
         assert e.value.path == 'excitation.sources[0]'
+
+
+def test_a_profiled_layer_is_refused():
+    from dataclasses import dataclass
+
+    @dataclass(frozen=True)
+    class ProfiledLayer:
+        thickness: object
+        background: object = None
+        regions: tuple = ()
+        layers: tuple = ()
+
+    prob = rcwa.Problem(stack=rcwa.Stack(period=(500.0, 500.0), layers=(ProfiledLayer(thickness=50.0, background=2.0),)),
+                        excitation=rcwa.Excitation(wavelength=600.0, sources=(rcwa.PlaneWave(),)))
+    with pytest.raises(rcwa.UnsupportedFeatureError) as e:
+        rcwa._resolve(prob, rcwa.Numerics(orders=(1, 1)))
+    assert e.value.path == 'stack.layers[0]'

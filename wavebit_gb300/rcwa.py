@@ -334,6 +334,10 @@ def _resolve(problem, numerics):
         if getattr(layer, 'regions', ()):
             raise UnsupportedFeatureError('region (shape) layers are outside the GB300 raster path',
                                           path=f'stack.layers[{i}]')
+        if hasattr(layer, 'layers') or not hasattr(layer, 'epsilon'):
+            # a profiled layer is sliced by height, its material may grade with height
+            raise UnsupportedFeatureError('profiled (height-dependent) layers are outside the GB300 raster path',
+                                          path=f'stack.layers[{i}]')
         if getattr(layer, 'mu', None) is not None:
             raise UnsupportedFeatureError('magnetic layers are outside the GB300 raster path',
                                           path=f'stack.layers[{i}].mu')
