@@ -90,6 +90,12 @@ def test_lifecycle_with_a_direct_wavevector_on_the_cpu(name, monkeypatch):
         B = len(r['wavelengths'])
         res = p._solve_etm(r, conv, np.tile(np.arange(len(r['rasters'])), (B, 1)))
         _check(res, c, tag, 1e-11, name)
+        # one wavelength of the two, with its own reference entries
+        one = res.reflection.at_wavelength_index(1)
+        assert one.wavelengths == res.wavelengths[1:] and torch.equal(one.power, res.reflection.power[1:])
+        assert len(one.reference['incident_power']) == 1 and len(one.reference['plane']) == 1
+        with pytest.raises(IndexError):
+            res.reflection.at_wavelength_index(2)
 
 
 def test_direct_wavevector_refusals():

@@ -568,6 +568,31 @@ class DiffractionOrders(NamedTuple):
     field_p = property(lambda self: _incident_scaled(self.amplitude_ratio_p, self.reference))
     field_xyz = property(lambda self: _incident_scaled(self.amplitude_ratio_xyz, self.reference))
 
+    #: entries of ``reference`` / ``metadata`` that carry a wavelength axis (contracts.py:216-219)
+    _PER_WAVELENGTH = ('plane', 'epsilon', 'mu', 'cell_measure', 'incident_power', 'power_defined',
+                       'efficiency_defined')
+
+    def at_wavelength_index(self, index):
+        """These orders at the wavelength in position ``index``, as a length-1 wavelength axis
+        (contracts.py:269-285): every array and every per-wavelength reference entry sliced."""
+        i = int(index)
+        if not 0 <= i < len(self.wavelengths):
+            raise IndexError(i)
+        cut = lambda a: None if a is None else a[i:i + 1]
+        maps = []
+        for mapping in (self.reference, self.metadata):
+            m = dict(mapping or {})
+            for key in self._PER_WAVELENGTH:
+                v = m.get(key)
+                if v is not None and not isinstance(v, str) and len(v) == len(self.wavelengths):
+                    m[key] = v[i:i + 1]
+            maps.append(m)
+        return self._replace(wavelengths=tuple(self.wavelengths)[i:i + 1], efficiency=cut(self.efficiency),
+                             amplitude_ratio_s=cut(self.amplitude_ratio_s), amplitude_ratio_p=cut(self.amplitude_ratio_p),
+                             power=cut(self.power), amplitude_ratio_xyz=cut(self.amplitude_ratio_xyz),
+                             k_parallel=cut(self.k_parallel), k_normal=cut(self.k_normal),
+                             reference=maps[0], metadata=maps[1])
+
     def order(self, m, n=0):
         """Order ``(m, n)`` as one :class:`DiffractionOrder` (contracts.py:259-267); KeyError when
         the order is not retained."""
