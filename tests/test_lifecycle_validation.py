@@ -476,3 +476,17 @@ def test_a_profiled_layer_is_refused():
     with pytest.raises(rcwa.UnsupportedFeatureError) as e:
         rcwa._resolve(prob, rcwa.Numerics(orders=(1, 1)))
     assert e.value.path == 'stack.layers[0]'
+
+
+def test_readings_without_amplitudes_keep_the_wavevectors():
+    """run(amplitudes=False): the amplitude-derived readings are None, never zeros; the
+    wavevectors and port references, which need no amplitude, are still given."""
+    import torch
+    R = torch.zeros((1, 3, 5), dtype=torch.float64)
+    ports = dict(wavelengths=[600.0], thetas=[0.1], phi=0.0, period=(500.0, 500.0), eps_top=1.0, eps_bot=2.0,
+                 pol=(1.0, 0.0), amplitude=1.0, length='nm', top_plane=10.0, side='top')
+    refl, trans = rcwa._diffraction_orders(R, R, None, (600.0,), 2, 1, ports=ports)
+    for o in (refl, trans):
+        assert o.power is None and o.amplitude_ratio_xyz is None and o.amplitude_ratio_s is None
+        assert o.k_normal.shape == (1, 3, 5) and o.reference['incident_power'] is None
+    assert refl.reference['port'] == 'top' and trans.reference['plane'] == (0.0,)
