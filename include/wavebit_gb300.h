@@ -164,7 +164,10 @@ int wb_scattering_matrix(wb_handle* h, int B, int L, int hu, int hv, const wb_co
 /* The same solve from HOST buffers: rasters in, efficiencies out. Copies inputs to the
  * device, assembles the L layers (stage A), solves the B problems, copies R, T and status
  * back and synchronises. eps: host (L, ny, nx); the other arrays as in wb_solve_batch but in
- * host memory. Reference: the rcwa.run(problem) lifecycle, rcwa/_lifecycle.py:698-803. */
+ * host memory (pinned memory makes the copies asynchronous DMA). The device block that stages
+ * inputs, slots and outputs belongs to the handle: allocated by the first call, grown only when
+ * a later call needs more, freed by wb_destroy. Reference: the rcwa.run(problem) lifecycle,
+ * rcwa/_lifecycle.py:698-803. */
 int wb_solve_host(wb_handle* h, int B, int L, int ny, int nx, int hu, int hv,
                   const wb_complex* eps, const int32_t* layer_index, const double* thickness,
                   const double* wavelength, const double* period, const double* theta,

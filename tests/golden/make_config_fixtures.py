@@ -1,0 +1,89 @@
+"""Golden per-order efficiencies of the benchmark configurations, from the reference itself.
+
+Run where the reference source tree is available (read-only)::
+
+    PYTHONPATH=tests/golden/refshim python tests/golden/make_config_fixtures.py --reference <root>
+
+It writes ``ref_configs.npz``, the reference's public ``rcwa.run`` (NumPy backend, SMM, sampled
+Li, fixed nesting, complex128) on the workloads the benchmark measures, at their full sizes:
+
+* ``grating_1d`` -- the quickstart 1D grating (orders (10, 0), s);
+* ``crossed_slice`` -- four of the 128 wavelengths of the crossed-grating sweep: the three
+  seeded 256x256 binary rasters and the 50 nm eps = -20+1.5j layer, orders (7, 7) (N = 225,
+  450x450 mode matrices), s and p;
+* ``mixed_points`` -- two of the 1024 (wavelength, theta) points of the orders-(12, 12) sweep:
+  four seeded 256x256 binary rasters (N = 625, 1250x1250 mode matrices), s and p.
+
+The rasters come from the seeded generators of ``wavebit_gb300/workloads.py`` and are stored with
+the results (compressed: they are a few rectangles and discs), so the tests need neither the
+generator's arithmetic nor the reference. Layers are stored in kernel order (entry face first).
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+sys.path.insert(0, ROOT)
+
+import make_fixtures as MF  # noqa: E402
+from wavebit_gb300 import workloads as WL  # noqa: E402
+
+#: wavelength indices of the crossed-grating sweep's slice (of 128 over 400-1000 nm)
+CROSSED_INDICES = (0, 41, 86, 127)
+#: (wavelength index of 256, theta index of {0, 0.2, 0.4, 0.6}) of the orders-(12, 12) points
+MIXED_POINTS = ((37, 3), (201, 1))
+
+
+def _case(name, eps, thickness, wavelength, orders, theta, eps_top, eps_bot, period):
+    return dict(name=name, structure=np.asarray(eps, complex), thickness=list(thickness),
+                wavelength=float(wavelength), period=tuple(period), orders=tuple(orders), theta=float(theta),
+                phi=0.0, eps_top=eps_top, eps_bot=eps_bot)
+
+
+def config_cases():
+    cases = []
+    g = WL.grating_1d()
+    cases.append(_case('grating_1d', g['eps'], g['thickness'], g['wavelengths'][0], g['orders'], 0.0,
+                       g['eps_top'], g['eps_bot'], g['period']))
+    c = WL.crossed_sweep()
+    for i in CROSSED_INDICES:
+        cases.append(_case(f'crossed_{i}', c['eps'], c['thickness'], c['wavelengths'][i], c['orders'], 0.0,
+                           c['eps_top'], c['eps_bot'], c['period']))
+    m = WL.mixed_sweep()
+    for wi, ti in MIXED_POINTS:
+        p = wi * 4 + ti
+        cases.append(_case(f'mixed_{wi}_{ti}', m['eps'], m['thickness'], m['wavelengths'][p], m['orders'],
+                           m['thetas'][p], m['eps_top'], m['eps_bot'], m['period']))
+    return cases
+
+
+def main():
+    MF.use_reference()
+    out = {}
+    names = []
+    stacks = {}
+    for case in config_cases():
+        n = case['name']
+        names.append(n)
+        key = n.split('_')[0]
+        if key not in stacks:
+            stacks[key] = case['structure']
+            out[f'{key}__structure'] = case['structure']
+        for k in ('thickness', 'wavelength', 'period', 'orders', 'theta', 'phi', 'eps_top', 'eps_bot'):
+            out[f'{n}__{k}'] = np.asarray(case[k])
+        out[f'{n}__stack'] = np.asarray(key)
+        for pol in ('s', 'p'):
+            R, T, _ = MF.run_ref(case, pol)
+            out[f'{n}__R_{pol}'] = R
+            out[f'{n}__T_{pol}'] = T
+        print(n, 'R+T =', float(out[f'{n}__R_s'].sum() + out[f'{n}__T_s'].sum()), flush=True)
+    out['names'] = np.array(names)
+    np.savez_compressed(os.path.join(HERE, 'ref_configs.npz'), **out)
+    print('ref_configs.npz:', len(names), 'cases')
+
+
+if __name__ == '__main__':
+    main()

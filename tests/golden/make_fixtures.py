@@ -1,8 +1,9 @@
 """Generate the golden fixtures in this folder from the reference implementation.
 
-Run in a container that holds the reference source tree (read-only) with::
+Run where the reference source tree is available (read-only), naming its root with
+``--reference`` or the ``WAVEBIT_REFERENCE`` environment variable::
 
-    PYTHONPATH=tests/golden/refshim:/root/reference/src python tests/golden/make_fixtures.py
+    PYTHONPATH=tests/golden/refshim python tests/golden/make_fixtures.py --reference <root>
 
 It writes
 
@@ -49,7 +50,24 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = '/root/reference'
+#: the reference's source root (holding ``src/wavebit`` and its ``tests/``), set by
+#: :func:`use_reference` from ``--reference`` or ``WAVEBIT_REFERENCE``
+REF = None
+
+
+def use_reference(argv=None):
+    """Resolve the reference root from ``--reference PATH`` (or ``WAVEBIT_REFERENCE``) and put
+    its ``src`` on the import path."""
+    global REF
+    argv = list(sys.argv[1:] if argv is None else argv)
+    root = os.environ.get('WAVEBIT_REFERENCE')
+    if '--reference' in argv:
+        root = argv[argv.index('--reference') + 1]
+    if not root or not os.path.isdir(os.path.join(root, 'src', 'wavebit')):
+        raise SystemExit('name the reference source root with --reference PATH or WAVEBIT_REFERENCE')
+    REF = root
+    sys.path.insert(0, os.path.join(REF, 'src'))
+    return REF
 
 
 def _rast(rng, ny, nx, values=(12.25,), n_shapes=3, background=1.0):
@@ -580,7 +598,7 @@ def make_reticolo_cases():
 
 
 if __name__ == '__main__':
-    sys.path.insert(0, os.path.join(REF, 'src'))
+    use_reference()
     make_ref_cases()
     make_integrated_cases()
     make_scattering_cases()

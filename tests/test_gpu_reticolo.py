@@ -49,7 +49,7 @@ def test_gpu_matches_reticolo_orders_from_below(name):
     d = np.load(os.path.join(GOLDEN, 'reticolo_cases.npz'))
     c = {k.split('__', 1)[1]: d[k] for k in d.files if k.startswith(name + '__')}
     h, per = int(c['h']), float(c['period'])
-    st = np.ascontiguousarray(np.asarray(c['structure'], complex)[::-1])
+    st = np.asarray(c['structure'], complex)[::-1].copy()   # a fresh array: positive strides even for one layer
     L = st.shape[0]
     n_top, n_bot = np.sqrt(complex(c['top'])).real, np.sqrt(complex(c['bot'])).real
     theta_b = float(np.arcsin(n_top * np.sin(float(c['theta'])) / n_bot))

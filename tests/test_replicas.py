@@ -65,11 +65,15 @@ def test_reference_arm_under_torchrun_prints_once_from_rank_zero():
     env = dict(os.environ, OMP_NUM_THREADS='2', MKL_NUM_THREADS='2', OPENBLAS_NUM_THREADS='2')
     cmd = [sys.executable, '-m', 'torch.distributed.run', '--nnodes=1', '--nproc-per-node', '2',
            '--master-addr', '127.0.0.1', '--master-port', str(_free_port()), os.path.join(ROOT, 'bench.py'),
-           '--impl', 'reference', '--gpus', '2', '--steps', '1', '--warmup', '0', '--ref-sample', '1']
+           '--impl', 'reference', '--gpus', '2', '--steps', '1', '--warmup', '0', '--workload', 'crossed_sweep']
     res = subprocess.run(cmd, capture_output=True, text=True, timeout=600, env=env, cwd=ROOT)
     assert res.returncode == 0, res.stderr[-2000:]
     lines = [l for l in res.stdout.splitlines() if l.startswith('{')]
     assert len(lines) == 1
     line = json.loads(lines[0])
     assert line['impl'] == 'reference' and line['n_gpus'] == 2 and line['unit'] == 'solves/s'
-    assert line['cpu_baseline']['kind'] == 'port' and line['e2e']['h2d_bytes_per_step'] == 0
+    sys.path.insert(0, ROOT)
+    import bench
+    want = 'reference' if bench.reference_available() else 'port'
+    assert line['cpu_baseline']['kind'] == want and line['e2e']['h2d_bytes_per_step'] == 0
+    assert line['steps'] == 1 and line['metric'] == bench.metric('crossed_sweep', 'double')

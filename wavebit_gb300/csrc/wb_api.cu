@@ -18,6 +18,10 @@ struct wb_handle {
   wb::Arena arena;
   void* buf = nullptr;
   size_t buf_bytes = 0;
+  // device staging block of wb_solve_host (inputs, slots, outputs), kept between calls and grown
+  // only when a call needs more; separate from the arena, which the solve itself uses
+  void* io = nullptr;
+  size_t io_bytes = 0;
 };
 
 namespace {
@@ -101,7 +105,12 @@ int wb_create(int device, size_t hbm_budget, wb_handle** out) {
 
 int wb_destroy(wb_handle* h) {
   if (!h) return WB_OK;
-  if (h->buf) { cudaSetDevice(h->device); cudaDeviceSynchronize(); cudaFree(h->buf); }
+  if (h->buf || h->io) {
+    cudaSetDevice(h->device);
+    cudaDeviceSynchronize();
+    if (h->buf) cudaFree(h->buf);
+    if (h->io) cudaFree(h->io);
+  }
   delete h;
   return WB_OK;
 }
@@ -314,8 +323,21 @@ int wb_solve_host(wb_handle* h, int B, int L, int ny, int nx, int hu, int hv,
   const size_t o_R = take(sizeof(double) * 3 * B * N), o_T = take(sizeof(double) * 3 * B * N);
   const size_t o_st = take(sizeof(int32_t) * B), o_ast = take(sizeof(int32_t));
   const size_t o_tmp = take(sizeof(wb_complex) * 3 * L * NN);   // slot planes before regrouping
-  char* dev = nullptr;
-  if (cudaMalloc(&dev, off) != cudaSuccess) { cudaGetLastError(); return fail(WB_E_NOMEM, "wb_solve_host: cudaMalloc(%zu)", off); }
+  if (off > h->io_bytes) {
+    if (h->io) {
+      cudaError_t e = cudaDeviceSynchronize();
+      if (e != cudaSuccess) return fail(WB_E_CUDA, "wb_solve_host: synchronise before growing: %s", cudaGetErrorString(e));
+      cudaFree(h->io);
+      h->io = nullptr; h->io_bytes = 0;
+    }
+    if (cudaMalloc(&h->io, off) != cudaSuccess) {
+      cudaGetLastError();
+      h->io = nullptr;
+      return fail(WB_E_NOMEM, "wb_solve_host: cudaMalloc(%zu)", off);
+    }
+    h->io_bytes = off;
+  }
+  char* dev = (char*)h->io;
   cudaStream_t s = nullptr;
   auto H2D = [&](size_t o, const void* p, size_t b) { cudaMemcpyAsync(dev + o, p, b, cudaMemcpyHostToDevice, s); };
   H2D(o_eps, eps, sizeof(wb_complex) * L * ny * nx);
@@ -360,8 +382,10 @@ int wb_solve_host(wb_handle* h, int B, int L, int ny, int nx, int hu, int hv,
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) rc = fail(WB_E_CUDA, "wb_solve_host: %s", cudaGetErrorString(e));
     else if (ast) for (int b = 0; b < B; ++b) status[b] |= ast;
+  } else {
+    cudaStreamSynchronize(s);   // nothing queued may still read the caller's host buffers
+    cudaGetLastError();
   }
-  cudaFree(dev);
   return rc;
 }
 

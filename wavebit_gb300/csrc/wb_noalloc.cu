@@ -10,8 +10,9 @@
 //
 // The array is WB_NOALLOC_SCRATCH_BYTES (32 MiB) and every GPU that loads libwbgpu.so holds
 // it until the process exits. Layers are assembled one at a time through it, so the limit is
-// per layer: assemble_workspace_bytes(1, ny, nx, hu, hv) must fit (e.g. a 256x256 raster up to
-// orders (12, 12)). Larger requests are refused with WB_E_INVALID before any GPU work.
+// per layer: assemble_workspace_bytes(1, ny, nx, hu, hv) must fit (a 256x256 raster fits up to
+// orders (14, 14), about 30 MiB; (15, 15) needs about 38 MiB). Larger requests are refused with
+// WB_E_INVALID before any GPU work.
 //
 // All calls share the one array and each leaves its contents behind. Nothing in it has to start
 // at zero: every scratch entry the assembly reads it has written earlier in the same call. Calls

@@ -238,8 +238,10 @@ def scattering_matrix(W, V, q, inp, hu, hv, handle=None):
 
 
 def solve_host(eps, layer_index, thickness, wavelength, period, theta, phi, eps_top, eps_bot, pol,
-               hu, hv, precision='double', handle=None):
-    """Whole solve from host (NumPy) buffers through ``wb_solve_host``."""
+               hu, hv, precision='double', handle=None, out=None):
+    """Whole solve from host (NumPy) buffers through ``wb_solve_host``. ``out`` = (R, T, status)
+    host arrays of shapes (B, 3, N), (B, 3, N), (B,) to write into (pinned ones make the copies
+    asynchronous DMA); fresh arrays otherwise."""
     eps = np.ascontiguousarray(eps, dtype=np.complex128)
     L, ny, nx = eps.shape
     li = np.ascontiguousarray(layer_index, dtype=np.int32)
@@ -253,9 +255,16 @@ def solve_host(eps, layer_index, thickness, wavelength, period, theta, phi, eps_
                 et=np.ascontiguousarray(eps_top, np.complex128).reshape(B),
                 eb=np.ascontiguousarray(eps_bot, np.complex128).reshape(B),
                 pol=np.ascontiguousarray(pol, np.complex128).reshape(B, 2))
-    R = np.empty((B, 3, N), np.float64)
-    T = np.empty((B, 3, N), np.float64)
-    status = np.zeros(B, np.int32)
+    if out is None:
+        R = np.empty((B, 3, N), np.float64)
+        T = np.empty((B, 3, N), np.float64)
+        status = np.zeros(B, np.int32)
+    else:
+        R, T, status = out
+        if (R.shape != (B, 3, N) or T.shape != (B, 3, N) or status.shape != (B,) or R.dtype != np.float64
+                or T.dtype != np.float64 or status.dtype != np.int32 or not all(a.flags.c_contiguous for a in out)):
+            raise ValueError('out must be C-contiguous (B, 3, N) float64, (B, 3, N) float64 and (B,) int32 arrays')
+        status[...] = 0
     h = handle or _lib.handle(0)
     _lib.check(h.lib.wb_solve_host(
         h.h, B, li.shape[1], ny, nx, hu, hv, eps.ctypes.data, li.ctypes.data, arrs['th'].ctypes.data,
