@@ -201,6 +201,18 @@ size_t wb_assemble_li_noalloc_limit(void);
  * handles (for accounting: take differences around a region). The handle is not consulted. */
 long long wb_kernel_launches(wb_handle* h);
 
+/* Launch-shape tunables, process-wide: 0 restores the library's own choice. The autotuner
+ * (wavebit_gb300/autotune.py) times candidates per (orders, layers, batch) bucket and sets them
+ * before each batch; results never depend on them. No counterpart in the reference (its backends
+ * leave launch shapes to LAPACK and torch). */
+#define WB_TUNE_QR_THREADS 0     /* threads of a QR-sweep CTA (64..1024, multiple of 32) */
+#define WB_TUNE_HRD_THREADS 1    /* threads of a Hessenberg-reduction CTA (64..1024, multiple of 32) */
+#define WB_TUNE_LU_THREADS 2     /* reserved: threads of an LU / triangular-solve CTA */
+#define WB_TUNE_COUNT 8
+int wb_set_tuning(int key, int value);
+/* The current value of a tunable (0 = the library's own choice), or -1 for an unknown key. */
+int wb_get_tuning(int key);
+
 #ifdef __cplusplus
 }
 #endif

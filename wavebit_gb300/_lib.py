@@ -39,6 +39,8 @@ SIGNATURES = {
     'wb_solve_workspace_bytes': (_sz, [_i, _i, _i, _i]),
     'wb_workspace_bytes': (_sz, [_i, _i, _i, _i, _i]),
     'wb_kernel_launches': (_ll, [_vp]),
+    'wb_set_tuning': (_i, [_i, _i]),
+    'wb_get_tuning': (_i, [_i]),
     'wb_assemble_li_noalloc': (_i, [_vp, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     'wb_assemble_li_noalloc_limit': (_sz, []),
 }

@@ -391,4 +391,17 @@ int wb_solve_host(wb_handle* h, int B, int L, int ny, int nx, int hu, int hv,
 
 long long wb_kernel_launches(wb_handle* h) { (void)h; return wb::launch_count(); }
 
+static_assert(WB_TUNE_QR_THREADS == wb::kTuneQrThreads && WB_TUNE_HRD_THREADS == wb::kTuneHrdThreads &&
+                  WB_TUNE_LU_THREADS == wb::kTuneLuThreads && WB_TUNE_COUNT == wb::kTuneKeys,
+              "public and internal tuning keys agree");
+
+int wb_set_tuning(int key, int value) {
+  if (key < 0 || key >= WB_TUNE_COUNT) return fail(WB_E_INVALID, "wb_set_tuning: key %d outside [0, %d)", key, WB_TUNE_COUNT);
+  if (value < 0) return fail(WB_E_INVALID, "wb_set_tuning: value %d < 0", value);
+  wb::set_tuning(key, value);
+  return WB_OK;
+}
+
+int wb_get_tuning(int key) { return (key >= 0 && key < WB_TUNE_COUNT) ? wb::tuning(key) : -1; }
+
 }  // extern "C"

@@ -19,7 +19,6 @@
 
 namespace wb {
 
-constexpr int EIG_THREADS = 256;
 
 __device__ __forceinline__ double shfl_xor(double v, int off) { return __shfl_xor_sync(0xffffffffu, v, off); }
 __device__ __forceinline__ float shfl_xor(float v, int off) { return __shfl_xor_sync(0xffffffffu, v, off); }
@@ -95,12 +94,30 @@ template <class R> __device__ __forceinline__ Refl<R> make_reflector(Cx<R> alpha
 
 // ------------------------------------------------------------- 1. Hessenberg reduction
 // H := Q^H A Q, reflectors stored below the subdiagonal (v_0 = 1 implicit), tau[k].
+//
+// Both sides of reflector k are applied in one pass over the trailing columns. With y = A v
+// (all rows) and c = v^H y, the right update A' = A - t y v^H and the left update
+// A'' = A' - conj(t) v (v^H A') combine, column by column, into
+//   A''[:, j] = A[:, j] - t y conj(v_j) - conj(t) v z_j,   z_j = v^H A[:, j] - t c conj(v_j),
+// so each step reads the trailing matrix twice (y, then each column's z_j and its update) and
+// writes it once. Every load-modify-store sweep issues kUnroll loads before its stores, so one
+// memory latency serves kUnroll elements per lane.
+constexpr int kUnroll = 4;
+
 template <class R>
-__global__ void __launch_bounds__(EIG_THREADS) gehrd_kernel(Cx<R>* __restrict__ Aall, int n, int lda,
-                                                            long long a_bs, Cx<R>* __restrict__ tau_all) {
+__device__ __forceinline__ Cx<R> block_sum_cx(Cx<R> v, R* red) {
+  Cx<R> r;
+  r.x = block_sum(v.x, red);
+  r.y = block_sum(v.y, red);
+  return r;
+}
+
+template <class R>
+__global__ void __launch_bounds__(1024) gehrd_kernel(Cx<R>* __restrict__ Aall, int n, int lda,
+                                                     long long a_bs, Cx<R>* __restrict__ tau_all) {
   using C_ = Cx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
-  C_* sv = reinterpret_cast<C_*>(smraw);          // v (n), then t*y (n)
+  C_* sv = reinterpret_cast<C_*>(smraw);          // v (n), then y = A v (n)
   __shared__ R red[32];
   __shared__ C_ s_tau;
   C_* A = Aall + blockIdx.x * a_bs;
@@ -133,30 +150,50 @@ __global__ void __launch_bounds__(EIG_THREADS) gehrd_kernel(Cx<R>* __restrict__ 
     __syncthreads();
     // every thread has read alpha = A(k+1, k) by now; column k is not touched again in this step
     if (tid == 0) col[k + 1] = cxmk<R>(r.beta, R(0.0));
-    const C_ t = s_tau;
-    // right: y = A[:, k+1:n] v ; A[:, k+1:n] -= t y v^H  (all rows)
+    const C_ t = s_tau, tc = cxconj(t);
+    // y = A[:, k+1:n] v, one row per thread (loads only: they pipeline)
     for (int i = tid; i < n; i += blockDim.x) {
-      C_ acc = cxzero<R>();
-      for (int j = 0; j < m; ++j) acc = cxfma(A[i + (long long)(k + 1 + j) * lda], sv[j], acc);
-      sy[i] = t * acc;
+      const C_* ai = A + i + (long long)(k + 1) * lda;
+      C_ acc0 = cxzero<R>(), acc1 = cxzero<R>();
+      int j = 0;
+      for (; j + 1 < m; j += 2) {
+        acc0 = cxfma(ai[(long long)j * lda], sv[j], acc0);
+        acc1 = cxfma(ai[(long long)(j + 1) * lda], sv[j + 1], acc1);
+      }
+      if (j < m) acc0 = cxfma(ai[(long long)j * lda], sv[j], acc0);
+      sy[i] = acc0 + acc1;
     }
     __syncthreads();
-    for (int j = warp; j < m; j += nw) {
-      C_* cj = A + (long long)(k + 1 + j) * lda;
-      const C_ vjc = cxconj(sv[j]);
-      for (int i = lane; i < n; i += 32) cj[i] = cj[i] - sy[i] * vjc;
-    }
-    __syncthreads();
-    // left: z_j = v^H A[k+1:n, j] ; A[k+1:n, j] -= conj(t) v z_j   for j = k+1 .. n-1
-    const C_ tc = cxconj(t);
-    for (int j = warp; j < m; j += nw) {
-      C_* cj = A + (long long)(k + 1 + j) * lda;
+    C_ cp = cxzero<R>();
+    for (int i = tid; i < m; i += blockDim.x) cp = cxfma_conj(sv[i], sy[k + 1 + i], cp);
+    const C_ c = block_sum_cx(cp, red);
+    const C_ tcoef = t * c;
+    // both sides, one warp per trailing column
+    for (int jj = warp; jj < m; jj += nw) {
+      C_* cj = A + (long long)(k + 1 + jj) * lda;
       C_ acc = cxzero<R>();
       for (int i = lane; i < m; i += 32) acc = cxfma_conj(sv[i], cj[k + 1 + i], acc);
       acc.x = warp_sum(acc.x);
       acc.y = warp_sum(acc.y);
-      const C_ f = tc * acc;
-      for (int i = lane; i < m; i += 32) cj[k + 1 + i] = cj[k + 1 + i] - sv[i] * f;
+      const C_ vjc = cxconj(sv[jj]);
+      const C_ z = acc - tcoef * vjc;
+      const C_ a1 = t * vjc, a2 = tc * z;
+      for (int i0 = lane; i0 < n; i0 += 32 * kUnroll) {
+        C_ val[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+          const int i = i0 + 32 * u;
+          if (i < n) val[u] = cj[i];
+        }
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+          const int i = i0 + 32 * u;
+          if (i >= n) continue;
+          C_ nv = val[u] - sy[i] * a1;
+          if (i > k) nv = nv - sv[i - k - 1] * a2;
+          cj[i] = nv;
+        }
+      }
     }
     __syncthreads();
   }
@@ -164,7 +201,7 @@ __global__ void __launch_bounds__(EIG_THREADS) gehrd_kernel(Cx<R>* __restrict__ 
 
 // ------------------------------------------------------------------ 2. form Q = Z
 template <class R>
-__global__ void __launch_bounds__(EIG_THREADS) unghr_kernel(Cx<R>* __restrict__ Aall, int n, int lda,
+__global__ void __launch_bounds__(1024) unghr_kernel(Cx<R>* __restrict__ Aall, int n, int lda,
                                                             long long a_bs, const Cx<R>* __restrict__ tau_all,
                                                             Cx<R>* __restrict__ Zall, int ldz, long long z_bs) {
   using C_ = Cx<R>;
@@ -192,7 +229,15 @@ __global__ void __launch_bounds__(EIG_THREADS) unghr_kernel(Cx<R>* __restrict__ 
       acc.x = warp_sum(acc.x);
       acc.y = warp_sum(acc.y);
       const C_ f = t * acc;
-      for (int i = lane; i < m; i += 32) cj[k + 1 + i] = cj[k + 1 + i] - sv[i] * f;
+      for (int i0 = lane; i0 < m; i0 += 32 * kUnroll) {
+        C_ val[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u)
+          if (i0 + 32 * u < m) val[u] = cj[k + 1 + i0 + 32 * u];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u)
+          if (i0 + 32 * u < m) cj[k + 1 + i0 + 32 * u] = val[u] - sv[i0 + 32 * u] * f;
+      }
     }
     __syncthreads();
   }
@@ -242,7 +287,7 @@ template <class R> __device__ __forceinline__ Rot<R> chase_reflector(Cx<R> alpha
 }
 
 template <class R>
-__global__ void __launch_bounds__(EIG_THREADS) hseqr_kernel(Cx<R>* __restrict__ Hall, int n, int ldh,
+__global__ void __launch_bounds__(1024) hseqr_kernel(Cx<R>* __restrict__ Hall, int n, int ldh,
                                                             long long h_bs, Cx<R>* __restrict__ Zall, int ldz,
                                                             long long z_bs, Cx<R>* __restrict__ w_all,
                                                             int32_t* __restrict__ status, int st_div, int itmax) {
@@ -250,14 +295,15 @@ __global__ void __launch_bounds__(EIG_THREADS) hseqr_kernel(Cx<R>* __restrict__ 
   extern __shared__ __align__(16) unsigned char smraw[];
   C_* sphase = reinterpret_cast<C_*>(smraw);
   __shared__ int ired[32];
-  __shared__ C_ s_t1, s_v2, s_v0, s_sc;
-  __shared__ R s_t2, s_v1;
+  __shared__ C_ s_t1[2], s_v2[2], s_sc;
+  __shared__ R s_t2[2];
   __shared__ int s_done;
+  constexpr int kChunk = sizeof(R) <= 4 ? 4 : 2;   // worker items whose loads are issued together
   C_* H = Hall + blockIdx.x * h_bs;
   C_* Z = Zall + blockIdx.x * z_bs;
   C_* w = w_all + (long long)blockIdx.x * n;
   int32_t* st = status ? status + blockIdx.x / st_div : nullptr;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, warp = tid >> 5;
   const R ulp = RealT<R>::eps();
   const R smlnum = RealT<R>::tiny() * (R((double)n) / ulp);
   auto h = [&](int i, int j) -> C_& { return H[i + (long long)j * ldh]; };
@@ -349,40 +395,82 @@ __global__ void __launch_bounds__(EIG_THREADS) hseqr_kernel(Cx<R>* __restrict__ 
         R sc = cxabs1(h11s) + rabs(h21);
         if (sc == R(0.0)) sc = R(1.0);
         R isc = R(1.0) / sc;
-        s_v0 = h11s * isc;
-        s_v1 = h21 * isc;
+        // the first reflector of the sweep, from the shifted first column
+        Rot<R> rf = chase_reflector(h11s * isc, h21 * isc);
+        s_t1[l & 1] = rf.t1; s_v2[l & 1] = rf.v2; s_t2[l & 1] = rf.t2;
       }
       __syncthreads();
+      // Bulge chase, one CTA barrier per step. Reflector k acts on rows/columns (k, k+1). The core
+      // lane (thread 0) owns the elements where its left and right applications meet -- rows
+      // k..min(k+2, i) of columns k, k+1 -- and, having updated them, builds reflector k+1 from
+      // its own (k+1, k), (k+2, k) and publishes it (double-buffered in shared memory). The worker
+      // warps (all but warp 0) apply reflector k everywhere else, in one phase, since those
+      // elements are disjoint: rows k, k+1 of columns k+2..n-1 (left), rows 0..k-1 of columns
+      // k, k+1 (right) and Z's columns k, k+1. Each worker issues the loads of up to kChunk items
+      // before it updates any, so that one memory latency serves the chunk.
       for (int k = l; k < i; ++k) {
-        if (tid == 0) {
-          C_ a0; R a1;
-          if (k > l) { a0 = h(k, k - 1); a1 = h(k + 1, k - 1).x; } else { a0 = s_v0; a1 = s_v1; }
-          Rot<R> rf = chase_reflector(a0, a1);
-          if (k > l) { h(k, k - 1) = rf.identity ? a0 : cxmk<R>(rf.beta, R(0.0)); h(k + 1, k - 1) = cxzero<R>(); }
-          s_t1 = rf.t1; s_v2 = rf.v2; s_t2 = rf.t2;
-        }
-        __syncthreads();
-        const C_ t1 = s_t1, v2 = s_v2;
-        const R t2 = s_t2;
+        const int sl = k & 1;
+        const C_ t1 = s_t1[sl], v2 = s_v2[sl];
+        const R t2 = s_t2[sl];
         const C_ t1c = cxconj(t1), v2c = cxconj(v2);
-        // left: rows k, k+1, columns k..n-1
-        for (int j = k + tid; j < n; j += blockDim.x) {
-          C_ a = h(k, j), b = h(k + 1, j);
-          C_ sum = t1c * a + b * t2;
-          h(k, j) = a - sum;
-          h(k + 1, j) = b - sum * v2;
-        }
-        __syncthreads();
-        // right: columns k, k+1, rows 0..min(k+2, i); and Z rows 0..n-1
-        const int rlast = min(k + 2, i);
-        for (int e = tid; e <= rlast + n; e += blockDim.x) {
-          C_* pa; C_* pb;
-          if (e <= rlast) { pa = &h(e, k); pb = &h(e, k + 1); }
-          else { int j = e - rlast - 1; pa = Z + j + (long long)k * ldz; pb = Z + j + (long long)(k + 1) * ldz; }
-          C_ a = *pa, b = *pb;
-          C_ sum = t1 * a + b * t2;
-          *pa = a - sum;
-          *pb = b - sum * v2c;
+        if (warp == 0) {
+          if (tid == 0) {
+            const bool has2 = (k + 2 <= i);
+            C_ h00 = h(k, k), h01 = h(k, k + 1), h10 = h(k + 1, k), h11 = h(k + 1, k + 1);
+            C_ h21 = has2 ? h(k + 2, k + 1) : cxzero<R>();
+            C_ sum = t1c * h00 + h10 * t2;             // left on columns k, k+1
+            h00 = h00 - sum; h10 = h10 - sum * v2;
+            sum = t1c * h01 + h11 * t2;
+            h01 = h01 - sum; h11 = h11 - sum * v2;
+            sum = t1 * h00 + h01 * t2;                 // right on rows k, k+1, k+2
+            h00 = h00 - sum; h01 = h01 - sum * v2c;
+            sum = t1 * h10 + h11 * t2;
+            h10 = h10 - sum; h11 = h11 - sum * v2c;
+            sum = h21 * t2;                            // (k+2, k) is zero before this step
+            C_ h20 = -sum;
+            h21 = h21 - sum * v2c;
+            h(k, k) = h00; h(k, k + 1) = h01; h(k + 1, k + 1) = h11;
+            if (has2) h(k + 2, k + 1) = h21;
+            if (k + 1 < i) {
+              Rot<R> rn = chase_reflector(h10, h20.x);
+              h(k + 1, k) = rn.identity ? h10 : cxmk<R>(rn.beta, R(0.0));
+              h(k + 2, k) = cxzero<R>();
+              s_t1[sl ^ 1] = rn.t1; s_v2[sl ^ 1] = rn.v2; s_t2[sl ^ 1] = rn.t2;
+            } else {
+              h(k + 1, k) = h10;
+              if (has2) h(k + 2, k) = h20;
+            }
+          }
+        } else {
+          const int wt = blockDim.x - 32, wid = tid - 32;
+          const int nL = max(0, n - (k + 2)), nR = k, total = nL + nR + n;
+          for (int base = wid; base < total; base += kChunk * wt) {
+            C_* pa[kChunk];
+            C_* pb[kChunk];
+            C_ a[kChunk], b[kChunk];
+#pragma unroll
+            for (int u = 0; u < kChunk; ++u) {
+              int e = base + u * wt;
+              if (e < nL) { pa[u] = &h(k, k + 2 + e); pb[u] = pa[u] + 1; }
+              else if (e < nL + nR) { e -= nL; pa[u] = &h(e, k); pb[u] = &h(e, k + 1); }
+              else if (e < total) { e -= nL + nR; pa[u] = Z + e + (long long)k * ldz; pb[u] = pa[u] + ldz; }
+              else { pa[u] = nullptr; pb[u] = nullptr; }
+            }
+#pragma unroll
+            for (int u = 0; u < kChunk; ++u)
+              if (pa[u]) { a[u] = *pa[u]; b[u] = *pb[u]; }
+#pragma unroll
+            for (int u = 0; u < kChunk; ++u) {
+              if (!pa[u]) continue;
+              if (base + u * wt < nL) {
+                const C_ sum = t1c * a[u] + b[u] * t2;
+                *pa[u] = a[u] - sum; *pb[u] = b[u] - sum * v2;
+              } else {
+                const C_ sum = t1 * a[u] + b[u] * t2;
+                *pa[u] = a[u] - sum; *pb[u] = b[u] - sum * v2c;
+              }
+            }
+          }
         }
         __syncthreads();
       }
@@ -493,6 +581,29 @@ __global__ void normalize_columns_kernel(Cx<R>* __restrict__ Wall, int n, int ld
   for (int r = lane; r < n; r += 32) c[r] = c[r] * inv;
 }
 
+// Threads of one QR-sweep CTA. A bulge step has about 2n independent element pairs to update,
+// one memory latency deep; the fewer matrices share an SM, the more threads each needs to keep
+// enough loads in flight. The tunable WB_TUNE_QR_THREADS overrides the choice (the autotuner sets it).
+int qr_threads(int batch, int n) {
+  const int forced = tuning(kTuneQrThreads);
+  if (forced >= 64 && forced <= 1024 && forced % 32 == 0) return forced;
+  const int per_sm = (batch + sm_count() - 1) / sm_count();
+  int t = per_sm <= 1 ? 1024 : per_sm <= 2 ? 512 : 256;
+  while (t > 128 && t / 2 >= 2 * n) t /= 2;       // small matrices: no idle warps
+  return t;
+}
+
+// Threads of one Hessenberg-reduction (and Q-forming) CTA: one warp per trailing column, so as
+// many warps as fit when few matrices share an SM. WB_TUNE_HRD_THREADS overrides the choice.
+int hrd_threads(int batch, int n) {
+  const int forced = tuning(kTuneHrdThreads);
+  if (forced >= 64 && forced <= 1024 && forced % 32 == 0) return forced;
+  const int per_sm = (batch + sm_count() - 1) / sm_count();
+  int t = per_sm <= 1 ? 1024 : per_sm <= 2 ? 512 : 256;
+  while (t > 128 && t / 32 > n) t /= 2;
+  return t;
+}
+
 template <class R>
 void geev_schur(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a_bs, Cx<R>* Z, int ldz,
                 long long z_bs, Cx<R>* w, Cx<R>* tau, int32_t* status, int st_div) {
@@ -500,13 +611,14 @@ void geev_schur(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a
   size_t sm = 2 * (size_t)n * sizeof(Cx<R>);
   cudaFuncSetAttribute(gehrd_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   cudaFuncSetAttribute(unghr_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  gehrd_kernel<R><<<batch, EIG_THREADS, sm, s>>>(A, n, lda, a_bs, tau); note_launch();
-  unghr_kernel<R><<<batch, EIG_THREADS, sm, s>>>(A, n, lda, a_bs, tau, Z, ldz, z_bs); note_launch();
+  const int th = hrd_threads(batch, n);
+  gehrd_kernel<R><<<batch, th, sm, s>>>(A, n, lda, a_bs, tau); note_launch();
+  unghr_kernel<R><<<batch, th, sm, s>>>(A, n, lda, a_bs, tau, Z, ldz, z_bs); note_launch();
   int itmax = 30 * (n > 10 ? n : 10);
   size_t sm2 = (size_t)n * sizeof(Cx<R>);
   cudaFuncSetAttribute(hseqr_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
-  hseqr_kernel<R><<<batch, EIG_THREADS, sm2, s>>>(A, n, lda, a_bs, Z, ldz, z_bs, w, status, st_div < 1 ? 1 : st_div,
-                                                  itmax); note_launch();
+  hseqr_kernel<R><<<batch, qr_threads(batch, n), sm2, s>>>(A, n, lda, a_bs, Z, ldz, z_bs, w, status,
+                                                           st_div < 1 ? 1 : st_div, itmax); note_launch();
 }
 
 template <class R>

@@ -9,6 +9,15 @@ namespace wb {
 void note_launch();
 long long launch_count();
 
+// Launch-shape tunables (process-wide; 0 = the library's own choice). Set through
+// wb_set_tuning by the autotuner; read at every launch.
+// (the same numbers as the public WB_TUNE_* keys)
+enum TuneKey { kTuneQrThreads = 0, kTuneHrdThreads = 1, kTuneLuThreads = 2, kTuneKeys = 8 };
+int tuning(int key);
+void set_tuning(int key, int value);
+// multiprocessor count of the current device (cached per device)
+int sm_count();
+
 // ---- dense linear algebra (wb_linalg.cu)
 void zgemm(cudaStream_t s, int batch, int m, int n, int k, cplx alpha,
            const cplx* A, long long a_rs, long long a_cs, long long a_bs,
@@ -20,6 +29,11 @@ void zgetrf(cudaStream_t s, int batch, int n, cplx* A, int lda, long long a_bs, 
 void zgetrs(cudaStream_t s, int batch, int n, const cplx* LU, int lda, long long a_bs,
             const int* ipiv, long long piv_bs, cplx* B, int nrhs, int ldb, long long b_bs, int trans);
 void zset_identity(cudaStream_t s, int batch, int n, cplx* A, int lda, long long a_bs);
+// C = alpha A B + beta C of FP64 operands with double-float accumulation on the FP32 pipes
+// (about 2^-48 unit roundoff); A of batch entry z at A + (a_idx ? a_idx[z] : z) * a_bs
+void zgemm_dd_idx(cudaStream_t s, int batch, int m, int n, int k, double2 alpha, const cplx* A, long long a_rs,
+                  long long a_cs, long long a_bs, const int* a_idx, const cplx* B, long long b_rs, long long b_cs,
+                  long long b_bs, double2 beta, cplx* C, long long c_rs, long long c_cs, long long c_bs);
 
 // templated over R in {double, float, df64}; alpha/beta are passed as doubles
 template <class R>

@@ -166,6 +166,131 @@ void gemm_idx(cudaStream_t s, int batch, int m, int n, int k, double2 alpha,
                                       c_cs, c_bs, a_idx); note_launch();
 }
 
+// ------------------------------------------------- FP64 products accumulated in double-float
+// C = alpha A B + beta C for FP64 (complex128) operands, with the products and sums carried in
+// double-float arithmetic on the FP32 pipes instead of the FP64 ones: each operand is split on
+// load into hi + lo FP32 words (48 significant bits), and each real product-accumulate is
+//   p = ah bh (rounded), e = fma(ah, bh, -p) + ah bl + al bh       (Dekker's product; al bl dropped)
+//   hi + err = hi + p exactly (Knuth's two-sum),  lo += err + e
+// with one renormalisation of (hi, lo) per K tile. About 12 FP32 instructions per real
+// multiply-add against one FP64 instruction, on pipes 64x wider on GB300: about 5x the DFMA rate
+// at a unit roundoff of about 2^-48 (the error grows like K 2^-48 of sum |a||b| in the worst case).
+// Used by the mixed form for the products whose results must be FP64-accurate (the Newton
+// residual Omega^2 W and V = Omega_R W), never by the plain FP64 form.
+namespace {
+struct DD { float hi, lo; };
+__device__ __forceinline__ void dd_mac(DD& acc, float ah, float al, float bh, float bl) {
+  const float p = __fmul_rn(ah, bh);
+  float e = __fmaf_rn(ah, bh, -p);
+  e = __fmaf_rn(ah, bl, e);
+  e = __fmaf_rn(al, bh, e);
+  const float s = __fadd_rn(acc.hi, p);
+  const float bb = __fsub_rn(s, acc.hi);
+  const float err = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  acc.hi = s;
+  acc.lo = __fadd_rn(acc.lo, __fadd_rn(err, e));
+}
+__device__ __forceinline__ void dd_norm(DD& a) {
+  const float s = __fadd_rn(a.hi, a.lo);
+  a.lo = __fsub_rn(a.lo, __fsub_rn(s, a.hi));
+  a.hi = s;
+}
+// (re.hi, re.lo, im.hi, im.lo) of an FP64 complex value
+__device__ __forceinline__ float4 dd_split(double2 v) {
+  const float rh = (float)v.x, ih = (float)v.y;
+  return make_float4(rh, (float)(v.x - (double)rh), ih, (float)(v.y - (double)ih));
+}
+}  // namespace
+
+__global__ void __launch_bounds__(256) gemm_dd_kernel(
+    int m, int n, int k, double2 alpha, const double2* __restrict__ A, long long a_rs, long long a_cs,
+    long long a_bs, const int* __restrict__ a_idx, const double2* __restrict__ B, long long b_rs, long long b_cs,
+    long long b_bs, double2 beta, double2* __restrict__ C, long long c_rs, long long c_cs, long long c_bs) {
+  __shared__ float4 sA[GK][GT + 1];
+  __shared__ float4 sB[GK][GT + 1];
+  const int bz = blockIdx.z;
+  A += (a_idx ? (long long)a_idx[bz] : (long long)bz) * a_bs; B += bz * b_bs; C += bz * c_bs;
+  const int row0 = blockIdx.x * GT, col0 = blockIdx.y * GT;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  DD re[4][4], im[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) { re[i][j] = DD{0.f, 0.f}; im[i][j] = DD{0.f, 0.f}; }
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int k0 = 0; k0 < k; k0 += GK) {
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int idx = tid + e * 256;
+      const int r = idx % GT, c = idx / GT;
+      const int gr = row0 + r, gc = k0 + c;
+      sA[c][r] = (gr < m && gc < k) ? dd_split(A[gr * a_rs + gc * a_cs]) : zero4;
+    }
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int idx = tid + e * 256;
+      const int r = idx % GK, c = idx / GK;
+      const int gr = k0 + r, gc = col0 + c;
+      sB[r][c] = (gr < k && gc < n) ? dd_split(B[gr * b_rs + gc * b_cs]) : zero4;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GK; ++kk) {
+      float4 a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = sA[kk][tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = sB[kk][ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          // (ar + i ai)(br + i bi): re += ar br - ai bi, im += ar bi + ai br
+          dd_mac(re[i][j], a[i].x, a[i].y, b[j].x, b[j].y);
+          dd_mac(re[i][j], -a[i].z, -a[i].w, b[j].z, b[j].w);
+          dd_mac(im[i][j], a[i].x, a[i].y, b[j].z, b[j].w);
+          dd_mac(im[i][j], a[i].z, a[i].w, b[j].x, b[j].y);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) { dd_norm(re[i][j]); dd_norm(im[i][j]); }
+    __syncthreads();
+  }
+  const bool zero_beta = (beta.x == 0.0 && beta.y == 0.0);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gr = row0 + tx + 16 * i;
+    if (gr >= m) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gc = col0 + ty + 16 * j;
+      if (gc >= n) continue;
+      double2* p = C + gr * c_rs + gc * c_cs;
+      const double2 v = make_double2((double)re[i][j].hi + (double)re[i][j].lo,
+                                     (double)im[i][j].hi + (double)im[i][j].lo);
+      double2 o = make_double2(alpha.x * v.x - alpha.y * v.y, alpha.x * v.y + alpha.y * v.x);
+      if (!zero_beta) {
+        const double2 c = *p;
+        o.x += beta.x * c.x - beta.y * c.y;
+        o.y += beta.x * c.y + beta.y * c.x;
+      }
+      *p = o;
+    }
+  }
+}
+
+void zgemm_dd_idx(cudaStream_t s, int batch, int m, int n, int k, double2 alpha, const cplx* A, long long a_rs,
+                  long long a_cs, long long a_bs, const int* a_idx, const cplx* B, long long b_rs, long long b_cs,
+                  long long b_bs, double2 beta, cplx* C, long long c_rs, long long c_cs, long long c_bs) {
+  if (batch <= 0 || m <= 0 || n <= 0) return;
+  dim3 grid((m + GT - 1) / GT, (n + GT - 1) / GT, batch);
+  gemm_dd_kernel<<<grid, 256, 0, s>>>(m, n, k, alpha, A, a_rs, a_cs, a_bs, a_idx, B, b_rs, b_cs, b_bs, beta, C,
+                                      c_rs, c_cs, c_bs);
+  note_launch();
+}
+
 // ----------------------------------------------------------------------- LU factorisation
 // One CTA per matrix, right-looking, panel width LU_NB. Pivot choice is the largest |re|+|im|
 // in the column (the LAPACK izamax measure). Row swaps are applied across the full width.

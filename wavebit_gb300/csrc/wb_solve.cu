@@ -38,6 +38,26 @@ static unsigned long long g_launches = 0;
 void note_launch() { __atomic_add_fetch(&g_launches, 1ULL, __ATOMIC_RELAXED); }
 long long launch_count() { return (long long)__atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 
+static int g_tuning[kTuneKeys] = {0};
+int tuning(int key) { return (key >= 0 && key < kTuneKeys) ? __atomic_load_n(&g_tuning[key], __ATOMIC_RELAXED) : 0; }
+void set_tuning(int key, int value) {
+  if (key >= 0 && key < kTuneKeys) __atomic_store_n(&g_tuning[key], value, __ATOMIC_RELAXED);
+}
+int sm_count() {
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) { cudaGetLastError(); return 148; }
+  if (!cached[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) {
+      cudaGetLastError();
+      v = 148;
+    }
+    cached[dev] = v;
+  }
+  return cached[dev];
+}
+
 // --------------------------------------------------------------------------- ports
 // Per solve: order wavevectors, per-order s/p frame, half-space kz, gap waves and the diagonal
 // S blocks of the superstrate->gap and gap->substrate interfaces. The incident wavevector is
@@ -737,6 +757,30 @@ __global__ void omw_resid_kernel(long long total, int N, int n, const int* __res
   R[idx] = cxmk<float>((float)res.x, (float)res.y);
 }
 
+// V = Omega_R W / q from the products T = epy W_bot and U = epx W_top (solve_2d.py:2393-2448):
+//   V_top = -T - diag(kx ky) W_top + diag(kx^2) W_bot,  V_bot = U - diag(ky^2) W_top + diag(ky kx) W_bot
+__global__ void vmodes_epilogue_kernel(long long total, int N, int n, const int* __restrict__ pair_solve,
+                                       const double* __restrict__ kx, const double* __restrict__ ky,
+                                       const cplx* __restrict__ T, const cplx* __restrict__ U,
+                                       const cplx* __restrict__ W, const cplx* __restrict__ q, cplx* __restrict__ V) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= total) return;
+  const long long n2 = (long long)n * n, Nn = (long long)N * n;
+  const long long p = idx / n2, rem = idx % n2;
+  const int r = (int)(rem % n), j = (int)(rem / n);
+  const bool top = r < N;
+  const int i = top ? r : r - N;
+  const long long o = (long long)pair_solve[p] * N + i;
+  const double a = kx[o], b = ky[o];
+  const cplx* Wp = W + p * n2;
+  const cplx wt = Wp[i + (long long)j * n], wb = Wp[N + i + (long long)j * n];
+  const long long h = p * Nn + i + (long long)j * N;
+  cplx v;
+  if (top) v = cadd(cneg(T[h]), cadd(cscale(wt, -(a * b)), cscale(wb, a * a)));
+  else v = cadd(U[h], cadd(cscale(wt, -(b * b)), cscale(wb, b * a)));
+  V[idx] = cdiv(v, q[p * n + j]);
+}
+
 // every slot a diagonal 32 x 32 block with distinct entries, so unused slots converge at once
 __global__ void group_init_kernel(int cap, cplx* __restrict__ A, int* __restrict__ count) {
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -1035,13 +1079,15 @@ void stage_b_newton(cudaStream_t s, int P, int N, const cplx* conv, const int* p
     if (it > 0) convert<double, float>(s, (const Cx<double>*)Wd, nb.F1, tot);
     cudaMemcpyAsync(nb.F2, nb.F1, sizeof(F) * tot, cudaMemcpyDeviceToDevice, s);   // W in FP32 for W E
     getrf<float>(s, P, n, nb.F1, n, n2, nb.piv, n, st, st_div);                    // LU of W in FP32
-    const Cx<double>* Wc = (const Cx<double>*)Wd;
-    gemm_idx<double>(s, P, N, n, N, one, cv, 1, N, 3 * NN, pair_layer, Wc, 1, n, n2, zero, Tm, 1, N, Nn);
-    gemm_idx<double>(s, P, N, n, N, one, cv + NN, 1, N, 3 * NN, pair_layer, Wc + N, 1, n, n2, zero, Um, 1, N, Nn);
+    // the residual's three slot products, FP64 operands accumulated in double-float (FP32 pipes)
+    zgemm_dd_idx(s, P, N, n, N, one, conv, 1, N, 3 * NN, pair_layer, Wd, 1, n, n2, zero, (cplx*)Tm, 1, N, Nn);
+    zgemm_dd_idx(s, P, N, n, N, one, conv + NN, 1, N, 3 * NN, pair_layer, Wd + N, 1, n, n2, zero, (cplx*)Um, 1, N,
+                 Nn);
     omw_s_kernel<<<nblk(totN, 256), 256, 0, s>>>(totN, N, n, pair_solve, kx, ky, (const cplx*)Tm, (const cplx*)Um,
                                                  (cplx*)Sm);
     note_launch();
-    gemm_idx<double>(s, P, N, n, N, one, cv + 2 * NN, 1, N, 3 * NN, pair_layer, Sm, 1, N, Nn, zero, Ym, 1, N, Nn);
+    zgemm_dd_idx(s, P, N, n, N, one, conv + 2 * NN, 1, N, 3 * NN, pair_layer, (const cplx*)Sm, 1, N, Nn, zero,
+                 (cplx*)Ym, 1, N, Nn);
     omw_resid_kernel<<<nblk(tot, 256), 256, 0, s>>>(tot, N, n, pair_solve, kx, ky, (const cplx*)Tm, (const cplx*)Um,
                                                     (const cplx*)Ym, Wd, nb.lam, nb.F4);
     note_launch();
@@ -1069,12 +1115,13 @@ void stage_b_newton(cudaStream_t s, int P, int N, const cplx* conv, const int* p
   // q, X, V and the s/p rotation in FP64, then the double-float form the cascade reads
   modeq_kernel<double><<<P, 256, 0, s>>>(P, n, (const Cx<double>*)nb.lam, pair_solve, pair_thick, wavelength, w, q, X, st);
   note_launch();
-  {
-    dim3 gr((N + 63) / 64, (n + 63) / 64, P * 2);
-    vmodes_kernel<double><<<gr, 256, 0, s>>>(N, conv, 3 * NN, pair_layer, pair_solve, kx, ky, (const Cx<double>*)Wd, q,
-                                             (Cx<double>*)Vd, n2);
-    note_launch();
-  }
+  // V = Omega_R W / q: the two slot products in double-float (T = epy W_bot, U = epx W_top into
+  // the residual's scratch), the diagonal terms and the division by q elementwise
+  zgemm_dd_idx(s, P, N, n, N, one, conv + NN, 1, N, 3 * NN, pair_layer, Wd + N, 1, n, n2, zero, (cplx*)Tm, 1, N, Nn);
+  zgemm_dd_idx(s, P, N, n, N, one, conv, 1, N, 3 * NN, pair_layer, Wd, 1, n, n2, zero, (cplx*)Um, 1, N, Nn);
+  vmodes_epilogue_kernel<<<nblk(tot, 256), 256, 0, s>>>(tot, N, n, pair_solve, kx, ky, (const cplx*)Tm, (const cplx*)Um,
+                                                        Wd, q, Vd);
+  note_launch();
   sp_rotate_kernel<double><<<nblk((long long)P * N * n, 256), 256, 0, s>>>(P, N, pair_solve, c, sn, (Cx<double>*)Wd,
                                                                           (Cx<double>*)Vd, n2);
   note_launch();
