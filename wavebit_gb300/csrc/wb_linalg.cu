@@ -432,12 +432,244 @@ __global__ void __launch_bounds__(LU_THREADS) getrf_kernel(
   }
 }
 
+// ------------------------------------------------ LU across the GPU for small batches
+// When a batch holds fewer matrices than the GPU has room for (the cascade factors one layer of
+// every solve at a time), one CTA per matrix leaves most SMs idle. The blocked right-looking LU
+// then runs as three launches per panel of LU_PB columns:
+//   lu_panel_kernel      one CTA per matrix: partial pivoting down the panel, swaps inside it
+//   lu_swap_trsm_kernel  one thread per column outside the panel: the panel's row swaps, then
+//                        U12 = L11^-1 A12 for the trailing columns
+//   lu_update_kernel     A22 -= L21 U12 in 64 x 64 tiles over every SM
+// The pivots are the single-CTA kernel's (largest |re| + |im|, first index on ties).
+constexpr int LU_PB = 32;            // panel width
+constexpr int LU_PANEL_THREADS = 1024;
+
+namespace {
+__device__ __forceinline__ double lu_shfl_down(double v, int o) { return __shfl_down_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ float lu_shfl_down(float v, int o) { return __shfl_down_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ df64 lu_shfl_down(df64 v, int o) {
+  return df64(__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o));
+}
+__device__ __forceinline__ double lu_shfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ float lu_shfl(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ df64 lu_shfl(df64 v, int src) {
+  return df64(__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src));
+}
+// (value, index) maximum over the block; ties go to the smaller index
+template <class R>
+__device__ void lu_block_argmax(R v, int idx, R* wv, int* wi, R& out_v, int& out_i) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    R ov = lu_shfl_down(v, o);
+    int oi = __shfl_down_sync(0xffffffffu, idx, o);
+    if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+  }
+  if (lane == 0) { wv[warp] = v; wi[warp] = idx; }
+  __syncthreads();
+  if (warp == 0) {
+    v = lane < nw ? wv[lane] : R(-1.0);
+    idx = lane < nw ? wi[lane] : 0x7fffffff;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      R ov = lu_shfl_down(v, o);
+      int oi = __shfl_down_sync(0xffffffffu, idx, o);
+      if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+    }
+    if (lane == 0) { wv[0] = v; wi[0] = idx; }
+  }
+  __syncthreads();
+  out_v = wv[0]; out_i = wi[0];
+  __syncthreads();
+}
+}  // namespace
+
+template <class R>
+__global__ void __launch_bounds__(LU_PANEL_THREADS) lu_panel_kernel(
+    Cx<R>* __restrict__ Aall, int n, int lda, long long a_bs, int* __restrict__ ipiv_all, long long piv_bs,
+    int32_t* __restrict__ status, int st_div, int k0, int kb) {
+  using C_ = Cx<R>;
+  __shared__ R wv[32];
+  __shared__ int wi[32];
+  __shared__ C_ prow[LU_PB];
+  C_* A = Aall + blockIdx.x * a_bs;
+  int* ipiv = ipiv_all + (long long)blockIdx.x * piv_bs;
+  int32_t* st = status ? status + blockIdx.x / st_div : nullptr;
+  const int tid = threadIdx.x;
+  auto a = [&](int i, int j) -> C_& { return A[i + (long long)j * lda]; };
+  for (int j = k0; j < k0 + kb; ++j) {
+    R best = R(-1.0); int bi = j;
+    for (int i = j + tid; i < n; i += blockDim.x) {
+      const R v = cxabs1(a(i, j));
+      if (v > best) { best = v; bi = i; }
+    }
+    R pv; int p;
+    lu_block_argmax<R>(best, bi, wv, wi, pv, p);
+    if (tid == 0) ipiv[j] = p;
+    // swap rows j, p inside the panel; the pivot row to shared memory
+    if (tid < kb) {
+      const int c = k0 + tid;
+      C_ x = a(j, c), y = a(p, c);
+      if (p != j) { a(j, c) = y; a(p, c) = x; }
+      prow[tid] = (p != j) ? y : x;
+    }
+    __syncthreads();
+    const C_ piv = prow[j - k0];
+    if (piv.x == R(0.0) && piv.y == R(0.0)) {
+      if (tid == 0) wb_flag(st, WB_ST_SINGULAR);
+      continue;
+    }
+    const C_ rp = cxinv(piv);
+    const int ce = k0 + kb;
+    for (int i = j + 1 + tid; i < n; i += blockDim.x) {
+      const C_ l = a(i, j) * rp;
+      a(i, j) = l;
+      for (int c0 = j + 1; c0 < ce; c0 += 8) {
+        C_ v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (c0 + u < ce) v[u] = a(i, c0 + u);
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (c0 + u < ce) a(i, c0 + u) = v[u] - l * prow[c0 + u - k0];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// One thread per column c outside the panel [k0, k0 + kb): the panel's row swaps in order, and
+// for trailing columns U12 = L11^-1 A12 (L11 unit lower, from shared memory).
+template <class R>
+__global__ void __launch_bounds__(256) lu_swap_trsm_kernel(Cx<R>* __restrict__ Aall, int n, int lda, long long a_bs,
+                                                           const int* __restrict__ ipiv_all, long long piv_bs, int k0,
+                                                           int kb) {
+  using C_ = Cx<R>;
+  __shared__ C_ sL[LU_PB][LU_PB + 1];
+  __shared__ int sp[LU_PB];
+  C_* A = Aall + blockIdx.y * a_bs;
+  const int* ipiv = ipiv_all + (long long)blockIdx.y * piv_bs;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < kb * kb; e += blockDim.x) {
+    const int r = e % kb, c = e / kb;
+    sL[r][c] = A[k0 + r + (long long)(k0 + c) * lda];
+  }
+  if (tid < kb) sp[tid] = ipiv[k0 + tid];
+  __syncthreads();
+  int c = blockIdx.x * blockDim.x + tid;
+  if (c >= n - kb) return;
+  if (c >= k0) c += kb;                      // skip the panel
+  C_* col = A + (long long)c * lda;
+  for (int j = 0; j < kb; ++j) {
+    const int p = sp[j];
+    if (p != k0 + j) {
+      const C_ x = col[k0 + j], y = col[p];
+      col[k0 + j] = y; col[p] = x;
+    }
+  }
+  if (c < k0) return;
+  C_ x[LU_PB];
+#pragma unroll
+  for (int r = 0; r < LU_PB; ++r)
+    if (r < kb) x[r] = col[k0 + r];
+#pragma unroll
+  for (int r = 1; r < LU_PB; ++r) {
+    if (r >= kb) break;
+    C_ acc = x[r];
+#pragma unroll
+    for (int t = 0; t < LU_PB; ++t)
+      if (t < r) acc = acc - sL[r][t] * x[t];
+    x[r] = acc;
+  }
+#pragma unroll
+  for (int r = 1; r < LU_PB; ++r)
+    if (r < kb) col[k0 + r] = x[r];
+}
+
+// A22 -= L21 U12 on rows and columns [c0, n), K = kb <= LU_PB
+template <class R>
+__global__ void __launch_bounds__(256) lu_update_kernel(Cx<R>* __restrict__ Aall, int n, int lda, long long a_bs,
+                                                        int k0, int kb) {
+  using C_ = Cx<R>;
+  constexpr int KC = 16;                       // K chunk held in shared memory
+  __shared__ C_ sL[KC][GT + 1];
+  __shared__ C_ sU[KC][GT + 1];
+  C_* A = Aall + blockIdx.z * a_bs;
+  const int c0 = k0 + kb;
+  const int row0 = c0 + blockIdx.x * GT, col0 = c0 + blockIdx.y * GT;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  C_ acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = cxzero<R>();
+  for (int q0 = 0; q0 < kb; q0 += KC) {
+    if (q0 > 0) __syncthreads();
+    for (int e = tid; e < GT * KC; e += blockDim.x) {
+      const int r = e % GT, k = e / GT;
+      sL[k][r] = (q0 + k < kb && row0 + r < n) ? A[row0 + r + (long long)(k0 + q0 + k) * lda] : cxzero<R>();
+    }
+    for (int e = tid; e < GT * KC; e += blockDim.x) {
+      const int k = e % KC, c = e / KC;
+      sU[k][c] = (q0 + k < kb && col0 + c < n) ? A[k0 + q0 + k + (long long)(col0 + c) * lda] : cxzero<R>();
+    }
+    __syncthreads();
+    const int kend = min(KC, kb - q0);
+    for (int kk = 0; kk < kend; ++kk) {
+      C_ a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = sL[kk][tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = sU[kk][ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = cxfma(a[i], b[j], acc[i][j]);
+    }
+  }
+  C_ old[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gr = row0 + tx + 16 * i, gc = col0 + ty + 16 * j;
+      if (gr < n && gc < n) old[i][j] = A[gr + (long long)gc * lda];
+    }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gr = row0 + tx + 16 * i, gc = col0 + ty + 16 * j;
+      if (gr < n && gc < n) A[gr + (long long)gc * lda] = old[i][j] - acc[i][j];
+    }
+}
+
 template <class R>
 void getrf(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a_bs, int* ipiv, long long piv_bs,
            int32_t* status, int st_div) {
   if (batch <= 0 || n <= 0) return;
-  getrf_kernel<R><<<batch, LU_THREADS, 0, s>>>(A, n, lda, a_bs, ipiv, piv_bs, status, st_div < 1 ? 1 : st_div);
-  note_launch();
+  st_div = st_div < 1 ? 1 : st_div;
+  if (batch >= 2 * sm_count() || n < 2 * LU_PB) {
+    getrf_kernel<R><<<batch, LU_THREADS, 0, s>>>(A, n, lda, a_bs, ipiv, piv_bs, status, st_div);
+    note_launch();
+    return;
+  }
+  for (int k0 = 0; k0 < n; k0 += LU_PB) {
+    const int kb = min(LU_PB, n - k0);
+    lu_panel_kernel<R><<<batch, LU_PANEL_THREADS, 0, s>>>(A, n, lda, a_bs, ipiv, piv_bs, status, st_div, k0, kb);
+    note_launch();
+    if (n - kb > 0) {
+      dim3 g2((n - kb + 255) / 256, batch);
+      lu_swap_trsm_kernel<R><<<g2, 256, 0, s>>>(A, n, lda, a_bs, ipiv, piv_bs, k0, kb);
+      note_launch();
+    }
+    const int m = n - k0 - kb;
+    if (m > 0) {
+      dim3 g3((m + GT - 1) / GT, (m + GT - 1) / GT, batch);
+      lu_update_kernel<R><<<g3, 256, 0, s>>>(A, n, lda, a_bs, k0, kb);
+      note_launch();
+    }
+  }
 }
 
 // --------------------------------------------------------------------- triangular solves
@@ -568,10 +800,131 @@ __global__ void __launch_bounds__(256) getrs_kernel(
   }
 }
 
+// Few right-hand sides (the cascade's incidence columns): one CTA per matrix holds X = B
+// (n x NC) in shared memory and substitutes 32 rows at a time. Per block: the 32 x 32 diagonal
+// block is staged in shared memory, warp 0 solves it with the block's rows in its lanes
+// (shuffles carry each solved row to the others), then every thread takes rows below (above,
+// going back) and subtracts the block's contribution, reading L (U) down its columns, coalesced.
+constexpr int NS_B = 32;
+constexpr int NS_THREADS = 1024;
+
+template <class R, int NC>
+__global__ void __launch_bounds__(NS_THREADS) getrs_narrow_kernel(
+    const Cx<R>* __restrict__ LUall, int n, int lda, long long a_bs, const int* __restrict__ ipiv_all,
+    long long piv_bs, Cx<R>* __restrict__ Ball, int nrhs, int ldb, long long b_bs) {
+  using C_ = Cx<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C_* X = reinterpret_cast<C_*>(smraw);            // (n, NC), row-major
+  __shared__ C_ sD[NS_B][NS_B + 1];
+  const C_* LU = LUall + blockIdx.x * a_bs;
+  const int* ipiv = ipiv_all + (long long)blockIdx.x * piv_bs;
+  C_* B = Ball + blockIdx.x * b_bs;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int e = tid; e < n * NC; e += blockDim.x) {
+    const int r = e % n, c = e / n;
+    X[r * NC + c] = (c < nrhs) ? B[r + (long long)c * ldb] : cxzero<R>();
+  }
+  __syncthreads();
+  if (tid < nrhs) {                                // the row swaps, in order, one column each
+    for (int j = 0; j < n; ++j) {
+      const int p = ipiv[j];
+      if (p != j) { const C_ t = X[j * NC + tid]; X[j * NC + tid] = X[p * NC + tid]; X[p * NC + tid] = t; }
+    }
+  }
+  for (int sweep = 0; sweep < 2; ++sweep) {
+    const bool fwd = sweep == 0;                   // L (unit lower), then U (upper)
+    const int nblk = (n + NS_B - 1) / NS_B;
+    for (int bi = 0; bi < nblk; ++bi) {
+      const int i0 = fwd ? bi * NS_B : max(0, n - (bi + 1) * NS_B);
+      const int ib = fwd ? min(NS_B, n - i0) : (n - bi * NS_B) - i0;
+      __syncthreads();
+      for (int e = tid; e < NS_B * NS_B; e += blockDim.x) {
+        const int r = e % NS_B, c = e / NS_B;
+        sD[r][c] = (r < ib && c < ib) ? LU[i0 + r + (long long)(i0 + c) * lda] : cxzero<R>();
+      }
+      __syncthreads();
+      if (warp == 0) {
+        C_ x[NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) x[c] = lane < ib ? X[(i0 + lane) * NC + c] : cxzero<R>();
+        if (fwd) {
+          for (int t = 0; t < ib; ++t) {
+            const C_ l = sD[lane][t];
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+              C_ xt;
+              xt.x = lu_shfl(x[c].x, t);
+              xt.y = lu_shfl(x[c].y, t);
+              if (lane > t) x[c] = x[c] - l * xt;
+            }
+          }
+        } else {
+          for (int t = ib - 1; t >= 0; --t) {
+            if (lane == t) {
+              const C_ d = sD[t][t];
+#pragma unroll
+              for (int c = 0; c < NC; ++c) x[c] = cxdiv(x[c], d);
+            }
+            const C_ u = sD[lane][t];
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+              C_ xt;
+              xt.x = lu_shfl(x[c].x, t);
+              xt.y = lu_shfl(x[c].y, t);
+              if (lane < t) x[c] = x[c] - u * xt;
+            }
+          }
+        }
+        if (lane < ib) {
+#pragma unroll
+          for (int c = 0; c < NC; ++c) X[(i0 + lane) * NC + c] = x[c];
+        }
+      }
+      __syncthreads();
+      // the block's contribution to the rows still to solve
+      const int rs = fwd ? i0 + ib : 0, re = fwd ? n : i0;
+      for (int i = rs + tid; i < re; i += blockDim.x) {
+        C_ acc[NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) acc[c] = X[i * NC + c];
+        const C_* li = LU + i + (long long)i0 * lda;
+        for (int t = 0; t < ib; ++t) {
+          const C_ l = li[(long long)t * lda];
+#pragma unroll
+          for (int c = 0; c < NC; ++c) acc[c] = acc[c] - l * X[(i0 + t) * NC + c];
+        }
+#pragma unroll
+        for (int c = 0; c < NC; ++c) X[i * NC + c] = acc[c];
+      }
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < n * nrhs; e += blockDim.x) {
+    const int r = e % n, c = e / n;
+    B[r + (long long)c * ldb] = X[r * NC + c];
+  }
+}
+
+template <class R, int NC>
+static bool getrs_narrow(cudaStream_t s, int batch, int n, const Cx<R>* LU, int lda, long long a_bs, const int* ipiv,
+                         long long piv_bs, Cx<R>* B, int nrhs, int ldb, long long b_bs) {
+  const size_t sm = (size_t)n * NC * sizeof(Cx<R>);
+  if (sm > (size_t)200 * 1024) return false;
+  cudaFuncSetAttribute(getrs_narrow_kernel<R, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  getrs_narrow_kernel<R, NC><<<batch, NS_THREADS, sm, s>>>(LU, n, lda, a_bs, ipiv, piv_bs, B, nrhs, ldb, b_bs);
+  note_launch();
+  return true;
+}
+
 template <class R>
 void getrs(cudaStream_t s, int batch, int n, const Cx<R>* LU, int lda, long long a_bs, const int* ipiv,
            long long piv_bs, Cx<R>* B, int nrhs, int ldb, long long b_bs, int trans) {
   if (batch <= 0 || n <= 0 || nrhs <= 0) return;
+  if (trans == 0 && n >= 64 && batch < 4 * sm_count()) {
+    if (nrhs <= 3 && getrs_narrow<R, 3>(s, batch, n, LU, lda, a_bs, ipiv, piv_bs, B, nrhs, ldb, b_bs)) return;
+    if (nrhs > 3 && nrhs <= 6 && getrs_narrow<R, 6>(s, batch, n, LU, lda, a_bs, ipiv, piv_bs, B, nrhs, ldb, b_bs))
+      return;
+  }
   dim3 grid((nrhs + SV_W - 1) / SV_W, batch);
   getrs_kernel<R><<<grid, 256, 0, s>>>(LU, n, lda, a_bs, ipiv, piv_bs, B, nrhs, ldb, b_bs, trans); note_launch();
 }
