@@ -286,8 +286,147 @@ template <class R> __device__ __forceinline__ Rot<R> chase_reflector(Cx<R> alpha
   return r;
 }
 
+// One sweep of the bulge chase with the workers' operands carried in registers (FP32 form).
+// Every worker owns up to kCarry element pairs for the whole sweep, with a step-invariant map:
+// item e < n is row e of Z; item e = n + q is, while q >= k, column q + 2 of H (rows k, k+1:
+// the left update) and, from step q + 1 on, row q of H (columns k, k+1: the right update).
+// An item keeps the value it pairs with this step (cy) and the next one (n1, loaded one step
+// ahead), so a step's critical path holds no memory read: it updates (cy, n1), stores the
+// finished element, keeps the other and issues the load for the next step (an element no step
+// touches in between). The two values that cross between threads go through shared memory,
+// double buffered by step parity: H(k+1, k+2) from column k+2's item to the core lane, and
+// H(k, k+1) from the core to the item of row k as it joins the right update. Results are those of
+// the chunked loop in hseqr_kernel, operation for operation.
+constexpr int kCarry = 4;
+// largest QR-sweep CTA: 85 registers a thread, room for the carried pairs without spills
+constexpr int kQrMaxThreads = 768;
+
 template <class R>
-__global__ void __launch_bounds__(1024) hseqr_kernel(Cx<R>* __restrict__ Hall, int n, int ldh,
+__device__ void chase_sweep_carry(Cx<R>* __restrict__ H, int ldh, Cx<R>* __restrict__ Z, int ldz, int n, int l,
+                                  int i, Cx<R>* s_t1, Cx<R>* s_v2, R* s_t2, Cx<R>* s_c01, Cx<R>* s_h01) {
+  using C_ = Cx<R>;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  auto h = [&](int r, int c) -> C_& { return H[r + (long long)c * ldh]; };
+  const int wt = blockDim.x - 32, wid = tid - 32;
+  const int nitems = 2 * n - 2;
+  const C_ zero = cxzero<R>();
+  C_ cy[kCarry], n1[kCarry];
+  // core lane state: the 2 x 2 block at (k, k) and H(k+2, k+1) in shared memory (so that the
+  // workers' registers are not spent on it); the elements two steps ahead, whose loads are in
+  // flight across a step, in registers
+  __shared__ C_ cs[5];
+  enum { C00, C01, C10, C11, C21 };
+  C_ p22 = zero, p32 = zero;
+  if (warp > 0) {
+#pragma unroll
+    for (int u = 0; u < kCarry; ++u) {
+      const int e = wid + u * wt;
+      cy[u] = zero; n1[u] = zero;
+      if (e >= nitems) continue;
+      if (e < n) {
+        cy[u] = Z[e + (long long)l * ldz]; n1[u] = Z[e + (long long)(l + 1) * ldz];
+      } else {
+        const int q = e - n;
+        if (q < l) { cy[u] = h(q, l); n1[u] = h(q, l + 1); }
+        else { cy[u] = h(l, q + 2); n1[u] = h(l + 1, q + 2); }
+      }
+    }
+  } else if (tid == 0) {
+    cs[C00] = h(l, l); cs[C01] = h(l, l + 1); cs[C10] = h(l + 1, l); cs[C11] = h(l + 1, l + 1);
+    cs[C21] = (l + 2 <= i) ? h(l + 2, l + 1) : zero;
+    if (l + 2 <= i) p22 = h(l + 2, l + 2);
+    if (l + 3 <= i) p32 = h(l + 3, l + 2);
+  }
+  for (int k = l; k < i; ++k) {
+    const int sl = k & 1, sn = sl ^ 1;
+    const C_ t1 = s_t1[sl], v2 = s_v2[sl];
+    const R t2 = s_t2[sl];
+    const C_ t1c = cxconj(t1), v2c = cxconj(v2);
+    if (warp == 0) {
+      if (tid == 0) {
+        const C_ c00 = cs[C00], c10 = cs[C10], c11 = cs[C11], c21 = cs[C21];
+        const C_ c01 = (k > l) ? s_c01[sl] : cs[C01];
+        const bool has2 = (k + 2 <= i);
+        C_ sum = t1c * c00 + c10 * t2;             // left on columns k, k+1
+        C_ h00 = c00 - sum, h10 = c10 - sum * v2;
+        sum = t1c * c01 + c11 * t2;
+        C_ h01 = c01 - sum, h11 = c11 - sum * v2;
+        sum = t1 * h00 + h01 * t2;                 // right on rows k, k+1, k+2
+        h00 = h00 - sum; h01 = h01 - sum * v2c;
+        sum = t1 * h10 + h11 * t2;
+        h10 = h10 - sum; h11 = h11 - sum * v2c;
+        C_ h21 = has2 ? c21 : zero;
+        sum = h21 * t2;
+        const C_ h20 = -sum;
+        h21 = h21 - sum * v2c;
+        h(k, k) = h00; h(k, k + 1) = h01;
+        s_h01[sn] = h01;
+        if (k + 1 < i) {
+          Rot<R> rn = chase_reflector(h10, h20.x);
+          h(k + 1, k) = rn.identity ? h10 : cxmk<R>(rn.beta, R(0.0));
+          h(k + 2, k) = zero;
+          s_t1[sn] = rn.t1; s_v2[sn] = rn.v2; s_t2[sn] = rn.t2;
+          cs[C00] = h11; cs[C10] = h21; cs[C11] = p22; cs[C21] = p32;
+          p22 = (k + 3 <= i) ? h(k + 3, k + 3) : zero;
+          p32 = (k + 4 <= i) ? h(k + 4, k + 3) : zero;
+        } else {
+          h(k + 1, k) = h10; h(k + 1, k + 1) = h11;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < kCarry; ++u) {
+        const int e = wid + u * wt;
+        if (e >= nitems) continue;
+        if (e < n) {                                                   // Z row e
+          const C_ sum = t1 * cy[u] + n1[u] * t2;
+          Z[e + (long long)k * ldz] = cy[u] - sum;
+          cy[u] = n1[u] - sum * v2c;
+          n1[u] = (k + 2 < n) ? Z[e + (long long)(k + 2) * ldz] : zero;
+          continue;
+        }
+        const int q = e - n;
+        if (q < k) {                                                   // H row q, right update
+          if (q == k - 1 && k > l) cy[u] = s_h01[sl];                  // joins: n1 is its own
+          const C_ sum = t1 * cy[u] + n1[u] * t2;
+          h(q, k) = cy[u] - sum;
+          cy[u] = n1[u] - sum * v2c;
+          n1[u] = (k + 2 < n) ? h(q, k + 2) : zero;
+        } else {                                                       // H column q + 2, left update
+          const int j = q + 2;
+          const C_ sum = t1c * cy[u] + n1[u] * t2;
+          const C_ a = cy[u] - sum, b = n1[u] - sum * v2;
+          h(k, j) = a;
+          if (q == k) {              // last left step: H(k+1, k+2) to the core, then rows join
+            h(k + 1, j) = b;
+            s_c01[sn] = b;
+            n1[u] = a;
+          } else {
+            cy[u] = b;
+            n1[u] = (k + 2 < n) ? h(k + 2, j) : zero;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // the carried elements of the last step
+  if (warp > 0) {
+#pragma unroll
+    for (int u = 0; u < kCarry; ++u) {
+      const int e = wid + u * wt;
+      if (e >= nitems) continue;
+      if (e < n) { Z[e + (long long)i * ldz] = cy[u]; continue; }
+      const int q = e - n;
+      if (q < i - 1) h(q, i) = cy[u];
+      else if (q > i - 1) h(i, q + 2) = cy[u];
+    }
+  }
+  __syncthreads();
+}
+
+template <class R>
+__global__ void __launch_bounds__(kQrMaxThreads) hseqr_kernel(Cx<R>* __restrict__ Hall, int n, int ldh,
                                                             long long h_bs, Cx<R>* __restrict__ Zall, int ldz,
                                                             long long z_bs, Cx<R>* __restrict__ w_all,
                                                             int32_t* __restrict__ status, int st_div, int itmax) {
@@ -295,7 +434,7 @@ __global__ void __launch_bounds__(1024) hseqr_kernel(Cx<R>* __restrict__ Hall, i
   extern __shared__ __align__(16) unsigned char smraw[];
   C_* sphase = reinterpret_cast<C_*>(smraw);
   __shared__ int ired[32];
-  __shared__ C_ s_t1[2], s_v2[2], s_sc;
+  __shared__ C_ s_t1[2], s_v2[2], s_sc, s_c01[2], s_h01[2];
   __shared__ R s_t2[2];
   __shared__ int s_done;
   constexpr int kChunk = sizeof(R) <= 4 ? 4 : 2;   // worker items whose loads are issued together
@@ -408,7 +547,9 @@ __global__ void __launch_bounds__(1024) hseqr_kernel(Cx<R>* __restrict__ Hall, i
       // elements are disjoint: rows k, k+1 of columns k+2..n-1 (left), rows 0..k-1 of columns
       // k, k+1 (right) and Z's columns k, k+1. Each worker issues the loads of up to kChunk items
       // before it updates any, so that one memory latency serves the chunk.
-      for (int k = l; k < i; ++k) {
+      const bool carry = sizeof(R) == 4 && 2 * n - 2 <= kCarry * ((int)blockDim.x - 32);
+      if (carry) chase_sweep_carry<R>(H, ldh, Z, ldz, n, l, i, s_t1, s_v2, s_t2, s_c01, s_h01);
+      for (int k = carry ? i : l; k < i; ++k) {
         const int sl = k & 1;
         const C_ t1 = s_t1[sl], v2 = s_v2[sl];
         const R t2 = s_t2[sl];
@@ -584,12 +725,16 @@ __global__ void normalize_columns_kernel(Cx<R>* __restrict__ Wall, int n, int ld
 // Threads of one QR-sweep CTA. A bulge step has about 2n independent element pairs to update,
 // one memory latency deep; the fewer matrices share an SM, the more threads each needs to keep
 // enough loads in flight. The tunable WB_TUNE_QR_THREADS overrides the choice (the autotuner sets it).
-int qr_threads(int batch, int n) {
+int qr_threads(int batch, int n, bool carried) {
   const int forced = tuning(kTuneQrThreads);
-  if (forced >= 64 && forced <= 1024 && forced % 32 == 0) return forced;
+  if (forced >= 64 && forced <= kQrMaxThreads && forced % 32 == 0) return forced;
   const int per_sm = (batch + sm_count() - 1) / sm_count();
-  int t = per_sm <= 1 ? 1024 : per_sm <= 2 ? 512 : 256;
+  int t = per_sm <= 1 ? kQrMaxThreads : per_sm <= 2 ? 512 : 256;
   while (t > 128 && t / 2 >= 2 * n) t /= 2;       // small matrices: no idle warps
+  if (carried) {                                  // enough workers to hold every pair in registers
+    const int need = ((2 * n - 2 + kCarry - 1) / kCarry + 31) / 32 * 32 + 32;
+    if (need <= kQrMaxThreads && need > t) t = need;
+  }
   return t;
 }
 
@@ -617,7 +762,7 @@ void geev_schur(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a
   int itmax = 30 * (n > 10 ? n : 10);
   size_t sm2 = (size_t)n * sizeof(Cx<R>);
   cudaFuncSetAttribute(hseqr_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
-  hseqr_kernel<R><<<batch, qr_threads(batch, n), sm2, s>>>(A, n, lda, a_bs, Z, ldz, z_bs, w, status,
+  hseqr_kernel<R><<<batch, qr_threads(batch, n, sizeof(R) == 4), sm2, s>>>(A, n, lda, a_bs, Z, ldz, z_bs, w, status,
                                                            st_div < 1 ? 1 : st_div, itmax); note_launch();
 }
 
