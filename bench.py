@@ -292,18 +292,23 @@ def hbm_peak():
         return 6800.0, 'fallback 6.8 TB/s'
 
 
-def fp64_peak(torch, dev):
-    """cuBLAS DGEMM 4096^3 rate measured now (the FP64 roofline denominator)."""
-    a = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
-    b = torch.randn_like(a)
-    a @ b
-    torch.cuda.synchronize()
-    best = 0.0
-    for _ in range(3):
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.record(); a @ b; e.record(); e.synchronize()
-        best = max(best, 2 * 4096 ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
-    return best
+#: DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic byte of the QR
+#: sweep, from one small-case capture of each kernel (profiles/hseqr_*); the bench scales its live
+#: algorithmic bytes by it. Absent until captured.
+QR_TRAFFIC_PER_ALGORITHMIC_BYTE = {}
+QR_TRAFFIC_SOURCE = None
+
+
+def qr_profile(handle, real_type):
+    """Summed CUDA-event time, launches and algorithmic bytes of the QR sweeps recorded since
+    wb_profile_qr(1); profiling is switched off again."""
+    import ctypes
+    from wavebit_gb300 import _lib
+    ms, la, by = ctypes.c_double(0), ctypes.c_longlong(0), ctypes.c_double(0)
+    _lib.check(handle.lib.wb_profile_qr_read(real_type, ctypes.byref(ms), ctypes.byref(la), ctypes.byref(by)))
+    _lib.check(handle.lib.wb_profile_qr(0))
+    return {'ms': ms.value, 'launches': la.value, 'bytes': by.value,
+            'type': {0: 'double', 1: 'float', 2: 'df64'}[real_type]}
 
 
 def batch_inputs(cfg, B):
@@ -330,12 +335,17 @@ def profile_calls(args):
     x = batch_inputs(cfg, B)
     inp = E.BatchInputs(x['li'], x['th'], x['wl'], x['per'], x['theta'], x['phi'], x['et'], x['eb'], x['pol'],
                         device=dev)
+    from wavebit_gb300 import _lib
+    h = _lib.handle(0)
+    _lib.check(h.lib.wb_profile_qr(1))
     st = None
     for _ in range(args.profile_calls):
         R, T, st = E.solve_batch(conv, inp, precision=precision)
     torch.cuda.synchronize()
+    qr = qr_profile(h, 0 if precision == 'double' else 1 if precision == 'mixed' else 2)
     print(f'{args.workload} {precision} solves={B} calls={args.profile_calls} '
-          f'status_nonzero={int((st.cpu().numpy() & ~8).astype(bool).sum())}')
+          f'status_nonzero={int((st.cpu().numpy() & ~8).astype(bool).sum())} '
+          f"qr_sweep_{qr['type']}: launches={qr['launches']} ms={qr['ms']:.1f} algorithmic_bytes={qr['bytes']:.6g}")
 
 
 def adjoint_check(args):
@@ -455,6 +465,7 @@ def main():
     barrier()
     stream = torch.cuda.current_stream()
     launches0 = handle.launches()
+    _lib.check(handle.lib.wb_profile_qr(1))       # live CUDA-event timing of the QR sweeps
     clocks = ClockSampler(local)
     clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -466,6 +477,7 @@ def main():
     barrier()
     clk = clocks.stop()
     launches = handle.launches() - launches0
+    qr = qr_profile(handle, 0 if precision == 'double' else 1 if precision == 'mixed' else 2)
     t = ev0.elapsed_time(ev1) / 1e3
     R0, T0 = out[0].clone(), out[1].clone()
     st = out[2].cpu().numpy()
@@ -515,50 +527,30 @@ def main():
             oracle_check['fp64_within_1e-10'] = oracle_check['max_abs_dRT_fp64'] <= 1e-10
         oracle_check['note'] = 'relative to the largest efficiency of the point; columns given (s), pure s, pure p'
 
-    # stage-B (eigen-solve pipeline) timing for the roofline: one wb_layer_modes launch over the
-    # batch's P = B*L (solve, layer) pairs, FP64, on the launching stream
+    # roofline of the dominant kernel, the Schur-form QR sweep of the running form: its launches
+    # timed live with CUDA events on the launching stream over the timed region, against the
+    # measured HBM copy bandwidth (the sweep is bound by moving H and Z, one bulge step at a time)
     roof = None
     if rank == 0:
-        from wavebit_gb300.adjoint import ports
-        P = B * L
-        kxs, kys = [], []
-        for b in range(B):
-            pv = ports(float(x['wl'][b]), cfg['period'], float(x['theta'][b]), 0.0, cfg['eps_top'], cfg['eps_bot'],
-                       hu, hv, 'cpu')
-            for _ in range(L):
-                kxs.append(pv['kx'].numpy()); kys.append(pv['ky'].numpy())
-        kxs, kys = np.array(kxs), np.array(kys)
-        pl = np.tile(np.arange(L), B)
-        E.layer_modes(conv, pl, kxs, kys, handle=handle)   # warm
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        E.layer_modes(conv, pl, kxs, kys, handle=handle)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        tb = e0.elapsed_time(e1) / 1e3
+        hbm, hbm_src = hbm_peak()
         n = 2 * N
-        flops = P * (4 + 100 + 8) * n ** 3            # per pair: Omega^2 4n^3 + eig 100n^3 + V 8n^3
-        issued = P * (4 + 13.3 + 5.3 + 36 + 2.7 + 8 + 4) * n ** 3
-        peak = fp64_peak(torch, dev)
-        roof = {'bound': 'tensor', 'pipe': 'FP64 FMA (DFMA; DMMA issues at the same rate on GB300, so the '
-                'plain form uses DFMA; the roofline is the cuBLAS DGEMM rate measured in this run)',
-                'kernel': 'stage B, FP64: wb_layer_modes (Omega^2 GEMM, Hessenberg, shifted QR, back-substitution, '
-                          'V GEMM)',
-                'achieved': flops / tb / 1e12, 'peak': peak, 'unit': 'TFLOP/s', 'frac': flops / tb / 1e12 / peak,
-                'frac_convention': 'eig counted as 100 n^3 (the survey convention, about 4x the Golub-Van Loan '
-                                   'estimate of a complex Schur form with vectors)',
-                'issued_flops_achieved': issued / tb / 1e12, 'issued_frac': issued / tb / 1e12 / peak,
-                'issued_convention': 'per pair: Omega^2 4 n^3, Hessenberg 13.3 n^3, Q 5.3 n^3, QR sweeps 36 n^3 '
-                                     '(single-shift, about 3 sweeps per eigenvalue), back-substitution 2.7 n^3, '
-                                     'W = Z X 8 n^3, V 4 n^3',
-                'peak_source': 'cuBLAS DGEMM 4096^3 measured in this run (MEASURED_PEAKS.json has no FP64 entry)',
-                'flops_per_launch': flops, 'launch_ms': tb * 1e3, 'pairs_per_launch': P,
-                'traffic': None,
+        achieved = qr['bytes'] / (qr['ms'] * 1e-3) / 1e9 if qr['ms'] > 0 else None
+        per_launch = qr['bytes'] / qr['launches'] if qr['launches'] else None
+        ratio = QR_TRAFFIC_PER_ALGORITHMIC_BYTE.get(qr['type'])
+        roof = {'bound': 'hbm', 'kernel': f"wb::hseqr_kernel<{qr['type']}> (Schur-form QR sweeps, {B * L} "
+                f"matrices of {n}x{n} per launch, one CTA each)",
+                'achieved': achieved, 'peak': hbm, 'unit': 'GB/s', 'frac': achieved / hbm if achieved else None,
+                'peak_source': hbm_src,
+                'algorithmic_bytes_per_launch': per_launch,
+                'bytes_convention': 'every bulge step reads and writes each of its 2n - 2 element pairs\' moving '
+                                    'element once (H row or column, Z row), counted on the device per step',
+                'launch_ms': qr['ms'] / qr['launches'] if qr['launches'] else None, 'launches': qr['launches'],
+                'traffic': per_launch * ratio if (per_launch and ratio) else None,
+                'traffic_source': QR_TRAFFIC_SOURCE if ratio else None,
+                'share_of_step': (qr['ms'] / 1e3) / t if t > 0 else None,
                 'whole_step': {'achieved': (280 * L + 192) * n ** 3 * B / (t / args.steps) / 1e12,
                                'unit': 'TFLOP/s', 'flops_convention': '(280 L + 192) n^3 per solve (the reference '
-                               'formulation; the cascade here does about 53 n^3 per layer against its 168 n^3, so '
-                               'this rate can exceed the peak)'}}
+                               'formulation; the cascade here does about 53 n^3 per layer against its 168 n^3)'}}
 
     # stage A (convolution-matrix assembly of the stack's layers): HBM bytes per layer are the
     # raster read plus the three N x N slots written

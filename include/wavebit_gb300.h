@@ -213,6 +213,16 @@ int wb_set_tuning(int key, int value);
 /* The current value of a tunable (0 = the library's own choice), or -1 for an unknown key. */
 int wb_get_tuning(int key);
 
+/* Live timing of the Schur-form QR sweeps, the eigen-solve's dominant kernel, for measurement:
+ * while enabled, CUDA events are recorded on the launching stream around every sweep launch.
+ * wb_profile_qr(1) clears and enables, wb_profile_qr(0) clears and disables. wb_profile_qr_read
+ * gives, for real type 0 (FP64), 1 (FP32) or 2 (double-float), the summed event time in ms, the
+ * number of launches and their algorithmic bytes (every bulge step moves each of its 2n - 2
+ * element pairs' moving element once, in and out). It synchronises on the recorded events. No
+ * counterpart in the reference. */
+int wb_profile_qr(int enable);
+int wb_profile_qr_read(int real_type, double* ms, long long* launches, double* bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -41,6 +41,8 @@ SIGNATURES = {
     'wb_kernel_launches': (_ll, [_vp]),
     'wb_set_tuning': (_i, [_i, _i]),
     'wb_get_tuning': (_i, [_i]),
+    'wb_profile_qr': (_i, [_i]),
+    'wb_profile_qr_read': (_i, [_i, _vp, _vp, _vp]),
     'wb_assemble_li_noalloc': (_i, [_vp, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     'wb_assemble_li_noalloc_limit': (_sz, []),
 }

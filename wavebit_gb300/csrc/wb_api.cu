@@ -404,4 +404,17 @@ int wb_set_tuning(int key, int value) {
 
 int wb_get_tuning(int key) { return (key >= 0 && key < WB_TUNE_COUNT) ? wb::tuning(key) : -1; }
 
+int wb_profile_qr(int enable) {
+  wb::qr_profile(enable != 0);
+  return cuda_check("wb_profile_qr");
+}
+
+int wb_profile_qr_read(int real_type, double* ms, long long* launches, double* bytes) {
+  if (!ms || !launches || !bytes) return fail(WB_E_INVALID, "wb_profile_qr_read: NULL argument");
+  const int rc = wb::qr_profile_read(real_type, ms, launches, bytes);
+  if (rc == 1) return fail(WB_E_INVALID, "wb_profile_qr_read: real type %d outside 0..2", real_type);
+  if (rc == 2) return cuda_check("wb_profile_qr_read");
+  return WB_OK;
+}
+
 }  // extern "C"

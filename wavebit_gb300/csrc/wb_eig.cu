@@ -13,6 +13,9 @@
 //
 // Every iteration is capped; a matrix that hits the cap gets WB_ST_NOCONV in its status word
 // and NaN eigenvalues, and the kernel returns normally.
+#include <mutex>
+#include <utility>
+#include <vector>
 #include "wb_common.cuh"
 #include "wb_num.cuh"
 #include "wb_kernels.h"
@@ -301,6 +304,16 @@ constexpr int kCarry = 4;
 // largest QR-sweep CTA: 85 registers a thread, room for the carried pairs without spills
 constexpr int kQrMaxThreads = 768;
 
+// Algorithmic bytes of the QR sweeps, per real type (0 double, 1 float, 2 df64): every bulge step
+// reads and writes each of its 2n - 2 element pairs' moving element once (the minimum of the
+// single-shift sweep: Z's row, H's row or column carries the other element), so a step moves
+// 2 (2n - 2) complex values. Each CTA adds its steps' bytes at the end.
+__device__ unsigned long long g_qr_bytes[3];
+template <class R> struct QrSlot;
+template <> struct QrSlot<double> { static constexpr int v = 0; };
+template <> struct QrSlot<float> { static constexpr int v = 1; };
+template <> struct QrSlot<df64> { static constexpr int v = 2; };
+
 template <class R>
 __device__ void chase_sweep_carry(Cx<R>* __restrict__ H, int ldh, Cx<R>* __restrict__ Z, int ldz, int n, int l,
                                   int i, Cx<R>* s_t1, Cx<R>* s_v2, R* s_t2, Cx<R>* s_c01, Cx<R>* s_h01) {
@@ -469,6 +482,7 @@ __global__ void __launch_bounds__(kQrMaxThreads) hseqr_kernel(Cx<R>* __restrict_
   __syncthreads();
   int i = n - 1;
   int total = 0;
+  long long steps = 0;
   bool failed = false;
   while (i >= 0 && !failed) {
     int its = 0;
@@ -503,6 +517,7 @@ __global__ void __launch_bounds__(kQrMaxThreads) hseqr_kernel(Cx<R>* __restrict_
       if (tid == 0 && l > 0) h(l, l - 1) = cxzero<R>();
       if (its >= 60 || total >= itmax) { failed = true; break; }
       ++its; ++total;
+      steps += i - l;
       // --- shift and first reflector vector (thread 0)
       if (tid == 0) {
         C_ t;
@@ -648,6 +663,9 @@ __global__ void __launch_bounds__(kQrMaxThreads) hseqr_kernel(Cx<R>* __restrict_
     for (int j = tid; j <= i; j += blockDim.x) w[j] = cxmk<R>(R(NAN), R(NAN));
     if (tid == 0) wb_flag(st, WB_ST_NOCONV);
   }
+  if (tid == 0)
+    atomicAdd(&g_qr_bytes[QrSlot<R>::v],
+              (unsigned long long)steps * (unsigned long long)(2 * n - 2) * 2ULL * sizeof(C_));
 }
 
 // -------------------------------------------------- 4. eigenvectors of the triangular T
@@ -722,6 +740,47 @@ __global__ void normalize_columns_kernel(Cx<R>* __restrict__ Wall, int n, int ld
   for (int r = lane; r < n; r += 32) c[r] = c[r] * inv;
 }
 
+// Live timing of the QR-sweep launches (per real type), for the benchmark's roofline: CUDA
+// events recorded on the launching stream around every hseqr launch while profiling is on.
+namespace {
+struct QrProfile {
+  bool on = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[3];
+};
+QrProfile g_qrp;
+std::mutex g_qrp_mutex;
+}  // namespace
+
+void qr_profile(bool on) {
+  std::lock_guard<std::mutex> lock(g_qrp_mutex);
+  for (auto& v : g_qrp.ev)
+    for (auto& e : v) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  for (auto& v : g_qrp.ev) v.clear();
+  unsigned long long zero[3] = {0, 0, 0};
+  cudaMemcpyToSymbol(g_qr_bytes, zero, sizeof(zero));
+  g_qrp.on = on;
+}
+
+int qr_profile_read(int slot, double* ms, long long* launches, double* bytes) {
+  if (slot < 0 || slot > 2) return 1;
+  std::lock_guard<std::mutex> lock(g_qrp_mutex);
+  double t = 0.0;
+  for (auto& e : g_qrp.ev[slot]) {
+    float x = 0.f;
+    if (cudaEventSynchronize(e.second) != cudaSuccess || cudaEventElapsedTime(&x, e.first, e.second) != cudaSuccess) {
+      cudaGetLastError();
+      return 2;
+    }
+    t += x;
+  }
+  unsigned long long b[3] = {0, 0, 0};
+  if (cudaMemcpyFromSymbol(b, g_qr_bytes, sizeof(b)) != cudaSuccess) { cudaGetLastError(); return 2; }
+  *ms = t;
+  *launches = (long long)g_qrp.ev[slot].size();
+  *bytes = (double)b[slot];
+  return 0;
+}
+
 // Threads of one QR-sweep CTA. A bulge step has about 2n independent element pairs to update,
 // one memory latency deep; the fewer matrices share an SM, the more threads each needs to keep
 // enough loads in flight. The tunable WB_TUNE_QR_THREADS overrides the choice (the autotuner sets it).
@@ -762,8 +821,19 @@ void geev_schur(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a
   int itmax = 30 * (n > 10 ? n : 10);
   size_t sm2 = (size_t)n * sizeof(Cx<R>);
   cudaFuncSetAttribute(hseqr_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  bool timed = false;
+  {
+    std::lock_guard<std::mutex> lock(g_qrp_mutex);
+    if (g_qrp.on && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
+      timed = true;
+      g_qrp.ev[QrSlot<R>::v].push_back({e0, e1});
+    }
+  }
+  if (timed) cudaEventRecord(e0, s);
   hseqr_kernel<R><<<batch, qr_threads(batch, n, sizeof(R) == 4), sm2, s>>>(A, n, lda, a_bs, Z, ldz, z_bs, w, status,
                                                            st_div < 1 ? 1 : st_div, itmax); note_launch();
+  if (timed) cudaEventRecord(e1, s);
 }
 
 template <class R>

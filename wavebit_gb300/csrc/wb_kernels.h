@@ -17,6 +17,10 @@ int tuning(int key);
 void set_tuning(int key, int value);
 // multiprocessor count of the current device (cached per device)
 int sm_count();
+// live timing of the QR-sweep launches (wb_eig.cu): on/off (clears), and per real type
+// (0 double, 1 float, 2 df64) the summed event time, launches and algorithmic bytes
+void qr_profile(bool on);
+int qr_profile_read(int slot, double* ms, long long* launches, double* bytes);
 
 // ---- dense linear algebra (wb_linalg.cu)
 void zgemm(cudaStream_t s, int batch, int m, int n, int k, cplx alpha,
