@@ -294,9 +294,11 @@ def hbm_peak():
 
 #: DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic byte of the QR
 #: sweep, from one small-case capture of each kernel (profiles/hseqr_*); the bench scales its live
-#: algorithmic bytes by it. Absent until captured.
-QR_TRAFFIC_PER_ALGORITHMIC_BYTE = {}
-QR_TRAFFIC_SOURCE = None
+#: algorithmic bytes by it.
+QR_TRAFFIC_PER_ALGORITHMIC_BYTE = {'float': 643547068928 / 7.58558e11}
+QR_TRAFFIC_SOURCE = ('ncu dram__bytes_read.sum + dram__bytes_write.sum of one hseqr_kernel<float> launch on 4 '
+                     'solves (16 matrices, 643.5 GB against 758.6 GB algorithmic), scaled by the live '
+                     'algorithmic bytes (profiles/hseqr_fp32_orders12_4solves.md)')
 
 
 def qr_profile(handle, real_type):
