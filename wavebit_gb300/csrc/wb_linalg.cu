@@ -916,10 +916,133 @@ static bool getrs_narrow(cudaStream_t s, int batch, int n, const Cx<R>* LU, int 
   return true;
 }
 
+// Many right-hand sides (the cascade's n-column solves): a blocked substitution across the GPU.
+// The row interchanges are applied first (trans 0) or last (trans 1), one thread per column;
+// then, per block of TB_NB rows, trsm_diag_kernel solves the diagonal block for every column
+// (the block and 64 columns in shared memory, one thread per column) and the batched GEMM
+// subtracts the block's contribution from the rows still to solve (K = TB_NB). The
+// substitution order and pivots are those of getrs_kernel; only the summation order differs.
+constexpr int TB_NB = 64;
+constexpr int TB_W = 64;
+
+template <class R>
+__global__ void laswp_kernel(Cx<R>* __restrict__ Ball, int n, int nrhs, int ldb, long long b_bs,
+                             const int* __restrict__ ipiv_all, long long piv_bs, int forward) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nrhs) return;
+  Cx<R>* col = Ball + blockIdx.y * b_bs + (long long)c * ldb;
+  const int* ipiv = ipiv_all + (long long)blockIdx.y * piv_bs;
+  if (forward) {
+    for (int j = 0; j < n; ++j) {
+      const int p = ipiv[j];
+      if (p != j) { const Cx<R> t = col[j]; col[j] = col[p]; col[p] = t; }
+    }
+  } else {
+    for (int j = n - 1; j >= 0; --j) {
+      const int p = ipiv[j];
+      if (p != j) { const Cx<R> t = col[j]; col[j] = col[p]; col[p] = t; }
+    }
+  }
+}
+
+// op(A)'s diagonal block [i0, i0 + ib) solved for TB_W columns: lower (forward) or upper
+// (backward) triangle, unit or stored diagonal; op(A) = A (trans 0) or A^T (trans 1).
+template <class R>
+__global__ void __launch_bounds__(TB_W) trsm_diag_kernel(const Cx<R>* __restrict__ LUall, int lda, long long a_bs,
+                                                         Cx<R>* __restrict__ Ball, int nrhs, int ldb, long long b_bs,
+                                                         int i0, int ib, int lower, int unit, int trans) {
+  using C_ = Cx<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C_* sL = reinterpret_cast<C_*>(smraw);                 // (TB_NB, TB_NB + 1)
+  C_* sX = sL + TB_NB * (TB_NB + 1);                     // (TB_NB, TB_W + 1)
+  const C_* LU = LUall + blockIdx.y * a_bs;
+  C_* B = Ball + blockIdx.y * b_bs;
+  const int c0 = blockIdx.x * TB_W, tid = threadIdx.x;
+  const int w = min(TB_W, nrhs - c0);
+  for (int e = tid; e < TB_NB * TB_NB; e += blockDim.x) {
+    const int r = e % TB_NB, t = e / TB_NB;
+    C_ v = cxzero<R>();
+    if (r < ib && t < ib) v = trans ? LU[i0 + t + (long long)(i0 + r) * lda] : LU[i0 + r + (long long)(i0 + t) * lda];
+    sL[r * (TB_NB + 1) + t] = v;
+  }
+  for (int e = tid; e < TB_NB * TB_W; e += blockDim.x) {
+    const int r = e % TB_NB, c = e / TB_NB;
+    sX[r * (TB_W + 1) + c] = (r < ib && c < w) ? B[i0 + r + (long long)(c0 + c) * ldb] : cxzero<R>();
+  }
+  __syncthreads();
+  if (tid < w) {
+    auto L = [&](int r, int t) -> C_ { return sL[r * (TB_NB + 1) + t]; };
+    auto X = [&](int r) -> C_& { return sX[r * (TB_W + 1) + tid]; };
+    if (lower) {
+      for (int r = 0; r < ib; ++r) {
+        C_ acc = X(r);
+        for (int t = 0; t < r; ++t) acc = acc - L(r, t) * X(t);
+        if (!unit) acc = cxdiv(acc, L(r, r));
+        X(r) = acc;
+      }
+    } else {
+      for (int r = ib - 1; r >= 0; --r) {
+        C_ acc = X(r);
+        for (int t = r + 1; t < ib; ++t) acc = acc - L(r, t) * X(t);
+        if (!unit) acc = cxdiv(acc, L(r, r));
+        X(r) = acc;
+      }
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < TB_NB * TB_W; e += blockDim.x) {
+    const int r = e % TB_NB, c = e / TB_NB;
+    if (r < ib && c < w) B[i0 + r + (long long)(c0 + c) * ldb] = sX[r * (TB_W + 1) + c];
+  }
+}
+
+template <class R>
+static void getrs_blocked(cudaStream_t s, int batch, int n, const Cx<R>* LU, int lda, long long a_bs, const int* ipiv,
+                          long long piv_bs, Cx<R>* B, int nrhs, int ldb, long long b_bs, int trans) {
+  const dim3 gs((nrhs + 127) / 128, batch);
+  if (trans == 0) { laswp_kernel<R><<<gs, 128, 0, s>>>(B, n, nrhs, ldb, b_bs, ipiv, piv_bs, 1); note_launch(); }
+  const size_t sm = sizeof(Cx<R>) * ((size_t)TB_NB * (TB_NB + 1) + (size_t)TB_NB * (TB_W + 1));
+  cudaFuncSetAttribute(trsm_diag_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const dim3 gd((nrhs + TB_W - 1) / TB_W, batch);
+  const double2 m1 = make_double2(-1.0, 0.0), p1 = make_double2(1.0, 0.0);
+  // forward: L (unit lower) for trans 0, U^T (lower, stored diagonal) for trans 1
+  for (int i0 = 0; i0 < n; i0 += TB_NB) {
+    const int ib = min(TB_NB, n - i0), i1 = i0 + ib, m = n - i1;
+    trsm_diag_kernel<R><<<gd, TB_W, sm, s>>>(LU, lda, a_bs, B, nrhs, ldb, b_bs, i0, ib, 1, trans == 0, trans);
+    note_launch();
+    if (m > 0) {
+      if (trans == 0)
+        gemm<R>(s, batch, m, nrhs, ib, m1, LU + i1 + (long long)i0 * lda, 1, lda, a_bs, B + i0, 1, ldb, b_bs, p1,
+                B + i1, 1, ldb, b_bs);
+      else
+        gemm<R>(s, batch, m, nrhs, ib, m1, LU + i0 + (long long)i1 * lda, lda, 1, a_bs, B + i0, 1, ldb, b_bs, p1,
+                B + i1, 1, ldb, b_bs);
+    }
+  }
+  // backward: U (upper, stored diagonal) for trans 0, L^T (unit upper) for trans 1
+  for (int i1 = n; i1 > 0; i1 -= TB_NB) {
+    const int i0 = max(0, i1 - TB_NB), ib = i1 - i0;
+    trsm_diag_kernel<R><<<gd, TB_W, sm, s>>>(LU, lda, a_bs, B, nrhs, ldb, b_bs, i0, ib, 0, trans == 1, trans);
+    note_launch();
+    if (i0 > 0) {
+      if (trans == 0)
+        gemm<R>(s, batch, i0, nrhs, ib, m1, LU + (long long)i0 * lda, 1, lda, a_bs, B + i0, 1, ldb, b_bs, p1, B, 1,
+                ldb, b_bs);
+      else
+        gemm<R>(s, batch, i0, nrhs, ib, m1, LU + i0, lda, 1, a_bs, B + i0, 1, ldb, b_bs, p1, B, 1, ldb, b_bs);
+    }
+  }
+  if (trans == 1) { laswp_kernel<R><<<gs, 128, 0, s>>>(B, n, nrhs, ldb, b_bs, ipiv, piv_bs, 0); note_launch(); }
+}
+
 template <class R>
 void getrs(cudaStream_t s, int batch, int n, const Cx<R>* LU, int lda, long long a_bs, const int* ipiv,
            long long piv_bs, Cx<R>* B, int nrhs, int ldb, long long b_bs, int trans) {
   if (batch <= 0 || n <= 0 || nrhs <= 0) return;
+  if (nrhs >= 32 && n >= 2 * TB_NB) {
+    getrs_blocked<R>(s, batch, n, LU, lda, a_bs, ipiv, piv_bs, B, nrhs, ldb, b_bs, trans);
+    return;
+  }
   if (trans == 0 && n >= 64 && batch < 4 * sm_count()) {
     if (nrhs <= 3 && getrs_narrow<R, 3>(s, batch, n, LU, lda, a_bs, ipiv, piv_bs, B, nrhs, ldb, b_bs)) return;
     if (nrhs > 3 && nrhs <= 6 && getrs_narrow<R, 6>(s, batch, n, LU, lda, a_bs, ipiv, piv_bs, B, nrhs, ldb, b_bs))
