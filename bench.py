@@ -420,10 +420,15 @@ def main():
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-compare', action='store_true', help='skip the other form and the oracle check')
     ap.add_argument('--profile-calls', type=int, default=0)
+    ap.add_argument('--tensor-cores', default='on', choices=['on', 'off'],
+                    help='off: the FP32 complex products on the SIMT kernel instead of tcgen05 (for comparison)')
     ap.add_argument('--pixels', type=int, default=16)
     ap.add_argument('--adjoint-wavelengths', type=int, default=32)
     args = ap.parse_args()
     world, rank, local = _dist()
+    if args.tensor_cores == 'off' and args.impl != 'reference':
+        from wavebit_gb300 import _lib
+        _lib.check(_lib.load().wb_set_tuning(_lib.WB_TUNE_TENSOR_CORES, 1))
     if args.workload == 'adjoint_layer':
         return adjoint_check(args)
     if args.impl == 'reference':

@@ -208,10 +208,16 @@ long long wb_kernel_launches(wb_handle* h);
 #define WB_TUNE_QR_THREADS 0     /* threads of a QR-sweep CTA (64..1024, multiple of 32) */
 #define WB_TUNE_HRD_THREADS 1    /* threads of a Hessenberg-reduction CTA (64..1024, multiple of 32) */
 #define WB_TUNE_LU_THREADS 2     /* reserved: threads of an LU / triangular-solve CTA */
+#define WB_TUNE_TENSOR_CORES 3   /* 1: FP32 complex products on the SIMT kernel instead of tcgen05 */
 #define WB_TUNE_COUNT 8
 int wb_set_tuning(int key, int value);
 /* The current value of a tunable (0 = the library's own choice), or -1 for an unknown key. */
 int wb_get_tuning(int key);
+
+/* CTAs of the tensor-core complex product (tcgen05, 3xTF32) whose bounded wait on their own
+ * MMAs ran out since the library was loaded (they skip their output and raise this count); 0 in
+ * a healthy run, -1 if the counter cannot be read. No counterpart in the reference. */
+long long wb_tensor_core_errors(void);
 
 /* Live timing of the Schur-form QR sweeps, the eigen-solve's dominant kernel, for measurement:
  * while enabled, CUDA events are recorded on the launching stream around every sweep launch.

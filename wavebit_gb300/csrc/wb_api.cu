@@ -392,7 +392,8 @@ int wb_solve_host(wb_handle* h, int B, int L, int ny, int nx, int hu, int hv,
 long long wb_kernel_launches(wb_handle* h) { (void)h; return wb::launch_count(); }
 
 static_assert(WB_TUNE_QR_THREADS == wb::kTuneQrThreads && WB_TUNE_HRD_THREADS == wb::kTuneHrdThreads &&
-                  WB_TUNE_LU_THREADS == wb::kTuneLuThreads && WB_TUNE_COUNT == wb::kTuneKeys,
+                  WB_TUNE_LU_THREADS == wb::kTuneLuThreads && WB_TUNE_TENSOR_CORES == wb::kTuneTensorCores &&
+                  WB_TUNE_COUNT == wb::kTuneKeys,
               "public and internal tuning keys agree");
 
 int wb_set_tuning(int key, int value) {
@@ -403,6 +404,8 @@ int wb_set_tuning(int key, int value) {
 }
 
 int wb_get_tuning(int key) { return (key >= 0 && key < WB_TUNE_COUNT) ? wb::tuning(key) : -1; }
+
+long long wb_tensor_core_errors(void) { return wb::tc_errors(); }
 
 int wb_profile_qr(int enable) {
   wb::qr_profile(enable != 0);

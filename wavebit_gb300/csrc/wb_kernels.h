@@ -12,7 +12,7 @@ long long launch_count();
 // Launch-shape tunables (process-wide; 0 = the library's own choice). Set through
 // wb_set_tuning by the autotuner; read at every launch.
 // (the same numbers as the public WB_TUNE_* keys)
-enum TuneKey { kTuneQrThreads = 0, kTuneHrdThreads = 1, kTuneLuThreads = 2, kTuneKeys = 8 };
+enum TuneKey { kTuneQrThreads = 0, kTuneHrdThreads = 1, kTuneLuThreads = 2, kTuneTensorCores = 3, kTuneKeys = 8 };
 int tuning(int key);
 void set_tuning(int key, int value);
 // multiprocessor count of the current device (cached per device)
@@ -40,6 +40,12 @@ void zgemm_dd_idx(cudaStream_t s, int batch, int m, int n, int k, double2 alpha,
                   long long b_bs, double2 beta, cplx* C, long long c_rs, long long c_cs, long long c_bs);
 
 // templated over R in {double, float, df64}; alpha/beta are passed as doubles
+// complex FP32 products on the tensor cores (wb_tc.cu): false when not applicable (small
+// shapes, switched off by WB_TUNE_TENSOR_CORES = 1); the count of CTAs that timed out
+bool tc_cgemm(cudaStream_t s, int batch, int m, int n, int k, double2 alpha, const Cx<float>* A, long long a_rs,
+              long long a_cs, long long a_bs, const Cx<float>* B, long long b_rs, long long b_cs, long long b_bs,
+              double2 beta, Cx<float>* C, long long c_rs, long long c_cs, long long c_bs);
+long long tc_errors();
 template <class R>
 void gemm(cudaStream_t s, int batch, int m, int n, int k, double2 alpha,
           const Cx<R>* A, long long a_rs, long long a_cs, long long a_bs,

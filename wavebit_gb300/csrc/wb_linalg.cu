@@ -137,6 +137,11 @@ void gemm(cudaStream_t s, int batch, int m, int n, int k, double2 alpha,
           const Cx<R>* B, long long b_rs, long long b_cs, long long b_bs,
           double2 beta, Cx<R>* C, long long c_rs, long long c_cs, long long c_bs) {
   if (batch <= 0 || m <= 0 || n <= 0) return;
+  if constexpr (sizeof(R) == 4) {      // FP32: the tensor cores (3xTF32) for all but small products
+    if (tc_cgemm(s, batch, m, n, k, alpha, (const Cx<float>*)A, a_rs, a_cs, a_bs, (const Cx<float>*)B, b_rs, b_cs,
+                 b_bs, beta, (Cx<float>*)C, c_rs, c_cs, c_bs))
+      return;
+  }
   if (n <= 8 && k > 0 && a_rs == 1 && b_rs == 1 && c_rs == 1) {
     dim3 g((m + NW_ROWS - 1) / NW_ROWS, batch);
     if (n <= 3)
@@ -916,7 +921,8 @@ static bool getrs_narrow(cudaStream_t s, int batch, int n, const Cx<R>* LU, int 
   return true;
 }
 
-// Many right-hand sides (the cascade's n-column solves): a blocked substitution across the GPU.
+// Many right-hand sides (the cascade's n-column solves, FP32 form): a blocked substitution across
+// the GPU. (The FP64 instantiation keeps getrs_kernel: its time is FP64 issue either way.)
 // The row interchanges are applied first (trans 0) or last (trans 1), one thread per column;
 // then, per block of TB_NB rows, trsm_diag_kernel solves the diagonal block for every column
 // (the block and 64 columns in shared memory, one thread per column) and the batched GEMM
@@ -1039,7 +1045,7 @@ template <class R>
 void getrs(cudaStream_t s, int batch, int n, const Cx<R>* LU, int lda, long long a_bs, const int* ipiv,
            long long piv_bs, Cx<R>* B, int nrhs, int ldb, long long b_bs, int trans) {
   if (batch <= 0 || n <= 0 || nrhs <= 0) return;
-  if (nrhs >= 32 && n >= 2 * TB_NB) {
+  if (sizeof(R) == 4 && nrhs >= 32 && n >= 2 * TB_NB) {     // FP32: the cascade of the mixed form
     getrs_blocked<R>(s, batch, n, LU, lda, a_bs, ipiv, piv_bs, B, nrhs, ldb, b_bs, trans);
     return;
   }
