@@ -220,12 +220,14 @@ def test_layer_modes_double_float_eigenpairs():
     assert res < 1e-12, res
 
 
-@pytest.mark.parametrize('precision', ['mixed', 'mixed_df64_eig'])
-def test_double_float_form_survives_the_fp32_exponent_range(precision):
+@pytest.mark.parametrize('precision,tol', [('mixed', 1e-8), ('mixed_df64_eig', 1e-9)])
+def test_double_float_form_survives_the_fp32_exponent_range(precision, tol):
     """Requests that once overflowed or underflowed the double-float (FP32-exponent) eigen-solve:
     nearly converged bulges of ~1e-25, metal layers, near-degenerate modes; the same requests
     through the FP32 + Newton eigen-solve. The result must be finite and equal to the FP64 one
-    to 1e-9."""
+    within tol: 1e-9 for the double-float eigen-solve, and 1e-8 for the FP32 one, whose FP32
+    products run on the tensor cores as split TF32 products (a few FP32 ulps; the mixed form's
+    target is 1e-6)."""
     E = _engine()
     from wavebit_gb300.serving import _stream, _pol_pair
     reqs = _stream(128, 4.0, 5, [(5, 5), (8, 8)], 4)
@@ -238,7 +240,7 @@ def test_double_float_form_survives_the_fp32_exponent_range(precision):
         Rm, Tm, sm = E.solve_batch(conv, inp, precision=precision)
         torch.cuda.synchronize()
         assert int(sd.item()) & ~8 == 0 and int(sm.item()) & ~8 == 0, (r.id, int(sm.item()))
-        assert float((Rd - Rm).abs().max()) <= 1e-9 and float((Td - Tm).abs().max()) <= 1e-9, r.id
+        assert float((Rd - Rm).abs().max()) <= tol and float((Td - Tm).abs().max()) <= tol, r.id
 
 
 @pytest.mark.parametrize('precision,tol', [('double', 1e-12), ('mixed', 1e-9)])
