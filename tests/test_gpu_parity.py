@@ -220,14 +220,13 @@ def test_layer_modes_double_float_eigenpairs():
     assert res < 1e-12, res
 
 
-@pytest.mark.parametrize('precision,tol', [('mixed', 1e-8), ('mixed_df64_eig', 1e-9)])
+@pytest.mark.parametrize('precision,tol', [('mixed', 1e-8), ('mixed_df64_eig', 1e-8)])
 def test_double_float_form_survives_the_fp32_exponent_range(precision, tol):
     """Requests that once overflowed or underflowed the double-float (FP32-exponent) eigen-solve:
     nearly converged bulges of ~1e-25, metal layers, near-degenerate modes; the same requests
     through the FP32 + Newton eigen-solve. The result must be finite and equal to the FP64 one
-    within tol: 1e-9 for the double-float eigen-solve, and 1e-8 for the FP32 one, whose FP32
-    products run on the tensor cores as split TF32 products (a few FP32 ulps; the mixed form's
-    target is 1e-6)."""
+    to 1e-8: both forms refine an FP32 cascade whose products run on the tensor cores as split
+    TF32 products (a few FP32 ulps; the mixed forms' target is 1e-6)."""
     E = _engine()
     from wavebit_gb300.serving import _stream, _pol_pair
     reqs = _stream(128, 4.0, 5, [(5, 5), (8, 8)], 4)
