@@ -203,8 +203,10 @@ long long wb_kernel_launches(wb_handle* h);
 
 /* Launch-shape tunables, process-wide: 0 restores the library's own choice. The autotuner
  * (wavebit_gb300/autotune.py) times candidates per (orders, layers, batch) bucket and sets them
- * before each batch; results never depend on them. No counterpart in the reference (its backends
- * leave launch shapes to LAPACK and torch). */
+ * before each batch. Thread counts never change a result; WB_TUNE_TENSOR_CORES = 1 moves the FP32
+ * complex products from the tensor cores (split TF32) to FP32 SIMT, which changes their rounding
+ * within FP32 accuracy. No counterpart in the reference (its backends leave launch shapes to
+ * LAPACK and torch). */
 #define WB_TUNE_QR_THREADS 0     /* threads of a QR-sweep CTA (64..1024, multiple of 32) */
 #define WB_TUNE_HRD_THREADS 1    /* threads of a Hessenberg-reduction CTA (64..1024, multiple of 32) */
 #define WB_TUNE_LU_THREADS 2     /* reserved: threads of an LU / triangular-solve CTA */

@@ -70,6 +70,16 @@ __global__ void __launch_bounds__(256) gemm_kernel(
   }
   const C_ alpha = cxfrom<R>(alpha_d), beta = cxfrom<R>(beta_d);
   const bool zero_beta = (beta_d.x == 0.0 && beta_d.y == 0.0);
+  C_ old[4][4];
+  if (!zero_beta) {                 // every load before any store: one latency, not sixteen
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int gr = row0 + tx + 16 * i, gc = col0 + ty + 16 * j;
+        old[i][j] = (gr < m && gc < n) ? C[gr * c_rs + gc * c_cs] : cxzero<R>();
+      }
+  }
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     int gr = row0 + tx + 16 * i;
@@ -78,10 +88,9 @@ __global__ void __launch_bounds__(256) gemm_kernel(
     for (int j = 0; j < 4; ++j) {
       int gc = col0 + ty + 16 * j;
       if (gc >= n) continue;
-      C_* p = C + gr * c_rs + gc * c_cs;
       C_ v = alpha * acc[i][j];
-      if (!zero_beta) v = cxfma(beta, *p, v);
-      *p = v;
+      if (!zero_beta) v = cxfma(beta, old[i][j], v);
+      C[gr * c_rs + gc * c_cs] = v;
     }
   }
 }

@@ -14,11 +14,13 @@
 // FP32 ulps of sum |a||b|, like an FP32 SIMT product.
 //
 // Data path per CTA (128 threads): every thread loads its share of the A and B tiles from global
-// memory, splits and de-interleaves them into the canonical no-swizzle K-major layout in shared
-// memory (double-buffered), one thread issues the MMAs and commits them to an mbarrier; the
-// accumulator (128 lanes x 128 columns of tensor memory) is read back with tcgen05.ld and the
-// epilogue applies alpha and beta. Every mbarrier wait is bounded: on a timeout the CTA raises
-// g_tc_error, waits (bounded) for its own MMAs, frees its tensor memory and returns.
+// memory one block ahead into registers, then splits and de-interleaves them into the canonical
+// no-swizzle K-major layout in shared memory (double-buffered); one thread issues the MMAs and
+// commits them to an mbarrier. The accumulator (128 lanes x 128 columns of tensor memory) is
+// read back with tcgen05.ld; with real alpha and beta every lane writes its row's real or
+// imaginary parts directly, otherwise the tile goes through shared memory to be combined. Every
+// mbarrier wait is bounded: on a timeout the CTA raises g_tc_error, waits (bounded) for its own
+// MMAs, frees its tensor memory and returns.
 #pragma once
 #include <stdint.h>
 #include "wb_common.cuh"
@@ -129,6 +131,25 @@ __global__ void __launch_bounds__(kThreads) cgemm_kernel(int m, int n, int k, fl
   const int nkb = (k + kKb - 1) / kKb;
   uint32_t issued[2] = {0, 0};        // commits made on each barrier
   bool ok = true;
+  // this thread's share of a block: 4 complex of A (64 x 8) and 8 of B (8 x 128), loaded into
+  // registers one block ahead so that the global latency overlaps the staging and the MMAs
+  constexpr int kAp = kTileM * kKb / kThreads, kBp = kKb * kTileN / kThreads;
+  Cx<float> ra[kAp], rb[kBp];
+  auto load_block = [&](int k0) {
+#pragma unroll
+    for (int u = 0; u < kAp; ++u) {
+      const int e = tid + u * kThreads, r = e % kTileM, q = e / kTileM;
+      ra[u].x = 0.f; ra[u].y = 0.f;
+      if (row0 + r < m && k0 + q < k) ra[u] = A[(row0 + r) * a_rs + (k0 + q) * a_cs];
+    }
+#pragma unroll
+    for (int u = 0; u < kBp; ++u) {
+      const int e = tid + u * kThreads, q = e % kKb, c = e / kKb;
+      rb[u].x = 0.f; rb[u].y = 0.f;
+      if (k0 + q < k && col0 + c < n) rb[u] = B[(k0 + q) * b_rs + (col0 + c) * b_cs];
+    }
+  };
+  if (nkb > 0) load_block(0);
   for (int kb = 0; kb < nkb && ok; ++kb) {
     const int buf = kb & 1;
     unsigned char* st = smem + buf * kStage;
@@ -137,38 +158,32 @@ __global__ void __launch_bounds__(kThreads) cgemm_kernel(int m, int n, int k, fl
     }
     __syncthreads();
     if (s_fail) { ok = false; break; }
-    const int k0 = kb * kKb;
+    float* ah = reinterpret_cast<float*>(st);
+    float* al = reinterpret_cast<float*>(st + kPlane);
+    float* bh = reinterpret_cast<float*>(st + 2 * kPlane);
+    float* bl = reinterpret_cast<float*>(st + 3 * kPlane);
     // A: 64 x 8 complex -> the 128 x 16 real expansion, hi and lo planes
-    for (int e = tid; e < kTileM * kKb; e += kThreads) {
-      const int r = e % kTileM, q = e / kTileM;
-      float re = 0.f, im = 0.f;
-      if (row0 + r < m && k0 + q < k) {
-        const Cx<float> v = A[(row0 + r) * a_rs + (k0 + q) * a_cs];
-        re = v.x; im = v.y;
-      }
+#pragma unroll
+    for (int u = 0; u < kAp; ++u) {
+      const int e = tid + u * kThreads, r = e % kTileM, q = e / kTileM;
+      const float re = ra[u].x, im = ra[u].y;
       const float rh = tf32_hi(re), ih = tf32_hi(im);
       const float rl = re - rh, il = im - ih;
-      float* ah = reinterpret_cast<float*>(st);
-      float* al = reinterpret_cast<float*>(st + kPlane);
       ah[plane_off(r, q) >> 2] = rh;           al[plane_off(r, q) >> 2] = rl;
       ah[plane_off(r, q + 8) >> 2] = -ih;      al[plane_off(r, q + 8) >> 2] = -il;
       ah[plane_off(r + 64, q) >> 2] = ih;      al[plane_off(r + 64, q) >> 2] = il;
       ah[plane_off(r + 64, q + 8) >> 2] = rh;  al[plane_off(r + 64, q + 8) >> 2] = rl;
     }
     // B: 8 x 128 complex -> 16 x 128 real, K-major by column
-    for (int e = tid; e < kKb * kTileN; e += kThreads) {
-      const int q = e % kKb, c = e / kKb;
-      float re = 0.f, im = 0.f;
-      if (k0 + q < k && col0 + c < n) {
-        const Cx<float> v = B[(k0 + q) * b_rs + (col0 + c) * b_cs];
-        re = v.x; im = v.y;
-      }
+#pragma unroll
+    for (int u = 0; u < kBp; ++u) {
+      const int e = tid + u * kThreads, q = e % kKb, c = e / kKb;
+      const float re = rb[u].x, im = rb[u].y;
       const float rh = tf32_hi(re), ih = tf32_hi(im);
-      float* bh = reinterpret_cast<float*>(st + 2 * kPlane);
-      float* bl = reinterpret_cast<float*>(st + 3 * kPlane);
       bh[plane_off(c, q) >> 2] = rh;      bl[plane_off(c, q) >> 2] = re - rh;
       bh[plane_off(c, q + 8) >> 2] = ih;  bl[plane_off(c, q + 8) >> 2] = im - ih;
     }
+    if (kb + 1 < nkb) load_block((kb + 1) * kKb);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     if (tid == 0) {
@@ -176,11 +191,11 @@ __global__ void __launch_bounds__(kThreads) cgemm_kernel(int m, int n, int k, fl
       const uint32_t base = smem_u32(st);
 #pragma unroll
       for (int j = 0; j < 2; ++j) {                  // the two K = 8 chunks of the block
-        const uint64_t ah = sdesc(base + 256 * j), al = sdesc(base + kPlane + 256 * j);
-        const uint64_t bh = sdesc(base + 2 * kPlane + 256 * j), bl = sdesc(base + 3 * kPlane + 256 * j);
-        mma_tf32(tmem, ah, bh, (kb > 0 || j > 0) ? 1u : 0u);
-        mma_tf32(tmem, ah, bl, 1u);
-        mma_tf32(tmem, al, bh, 1u);
+        const uint64_t dah = sdesc(base + 256 * j), dal = sdesc(base + kPlane + 256 * j);
+        const uint64_t dbh = sdesc(base + 2 * kPlane + 256 * j), dbl = sdesc(base + 3 * kPlane + 256 * j);
+        mma_tf32(tmem, dah, dbh, (kb > 0 || j > 0) ? 1u : 0u);
+        mma_tf32(tmem, dah, dbl, 1u);
+        mma_tf32(tmem, dal, dbh, 1u);
       }
       mma_commit(&bars[buf]);
     }
@@ -194,9 +209,14 @@ __global__ void __launch_bounds__(kThreads) cgemm_kernel(int m, int n, int k, fl
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const bool good = ok && !s_fail && nkb > 0;
-  float* Dsm = reinterpret_cast<float*>(smem);      // 128 rows x (kTileN + 1)
+  // Real alpha and beta (every use in this library): each lane writes its own row's component
+  // straight from tensor memory -- lanes 0..63 the real parts, 64..127 the imaginary parts.
+  const bool real_ab = (alpha.y == 0.f && beta.y == 0.f);
+  float* Dsm = reinterpret_cast<float*>(smem);      // 128 rows x (kTileN + 1), complex alpha/beta only
   if (good) {
     const int lane_row = warp * 32 + (tid & 31);
+    const int gr = row0 + (lane_row & 63), comp = lane_row >> 6;
+    const bool zero_beta = (beta.x == 0.f && beta.y == 0.f);
 #pragma unroll 1
     for (int c0 = 0; c0 < kTileN; c0 += 16) {
       uint32_t v[16];
@@ -207,8 +227,26 @@ __global__ void __launch_bounds__(kThreads) cgemm_kernel(int m, int n, int k, fl
             "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
           : "r"(addr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (real_ab) {
+        if (gr < m) {
+          float* p0 = reinterpret_cast<float*>(C + gr * c_rs + (col0 + c0) * c_cs) + comp;
+          const long long step = 2 * c_cs;           // floats between consecutive columns
+          float old[16];
+          if (!zero_beta) {                          // all loads first: one latency per 16 outputs
 #pragma unroll
-      for (int j = 0; j < 16; ++j) Dsm[lane_row * (kTileN + 1) + c0 + j] = __uint_as_float(v[j]);
+            for (int j = 0; j < 16; ++j) old[j] = (col0 + c0 + j < n) ? p0[j * step] : 0.f;
+          }
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            if (col0 + c0 + j >= n) break;
+            const float d = alpha.x * __uint_as_float(v[j]);
+            p0[j * step] = zero_beta ? d : d + beta.x * old[j];
+          }
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) Dsm[lane_row * (kTileN + 1) + c0 + j] = __uint_as_float(v[j]);
+      }
     }
   } else if (tid == 0) {
     atomicAdd(&g_tc_error, 1u);
@@ -216,23 +254,28 @@ __global__ void __launch_bounds__(kThreads) cgemm_kernel(int m, int n, int k, fl
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
-  if (!good) return;
+  if (!good || real_ab) return;
   const bool zero_beta = (beta.x == 0.f && beta.y == 0.f);
-  for (int e = tid; e < kTileM * kTileN; e += kThreads) {
-    const int r = e % kTileM, c = e / kTileM;
-    const int gr = row0 + r, gc = col0 + c;
-    if (gr >= m || gc >= n) continue;
-    const float dr = Dsm[r * (kTileN + 1) + c], di = Dsm[(r + 64) * (kTileN + 1) + c];
-    Cx<float>* p = C + gr * c_rs + gc * c_cs;
-    Cx<float> o;
-    o.x = alpha.x * dr - alpha.y * di;
-    o.y = alpha.x * di + alpha.y * dr;
-    if (!zero_beta) {
-      const Cx<float> cv = *p;
-      o.x += beta.x * cv.x - beta.y * cv.y;
-      o.y += beta.x * cv.y + beta.y * cv.x;
+  constexpr int kPer = kTileM * kTileN / kThreads;
+  for (int u0 = 0; u0 < kPer; u0 += 8) {              // 8 outputs a thread: loads, then stores
+    Cx<float> cv[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = tid + (u0 + u) * kThreads, r = e % kTileM, c = e / kTileM;
+      cv[u].x = 0.f; cv[u].y = 0.f;
+      if (!zero_beta && row0 + r < m && col0 + c < n) cv[u] = C[(row0 + r) * c_rs + (col0 + c) * c_cs];
     }
-    *p = o;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = tid + (u0 + u) * kThreads, r = e % kTileM, c = e / kTileM;
+      const int gr = row0 + r, gc = col0 + c;
+      if (gr >= m || gc >= n) continue;
+      const float dr = Dsm[r * (kTileN + 1) + c], di = Dsm[(r + 64) * (kTileN + 1) + c];
+      Cx<float> o;
+      o.x = alpha.x * dr - alpha.y * di + beta.x * cv[u].x - beta.y * cv[u].y;
+      o.y = alpha.x * di + alpha.y * dr + beta.x * cv[u].y + beta.y * cv[u].x;
+      C[gr * c_rs + gc * c_cs] = o;
+    }
   }
 }
 
