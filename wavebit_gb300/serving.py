@@ -80,10 +80,16 @@ def _pol_pair(pol):
 class GpuBackend:
     """libwbgpu.so behind the serving loop: one handle and one CUDA stream per worker."""
 
-    def __init__(self, n_workers, hbm_budget, precision='double', device=0, eig_cache=False, coefficients='sampled'):
+    def __init__(self, n_workers, hbm_budget, precision='double', device=0, eig_cache=False, coefficients='sampled',
+                 tuning=None):
         import torch
         from . import _lib, engine
         self.torch, self.lib, self.engine = torch, _lib, engine
+        # launch shapes chosen offline per bucket (wavebit_gb300/autotune.py), applied per batch
+        self.tuner = None
+        if tuning:
+            from .autotune import Autotuner
+            self.tuner = Autotuner(path=tuning)
         self.device = torch.device('cuda', device)
         torch.cuda.set_device(self.device)
         self.precision = precision
@@ -225,6 +231,8 @@ class GpuBackend:
                                      [r.eps_top for r in reqs], [r.eps_bot for r in reqs],
                                      [_pol_pair(r.pol) for r in reqs], device=self.device)
             prec = self.fallback_precision if reqs[0].retry and self.fallback_precision else self.precision
+            if self.tuner is not None:
+                self.tuner.apply(self.tuner.lookup((hu, hv), L, len(reqs), prec))
             if self.eig_modes and not reqs[0].retry:
                 q, W, V = self.modes_for(reqs, keys_all, conv, index, worker)
                 R, T, st = engine.smm_solve(W, V, q, inp, hu, hv, precision=self.precision,
@@ -393,6 +401,7 @@ def main():
     ap.add_argument('--eig-cache', action='store_true', help='keep per-layer eigenpairs on the device')
     ap.add_argument('--coefficients', default='sampled', choices=['sampled', 'integrated'],
                     help='Li coefficients: sampled staircase or integrated segments of the compressed raster')
+    ap.add_argument('--tuning', default=None, help='JSON of launch shapes per bucket (python -m wavebit_gb300.autotune)')
     ap.add_argument('--repeat', type=int, default=1,
                     help='replay each request this many times (as new requests), e.g. to exercise the caches')
     args = ap.parse_args()
@@ -401,7 +410,7 @@ def main():
     if args.repeat > 1:
         reqs = _repeat(reqs, args.repeat, args.rate)
     backend = GpuBackend(args.workers, int(args.budget_gb * 2 ** 30), args.precision, eig_cache=args.eig_cache,
-                         coefficients=args.coefficients)
+                         coefficients=args.coefficients, tuning=args.tuning)
     server = Server(backend, args.workers, args.max_batch)
     _, stats = server.run(reqs)
     stats.update(precision=args.precision, rate=args.rate, workers=args.workers, orders=args.orders,
