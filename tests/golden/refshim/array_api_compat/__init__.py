@@ -2,9 +2,10 @@
 
 Test infrastructure only: it lets the reference package be imported in a container where the
 real ``array_api_compat`` is not installed, so that golden fixtures can be generated from the
-reference's own NumPy path. Only the NumPy namespace is provided (NumPy 2.x already implements
-the standard names the reference uses); ``array_namespace`` maps NumPy arrays and Python
-scalars to it.
+reference's own NumPy and PyTorch paths. ``array_namespace`` maps NumPy arrays and Python scalars
+to the NumPy namespace (NumPy 2.x already implements the standard names the reference uses) and
+torch tensors to the torch one (``array_api_compat.torch``, the standard's names mapped onto
+torch).
 """
 import numpy as _np
 
@@ -26,13 +27,15 @@ def array_namespace(*xs, **_kw):
 
 
 def to_device(x, device, /, **_kw):
-    if device in (None, 'cpu'):
+    if type(x).__module__.startswith('torch'):
+        return x.to(device)
+    if device is None or str(device) == 'cpu':
         return x
     raise ValueError(f'numpy arrays live on the cpu, not {device!r}')
 
 
 def device(x, /):
-    return 'cpu'
+    return x.device if type(x).__module__.startswith('torch') else 'cpu'
 
 
 def is_numpy_array(x):

@@ -402,6 +402,8 @@ def main():
     ap.add_argument('--coefficients', default='sampled', choices=['sampled', 'integrated'],
                     help='Li coefficients: sampled staircase or integrated segments of the compressed raster')
     ap.add_argument('--tuning', default=None, help='JSON of launch shapes per bucket (python -m wavebit_gb300.autotune)')
+    ap.add_argument('--save-results', default=None,
+                    help='write every request\'s R, T, status and latency to this .npz (to compare two forms)')
     ap.add_argument('--repeat', type=int, default=1,
                     help='replay each request this many times (as new requests), e.g. to exercise the caches')
     args = ap.parse_args()
@@ -412,7 +414,16 @@ def main():
     backend = GpuBackend(args.workers, int(args.budget_gb * 2 ** 30), args.precision, eig_cache=args.eig_cache,
                          coefficients=args.coefficients, tuning=args.tuning)
     server = Server(backend, args.workers, args.max_batch)
-    _, stats = server.run(reqs)
+    results, stats = server.run(reqs)
+    if args.save_results:
+        out = {}
+        for r in results:
+            if r.R is not None:
+                out[f'{r.id}__R'] = np.asarray(r.R)
+                out[f'{r.id}__T'] = np.asarray(r.T)
+            out[f'{r.id}__status'] = np.asarray(r.status)
+            out[f'{r.id}__latency'] = np.asarray(r.latency if r.latency is not None else np.nan)
+        np.savez_compressed(args.save_results, **out)
     stats.update(precision=args.precision, rate=args.rate, workers=args.workers, orders=args.orders,
                  max_layers=args.max_layers, gpu_launches=backend.launches(), eig_cache=args.eig_cache,
                  eig_hits=backend.eig_hits, eig_misses=backend.eig_misses, repeat=args.repeat,
