@@ -417,7 +417,7 @@ def main():
     results, stats = server.run(reqs)
     if args.save_results:
         out = {}
-        for r in results:
+        for r in results.values():
             if r.R is not None:
                 out[f'{r.id}__R'] = np.asarray(r.R)
                 out[f'{r.id}__T'] = np.asarray(r.T)
