@@ -14,9 +14,10 @@ NumPy, the route the reference takes for a stack of permittivity rasters under
 
 Each function cites the reference lines it follows (paths inside ``src/wavebit``). Scope: real
 incidence angles from a lossless superstrate with ``Re(eps) > 0``, non-magnetic isotropic
-media, top-side plane-wave incidence on the specular order. The reference's exceptional-point
-rebuilds (``solve_2d.py:2463-2575``) are not restated; ``layer_modes_2d`` reports a grazing
-layer through ``status`` instead, exactly where the reference would take its rebuild branch.
+media, top-side plane-wave incidence on the specular order. Of the reference's exceptional-point
+handling (``solve_2d.py:2463-2575``) the grazing-cluster rebuild is restated
+(``rebuild_grazing_cluster``, on request); the defective-pair and cluster rebuilds are not, and
+``layer_modes_2d`` reports a grazing layer through ``status``.
 
 Parity of this module is pinned by ``tests/test_oracle_golden.py`` against fixtures generated
 from the reference itself (``tests/golden/make_fixtures.py``) and against the reference's own
@@ -257,11 +258,13 @@ def layer_operator(kxg, kyg, epx, epy, epz_i):
     return omega2, omega_r
 
 
-def layer_modes_2d(kxg, kyg, epx, epy, epz_i):
+def layer_modes_2d(kxg, kyg, epx, epy, epz_i, rebuild=False):
     """``(W, V, q, status)`` of one 2D layer (solve_2d.py:2303-2460).
 
     ``status`` is 0, or 1 where ``min|w| < 1e-9 max|w|`` (the grazing gate at
-    solve_2d.py:2463-2464, whose rebuild this oracle does not restate).
+    solve_2d.py:2463-2464). With ``rebuild`` such a layer's cluster is re-derived from the
+    first-order problem (:func:`rebuild_grazing_cluster`) and status goes back to 0, or
+    ``FloatingPointError`` is raised where the cluster is numerically defective.
     """
     omega2, omega_r = layer_operator(kxg, kyg, epx, epy, epz_i)
     w, W = np.linalg.eig(omega2)
@@ -269,7 +272,72 @@ def layer_modes_2d(kxg, kyg, epx, epy, epz_i):
     V = (omega_r @ W) / q
     aw = np.abs(w)
     status = int(np.min(aw) < _COUPLED_REL * np.max(aw))
+    if status and rebuild:
+        out = rebuild_grazing_cluster(w, W, V, q, left_factor(kxg, kyg, epz_i), omega_r)
+        if out is not None:
+            W, V, q = out
+            status = 0
     return W, V, q, w, status
+
+
+_DEFECTIVE_REL = 1e-10   # solve_2d.py:73
+
+
+def left_factor(kxg, kyg, epz_i):
+    """``Omega_L = [[-Cc, B], [-D, E]]`` (solve_2d.py:2380-2390, 2470-2471), with
+    ``Omega2 = Omega_L Omega_R`` for a non-magnetic layer."""
+    N = kxg.shape[0]
+    I = np.eye(N, dtype=np.complex128)
+    Bm = (kxg[:, None] * epz_i) * kxg[None, :] - I
+    Dm = (kyg[:, None] * epz_i) * kyg[None, :] - I
+    Cc = (kxg[:, None] * epz_i) * kyg[None, :]
+    Em = (kyg[:, None] * epz_i) * kxg[None, :]
+    return np.block([[-Cc, Bm], [-Dm, Em]])
+
+
+def rebuild_grazing_cluster(w, W, V, q, omega_l, omega_r):
+    """The grazing cluster re-derived from the coupled first-order problem
+    (solve_2d.py:118-222): the clusters of ``Omega_L Omega_R`` and ``Omega_R Omega_L`` as
+    orthonormal bases, the factors restricted to them, the small first-order eigenproblem,
+    ``k`` of its pairs chosen jointly independent, each rooted by ``mode_q``. ``None`` where the
+    two clusters differ in size; ``FloatingPointError`` where the coupled rates split by less
+    than 1e-10 of the modal scale."""
+    aw = np.abs(w)
+    J = np.where(aw < _COUPLED_REL * aw.max())[0]
+    wh, Vh = np.linalg.eig(omega_r @ omega_l)
+    Jh = np.where(np.abs(wh) < _COUPLED_REL * np.abs(wh).max())[0]
+    if len(Jh) != len(J):
+        return None
+    k = len(J)
+    QE = np.linalg.qr(W[:, J])[0]
+    QH = np.linalg.qr(Vh[:, Jh])[0]
+    Rr = QH.conj().T @ (omega_r @ QE)
+    Lr = QE.conj().T @ (omega_l @ QH)
+    Zk = np.zeros((k, k), np.complex128)
+    mu, g = np.linalg.eig(np.block([[Zk, Lr], [Rr, Zk]]))
+    g = g / np.linalg.norm(g, axis=0, keepdims=True)
+    chosen, re_, rh_ = [], g[:k].copy(), g[k:].copy()
+    for _ in range(k):
+        score = np.linalg.norm(re_, axis=0) ** 2 + np.linalg.norm(rh_, axis=0) ** 2
+        score[chosen] = -1.0
+        c = int(np.argmax(score))
+        chosen.append(c)
+        for m in (re_, rh_):
+            v = m[:, c]
+            nv = np.linalg.norm(v)
+            if nv > 1e-150:
+                u = v / nv
+                m -= u[:, None] * (u.conj() @ m)[None, :]
+    if np.abs(mu[chosen]).min() < _DEFECTIVE_REL * np.sqrt(aw.max()):
+        raise FloatingPointError('a 2D layer eigenmode pair is numerically defective at a grazing condition')
+    W, V, q = W.copy(), V.copy(), q.copy()
+    for i, c in enumerate(chosen):
+        qi = mode_q(np.asarray([mu[c] ** 2]))[0]
+        gh = g[k:, c] if abs(qi - mu[c]) <= abs(qi + mu[c]) else -g[k:, c]
+        W[:, J[i]] = QE @ g[:k, c]
+        V[:, J[i]] = QH @ gh
+        q[J[i]] = qi
+    return W, V, q
 
 
 def order_azimuth(ky, kx, phi):
@@ -433,7 +501,7 @@ def amplitude_ratios(amps, hu, hv):
 
 
 def solve_stack(structure, thickness, wavelength, period, hu, hv, theta=0.0, phi=0.0,
-                eps_top=1.0, eps_bot=1.0, polarization='s', conv=None, keep=False):
+                eps_top=1.0, eps_bot=1.0, polarization='s', conv=None, keep=False, rebuild_grazing=False):
     """One SMM solve of a raster stack (scattering.py:1185-1456; engine.py:7836-7880).
 
     ``structure`` is ``(L, ny, nx)`` relative permittivity, ``thickness`` ``(L,)`` in the
@@ -473,7 +541,7 @@ def solve_stack(structure, thickness, wavelength, period, hu, hv, theta=0.0, phi
     status = []
     layers = []
     for i in range(L):
-        W, V, q, w, st = layer_modes_2d(kxg, kyg, epx_all[i], epy_all[i], epz_i_all[i])
+        W, V, q, w, st = layer_modes_2d(kxg, kyg, epx_all[i], epy_all[i], epz_i_all[i], rebuild=rebuild_grazing)
         status.append(st)
         big_W, big_V = sp_modes_2d(W, V, c, s, N)
         X = np.diag(np.exp(-k0 * thickness[i] * q))

@@ -877,6 +877,55 @@ class Prepared:
                                  np.full(k, r['eps_top']), np.full(k, r['eps_bot']), np.tile(r['pol'], (k, 1)))
         return engine.solve_batch(conv, inp, precision=precision, amplitudes=amplitudes, handle=self.handle)
 
+    def _rebuild_grazing(self, r, conv, layer_index, idx, wl, theta, amplitudes, merge):
+        """The solves ``idx`` the kernels flagged grazing (a layer eigenvalue zero to round-off),
+        again: FP64 modes from the kernels, every flagged layer's cluster re-derived on the host
+        (``graze.rebuild_grazing_cluster``, solve_2d.py:118-222 and :2463-2488 of the
+        reference), then stage C on the device from the repaired modes. A numerically defective
+        cluster raises NumericalError('rcwa.singular') with the reference's remedy. Returns the
+        solves whose flag was cleared."""
+        from . import graze
+        from .adjoint import ports
+        hu, hv = conv.hu, conv.hv
+        li = np.asarray(layer_index)[idx]
+        k, L = li.shape
+        kxs, kys = [], []
+        for b in idx:
+            pv = ports(float(wl[b]), tuple(r['period']), float(theta[b]), float(r['phi']), r['eps_top'], r['eps_bot'],
+                       hu, hv, 'cpu')
+            for _ in range(L):
+                kxs.append(pv['kx'].numpy()); kys.append(pv['ky'].numpy())
+        kxs, kys = np.array(kxs), np.array(kys)
+        w, q, W, V, _ = engine.layer_modes(conv, li.reshape(-1), kxs, kys, precision='double', handle=self.handle)
+        wh, qh, Wh, Vh = (t.cpu().numpy().copy() for t in (w, q, W, V))
+        slots = [conv.slot(s_).cpu().numpy() for s_ in range(3)]
+        still = np.zeros(k, dtype=bool)
+        for p in range(k * L):
+            if not graze.grazing(wh[p]):
+                continue
+            lay = int(li.reshape(-1)[p])
+            omega_l, omega_r = graze.layer_factors(kxs[p], kys[p], slots[0][lay], slots[1][lay], slots[2][lay])
+            try:
+                out = graze.rebuild_grazing_cluster(wh[p], Wh[p], Vh[p], qh[p], omega_l, omega_r)
+            except FloatingPointError as exc:
+                raise NumericalError(str(exc), code='rcwa.singular') from None
+            if out is None:
+                still[p // L] = True                  # structure not understood: the flag stays
+                continue
+            Wh[p], Vh[p], qh[p] = out
+        dev = W.device
+        inp = engine.BatchInputs(li, np.tile(r['thickness'], (k, 1)), wl[idx], np.tile(r['period'], (k, 1)),
+                                 theta[idx], np.full(k, r['phi']), np.full(k, r['eps_top']), np.full(k, r['eps_bot']),
+                                 np.tile(r['pol'], (k, 1)))
+        res = list(engine.smm_solve(torch.as_tensor(Wh, device=dev), torch.as_tensor(Vh, device=dev),
+                                    torch.as_tensor(qh, device=dev), inp, hu, hv, precision='double',
+                                    amplitudes=amplitudes, handle=self.handle))
+        stt = res[2]
+        stt &= ~_lib.WB_ST_GRAZING
+        stt[torch.as_tensor(np.nonzero(still)[0], device=stt.device)] |= _lib.WB_ST_GRAZING
+        merge(idx, res)
+        return tuple(int(b) for b, s_ in zip(idx, still) if not s_)
+
     def _solve(self, r, conv, layer_index, amplitudes=False, scattering=False, fields=False):
         """Solve every wavelength of ``r`` with the layers ``layer_index[b]`` of ``conv``; with
         ``scattering`` also keep the stack's scattering matrix of each (at the same, possibly
@@ -902,12 +951,18 @@ class Prepared:
             st = status.cpu().numpy()
         moved = self._detune(r, conv, layer_index, wl, th, st, merge, amplitudes)
         st = status.cpu().numpy()
+        flagged = np.nonzero(st & _lib.WB_ST_GRAZING)[0]
+        rebuilt = ()
+        if flagged.size:
+            # correct or loud at a grazing order: the layer's cluster is re-derived from the
+            # first-order problem, or the solve is refused as numerically defective
+            rebuilt = self._rebuild_grazing(r, conv, layer_index, flagged, wl, th, amplitudes, merge)
+            st = status.cpu().numpy()
         grazing = np.nonzero(st & _lib.WB_ST_GRAZING)[0]
         if grazing.size:
-            warnings.warn(f'a layer mode sits on its cutoff at {grazing.size} wavelength(s); the GB300 path does '
-                          'not rebuild exceptional points, so those results may be inaccurate. '
-                          'rcwa.Numerics(detuning=1e-12) retries them slightly detuned.', RayleighPointWarning,
-                          stacklevel=3)
+            warnings.warn(f'a layer mode sits on its cutoff at {grazing.size} wavelength(s) and its cluster could not '
+                          'be re-derived, so those results may be inaccurate. rcwa.Numerics(detuning=1e-12) retries '
+                          'them slightly detuned.', RayleighPointWarning, stacklevel=3)
         bad = st & ~_lib.WB_ST_GRAZING
         if np.any(bad & _lib.WB_ST_SINGULAR):
             raise NumericalError('a factorization met an exact zero pivot', code='rcwa.singular')
@@ -918,6 +973,7 @@ class Prepared:
                 'grazing': tuple(bool(s & _lib.WB_ST_GRAZING) for s in st),
                 'status': st, 'precision': self.precision,
                 'fallback_solves': tuple(int(i) for i in fallback), 'detuned': moved,
+                'grazing_rebuilt': tuple(int(i) for i in rebuilt),
                 **_defined_flags(B, R.device, self.numerics)}
         S = self._scattering(r, conv, np.asarray(layer_index), wl, th) if scattering else None
         states = self._field_states(r, conv, np.asarray(layer_index), wl, th) if fields else None
