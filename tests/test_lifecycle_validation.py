@@ -179,13 +179,35 @@ def test_auto_detune_ladder_moves_the_wavelength_then_the_angle(monkeypatch):
 
 
 def test_a_grazing_mode_without_detuning_warns(monkeypatch):
+    """A grazing solve whose cluster the rebuild cannot take (its two products' clusters
+    differ in size) keeps its flag and warns."""
     from wavebit_gb300 import _lib
     monkeypatch.setattr(rcwa.engine, 'BatchInputs', _FakeInputs)
     monkeypatch.setattr(rcwa.engine, 'solve_batch', _fake_solver(lambda w, t: _lib.WB_ST_GRAZING if w == 700.0 else 0))
     p, r = _prepared(None)
+    seen = []
+    monkeypatch.setattr(type(p), '_rebuild_grazing', lambda self, *a: seen.append(list(a[3])) or ())
     with pytest.warns(rcwa.RayleighPointWarning):
         res = p._solve(r, None, np.zeros((3, 1), int))
+    assert seen == [[1]]
     assert res.diagnostics['grazing'] == (False, True, False) and res.diagnostics['detuned'] == {}
+    assert res.diagnostics['grazing_rebuilt'] == ()
+
+
+def test_a_defective_graze_is_refused_with_the_reference_code(monkeypatch):
+    """A grazing cluster the rebuild finds numerically defective ends the run with the
+    reference's NumericalError (rcwa.singular) and its detuning remedy."""
+    from wavebit_gb300 import _lib, graze
+    monkeypatch.setattr(rcwa.engine, 'BatchInputs', _FakeInputs)
+    monkeypatch.setattr(rcwa.engine, 'solve_batch', _fake_solver(lambda w, t: _lib.WB_ST_GRAZING if w == 700.0 else 0))
+    p, r = _prepared(None)
+
+    def refuse(self, *a):
+        raise rcwa.NumericalError(graze.DEFECTIVE_MESSAGE, code='rcwa.singular')
+    monkeypatch.setattr(type(p), '_rebuild_grazing', refuse)
+    with pytest.raises(rcwa.NumericalError) as e:
+        p._solve(r, None, np.zeros((3, 1), int))
+    assert e.value.code == 'rcwa.singular' and 'detuning' in str(e.value)
 
 
 def test_a_failed_solve_is_a_numerical_error_with_the_reference_code(monkeypatch):
