@@ -161,6 +161,28 @@ int wb_scattering_matrix(wb_handle* h, int B, int L, int hu, int hv, const wb_co
                          wb_complex* S11, wb_complex* S12, wb_complex* S21, wb_complex* S22, int32_t* status,
                          void* stream);
 
+/* The ETM connecting algorithm (Numerics(algorithm='etm')) from given modes, FP64: the enhanced
+ * transmittance matrix recursion bottom-up and the final matching at the superstrate. Inputs and
+ * outputs as wb_smm_solve (FP64 form). Reference: rcwa/_engine/solve_2d.py:2619-2843 (the 2D ETM
+ * path), solve_1d.py:1389-1520 (final_matching). */
+int wb_etm_solve(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* W, const wb_complex* V,
+                 const wb_complex* q, const double* thickness, const double* wavelength, const double* period,
+                 const double* theta, const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,
+                 const wb_complex* pol, double* R, double* T, wb_complex* amps, int32_t* status, void* stream);
+
+/* Every layer's mode amplitudes inside the stack, for the field reconstruction, from given modes
+ * (FP64). Inputs as wb_smm_solve without pol, plus C (device, (B, 2N, k) column-major per solve):
+ * k incidence columns in the superstrate's port variables. Outputs (device): plus, minus_top,
+ * minus_bottom (B, L, 2N, k): each layer's down-going amplitudes at its top face and its up-going
+ * ones at its top and bottom faces, in the layer's s/p-rotated mode basis; cref, ctrn (B, 2N, k):
+ * the reflected and transmitted columns in the half-space port variables. Reference:
+ * rcwa/_engine/scattering.py:236-350 (_below_reflections, _field_state). */
+int wb_layer_amplitudes(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* W, const wb_complex* V,
+                        const wb_complex* q, const double* thickness, const double* wavelength, const double* period,
+                        const double* theta, const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,
+                        const wb_complex* C, int k, wb_complex* plus, wb_complex* minus_top, wb_complex* minus_bottom,
+                        wb_complex* cref, wb_complex* ctrn, int32_t* status, void* stream);
+
 /* The same solve from HOST buffers: rasters in, efficiencies out. Copies inputs to the
  * device, assembles the L layers (stage A), solves the B problems, copies R, T and status
  * back and synchronises. eps: host (L, ny, nx); the other arrays as in wb_solve_batch but in

@@ -142,10 +142,10 @@ def test_lifecycle_from_below_on_the_cpu(name, monkeypatch):
     the stage-B kernel), amplitudes, readings, fields and boundary fields mapped back to the
     scene's frame -- against the reference's own bottom-lit run."""
     from wavebit_gb300 import engine
-    from test_fields import _oracle_layer_modes
+    from test_fields import use_cpu_stages
     c = _case(name)
     hu, hv = (int(v) for v in c['orders'])
-    monkeypatch.setattr(engine, 'layer_modes', _oracle_layer_modes)
+    use_cpu_stages(monkeypatch)
     num = rcwa.Numerics(orders=(hu, hv), algorithm='etm')
     for tag, pol in POLS:
         r = rcwa._resolve(_problem(c, pol), num)

@@ -76,10 +76,10 @@ def test_lifecycle_with_a_direct_wavevector_on_the_cpu(name, monkeypatch):
     """The lifecycle over two wavelengths (the ETM over the oracle's modes in place of the stage-B
     kernel): R, T, the amplitude ratios and the orders' wavevectors against the reference's run."""
     from wavebit_gb300 import engine
-    from test_fields import _oracle_layer_modes
+    from test_fields import use_cpu_stages
     c = _case(name)
     hu, hv = (int(v) for v in c['orders'])
-    monkeypatch.setattr(engine, 'layer_modes', _oracle_layer_modes)
+    use_cpu_stages(monkeypatch)
     num = rcwa.Numerics(orders=(hu, hv), algorithm='etm')
     for tag, pol in POLS:
         r = rcwa._resolve(_problem(c, pol), num)

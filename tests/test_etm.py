@@ -98,13 +98,13 @@ def test_etm_refuses_a_scattering_matrix():
 def test_lifecycle_etm_on_the_cpu(name, monkeypatch):
     """Prepared._solve_etm with the stage-B kernel replaced by the oracle on the CPU."""
     from wavebit_gb300 import engine
-    from test_fields import _oracle_layer_modes
+    from test_fields import use_cpu_stages
     c = _case(name)
     hu, hv = (int(v) for v in c['orders'])
     st = np.asarray(c['structure'], complex)
     conv_np = O.to_conv_mat_raster_sampled(st, hu, hv)
     conv = engine.ConvStack.from_matrices(*(torch.as_tensor(a) for a in conv_np), hu, hv)
-    monkeypatch.setattr(engine, 'layer_modes', _oracle_layer_modes)
+    use_cpu_stages(monkeypatch)
     num = rcwa.Numerics(orders=(hu, hv), algorithm='etm')
     r = rcwa._resolve(_problem(c), num)
     p = rcwa.Prepared.__new__(rcwa.Prepared)
@@ -145,3 +145,50 @@ def test_lifecycle_etm_matches_the_reference_on_the_gpu(name):
             a, b = getattr(etm.outputs[port], key), getattr(smm.outputs[port], key)
             scale = torch.abs(b).max().item() if key == 'power' else max(1.0, torch.abs(b).max().item())
             assert torch.abs(a - b).max().item() <= 1e-9 * scale, (name, port, key)
+
+
+def _given_modes(c, wavelengths, device):
+    """(W, V, q, inp) of the case at several wavelengths, the oracle's modes, on `device`."""
+    from wavebit_gb300 import engine
+    hu, hv = (int(v) for v in c['orders'])
+    st, th = np.asarray(c['structure'], complex), np.asarray(c['thickness'], float)
+    per = tuple(float(p) for p in c['period'])
+    conv = O.to_conv_mat_raster_sampled(st, hu, hv)
+    Ws, Vs, qs = [], [], []
+    for wl in wavelengths:
+        pv = ports(wl, per, float(c['theta']), float(c['phi']), complex(c['eps_top']), complex(c['eps_bot']), hu, hv,
+                   'cpu')
+        for i in range(st.shape[0]):
+            W, V, q, _, _ = O.layer_modes_2d(pv['kx'].numpy() + 0j, pv['ky'].numpy() + 0j, conv[0][i], conv[1][i],
+                                             conv[2][i])
+            Ws.append(W); Vs.append(V); qs.append(q)
+    B, L = len(wavelengths), st.shape[0]
+    inp = engine.BatchInputs(np.tile(np.arange(L), (B, 1)), np.tile(th, (B, 1)), wavelengths, np.tile(per, (B, 1)),
+                             np.full(B, float(c['theta'])), np.full(B, float(c['phi'])),
+                             np.full(B, complex(c['eps_top'])), np.full(B, complex(c['eps_bot'])),
+                             np.tile([0.6, 0.8j], (B, 1)), device=device)
+    return tuple(torch.as_tensor(np.stack(a), device=device) for a in (Ws, Vs, qs)) + (inp,)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('name', ['crossed_1', 'crossed_4', 'metal_substrate', 'tir'])
+def test_etm_kernels_match_the_torch_recursion(name):
+    """wb_etm_solve (the library's LU and GEMM kernels) against the torch restatement of the same
+    recursion on the same modes, three wavelengths in one batch: R, T and the Fresnel amplitudes
+    to 1e-12."""
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from wavebit_gb300 import engine
+    from test_fields import _torch_etm_solve
+    c = _case(name)
+    hu, hv = (int(v) for v in c['orders'])
+    wls = [float(c['wavelength']) * f for f in (1.0, 1.07, 0.93)]
+    W, V, q, inp = _given_modes(c, wls, 'cuda')
+    R, T, st, amps = engine.etm_solve(W, V, q, inp, hu, hv, amplitudes=True)
+    W0, V0, q0, inp0 = _given_modes(c, wls, 'cpu')
+    R0, T0, _, a0 = _torch_etm_solve(W0, V0, q0, inp0, hu, hv, amplitudes=True)
+    assert int(st.abs().sum()) == 0
+    scale = max(float(R0.abs().max()), float(T0.abs().max()))
+    assert float((R.cpu() - R0).abs().max()) <= 1e-12 * scale, name
+    assert float((T.cpu() - T0).abs().max()) <= 1e-12 * scale, name
+    assert float((amps.cpu() - a0).abs().max()) <= 1e-12 * float(a0.abs().max()), name

@@ -123,6 +123,53 @@ def _oracle_layer_modes(conv, pair_layer, kx, ky, precision='double', handle=Non
     return w, q, W, V, torch.zeros(len(out[0]), dtype=torch.int32)
 
 
+def _solve_ports(inp, b, hu, hv, device):
+    from wavebit_gb300.adjoint import ports
+    return ports(float(inp.wavelength[b]), tuple(float(v) for v in inp.period[b]), float(inp.theta[b]),
+                 float(inp.phi[b]), complex(inp.eps_top[b]), complex(inp.eps_bot[b]), hu, hv, device)
+
+
+def _torch_layer_amplitudes(W, V, q, inp, hu, hv, C, handle=None):
+    """A CPU stand-in for engine.layer_amplitudes: the torch restatement, solve by solve."""
+    B, L = inp.B, inp.L
+    out = [[], [], [], [], []]
+    for b in range(B):
+        pv = _solve_ports(inp, b, hu, hv, W.device)
+        modes = [(W[b * L + l], V[b * L + l], q[b * L + l]) for l in range(L)]
+        faces, cref, ctrn = F.layer_faces(modes, inp.thickness[b].tolist(), 2 * np.pi / float(inp.wavelength[b]),
+                                          pv, C[b])
+        for j in range(3):
+            out[j].append(torch.stack([f[j] for f in faces]))
+        out[3].append(cref)
+        out[4].append(ctrn)
+    return tuple(torch.stack(x) for x in out) + (torch.zeros(B, dtype=torch.int32),)
+
+
+def _torch_etm_solve(W, V, q, inp, hu, hv, amplitudes=False, handle=None):
+    """A CPU stand-in for engine.etm_solve: the torch restatement of the ETM, solve by solve."""
+    from wavebit_gb300 import etm as E
+    B, L = inp.B, inp.L
+    out = [[], [], []]
+    for b in range(B):
+        pv = _solve_ports(inp, b, hu, hv, W.device)
+        modes = [(W[b * L + l], V[b * L + l], q[b * L + l]) for l in range(L)]
+        res = E.etm_solve(modes, inp.thickness[b].tolist(), 2 * np.pi / float(inp.wavelength[b]), pv,
+                          tuple(complex(v) for v in inp.pol[b]), 2 * hu + 1, 2 * hv + 1, amplitudes=True)
+        for lst, a in zip(out, res):
+            lst.append(a)
+    R, T, amps = (torch.stack(x) for x in out)
+    return (R, T, torch.zeros(B, dtype=torch.int32)) + ((amps,) if amplitudes else ())
+
+
+def use_cpu_stages(monkeypatch):
+    """Stand the oracle in for stage B and the torch restatements for the cascade kernels the
+    lifecycle calls on given modes, so that its bookkeeping runs on the CPU."""
+    from wavebit_gb300 import engine
+    monkeypatch.setattr(engine, 'layer_modes', _oracle_layer_modes)
+    monkeypatch.setattr(engine, 'layer_amplitudes', _torch_layer_amplitudes)
+    monkeypatch.setattr(engine, 'etm_solve', _torch_etm_solve)
+
+
 @pytest.mark.parametrize('name', ['crossed_0', 'symmetric_pillar'])
 def test_lifecycle_field_states_on_the_cpu(name, monkeypatch):
     """Prepared._field_states and Result.field with the stage-B kernel replaced by the oracle on
@@ -133,7 +180,7 @@ def test_lifecycle_field_states_on_the_cpu(name, monkeypatch):
     st = np.asarray(c['structure'], complex)
     conv_np = O.to_conv_mat_raster_sampled(st, hu, hv)
     conv = engine.ConvStack.from_matrices(*(torch.as_tensor(a) for a in conv_np), hu, hv)
-    monkeypatch.setattr(engine, 'layer_modes', _oracle_layer_modes)
+    use_cpu_stages(monkeypatch)
     for pol in ('s', 'p'):
         r = rcwa._resolve(_problem(c, pol), rcwa.Numerics(orders=(hu, hv)))
         p = rcwa.Prepared.__new__(rcwa.Prepared)
@@ -265,3 +312,30 @@ def test_coordinate_rules_follow_the_reference():
     for bad in ([[0.1, 0.2]], [0.1 + 1j]):
         with pytest.raises(ValueError):
             F.height_points(bad, np.array([1.0]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('name', ['crossed_0', 'symmetric_pillar'])
+def test_layer_amplitude_kernels_match_the_torch_recursion(name):
+    """wb_layer_amplitudes (the cascade kernels' recursion with the per-layer amplitudes kept)
+    against the torch restatement on the same modes, two wavelengths and three incidence columns
+    in one batch: every layer's plus, minus_top and minus_bottom and the reflected and
+    transmitted columns to 1e-12 of their largest entry."""
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from wavebit_gb300 import engine
+    from test_etm import _given_modes
+    c = _case(name)
+    hu, hv = (int(v) for v in c['orders'])
+    N = (2 * hu + 1) * (2 * hv + 1)
+    wls = [float(np.asarray(c['wavelength']).reshape(-1)[0]) * f for f in (1.0, 1.11)]
+    rng = np.random.default_rng(5)
+    Cn = rng.standard_normal((2, 2 * N, 3)) + 1j * rng.standard_normal((2, 2 * N, 3))
+    W, V, q, inp = _given_modes(c, wls, 'cuda')
+    got = engine.layer_amplitudes(W, V, q, inp, hu, hv, torch.as_tensor(Cn, device='cuda'))
+    W0, V0, q0, inp0 = _given_modes(c, wls, 'cpu')
+    want = _torch_layer_amplitudes(W0, V0, q0, inp0, hu, hv, torch.as_tensor(Cn))
+    assert int(got[5].abs().sum()) == 0
+    for a, b, label in zip(got[:5], want[:5], ('plus', 'minus_top', 'minus_bottom', 'cref', 'ctrn')):
+        assert a.shape == b.shape, label
+        assert float((a.cpu() - b).abs().max()) <= 1e-12 * float(b.abs().max()), (name, label)

@@ -76,8 +76,8 @@ def test_the_oracle_gain_film_is_the_airy_film(eta, theta, pol):
 def test_lifecycle_gain_film_on_the_cpu(eta, side, monkeypatch):
     """rcwa's resolve and the ETM over the oracle's modes in place of the stage-B kernel."""
     from wavebit_gb300 import engine
-    from test_fields import _oracle_layer_modes
-    monkeypatch.setattr(engine, 'layer_modes', _oracle_layer_modes)
+    from test_fields import use_cpu_stages
+    use_cpu_stages(monkeypatch)
     num = rcwa.Numerics(orders=(1, 1), algorithm='etm')
     for theta in THETAS:
         for pol in ('s', 'p'):

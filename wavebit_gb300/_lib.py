@@ -35,6 +35,8 @@ SIGNATURES = {
     'wb_scattering_matrix': (_i, [_vp, _i, _i, _i, _i] + [_vp] * 16),
     'wb_smm_solve': (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                           _vp, _vp, _vp, _vp, _i, _vp]),
+    'wb_etm_solve': (_i, [_vp, _i, _i, _i, _i] + [_vp] * 16),
+    'wb_layer_amplitudes': (_i, [_vp, _i, _i, _i, _i] + [_vp] * 11 + [_i] + [_vp] * 7),
     'wb_solve_host': (_i, [_vp, _i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                            _vp, _vp, _vp, _vp, _i]),
     'wb_solve_workspace_bytes': (_sz, [_i, _i, _i, _i]),

@@ -264,6 +264,65 @@ int wb_smm_solve(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* W
   return cuda_check("wb_smm_solve");
 }
 
+int wb_etm_solve(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* W, const wb_complex* V,
+                 const wb_complex* q, const double* thickness, const double* wavelength, const double* period,
+                 const double* theta, const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,
+                 const wb_complex* pol, double* R, double* T, wb_complex* amps, int32_t* status, void* stream) {
+  wb::TraceRange trace_("wb:etm_solve");
+  if (!h || !W || !V || !q || !thickness || !wavelength || !period || !theta || !phi || !eps_top || !eps_bot ||
+      !pol || !R || !T || !status)
+    return fail(WB_E_INVALID, "wb_etm_solve: NULL argument");
+  if (B <= 0 || L <= 0 || !valid_orders(hu, hv)) return fail(WB_E_INVALID, "wb_etm_solve: bad sizes B=%d L=%d", B, L);
+  cudaSetDevice(h->device);
+  const int N = (2 * hu + 1) * (2 * hv + 1);
+  int chunk = B;
+  while (chunk > 1 && wb::etm_chunk_bytes(N, L, chunk) > h->budget) chunk = (chunk + 1) / 2;
+  int rc = reserve(h, wb::etm_chunk_bytes(N, L, chunk));
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaMemsetAsync(status, 0, sizeof(int32_t) * B, s);
+  wb::SolveDesc d{B, L, hu, hv, nullptr, nullptr, thickness, wavelength, period, theta, phi, (const cplx*)eps_top,
+                  (const cplx*)eps_bot, (const cplx*)pol};
+  wb::SolveOut o{R, T, (cplx*)amps, status};
+  for (int first = 0; first < B; first += chunk) {
+    int count = std::min(chunk, B - first);
+    if (wb::etm_chunk(s, h->arena, d, (const cplx*)W, (const cplx*)V, (const cplx*)q, first, count, o) != 0)
+      return fail(WB_E_NOMEM, "wb_etm_solve: arena exhausted for a chunk of %d", count);
+  }
+  return cuda_check("wb_etm_solve");
+}
+
+int wb_layer_amplitudes(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* W, const wb_complex* V,
+                        const wb_complex* q, const double* thickness, const double* wavelength, const double* period,
+                        const double* theta, const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,
+                        const wb_complex* C, int k, wb_complex* plus, wb_complex* minus_top, wb_complex* minus_bottom,
+                        wb_complex* cref, wb_complex* ctrn, int32_t* status, void* stream) {
+  wb::TraceRange trace_("wb:layer_amplitudes");
+  if (!h || !W || !V || !q || !thickness || !wavelength || !period || !theta || !phi || !eps_top || !eps_bot || !C ||
+      !plus || !minus_top || !minus_bottom || !cref || !ctrn || !status)
+    return fail(WB_E_INVALID, "wb_layer_amplitudes: NULL argument");
+  if (B <= 0 || L <= 0 || k <= 0 || !valid_orders(hu, hv))
+    return fail(WB_E_INVALID, "wb_layer_amplitudes: bad sizes B=%d L=%d k=%d", B, L, k);
+  cudaSetDevice(h->device);
+  const int N = (2 * hu + 1) * (2 * hv + 1);
+  int chunk = B;
+  while (chunk > 1 && wb::amplitudes_chunk_bytes(N, L, chunk, k) > h->budget) chunk = (chunk + 1) / 2;
+  int rc = reserve(h, wb::amplitudes_chunk_bytes(N, L, chunk, k));
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaMemsetAsync(status, 0, sizeof(int32_t) * B, s);
+  wb::SolveDesc d{B, L, hu, hv, nullptr, nullptr, thickness, wavelength, period, theta, phi, (const cplx*)eps_top,
+                  (const cplx*)eps_bot, nullptr};
+  for (int first = 0; first < B; first += chunk) {
+    int count = std::min(chunk, B - first);
+    if (wb::amplitudes_chunk(s, h->arena, d, (const cplx*)W, (const cplx*)V, (const cplx*)q, (const cplx*)C, k, first,
+                             count, (cplx*)plus, (cplx*)minus_top, (cplx*)minus_bottom, (cplx*)cref, (cplx*)ctrn,
+                             status) != 0)
+      return fail(WB_E_NOMEM, "wb_layer_amplitudes: arena exhausted for a chunk of %d", count);
+  }
+  return cuda_check("wb_layer_amplitudes");
+}
+
 int wb_scattering_matrix(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* W, const wb_complex* V,
                          const wb_complex* q, const double* thickness, const double* wavelength, const double* period,
                          const double* theta, const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,

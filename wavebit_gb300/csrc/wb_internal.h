@@ -68,6 +68,16 @@ int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int co
 size_t scattering_chunk_bytes(int N, int L, int chunk);
 int scattering_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* W, const cplx* V, const cplx* q,
                      int first, int count, cplx* S11, cplx* S12, cplx* S21, cplx* S22, int32_t* status);
+// The ETM connecting algorithm from given modes (wb_etm_solve), FP64; outputs as solve_chunk.
+size_t etm_chunk_bytes(int N, int L, int chunk);
+int etm_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* W, const cplx* V, const cplx* q,
+              int first, int count, const SolveOut& out);
+// Every layer's mode amplitudes for k incidence columns (wb_layer_amplitudes), FP64: Cin (B, n, k);
+// plus / minus_top / minus_bottom (B, L, n, k); cref / ctrn (B, n, k); all column-major per block.
+size_t amplitudes_chunk_bytes(int N, int L, int chunk, int k);
+int amplitudes_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* W, const cplx* V, const cplx* q,
+                     const cplx* Cin, int k, int first, int count, cplx* plus, cplx* minus_top, cplx* minus_bottom,
+                     cplx* cref, cplx* ctrn, int32_t* status);
 size_t smm_chunk_bytes(int N, int L, int chunk, int precision);
 int smm_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* W, const cplx* V, const cplx* q,
               int first, int count, const SolveOut& out, int precision);

@@ -1785,6 +1785,29 @@ __global__ void xq_kernel(int P, int n, const cplx* __restrict__ q, const int* _
   X[idx] = cexp_(cscale(q[idx], -k0 * thick[p]));
 }
 
+// Ports, pairs, the s/p-rotated modes and X for a chunk of solves from given modes (the preamble
+// of wb_smm_solve, wb_etm_solve and wb_layer_amplitudes).
+static void given_modes(cudaStream_t s, const SolveDesc& d, const cplx* Wm, const cplx* Vm, const cplx* qm, int first,
+                        int Bc, const PortVectors& pv, int* pair_layer, int* pair_solve, double* pair_thick,
+                        cplx* OM, cplx* Zb, cplx* X) {
+  const int N = (2 * d.hu + 1) * (2 * d.hv + 1), n = 2 * N, L = d.n_layers, P = Bc * L;
+  const long long n2 = (long long)n * n;
+  ports_kernel<<<Bc, 128, 0, s>>>(Bc, d.hu, d.hv, d.wavelength + first, d.period + 2 * first, d.theta + first,
+                                  d.phi + first, d.eps_top + first, d.eps_bot + first, nullptr, pv); note_launch();
+  pairs_kernel<<<nblk(P, 128), 128, 0, s>>>(Bc, L, nullptr, d.thickness + (long long)first * L, pair_layer,
+                                            pair_solve, pair_thick);
+  note_launch();
+  const long long off = (long long)first * L;
+  cudaMemcpyAsync(OM, Wm + off * n2, sizeof(cplx) * P * n2, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(Zb, Vm + off * n2, sizeof(cplx) * P * n2, cudaMemcpyDeviceToDevice, s);
+  xq_kernel<<<nblk((long long)P * n, 256), 256, 0, s>>>(P, n, qm + off * n, pair_solve, pair_thick,
+                                                        d.wavelength + first, X);
+  note_launch();
+  sp_rotate_kernel<double><<<nblk((long long)P * N * n, 256), 256, 0, s>>>(P, N, pair_solve, pv.c, pv.s,
+                                                                          (Cx<double>*)OM, (Cx<double>*)Zb, n2);
+  note_launch();
+}
+
 size_t smm_chunk_bytes(int N, int L, int chunk, int precision) {
   return solve_chunk_bytes(N, L, chunk, precision == 0 ? 0 : 4);
 }
@@ -1817,19 +1840,7 @@ int smm_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* Wm, con
   int* pivV = ar.get<int>((size_t)P * n);
   int* pivM = ar.get<int>((size_t)P * n);
   if (!ar.ok()) return -1;
-  ports_kernel<<<Bc, 128, 0, s>>>(Bc, d.hu, d.hv, d.wavelength + first, d.period + 2 * first, d.theta + first,
-                                  d.phi + first, d.eps_top + first, d.eps_bot + first, nullptr, pv); note_launch();
-  pairs_kernel<<<nblk(P, 128), 128, 0, s>>>(Bc, L, nullptr, d.thickness + (long long)first * L, pair_layer,
-                                            pair_solve, pair_thick);
-  note_launch();
-  const long long off = (long long)first * L;
-  cudaMemcpyAsync(OM, Wm + off * n2, sizeof(cplx) * P * n2, cudaMemcpyDeviceToDevice, s);
-  cudaMemcpyAsync(Zb, Vm + off * n2, sizeof(cplx) * P * n2, cudaMemcpyDeviceToDevice, s);
-  xq_kernel<<<nblk((long long)P * n, 256), 256, 0, s>>>(P, n, qm + off * n, pair_solve, pair_thick, d.wavelength + first, X);
-  note_launch();
-  sp_rotate_kernel<double><<<nblk((long long)P * N * n, 256), 256, 0, s>>>(P, N, pair_solve, pv.c, pv.s,
-                                                                          (Cx<double>*)OM, (Cx<double>*)Zb, n2);
-  note_launch();
+  given_modes(s, d, Wm, Vm, qm, first, Bc, pv, pair_layer, pair_solve, pair_thick, OM, Zb, X);
   if (precision == 0) {
     using R = double;
     getrf<R>(s, P, n, (Cx<R>*)OM, n, n2, pivW, n, st, L);
@@ -2086,6 +2097,326 @@ int scattering_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* 
     centre_frame_kernel<<<gb, 256, 0, s>>>(Bc, d.hu, d.hv, sb.ctrn, n2, (o ? S12 : S21) + (long long)first * n2);
     note_launch();
   }
+  return 0;
+}
+
+// ---------------------------------------- per-layer field amplitudes (wb_layer_amplitudes)
+// The cascade's own state inside the stack, for the field reconstruction (scattering.py:236-350,
+// _below_reflections and _field_state): for the k columns of Cin, every layer's mode amplitudes
+// at its top face, plus = (b1 + b2)/2 (down-going) and minus_top = (b1 - b2)/2 (up-going), with
+// b1 = bW^-1 wg (g + h), b2 = bV^-1 vg (g - h) from the gap above it (g_l, h_l = R_l g_l), and the
+// up-going amplitudes read at its bottom face from the gap below, minus_bottom = (b1' - b2')/2 with
+// g_{l+1}, h_{l+1} = R_{l+1} g_{l+1} and the same layer's bW, bV. The reflected and transmitted
+// columns come out as in cascade_columns. FP64 throughout.
+
+// plus = (r1 + r2)/2 and minus = (r1 - r2)/2 (minus only when plus is null): k columns per batch
+__global__ void halves_kernel(int B, int n, int k, const cplx* __restrict__ r1, const cplx* __restrict__ r2,
+                              long long bs, cplx* __restrict__ plus, cplx* __restrict__ minus, long long out_bs) {
+  const long long nk = (long long)n * k;
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * nk) return;
+  const long long b = idx / nk, rem = idx % nk;
+  const cplx a = r1[b * bs + rem], c = r2[b * bs + rem];
+  if (plus) plus[b * out_bs + rem] = cscale(cadd(a, c), 0.5);
+  minus[b * out_bs + rem] = cscale(csub(a, c), 0.5);
+}
+
+struct AmplitudeBufs {
+  PortVectors pv;
+  int *pair_layer, *pair_solve;
+  double* pair_thick;
+  cplx *OM, *Zb, *X, *Mk, *Rk, *S1, *S2, *S3, *g, *h, *r1, *r2;
+  int *pivW, *pivV, *pivM, *pivS;
+  template <class A> bool carve(A& ar, int Bc, int L, int N, int k) {
+    const size_t n = 2 * (size_t)N, n2 = n * n, P = (size_t)Bc * L, vk = n * (size_t)k;
+    PortVectors& v = pv;
+    v.kx = ar.template get<double>((size_t)Bc * N); v.ky = ar.template get<double>((size_t)Bc * N);
+    v.c = ar.template get<double>((size_t)Bc * N); v.s = ar.template get<double>((size_t)Bc * N);
+    v.kz_top = ar.template get<cplx>((size_t)Bc * N); v.kz_bot = ar.template get<cplx>((size_t)Bc * N);
+    v.wg = ar.template get<cplx>(Bc * n); v.vg = ar.template get<cplx>(Bc * n);
+    v.r11 = ar.template get<cplx>(Bc * n); v.r12 = ar.template get<cplx>(Bc * n);
+    v.r21 = ar.template get<cplx>(Bc * n); v.r22 = ar.template get<cplx>(Bc * n);
+    v.t11 = ar.template get<cplx>(Bc * n); v.t21 = ar.template get<cplx>(Bc * n);
+    v.nt = ar.template get<cplx>(Bc); v.nb = ar.template get<cplx>(Bc);
+    pair_layer = ar.template get<int>(P); pair_solve = ar.template get<int>(P);
+    pair_thick = ar.template get<double>(P);
+    OM = ar.template get<cplx>(P * n2); Zb = ar.template get<cplx>(P * n2); X = ar.template get<cplx>(P * n);
+    pivW = ar.template get<int>(P * n); pivV = ar.template get<int>(P * n);
+    Mk = ar.template get<cplx>(P * n2); pivM = ar.template get<int>(P * n);
+    Rk = ar.template get<cplx>((P + Bc) * n2);
+    S1 = ar.template get<cplx>(Bc * n2); S2 = ar.template get<cplx>(Bc * n2); S3 = ar.template get<cplx>(Bc * n2);
+    pivS = ar.template get<int>(Bc * n);
+    g = ar.template get<cplx>(Bc * vk); h = ar.template get<cplx>(Bc * vk);
+    r1 = ar.template get<cplx>(Bc * vk); r2 = ar.template get<cplx>(Bc * vk);
+    return ar.ok();
+  }
+};
+
+size_t amplitudes_chunk_bytes(int N, int L, int chunk, int k) {
+  ByteCount c;
+  AmplitudeBufs ab;
+  ab.carve(c, chunk, L, N, k);
+  return c.b;
+}
+
+int amplitudes_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* Wm, const cplx* Vm, const cplx* qm,
+                     const cplx* Cin, int k, int first, int count, cplx* plus, cplx* minus_top, cplx* minus_bottom,
+                     cplx* cref, cplx* ctrn, int32_t* status) {
+  typedef Cx<double> C;
+  const int N = (2 * d.hu + 1) * (2 * d.hv + 1), n = 2 * N, L = d.n_layers;
+  const long long n2 = (long long)n * n, vk = (long long)n * k;
+  const long long lay_bs = (long long)L * n2, lay_ps = (long long)L * n, r_bs = (long long)(L + 1) * n2;
+  const int Bc = count, P = Bc * L;
+  int32_t* st = status + first;
+  ar.reset();
+  AmplitudeBufs a;
+  if (!a.carve(ar, Bc, L, N, k)) return -1;
+  given_modes(s, d, Wm, Vm, qm, first, Bc, a.pv, a.pair_layer, a.pair_solve, a.pair_thick, a.OM, a.Zb, a.X);
+  getrf<double>(s, P, n, (C*)a.OM, n, n2, a.pivW, n, st, L);
+  getrf<double>(s, P, n, (C*)a.Zb, n, n2, a.pivV, n, st, L);
+  cascade_factor<double>(s, Bc, L, N, (C*)a.OM, (C*)a.Zb, a.pivW, a.pivV, a.X, a.pv, st, (C*)a.Mk, a.pivM,
+                         (C*)a.Rk, (C*)a.S1, (C*)a.S2, (C*)a.S3, a.pivS, nullptr, nullptr);
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  const unsigned gk = nblk((long long)Bc * vk, 256);
+  const cplx* Cb = Cin + (long long)first * vk;
+  // the reflected columns and g_0, h_0 (cascade_columns' top)
+  top_kernel<double><<<nblk((long long)Bc * n2, 256), 256, 0, s>>>(Bc, n, (const C*)a.Rk, r_bs, a.pv.r22, (C*)a.S1,
+                                                                   n2);
+  note_launch();
+  getrf<double>(s, Bc, n, (C*)a.S1, n, n2, a.pivS, n, st, 1);
+  dscale_cols_kernel<<<gk, 256, 0, s>>>(Bc, n, k, a.pv.r21, Cb, vk, nullptr, nullptr, 0, a.g, vk); note_launch();
+  getrs<double>(s, Bc, n, (const C*)a.S1, n, n2, a.pivS, n, (C*)a.g, k, n, vk, 0);
+  gemm<double>(s, Bc, n, k, n, one, (const C*)a.Rk, 1, n, r_bs, (const C*)a.g, 1, n, vk, zero, (C*)a.h, 1, n, vk);
+  dscale_cols_kernel<<<gk, 256, 0, s>>>(Bc, n, k, a.pv.r11, Cb, vk, a.pv.r12, a.h, vk, cref + (long long)first * vk,
+                                        vk);
+  note_launch();
+  const long long o_bs = (long long)L * vk;                 // outputs (B, L, n, k)
+  for (int l = 0; l < L; ++l) {
+    const C* bWl = (const C*)(a.OM + l * n2);
+    const C* bVl = (const C*)(a.Zb + l * n2);
+    const long long o = (long long)first * o_bs + (long long)l * vk;
+    gh_cols_kernel<<<gk, 256, 0, s>>>(Bc, n, k, a.g, a.h, a.pv.wg, a.pv.vg, a.r1, a.r2, vk); note_launch();
+    getrs<double>(s, Bc, n, bWl, n, lay_bs, a.pivW + (long long)l * n, lay_ps, (C*)a.r1, k, n, vk, 0);   // b1
+    getrs<double>(s, Bc, n, bVl, n, lay_bs, a.pivV + (long long)l * n, lay_ps, (C*)a.r2, k, n, vk, 0);   // b2
+    halves_kernel<<<gk, 256, 0, s>>>(Bc, n, k, a.r1, a.r2, vk, plus + o, minus_top + o, o_bs); note_launch();
+    ct_cols_kernel<<<gk, 256, 0, s>>>(Bc, n, k, a.r1, a.r2, a.X + (long long)l * n, lay_ps, a.g, vk); note_launch();
+    getrs<double>(s, Bc, n, (const C*)(a.Mk + l * n2), n, lay_bs, a.pivM + (long long)l * n, lay_ps, (C*)a.g, k, n,
+                  vk, 0);                                                                         // g_{l+1}
+    gemm<double>(s, Bc, n, k, n, one, (const C*)(a.Rk + (l + 1) * n2), 1, n, r_bs, (const C*)a.g, 1, n, vk, zero,
+                 (C*)a.h, 1, n, vk);                                                              // h_{l+1}
+    gh_cols_kernel<<<gk, 256, 0, s>>>(Bc, n, k, a.g, a.h, a.pv.wg, a.pv.vg, a.r1, a.r2, vk); note_launch();
+    getrs<double>(s, Bc, n, bWl, n, lay_bs, a.pivW + (long long)l * n, lay_ps, (C*)a.r1, k, n, vk, 0);
+    getrs<double>(s, Bc, n, bVl, n, lay_bs, a.pivV + (long long)l * n, lay_ps, (C*)a.r2, k, n, vk, 0);
+    halves_kernel<<<gk, 256, 0, s>>>(Bc, n, k, a.r1, a.r2, vk, nullptr, minus_bottom + o, o_bs); note_launch();
+  }
+  dscale_cols_kernel<<<gk, 256, 0, s>>>(Bc, n, k, a.pv.t21, a.g, vk, nullptr, nullptr, 0,
+                                        ctrn + (long long)first * vk, vk);
+  note_launch();
+  return 0;
+}
+
+// ------------------------------------------------- ETM connecting algorithm (wb_etm_solve)
+// The enhanced transmittance matrix recursion (solve_2d.py:2619-2843, solve_1d.py:1389-1520) on
+// given modes, bottom-up from the substrate's field matrices F = diag(1, -i kz_bot/eps_bot),
+// G = diag(-i kz_bot, 1):
+//   a = (bW^-1 F + bV^-1 G)/2,  b = (bW^-1 F - bV^-1 G)/2,  Y = X b a^-1 X,
+//   F <- bW (I + Y),  G <- bV (I - Y),  T <- T a^-1 X,
+// then the final matching at the superstrate, [[D1, -F], [D2, -G]] x = c with D1 = diag(1, i kz_top/
+// eps_top), D2 = diag(i kz_top, 1), for the three incidence columns; the reflected amplitudes are
+// x[:n] (p part with the port sign the efficiency kernel reads) and the transmitted T x[n:].
+// T is kept transposed (Tt = X a^-T Tt) so that every solve is a transposed LU solve.
+
+// F = diag(1 (N), -i kz_bot/eps_bot (N)), G = diag(-i kz_bot (N), 1 (N)), Tt = I
+__global__ void etm_init_kernel(int B, int N, const cplx* __restrict__ kz_bot, const cplx* __restrict__ eps_bot,
+                                cplx* __restrict__ F, cplx* __restrict__ G, cplx* __restrict__ Tt) {
+  const int n = 2 * N;
+  const long long n2 = (long long)n * n;
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * n2) return;
+  const long long b = idx / n2, rem = idx % n2;
+  const int i = (int)(rem % n), j = (int)(rem / n);
+  cplx f = cmk(0.0, 0.0), g = cmk(0.0, 0.0), t = cmk(0.0, 0.0);
+  if (i == j) {
+    const cplx mik = (i < N) ? cmul(cmk(0.0, -1.0), kz_bot[b * N + i]) : cmul(cmk(0.0, -1.0), kz_bot[b * N + i - N]);
+    f = (i < N) ? cmk(1.0, 0.0) : cdiv(mik, eps_bot[b]);
+    g = (i < N) ? mik : cmk(1.0, 0.0);
+    t = cmk(1.0, 0.0);
+  }
+  F[idx] = f; G[idx] = g; Tt[idx] = t;
+}
+
+// A = (S1 + S2)/2 and Bt = ((S1 - S2)/2)^T
+__global__ void etm_ab_kernel(int B, int n, const cplx* __restrict__ S1, const cplx* __restrict__ S2,
+                              cplx* __restrict__ A, cplx* __restrict__ Bt) {
+  const long long n2 = (long long)n * n;
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * n2) return;
+  const long long b = idx / n2, rem = idx % n2;
+  const int i = (int)(rem % n), j = (int)(rem / n);
+  const cplx s1 = S1[idx], s2 = S2[idx];
+  A[idx] = cscale(cadd(s1, s2), 0.5);
+  Bt[b * n2 + j + (long long)i * n] = cscale(csub(s1, s2), 0.5);
+}
+
+// Y(i, j) = X_i Zt(j, i) X_j (Zt = (b a^-1)^T) into Y, and Tt(i, j) *= X_i
+__global__ void etm_y_kernel(int B, int n, const cplx* __restrict__ Zt, const cplx* __restrict__ X, long long x_bs,
+                             cplx* __restrict__ Y, cplx* __restrict__ Tt) {
+  const long long n2 = (long long)n * n;
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * n2) return;
+  const long long b = idx / n2, rem = idx % n2;
+  const int i = (int)(rem % n), j = (int)(rem / n);
+  const cplx xi = X[b * x_bs + i];
+  Y[idx] = cmul(cmul(xi, Zt[b * n2 + j + (long long)i * n]), X[b * x_bs + j]);
+  Tt[idx] = cmul(xi, Tt[idx]);
+}
+
+// the final matching matrix [[D1, -F], [D2, -G]] (2n x 2n, column-major) and its three columns
+__global__ void etm_final_kernel(int B, int N, const cplx* __restrict__ F, const cplx* __restrict__ G,
+                                 const cplx* __restrict__ kz_top, const cplx* __restrict__ eps_top,
+                                 const cplx* __restrict__ nt, const cplx* __restrict__ pol, cplx* __restrict__ A,
+                                 cplx* __restrict__ cols) {
+  const int n = 2 * N, m = 2 * n;
+  const long long n2 = (long long)n * n, m2 = (long long)m * m;
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * m2) return;
+  const long long b = idx / m2, rem = idx % m2;
+  const int i = (int)(rem % m), j = (int)(rem / m);
+  const cplx I1 = cmk(0.0, 1.0);
+  cplx v = cmk(0.0, 0.0);
+  if (j >= n) {
+    const long long e = b * n2 + (i % n) + (long long)(j - n) * n;
+    v = cneg(i < n ? F[e] : G[e]);
+  } else if (i == j) {                                          // D1
+    v = (i < N) ? cmk(1.0, 0.0) : cdiv(cmul(I1, kz_top[b * N + i - N]), eps_top[b]);
+  } else if (i == j + n) {                                      // D2
+    v = (j < N) ? cmul(I1, kz_top[b * N + j]) : cmk(1.0, 0.0);
+  }
+  A[idx] = v;
+  if (j < 3) {
+    // incidence columns: the given polarization, pure s (sin, cos of pi/2), pure p
+    cplx as, ap;
+    if (j == 0) { as = pol[2 * b]; ap = pol[2 * b + 1]; }
+    else if (j == 1) { as = cmk(1.0, 0.0); ap = cmk(6.123233995736766e-17, 0.0); }
+    else { as = cmk(0.0, 0.0); ap = cmk(1.0, 0.0); }
+    const int spec = N / 2;
+    const cplx kzi = kz_top[b * N + spec], ntb = nt[b];
+    cplx c = cmk(0.0, 0.0);
+    if (i == spec) c = cneg(as);
+    else if (i == N + spec) c = cmul(ap, cdiv(cmul(ntb, kzi), eps_top[b]));
+    else if (i == 2 * N + spec) c = cmul(cmul(I1, as), kzi);
+    else if (i == 3 * N + spec) c = cmul(cmul(I1, ntb), ap);
+    cols[b * 3 * (long long)m + i + (long long)j * m] = c;
+  }
+}
+
+// cref = [x_s; -x_p] from the final matching's first n unknowns (three columns)
+__global__ void etm_cref_kernel(int B, int N, const cplx* __restrict__ x, cplx* __restrict__ cref) {
+  const int n = 2 * N;
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * n * 3) return;
+  const long long b = idx / (n * 3);
+  const int rem = (int)(idx % (n * 3)), i = rem % n, c = rem / n;
+  const cplx v = x[b * 6 * (long long)n + i + (long long)c * 2 * n];
+  cref[idx] = i < N ? v : cneg(v);
+}
+
+struct EtmBufs {
+  PortVectors pv;
+  int *pair_layer, *pair_solve;
+  double* pair_thick;
+  cplx *OM, *Zb, *LW, *LV, *X, *F, *G, *S1, *S2, *A, *Tt, *Fin, *xc, *cref, *ctrn;
+  int *pivW, *pivV, *pivA, *pivF;
+  template <class Ar> bool carve(Ar& ar, int Bc, int L, int N) {
+    const size_t n = 2 * (size_t)N, n2 = n * n, P = (size_t)Bc * L;
+    PortVectors& v = pv;
+    v.kx = ar.template get<double>((size_t)Bc * N); v.ky = ar.template get<double>((size_t)Bc * N);
+    v.c = ar.template get<double>((size_t)Bc * N); v.s = ar.template get<double>((size_t)Bc * N);
+    v.kz_top = ar.template get<cplx>((size_t)Bc * N); v.kz_bot = ar.template get<cplx>((size_t)Bc * N);
+    v.wg = ar.template get<cplx>(Bc * n); v.vg = ar.template get<cplx>(Bc * n);
+    v.r11 = ar.template get<cplx>(Bc * n); v.r12 = ar.template get<cplx>(Bc * n);
+    v.r21 = ar.template get<cplx>(Bc * n); v.r22 = ar.template get<cplx>(Bc * n);
+    v.t11 = ar.template get<cplx>(Bc * n); v.t21 = ar.template get<cplx>(Bc * n);
+    v.nt = ar.template get<cplx>(Bc); v.nb = ar.template get<cplx>(Bc);
+    pair_layer = ar.template get<int>(P); pair_solve = ar.template get<int>(P);
+    pair_thick = ar.template get<double>(P);
+    OM = ar.template get<cplx>(P * n2); Zb = ar.template get<cplx>(P * n2);
+    LW = ar.template get<cplx>(P * n2); LV = ar.template get<cplx>(P * n2);
+    X = ar.template get<cplx>(P * n);
+    pivW = ar.template get<int>(P * n); pivV = ar.template get<int>(P * n);
+    F = ar.template get<cplx>(Bc * n2); G = ar.template get<cplx>(Bc * n2);
+    S1 = ar.template get<cplx>(Bc * n2); S2 = ar.template get<cplx>(Bc * n2);
+    A = ar.template get<cplx>(Bc * n2); Tt = ar.template get<cplx>(Bc * n2);
+    pivA = ar.template get<int>(Bc * n);
+    Fin = ar.template get<cplx>(Bc * 4 * n2); pivF = ar.template get<int>(Bc * 2 * n);
+    xc = ar.template get<cplx>(Bc * 6 * n);
+    cref = ar.template get<cplx>(Bc * 3 * n); ctrn = ar.template get<cplx>(Bc * 3 * n);
+    return ar.ok();
+  }
+};
+
+size_t etm_chunk_bytes(int N, int L, int chunk) {
+  ByteCount c;
+  EtmBufs eb;
+  eb.carve(c, chunk, L, N);
+  return c.b;
+}
+
+int etm_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* Wm, const cplx* Vm, const cplx* qm,
+              int first, int count, const SolveOut& out) {
+  typedef Cx<double> C;
+  const int N = (2 * d.hu + 1) * (2 * d.hv + 1), n = 2 * N, L = d.n_layers;
+  const long long n2 = (long long)n * n, lay_bs = (long long)L * n2, lay_ps = (long long)L * n;
+  const int Bc = count, P = Bc * L;
+  int32_t* st = out.status + first;
+  ar.reset();
+  EtmBufs e;
+  if (!e.carve(ar, Bc, L, N)) return -1;
+  given_modes(s, d, Wm, Vm, qm, first, Bc, e.pv, e.pair_layer, e.pair_solve, e.pair_thick, e.OM, e.Zb, e.X);
+  cudaMemcpyAsync(e.LW, e.OM, sizeof(cplx) * P * n2, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(e.LV, e.Zb, sizeof(cplx) * P * n2, cudaMemcpyDeviceToDevice, s);
+  getrf<double>(s, P, n, (C*)e.LW, n, n2, e.pivW, n, st, L);
+  getrf<double>(s, P, n, (C*)e.LV, n, n2, e.pivV, n, st, L);
+  const unsigned gn2 = nblk((long long)Bc * n2, 256);
+  etm_init_kernel<<<gn2, 256, 0, s>>>(Bc, N, e.pv.kz_bot, d.eps_bot + first, e.F, e.G, e.Tt); note_launch();
+  const double2 one = make_double2(1, 0), mone = make_double2(-1, 0);
+  for (int l = L - 1; l >= 0; --l) {
+    cudaMemcpyAsync(e.S1, e.F, sizeof(cplx) * Bc * n2, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(e.S2, e.G, sizeof(cplx) * Bc * n2, cudaMemcpyDeviceToDevice, s);
+    getrs<double>(s, Bc, n, (const C*)(e.LW + l * n2), n, lay_bs, e.pivW + (long long)l * n, lay_ps, (C*)e.S1, n, n,
+                  n2, 0);                                                                         // bW^-1 F
+    getrs<double>(s, Bc, n, (const C*)(e.LV + l * n2), n, lay_bs, e.pivV + (long long)l * n, lay_ps, (C*)e.S2, n, n,
+                  n2, 0);                                                                         // bV^-1 G
+    etm_ab_kernel<<<gn2, 256, 0, s>>>(Bc, n, e.S1, e.S2, e.A, e.F); note_launch();               // a, b^T
+    getrf<double>(s, Bc, n, (C*)e.A, n, n2, e.pivA, n, st, 1);
+    getrs<double>(s, Bc, n, (const C*)e.A, n, n2, e.pivA, n, (C*)e.F, n, n, n2, 1);              // (b a^-1)^T
+    getrs<double>(s, Bc, n, (const C*)e.A, n, n2, e.pivA, n, (C*)e.Tt, n, n, n2, 1);             // a^-T Tt
+    etm_y_kernel<<<gn2, 256, 0, s>>>(Bc, n, e.F, e.X + (long long)l * n, lay_ps, e.S1, e.Tt); note_launch();
+    cudaMemcpy2DAsync(e.F, sizeof(cplx) * n2, e.OM + l * n2, sizeof(cplx) * lay_bs, sizeof(cplx) * n2, Bc,
+                      cudaMemcpyDeviceToDevice, s);
+    cudaMemcpy2DAsync(e.G, sizeof(cplx) * n2, e.Zb + l * n2, sizeof(cplx) * lay_bs, sizeof(cplx) * n2, Bc,
+                      cudaMemcpyDeviceToDevice, s);
+    gemm<double>(s, Bc, n, n, n, one, (const C*)(e.OM + l * n2), 1, n, lay_bs, (const C*)e.S1, 1, n, n2, one,
+                 (C*)e.F, 1, n, n2);                                                              // bW (I + Y)
+    gemm<double>(s, Bc, n, n, n, mone, (const C*)(e.Zb + l * n2), 1, n, lay_bs, (const C*)e.S1, 1, n, n2, one,
+                 (C*)e.G, 1, n, n2);                                                              // bV (I - Y)
+  }
+  const long long m2 = 4 * n2;
+  etm_final_kernel<<<nblk((long long)Bc * m2, 256), 256, 0, s>>>(Bc, N, e.F, e.G, e.pv.kz_top, d.eps_top + first,
+                                                                 e.pv.nt, d.pol + 2 * first, e.Fin, e.xc);
+  note_launch();
+  getrf<double>(s, Bc, 2 * n, (C*)e.Fin, 2 * n, m2, e.pivF, 2 * n, st, 1);
+  getrs<double>(s, Bc, 2 * n, (const C*)e.Fin, 2 * n, m2, e.pivF, 2 * n, (C*)e.xc, 3, 2 * n, 6LL * n, 0);
+  const long long v3 = 3LL * n;
+  etm_cref_kernel<<<nblk((long long)Bc * v3, 256), 256, 0, s>>>(Bc, N, e.xc, e.cref); note_launch();
+  const double2 zero = make_double2(0, 0);
+  gemm<double>(s, Bc, n, 3, n, one, (const C*)e.Tt, n, 1, n2, (const C*)(e.xc + n), 1, 2 * n, 6LL * n, zero,
+               (C*)e.ctrn, 1, n, v3);                                                             // T x[n:]
+  efficiency_kernel<double><<<nblk((long long)Bc * N * 3, 256), 256, 0, s>>>(
+      Bc, N, (const C*)e.cref, (const C*)e.ctrn, v3, e.pv, d.eps_top + first, d.eps_bot + first, d.pol + 2 * first,
+      out.R + (long long)first * 3 * N, out.T + (long long)first * 3 * N,
+      out.amps ? out.amps + (long long)first * 12 * N : nullptr, st);
+  note_launch();
   return 0;
 }
 

@@ -213,6 +213,61 @@ def smm_solve(W, V, q, inp, hu, hv, precision='double', amplitudes=False, handle
     return res + ((amps,) if amplitudes else ())
 
 
+def etm_solve(W, V, q, inp, hu, hv, amplitudes=False, handle=None):
+    """The ETM connecting algorithm from given modes (wb_etm_solve, FP64). ``W, V, q`` and
+    ``inp`` as for :func:`smm_solve`. Returns ``(R, T, status[, amps])`` in its layout."""
+    _check_modes(W, V, q, inp, hu, hv)
+    dev = W.device
+    N = n_orders(hu, hv)
+    B, L = inp.B, inp.L
+    Wc = W.transpose(-1, -2).contiguous()
+    Vc = V.transpose(-1, -2).contiguous()
+    qc = q.contiguous()
+    R = torch.empty((B, 3, N), dtype=torch.float64, device=dev)
+    T = torch.empty_like(R)
+    status = torch.zeros(B, dtype=torch.int32, device=dev)
+    amps = torch.empty((B, 3, 4, N), dtype=torch.complex128, device=dev) if amplitudes else None
+    h = handle or _lib.handle(dev.index or 0)
+    _lib.check(h.lib.wb_etm_solve(
+        h.h, B, L, hu, hv, Wc.data_ptr(), Vc.data_ptr(), qc.data_ptr(), inp.thickness.data_ptr(),
+        inp.wavelength.data_ptr(), inp.period.data_ptr(), inp.theta.data_ptr(), inp.phi.data_ptr(),
+        inp.eps_top.data_ptr(), inp.eps_bot.data_ptr(), inp.pol.data_ptr(), R.data_ptr(), T.data_ptr(),
+        amps.data_ptr() if amps is not None else None, status.data_ptr(), _stream()))
+    nu, nv = 2 * hu + 1, 2 * hv + 1
+    res = (R.view(B, 3, nv, nu), T.view(B, 3, nv, nu), status)
+    return res + ((amps,) if amplitudes else ())
+
+
+def layer_amplitudes(W, V, q, inp, hu, hv, C, handle=None):
+    """Every layer's mode amplitudes for the incidence columns ``C`` (B, 2N, k) from given modes
+    (wb_layer_amplitudes, FP64). ``W, V, q`` and ``inp`` as for :func:`smm_solve`. Returns
+    ``(plus, minus_top, minus_bottom, cref, ctrn, status)``: the first three (B, L, 2N, k), the
+    reflected and transmitted columns (B, 2N, k), in natural orientation."""
+    _check_modes(W, V, q, inp, hu, hv)
+    dev = W.device
+    n = 2 * n_orders(hu, hv)
+    B, L = inp.B, inp.L
+    if C.dim() != 3 or C.shape[0] != B or C.shape[1] != n:
+        raise ValueError(f'incidence columns of shape {tuple(C.shape)}, expected ({B}, {n}, k)')
+    k = C.shape[2]
+    Wc = W.transpose(-1, -2).contiguous()
+    Vc = V.transpose(-1, -2).contiguous()
+    qc = q.contiguous()
+    Cc = C.to(device=dev, dtype=torch.complex128).transpose(-1, -2).contiguous()
+    out = torch.empty((3, B, L, k, n), dtype=torch.complex128, device=dev)
+    ends = torch.empty((2, B, k, n), dtype=torch.complex128, device=dev)
+    status = torch.zeros(B, dtype=torch.int32, device=dev)
+    h = handle or _lib.handle(dev.index or 0)
+    _lib.check(h.lib.wb_layer_amplitudes(
+        h.h, B, L, hu, hv, Wc.data_ptr(), Vc.data_ptr(), qc.data_ptr(), inp.thickness.data_ptr(),
+        inp.wavelength.data_ptr(), inp.period.data_ptr(), inp.theta.data_ptr(), inp.phi.data_ptr(),
+        inp.eps_top.data_ptr(), inp.eps_bot.data_ptr(), Cc.data_ptr(), k, out[0].data_ptr(), out[1].data_ptr(),
+        out[2].data_ptr(), ends[0].data_ptr(), ends[1].data_ptr(), status.data_ptr(), _stream()))
+    out = out.transpose(-1, -2)
+    ends = ends.transpose(-1, -2)
+    return out[0], out[1], out[2], ends[0], ends[1], status
+
+
 def scattering_matrix(W, V, q, inp, hu, hv, handle=None):
     """The stack's scattering matrix at its half-space ports from given modes
     (wb_scattering_matrix). ``W, V, q`` and ``inp`` as for :func:`smm_solve`. Returns

@@ -4,9 +4,11 @@ The reference keeps, per wavelength, every layer's ``(+, -)`` mode amplitudes of
 column, read off the S-matrix cascade (rcwa/_engine/scattering.py:236-350), and sums the
 collocated phasors from them on request (rcwa/results.py:148-229,
 rcwa/_engine/field_result.py:332-700, rcwa/_engine/fields.py:630-790). Here the modes are the
-stage-B kernels' (wb_layer_modes, FP64); the amplitudes come from the cascade's own recursion
-(:func:`wavebit_gb300.adjoint.cascade_forward`) and the synthesis is batched matrix products,
-all on the device that holds the modes. ``'plain'`` reconstruction only.
+stage-B kernels' (wb_layer_modes, FP64); the amplitudes come from the cascade kernels' own
+recursion (``wb_layer_amplitudes``, :func:`wavebit_gb300.engine.layer_amplitudes`) and the
+synthesis is batched matrix products on the device that holds the modes.
+:func:`layer_amplitudes` restates the same recursion in torch (the adjoint's
+:func:`wavebit_gb300.adjoint.cascade_forward`), for modes held on the host.
 
 Conventions (the reference's): ``x`` and ``y`` are measured from the cell centre, ``z`` upward
 from the stack's bottom face, a face belongs to the layer above it; values are
@@ -84,18 +86,16 @@ def sp_rotate(W, V, c, s):
     return bw, bv
 
 
-def layer_amplitudes(modes, thickness, k0, pv, C):
-    """Every layer's ``(+, -)`` amplitudes for the incidence columns ``C`` (n, k): ``+`` at the
-    layer's top face, ``-`` at its bottom face (scattering.py:270-350). ``modes`` is a list of
-    ``(W, V, q)`` (Cartesian, entry face first), ``pv`` the port vectors of
-    :func:`wavebit_gb300.adjoint.ports`.
+def layer_faces(modes, thickness, k0, pv, C):
+    """Every layer's ``(plus, minus_top, minus_bottom)`` for the incidence columns ``C`` (n, k),
+    and the reflected and transmitted columns: the torch restatement of ``wb_layer_amplitudes``
+    (scattering.py:270-350). ``modes`` is a list of ``(W, V, q)`` (Cartesian, entry face first),
+    ``pv`` the port vectors of :func:`wavebit_gb300.adjoint.ports`.
 
     With ``g``, ``h = R g`` the gap amplitudes above a layer and ``bW``, ``bV`` its rotated modes,
     the layer's amplitudes at that face are ``(b1 + b2)/2`` down and ``(b1 - b2)/2`` up,
-    ``b1 = bW^-1 wg (g + h)``, ``b2 = bV^-1 vg (g - h)``; the ``-`` amplitude is read at the bottom
-    face from the gap below, except for a mode with ``|k0 q d| < 1``, whose two amplitudes
-    nearly cancel in the field and which takes its top-face value carried down by
-    ``exp(k0 q d)`` (modal_gradient.two_face)."""
+    ``b1 = bW^-1 wg (g + h)``, ``b2 = bV^-1 vg (g - h)``; ``minus_bottom`` is the same up-going
+    half from the gap below the layer, with the same layer's ``bW``, ``bV``."""
     bW, bV, Xs = [], [], []
     for (W, V, q), d in zip(modes, thickness):
         bw, bv = sp_rotate(W, V, pv['c'], pv['s'])
@@ -103,19 +103,35 @@ def layer_amplitudes(modes, thickness, k0, pv, C):
         Xs.append(torch.exp(-k0 * float(d) * q))
     cref, ctrn, sv = cascade_forward(bW, bV, Xs, pv, C)
     wg, vg = pv['wg'][:, None], pv['vg'][:, None]
-    out = []
-    for l, ((W, V, q), d) in enumerate(zip(modes, thickness)):
+    faces = []
+    for l in range(len(modes)):
         b1, b2 = sv['td'][l]['b1'], sv['td'][l]['b2']
-        plus = 0.5 * (b1 + b2)
-        minus_top = 0.5 * (b1 - b2)
         gn = sv['g'][l + 1]
         hn = sv['Rk'][l + 1] @ gn
         minus_bottom = 0.5 * (torch.linalg.solve(bW[l], wg * (gn + hn)) - torch.linalg.solve(bV[l], vg * (gn - hn)))
+        faces.append((0.5 * (b1 + b2), 0.5 * (b1 - b2), minus_bottom))
+    return faces, cref, ctrn
+
+
+def layer_amplitudes(modes, thickness, k0, pv, C):
+    """Every layer's ``(+, -)`` amplitudes and the reflected and transmitted columns, by the torch
+    recursion (:func:`layer_faces` and :func:`face_amplitudes`)."""
+    faces, cref, ctrn = layer_faces(modes, thickness, k0, pv, C)
+    return face_amplitudes(faces, [q for _, _, q in modes], thickness, k0), cref, ctrn
+
+
+def face_amplitudes(faces, qs, thickness, k0):
+    """Each layer's ``(+, -)`` amplitudes from its ``(plus, minus_top, minus_bottom)``: the ``-``
+    amplitude is read at the bottom face, except for a mode with ``|k0 q d| < 1``, whose two
+    amplitudes nearly cancel in the field and which takes its top-face value carried down by
+    ``exp(k0 q d)`` (scattering.py:225-232, modal_gradient.two_face)."""
+    out = []
+    for (plus, minus_top, minus_bottom), q, d in zip(faces, qs, thickness):
         kd = k0 * float(d)
         keep = (torch.abs(q * kd) < TOP_FACE)[:, None]
         carried = torch.exp(torch.where(keep[:, 0], kd * q, torch.zeros_like(q)))[:, None] * minus_top
         out.append((plus, torch.where(keep, carried, minus_bottom)))
-    return out, cref, ctrn
+    return out
 
 
 def order_waves(kx, ky, c, s, kzt, kzb, n_top, n_bot, ratios, pol):
@@ -422,17 +438,30 @@ def order_parity(hu, hv, device):
     return torch.as_tensor(m.reshape(-1) % 2 == 1, device=device)
 
 
-def build_state(modes, epz_i, thickness, wavelength, pv, pol, hu, hv, rasters=None):
-    """The :class:`FieldState` of one wavelength from its layers' ``(W, V, q)`` (Cartesian,
-    entry face first), their corner-frame ``epz_i`` slots and the port vectors ``pv``; ``pol``
-    is the source's ``(a_s, a_p)``."""
-    dev = pv['kx'].device
-    k0 = 2 * math.pi / float(wavelength)
+def incident_column(pv, pol):
+    """The incident column ``(2N, 1)`` in the superstrate's port variables: ``a_s`` on the
+    specular order's s entry, ``-i n_top a_p`` on its p entry."""
     N = pv['kx'].shape[0]
-    C = torch.zeros((2 * N, 1), dtype=torch.complex128, device=dev)
+    C = torch.zeros((2 * N, 1), dtype=torch.complex128, device=pv['kx'].device)
     C[N // 2, 0] = complex(pol[0])
     C[N + N // 2, 0] = -1j * complex(pv['nt']) * complex(pol[1])
-    amps, cref, ctrn = layer_amplitudes(modes, thickness, k0, pv, C)
+    return C
+
+
+def build_state(modes, epz_i, thickness, wavelength, pv, pol, hu, hv, rasters=None, faces=None):
+    """The :class:`FieldState` of one wavelength from its layers' ``(W, V, q)`` (Cartesian,
+    entry face first), their corner-frame ``epz_i`` slots and the port vectors ``pv``; ``pol``
+    is the source's ``(a_s, a_p)``. ``faces``: the incident column's amplitudes as
+    ``wb_layer_amplitudes`` returns them for this solve, ``(plus, minus_top, minus_bottom)`` each
+    (L, 2N, 1) and ``(cref, ctrn)`` each (2N, 1); without it the torch recursion computes them."""
+    dev = pv['kx'].device
+    k0 = 2 * math.pi / float(wavelength)
+    if faces is None:
+        amps, cref, ctrn = layer_amplitudes(modes, thickness, k0, pv, incident_column(pv, pol))
+    else:
+        ptop, mtop, mbot, cref, ctrn = faces
+        amps = face_amplitudes([(ptop[l], mtop[l], mbot[l]) for l in range(len(modes))],
+                               [q for _, _, q in modes], thickness, k0)
     rasters = rasters if rasters is not None else [None] * len(modes)
     layers = tuple(LayerState(W, V, q, float(d), e, plus[:, 0], minus[:, 0], r)
                    for (W, V, q), d, e, (plus, minus), r in zip(modes, thickness, epz_i, amps, rasters))

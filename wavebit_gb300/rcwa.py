@@ -984,23 +984,27 @@ class Prepared:
                       ports=_ports_context(r, wl, th), provenance=_provenance(r, self.numerics, self.precision))
 
     def _solve_etm(self, r, conv, layer_index, fields=False):
-        """``Numerics(algorithm='etm')``: the ETM recursion over the FP64 modes of every
-        (wavelength, layer) pair (:mod:`wavebit_gb300.etm`), a cross-check of the cascade on the
-        same modes. Fields, when asked for, are read off the cascade's state as with the SMM."""
-        from .etm import etm_solve
+        """``Numerics(algorithm='etm')``: the ETM recursion (``wb_etm_solve``) over the FP64 modes
+        of every (wavelength, layer) pair, a cross-check of the cascade on the same modes. Fields,
+        when asked for, are read off the cascade's state as with the SMM."""
         hu, hv = r['orders']
         B, L = layer_index.shape
         n = 2 * engine.n_orders(hu, hv)
         wl = np.asarray(r['wavelengths'], dtype=np.float64).copy()
         th = np.asarray(r['thetas'], dtype=np.float64).copy()
-        Rs, Ts, As = [None] * B, [None] * B, [None] * B
+        parts = []
         for idx, pvs, q, W, V in self._mode_chunks(r, conv, layer_index, wl, th, (2 * L + 4) * n * n * 16):
-            for i, b in enumerate(idx):
-                modes = [(W[i * L + l], V[i * L + l], q[i * L + l]) for l in range(L)]
-                Rs[b], Ts[b], As[b] = etm_solve(modes, r['thickness'], 2 * math.pi / float(wl[b]), pvs[i],
-                                                r['pol'], 2 * hu + 1, 2 * hv + 1, amplitudes=True)
-        R, T, amps = torch.stack(Rs), torch.stack(Ts), torch.stack(As)
-        if not (bool(torch.isfinite(R).all()) and bool(torch.isfinite(T).all())):
+            k = len(idx)
+            inp = engine.BatchInputs(layer_index[idx], np.tile(r['thickness'], (k, 1)), wl[idx],
+                                     np.tile(r['period'], (k, 1)), th[idx], np.full(k, r['phi']),
+                                     np.full(k, r['eps_top']), np.full(k, r['eps_bot']), np.tile(r['pol'], (k, 1)),
+                                     device=W.device)
+            parts.append(engine.etm_solve(W, V, q, inp, hu, hv, amplitudes=True, handle=self.handle))
+        R, T, stt, amps = (torch.cat([p_[j] for p_ in parts]) for j in range(4))
+        st = stt.cpu().numpy()
+        if np.any(st & _lib.WB_ST_SINGULAR):
+            raise NumericalError('an ETM factorization met an exact zero pivot', code='rcwa.singular')
+        if np.any(st) or not (bool(torch.isfinite(R).all()) and bool(torch.isfinite(T).all())):
             raise NumericalError('the ETM solve produced non-finite results', code='rcwa.nonfinite')
         st = np.zeros(B, dtype=np.int32)
         diag = {'solve_path': ('2d',) * B, 'algorithm': 'etm', 'effective_wavelengths': tuple(float(v) for v in wl),
@@ -1046,12 +1050,22 @@ class Prepared:
         B, L = layer_index.shape
         n = 2 * engine.n_orders(hu, hv)
         states = []
-        for idx, pvs, q, W, V in self._mode_chunks(r, conv, layer_index, wl, th, (2 * L + 2) * n * n * 16):
+        for idx, pvs, q, W, V in self._mode_chunks(r, conv, layer_index, wl, th, (6 * L + 2) * n * n * 16):
+            k = len(idx)
+            inp = engine.BatchInputs(layer_index[idx], np.tile(r['thickness'], (k, 1)), wl[idx],
+                                     np.tile(r['period'], (k, 1)), th[idx], np.full(k, r['phi']),
+                                     np.full(k, r['eps_top']), np.full(k, r['eps_bot']), np.tile(r['pol'], (k, 1)),
+                                     device=W.device)
+            C = torch.stack([F.incident_column(pv, r['pol']) for pv in pvs])
+            plus, mtop, mbot, cref, ctrn, st = engine.layer_amplitudes(W, V, q, inp, hu, hv, C, handle=self.handle)
+            if np.any(st.cpu().numpy() & _lib.WB_ST_SINGULAR):
+                raise NumericalError('a layer factorization met an exact zero pivot', code='rcwa.singular')
             for i, b in enumerate(idx):
                 modes = [(W[i * L + l], V[i * L + l], q[i * L + l]) for l in range(L)]
                 epz = [conv.slot(2)[int(layer_index[b][l])] for l in range(L)]
                 rasters = [r['rasters'][int(layer_index[b][l])] for l in range(L)]
-                states.append(F.build_state(modes, epz, r['thickness'], wl[b], pvs[i], r['pol'], hu, hv, rasters))
+                states.append(F.build_state(modes, epz, r['thickness'], wl[b], pvs[i], r['pol'], hu, hv, rasters,
+                                            faces=(plus[i], mtop[i], mbot[i], cref[i], ctrn[i])))
         return tuple(states)
 
     def _scattering(self, r, conv, layer_index, wl, th):
