@@ -56,7 +56,8 @@ typedef struct wb_handle wb_handle;
 
 /* Version of this ABI (major * 100 + minor): 2.0 = the precision codes above (WB_PRECISION_MIXED
  * is the FP32 eigen-solve with Newton steps), wb_smm_solve and wb_workspace_bytes; 2.1 adds
- * wb_assemble_li_integrated and wb_scattering_matrix. */
+ * wb_assemble_li_integrated and wb_scattering_matrix; 2.2 adds the reverse passes wb_smm_solve_vjp,
+ * wb_layer_modes_vjp and wb_assemble_li_vjp. */
 int wb_version(void);
 
 /* Message of the calling thread's last failure, NUL-terminated, truncated to len. */
@@ -145,6 +146,45 @@ int wb_smm_solve(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* W
                  const double* theta, const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,
                  const wb_complex* pol, double* R, double* T, wb_complex* amps, int32_t* status, int precision,
                  void* stream);
+
+/* Reverse passes (vector-Jacobian products), FP64, on the device. Cotangents follow torch's
+ * convention: for a real loss l and a complex z = x + iy the cotangent is dl/dx + i dl/dy (a real
+ * input's gradient is its real part). Cotangent inputs marked "or NULL" count as zero. They
+ * replace the reference's differentiated backends for this path: rcwa/_engine/modal_gradient.py
+ * :56-251 (eigen-solve generator with broadened reciprocal gaps), _common/backend.py:1724-1759
+ * (_eig_grad), and torch autograd through scattering.py:116-200, 907-994 and
+ * factorization.py:289-671.
+ *
+ * Reverse of wb_smm_solve (FP64 form): from the cotangents g_R, g_T (device, (B, 3, N), or NULL)
+ * of its R and T, the cotangents of its W, V (B*L, 2N, 2N), q (B*L, 2N) and thickness (B, L),
+ * all overwritten. The cascade is recomputed with its intermediates, chunked by the handle's
+ * budget. Inputs as wb_smm_solve; status (B) gets WB_ST_SINGULAR for a singular factor. */
+int wb_smm_solve_vjp(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* W, const wb_complex* V,
+                     const wb_complex* q, const double* thickness, const double* wavelength, const double* period,
+                     const double* theta, const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,
+                     const wb_complex* pol, const double* g_R, const double* g_T, wb_complex* g_W, wb_complex* g_V,
+                     wb_complex* g_q, double* g_thickness, int32_t* status, void* stream);
+
+/* Reverse of wb_layer_modes: from the cotangents of its outputs w, q (n_pairs, 2N) and W, V
+ * (n_pairs, 2N, 2N) (each or NULL), the cotangents g_conv (device, (n_conv, 3, N, N), overwritten)
+ * of the slots epx, epy, epz_i, summed over the pairs that read each layer. The other inputs are
+ * wb_layer_modes's inputs and outputs. Each mode's scale is a free gauge that no RCWA answer
+ * depends on, so the eigenvector cotangent's component along it is dropped; exactly degenerate
+ * eigenvalues use the broadened gap conj(d)/(|d|^2 + (2N u max|w|)^2). status (n_pairs) or NULL. */
+int wb_layer_modes_vjp(wb_handle* h, int n_pairs, int hu, int hv, int n_conv, const wb_complex* conv,
+                       const int32_t* pair_layer, const double* kx, const double* ky, const wb_complex* w,
+                       const wb_complex* q, const wb_complex* W, const wb_complex* V, const wb_complex* g_w,
+                       const wb_complex* g_q, const wb_complex* g_W, const wb_complex* g_V, wb_complex* g_conv,
+                       int32_t* status, void* stream);
+
+/* Reverse of wb_assemble_li (sampled coefficients, fixed nesting): from the cotangents of the
+ * slots (device, each (L, N, N) column-major, or NULL) the cotangent g_eps (device, (L, ny, nx),
+ * overwritten) of the rasters. eps is the forward's input, epx and epz_i its outputs (their
+ * inverses' reverse needs them). status (1) or NULL. */
+int wb_assemble_li_vjp(wb_handle* h, const wb_complex* eps, int L, int ny, int nx, int hu, int hv,
+                       const wb_complex* epx, const wb_complex* epz_i, const wb_complex* g_epx,
+                       const wb_complex* g_epy, const wb_complex* g_epz_i, wb_complex* g_eps, int32_t* status,
+                       void* stream);
 
 /* The stack's scattering matrix at its two half-space ports, as the reference publishes it
  * (Outputs(scattering=True), result.scattering), from given modes (FP64). Inputs as wb_smm_solve

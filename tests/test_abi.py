@@ -34,7 +34,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_abi_version(lib):
-    assert lib.wb_version() == 201
+    assert lib.wb_version() == 202
 
 
 def test_binding_table_covers_the_header():
@@ -128,6 +128,31 @@ def test_scattering_matrix_refuses_bad_arguments_before_any_device_work(lib):
     assert 'wb_scattering_matrix' in _lib.last_error()
 
 
+def test_reverse_passes_refuse_bad_arguments_before_any_device_work(lib):
+    """The wb_*_vjp entry points check pointers and sizes on the host: NULL required arguments,
+    empty batches and bad orders are WB_E_INVALID with a message naming the entry point; the
+    optional cotangents may be NULL."""
+    from wavebit_gb300 import _lib
+    fake = ctypes.create_string_buffer(64)
+    p = ctypes.addressof(fake)
+    smm = lambda B, h=p, out=p: (h, B, 2, 1, 1) + (p,) * 11 + (None, None, out, p, p, p, p, None)
+    assert lib.wb_smm_solve_vjp(*smm(2, h=None)) == _lib.WB_E_INVALID
+    assert 'NULL' in _lib.last_error()
+    assert lib.wb_smm_solve_vjp(*smm(2, out=None)) == _lib.WB_E_INVALID
+    assert lib.wb_smm_solve_vjp(*smm(0)) == _lib.WB_E_INVALID
+    assert 'wb_smm_solve_vjp' in _lib.last_error()
+    modes = lambda P, hu=1, conv=p: (p, P, hu, 1, 2, conv) + (p,) * 7 + (None,) * 4 + (p, None, None)
+    assert lib.wb_layer_modes_vjp(*modes(3, conv=None)) == _lib.WB_E_INVALID
+    assert lib.wb_layer_modes_vjp(*modes(0)) == _lib.WB_E_INVALID
+    assert lib.wb_layer_modes_vjp(*modes(3, hu=-2)) == _lib.WB_E_INVALID
+    assert 'wb_layer_modes_vjp' in _lib.last_error()
+    asm = lambda L, hv=1, g=p: (p, p, L, 8, 8, 1, hv, p, p, None, None, None, g, None, None)
+    assert lib.wb_assemble_li_vjp(*asm(2, g=None)) == _lib.WB_E_INVALID
+    assert lib.wb_assemble_li_vjp(*asm(0)) == _lib.WB_E_INVALID
+    assert lib.wb_assemble_li_vjp(*asm(2, hv=43)) == _lib.WB_E_INVALID
+    assert 'wb_assemble_li_vjp' in _lib.last_error()
+
+
 def test_header_is_plain_c_and_a_c_program_links(lib, tmp_path):
     """The boundary is a C ABI: the public header compiles as strict C99 (no C++ or torch types)
     and a C program links libwbgpu.so and calls its host-only entry points."""
@@ -157,4 +182,4 @@ int main(void) {
     run = subprocess.run([str(exe)], capture_output=True, text=True)
     assert run.returncode == 0, run.stderr
     version, rc, first, last, ws = run.stdout.split()
-    assert (int(version), int(rc), int(first), int(last)) == (201, 0, -2, 2) and int(ws) > 0
+    assert (int(version), int(rc), int(first), int(last)) == (202, 0, -2, 2) and int(ws) > 0

@@ -48,6 +48,9 @@ SIGNATURES = {
     'wb_tensor_core_errors': (_ll, []),
     'wb_profile_qr_read': (_i, [_i, _vp, _vp, _vp]),
     'wb_assemble_li_noalloc': (_i, [_vp, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
+    'wb_smm_solve_vjp': (_i, [_vp, _i, _i, _i, _i] + [_vp] * 19),
+    'wb_layer_modes_vjp': (_i, [_vp, _i, _i, _i, _i] + [_vp] * 15),
+    'wb_assemble_li_vjp': (_i, [_vp, _vp, _i, _i, _i, _i, _i] + [_vp] * 8),
     'wb_assemble_li_noalloc_limit': (_sz, []),
 }
 

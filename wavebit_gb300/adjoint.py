@@ -20,10 +20,13 @@ reverse pass:
 * Li's rules      outer inverse, block-Toeplitz gather, staircase series (an exact corrected DFT,
                   linear in the raster), inner Toeplitz inverses, 1/eps  (factorization.py:289-671)
 
-The forward of stages A and B runs on the CUDA kernels (libwbgpu.so, ``impl='gb300'``); the
-cascade and every reverse pass are dense complex algebra on the device through torch
-(cuBLAS/cuSOLVER). ``impl='torch'`` runs stages A and B in torch as well, which is what the
-CPU tests use to check the reverse formulas against finite differences.
+With ``impl='gb300'`` every stage and every reverse pass runs on the library's kernels through
+its C ABI: wb_assemble_li, wb_layer_modes and wb_smm_solve forward, then wb_smm_solve_vjp,
+wb_layer_modes_vjp and wb_assemble_li_vjp (csrc/wb_vjp.h: the same formulas as the functions
+below, batched over the wavelengths of a chunk). ``impl='torch'`` evaluates the formulas below
+in torch, stage by stage and one wavelength at a time; it is the restatement the kernels are
+held to and what the CPU tests check against finite differences. The wavelength gradient (a
+forward tangent) runs the torch restatement over the kernels' stage-A slots and eigenpairs.
 """
 import math
 
@@ -542,6 +545,9 @@ def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weigh
         raise ValueError("fourier_coefficients must be 'sampled' or 'integrated'")
     device = device or ('cuda' if impl == 'gb300' else 'cpu')
     eps = torch.as_tensor(eps, dtype=torch.complex128, device=device)
+    if impl == 'gb300' and not grad_wavelength:
+        return _solve_and_grad_kernels(eps, thickness, wavelengths, period, hu, hv, weights_R, weights_T, theta, phi,
+                                       eps_top, eps_bot, pol, device, grad, hbm_budget)
     L = eps.shape[0]
     N = (2 * hu + 1) * (2 * hv + 1)
     n = 2 * N
@@ -627,6 +633,66 @@ def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weigh
         return (loss, torch.stack(Rs), torch.stack(Ts), None, None) + extra
     g_eps = torch.stack([li_conv_adjoint(g_conv[l], hu, hv, saved_a[l][1]) for l in range(L)])
     return (loss, torch.stack(Rs), torch.stack(Ts), g_eps.real, g_th) + extra
+
+
+def _solve_and_grad_kernels(eps, thickness, wavelengths, period, hu, hv, weights_R, weights_T, theta, phi, eps_top,
+                            eps_bot, pol, device, grad, hbm_budget):
+    """:func:`solve_and_grad` with every stage and every reverse pass on the library's kernels:
+    wb_assemble_li, then per chunk of wavelengths wb_layer_modes (FP64), wb_smm_solve (FP64),
+    wb_smm_solve_vjp and wb_layer_modes_vjp, and finally wb_assemble_li_vjp. The chunk's modes
+    are dropped after its reverse pass."""
+    from . import engine
+    L = eps.shape[0]
+    N = (2 * hu + 1) * (2 * hv + 1)
+    n = 2 * N
+    cs = engine.assemble(eps, hu, hv)
+    wls = [float(v) for v in np.atleast_1d(wavelengths)]
+    B = len(wls)
+    th = [float(t) for t in np.asarray(thickness, dtype=np.float64).reshape(L)]
+    chunk = _chunk_size(L, n, hbm_budget, device) or B
+    wR_all = np.asarray(weights_R, dtype=np.float64).reshape(B, N)
+    wT_all = np.asarray(weights_T, dtype=np.float64).reshape(B, N)
+    g_conv = torch.zeros_like(cs.buf)
+    g_th = torch.zeros(L, dtype=torch.float64, device=device)
+    loss = 0.0
+    Rs, Ts = [], []
+    for b0 in range(0, B, chunk):
+        lam = wls[b0:b0 + chunk]
+        Bc = len(lam)
+        pvs = [ports(x, period, theta, phi, eps_top, eps_bot, hu, hv, device) for x in lam]
+        kx = torch.stack([pv['kx'] for pv in pvs for _ in range(L)])
+        ky = torch.stack([pv['ky'] for pv in pvs for _ in range(L)])
+        pl = np.tile(np.arange(L), Bc)
+        w, q, W, V, st = engine.layer_modes(cs, pl, kx, ky, precision='double')
+        if int((st.cpu().numpy() & 2).sum()):
+            raise RuntimeError('the eigen-solve did not converge')
+        inp = engine.BatchInputs([list(range(L))] * Bc, [th] * Bc, lam, [list(period)] * Bc, [theta] * Bc,
+                                 [phi] * Bc, [complex(eps_top)] * Bc, [complex(eps_bot)] * Bc, [list(pol)] * Bc,
+                                 device=device)
+        R, T, st = engine.smm_solve(W, V, q, inp, hu, hv, precision='double')
+        R0, T0 = R[:, 0].reshape(Bc, N), T[:, 0].reshape(Bc, N)
+        wR = torch.as_tensor(wR_all[b0:b0 + Bc], device=device)
+        wT = torch.as_tensor(wT_all[b0:b0 + Bc], device=device)
+        loss += float((wR * R0).sum() + (wT * T0).sum())
+        Rs.append(R0); Ts.append(T0)
+        if not grad:
+            continue
+        gR = torch.zeros((Bc, 3, N), dtype=torch.float64, device=device)
+        gT = torch.zeros_like(gR)
+        gR[:, 0] = wR
+        gT[:, 0] = wT
+        gW, gV, gq, gth, st = engine.smm_solve_vjp(W, V, q, inp, hu, hv, gR, gT)
+        if int((st.cpu().numpy() & 1).sum()):
+            raise RuntimeError('a cascade factor is singular')
+        g_th += gth.sum(dim=0)
+        gc, _ = engine.layer_modes_vjp(cs, pl, kx, ky, w, q, W, V, g_q=gq, g_W=gW, g_V=gV)
+        g_conv += gc.buf
+        del w, q, W, V, gW, gV, gq
+    Rt, Tt = torch.cat(Rs), torch.cat(Ts)
+    if not grad:
+        return loss, Rt, Tt, None, None
+    g_eps = engine.assemble_vjp(eps, cs, engine.ConvStack(g_conv, hu, hv))
+    return loss, Rt, Tt, g_eps.real, g_th
 
 
 class EfficiencyLoss(torch.autograd.Function):

@@ -14,9 +14,9 @@ PKG = os.path.dirname(HERE)
 ROOT = os.path.dirname(PKG)
 LIB = os.path.join(PKG, 'libwbgpu.so')
 OBJ = os.path.join(PKG, '_build')
-SOURCES = ['wb_linalg.cu', 'wb_eig.cu', 'wb_assemble.cu', 'wb_solve.cu', 'wb_api.cu', 'wb_noalloc.cu', 'wb_tc.cu']
+SOURCES = ['wb_linalg.cu', 'wb_eig.cu', 'wb_assemble.cu', 'wb_solve.cu', 'wb_api.cu', 'wb_noalloc.cu', 'wb_tc.cu', 'wb_vjp.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
-FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '--expt-relaxed-constexpr',
+FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '--expt-relaxed-constexpr', '--extended-lambda',
          '-I', os.path.join(ROOT, 'include')]
 
 

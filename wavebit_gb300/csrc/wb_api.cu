@@ -76,7 +76,7 @@ int noalloc_fail(const char* msg) { g_err = msg; return WB_E_INVALID; }
 
 extern "C" {
 
-int wb_version(void) { return 201; }
+int wb_version(void) { return 202; }
 
 int wb_last_error(char* buf, size_t len) {
   if (!buf || len == 0) return WB_E_INVALID;
@@ -146,6 +146,76 @@ int wb_assemble_li(wb_handle* h, const wb_complex* eps, int L, int ny, int nx, i
   cudaStream_t s = (cudaStream_t)stream;
   wb::assemble_li(s, (const cplx*)eps, L, ny, nx, hu, hv, (cplx*)epx, (cplx*)epy, (cplx*)epz_i, h->buf, status);
   return cuda_check("wb_assemble_li");
+}
+
+int wb_assemble_li_vjp(wb_handle* h, const wb_complex* eps, int L, int ny, int nx, int hu, int hv,
+                       const wb_complex* epx, const wb_complex* epz_i, const wb_complex* g_epx,
+                       const wb_complex* g_epy, const wb_complex* g_epz_i, wb_complex* g_eps, int32_t* status,
+                       void* stream) {
+  wb::TraceRange trace_("wb:assemble_li_vjp");
+  if (!h || !eps || !epx || !epz_i || !g_eps) return fail(WB_E_INVALID, "wb_assemble_li_vjp: NULL argument");
+  if (L <= 0 || ny <= 0 || nx <= 0 || !valid_orders(hu, hv))
+    return fail(WB_E_INVALID, "wb_assemble_li_vjp: bad sizes L=%d ny=%d nx=%d orders=(%d,%d)", L, ny, nx, hu, hv);
+  cudaSetDevice(h->device);
+  int rc = reserve(h, wb::assemble_vjp_bytes(L, ny, nx, hu, hv));
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (status) cudaMemsetAsync(status, 0, sizeof(int32_t), s);
+  if (wb::assemble_vjp_run(s, h->arena, L, ny, nx, hu, hv, (const cplx*)eps, (const cplx*)epx, (const cplx*)epz_i,
+                           (const cplx*)g_epx, (const cplx*)g_epy, (const cplx*)g_epz_i, (cplx*)g_eps, status) != 0)
+    return fail(WB_E_NOMEM, "wb_assemble_li_vjp: arena exhausted");
+  return cuda_check("wb_assemble_li_vjp");
+}
+
+int wb_layer_modes_vjp(wb_handle* h, int n_pairs, int hu, int hv, int n_conv, const wb_complex* conv,
+                       const int32_t* pair_layer, const double* kx, const double* ky, const wb_complex* w,
+                       const wb_complex* q, const wb_complex* W, const wb_complex* V, const wb_complex* g_w,
+                       const wb_complex* g_q, const wb_complex* g_W, const wb_complex* g_V, wb_complex* g_conv,
+                       int32_t* status, void* stream) {
+  wb::TraceRange trace_("wb:layer_modes_vjp");
+  if (!h || !conv || !pair_layer || !kx || !ky || !w || !q || !W || !V || !g_conv)
+    return fail(WB_E_INVALID, "wb_layer_modes_vjp: NULL argument");
+  if (n_pairs <= 0 || n_conv <= 0 || !valid_orders(hu, hv))
+    return fail(WB_E_INVALID, "wb_layer_modes_vjp: bad sizes n_pairs=%d n_conv=%d", n_pairs, n_conv);
+  cudaSetDevice(h->device);
+  const int N = (2 * hu + 1) * (2 * hv + 1);
+  const int chunk = wb::layer_modes_vjp_chunk(n_pairs, N, h->budget);
+  int rc = reserve(h, wb::layer_modes_vjp_bytes(N, chunk));
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (status) cudaMemsetAsync(status, 0, sizeof(int32_t) * n_pairs, s);
+  if (wb::layer_modes_vjp_run(s, h->arena, h->buf_bytes, n_pairs, N, n_conv, (const cplx*)conv,
+                              (const int*)pair_layer, kx, ky, (const cplx*)w, (const cplx*)q, (const cplx*)W,
+                              (const cplx*)V, (const cplx*)g_w, (const cplx*)g_q, (const cplx*)g_W, (const cplx*)g_V,
+                              (cplx*)g_conv, status) != 0)
+    return fail(WB_E_NOMEM, "wb_layer_modes_vjp: arena exhausted for a chunk of %d pairs", chunk);
+  return cuda_check("wb_layer_modes_vjp");
+}
+
+int wb_smm_solve_vjp(wb_handle* h, int B, int L, int hu, int hv, const wb_complex* W, const wb_complex* V,
+                     const wb_complex* q, const double* thickness, const double* wavelength, const double* period,
+                     const double* theta, const double* phi, const wb_complex* eps_top, const wb_complex* eps_bot,
+                     const wb_complex* pol, const double* g_R, const double* g_T, wb_complex* g_W, wb_complex* g_V,
+                     wb_complex* g_q, double* g_thickness, int32_t* status, void* stream) {
+  wb::TraceRange trace_("wb:smm_solve_vjp");
+  if (!h || !W || !V || !q || !thickness || !wavelength || !period || !theta || !phi || !eps_top || !eps_bot ||
+      !pol || !g_W || !g_V || !g_q || !g_thickness || !status)
+    return fail(WB_E_INVALID, "wb_smm_solve_vjp: NULL argument");
+  if (B <= 0 || L <= 0 || !valid_orders(hu, hv))
+    return fail(WB_E_INVALID, "wb_smm_solve_vjp: bad sizes B=%d L=%d", B, L);
+  cudaSetDevice(h->device);
+  const int N = (2 * hu + 1) * (2 * hv + 1);
+  const int chunk = wb::smm_vjp_chunk(B, N, L, h->budget);
+  int rc = reserve(h, wb::smm_vjp_bytes(N, L, chunk));
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaMemsetAsync(status, 0, sizeof(int32_t) * B, s);
+  wb::SolveDesc d{B, L, hu, hv, nullptr, nullptr, thickness, wavelength, period, theta, phi, (const cplx*)eps_top,
+                  (const cplx*)eps_bot, (const cplx*)pol};
+  if (wb::smm_vjp_run(s, h->arena, h->buf_bytes, d, (const cplx*)W, (const cplx*)V, (const cplx*)q, g_R, g_T,
+                      (cplx*)g_W, (cplx*)g_V, (cplx*)g_q, g_thickness, status) != 0)
+    return fail(WB_E_NOMEM, "wb_smm_solve_vjp: arena exhausted for a chunk of %d solves", chunk);
+  return cuda_check("wb_smm_solve_vjp");
 }
 
 int wb_assemble_li_integrated(wb_handle* h, const wb_complex* eps, int L, int ny, int nx, const double* x_edges,

@@ -78,6 +78,26 @@ size_t amplitudes_chunk_bytes(int N, int L, int chunk, int k);
 int amplitudes_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* W, const cplx* V, const cplx* q,
                      const cplx* Cin, int k, int first, int count, cplx* plus, cplx* minus_top, cplx* minus_bottom,
                      cplx* cref, cplx* ctrn, int32_t* status);
+// Reverse passes (wb_vjp.cu), FP64. Each returns -1 when the arena cannot hold one chunk.
+// Stage B: P pairs; the slot cotangents gconv (n_conv, 3, N, N) are overwritten.
+size_t layer_modes_vjp_bytes(int N, int P);
+int layer_modes_vjp_chunk(int P, int N, size_t budget);
+int layer_modes_vjp_run(cudaStream_t s, Arena& ar, size_t budget, int P, int N, int n_conv, const cplx* conv,
+                        const int* pair_layer, const double* kx, const double* ky, const cplx* w, const cplx* q,
+                        const cplx* W, const cplx* V, const cplx* gw, const cplx* gq, const cplx* gW, const cplx* gV,
+                        cplx* gconv, int32_t* status);
+// Stage C: the cotangents of W, V (B*L, n, n), q (B*L, n) and the thicknesses (B, L) from those
+// of R and T (B, 3, N), through the FP64 cascade recomputed with its tape.
+size_t smm_vjp_bytes(int N, int L, int Bc);
+int smm_vjp_chunk(int B, int N, int L, size_t budget);
+int smm_vjp_run(cudaStream_t s, Arena& ar, size_t budget, const SolveDesc& d, const cplx* W, const cplx* V,
+                const cplx* q, const double* gR, const double* gT, cplx* gW, cplx* gV, cplx* gq, double* g_thick,
+                int32_t* status);
+// Stage A (sampled coefficients): the rasters' cotangents from those of the three slots.
+size_t assemble_vjp_bytes(int L, int ny, int nx, int hu, int hv);
+int assemble_vjp_run(cudaStream_t s, Arena& ar, int L, int ny, int nx, int hu, int hv, const cplx* eps,
+                     const cplx* epx, const cplx* epz, const cplx* gepx, const cplx* gepy, const cplx* gepz,
+                     cplx* g_eps, int32_t* status);
 size_t smm_chunk_bytes(int N, int L, int chunk, int precision);
 int smm_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, const cplx* W, const cplx* V, const cplx* q,
               int first, int count, const SolveOut& out, int precision);

@@ -28,6 +28,11 @@ void zgemm(cudaStream_t s, int batch, int m, int n, int k, cplx alpha,
            const cplx* B, long long b_rs, long long b_cs, long long b_bs,
            cplx beta, cplx* C, long long c_rs, long long c_cs, long long c_bs);
 // status (if non-null) of batch element e is status[e / st_div]
+// zgemm with either operand conjugated on load (conj_a / conj_b); with transposed strides that is
+// A^H or B^H without a copy
+void zgemm_conj(cudaStream_t s, int batch, int m, int n, int k, cplx alpha, const cplx* A, long long a_rs,
+                long long a_cs, long long a_bs, bool conj_a, const cplx* B, long long b_rs, long long b_cs,
+                long long b_bs, bool conj_b, cplx beta, cplx* C, long long c_rs, long long c_cs, long long c_bs);
 void zgetrf(cudaStream_t s, int batch, int n, cplx* A, int lda, long long a_bs, int* ipiv, long long piv_bs,
             int32_t* status, int st_div);
 void zgetrs(cudaStream_t s, int batch, int n, const cplx* LU, int lda, long long a_bs,

@@ -19,7 +19,9 @@ namespace wb {
 constexpr int GT = 64;   // CTA tile
 constexpr int GK = 8;    // K step
 
-template <class R>
+// CA / CB: the operand's elements are conjugated on load (op(A) = conj(A) under the given
+// strides, so a (rs, cs) swap with CA gives A^H).
+template <class R, bool CA = false, bool CB = false>
 __global__ void __launch_bounds__(256) gemm_kernel(
     int m, int n, int k, double2 alpha_d,
     const Cx<R>* __restrict__ A, long long a_rs, long long a_cs, long long a_bs,
@@ -44,14 +46,16 @@ __global__ void __launch_bounds__(256) gemm_kernel(
       int idx = tid + e * 256;
       int r = idx % GT, c = idx / GT;
       int gr = row0 + r, gc = k0 + c;
-      sA[c][r] = (gr < m && gc < k) ? A[gr * a_rs + gc * a_cs] : cxzero<R>();
+      C_ v = (gr < m && gc < k) ? A[gr * a_rs + gc * a_cs] : cxzero<R>();
+      sA[c][r] = CA ? cxconj(v) : v;
     }
 #pragma unroll
     for (int e = 0; e < 2; ++e) {
       int idx = tid + e * 256;
       int r = idx % GK, c = idx / GK;
       int gr = k0 + r, gc = col0 + c;
-      sB[r][c] = (gr < k && gc < n) ? B[gr * b_rs + gc * b_cs] : cxzero<R>();
+      C_ v = (gr < k && gc < n) ? B[gr * b_rs + gc * b_cs] : cxzero<R>();
+      sB[r][c] = CB ? cxconj(v) : v;
     }
     __syncthreads();
 #pragma unroll
@@ -1115,6 +1119,30 @@ void zgemm(cudaStream_t s, int batch, int m, int n, int k, cplx alpha,
            cplx beta, cplx* C, long long c_rs, long long c_cs, long long c_bs) {
   gemm<double>(s, batch, m, n, k, alpha, (const Cx<double>*)A, a_rs, a_cs, a_bs, (const Cx<double>*)B, b_rs, b_cs,
                b_bs, beta, (Cx<double>*)C, c_rs, c_cs, c_bs);
+}
+void zgemm_conj(cudaStream_t s, int batch, int m, int n, int k, cplx alpha, const cplx* A, long long a_rs,
+                long long a_cs, long long a_bs, bool conj_a, const cplx* B, long long b_rs, long long b_cs,
+                long long b_bs, bool conj_b, cplx beta, cplx* C, long long c_rs, long long c_cs, long long c_bs) {
+  if (batch <= 0 || m <= 0 || n <= 0) return;
+  if (!conj_a && !conj_b) {
+    zgemm(s, batch, m, n, k, alpha, A, a_rs, a_cs, a_bs, B, b_rs, b_cs, b_bs, beta, C, c_rs, c_cs, c_bs);
+    return;
+  }
+  using D = Cx<double>;
+  const D* a = (const D*)A;
+  const D* b = (const D*)B;
+  D* c = (D*)C;
+  dim3 grid((m + GT - 1) / GT, (n + GT - 1) / GT, batch);
+  if (conj_a && conj_b)
+    gemm_kernel<double, true, true><<<grid, 256, 0, s>>>(m, n, k, alpha, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs,
+                                                         beta, c, c_rs, c_cs, c_bs, nullptr);
+  else if (conj_a)
+    gemm_kernel<double, true, false><<<grid, 256, 0, s>>>(m, n, k, alpha, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs,
+                                                          beta, c, c_rs, c_cs, c_bs, nullptr);
+  else
+    gemm_kernel<double, false, true><<<grid, 256, 0, s>>>(m, n, k, alpha, a, a_rs, a_cs, a_bs, b, b_rs, b_cs, b_bs,
+                                                          beta, c, c_rs, c_cs, c_bs, nullptr);
+  note_launch();
 }
 void zgetrf(cudaStream_t s, int batch, int n, cplx* A, int lda, long long a_bs, int* ipiv, long long piv_bs,
             int32_t* status, int st_div) {

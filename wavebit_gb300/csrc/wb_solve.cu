@@ -1808,6 +1808,12 @@ static void given_modes(cudaStream_t s, const SolveDesc& d, const cplx* Wm, cons
   note_launch();
 }
 
+// The port vectors of solves first .. first + Bc - 1 (used by the reverse passes, wb_vjp.cu).
+void compute_ports(cudaStream_t s, const SolveDesc& d, int first, int Bc, const PortVectors& pv) {
+  ports_kernel<<<Bc, 128, 0, s>>>(Bc, d.hu, d.hv, d.wavelength + first, d.period + 2 * first, d.theta + first,
+                                  d.phi + first, d.eps_top + first, d.eps_bot + first, nullptr, pv); note_launch();
+}
+
 size_t smm_chunk_bytes(int N, int L, int chunk, int precision) {
   return solve_chunk_bytes(N, L, chunk, precision == 0 ? 0 : 4);
 }

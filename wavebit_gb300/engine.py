@@ -213,6 +213,94 @@ def smm_solve(W, V, q, inp, hu, hv, precision='double', amplitudes=False, handle
     return res + ((amps,) if amplitudes else ())
 
 
+def smm_solve_vjp(W, V, q, inp, hu, hv, g_R=None, g_T=None, handle=None):
+    """Reverse of :func:`smm_solve` in the FP64 form (wb_smm_solve_vjp): from the cotangents of
+    R and T (``(B, 3, N)`` or ``(B, 3, n_v, n_u)``, either may be None) the cotangents
+    ``(g_W, g_V, g_q, g_thickness)`` of W, V (B*L, n, n, natural orientation), q (B*L, n) and the
+    thicknesses (B, L). The cascade is recomputed on the device with its intermediates."""
+    _check_modes(W, V, q, inp, hu, hv)
+    dev = W.device
+    N = n_orders(hu, hv)
+    n = 2 * N
+    B, L = inp.B, inp.L
+    Wc = W.transpose(-1, -2).contiguous()
+    Vc = V.transpose(-1, -2).contiguous()
+    qc = q.contiguous()
+    gR = None if g_R is None else _f64(g_R, dev).reshape(B, 3, N).contiguous()
+    gT = None if g_T is None else _f64(g_T, dev).reshape(B, 3, N).contiguous()
+    gW = torch.empty((B * L, n, n), dtype=torch.complex128, device=dev)
+    gV = torch.empty_like(gW)
+    gq = torch.empty((B * L, n), dtype=torch.complex128, device=dev)
+    gth = torch.empty((B, L), dtype=torch.float64, device=dev)
+    status = torch.zeros(B, dtype=torch.int32, device=dev)
+    h = handle or _lib.handle(dev.index or 0)
+    _lib.check(h.lib.wb_smm_solve_vjp(
+        h.h, B, L, hu, hv, Wc.data_ptr(), Vc.data_ptr(), qc.data_ptr(), inp.thickness.data_ptr(),
+        inp.wavelength.data_ptr(), inp.period.data_ptr(), inp.theta.data_ptr(), inp.phi.data_ptr(),
+        inp.eps_top.data_ptr(), inp.eps_bot.data_ptr(), inp.pol.data_ptr(),
+        gR.data_ptr() if gR is not None else None, gT.data_ptr() if gT is not None else None,
+        gW.data_ptr(), gV.data_ptr(), gq.data_ptr(), gth.data_ptr(), status.data_ptr(), _stream()))
+    return gW.transpose(-1, -2), gV.transpose(-1, -2), gq, gth, status
+
+
+def layer_modes_vjp(conv, pair_layer, kx, ky, w, q, W, V, g_w=None, g_q=None, g_W=None, g_V=None, handle=None):
+    """Reverse of :func:`layer_modes` (wb_layer_modes_vjp): the slot cotangents, summed over the
+    pairs that read each layer, as a :class:`ConvStack` (``.slot(k)`` in natural orientation),
+    and the per-pair status. W, V, g_W, g_V in natural orientation."""
+    dev = conv.buf.device
+    hu, hv = conv.hu, conv.hv
+    N = n_orders(hu, hv)
+    n = 2 * N
+    pair_layer = torch.as_tensor(pair_layer, dtype=torch.int32, device=dev).contiguous()
+    P = pair_layer.shape[0]
+    pl = pair_layer.cpu().numpy()
+    if P and (int(pl.min()) < 0 or int(pl.max()) >= conv.n_layers):
+        raise ValueError(f'pair_layer spans {int(pl.min())}..{int(pl.max())}; the convolution stack holds '
+                         f'{conv.n_layers} layers')
+    kx = _f64(kx, dev).reshape(P, N)
+    ky = _f64(ky, dev).reshape(P, N)
+    wc, qc = w.contiguous(), q.contiguous()
+    Wc = W.transpose(-1, -2).contiguous()
+    Vc = V.transpose(-1, -2).contiguous()
+    col = lambda t: None if t is None else t.transpose(-1, -2).contiguous()  # noqa: E731
+    gWc, gVc = col(g_W), col(g_V)
+    gwc = None if g_w is None else g_w.contiguous()
+    gqc = None if g_q is None else g_q.contiguous()
+    for t, shape in ((Wc, (P, n, n)), (Vc, (P, n, n)), (wc, (P, n)), (qc, (P, n)), (gWc, (P, n, n)),
+                     (gVc, (P, n, n)), (gwc, (P, n)), (gqc, (P, n))):
+        if t is not None and tuple(t.shape) != shape:
+            raise ValueError(f'expected {shape}, got {tuple(t.shape)}')
+    g = torch.empty((conv.n_layers, 3, N, N), dtype=torch.complex128, device=dev)
+    status = torch.zeros(P, dtype=torch.int32, device=dev)
+    ptr = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+    h = handle or _lib.handle(dev.index or 0)
+    _lib.check(h.lib.wb_layer_modes_vjp(
+        h.h, P, hu, hv, conv.n_layers, conv.buf.data_ptr(), pair_layer.data_ptr(), kx.data_ptr(), ky.data_ptr(),
+        wc.data_ptr(), qc.data_ptr(), Wc.data_ptr(), Vc.data_ptr(), ptr(gwc), ptr(gqc), ptr(gWc), ptr(gVc),
+        g.data_ptr(), status.data_ptr(), _stream()))
+    return ConvStack(g, hu, hv), status
+
+
+def assemble_vjp(eps, conv, g_conv, handle=None):
+    """Reverse of :func:`assemble` with sampled coefficients (wb_assemble_li_vjp): the cotangent
+    of the rasters ``eps`` (L, ny, nx) from the slot cotangents ``g_conv`` (a :class:`ConvStack`),
+    given the forward's slots ``conv``. Returns a complex (L, ny, nx) tensor (for a real raster,
+    its real part is the gradient)."""
+    eps = _c128(eps, 'cuda')
+    L, ny, nx = (int(v) for v in eps.shape)
+    hu, hv = conv.hu, conv.hv
+    epx = conv.buf[:, 0].contiguous()
+    epz = conv.buf[:, 2].contiguous()
+    g = [g_conv.buf[:, k].contiguous() for k in range(3)]
+    g_eps = torch.empty((L, ny, nx), dtype=torch.complex128, device=eps.device)
+    status = torch.zeros(1, dtype=torch.int32, device=eps.device)
+    h = handle or _lib.handle(eps.device.index or 0)
+    _lib.check(h.lib.wb_assemble_li_vjp(h.h, eps.data_ptr(), L, ny, nx, hu, hv, epx.data_ptr(), epz.data_ptr(),
+                                        g[0].data_ptr(), g[1].data_ptr(), g[2].data_ptr(), g_eps.data_ptr(),
+                                        status.data_ptr(), _stream()))
+    return g_eps
+
+
 def etm_solve(W, V, q, inp, hu, hv, amplitudes=False, handle=None):
     """The ETM connecting algorithm from given modes (wb_etm_solve, FP64). ``W, V, q`` and
     ``inp`` as for :func:`smm_solve`. Returns ``(R, T, status[, amps])`` in its layout."""
