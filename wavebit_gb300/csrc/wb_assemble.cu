@@ -19,9 +19,23 @@ namespace wb {
 
 // coefficient of order k (|k| <= 2h) of one staircase line a_0..a_{n-1}:
 //   sum_j (a_j - a_0)/n exp(-2 pi i k j / n) * sinc(k/n) exp(-i pi k / n)  (+ a_0 at k = 0)
+// The twiddles exp(-2 pi i p / n), p = k j mod n, come from a table of the line length built once
+// per block in dynamic shared memory (the same sincospi values the sum would compute term by
+// term), so a term is one complex multiply-add; lines longer than the table compute them in place.
+constexpr int kSeriesTable = 3072;                  // 48 KB of twiddles: no shared-memory opt-in
+
 __global__ void series_kernel(const cplx* __restrict__ in, long long n_lines, int lines_per_group,
                               long long group_stride, long long line_stride, long long pt_stride,
                               int npts, int h, int reciprocal, cplx* __restrict__ out) {
+  extern __shared__ cplx tw[];
+  const bool table = npts <= kSeriesTable;
+  if (table)
+    for (int p = threadIdx.x; p < npts; p += blockDim.x) {
+      double sn, cs;
+      sincospi(-2.0 * (double)p / (double)npts, &sn, &cs);
+      tw[p] = cmk(cs, sn);
+    }
+  __syncthreads();
   const int nk = 4 * h + 1;
   long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= n_lines * nk) return;
@@ -34,14 +48,22 @@ __global__ void series_kernel(const cplx* __restrict__ in, long long n_lines, in
   cplx acc = cmk(0.0, 0.0);
   if (npts > 1) {
     const int kmod = ((k % npts) + npts) % npts;
+    int p = kmod;                                     // (kmod * j) mod npts, advanced by kmod
     for (int j = 1; j < npts; ++j) {
       cplx aj = a[j * pt_stride];
       if (reciprocal) aj = cinv(aj);
       const cplx d = csub(aj, a0);
-      const long long p = ((long long)kmod * j) % npts;
-      double sn, cs;
-      sincospi(-2.0 * (double)p / (double)npts, &sn, &cs);
-      acc = cfma(d, cmk(cs, sn), acc);
+      cplx t;
+      if (table) {
+        t = tw[p];
+      } else {
+        double sn, cs;
+        sincospi(-2.0 * (double)p / (double)npts, &sn, &cs);
+        t = cmk(cs, sn);
+      }
+      acc = cfma(d, t, acc);
+      p += kmod;
+      if (p >= npts) p -= npts;
     }
     acc = cscale(acc, 1.0 / (double)npts);
   }
@@ -82,8 +104,8 @@ static void launch_series(cudaStream_t s, const cplx* in, long long lines, int l
     segment_series_kernel<<<blocks, 128, 0, s>>>(in, lines, lines_per_group, group_stride, line_stride, pt_stride,
                                                  npts, h, reciprocal, edges, lines_per_seg, n_seg_rows, out);
   else
-    series_kernel<<<blocks, 128, 0, s>>>(in, lines, lines_per_group, group_stride, line_stride, pt_stride, npts,
-                                         h, reciprocal, out);
+    series_kernel<<<blocks, 128, npts <= kSeriesTable ? sizeof(cplx) * npts : 0, s>>>(
+        in, lines, lines_per_group, group_stride, line_stride, pt_stride, npts, h, reciprocal, out);
   note_launch();
 }
 

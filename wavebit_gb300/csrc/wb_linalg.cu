@@ -7,6 +7,7 @@
 // to save bandwidth: a 64x64 CTA tile with 4x4 register blocking is far above the arithmetic
 // intensity HBM needs. FP64 mma.sync runs at the same rate as DFMA on this part, so plain
 // fused multiply-adds are used. The float and df64 instantiations run on the FP32 pipes.
+#include <type_traits>
 #include "wb_common.cuh"
 #include "wb_num.cuh"
 #include "wb_kernels.h"
@@ -934,8 +935,10 @@ static bool getrs_narrow(cudaStream_t s, int batch, int n, const Cx<R>* LU, int 
   return true;
 }
 
-// Many right-hand sides (the cascade's n-column solves, FP32 form): a blocked substitution across
-// the GPU. (The FP64 instantiation keeps getrs_kernel: its time is FP64 issue either way.)
+// Many right-hand sides: a blocked substitution across the GPU. The FP32 form's cascade always
+// takes it; FP64 takes it only for batches too small to fill the GPU with getrs_kernel's CTAs
+// (stage A's outer inverses: a few N x N systems with N right-hand sides), since a large FP64
+// batch is bound by FP64 issue either way.
 // The row interchanges are applied first (trans 0) or last (trans 1), one thread per column;
 // then, per block of TB_NB rows, trsm_diag_kernel solves the diagonal block for every column
 // (the block and 64 columns in shared memory, one thread per column) and the batched GEMM
@@ -1059,6 +1062,11 @@ void getrs(cudaStream_t s, int batch, int n, const Cx<R>* LU, int lda, long long
            long long piv_bs, Cx<R>* B, int nrhs, int ldb, long long b_bs, int trans) {
   if (batch <= 0 || n <= 0 || nrhs <= 0) return;
   if (sizeof(R) == 4 && nrhs >= 32 && n >= 2 * TB_NB) {     // FP32: the cascade of the mixed form
+    getrs_blocked<R>(s, batch, n, LU, lda, a_bs, ipiv, piv_bs, B, nrhs, ldb, b_bs, trans);
+    return;
+  }
+  if (std::is_same<R, double>::value && nrhs >= 2 * SV_W && n >= 2 * TB_NB &&
+      (long long)batch * ((nrhs + SV_W - 1) / SV_W) < sm_count()) {
     getrs_blocked<R>(s, batch, n, LU, lda, a_bs, ipiv, piv_bs, B, nrhs, ldb, b_bs, trans);
     return;
   }
