@@ -333,7 +333,15 @@ def profile_calls(args):
     cfg = load_workload(args.workload, B)
     hu, hv = cfg['orders']
     dev = torch.device('cuda', 0)
-    conv = E.assemble(torch.as_tensor(cfg['eps'], device=dev), hu, hv)
+    eps_dev = torch.as_tensor(cfg['eps'], device=dev)
+    E.assemble(eps_dev, hu, hv)                        # warm (library load, arena)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    conv = E.assemble(eps_dev, hu, hv)
+    ev1.record()
+    torch.cuda.synchronize()
+    stage_a_ms = ev0.elapsed_time(ev1)
     x = batch_inputs(cfg, B)
     inp = E.BatchInputs(x['li'], x['th'], x['wl'], x['per'], x['theta'], x['phi'], x['et'], x['eb'], x['pol'],
                         device=dev)
@@ -347,7 +355,8 @@ def profile_calls(args):
     qr = qr_profile(h, 0 if precision == 'double' else 1 if precision == 'mixed' else 2)
     print(f'{args.workload} {precision} solves={B} calls={args.profile_calls} '
           f'status_nonzero={int((st.cpu().numpy() & ~8).astype(bool).sum())} '
-          f"qr_sweep_{qr['type']}: launches={qr['launches']} ms={qr['ms']:.1f} algorithmic_bytes={qr['bytes']:.6g}")
+          f"qr_sweep_{qr['type']}: launches={qr['launches']} ms={qr['ms']:.1f} algorithmic_bytes={qr['bytes']:.6g} "
+          f"stage_a_ms={stage_a_ms:.2f}")
 
 
 def adjoint_check(args):
@@ -422,6 +431,9 @@ def main():
     ap.add_argument('--profile-calls', type=int, default=0)
     ap.add_argument('--tensor-cores', default='on', choices=['on', 'off'],
                     help='off: the FP32 complex products on the SIMT kernel instead of tcgen05 (for comparison)')
+    ap.add_argument('--qr-prefetch', type=int, default=0,
+                    help="the FP32 QR sweep's L2 prefetch distance (WB_TUNE_QR_PREFETCH: 0 the library's choice, "
+                         "1 none, d >= 2 d bulge steps ahead)")
     ap.add_argument('--pixels', type=int, default=16)
     ap.add_argument('--adjoint-wavelengths', type=int, default=32)
     args = ap.parse_args()
@@ -429,6 +441,9 @@ def main():
     if args.tensor_cores == 'off' and args.impl != 'reference':
         from wavebit_gb300 import _lib
         _lib.check(_lib.load().wb_set_tuning(_lib.WB_TUNE_TENSOR_CORES, 1))
+    if args.qr_prefetch and args.impl != 'reference':
+        from wavebit_gb300 import _lib
+        _lib.check(_lib.load().wb_set_tuning(_lib.WB_TUNE_QR_PREFETCH, args.qr_prefetch))
     if args.workload == 'adjoint_layer':
         return adjoint_check(args)
     if args.impl == 'reference':
