@@ -431,9 +431,6 @@ def main():
     ap.add_argument('--profile-calls', type=int, default=0)
     ap.add_argument('--tensor-cores', default='on', choices=['on', 'off'],
                     help='off: the FP32 complex products on the SIMT kernel instead of tcgen05 (for comparison)')
-    ap.add_argument('--qr-prefetch', type=int, default=0,
-                    help="the FP32 QR sweep's L2 prefetch distance (WB_TUNE_QR_PREFETCH: 0 the library's choice, "
-                         "1 none, d >= 2 d bulge steps ahead)")
     ap.add_argument('--pixels', type=int, default=16)
     ap.add_argument('--adjoint-wavelengths', type=int, default=32)
     args = ap.parse_args()
@@ -441,9 +438,6 @@ def main():
     if args.tensor_cores == 'off' and args.impl != 'reference':
         from wavebit_gb300 import _lib
         _lib.check(_lib.load().wb_set_tuning(_lib.WB_TUNE_TENSOR_CORES, 1))
-    if args.qr_prefetch and args.impl != 'reference':
-        from wavebit_gb300 import _lib
-        _lib.check(_lib.load().wb_set_tuning(_lib.WB_TUNE_QR_PREFETCH, args.qr_prefetch))
     if args.workload == 'adjoint_layer':
         return adjoint_check(args)
     if args.impl == 'reference':

@@ -39,7 +39,7 @@ def test_coordinate_descent_finds_the_fastest_shapes_and_persists_them(tmp_path)
     key = AT.bucket_key((12, 12), 4, 38, 'mixed')
     assert key == '12x12/L4/B38/mixed'
     best = tuner.tune(key, lambda: runs.append(1))
-    assert best == {'qr_threads': 512, 'hrd_threads': 1024, 'qr_prefetch': 0}
+    assert best == {'qr_threads': 512, 'hrd_threads': 1024}
     assert tuner.current() == best                    # applied
     assert runs                                       # the run was executed by the trials
     saved = json.load(open(path))
@@ -51,11 +51,11 @@ def test_coordinate_descent_finds_the_fastest_shapes_and_persists_them(tmp_path)
     got = t2.lookup((12, 12), 4, 30, 'mixed')
     assert got == best
     t2.apply(got)
-    assert lib2.values == {0: 512, 1: 1024, 4: 0}
+    assert lib2.values == {0: 512, 1: 1024}
     assert t2.lookup((12, 12), 4, 30, 'double') is None
     assert t2.lookup((11, 11), 4, 38, 'mixed') is None
     t2.reset()
-    assert t2.current() == {'qr_threads': 0, 'hrd_threads': 0, 'qr_prefetch': 0}
+    assert t2.current() == {'qr_threads': 0, 'hrd_threads': 0}
 
 
 def test_a_candidate_must_beat_the_current_choice_by_the_margin():
@@ -65,7 +65,7 @@ def test_a_candidate_must_beat_the_current_choice_by_the_margin():
         run()
         return 1.0 - (0.01 if lib.values.get(0, 0) == 256 else 0.0)    # 1% better: under the 2% margin
     tuner = AT.Autotuner(lib=lib, timer=flat)
-    assert tuner.tune('k', lambda: None) == {'qr_threads': 0, 'hrd_threads': 0, 'qr_prefetch': 0}
+    assert tuner.tune('k', lambda: None) == {'qr_threads': 0, 'hrd_threads': 0}
 
 
 def test_batch_limit_maximises_solves_per_second(tmp_path):

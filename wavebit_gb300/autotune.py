@@ -4,8 +4,7 @@ A *bucket* is one shape of work: orders, layer count, batch size and precision f
 the tuner times candidate settings of the launch-shape tunables that ``wb_set_tuning`` exposes:
 
 * ``qr_threads`` (``WB_TUNE_QR_THREADS``): threads of a QR-sweep CTA;
-* ``hrd_threads`` (``WB_TUNE_HRD_THREADS``): threads of a Hessenberg-reduction CTA;
-* ``qr_prefetch`` (``WB_TUNE_QR_PREFETCH``): the FP32 QR sweep's L2 prefetch distance.
+* ``hrd_threads`` (``WB_TUNE_HRD_THREADS``): threads of a Hessenberg-reduction CTA.
 
 It searches by coordinate descent from the library's own choice (0), one tunable at a time,
 keeping a candidate only when it is faster by more than ``min_gain``. The choices are persisted
@@ -28,7 +27,6 @@ import time
 KNOBS = {
     'qr_threads': (0, (0, 256, 384, 512, 768)),
     'hrd_threads': (1, (0, 256, 512, 1024)),
-    'qr_prefetch': (4, (0, 1, 2, 4, 8)),
 }
 
 

@@ -314,20 +314,7 @@ template <> struct QrSlot<double> { static constexpr int v = 0; };
 template <> struct QrSlot<float> { static constexpr int v = 1; };
 template <> struct QrSlot<df64> { static constexpr int v = 2; };
 
-// pf > 0: the idle lanes of the core lane's warp ask L2, at step k, for what the workers will
-// load at step k + pf: Z's column k + 2 + pf and H's column k + 2 + pf above the diagonal (one bulk
-// prefetch each, when 16-byte aligned) and H's row k + 2 + pf right of it (one line per element).
-// A prefetch changes no value; it lets the workers' loads, issued one step ahead, find their lines
-// in L2 rather than DRAM. The distance is a template constant and the workers' code is unchanged,
-// so the sweep keeps its registers.
-__device__ __forceinline__ void prefetch_l2(const void* p) {
-  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-}
-__device__ __forceinline__ void prefetch_l2_bulk(const void* p, unsigned bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
-}
-
-template <class R, int pf>
+template <class R>
 __device__ void chase_sweep_carry(Cx<R>* __restrict__ H, int ldh, Cx<R>* __restrict__ Z, int ldz, int n, int l,
                                   int i, Cx<R>* s_t1, Cx<R>* s_v2, R* s_t2, Cx<R>* s_c01, Cx<R>* s_h01) {
   using C_ = Cx<R>;
@@ -369,18 +356,6 @@ __device__ void chase_sweep_carry(Cx<R>* __restrict__ H, int ldh, Cx<R>* __restr
     const R t2 = s_t2[sl];
     const C_ t1c = cxconj(t1), v2c = cxconj(v2);
     if (warp == 0) {
-      if (pf > 0 && tid > 0) {
-        const int c = k + 2 + pf;
-        if (c <= i) {
-          const C_* zc = Z + (long long)c * ldz;
-          const C_* hc = H + (long long)c * ldh;
-          const unsigned zb = (unsigned)(n * sizeof(C_)), hb = (unsigned)(((c * sizeof(C_)) + 15) & ~15u);
-          if (tid == 1 && ((uintptr_t)zc & 15) == 0 && (zb & 15) == 0) prefetch_l2_bulk(zc, zb);
-          if (tid == 2 && ((uintptr_t)hc & 15) == 0 && hb <= (unsigned)(n * sizeof(C_)) && (n * sizeof(C_)) % 16 == 0)
-            prefetch_l2_bulk(hc, hb);
-          for (int j = c + tid - 2; j < n; j += 30) prefetch_l2(&h(c, j));     // lanes 3..31: j >= c + 1
-        }
-      }
       if (tid == 0) {
         const C_ c00 = cs[C00], c10 = cs[C10], c11 = cs[C11], c21 = cs[C21];
         const C_ c01 = (k > l) ? s_c01[sl] : cs[C01];
@@ -463,7 +438,7 @@ __device__ void chase_sweep_carry(Cx<R>* __restrict__ H, int ldh, Cx<R>* __restr
   __syncthreads();
 }
 
-template <class R, int PF = 0>
+template <class R>
 __global__ void __launch_bounds__(kQrMaxThreads) hseqr_kernel(Cx<R>* __restrict__ Hall, int n, int ldh,
                                                             long long h_bs, Cx<R>* __restrict__ Zall, int ldz,
                                                             long long z_bs, Cx<R>* __restrict__ w_all,
@@ -588,7 +563,7 @@ __global__ void __launch_bounds__(kQrMaxThreads) hseqr_kernel(Cx<R>* __restrict_
       // k, k+1 (right) and Z's columns k, k+1. Each worker issues the loads of up to kChunk items
       // before it updates any, so that one memory latency serves the chunk.
       const bool carry = sizeof(R) == 4 && 2 * n - 2 <= kCarry * ((int)blockDim.x - 32);
-      if (carry) chase_sweep_carry<R, PF>(H, ldh, Z, ldz, n, l, i, s_t1, s_v2, s_t2, s_c01, s_h01);
+      if (carry) chase_sweep_carry<R>(H, ldh, Z, ldz, n, l, i, s_t1, s_v2, s_t2, s_c01, s_h01);
       for (int k = carry ? i : l; k < i; ++k) {
         const int sl = k & 1;
         const C_ t1 = s_t1[sl], v2 = s_v2[sl];
@@ -833,31 +808,6 @@ int hrd_threads(int batch, int n) {
   return t;
 }
 
-// L2 prefetch distance of the FP32 QR sweep, in bulge steps (0: none), one of 0, 2, 4, 8.
-// WB_TUNE_QR_PREFETCH: 0 = the library's choice (kQrPrefetch), 1 = none, d >= 2 = the largest
-// available distance not above d.
-constexpr int kQrPrefetch = 0;
-int qr_prefetch() {
-  const int v = tuning(kTuneQrPrefetch);
-  const int d = v == 0 ? kQrPrefetch : v == 1 ? 0 : v;
-  return d >= 8 ? 8 : d >= 4 ? 4 : d >= 2 ? 2 : 0;
-}
-
-template <class R>
-void launch_hseqr(cudaStream_t s, int batch, int threads, size_t sm, Cx<R>* A, int n, int lda, long long a_bs,
-                  Cx<R>* Z, int ldz, long long z_bs, Cx<R>* w, int32_t* status, int st_div, int itmax) {
-  const int pf = sizeof(R) == 4 ? qr_prefetch() : 0;      // only the FP32 form carries its operands
-  if (pf == 2)
-    hseqr_kernel<R, 2><<<batch, threads, sm, s>>>(A, n, lda, a_bs, Z, ldz, z_bs, w, status, st_div, itmax);
-  else if (pf == 4)
-    hseqr_kernel<R, 4><<<batch, threads, sm, s>>>(A, n, lda, a_bs, Z, ldz, z_bs, w, status, st_div, itmax);
-  else if (pf == 8)
-    hseqr_kernel<R, 8><<<batch, threads, sm, s>>>(A, n, lda, a_bs, Z, ldz, z_bs, w, status, st_div, itmax);
-  else
-    hseqr_kernel<R, 0><<<batch, threads, sm, s>>>(A, n, lda, a_bs, Z, ldz, z_bs, w, status, st_div, itmax);
-  note_launch();
-}
-
 template <class R>
 void geev_schur(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a_bs, Cx<R>* Z, int ldz,
                 long long z_bs, Cx<R>* w, Cx<R>* tau, int32_t* status, int st_div) {
@@ -870,12 +820,7 @@ void geev_schur(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a
   unghr_kernel<R><<<batch, th, sm, s>>>(A, n, lda, a_bs, tau, Z, ldz, z_bs); note_launch();
   int itmax = 30 * (n > 10 ? n : 10);
   size_t sm2 = (size_t)n * sizeof(Cx<R>);
-  cudaFuncSetAttribute(hseqr_kernel<R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
-  if (sizeof(R) == 4) {
-    cudaFuncSetAttribute(hseqr_kernel<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
-    cudaFuncSetAttribute(hseqr_kernel<R, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
-    cudaFuncSetAttribute(hseqr_kernel<R, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
-  }
+  cudaFuncSetAttribute(hseqr_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   bool timed = false;
   {
@@ -886,8 +831,8 @@ void geev_schur(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a
     }
   }
   if (timed) cudaEventRecord(e0, s);
-  launch_hseqr<R>(s, batch, qr_threads(batch, n, sizeof(R) == 4), sm2, A, n, lda, a_bs, Z, ldz, z_bs, w, status,
-                  st_div < 1 ? 1 : st_div, itmax);
+  hseqr_kernel<R><<<batch, qr_threads(batch, n, sizeof(R) == 4), sm2, s>>>(A, n, lda, a_bs, Z, ldz, z_bs, w, status,
+                                                           st_div < 1 ? 1 : st_div, itmax); note_launch();
   if (timed) cudaEventRecord(e1, s);
 }
 
