@@ -172,3 +172,24 @@ def test_resident_eigenpairs_are_reused_and_give_the_same_results(precision, tol
     for r in reqs:
         a, m = ref[r.id], got[r.id]
         assert np.abs(a.R - m.R).max() <= tol and np.abs(a.T - m.T).max() <= tol, r.id
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('precision', ['double', 'mixed'])
+def test_captured_batches_replay_to_the_eager_results(precision):
+    """With graphs on, every batch shape is solved eagerly once, captured, and replayed for the
+    later batches of that shape; the replayed results equal the eager loop's."""
+    torch = pytest.importorskip('torch')
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from wavebit_gb300.serving import GpuBackend, _repeat, _stream
+    reqs = _repeat(_stream(8, rate=400.0, seed=17, orders=[(3, 3)], max_layers=2, sides=(32,)), 4, 400.0)
+    ref, st0 = Server(GpuBackend(1, 6 << 30, precision), n_workers=1, max_batch=2).run(reqs, realtime=False)
+    be = GpuBackend(1, 6 << 30, precision, graphs=True)
+    got, st = Server(be, n_workers=1, max_batch=2).run(reqs, realtime=False)
+    assert st['completed'] == len(reqs) and st0['completed'] == len(reqs)
+    assert be.graph_captures >= 1 and be.graph_replays >= 1 and not be.graph_refused
+    for r in reqs:
+        a, m = ref[r.id], got[r.id]
+        scale = max(np.abs(a.R).max(), np.abs(a.T).max())
+        assert np.abs(a.R - m.R).max() <= 1e-12 * scale and np.abs(a.T - m.T).max() <= 1e-12 * scale, r.id

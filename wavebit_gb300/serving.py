@@ -81,7 +81,7 @@ class GpuBackend:
     """libwbgpu.so behind the serving loop: one handle and one CUDA stream per worker."""
 
     def __init__(self, n_workers, hbm_budget, precision='double', device=0, eig_cache=False, coefficients='sampled',
-                 tuning=None):
+                 tuning=None, graphs=False, max_graphs=32):
         import torch
         from . import _lib, engine
         self.torch, self.lib, self.engine = torch, _lib, engine
@@ -120,6 +120,15 @@ class GpuBackend:
             self.eig_budget = self.cache_budget // 2
             self.cache_budget -= self.eig_budget
         self.eig_hits = self.eig_misses = 0
+        # captured batches: per (worker, orders, layers, batch size, form) one CUDA graph of the
+        # whole wb_solve_batch launch sequence over static device buffers, replayed for every
+        # later batch of the same shape (the library allocates nothing inside a solve: the
+        # worker's arena was reserved above, so the sequence is capturable)
+        self.graphs = bool(graphs)
+        self.max_graphs = int(max_graphs)
+        self.graph_cache = collections.OrderedDict()
+        self.graph_refused = set()
+        self.graph_captures = self.graph_replays = 0
         self.launches0 = self.handles[0].launches()     # the library's count is process-wide
 
     # ---- admission
@@ -209,6 +218,56 @@ class GpuBackend:
         return (torch.stack([self.eig[pk][0] for pk in flat]), torch.stack([self.eig[pk][1] for pk in flat]),
                 torch.stack([self.eig[pk][2] for pk in flat]))
 
+    # ---- captured batches
+    def _graph_solve(self, worker, reqs, conv_list, inp, prec):
+        """Solve the batch through this shape's CUDA graph: fill its static inputs (one slot set per
+        (solve, layer), the per-solve parameters), replay it on the worker's stream and return its
+        static outputs. The first batch of a shape runs eagerly on the static buffers and is then
+        captured; a shape whose capture fails is solved eagerly from then on."""
+        torch, engine = self.torch, self.engine
+        hu, hv = reqs[0].orders
+        B, L = len(reqs), reqs[0].eps.shape[0]
+        key = (worker, hu, hv, L, B, prec)
+        if key in self.graph_refused:
+            return None
+        stream = self.streams[worker]
+        entry = self.graph_cache.get(key)
+        fresh = entry is None
+        if fresh:
+            N = engine.n_orders(hu, hv)
+            conv_s = engine.ConvStack(torch.empty((B * L, 3, N, N), dtype=torch.complex128, device=self.device),
+                                      hu, hv)
+            inp_s = engine.BatchInputs(np.arange(B * L, dtype=np.int32).reshape(B, L), inp.thickness.clone(),
+                                       inp.wavelength.clone(), inp.period.clone(), inp.theta.clone(),
+                                       inp.phi.clone(), inp.eps_top.clone(), inp.eps_bot.clone(), inp.pol.clone(),
+                                       device=self.device)
+            entry = dict(conv=conv_s, inp=inp_s, graph=None, out=None)
+        conv_s, inp_s = entry['conv'], entry['inp']
+        for b in range(B):
+            for l in range(L):
+                conv_s.buf[b * L + l].copy_(conv_list[b][l], non_blocking=True)
+        for name in ('thickness', 'wavelength', 'period', 'theta', 'phi', 'eps_top', 'eps_bot', 'pol'):
+            getattr(inp_s, name).copy_(getattr(inp, name), non_blocking=True)
+        if not fresh:
+            self.graph_cache.move_to_end(key)
+            entry['graph'].replay()
+            self.graph_replays += 1
+            return entry['out']
+        out = engine.solve_batch(conv_s, inp_s, precision=prec, handle=self.handles[worker])
+        g = torch.cuda.CUDAGraph()
+        try:
+            with torch.cuda.graph(g, stream=stream):
+                entry['out'] = engine.solve_batch(conv_s, inp_s, precision=prec, handle=self.handles[worker])
+        except Exception:
+            self.graph_refused.add(key)
+            return out
+        entry['graph'] = g
+        self.graph_cache[key] = entry
+        self.graph_captures += 1
+        while len(self.graph_cache) > self.max_graphs:
+            self.graph_cache.popitem(last=False)
+        return out
+
     # ---- one batch
     def launch(self, worker, reqs):
         torch, engine = self.torch, self.engine
@@ -233,12 +292,17 @@ class GpuBackend:
             prec = self.fallback_precision if reqs[0].retry and self.fallback_precision else self.precision
             if self.tuner is not None:
                 self.tuner.apply(self.tuner.lookup((hu, hv), L, len(reqs), prec))
+            solved = None
             if self.eig_modes and not reqs[0].retry:
                 q, W, V = self.modes_for(reqs, keys_all, conv, index, worker)
-                R, T, st = engine.smm_solve(W, V, q, inp, hu, hv, precision=self.precision,
-                                            handle=self.handles[worker])
-            else:
-                R, T, st = engine.solve_batch(conv, inp, precision=prec, handle=self.handles[worker])
+                solved = engine.smm_solve(W, V, q, inp, hu, hv, precision=self.precision,
+                                          handle=self.handles[worker])
+            elif self.graphs and not reqs[0].retry:
+                slots = [[self.cache[k][0] for k in ks] for ks in keys_all]
+                solved = self._graph_solve(worker, reqs, slots, inp, prec)
+            if solved is None:
+                solved = engine.solve_batch(conv, inp, precision=prec, handle=self.handles[worker])
+            R, T, st = solved
             Rh = torch.empty(R.shape, dtype=R.dtype, pin_memory=True)
             Th = torch.empty(T.shape, dtype=T.dtype, pin_memory=True)
             sh = torch.empty(st.shape, dtype=st.dtype, pin_memory=True)
@@ -404,6 +468,8 @@ def main():
     ap.add_argument('--tuning', default=None, help='JSON of launch shapes per bucket (python -m wavebit_gb300.autotune)')
     ap.add_argument('--save-results', default=None,
                     help='write every request\'s R, T, status and latency to this .npz (to compare two forms)')
+    ap.add_argument('--graphs', action='store_true',
+                    help='replay each batch shape (orders, layers, batch size) through a captured CUDA graph')
     ap.add_argument('--repeat', type=int, default=1,
                     help='replay each request this many times (as new requests), e.g. to exercise the caches')
     args = ap.parse_args()
@@ -412,7 +478,7 @@ def main():
     if args.repeat > 1:
         reqs = _repeat(reqs, args.repeat, args.rate)
     backend = GpuBackend(args.workers, int(args.budget_gb * 2 ** 30), args.precision, eig_cache=args.eig_cache,
-                         coefficients=args.coefficients, tuning=args.tuning)
+                         coefficients=args.coefficients, tuning=args.tuning, graphs=args.graphs)
     server = Server(backend, args.workers, args.max_batch)
     results, stats = server.run(reqs)
     if args.save_results:
@@ -427,7 +493,8 @@ def main():
     stats.update(precision=args.precision, rate=args.rate, workers=args.workers, orders=args.orders,
                  max_layers=args.max_layers, gpu_launches=backend.launches(), eig_cache=args.eig_cache,
                  eig_hits=backend.eig_hits, eig_misses=backend.eig_misses, repeat=args.repeat,
-                 coefficients=args.coefficients)
+                 coefficients=args.coefficients, graphs=args.graphs, graph_captures=backend.graph_captures,
+                 graph_replays=backend.graph_replays)
     print(json.dumps(stats))
 
 
