@@ -375,7 +375,8 @@ def adjoint_check(args):
     wR, wT = np.zeros((Bw, N)), np.zeros((Bw, N))
     wT[:, N // 2] = 1.0
     kw = dict(wavelengths=cfg['wavelengths'], period=cfg['period'], hu=h, hv=h, theta=0.0, phi=0.0,
-              eps_top=cfg['eps_top'], eps_bot=cfg['eps_bot'], pol=(0.0, 1.0), impl='gb300', device='cuda')
+              eps_top=cfg['eps_top'], eps_bot=cfg['eps_bot'], pol=(0.0, 1.0), impl='gb300', device='cuda',
+              modes=args.precision or 'double')
     eps, th = cfg['eps'], cfg['thickness']
     AD.solve_and_grad(eps, th, weights_R=wR, weights_T=wT, grad=False, **kw)
     torch.cuda.synchronize()
@@ -405,7 +406,7 @@ def adjoint_check(args):
     fd_t = (AD.solve_and_grad(eps, tp, weights_R=wR, weights_T=wT, grad=False, **kw)[0]
             - AD.solve_and_grad(eps, tm, weights_R=wR, weights_T=wT, grad=False, **kw)[0]) / 2e-4
     print(json.dumps({'workload': f'adjoint_layer 128x128, orders ({h},{h}), {Bw} wavelengths, p, sum T(0,0)',
-                      'loss': loss, 'grad_seconds': t_grad, 'fd_pixels': len(pix),
+                      'modes': kw['modes'], 'loss': loss, 'grad_seconds': t_grad, 'fd_pixels': len(pix),
                       'max_abs_err_over_max_grad': {'fd_step_1e-6': err6, 'fd_step_1e-5': err5,
                                                     'fd_1e-6_vs_fd_1e-5': fdfd},
                       'thickness_grad': float(g_th[0]), 'thickness_fd': fd_t,

@@ -519,7 +519,7 @@ def _chunk_size(L, n, budget, device):
 
 def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weights_T, theta=0.0, phi=0.0,
                    eps_top=1.0, eps_bot=1.0, pol=(0.0, 1.0), impl='gb300', device=None, grad=True,
-                   hbm_budget=None, grad_wavelength=False, fourier_coefficients=None):
+                   hbm_budget=None, grad_wavelength=False, fourier_coefficients=None, modes='double'):
     """Loss = sum_b sum_i (weights_R[b, i] R[b, i] + weights_T[b, i] T[b, i]) over the given
     polarization's per-order efficiencies, and its gradients with respect to the raster
     permittivities (real part; shape of ``eps``) and the thicknesses.
@@ -536,6 +536,10 @@ def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weigh
     With ``grad_wavelength`` a sixth value is returned: ``d loss / d wavelength`` (B,), each
     wavelength's own term by a forward tangent (:func:`wavelength_tangent`).
 
+    ``modes`` is the eigen-solve of the kernel path (``impl='gb300'``): ``'double'`` (FP64) or
+    ``'mixed_df64'`` (the double-float eigen-solve on the FP32 pipes, FP64-class eigenpairs); the
+    cascade and every reverse pass are FP64 either way.
+
     ``fourier_coefficients`` may be ``'sampled'`` or ``'integrated'``: a differentiated raster
     keeps every pixel edge (factorization.py:3135-3150 of the reference), and over one segment
     per pixel the closed-form segment series is the exact staircase series the sampled rule
@@ -547,7 +551,7 @@ def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weigh
     eps = torch.as_tensor(eps, dtype=torch.complex128, device=device)
     if impl == 'gb300' and not grad_wavelength:
         return _solve_and_grad_kernels(eps, thickness, wavelengths, period, hu, hv, weights_R, weights_T, theta, phi,
-                                       eps_top, eps_bot, pol, device, grad, hbm_budget)
+                                       eps_top, eps_bot, pol, device, grad, hbm_budget, modes)
     L = eps.shape[0]
     N = (2 * hu + 1) * (2 * hv + 1)
     n = 2 * N
@@ -636,7 +640,7 @@ def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weigh
 
 
 def _solve_and_grad_kernels(eps, thickness, wavelengths, period, hu, hv, weights_R, weights_T, theta, phi, eps_top,
-                            eps_bot, pol, device, grad, hbm_budget):
+                            eps_bot, pol, device, grad, hbm_budget, modes='double'):
     """:func:`solve_and_grad` with every stage and every reverse pass on the library's kernels:
     wb_assemble_li, then per chunk of wavelengths wb_layer_modes (FP64), wb_smm_solve (FP64),
     wb_smm_solve_vjp and wb_layer_modes_vjp, and finally wb_assemble_li_vjp. The chunk's modes
@@ -663,7 +667,7 @@ def _solve_and_grad_kernels(eps, thickness, wavelengths, period, hu, hv, weights
         kx = torch.stack([pv['kx'] for pv in pvs for _ in range(L)])
         ky = torch.stack([pv['ky'] for pv in pvs for _ in range(L)])
         pl = np.tile(np.arange(L), Bc)
-        w, q, W, V, st = engine.layer_modes(cs, pl, kx, ky, precision='double')
+        w, q, W, V, st = engine.layer_modes(cs, pl, kx, ky, precision=modes)
         if int((st.cpu().numpy() & 2).sum()):
             raise RuntimeError('the eigen-solve did not converge')
         inp = engine.BatchInputs([list(range(L))] * Bc, [th] * Bc, lam, [list(period)] * Bc, [theta] * Bc,
