@@ -107,7 +107,9 @@ int wb_assemble_li_integrated(wb_handle* h, const wb_complex* eps, int L, int ny
  * cannot read it before the kernels do, so the caller keeps it in range); kx, ky: device
  * (n_pairs, N) normalised order wavevectors. Outputs (device): w (n_pairs, 2N) eigenvalues of Omega^2, q (n_pairs, 2N),
  * W and V (n_pairs, 2N, 2N) column-major, status (n_pairs). precision: WB_PRECISION_FP64 for
- * the FP64 eigen-solve, any other WB_PRECISION_* for the double-float one.
+ * the FP64 eigen-solve, WB_PRECISION_MIXED for the FP32 eigen-solve refined by Newton steps on
+ * the FP64 operator (the mixed form's stage B; FP64-class eigenpairs), any other WB_PRECISION_*
+ * for the double-float eigen-solve.
  * Reference: rcwa/_engine/solve_2d.py:2303-2460 (layer_modes_2d, no exceptional-point
  * rebuilds), _common/conventions.py:186-249 (mode_q), _common/backend.py:1767-1812 (eig). */
 int wb_layer_modes(wb_handle* h, int n_pairs, int hu, int hv, const wb_complex* conv,

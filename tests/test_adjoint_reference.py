@@ -29,7 +29,7 @@ def _case(name):
     return {k.split('__', 1)[1]: d[k] for k in d.files if k.startswith(name + '__')}
 
 
-def _ours(c, impl, device):
+def _ours(c, impl, device, modes='double'):
     h = int(c['orders'][0])
     N = (2 * h + 1) ** 2
     B = len(c['wavelengths'])
@@ -37,7 +37,8 @@ def _ours(c, impl, device):
     wT[:, N // 2] = 1.0
     loss, R, T, g_eps, g_th = AD.solve_and_grad(
         c['eps'][None].astype(np.complex128), np.array([float(c['thickness'])]), c['wavelengths'], (1000.0, 1000.0),
-        h, h, wR, wT, theta=0.0, phi=0.0, eps_top=1.0, eps_bot=2.25, pol=(0.0, 1.0), impl=impl, device=device)
+        h, h, wR, wT, theta=0.0, phi=0.0, eps_top=1.0, eps_bot=2.25, pol=(0.0, 1.0), impl=impl, device=device,
+        modes=modes)
     return loss, np.asarray(g_eps.cpu())[0], float(g_th.cpu()[0])
 
 
@@ -54,8 +55,11 @@ def test_torch_adjoint_matches_the_reference_gradient():
 
 
 @pytest.mark.gpu
-def test_kernel_adjoint_matches_the_reference_gradient_on_the_adjoint_layer_workload():
+@pytest.mark.parametrize('modes', ['double', 'mixed'])
+def test_kernel_adjoint_matches_the_reference_gradient_on_the_adjoint_layer_workload(modes):
+    """The kernel path (every stage and reverse pass on the library's kernels) with the FP64
+    eigen-solve and with the FP32 eigen-solve refined by Newton steps."""
     if not torch.cuda.is_available():
         pytest.skip('no CUDA device')
     c = _case('layer')
-    _check(c, *_ours(c, 'gb300', 'cuda'))
+    _check(c, *_ours(c, 'gb300', 'cuda', modes))

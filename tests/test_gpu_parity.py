@@ -203,8 +203,10 @@ def test_solve_batch_is_invariant_to_batch_position():
     assert np.abs(R[0] - o['R']).max() <= 1e-10 and np.abs(T[0] - o['T']).max() <= 1e-10
 
 
-def test_layer_modes_double_float_eigenpairs():
-    """The double-float eigen-solve returns FP64-class eigenpairs."""
+@pytest.mark.parametrize('precision', ['mixed_df64', 'mixed'])
+def test_layer_modes_double_float_eigenpairs(precision):
+    """The double-float eigen-solve ('mixed_df64') and the FP32 eigen-solve refined by Newton steps
+    ('mixed') return FP64-class eigenpairs."""
     E = _engine()
     rng = np.random.default_rng(5)
     eps = np.stack([_rast(rng, 20, 20)])
@@ -212,7 +214,7 @@ def test_layer_modes_double_float_eigenpairs():
     conv = E.assemble(torch.as_tensor(eps, device='cuda'), hu, hv)
     kx, ky = O.separable_kxy(640.0, (900.0, 900.0), O.incident_kxy(0.2, 0.4, 1.0), hu, hv)
     kxg, kyg = O.order_grid(kx, ky)
-    w, q, W, V, st = E.layer_modes(conv, [0], kxg.real[None], kyg.real[None], precision='mixed')
+    w, q, W, V, st = E.layer_modes(conv, [0], kxg.real[None], kyg.real[None], precision=precision)
     torch.cuda.synchronize()
     om2, _ = O.layer_operator(kxg, kyg, *(s[0].cpu().numpy() for s in (conv.epx, conv.epy, conv.epz_i)))
     wn, Wn = w[0].cpu().numpy(), W[0].cpu().numpy()

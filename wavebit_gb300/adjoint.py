@@ -536,9 +536,10 @@ def solve_and_grad(eps, thickness, wavelengths, period, hu, hv, weights_R, weigh
     With ``grad_wavelength`` a sixth value is returned: ``d loss / d wavelength`` (B,), each
     wavelength's own term by a forward tangent (:func:`wavelength_tangent`).
 
-    ``modes`` is the eigen-solve of the kernel path (``impl='gb300'``): ``'double'`` (FP64) or
-    ``'mixed_df64'`` (the double-float eigen-solve on the FP32 pipes, FP64-class eigenpairs); the
-    cascade and every reverse pass are FP64 either way.
+    ``modes`` is the eigen-solve of the kernel path (``impl='gb300'``): ``'double'`` (FP64),
+    ``'mixed'`` (FP32 refined by Newton steps on the FP64 operator) or ``'mixed_df64'`` (double-float
+    on the FP32 pipes); the last two give FP64-class eigenpairs. The cascade and every reverse pass
+    are FP64 in every case.
 
     ``fourier_coefficients`` may be ``'sampled'`` or ``'integrated'``: a differentiated raster
     keeps every pixel edge (factorization.py:3135-3150 of the reference), and over one segment

@@ -260,11 +260,12 @@ int wb_layer_modes(wb_handle* h, int n_pairs, int hu, int hv, const wb_complex* 
     return fail(WB_E_INVALID, "wb_layer_modes: precision %d", precision);
   cudaSetDevice(h->device);
   const int N = (2 * hu + 1) * (2 * hv + 1), n = 2 * N;
-  size_t need = wb::layer_modes_bytes(N, n_pairs);
+  size_t need = wb::layer_modes_bytes(N, n_pairs, precision);
   int rc = reserve(h, need);
   if (rc) return rc;
-  wb::layer_modes((cudaStream_t)stream, h->arena, n_pairs, N, (const cplx*)conv, (const int*)pair_layer, kx, ky,
-                  (cplx*)w, (cplx*)q, (cplx*)W, (cplx*)V, status, precision);
+  if (wb::layer_modes((cudaStream_t)stream, h->arena, n_pairs, N, (const cplx*)conv, (const int*)pair_layer, kx, ky,
+                      (cplx*)w, (cplx*)q, (cplx*)W, (cplx*)V, status, precision) != 0)
+    return fail(WB_E_NOMEM, "wb_layer_modes: arena exhausted for %d pairs", n_pairs);
   (void)n;
   return cuda_check("wb_layer_modes");
 }

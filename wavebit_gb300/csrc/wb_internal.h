@@ -55,10 +55,12 @@ struct SolveOut {
 };
 
 size_t solve_chunk_bytes(int N, int L, int chunk, int precision);
-size_t layer_modes_bytes(int N, int n_pairs);
-void layer_modes(cudaStream_t s, Arena& ar, int n_pairs, int N, const cplx* conv, const int* pair_layer,
-                 const double* kx, const double* ky, cplx* w, cplx* q, cplx* W, cplx* V, int32_t* status,
-                 int precision);
+size_t layer_modes_bytes(int N, int n_pairs, int precision);
+// precision 0: FP64 eigen-solve; 1: FP32 eigen-solve refined by Newton steps; others: double-float.
+// Returns -1 when the arena cannot hold the scratch.
+int layer_modes(cudaStream_t s, Arena& ar, int n_pairs, int N, const cplx* conv, const int* pair_layer,
+                const double* kx, const double* ky, cplx* w, cplx* q, cplx* W, cplx* V, int32_t* status,
+                int precision);
 // (3 planes of L) (N, N) slots -> (L, 3, N, N)
 void regroup_slots(cudaStream_t s, int L, int N, const cplx* planes, cplx* out);
 int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int count, const SolveOut& out,

@@ -1046,10 +1046,12 @@ struct NewtonBufs {
 
 // Outputs as stage_b<df64>: bigW in Wd and bigV in Vd as double-float, w/q/X in FP64.
 // Wd, Vd, Om: (P, n, n) complex128-sized buffers (FP64 W; scratch of the Omega^2 W products).
+// With for_cascade false the modes stay Cartesian FP64 W and V (wb_layer_modes' outputs): no s/p
+// rotation, no double-float conversion; c and sn are not read.
 void stage_b_newton(cudaStream_t s, int P, int N, const cplx* conv, const int* pair_layer, const int* pair_solve,
                     const double* pair_thick, const double* wavelength, const double* kx, const double* ky,
                     cplx* Wd, cplx* Vd, cplx* Om, NewtonBufs& nb, GroupBufs& gb, cplx* w, cplx* q, cplx* X,
-                    const double* c, const double* sn, int32_t* st, int st_div) {
+                    const double* c, const double* sn, int32_t* st, int st_div, bool for_cascade) {
   TraceRange trace_("wb:stage_b.newton");
   const int n = 2 * N;
   const long long n2 = (long long)n * n, NN = (long long)N * N, tot = (long long)P * n2;
@@ -1122,6 +1124,7 @@ void stage_b_newton(cudaStream_t s, int P, int N, const cplx* conv, const int* p
   vmodes_epilogue_kernel<<<nblk(tot, 256), 256, 0, s>>>(tot, N, n, pair_solve, kx, ky, (const cplx*)Tm, (const cplx*)Um,
                                                         Wd, q, Vd);
   note_launch();
+  if (!for_cascade) return;
   sp_rotate_kernel<double><<<nblk((long long)P * N * n, 256), 256, 0, s>>>(P, N, pair_solve, c, sn, (Cx<double>*)Wd,
                                                                           (Cx<double>*)Vd, n2);
   note_launch();
@@ -1711,7 +1714,7 @@ int solve_chunk(cudaStream_t s, Arena& ar, const SolveDesc& d, int first, int co
     if (!gb.carve(ar, P, n) || !ar.ok()) return -1;
     NewtonBufs nb{bW, bV, Mk, Rk, (Cx<float>*)wr, (Cx<float>*)taur, pivW, lam};
     stage_b_newton(s, P, N, d.conv, pair_layer, pair_solve, pair_thick, wl, pv.kx, pv.ky, (cplx*)OMr, (cplx*)Zbr,
-                   (cplx*)Xvr, nb, gb, w, q, X, pv.c, pv.s, st, L);
+                   (cplx*)Xvr, nb, gb, w, q, X, pv.c, pv.s, st, L, true);
     Cx<df64>* OM = (Cx<df64>*)OMr; Cx<df64>* Zb = (Cx<df64>*)Zbr;
     convert<df64, RC>(s, OM, bW, (long long)P * n2);
     convert<df64, RC>(s, Zb, bV, (long long)P * n2);
@@ -2436,14 +2439,52 @@ __global__ void fill_kernel(int n, double v, double* __restrict__ out) {
   if (i < n) out[i] = v;
 }
 
-size_t layer_modes_bytes(int N, int n_pairs) {
+size_t layer_modes_bytes(int N, int n_pairs, int precision) {
   const size_t n = 2 * (size_t)N, n2 = n * n, P = n_pairs;
   size_t b = 0;
   auto A = [&](size_t x) { b += (x + 255) & ~(size_t)255; };
   A(sizeof(int) * P); A(sizeof(double) * P); A(sizeof(double) * P);
+  if (precision == 1) {                       // FP32 eigen-solve with Newton steps
+    A(16 * P * n2);                                                   // Omega^2 W scratch
+    for (int k = 0; k < 4; ++k) A(8 * P * n2);                        // F1..F4
+    A(8 * P * n); A(8 * P * n);                                       // wr, tau
+    A(sizeof(int) * P * n);                                           // pivots
+    A(16 * P * n); A(16 * P * n);                                     // lambda, X
+    return b + GroupBufs::bytes((int)P, (int)n);
+  }
   A(16 * P * n2); A(16 * P * n2); A(16 * P * n2); A(16 * P * n2);
   for (int k = 0; k < 3; ++k) A(16 * P * n);
   return b;
+}
+
+// The FP32 eigen-solve refined by Newton steps (the mixed form's stage B), Cartesian FP64 modes
+// straight into W and V.
+static int layer_modes_newton(cudaStream_t s, Arena& ar, int P, int N, const cplx* conv, const int* pair_layer,
+                              const double* kx, const double* ky, cplx* w, cplx* q, cplx* W, cplx* V,
+                              int32_t* status) {
+  const int n = 2 * N;
+  const long long n2 = (long long)n * n;
+  ar.reset();
+  int* pair_solve = ar.get<int>(P);
+  double* zero = ar.get<double>(P);
+  double* lam1 = ar.get<double>(P);
+  cplx* Om = ar.get<cplx>((size_t)P * n2);
+  NewtonBufs nb;
+  nb.F1 = ar.get<Cx<float>>((size_t)P * n2); nb.F2 = ar.get<Cx<float>>((size_t)P * n2);
+  nb.F3 = ar.get<Cx<float>>((size_t)P * n2); nb.F4 = ar.get<Cx<float>>((size_t)P * n2);
+  nb.wr = ar.get<Cx<float>>((size_t)P * n); nb.tau = ar.get<Cx<float>>((size_t)P * n);
+  nb.piv = ar.get<int>((size_t)P * n);
+  nb.lam = ar.get<cplx>((size_t)P * n);
+  cplx* X = ar.get<cplx>((size_t)P * n);
+  GroupBufs gb;
+  if (!gb.carve(ar, P, n) || !ar.ok()) return -1;
+  iota_kernel<<<nblk(P, 128), 128, 0, s>>>(P, pair_solve); note_launch();
+  fill_kernel<<<nblk(P, 128), 128, 0, s>>>(P, 0.0, zero); note_launch();
+  fill_kernel<<<nblk(P, 128), 128, 0, s>>>(P, 1.0, lam1); note_launch();
+  if (status) cudaMemsetAsync(status, 0, sizeof(int32_t) * P, s);
+  stage_b_newton(s, P, N, conv, pair_layer, pair_solve, zero, lam1, kx, ky, W, V, Om, nb, gb, w, q, X, nullptr,
+                 nullptr, status, 1, false);
+  return 0;
 }
 
 template <class R>
@@ -2471,11 +2512,13 @@ void layer_modes_t(cudaStream_t s, Arena& ar, int P, int N, const cplx* conv, co
   convert<R, double>(s, Zb, (Cx<double>*)V, (long long)P * n2);
 }
 
-void layer_modes(cudaStream_t s, Arena& ar, int P, int N, const cplx* conv, const int* pair_layer,
-                 const double* kx, const double* ky, cplx* w, cplx* q, cplx* W, cplx* V, int32_t* status,
-                 int precision) {
+int layer_modes(cudaStream_t s, Arena& ar, int P, int N, const cplx* conv, const int* pair_layer,
+                const double* kx, const double* ky, cplx* w, cplx* q, cplx* W, cplx* V, int32_t* status,
+                int precision) {
+  if (precision == 1) return layer_modes_newton(s, ar, P, N, conv, pair_layer, kx, ky, w, q, W, V, status);
   if (precision == 0) layer_modes_t<double>(s, ar, P, N, conv, pair_layer, kx, ky, w, q, W, V, status);
   else layer_modes_t<df64>(s, ar, P, N, conv, pair_layer, kx, ky, w, q, W, V, status);
+  return ar.ok() ? 0 : -1;
 }
 
 __global__ void regroup_kernel(int L, long long NN, const cplx* __restrict__ planes, cplx* __restrict__ out) {
