@@ -115,6 +115,29 @@ __device__ __forceinline__ Cx<R> block_sum_cx(Cx<R> v, R* red) {
   return r;
 }
 
+// sum_i conj(v_i) c_i over i < m by one warp, the total in every lane. The FP32 form issues four
+// loads per lane before it accumulates (four partial sums), the other forms one.
+template <class R>
+__device__ __forceinline__ Cx<R> column_dot(const Cx<R>* v, const Cx<R>* c, int m, int lane) {
+  Cx<R> acc = cxzero<R>();
+  int i = lane;
+  if constexpr (sizeof(R) == 4) {
+    Cx<R> acc1 = cxzero<R>(), acc2 = cxzero<R>(), acc3 = cxzero<R>();
+    for (; i + 96 < m; i += 128) {
+      const Cx<R> c0 = c[i], c1 = c[i + 32], c2 = c[i + 64], c3 = c[i + 96];
+      acc = cxfma_conj(v[i], c0, acc);
+      acc1 = cxfma_conj(v[i + 32], c1, acc1);
+      acc2 = cxfma_conj(v[i + 64], c2, acc2);
+      acc3 = cxfma_conj(v[i + 96], c3, acc3);
+    }
+    acc = (acc + acc2) + (acc1 + acc3);
+  }
+  for (; i < m; i += 32) acc = cxfma_conj(v[i], c[i], acc);
+  acc.x = warp_sum(acc.x);
+  acc.y = warp_sum(acc.y);
+  return acc;
+}
+
 template <class R>
 __global__ void __launch_bounds__(1024) gehrd_kernel(Cx<R>* __restrict__ Aall, int n, int lda,
                                                      long long a_bs, Cx<R>* __restrict__ tau_all) {
@@ -154,11 +177,25 @@ __global__ void __launch_bounds__(1024) gehrd_kernel(Cx<R>* __restrict__ Aall, i
     // every thread has read alpha = A(k+1, k) by now; column k is not touched again in this step
     if (tid == 0) col[k + 1] = cxmk<R>(r.beta, R(0.0));
     const C_ t = s_tau, tc = cxconj(t);
-    // y = A[:, k+1:n] v, one row per thread (loads only: they pipeline)
+    // y = A[:, k+1:n] v, one row per thread (loads only: they pipeline). The FP32 form keeps four
+    // loads in flight per thread (its registers allow it; the FP64-sized forms are at the limit).
     for (int i = tid; i < n; i += blockDim.x) {
       const C_* ai = A + i + (long long)(k + 1) * lda;
       C_ acc0 = cxzero<R>(), acc1 = cxzero<R>();
       int j = 0;
+      if constexpr (sizeof(R) == 4) {
+        C_ acc2 = cxzero<R>(), acc3 = cxzero<R>();
+        for (; j + 3 < m; j += 4) {
+          const C_ a0 = ai[(long long)j * lda], a1 = ai[(long long)(j + 1) * lda];
+          const C_ a2 = ai[(long long)(j + 2) * lda], a3 = ai[(long long)(j + 3) * lda];
+          acc0 = cxfma(a0, sv[j], acc0);
+          acc1 = cxfma(a1, sv[j + 1], acc1);
+          acc2 = cxfma(a2, sv[j + 2], acc2);
+          acc3 = cxfma(a3, sv[j + 3], acc3);
+        }
+        acc0 = acc0 + acc2;
+        acc1 = acc1 + acc3;
+      }
       for (; j + 1 < m; j += 2) {
         acc0 = cxfma(ai[(long long)j * lda], sv[j], acc0);
         acc1 = cxfma(ai[(long long)(j + 1) * lda], sv[j + 1], acc1);
@@ -174,10 +211,7 @@ __global__ void __launch_bounds__(1024) gehrd_kernel(Cx<R>* __restrict__ Aall, i
     // both sides, one warp per trailing column
     for (int jj = warp; jj < m; jj += nw) {
       C_* cj = A + (long long)(k + 1 + jj) * lda;
-      C_ acc = cxzero<R>();
-      for (int i = lane; i < m; i += 32) acc = cxfma_conj(sv[i], cj[k + 1 + i], acc);
-      acc.x = warp_sum(acc.x);
-      acc.y = warp_sum(acc.y);
+      const C_ acc = column_dot<R>(sv, cj + k + 1, m, lane);
       const C_ vjc = cxconj(sv[jj]);
       const C_ z = acc - tcoef * vjc;
       const C_ a1 = t * vjc, a2 = tc * z;
@@ -227,10 +261,7 @@ __global__ void __launch_bounds__(1024) unghr_kernel(Cx<R>* __restrict__ Aall, i
     __syncthreads();
     for (int j = warp; j < m; j += nw) {
       C_* cj = Z + (long long)(k + 1 + j) * ldz;
-      C_ acc = cxzero<R>();
-      for (int i = lane; i < m; i += 32) acc = cxfma_conj(sv[i], cj[k + 1 + i], acc);
-      acc.x = warp_sum(acc.x);
-      acc.y = warp_sum(acc.y);
+      const C_ acc = column_dot<R>(sv, cj + k + 1, m, lane);
       const C_ f = t * acc;
       for (int i0 = lane; i0 < m; i0 += 32 * kUnroll) {
         C_ val[kUnroll];
