@@ -349,14 +349,18 @@ def profile_calls(args):
     h = _lib.handle(0)
     _lib.check(h.lib.wb_profile_qr(1))
     st = None
+    ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev2.record()
     for _ in range(args.profile_calls):
         R, T, st = E.solve_batch(conv, inp, precision=precision)
+    ev3.record()
     torch.cuda.synchronize()
+    solve_ms = ev2.elapsed_time(ev3) / args.profile_calls
     qr = qr_profile(h, 0 if precision == 'double' else 1 if precision == 'mixed' else 2)
     print(f'{args.workload} {precision} solves={B} calls={args.profile_calls} '
           f'status_nonzero={int((st.cpu().numpy() & ~8).astype(bool).sum())} '
           f"qr_sweep_{qr['type']}: launches={qr['launches']} ms={qr['ms']:.1f} algorithmic_bytes={qr['bytes']:.6g} "
-          f"stage_a_ms={stage_a_ms:.2f}")
+          f"stage_a_ms={stage_a_ms:.2f} solve_ms={solve_ms:.1f}")
 
 
 def adjoint_check(args):
@@ -432,6 +436,8 @@ def main():
     ap.add_argument('--profile-calls', type=int, default=0)
     ap.add_argument('--tensor-cores', default='on', choices=['on', 'off'],
                     help='off: the FP32 complex products on the SIMT kernel instead of tcgen05 (for comparison)')
+    ap.add_argument('--tune', action='append', default=[], metavar='KEY=VALUE',
+                    help='set a launch-shape tunable before the run (wb_set_tuning; keys WB_TUNE_*)')
     ap.add_argument('--pixels', type=int, default=16)
     ap.add_argument('--adjoint-wavelengths', type=int, default=32)
     args = ap.parse_args()
@@ -439,6 +445,11 @@ def main():
     if args.tensor_cores == 'off' and args.impl != 'reference':
         from wavebit_gb300 import _lib
         _lib.check(_lib.load().wb_set_tuning(_lib.WB_TUNE_TENSOR_CORES, 1))
+    if args.tune and args.impl != 'reference':
+        from wavebit_gb300 import _lib
+        for kv in args.tune:
+            key, val = (int(x) for x in kv.split('='))
+            _lib.check(_lib.load().wb_set_tuning(key, val))
     if args.workload == 'adjoint_layer':
         return adjoint_check(args)
     if args.impl == 'reference':

@@ -276,6 +276,7 @@ long long wb_kernel_launches(wb_handle* h);
 #define WB_TUNE_HRD_THREADS 1    /* threads of a Hessenberg-reduction CTA (64..1024, multiple of 32) */
 #define WB_TUNE_LU_THREADS 2     /* reserved: threads of an LU / triangular-solve CTA */
 #define WB_TUNE_TENSOR_CORES 3   /* 1: FP32 complex products on the SIMT kernel instead of tcgen05 */
+#define WB_TUNE_HRD_BLOCKED 4    /* 1: the FP32 Hessenberg reduction one column at a time instead of in panels */
 #define WB_TUNE_COUNT 8
 int wb_set_tuning(int key, int value);
 /* The current value of a tunable (0 = the library's own choice), or -1 for an unknown key. */

@@ -13,7 +13,7 @@ LIB_PATH = os.path.join(_HERE, 'libwbgpu.so')
 WB_OK = 0
 WB_E_INVALID, WB_E_NOMEM, WB_E_SINGULAR, WB_E_NOCONV, WB_E_NONFINITE, WB_E_CUDA = 1, 2, 3, 4, 5, 6
 WB_ST_SINGULAR, WB_ST_NOCONV, WB_ST_NONFINITE, WB_ST_GRAZING = 1, 2, 4, 8
-WB_TUNE_QR_THREADS, WB_TUNE_HRD_THREADS, WB_TUNE_LU_THREADS, WB_TUNE_TENSOR_CORES = 0, 1, 2, 3
+WB_TUNE_QR_THREADS, WB_TUNE_HRD_THREADS, WB_TUNE_LU_THREADS, WB_TUNE_TENSOR_CORES, WB_TUNE_HRD_BLOCKED = 0, 1, 2, 3, 4
 PRECISION = {'double': 0, 'fp64': 0, 'mixed': 1, 'mixed_fp32': 2, 'mixed_df64': 3, 'mixed_df64_eig': 4}
 
 _c = ctypes

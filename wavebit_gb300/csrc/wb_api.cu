@@ -523,7 +523,7 @@ long long wb_kernel_launches(wb_handle* h) { (void)h; return wb::launch_count();
 
 static_assert(WB_TUNE_QR_THREADS == wb::kTuneQrThreads && WB_TUNE_HRD_THREADS == wb::kTuneHrdThreads &&
                   WB_TUNE_LU_THREADS == wb::kTuneLuThreads && WB_TUNE_TENSOR_CORES == wb::kTuneTensorCores &&
-                  WB_TUNE_COUNT == wb::kTuneKeys,
+                  WB_TUNE_HRD_BLOCKED == wb::kTuneHrdBlocked && WB_TUNE_COUNT == wb::kTuneKeys,
               "public and internal tuning keys agree");
 
 int wb_set_tuning(int key, int value) {

@@ -236,6 +236,155 @@ __global__ void __launch_bounds__(1024) gehrd_kernel(Cx<R>* __restrict__ Aall, i
   }
 }
 
+// --------------------------------------- 1b. blocked Hessenberg reduction (FP32 form)
+// The same reflectors and storage as gehrd_kernel, kHrdPanel columns at a time in WY form. With
+// the panel's reflectors so far Q_j = I - V_j T_j V_j^H and Y_j = A V_j T_j (A as at the panel's
+// start), column c = k + j of Q_j^H A Q_j is
+//   b = a_c - Y_j V_j(c, :)^H,   then   b <- b - V_j T_j^H (V_j^H b)   (rows below k),
+// its reflector (tau_j, v_j) extends T (T[:j, j] = -tau_j T_j V_j^H v_j, T[j, j] = tau_j) and Y
+// (Y[:, j] = tau_j (A v_j - Y_j V_j^H v_j)); a_c and A v_j read columns the panel has not yet
+// written, so the panel makes one pass over the trailing columns per column. After the panel,
+// A <- Q^H (A - Y V^H) on the columns right of it, as batched products (geev_schur). Scratch per
+// matrix (column-major, ld n): V, conj(V), Y (n x kHrdPanel), W, X (kHrdPanel x n), T^H.
+constexpr int kHrdPanel = 32;
+
+template <class R>
+__global__ void __launch_bounds__(1024) gehrd_panel_kernel(Cx<R>* __restrict__ Aall, int n, int lda, long long a_bs,
+                                                           Cx<R>* __restrict__ tau_all, int k, int bb,
+                                                           Cx<R>* __restrict__ Wsall, long long ws_bs) {
+  using C_ = Cx<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C_* sb = reinterpret_cast<C_*>(smraw);          // (n) the column being reduced
+  C_* sv = sb + n;                                 // (n) its reflector
+  __shared__ C_ T[kHrdPanel][kHrdPanel + 1];
+  __shared__ C_ s_vc[kHrdPanel], s_w[kHrdPanel], s_u[kHrdPanel];
+  __shared__ R red[32];
+  __shared__ C_ s_tau, s_scale;
+  __shared__ R s_beta;
+  __shared__ int s_id;
+  C_* A = Aall + blockIdx.x * a_bs;
+  C_* tau = tau_all + (long long)blockIdx.x * n;
+  C_* ws = Wsall + blockIdx.x * ws_bs;
+  const long long nB = (long long)n * kHrdPanel;
+  C_* V = ws;
+  C_* Vc = ws + nB;
+  C_* Y = ws + 2 * nB;
+  C_* TH = ws + 5 * nB;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x, nw = nt >> 5;
+  for (int e = tid; e < kHrdPanel * (kHrdPanel + 1); e += nt) T[e / (kHrdPanel + 1)][e % (kHrdPanel + 1)] = cxzero<R>();
+  __syncthreads();
+  for (int j = 0; j < bb; ++j) {
+    const int c = k + j;
+    if (tid < j) s_vc[tid] = cxconj(V[c + (long long)tid * n]);
+    __syncthreads();
+    // b = a_c - Y_j conj(V_j(c, :))
+    for (int r = tid; r < n; r += nt) {
+      C_ acc = A[r + (long long)c * lda];
+      for (int l = 0; l < j; ++l) acc = acc - Y[r + (long long)l * n] * s_vc[l];
+      sb[r] = acc;
+    }
+    __syncthreads();
+    if (j > 0) {
+      // w = V_j^H b (rows below k), u = T_j^H w, b <- b - V_j u
+      for (int l = warp; l < j; l += nw) {
+        C_ acc = cxzero<R>();
+        for (int r = k + 1 + lane; r < n; r += 32) acc = cxfma_conj(V[r + (long long)l * n], sb[r], acc);
+        acc.x = warp_sum(acc.x);
+        acc.y = warp_sum(acc.y);
+        if (lane == 0) s_w[l] = acc;
+      }
+      __syncthreads();
+      if (tid < j) {
+        C_ acc = cxzero<R>();
+        for (int lp = 0; lp <= tid; ++lp) acc = cxfma_conj(T[lp][tid], s_w[lp], acc);
+        s_u[tid] = acc;
+      }
+      __syncthreads();
+      for (int r = k + 1 + tid; r < n; r += nt) {
+        C_ acc = sb[r];
+        for (int l = 0; l < j; ++l) acc = acc - V[r + (long long)l * n] * s_u[l];
+        sb[r] = acc;
+      }
+      __syncthreads();
+    }
+    // the reflector of (b[c+1]; b[c+2:])
+    R part = R(0.0);
+    for (int r = c + 2 + tid; r < n; r += nt) part = part + cxabs2(sb[r]);
+    const R xn2 = block_sum(part, red);
+    if (tid == 0) {
+      const Refl<R> rf = make_reflector(sb[c + 1], rsqrt_(xn2));
+      s_id = rf.identity ? 1 : 0;
+      s_tau = rf.identity ? cxzero<R>() : rf.tau;
+      s_scale = rf.scale;
+      s_beta = rf.beta;
+      tau[c] = s_tau;
+    }
+    __syncthreads();
+    const bool ident = s_id != 0;
+    const C_ tj = s_tau, scl = s_scale;
+    // v, V[:, j] and conj(V[:, j]), and column c in its final form
+    for (int r = tid; r < n; r += nt) {
+      C_ v = cxzero<R>();
+      if (!ident) {
+        if (r == c + 1) v = cxone<R>();
+        else if (r > c + 1) v = sb[r] * scl;
+      }
+      sv[r] = v;
+      V[r + (long long)j * n] = v;
+      Vc[r + (long long)j * n] = cxconj(v);
+      C_ a = sb[r];
+      if (!ident && r == c + 1) a = cxmk<R>(s_beta, R(0.0));
+      else if (!ident && r > c + 1) a = v;
+      A[r + (long long)c * lda] = a;
+    }
+    __syncthreads();
+    // w2 = V_j^H v, T[:j, j] = -tau T_j w2, T[j, j] = tau
+    if (j > 0) {
+      for (int l = warp; l < j; l += nw) {
+        C_ acc = cxzero<R>();
+        for (int r = c + 1 + lane; r < n; r += 32) acc = cxfma_conj(V[r + (long long)l * n], sv[r], acc);
+        acc.x = warp_sum(acc.x);
+        acc.y = warp_sum(acc.y);
+        if (lane == 0) s_w[l] = acc;
+      }
+      __syncthreads();
+      if (tid < j) {
+        C_ acc = cxzero<R>();
+        for (int lp = tid; lp < j; ++lp) acc = acc + T[tid][lp] * s_w[lp];
+        T[tid][j] = -(tj * acc);
+      }
+    }
+    if (tid == 0) T[j][j] = tj;
+    __syncthreads();
+    // Y[:, j] = tau (A[:, c+1:] v[c+1:] - Y_j w2), one row per thread, four loads in flight
+    const int m = n - c - 1;
+    for (int r = tid; r < n; r += nt) {
+      const C_* ar = A + r + (long long)(c + 1) * lda;
+      const C_* vv = sv + c + 1;
+      C_ acc0 = cxzero<R>(), acc1 = cxzero<R>(), acc2 = cxzero<R>(), acc3 = cxzero<R>();
+      int q = 0;
+      for (; q + 3 < m; q += 4) {
+        const C_ a0 = ar[(long long)q * lda], a1 = ar[(long long)(q + 1) * lda];
+        const C_ a2 = ar[(long long)(q + 2) * lda], a3 = ar[(long long)(q + 3) * lda];
+        acc0 = cxfma(a0, vv[q], acc0);
+        acc1 = cxfma(a1, vv[q + 1], acc1);
+        acc2 = cxfma(a2, vv[q + 2], acc2);
+        acc3 = cxfma(a3, vv[q + 3], acc3);
+      }
+      for (; q < m; ++q) acc0 = cxfma(ar[(long long)q * lda], vv[q], acc0);
+      C_ y = (acc0 + acc2) + (acc1 + acc3);
+      for (int l = 0; l < j; ++l) y = y - Y[r + (long long)l * n] * s_w[l];
+      Y[r + (long long)j * n] = ident ? cxzero<R>() : tj * y;
+    }
+    __syncthreads();
+  }
+  // T^H, column-major kHrdPanel x kHrdPanel, for the trailing update's X = T^H W
+  for (int e = tid; e < kHrdPanel * kHrdPanel; e += nt) {
+    const int r = e % kHrdPanel, cc = e / kHrdPanel;
+    TH[e] = (r < bb && cc < bb) ? cxconj(T[cc][r]) : cxzero<R>();
+  }
+}
+
 // ------------------------------------------------------------------ 2. form Q = Z
 template <class R>
 __global__ void __launch_bounds__(1024) unghr_kernel(Cx<R>* __restrict__ Aall, int n, int lda,
@@ -847,7 +996,36 @@ void geev_schur(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a
   cudaFuncSetAttribute(gehrd_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   cudaFuncSetAttribute(unghr_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   const int th = hrd_threads(batch, n);
-  gehrd_kernel<R><<<batch, th, sm, s>>>(A, n, lda, a_bs, tau); note_launch();
+  // the FP32 form at n >= 192 reduces in panels (Z, not yet formed, holds the panels' scratch:
+  // 5 n kHrdPanel + kHrdPanel^2 elements, within n * ldz from n = 161 on)
+  const bool blocked = sizeof(R) == 4 && n >= 192 && ldz >= n && tuning(kTuneHrdBlocked) != 1;
+  if (blocked) {
+    cudaFuncSetAttribute(gehrd_panel_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    const int BB = kHrdPanel;
+    const long long nB = (long long)n * BB;
+    Cx<R>* V = Z;
+    Cx<R>* Vc = Z + nB;
+    Cx<R>* Y = Z + 2 * nB;
+    Cx<R>* Wm = Z + 3 * nB;
+    Cx<R>* Xm = Z + 4 * nB;
+    Cx<R>* TH = Z + 5 * nB;
+    const double2 one = make_double2(1.0, 0.0), mone = make_double2(-1.0, 0.0), zero = make_double2(0.0, 0.0);
+    for (int k = 0; k + 2 < n; k += BB) {
+      const int bb = min(BB, n - 2 - k);
+      gehrd_panel_kernel<R><<<batch, th, sm, s>>>(A, n, lda, a_bs, tau, k, bb, Z, z_bs); note_launch();
+      const int c0 = k + bb, m = n - c0, rows = n - k - 1;
+      if (m <= 0) continue;
+      Cx<R>* Ac = A + (long long)c0 * lda;
+      // A[:, c0:] -= Y conj(V[c0:, :])^T
+      gemm<R>(s, batch, n, m, bb, mone, Y, 1, n, z_bs, Vc + c0, n, 1, z_bs, one, Ac, 1, lda, a_bs);
+      // W = V[k+1:, :]^H A[k+1:, c0:];  X = T^H W;  A[k+1:, c0:] -= V[k+1:, :] X
+      gemm<R>(s, batch, bb, m, rows, one, Vc + (k + 1), n, 1, z_bs, Ac + (k + 1), 1, lda, a_bs, zero, Wm, 1, BB, z_bs);
+      gemm<R>(s, batch, bb, m, bb, one, TH, 1, BB, z_bs, Wm, 1, BB, z_bs, zero, Xm, 1, BB, z_bs);
+      gemm<R>(s, batch, rows, m, bb, mone, V + (k + 1), 1, n, z_bs, Xm, 1, BB, z_bs, one, Ac + (k + 1), 1, lda, a_bs);
+    }
+  } else {
+    gehrd_kernel<R><<<batch, th, sm, s>>>(A, n, lda, a_bs, tau); note_launch();
+  }
   unghr_kernel<R><<<batch, th, sm, s>>>(A, n, lda, a_bs, tau, Z, ldz, z_bs); note_launch();
   int itmax = 30 * (n > 10 ? n : 10);
   size_t sm2 = (size_t)n * sizeof(Cx<R>);

@@ -12,7 +12,8 @@ long long launch_count();
 // Launch-shape tunables (process-wide; 0 = the library's own choice). Set through
 // wb_set_tuning by the autotuner; read at every launch.
 // (the same numbers as the public WB_TUNE_* keys)
-enum TuneKey { kTuneQrThreads = 0, kTuneHrdThreads = 1, kTuneLuThreads = 2, kTuneTensorCores = 3, kTuneKeys = 8 };
+enum TuneKey { kTuneQrThreads = 0, kTuneHrdThreads = 1, kTuneLuThreads = 2, kTuneTensorCores = 3, kTuneHrdBlocked = 4,
+               kTuneKeys = 8 };
 int tuning(int key);
 void set_tuning(int key, int value);
 // multiprocessor count of the current device (cached per device)
