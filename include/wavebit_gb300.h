@@ -57,8 +57,9 @@ typedef struct wb_handle wb_handle;
 /* Version of this ABI (major * 100 + minor): 2.0 = the precision codes above (WB_PRECISION_MIXED
  * is the FP32 eigen-solve with Newton steps), wb_smm_solve and wb_workspace_bytes; 2.1 adds
  * wb_assemble_li_integrated and wb_scattering_matrix; 2.2 adds the reverse passes wb_smm_solve_vjp,
- * wb_layer_modes_vjp and wb_assemble_li_vjp, and wb_layer_modes with WB_PRECISION_MIXED runs the
- * FP32 eigen-solve refined by Newton steps (before 2.2: the double-float one). */
+ * wb_layer_modes_vjp and wb_assemble_li_vjp, the tunable WB_TUNE_HRD_BLOCKED, and wb_layer_modes
+ * with WB_PRECISION_MIXED runs the FP32 eigen-solve refined by Newton steps (before 2.2: the
+ * double-float one). */
 int wb_version(void);
 
 /* Message of the calling thread's last failure, NUL-terminated, truncated to len. */
