@@ -385,6 +385,78 @@ __global__ void __launch_bounds__(1024) gehrd_panel_kernel(Cx<R>* __restrict__ A
   }
 }
 
+// --------------------------------------------- 2b. Q from the reflectors in panels (FP32 form)
+// Q = H_0 H_1 ... H_{n-3} is formed as unghr_kernel forms it, last reflectors first, but
+// kHrdPanel reflectors at a time: their product is I - V T V^H (T upper triangular, built
+// forward: T[:j, j] = -tau_j T_j V_j^H v_j, T[j, j] = tau_j), and Z's trailing block gets
+// Z <- Z - V (T (V^H Z)) as batched products. This kernel writes the panel's V, conj(V) (n x
+// kHrdPanel) and T (column-major kHrdPanel x kHrdPanel) into the scratch.
+template <class R>
+__global__ void __launch_bounds__(1024) unghr_panel_kernel(const Cx<R>* __restrict__ Aall, int n, int lda,
+                                                           long long a_bs, const Cx<R>* __restrict__ tau_all, int k0,
+                                                           int bb, Cx<R>* __restrict__ Wsall, long long ws_bs) {
+  using C_ = Cx<R>;
+  __shared__ C_ T[kHrdPanel][kHrdPanel + 1];
+  __shared__ C_ s_w[kHrdPanel];
+  const C_* A = Aall + blockIdx.x * a_bs;
+  const C_* tau = tau_all + (long long)blockIdx.x * n;
+  C_* ws = Wsall + blockIdx.x * ws_bs;
+  const long long nB = (long long)n * kHrdPanel;
+  C_* V = ws;
+  C_* Vc = ws + nB;
+  C_* Tm = ws + 4 * nB;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x, nw = nt >> 5;
+  for (int e = tid; e < kHrdPanel * (kHrdPanel + 1); e += nt) T[e / (kHrdPanel + 1)][e % (kHrdPanel + 1)] = cxzero<R>();
+  for (long long e = tid; e < nB; e += nt) {
+    const int r = (int)(e % n), j = (int)(e / n), c = k0 + j;
+    C_ v = cxzero<R>();
+    if (j < bb) {
+      const C_ t = tau[c];
+      if (!(t.x == R(0.0) && t.y == R(0.0))) {
+        if (r == c + 1) v = cxone<R>();
+        else if (r > c + 1) v = A[r + (long long)c * lda];
+      }
+    }
+    V[e] = v;
+    Vc[e] = cxconj(v);
+  }
+  __syncthreads();
+  for (int j = 0; j < bb; ++j) {
+    const int c = k0 + j;
+    const C_ tj = tau[c];
+    for (int l = warp; l < j; l += nw) {
+      C_ acc = cxzero<R>();
+      for (int r = c + 1 + lane; r < n; r += 32) acc = cxfma_conj(V[r + (long long)l * n], V[r + (long long)j * n], acc);
+      acc.x = warp_sum(acc.x);
+      acc.y = warp_sum(acc.y);
+      if (lane == 0) s_w[l] = acc;
+    }
+    __syncthreads();
+    if (tid < j) {
+      C_ acc = cxzero<R>();
+      for (int lp = tid; lp < j; ++lp) acc = acc + T[tid][lp] * s_w[lp];
+      T[tid][j] = -(tj * acc);
+    }
+    if (tid == 0) T[j][j] = tj;
+    __syncthreads();
+  }
+  for (int e = tid; e < kHrdPanel * kHrdPanel; e += nt) {
+    const int r = e % kHrdPanel, cc = e / kHrdPanel;
+    Tm[e] = (r < bb && cc < bb) ? T[r][cc] : cxzero<R>();
+  }
+}
+
+// the reflectors' storage below the subdiagonal cleared, leaving H
+template <class R>
+__global__ void clear_below_subdiag_kernel(Cx<R>* __restrict__ Aall, int n, int lda, long long a_bs) {
+  Cx<R>* A = Aall + blockIdx.y * a_bs;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)n * n;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    if (i > j + 1) A[i + (long long)j * lda] = cxzero<R>();
+  }
+}
+
 // ------------------------------------------------------------------ 2. form Q = Z
 template <class R>
 __global__ void __launch_bounds__(1024) unghr_kernel(Cx<R>* __restrict__ Aall, int n, int lda,
@@ -990,7 +1062,7 @@ int hrd_threads(int batch, int n) {
 
 template <class R>
 void geev_schur(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a_bs, Cx<R>* Z, int ldz,
-                long long z_bs, Cx<R>* w, Cx<R>* tau, int32_t* status, int st_div) {
+                long long z_bs, Cx<R>* w, Cx<R>* tau, int32_t* status, int st_div, Cx<R>* ws, long long ws_bs) {
   if (batch <= 0 || n <= 0) return;
   size_t sm = 2 * (size_t)n * sizeof(Cx<R>);
   cudaFuncSetAttribute(gehrd_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -1026,7 +1098,32 @@ void geev_schur(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a
   } else {
     gehrd_kernel<R><<<batch, th, sm, s>>>(A, n, lda, a_bs, tau); note_launch();
   }
-  unghr_kernel<R><<<batch, th, sm, s>>>(A, n, lda, a_bs, tau, Z, ldz, z_bs); note_launch();
+  // Q in panels when the caller lends scratch (5 n kHrdPanel + kHrdPanel^2 elements a matrix)
+  if (blocked && ws && ws_bs >= 5LL * n * kHrdPanel + kHrdPanel * kHrdPanel) {
+    const int BB = kHrdPanel;
+    const long long nB = (long long)n * BB;
+    Cx<R>* V = ws;
+    Cx<R>* Vc = ws + nB;
+    Cx<R>* Wm = ws + 2 * nB;
+    Cx<R>* Xm = ws + 3 * nB;
+    Cx<R>* Tm = ws + 4 * nB;
+    const double2 one = make_double2(1.0, 0.0), mone = make_double2(-1.0, 0.0), zero = make_double2(0.0, 0.0);
+    set_identity<R>(s, batch, n, Z, ldz, z_bs);
+    const int nk = n - 2;                                  // reflectors 0 .. n - 3
+    for (int k0 = ((nk - 1) / BB) * BB; k0 >= 0; k0 -= BB) {
+      const int bb = min(BB, nk - k0), rows = n - k0 - 1;
+      unghr_panel_kernel<R><<<batch, th, 0, s>>>(A, n, lda, a_bs, tau, k0, bb, ws, ws_bs); note_launch();
+      Cx<R>* Zb = Z + (k0 + 1) + (long long)(k0 + 1) * ldz;
+      // W = V[k0+1:, :]^H Z_blk;  X = T W;  Z_blk -= V[k0+1:, :] X
+      gemm<R>(s, batch, bb, rows, rows, one, Vc + (k0 + 1), n, 1, ws_bs, Zb, 1, ldz, z_bs, zero, Wm, 1, BB, ws_bs);
+      gemm<R>(s, batch, bb, rows, bb, one, Tm, 1, BB, ws_bs, Wm, 1, BB, ws_bs, zero, Xm, 1, BB, ws_bs);
+      gemm<R>(s, batch, rows, rows, bb, mone, V + (k0 + 1), 1, n, ws_bs, Xm, 1, BB, ws_bs, one, Zb, 1, ldz, z_bs);
+    }
+    const unsigned gx = (unsigned)min((long long)sm_count(), ((long long)n * n + 255) / 256);
+    clear_below_subdiag_kernel<R><<<dim3(gx, batch), 256, 0, s>>>(A, n, lda, a_bs); note_launch();
+  } else {
+    unghr_kernel<R><<<batch, th, sm, s>>>(A, n, lda, a_bs, tau, Z, ldz, z_bs); note_launch();
+  }
   int itmax = 30 * (n > 10 ? n : 10);
   size_t sm2 = (size_t)n * sizeof(Cx<R>);
   cudaFuncSetAttribute(hseqr_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
@@ -1076,7 +1173,7 @@ void znormalize_columns(cudaStream_t s, int batch, int n, cplx* W, int ldw, long
 
 #define WB_EIG_INST(R)                                                                                   \
   template void geev_schur<R>(cudaStream_t, int, int, Cx<R>*, int, long long, Cx<R>*, int, long long,     \
-                              Cx<R>*, Cx<R>*, int32_t*, int);                                             \
+                              Cx<R>*, Cx<R>*, int32_t*, int, Cx<R>*, long long);                          \
   template void trevc<R>(cudaStream_t, int, int, const Cx<R>*, int, long long, Cx<R>*, int, long long);  \
   template void normalize_columns<R>(cudaStream_t, int, int, Cx<R>*, int, long long);
 WB_EIG_INST(double)

@@ -80,9 +80,11 @@ void ztrevc(cudaStream_t s, int batch, int n, const cplx* T, int ldt, long long 
             long long x_bs);
 void znormalize_columns(cudaStream_t s, int batch, int n, cplx* W, int ldw, long long w_bs);
 
+// ws (optional, batch stride ws_bs): scratch the FP32 form forms Q with in panels
 template <class R>
 void geev_schur(cudaStream_t s, int batch, int n, Cx<R>* A, int lda, long long a_bs, Cx<R>* Z, int ldz,
-                long long z_bs, Cx<R>* w, Cx<R>* tau, int32_t* status, int st_div);
+                long long z_bs, Cx<R>* w, Cx<R>* tau, int32_t* status, int st_div, Cx<R>* ws = nullptr,
+                long long ws_bs = 0);
 template <class R>
 void trevc(cudaStream_t s, int batch, int n, const Cx<R>* T, int ldt, long long t_bs, Cx<R>* X, int ldx,
            long long x_bs);

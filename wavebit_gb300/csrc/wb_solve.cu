@@ -1062,7 +1062,7 @@ void stage_b_newton(cudaStream_t s, int P, int N, const cplx* conv, const int* p
     dim3 gr((N + 63) / 64, (N + 63) / 64, P * 4);
     omega2_kernel<float><<<gr, 256, 0, s>>>(N, conv, 3 * NN, pair_layer, pair_solve, kx, ky, nb.F1, n2); note_launch();
   }
-  geev_schur<float>(s, P, n, nb.F1, n, n2, nb.F2, n, n2, nb.wr, nb.tau, st, st_div);
+  geev_schur<float>(s, P, n, nb.F1, n, n2, nb.F2, n, n2, nb.wr, nb.tau, st, st_div, nb.F3, n2);   // F3: free here
   trevc<float>(s, P, n, nb.F1, n, n2, nb.F3, n, n2);
   gemm<float>(s, P, n, n, n, one, nb.F2, 1, n, n2, nb.F3, 1, n, n2, zero, nb.F1, 1, n, n2);
   normalize_columns<float>(s, P, n, nb.F1, n, n2);
