@@ -265,6 +265,10 @@ class GpuBackend:
         self.graph_cache[key] = entry
         self.graph_captures += 1
         while len(self.graph_cache) > self.max_graphs:
+            # the evicted shape's last replay may still run on its worker's stream: let it finish
+            # before the graph is destroyed
+            old_key, _ = next(iter(self.graph_cache.items()))
+            self.streams[old_key[0]].synchronize()
             self.graph_cache.popitem(last=False)
         return out
 
