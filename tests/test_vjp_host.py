@@ -158,11 +158,15 @@ def test_stage_a_reverse_matches_the_torch_li_adjoint(host):
     assert rel(got, want) < 1e-10
 
 
-def test_three_reverse_passes_compose_to_the_adjoint_gradient(host):
+@pytest.mark.parametrize('kw', [dict(seed=1), dict(seed=8, L=3, ny=5, nx=7, hu=1, hv=2,
+                                                   wavelengths=(560.0, 610.0, 690.0), theta=0.4, phi=-0.7),
+                                dict(seed=9, L=1, ny=4, nx=4, hu=3, hv=0, wavelengths=(640.0,), theta=0.0,
+                                     phi=0.0, pol=(1.0, 0.0))])
+def test_three_reverse_passes_compose_to_the_adjoint_gradient(host, kw):
     """Stages C, B and A chained as a host of the C ABI would chain wb_smm_solve_vjp,
     wb_layer_modes_vjp and wb_assemble_li_vjp give solve_and_grad's raster and thickness
-    gradient."""
-    case = Case(seed=1)
+    gradient (crossed and 1D windows, one and three layers, oblique and normal incidence)."""
+    case = Case(**kw)
     wR, wT = weights(case, 2)
     gR, gT = eff_cotangents(case, wR, wT)
     gW, gV, gq, gth = run_stage_c(host, case, gR, gT)
