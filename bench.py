@@ -576,6 +576,9 @@ def main():
                 'traffic': per_launch * ratio if (per_launch and ratio) else None,
                 'traffic_source': QR_TRAFFIC_SOURCE if ratio else None,
                 'share_of_step': (qr['ms'] / 1e3) / t if t > 0 else None,
+                'limiter': ('the bulge step\'s barrier rather than bandwidth: ncu warp-state stalls of one launch on '
+                            '4 solves (FP32 form) give 7.2 barrier and 2.9 long-scoreboard cycles of 17.7 per issued '
+                            'instruction'),
                 'whole_step': {'achieved': (280 * L + 192) * n ** 3 * B / (t / args.steps) / 1e12,
                                'unit': 'TFLOP/s', 'flops_convention': '(280 L + 192) n^3 per solve (the reference '
                                'formulation; the cascade here does about 53 n^3 per layer against its 168 n^3)'}}
